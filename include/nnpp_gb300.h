@@ -1,0 +1,250 @@
+/*
+ * nnpp_gb300.h -- C ABI of the GB300 (sm_103a) nonlocal Nernst-Planck-Poisson hot path.
+ *
+ * The library replaces, for one GPU, the reference's
+ *   - neighbourhood build   build_clouds_hash(...)          src/helpers/grid.h:43-204
+ *   - bond-sum residuals    utils::Residuals(...) F1..F4,F11  src/helpers/utils.h:29-842
+ *   - potential operator    utils::NewtonMatrices(...) K11   src/helpers/utils.h:1794-1848
+ *     and its solve         Eigen::GMRES on K11              src/main.cpp:764-779
+ *   - step / front update   time loop of main()              src/main.cpp:547-1025
+ * behind plain C entry points: host pointers and sizes only, no C++ or torch types.
+ *
+ * Layout conventions (the reference's Eigen containers, column-major):
+ *   nodes   : double[3*N]   x[0..N-1], y[0..N-1], z[0..N-1]      (Eigen::MatrixXd N x 3)
+ *   clouds  : int[N*max]    entry (i, j) at j*N + i, -1 padded     (Eigen::MatrixXi N x max)
+ *   fields  : double[(S+1)*N] species k at k*N, the potential at S*N
+ *             (U1..U4 and U11 of the reference, S = 4)
+ *   phase   : int[N]        1 solid, 0 liquid                       (nodePhase)
+ *
+ * Error behaviour: every call returns an nnpp_status; no C++ exception crosses the ABI.
+ * NNPP_ERR_CAPACITY is the reference's std::runtime_error("Not enough room to store
+ * clouds") of grid.h:187-189.  nnpp_last_error() returns a message for the calling thread.
+ *
+ * Threading: a handle owns one CUDA stream and its device memory.  A handle is not
+ * thread-safe; distinct handles are.  All entry points are synchronous with respect to the
+ * host buffers they take.
+ */
+#ifndef NNPP_GB300_H
+#define NNPP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NNPP_NSPECIES 4
+#define NNPP_ABI_VERSION 1
+
+typedef enum nnpp_status {
+  NNPP_OK = 0,
+  NNPP_ERR_INVALID = 1,          /* bad argument (null pointer, size, parameter) */
+  NNPP_ERR_CAPACITY = 2,         /* neighbour list longer than max_node_no (grid.h:187-189) */
+  NNPP_ERR_NONFINITE = 3,        /* a NaN/Inf appeared in the state */
+  NNPP_ERR_CG_NO_CONVERGE = 4,   /* potential solve hit its iteration cap (strict mode) */
+  NNPP_ERR_CUDA = 5,             /* CUDA runtime error, or no GPU */
+  NNPP_ERR_UNSUPPORTED = 6,      /* valid for the reference, outside this library's scope */
+  NNPP_ERR_STATE = 7,            /* call order violated (e.g. step before neighbour build) */
+  NNPP_ERR_NOMEM = 8             /* device or host allocation failed */
+} nnpp_status;
+
+typedef enum nnpp_precision {
+  NNPP_FP64 = 0,    /* plain FP64: FP64 bond sums, FP64 Jacobi-CG for the potential */
+  NNPP_MIXED = 1    /* FP32 bond sums (compensated), FP32 inner CG + FP64 refinement */
+} nnpp_precision;
+
+typedef enum nnpp_order_mode {
+  NNPP_ORDER_REFERENCE = 0,  /* within-cell order of std::sort as in grid.h:90 (bit-exact) */
+  NNPP_ORDER_CANONICAL = 1   /* within-cell order by node index (stable counting sort)   */
+} nnpp_order_mode;
+
+/*
+ * Model parameters: the subset of utils::parameter (utils.h:2186-2485) that the hot path
+ * reads, for S = 4 transported species and the potential.  Species 0 follows the Mg2+
+ * branch of Residuals (utils.h:72-178: solid-solid bonds kept, BV factor on mixed bonds);
+ * species 1..3 follow the generic branch (utils.h:181-257: solid-solid bonds skipped).
+ */
+typedef struct nnpp_params {
+  double dt, dx, dy, dz;          /* time step, lattice spacing (data2[2..5])            */
+  double delta;                   /* horizon (data2[6])                                  */
+  double CSolid, CSat;            /* normalising and saturation concentration (data2[7,8]) */
+  double F, R, T;                 /* Faraday, gas constant, temperature (data2[49,48,47]) */
+  double vol_red;                 /* BV = 10^(-vol_red*(1-voln1rel)) on mixed Mg bonds (data2[50]) */
+  double z[NNPP_NSPECIES];        /* charges          (datac_k[0]) */
+  double D_solid[NNPP_NSPECIES];  /* D_kSolid         (datac_k[1]) */
+  double D_liquid[NNPP_NSPECIES]; /* D_kLiquid        (datac_k[2]) */
+  double s1[NNPP_NSPECIES];       /* s_k1 diffusion kernel exponent (datac_k[3]) */
+  double s2[NNPP_NSPECIES];       /* s_k2 migration kernel exponent (datac_k[4]) */
+  double K1[NNPP_NSPECIES];       /* K_kprop1         (datac_k[5]) */
+  double K2[NNPP_NSPECIES];       /* K_kprop2         (datac_k[6]) */
+  double sigma;                   /* sigma1           (datac11[1]) */
+  double s_phi;                   /* s111             (datac11[2]) */
+  double K_phi;                   /* K11prop1         (datac11[3]) */
+  double k_diss;                  /* dissolution rate of the Mg source on solid interface nodes */
+  double switch_width;            /* 0: hard dissolution switch; w>0: sigmoid((c-CSat/CSolid)/w) */
+  double c_floor;                 /* positivity clamp, 1e-8/CSolid in main.cpp:805-837 */
+  int    sub_step_no;             /* volume (voln1rel) update period, 8 in main.cpp:39 */
+  int    reserved;
+} nnpp_params;
+
+/* Per-run diagnostics, all accumulated in FP64 on the device. */
+typedef struct nnpp_diag {
+  int64_t steps_done;
+  int64_t solid_count;            /* main.cpp:914-922 */
+  double  voln1rel;               /* main.cpp:944-949 */
+  double  vol0rel;                /* main.cpp:474-480 */
+  double  mass[NNPP_NSPECIES];    /* sum_i c_k,i * dV, global ion-mass balance */
+  double  mg_mass_lost;           /* dV * sum_i (c_0,i(t=0) - c_0,i(t)) */
+  double  dissolved_total;        /* dV * dt * sum over steps of the dissolution source */
+  int64_t cg_iterations_total;    /* inner CG iterations over the run */
+  int64_t cg_solves;              /* potential solves over the run */
+  int64_t cg_not_converged;       /* solves that hit the iteration cap */
+  double  last_rel_residual;      /* FP64 ||b - A phi|| / ||b|| of the last solve */
+  int64_t outer_iterations_total; /* FP64 refinement sweeps (mixed) */
+} nnpp_diag;
+
+typedef struct nnpp_handle nnpp_handle;
+
+/* ---- library ------------------------------------------------------------------------- */
+
+/* Thread-local message of the last failing call ("" if none). */
+const char* nnpp_last_error(void);
+/* NNPP_ABI_VERSION. */
+int nnpp_abi_version(void);
+/* Number of CUDA devices visible (0 on a machine without a GPU); never fails. */
+int nnpp_device_count(void);
+
+/* Fill nnpp_params from the reference's positional control vectors: data2 (51 values,
+ * utils.h:2343-2395), datac1..datac4 (7 values each, utils.h:2397-2423) and datac11
+ * (4 values, utils.h:2480-2483).  k_diss and switch_width have no counterpart in the
+ * reference's data files.  Replaces utils::parameter::set_double. */
+nnpp_status nnpp_params_from_reference(const double* data2, const double* datac1,
+                                       const double* datac2, const double* datac3,
+                                       const double* datac4, const double* datac11,
+                                       double k_diss, double switch_width, nnpp_params* out);
+
+/* ---- neighbourhood build (grid.h:43-204) --------------------------------------------- */
+
+/* Stateless drop-in for build_clouds_hash(max_node_no, r, dx, dy, dz, nodes, clouds,
+ * cloud_lengths, max_cloud_length) (grid.h:43-44): the hash, index, corner and scan steps
+ * run on the GPU.  clouds (N*max_node_no, column-major, -1 padded, self at column 0) and
+ * cloud_lengths (N, self included) may each be NULL.  order_mode selects the within-cell
+ * order (NNPP_ORDER_REFERENCE reproduces the reference bit for bit). */
+nnpp_status nnpp_build_clouds_hash(int max_node_no, double r, double dx, double dy, double dz,
+                                   int n_nodes, const double* nodes_colmajor, int order_mode,
+                                   int* clouds_colmajor, int* cloud_lengths,
+                                   int* max_cloud_length);
+
+/* ---- simulation handle ---------------------------------------------------------------- */
+
+/* Create a handle for N nodes.  bcvalues/icvalues hold (S+1)*N doubles in the reference's
+ * file units: boundary values of the species are divided by CSolid (main.cpp:560-620,
+ * 676-712), the potential's is not; initial values are used as given (main.cpp:398-409).
+ * A node is Dirichlet for field f when bctypes[i] == 0 and bcvalues[f*N+i] != -1
+ * (main.cpp:676-712).  phase0 may be NULL: then phase = (ic_Mg > 0 + 1e-5) as in
+ * main.cpp:411-420. */
+nnpp_status nnpp_create(nnpp_handle** out, const nnpp_params* p, int n_nodes,
+                        const double* nodes_colmajor, const int* bctypes,
+                        const double* bcvalues, const double* icvalues, const int* phase0);
+nnpp_status nnpp_destroy(nnpp_handle* h);
+
+/* Build the neighbour lists for this handle (main.cpp:304-305 calls the reference with
+ * r = delta*(1+1e-5) and cells of 10*dx).  The optional outputs are as in
+ * nnpp_build_clouds_hash. */
+nnpp_status nnpp_build_neighbours(nnpp_handle* h, int max_node_no, double r, double cx,
+                                  double cy, double cz, int order_mode, int* clouds_colmajor,
+                                  int* cloud_lengths, int* max_cloud_length);
+
+/* Neighbour lists in CSR form, reference order, self excluded: row_ptr[N+1], cols[nnz].
+ * Call with cols == NULL to get nnz in *nnz_out first. */
+nnpp_status nnpp_get_neighbours_csr(nnpp_handle* h, int* row_ptr, int* cols, int64_t* nnz_out);
+
+/* Advance n_steps explicit steps on the device.  Each step: solve the potential from the
+ * current concentrations (FP64 tolerance tol, relative 2-norm), then advance c, apply the
+ * Dirichlet values and the positivity clamp, flip saturated solid nodes, update the
+ * diagnostics.  The step sequence is captured once into a CUDA graph per precision. */
+nnpp_status nnpp_forward(nnpp_handle* h, int n_steps, int precision);
+
+/* Solver settings: relative tolerance of the potential (default 1e-10), iteration cap of
+ * the CG (default 2000), strict != 0 turns a capped solve into NNPP_ERR_CG_NO_CONVERGE. */
+nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict);
+
+/* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
+ * NULL. */
+nnpp_status nnpp_get_state(nnpp_handle* h, double* c, double* phi, int* phase);
+/* Overwrite the state from host buffers (user node order); phase may be NULL. */
+nnpp_status nnpp_set_state(nnpp_handle* h, const double* c, const double* phi,
+                           const int* phase);
+nnpp_status nnpp_get_diagnostics(nnpp_handle* h, nnpp_diag* out);
+/* Per-node step of the last flip (-1 if never flipped), user order; N ints. */
+nnpp_status nnpp_get_flip_steps(nnpp_handle* h, int* flip_step);
+
+/* Host-buffer step, the call a host-side time loop makes: upload c (S*N) and phase (N),
+ * run one step with the handle's potential as warm start, download c, phi and phase.
+ * in and out buffers may alias. */
+nnpp_status nnpp_step_host(nnpp_handle* h, int precision, const double* c_in,
+                           const int* phase_in, double* c_out, double* phi_out,
+                           int* phase_out);
+
+/* Drop-in for utils::Residuals restricted to F1..F4 and F11 (utils.h:29-842) with
+ * U^{n+1} = U^n: F[k*N+i] = sum_KRk1 + sum_KRk2 - R_k for the species, F[S*N+i] the
+ * potential residual of utils.h:798-841 (0 on nodes without liquid-liquid bonds), with
+ * R_k the dissolution source of species 0 (0 for the others).  c: S*N, phi: N, phase: N,
+ * F: (S+1)*N, all user order.  voln1rel enters the BV factor. */
+nnpp_status nnpp_residuals(nnpp_handle* h, int precision, const double* c, const double* phi,
+                           const int* phase, double voln1rel, double* F);
+
+/* Solve the potential for the given concentrations and phase (user order) into phi
+ * (in: warm start, out: solution).  Returns the iteration count and FP64 relative
+ * residual. */
+nnpp_status nnpp_solve_potential(nnpp_handle* h, int precision, const double* c,
+                                 const int* phase, double* phi, int* iterations,
+                                 double* rel_residual);
+
+/* ---- differentiation ------------------------------------------------------------------ */
+
+/* Forward half of a forward/backward pair: from the handle's current state run n_steps
+ * steps, sampling the cumulative Mg mass loss dV*sum_i(c_0,i(0) - c_0,i(t)) every
+ * sample_every steps into mass_curve[n_steps/sample_every] (FP64), keeping a state
+ * checkpoint every ckpt_every steps for the backward pass.  The handle's state is left at
+ * the final step. */
+nnpp_status nnpp_forward_ckpt(nnpp_handle* h, int n_steps, int precision, int ckpt_every,
+                              int sample_every, double* mass_curve);
+
+/* Backward half: given dL/d(mass_curve) (same length), recompute each checkpoint segment
+ * and run the adjoint of the explicit step backwards, returning dL/dD_liquid[k] (the solid
+ * diffusivity D_solid[k] scales with D_liquid[k]) and dL/dk_diss.  The handle's state is
+ * restored to the end of the forward run. */
+nnpp_status nnpp_backward(nnpp_handle* h, const double* dL_dmass, double* grad_D,
+                          double* grad_k);
+
+/* ---- ensembles -------------------------------------------------------------------------- */
+
+typedef struct nnpp_ensemble nnpp_ensemble;
+
+/* Group handles (each already built) into one batched launch: every step of every member
+ * runs inside one CUDA graph with work lists over all members' nodes.  Members must use
+ * the same precision in nnpp_ensemble_forward.  tile and warps_per_node of 0 select the
+ * autotuned configuration. */
+nnpp_status nnpp_ensemble_create(nnpp_ensemble** out, nnpp_handle* const* members, int n);
+nnpp_status nnpp_ensemble_forward(nnpp_ensemble* e, int n_steps, int precision);
+nnpp_status nnpp_ensemble_destroy(nnpp_ensemble* e);
+
+/* ---- synthetic inputs --------------------------------------------------------------------- */
+
+/* Deterministic synthetic workloads in the reference's input layout (no input data of the
+ * reference's paper case is available).  kind: 0 lattice with a central solid block,
+ * 1 jittered lattice with a perturbed solid sphere, 2 jittered permuted lattice with a
+ * screw-shaped implant, 3 jittered lattice with a solid cylinder and an 8-node Dirichlet
+ * shell, 4 ensemble member (seeded inclusion, diffusivities and rate).  n_side nodes per
+ * axis.  nnpp_synth_count returns N. */
+int64_t nnpp_synth_count(int kind, int n_side);
+nnpp_status nnpp_synth_fill(int kind, int n_side, uint64_t seed, double* nodes_colmajor,
+                            int* bctypes, double* bcvalues, double* icvalues, int* phase0,
+                            nnpp_params* params);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NNPP_GB300_H */

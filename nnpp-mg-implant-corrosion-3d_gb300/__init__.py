@@ -1,0 +1,320 @@
+"""Python host binding of the GB300 NNPP library (libnnpp_gb300.so, C ABI in
+include/nnpp_gb300.h).
+
+The names mirror the reference's interface for the hot path:
+  build_clouds_hash(...)            grid.h:43-204
+  Simulation.residuals(...)         utils::Residuals, fields F1..F4 and F11 (utils.h:29-842)
+  Simulation.solve_potential(...)   K11 solve (utils.h:1794-1848, main.cpp:764-779)
+  Simulation.forward(...)           the time loop of main.cpp:547-1025 as an explicit step
+Every call goes to the CUDA library; there is no CPU fallback.  Loading fails loudly when
+the library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnnpp_gb300.so")
+
+NSPECIES = 4
+FP64 = 0
+MIXED = 1
+ORDER_REFERENCE = 0
+ORDER_CANONICAL = 1
+
+STATUS = {0: "NNPP_OK", 1: "NNPP_ERR_INVALID", 2: "NNPP_ERR_CAPACITY", 3: "NNPP_ERR_NONFINITE",
+          4: "NNPP_ERR_CG_NO_CONVERGE", 5: "NNPP_ERR_CUDA", 6: "NNPP_ERR_UNSUPPORTED",
+          7: "NNPP_ERR_STATE", 8: "NNPP_ERR_NOMEM"}
+
+
+class NNPPError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("delta", C.c_double), ("CSolid", C.c_double), ("CSat", C.c_double),
+                ("F", C.c_double), ("R", C.c_double), ("T", C.c_double), ("vol_red", C.c_double),
+                ("z", C.c_double * 4), ("D_solid", C.c_double * 4), ("D_liquid", C.c_double * 4),
+                ("s1", C.c_double * 4), ("s2", C.c_double * 4), ("K1", C.c_double * 4),
+                ("K2", C.c_double * 4), ("sigma", C.c_double), ("s_phi", C.c_double),
+                ("K_phi", C.c_double), ("k_diss", C.c_double), ("switch_width", C.c_double),
+                ("c_floor", C.c_double), ("sub_step_no", C.c_int), ("reserved", C.c_int)]
+
+    def copy(self):
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+
+class Diag(C.Structure):
+    _fields_ = [("steps_done", C.c_int64), ("solid_count", C.c_int64), ("voln1rel", C.c_double),
+                ("vol0rel", C.c_double), ("mass", C.c_double * 4), ("mg_mass_lost", C.c_double),
+                ("dissolved_total", C.c_double), ("cg_iterations_total", C.c_int64),
+                ("cg_solves", C.c_int64), ("cg_not_converged", C.c_int64),
+                ("last_rel_residual", C.c_double), ("outer_iterations_total", C.c_int64)]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if name == "mass" else v
+        return d
+
+
+_lib = None
+
+# exported symbols and their signatures (restype, argtypes)
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+_SIGS = {
+    "nnpp_last_error": (C.c_char_p, []),
+    "nnpp_abi_version": (C.c_int, []),
+    "nnpp_device_count": (C.c_int, []),
+    "nnpp_params_from_reference": (C.c_int, [_DP, _DP, _DP, _DP, _DP, _DP, C.c_double, C.c_double,
+                                             C.POINTER(Params)]),
+    "nnpp_build_clouds_hash": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_int, _DP, C.c_int, _IP, _IP, _IP]),
+    "nnpp_create": (C.c_int, [C.POINTER(_P), C.POINTER(Params), C.c_int, _DP, _IP, _DP, _DP, _IP]),
+    "nnpp_destroy": (C.c_int, [_P]),
+    "nnpp_build_neighbours": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, _IP, _IP, _IP]),
+    "nnpp_get_neighbours_csr": (C.c_int, [_P, _IP, _IP, C.POINTER(C.c_int64)]),
+    "nnpp_forward": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nnpp_set_solver": (C.c_int, [_P, C.c_double, C.c_int, C.c_int]),
+    "nnpp_get_state": (C.c_int, [_P, _DP, _DP, _IP]),
+    "nnpp_set_state": (C.c_int, [_P, _DP, _DP, _IP]),
+    "nnpp_get_diagnostics": (C.c_int, [_P, C.POINTER(Diag)]),
+    "nnpp_get_flip_steps": (C.c_int, [_P, _IP]),
+    "nnpp_step_host": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _DP, _IP]),
+    "nnpp_residuals": (C.c_int, [_P, C.c_int, _DP, _DP, _IP, C.c_double, _DP]),
+    "nnpp_solve_potential": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _IP, _DP]),
+    "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
+    "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
+    "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
+    "nnpp_ensemble_forward": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nnpp_ensemble_destroy": (C.c_int, [_P]),
+    "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
+    "nnpp_synth_fill": (C.c_int, [C.c_int, C.c_int, C.c_uint64, _DP, _IP, _DP, _DP, _IP,
+                                  C.POINTER(Params)]),
+}
+
+
+def lib():
+    """The loaded library; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libnnpp_gb300.so not built: run __graft_entry__.build() "
+                              "(or python build.py in the package directory)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _check(st):
+    if st != 0:
+        raise NNPPError(st, lib().nnpp_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP) if a is not None else None
+
+
+def device_count():
+    return lib().nnpp_device_count()
+
+
+# ------------------------------------------------------------------ inputs -------------
+def synth(kind, n_side, seed=0):
+    """Deterministic synthetic workload in the reference's input layout (see
+    nnpp_synth_fill): nodes (3, N) rows x/y/z, bctypes (N,), bcvalues (S+1, N),
+    icvalues (S+1, N), phase0 (N,), params."""
+    L = lib()
+    N = L.nnpp_synth_count(kind, n_side)
+    if N <= 0:
+        raise ValueError("bad synthetic kind/n_side")
+    nodes = np.empty((3, N), dtype=np.float64)
+    bct = np.empty(N, dtype=np.int32)
+    bcv = np.empty((NSPECIES + 1, N), dtype=np.float64)
+    icv = np.empty((NSPECIES + 1, N), dtype=np.float64)
+    ph = np.empty(N, dtype=np.int32)
+    p = Params()
+    _check(L.nnpp_synth_fill(kind, n_side, seed, _dp(nodes), _ip(bct), _dp(bcv), _dp(icv),
+                             _ip(ph), C.byref(p)))
+    return dict(nodes=nodes, bctypes=bct, bcvalues=bcv, icvalues=icv, phase0=ph, params=p, N=N)
+
+
+def params_from_reference(data2, datac, datac11, k_diss=0.0, switch_width=0.0):
+    """utils::parameter::set_double (utils.h:2343-2484) for the hot path's fields."""
+    d2 = np.ascontiguousarray(data2, dtype=np.float64)
+    dc = [np.ascontiguousarray(d, dtype=np.float64) for d in datac]
+    d11 = np.ascontiguousarray(datac11, dtype=np.float64)
+    p = Params()
+    _check(lib().nnpp_params_from_reference(_dp(d2), _dp(dc[0]), _dp(dc[1]), _dp(dc[2]),
+                                            _dp(dc[3]), _dp(d11), k_diss, switch_width,
+                                            C.byref(p)))
+    return p
+
+
+# ------------------------------------------------------------------ neighbour build -----
+def build_clouds_hash(max_node_no, r, dx, dy, dz, nodes, order_mode=ORDER_REFERENCE,
+                      want_clouds=True):
+    """Mirror of build_clouds_hash (grid.h:43-44).  nodes: (3, N) or (N, 3) float64.
+    Returns (clouds (N, max_node_no) int32, -1 padded, self at column 0; cloud_lengths (N,);
+    max_cloud_length).  Raises NNPPError(NNPP_ERR_CAPACITY) where the reference throws."""
+    xyz = _colmajor_nodes(nodes)
+    N = xyz.shape[1]
+    clouds = np.empty((max_node_no, N), dtype=np.int32) if want_clouds else None
+    lengths = np.empty(N, dtype=np.int32)
+    ml = C.c_int(0)
+    _check(lib().nnpp_build_clouds_hash(max_node_no, r, dx, dy, dz, N, _dp(xyz), order_mode,
+                                        _ip(clouds), _ip(lengths), C.byref(ml)))
+    return (clouds.T if want_clouds else None), lengths, ml.value
+
+
+def _colmajor_nodes(nodes):
+    a = np.asarray(nodes, dtype=np.float64)
+    if a.ndim != 2 or 3 not in a.shape:
+        raise ValueError("nodes must be (3, N) or (N, 3)")
+    if a.shape[0] != 3:
+        a = a.T
+    return np.ascontiguousarray(a)
+
+
+# ------------------------------------------------------------------ simulation ----------
+class Simulation:
+    """One NNPP instance on the GPU (an nnpp_handle)."""
+
+    def __init__(self, params, nodes, bctypes, bcvalues, icvalues, phase0=None):
+        self.params = params.copy()
+        xyz = _colmajor_nodes(nodes)
+        self.N = xyz.shape[1]
+        self._xyz = xyz
+        bct = np.ascontiguousarray(bctypes, dtype=np.int32)
+        bcv = np.ascontiguousarray(bcvalues, dtype=np.float64).reshape(NSPECIES + 1, self.N)
+        icv = np.ascontiguousarray(icvalues, dtype=np.float64).reshape(NSPECIES + 1, self.N)
+        ph = None if phase0 is None else np.ascontiguousarray(phase0, dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().nnpp_create(C.byref(h), C.byref(self.params), self.N, _dp(xyz), _ip(bct),
+                                 _dp(bcv), _dp(icv), _ip(ph)))
+        self._h = h
+
+    @classmethod
+    def from_synth(cls, inp):
+        return cls(inp["params"], inp["nodes"], inp["bctypes"], inp["bcvalues"],
+                   inp["icvalues"], inp["phase0"])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().nnpp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def build_neighbours(self, max_node_no=1024, r=None, cell=None,
+                         order_mode=ORDER_REFERENCE, want_clouds=False):
+        """main.cpp:304-305 convention by default: r = delta (1 + 1e-5), cells of 10 dx."""
+        p = self.params
+        if r is None:
+            r = p.delta * (1.0 + 1e-5)
+        if cell is None:
+            cell = (p.dx * 10.0, p.dy * 10.0, p.dz * 10.0)
+        clouds = np.empty((max_node_no, self.N), dtype=np.int32) if want_clouds else None
+        lengths = np.empty(self.N, dtype=np.int32)
+        ml = C.c_int(0)
+        _check(lib().nnpp_build_neighbours(self._h, max_node_no, r, cell[0], cell[1], cell[2],
+                                           order_mode, _ip(clouds), _ip(lengths), C.byref(ml)))
+        self.max_cloud_length = ml.value
+        return (clouds.T if want_clouds else None), lengths, ml.value
+
+    def neighbours_csr(self):
+        nnz = C.c_int64(0)
+        _check(lib().nnpp_get_neighbours_csr(self._h, None, None, C.byref(nnz)))
+        ptr = np.empty(self.N + 1, dtype=np.int32)
+        cols = np.empty(max(nnz.value, 1), dtype=np.int32)
+        _check(lib().nnpp_get_neighbours_csr(self._h, _ip(ptr), _ip(cols), C.byref(nnz)))
+        return ptr, cols[:nnz.value]
+
+    def set_solver(self, tol=1e-10, max_iter=2000, strict=False):
+        _check(lib().nnpp_set_solver(self._h, tol, max_iter, 1 if strict else 0))
+
+    def forward(self, n_steps, precision=MIXED):
+        _check(lib().nnpp_forward(self._h, n_steps, precision))
+
+    def state(self):
+        c = np.empty((NSPECIES, self.N), dtype=np.float64)
+        phi = np.empty(self.N, dtype=np.float64)
+        ph = np.empty(self.N, dtype=np.int32)
+        _check(lib().nnpp_get_state(self._h, _dp(c), _dp(phi), _ip(ph)))
+        return c, phi, ph
+
+    def set_state(self, c, phi=None, phase=None):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(NSPECIES, self.N)
+        phi = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
+        phase = None if phase is None else np.ascontiguousarray(phase, dtype=np.int32)
+        _check(lib().nnpp_set_state(self._h, _dp(c), _dp(phi), _ip(phase)))
+
+    def diagnostics(self):
+        d = Diag()
+        _check(lib().nnpp_get_diagnostics(self._h, C.byref(d)))
+        return d.as_dict()
+
+    def flip_steps(self):
+        f = np.empty(self.N, dtype=np.int32)
+        _check(lib().nnpp_get_flip_steps(self._h, _ip(f)))
+        return f
+
+    def step_host(self, c_in, phase_in=None, precision=MIXED, out=None):
+        """One step with host buffers in and out (nnpp_step_host)."""
+        c_in = np.ascontiguousarray(c_in, dtype=np.float64).reshape(NSPECIES, self.N)
+        if out is None:
+            out = (np.empty((NSPECIES, self.N)), np.empty(self.N), np.empty(self.N, dtype=np.int32))
+        phase_in = None if phase_in is None else np.ascontiguousarray(phase_in, dtype=np.int32)
+        _check(lib().nnpp_step_host(self._h, precision, _dp(c_in), _ip(phase_in), _dp(out[0]),
+                                    _dp(out[1]), _ip(out[2])))
+        return out
+
+    def residuals(self, c, phi, phase, voln1rel=0.0, precision=FP64):
+        """utils::Residuals F1..F4 and F11 with U^{n+1} = U^n; returns (S+1, N)."""
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(NSPECIES, self.N)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        F = np.empty((NSPECIES + 1, self.N), dtype=np.float64)
+        _check(lib().nnpp_residuals(self._h, precision, _dp(c), _dp(phi), _ip(phase), voln1rel,
+                                    _dp(F)))
+        return F
+
+    def solve_potential(self, c, phase, phi0=None, precision=MIXED):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(NSPECIES, self.N)
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        phi = np.zeros(self.N) if phi0 is None else np.array(phi0, dtype=np.float64)
+        it = C.c_int(0)
+        rel = C.c_double(0.0)
+        _check(lib().nnpp_solve_potential(self._h, precision, _dp(c), _ip(phase), _dp(phi),
+                                          C.byref(it), C.byref(rel)))
+        return phi, it.value, rel.value

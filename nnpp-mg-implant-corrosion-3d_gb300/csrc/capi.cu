@@ -1,0 +1,613 @@
+// capi.cu -- the C ABI (include/nnpp_gb300.h): handles, neighbour build, CUDA-graph step
+// loop, state transfer, drop-in residual/solve entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <vector>
+
+#include "handle.cuh"
+
+using namespace nnpp;
+
+struct nnpp_handle {
+  Handle h;
+};
+
+namespace {
+
+constexpr int kBlockHost = 256;
+
+__global__ void k_unpermute(const int* perm, int n, int fields, const double* in, double* out) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const int u = perm[a];
+    for (int f = 0; f < fields; ++f) out[(size_t)f * n + u] = in[(size_t)f * n + a];
+  }
+}
+
+nnpp_status check_params(const nnpp_params* p) {
+  if (!p) return set_error(NNPP_ERR_INVALID, "params is NULL");
+  if (!(p->dt > 0) || !(p->dx > 0) || !(p->dy > 0) || !(p->dz > 0) || !(p->delta > 0))
+    return set_error(NNPP_ERR_INVALID, "dt, dx, dy, dz and delta must be positive");
+  if (p->CSolid == 0.0 || p->K_phi == 0.0 || p->sigma == 0.0 || p->R == 0.0 || p->T == 0.0)
+    return set_error(NNPP_ERR_INVALID, "CSolid, K_phi, sigma, R and T must be non-zero");
+  for (int s = 0; s < S; ++s)
+    if (p->s1[s] != p->s_phi || p->s2[s] != p->s_phi)
+      return set_error(NNPP_ERR_UNSUPPORTED,
+                       "all kernel exponents s_k1, s_k2 and s111 must be equal (one weight per bond)");
+  if (p->switch_width < 0) return set_error(NNPP_ERR_INVALID, "switch_width must be >= 0");
+  return NNPP_OK;
+}
+
+nnpp_status push_settings(Handle& h) {
+  DevState ds;
+  NNPP_CUDA(cudaMemcpyAsync(&ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  ds.tol = h.tol;
+  ds.max_iter = h.max_iter;
+  ds.max_outer = h.max_outer;
+  ds.inner_rel = h.inner_rel;
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  return NNPP_OK;
+}
+
+nnpp_status read_state(Handle& h, DevState* ds) {
+  NNPP_CUDA(cudaMemcpyAsync(ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+void destroy_graphs(Handle& h) {
+  for (int k = 0; k < kGraphKinds; ++k)
+    for (int p = 0; p < 2; ++p)
+      for (int c = 0; c < 2; ++c) {
+        if (h.gexec[k][p][c]) cudaGraphExecDestroy(h.gexec[k][p][c]);
+        if (h.graph[k][p][c]) cudaGraphDestroy(h.graph[k][p][c]);
+        h.gexec[k][p][c] = nullptr;
+        h.graph[k][p][c] = nullptr;
+      }
+}
+
+// Adds a while node after the current capture position of `st`; returns its body graph.
+nnpp_status add_while(cudaStream_t st, cudaGraphConditionalHandle hc, cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  NNPP_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = hc;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  NNPP_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+  *body = np.conditional.phGraph_out[0];
+  NNPP_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                                cudaStreamSetCaptureDependencies));
+  return NNPP_OK;
+}
+
+// prep; while(outer) { cg_init; while(inner) { spmv; update } ; ir_update }
+nnpp_status capture_solve(Handle& h, const KParams& kp, int prec) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  NNPP_CUDA(cudaStreamGetCaptureInfo(h.st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle hout;
+  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 0, 0));
+  NNPP_TRY(launch_prep(h, kp, prec, h.st, hout, nullptr));
+  cudaGraph_t body_out;
+  NNPP_TRY(add_while(h.st, hout, &body_out));
+  NNPP_CUDA(cudaStreamBeginCaptureToGraph(h.st_b1, body_out, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+  cudaGraphConditionalHandle hin;
+  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hin, body_out, 0, 0));
+  NNPP_TRY(launch_cg_init(h, kp, prec, h.st_b1, hin));
+  cudaGraph_t body_in;
+  NNPP_TRY(add_while(h.st_b1, hin, &body_in));
+  NNPP_CUDA(cudaStreamBeginCaptureToGraph(h.st_b2, body_in, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+  NNPP_TRY(launch_cg_iter(h, kp, prec, h.st_b2, hin));
+  cudaGraph_t tmp;
+  NNPP_CUDA(cudaStreamEndCapture(h.st_b2, &tmp));
+  NNPP_TRY(launch_ir_update(h, kp, prec, h.st_b1, hout));
+  NNPP_CUDA(cudaStreamEndCapture(h.st_b1, &tmp));
+  return NNPP_OK;
+}
+
+nnpp_status build_graph(Handle& h, int kind, int prec, int cur) {
+  if (h.gexec[kind][prec][cur]) return NNPP_OK;
+  NNPP_CUDA(cudaStreamBeginCapture(h.st, cudaStreamCaptureModeThreadLocal));
+  nnpp_status st = NNPP_OK;
+  int c = cur;
+  const int nsteps = kind == kGraphStep2 ? 2 : 1;
+  for (int s = 0; s < nsteps && st == NNPP_OK; ++s) {
+    KParams kp = make_kparams(h, c);
+    st = capture_solve(h, kp, prec);
+    if (st == NNPP_OK && kind != kGraphSolve) {
+      st = launch_transport(h, kp, prec, h.st, nullptr);
+      c ^= 1;
+    }
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h.st, &g);
+  if (st != NNPP_OK) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return st;
+  }
+  if (e != cudaSuccess) return set_error(NNPP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return set_error(NNPP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  h.graph[kind][prec][cur] = g;
+  h.gexec[kind][prec][cur] = ex;
+  return NNPP_OK;
+}
+
+nnpp_status run_steps(Handle& h, int n_steps, int prec) {
+  NNPP_TRY(convert_state(h, prec));
+  NNPP_TRY(push_settings(h));
+  int done = 0;
+  while (n_steps - done >= 2) {
+    NNPP_TRY(build_graph(h, kGraphStep2, prec, h.cur));
+    NNPP_CUDA(cudaGraphLaunch(h.gexec[kGraphStep2][prec][h.cur], h.st));
+    done += 2;
+  }
+  if (n_steps - done == 1) {
+    NNPP_TRY(build_graph(h, kGraphStep1, prec, h.cur));
+    NNPP_CUDA(cudaGraphLaunch(h.gexec[kGraphStep1][prec][h.cur], h.st));
+    h.cur ^= 1;
+  }
+  return NNPP_OK;
+}
+
+nnpp_status check_after(Handle& h, long long nc_before) {
+  DevState ds;
+  NNPP_TRY(read_state(h, &ds));
+  if (ds.nonfinite) return set_error(NNPP_ERR_NONFINITE, "non-finite concentration in the state");
+  if (h.strict && ds.cg_nc > nc_before)
+    return set_error(NNPP_ERR_CG_NO_CONVERGE, "potential solve hit its iteration cap");
+  return NNPP_OK;
+}
+
+bool have_gpu() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
+#define NNPP_GUARD(hp)                                                            \
+  do {                                                                            \
+    if (!(hp)) return set_error(NNPP_ERR_INVALID, "handle is NULL");              \
+    clear_error();                                                                \
+    if (cudaSetDevice((hp)->h.device) != cudaSuccess) {                           \
+      cudaGetLastError();                                                         \
+      return set_error(NNPP_ERR_CUDA, "cudaSetDevice failed");                    \
+    }                                                                             \
+  } while (0)
+
+#define NNPP_NEED_BUILT(hp)                                                                   \
+  do {                                                                                        \
+    if (!(hp)->h.built)                                                                       \
+      return set_error(NNPP_ERR_STATE, "neighbour lists not built (call nnpp_build_neighbours)"); \
+  } while (0)
+
+struct StateBackup {
+  int cur, prec;
+  DBuf<double> phi;
+  DBuf<float4> clo;
+  DevState ds;
+};
+
+nnpp_status backup(Handle& h, StateBackup& b) {
+  b.cur = h.cur;
+  b.prec = h.state_prec;
+  if (!b.phi.alloc(h.N) || !b.clo.alloc(h.N)) return set_error(NNPP_ERR_NOMEM, "backup");
+  NNPP_CUDA(cudaMemcpyAsync(b.phi.get(), h.phi64.get(), sizeof(double) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.clo.get(), h.clo.get(), sizeof(float4) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_TRY(read_state(h, &b.ds));
+  return NNPP_OK;
+}
+
+nnpp_status restore(Handle& h, StateBackup& b) {
+  h.cur = b.cur;
+  h.state_prec = b.prec;
+  NNPP_CUDA(cudaMemcpyAsync(h.phi64.get(), b.phi.get(), sizeof(double) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.clo.get(), b.clo.get(), sizeof(float4) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &b.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+// Upload user-order c (S*N), phi (N, may be NULL), phase (N, may be NULL) into the current
+// buffers in precision prec.
+nnpp_status upload_state(Handle& h, const double* c, const double* phi, const int* phase, int prec) {
+  const size_t N = h.N;
+  NNPP_CUDA(cudaMemcpyAsync(h.user_stage.get(), c, sizeof(double) * S * N, cudaMemcpyHostToDevice, h.st));
+  if (phi)
+    NNPP_CUDA(cudaMemcpyAsync(h.user_stage.get() + S * N, phi, sizeof(double) * N, cudaMemcpyHostToDevice, h.st));
+  if (phase)
+    NNPP_CUDA(cudaMemcpyAsync(h.user_stage_i.get(), phase, sizeof(int) * N, cudaMemcpyHostToDevice, h.st));
+  if (prec != h.state_prec && !phase) NNPP_TRY(convert_state(h, prec));
+  return load_state(h, h.user_stage.get(), phi ? h.user_stage.get() + S * N : nullptr,
+                    phase ? h.user_stage_i.get() : nullptr, prec);
+}
+
+}  // namespace
+
+// ======================================================================== C ABI ==========
+extern "C" {
+
+int nnpp_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+nnpp_status nnpp_params_from_reference(const double* data2, const double* datac1, const double* datac2,
+                                       const double* datac3, const double* datac4,
+                                       const double* datac11, double k_diss, double switch_width,
+                                       nnpp_params* out) {
+  clear_error();
+  if (!data2 || !datac1 || !datac2 || !datac3 || !datac4 || !datac11 || !out)
+    return set_error(NNPP_ERR_INVALID, "params_from_reference: NULL input");
+  std::memset(out, 0, sizeof(*out));
+  // utils.h:2346-2395
+  out->dt = data2[2];
+  out->dx = data2[3];
+  out->dy = data2[4];
+  out->dz = data2[5];
+  out->delta = data2[6];
+  out->CSolid = data2[7];
+  out->CSat = data2[8];
+  out->T = data2[47];
+  out->R = data2[48];
+  out->F = data2[49];
+  out->vol_red = data2[50];
+  const double* dc[4] = {datac1, datac2, datac3, datac4};
+  for (int s = 0; s < S; ++s) {  // utils.h:2397-2423
+    out->z[s] = dc[s][0];
+    out->D_solid[s] = dc[s][1];
+    out->D_liquid[s] = dc[s][2];
+    out->s1[s] = dc[s][3];
+    out->s2[s] = dc[s][4];
+    out->K1[s] = dc[s][5];
+    out->K2[s] = dc[s][6];
+  }
+  out->sigma = datac11[1];  // utils.h:2480-2483
+  out->s_phi = datac11[2];
+  out->K_phi = datac11[3];
+  out->k_diss = k_diss;
+  out->switch_width = switch_width;
+  out->c_floor = 1.0e-8 / out->CSolid;  // main.cpp:806
+  out->sub_step_no = 8;                 // main.cpp:39
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_build_clouds_hash(int max_node_no, double r, double dx, double dy, double dz,
+                                   int n_nodes, const double* nodes_colmajor, int order_mode,
+                                   int* clouds_colmajor, int* cloud_lengths, int* max_cloud_length) {
+  clear_error();
+  if (n_nodes <= 0 || !nodes_colmajor) return set_error(NNPP_ERR_INVALID, "no nodes");
+  if (!have_gpu()) return set_error(NNPP_ERR_CUDA, "no CUDA device");
+  cudaStream_t st;
+  NNPP_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  nnpp_status res = NNPP_OK;
+  {
+    DBuf<double> xyz;
+    RefLists L;
+    if (!xyz.alloc(3 * (size_t)n_nodes)) {
+      res = set_error(NNPP_ERR_NOMEM, "nodes");
+    } else {
+      cudaMemcpyAsync(xyz.get(), nodes_colmajor, sizeof(double) * 3 * (size_t)n_nodes,
+                      cudaMemcpyHostToDevice, st);
+      res = build_ref_lists(st, n_nodes, xyz.get(), xyz.get() + n_nodes, xyz.get() + 2 * (size_t)n_nodes,
+                            max_node_no, r, dx, dy, dz, order_mode, L);
+      if (res == NNPP_OK) res = emit_padded(st, L, max_node_no, clouds_colmajor, cloud_lengths);
+      if (res == NNPP_OK && max_cloud_length) *max_cloud_length = L.max_len;
+    }
+    cudaStreamSynchronize(st);
+  }
+  cudaStreamDestroy(st);
+  return res;
+}
+
+nnpp_status nnpp_create(nnpp_handle** out, const nnpp_params* p, int n_nodes,
+                        const double* nodes_colmajor, const int* bctypes, const double* bcvalues,
+                        const double* icvalues, const int* phase0) {
+  clear_error();
+  if (!out) return set_error(NNPP_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  NNPP_TRY(check_params(p));
+  if (n_nodes <= 0 || !nodes_colmajor || !bctypes || !bcvalues || !icvalues)
+    return set_error(NNPP_ERR_INVALID, "create: missing inputs");
+  if (!have_gpu()) return set_error(NNPP_ERR_CUDA, "no CUDA device");
+  nnpp_handle* hp = new nnpp_handle();
+  Handle& h = hp->h;
+  h.p = *p;
+  h.N = n_nodes;
+  cudaGetDevice(&h.device);
+  auto fail = [&](nnpp_status st) {
+    nnpp_destroy(hp);
+    return st;
+  };
+  if (cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h.st_b1, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h.st_b2, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_error(NNPP_ERR_CUDA, "stream creation"));
+  const size_t N = n_nodes;
+  if (!h.ux.alloc(N) || !h.uy.alloc(N) || !h.uz.alloc(N)) return fail(set_error(NNPP_ERR_NOMEM, "nodes"));
+  if (cudaMemcpyAsync(h.ux.get(), nodes_colmajor, sizeof(double) * N, cudaMemcpyHostToDevice, h.st) ||
+      cudaMemcpyAsync(h.uy.get(), nodes_colmajor + N, sizeof(double) * N, cudaMemcpyHostToDevice, h.st) ||
+      cudaMemcpyAsync(h.uz.get(), nodes_colmajor + 2 * N, sizeof(double) * N, cudaMemcpyHostToDevice, h.st) ||
+      cudaStreamSynchronize(h.st))
+    return fail(set_error(NNPP_ERR_CUDA, "node upload"));
+  for (size_t i = 0; i < 3 * N; ++i)
+    if (!std::isfinite(nodes_colmajor[i])) return fail(set_error(NNPP_ERR_INVALID, "non-finite node coordinate"));
+  h.h_bctypes.assign(bctypes, bctypes + N);
+  h.h_bcv.assign(bcvalues, bcvalues + (S + 1) * N);
+  h.h_ic.assign(icvalues, icvalues + (S + 1) * N);
+  h.h_phase0.resize(N);
+  for (size_t i = 0; i < N; ++i)
+    h.h_phase0[i] = phase0 ? (phase0[i] != 0 ? 1 : 0) : (icvalues[i] > 0.0 + 10E-6 ? 1 : 0);
+  *out = hp;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_destroy(nnpp_handle* hp) {
+  if (!hp) return NNPP_OK;
+  Handle& h = hp->h;
+  cudaSetDevice(h.device);
+  if (h.st) cudaStreamSynchronize(h.st);
+  destroy_graphs(h);
+  if (h.st) cudaStreamDestroy(h.st);
+  if (h.st_b1) cudaStreamDestroy(h.st_b1);
+  if (h.st_b2) cudaStreamDestroy(h.st_b2);
+  delete hp;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, double cx, double cy,
+                                  double cz, int order_mode, int* clouds_colmajor, int* cloud_lengths,
+                                  int* max_cloud_length) {
+  NNPP_GUARD(hp);
+  Handle& h = hp->h;
+  destroy_graphs(h);
+  h.built = false;
+  NNPP_TRY(build_ref_lists(h.st, h.N, h.ux.get(), h.uy.get(), h.uz.get(), max_node_no, r, cx, cy, cz,
+                           order_mode, h.ref));
+  h.max_node_no = max_node_no;
+  NNPP_TRY(emit_padded(h.st, h.ref, max_node_no, clouds_colmajor, cloud_lengths));
+  if (max_cloud_length) *max_cloud_length = h.ref.max_len;
+  const nnpp_params& p = h.p;
+  NNPP_TRY(build_layout(h.st, h.ref, h.ux.get(), h.uy.get(), h.uz.get(), r, p.delta, p.dx,
+                        p.dx * p.dy * p.dz, p.s_phi, h.lay));
+  NNPP_TRY(step_alloc(h));
+  // per-node constants in internal order (main.cpp:676-712: Dirichlet where bctypes == 0
+  // and bcvalues != -1; species values divided by CSolid, the potential's not)
+  const size_t N = h.N;
+  std::vector<int> perm(N);
+  NNPP_CUDA(cudaMemcpyAsync(perm.data(), h.lay.perm.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  std::vector<unsigned char> dm(N, 0);
+  std::vector<double> bcv((S + 1) * N, 0.0);
+  for (size_t a = 0; a < N; ++a) {
+    const int u = perm[a];
+    for (int f = 0; f <= S; ++f) {
+      const double v = h.h_bcv[(size_t)f * N + u];
+      if (h.h_bctypes[u] == 0 && v != -1) {
+        dm[a] |= (unsigned char)(1u << f);
+        bcv[(size_t)f * N + a] = (f < S) ? v / p.CSolid : v;
+      }
+    }
+  }
+  NNPP_CUDA(cudaMemcpyAsync(h.dirmask.get(), dm.data(), N, cudaMemcpyHostToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.bcval.get(), bcv.data(), sizeof(double) * (S + 1) * N, cudaMemcpyHostToDevice, h.st));
+  // initial state (main.cpp:398-420 with the given phase)
+  DevState ds;
+  std::memset(&ds, 0, sizeof(ds));
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  h.cur = 0;
+  NNPP_TRY(upload_state(h, h.h_ic.data(), h.h_ic.data() + S * N, h.h_phase0.data(), NNPP_FP64));
+  NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, sizeof(int) * N, h.st));
+  NNPP_TRY(init_diag(h));
+  NNPP_TRY(push_settings(h));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.built = true;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_neighbours_csr(nnpp_handle* hp, int* row_ptr, int* cols, int64_t* nnz_out) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  Handle& h = hp->h;
+  if (nnz_out) *nnz_out = h.ref.nnz;
+  if (row_ptr)
+    NNPP_CUDA(cudaMemcpyAsync(row_ptr, h.ref.ptr.get(), sizeof(int) * (h.N + 1), cudaMemcpyDeviceToHost, h.st));
+  if (cols && h.ref.nnz > 0)
+    NNPP_CUDA(cudaMemcpyAsync(cols, h.ref.col.get(), sizeof(int) * h.ref.nnz, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_set_solver(nnpp_handle* hp, double tol, int max_iter, int strict) {
+  NNPP_GUARD(hp);
+  if (!(tol > 0) || max_iter < 1) return set_error(NNPP_ERR_INVALID, "tol must be > 0, max_iter >= 1");
+  Handle& h = hp->h;
+  h.tol = tol;
+  h.max_iter = max_iter;
+  h.strict = strict;
+  if (h.built) NNPP_TRY(push_settings(h));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_forward(nnpp_handle* hp, int n_steps, int precision) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (n_steps < 0) return set_error(NNPP_ERR_INVALID, "n_steps < 0");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  Handle& h = hp->h;
+  DevState before;
+  NNPP_TRY(read_state(h, &before));
+  NNPP_TRY(run_steps(h, n_steps, precision));
+  return check_after(h, before.cg_nc);
+}
+
+nnpp_status nnpp_get_state(nnpp_handle* hp, double* c, double* phi, int* phase) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  Handle& h = hp->h;
+  const size_t N = h.N;
+  NNPP_TRY(store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get()));
+  if (c) NNPP_CUDA(cudaMemcpyAsync(c, h.user_stage.get(), sizeof(double) * S * N, cudaMemcpyDeviceToHost, h.st));
+  if (phi)
+    NNPP_CUDA(cudaMemcpyAsync(phi, h.user_stage.get() + S * N, sizeof(double) * N, cudaMemcpyDeviceToHost, h.st));
+  if (phase) NNPP_CUDA(cudaMemcpyAsync(phase, h.user_stage_i.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_set_state(nnpp_handle* hp, const double* c, const double* phi, const int* phase) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (!c) return set_error(NNPP_ERR_INVALID, "c is NULL");
+  Handle& h = hp->h;
+  NNPP_TRY(upload_state(h, c, phi, phase, h.state_prec));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_diagnostics(nnpp_handle* hp, nnpp_diag* out) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (!out) return set_error(NNPP_ERR_INVALID, "out is NULL");
+  Handle& h = hp->h;
+  DevState ds;
+  NNPP_TRY(read_state(h, &ds));
+  const double dV = h.p.dx * h.p.dy * h.p.dz;
+  std::memset(out, 0, sizeof(*out));
+  out->steps_done = ds.steps;
+  out->solid_count = ds.solid_count;
+  out->voln1rel = ds.voln1rel;
+  out->vol0rel = ds.vol0rel;
+  for (int s = 0; s < S; ++s) out->mass[s] = ds.mass[s] * dV;
+  out->mg_mass_lost = (ds.mg_mass_t0 - ds.mg_mass_now) * dV;
+  out->dissolved_total = ds.dissolved * h.p.dt * dV;
+  out->cg_iterations_total = ds.cg_iters;
+  out->cg_solves = ds.cg_solves;
+  out->cg_not_converged = ds.cg_nc;
+  out->last_rel_residual = ds.last_relres;
+  out->outer_iterations_total = ds.outer_total;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_flip_steps(nnpp_handle* hp, int* flip_step) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (!flip_step) return set_error(NNPP_ERR_INVALID, "flip_step is NULL");
+  Handle& h = hp->h;
+  const size_t N = h.N;
+  std::vector<int> perm(N), fs(N);
+  NNPP_CUDA(cudaMemcpyAsync(perm.data(), h.lay.perm.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(fs.data(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  for (size_t a = 0; a < N; ++a) flip_step[perm[a]] = fs[a];
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_step_host(nnpp_handle* hp, int precision, const double* c_in, const int* phase_in,
+                           double* c_out, double* phi_out, int* phase_out) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  if (!c_in) return set_error(NNPP_ERR_INVALID, "c_in is NULL");
+  Handle& h = hp->h;
+  DevState before;
+  NNPP_TRY(read_state(h, &before));
+  NNPP_TRY(upload_state(h, c_in, nullptr, phase_in, precision));
+  NNPP_TRY(run_steps(h, 1, precision));
+  const size_t N = h.N;
+  NNPP_TRY(store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get()));
+  if (c_out) NNPP_CUDA(cudaMemcpyAsync(c_out, h.user_stage.get(), sizeof(double) * S * N, cudaMemcpyDeviceToHost, h.st));
+  if (phi_out)
+    NNPP_CUDA(cudaMemcpyAsync(phi_out, h.user_stage.get() + S * N, sizeof(double) * N, cudaMemcpyDeviceToHost, h.st));
+  if (phase_out)
+    NNPP_CUDA(cudaMemcpyAsync(phase_out, h.user_stage_i.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  return check_after(h, before.cg_nc);
+}
+
+nnpp_status nnpp_residuals(nnpp_handle* hp, int precision, const double* c, const double* phi,
+                           const int* phase, double voln1rel, double* F) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (!c || !phi || !phase || !F) return set_error(NNPP_ERR_INVALID, "residuals: NULL argument");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  Handle& h = hp->h;
+  StateBackup b;
+  NNPP_TRY(backup(h, b));
+  h.cur ^= 1;
+  nnpp_status st = upload_state(h, c, phi, phase, precision);
+  DBuf<double> Fd;
+  if (st == NNPP_OK && !Fd.alloc((S + 1) * (size_t)h.N)) st = set_error(NNPP_ERR_NOMEM, "residual output");
+  if (st == NNPP_OK) {
+    NNPP_CUDA(cudaMemcpyAsync(h.scratch_d.get(), &voln1rel, sizeof(double), cudaMemcpyHostToDevice, h.st));
+    KParams kp = make_kparams(h, h.cur);
+    kp.voln1rel_ptr = h.scratch_d.get();
+    st = launch_transport(h, kp, precision, h.st, Fd.get());
+    if (st == NNPP_OK) st = launch_prep(h, kp, precision, h.st, 0, Fd.get() + (size_t)S * h.N);
+    if (st == NNPP_OK) {
+      k_unpermute<<<h.grid, kBlockHost, 0, h.st>>>(h.lay.perm.get(), h.N, S + 1, Fd.get(), h.user_stage.get());
+      if (cudaGetLastError() != cudaSuccess) st = set_error(NNPP_ERR_CUDA, "unpermute");
+    }
+    if (st == NNPP_OK)
+      NNPP_CUDA(cudaMemcpyAsync(F, h.user_stage.get(), sizeof(double) * (S + 1) * h.N, cudaMemcpyDeviceToHost, h.st));
+    cudaStreamSynchronize(h.st);
+  }
+  nnpp_status st2 = restore(h, b);
+  return st != NNPP_OK ? st : st2;
+}
+
+nnpp_status nnpp_solve_potential(nnpp_handle* hp, int precision, const double* c, const int* phase,
+                                 double* phi, int* iterations, double* rel_residual) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (!c || !phase || !phi) return set_error(NNPP_ERR_INVALID, "solve_potential: NULL argument");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  Handle& h = hp->h;
+  StateBackup b;
+  NNPP_TRY(backup(h, b));
+  h.cur ^= 1;
+  nnpp_status st = upload_state(h, c, phi, phase, precision);
+  if (st == NNPP_OK) st = push_settings(h);
+  if (st == NNPP_OK) st = build_graph(h, kGraphSolve, precision, h.cur);
+  DevState ds0, ds1;
+  if (st == NNPP_OK) st = read_state(h, &ds0);
+  if (st == NNPP_OK && cudaGraphLaunch(h.gexec[kGraphSolve][precision][h.cur], h.st) != cudaSuccess)
+    st = set_error(NNPP_ERR_CUDA, "graph launch");
+  if (st == NNPP_OK) st = read_state(h, &ds1);
+  if (st == NNPP_OK) {
+    const size_t N = h.N;
+    st = store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get());
+    if (st == NNPP_OK) {
+      NNPP_CUDA(cudaMemcpyAsync(phi, h.user_stage.get() + S * N, sizeof(double) * N, cudaMemcpyDeviceToHost, h.st));
+      NNPP_CUDA(cudaStreamSynchronize(h.st));
+    }
+    if (iterations) *iterations = (int)(ds1.cg_iters - ds0.cg_iters);
+    if (rel_residual) *rel_residual = ds1.last_relres;
+    if (st == NNPP_OK && h.strict && ds1.cg_nc > ds0.cg_nc)
+      st = set_error(NNPP_ERR_CG_NO_CONVERGE, "potential solve hit its iteration cap");
+  }
+  nnpp_status st2 = restore(h, b);
+  return st != NNPP_OK ? st : st2;
+}
+
+}  // extern "C"

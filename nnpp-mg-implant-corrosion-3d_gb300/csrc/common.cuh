@@ -1,0 +1,198 @@
+// common.cuh -- device helpers and internal data structures of the GB300 NNPP library.
+#ifndef NNPP_COMMON_CUH
+#define NNPP_COMMON_CUH
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "nnpp_gb300.h"
+#include "nnpp_internal.h"
+
+namespace nnpp {
+
+constexpr int S = NNPP_NSPECIES;
+constexpr int kReduceSlots = 16;   // values reduced per block by the step kernels
+constexpr int kMaxPartialBlocks = 4096;
+
+// CUDA call check inside functions returning nnpp_status.
+#define NNPP_CUDA(call)                                                                     \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return ::nnpp::set_error(NNPP_ERR_CUDA, std::string(#call) + ": " +                   \
+                                                  cudaGetErrorString(e_));                  \
+  } while (0)
+
+#define NNPP_TRY(call)                  \
+  do {                                  \
+    nnpp_status s_ = (call);            \
+    if (s_ != NNPP_OK) return s_;       \
+  } while (0)
+
+// ---------------------------------------------------------------------------------------
+// Node records gathered by the bond kernels: one 32-byte (FP32) or 64-byte (FP64) aligned
+// record per node, so that a neighbour costs one or two sectors.
+struct __align__(32) Rec32 {
+  float c[S];     // concentrations (high word of the compensated pair)
+  float phi_hi;   // potential, high word
+  float phi_lo;   // potential, low word (phi = phi_hi + phi_lo to ~1e-14 absolute)
+  float phase;    // 1 solid, 0 liquid
+  float pad;
+};
+
+struct __align__(32) Rec64 {
+  double c[S];
+  double phi;
+  double phase;
+  double pad[2];
+};
+
+// Scalars that live on the device for the whole run (diagnostics, CG state, counters).
+struct DevState {
+  // diagnostics (nnpp_diag)
+  long long steps;
+  long long solid_count;
+  double voln1rel;
+  double vol0rel;
+  double mass[S];
+  double mg_mass_t0;
+  double dissolved;
+  long long cg_iters;
+  long long cg_solves;
+  long long cg_nc;
+  double last_relres;
+  long long outer_total;
+  int nonfinite;
+  int pad0;
+  // potential solve
+  double bnorm2;      // ||b_eff||^2
+  double rnorm2;      // ||r||^2 of the outer (FP64) residual
+  double rr0;         // inner: ||r||^2 at start
+  double rr;          // inner: current ||r||^2
+  double rz;          // inner: r.z
+  double alpha, beta;
+  double tol;         // relative tolerance of the solve
+  double inner_rel;   // inner relative reduction per refinement sweep
+  double inner_target;  // inner: stop when ||r||^2 <= inner_target
+  int inner_it;
+  int outer_it;
+  int max_iter;
+  int max_outer;
+  int solve_iters;    // inner iterations of the current solve
+  int pad1;
+  // per-step mass-curve sampling (adjoint forward)
+  double mg_mass_now;
+  // block tickets for last-block reductions
+  unsigned int ticket[8];
+};
+
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void two_sum_d(double a, double b, double& s, double& e) {
+  s = a + b;
+  double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Compensated reduction of (value, error) pairs over `width` lanes of a warp segment.
+template <int WIDTH>
+__device__ __forceinline__ float comp_reduce(float v) {
+  float err = 0.0f;
+#pragma unroll
+  for (int off = WIDTH / 2; off > 0; off >>= 1) {
+    float ov = __shfl_down_sync(0xffffffffu, v, off, WIDTH);
+    float oe = __shfl_down_sync(0xffffffffu, err, off, WIDTH);
+    float s, e;
+    two_sum(v, ov, s, e);
+    v = s;
+    err = err + oe + e;
+  }
+  return v + err;
+}
+
+template <int WIDTH>
+__device__ __forceinline__ double seg_reduce_d(double v) {
+#pragma unroll
+  for (int off = WIDTH / 2; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off, WIDTH);
+  return v;
+}
+
+template <int WIDTH>
+__device__ __forceinline__ int seg_or(int v) {
+#pragma unroll
+  for (int off = WIDTH / 2; off > 0; off >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, off, WIDTH);
+  return v;
+}
+
+// Block-wide sum of NV doubles per thread into block_out[NV] (thread 0 holds the result).
+template <int NV, int BLOCK>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* NV*BLOCK/32 */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if (lane == 0) smem[k * (BLOCK / 32) + wid] = x;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = (lane < BLOCK / 32) ? smem[k * (BLOCK / 32) + lane] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      v[k] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// Last-block pattern: every block writes its partials, the block that takes the final
+// ticket reduces them in block order (deterministic) and resets the ticket.
+// Returns true in the last block (all threads).
+__device__ __forceinline__ bool take_last_ticket(unsigned int* ticket, int* s_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int t = atomicAdd(ticket, 1u);
+    *s_flag = (t == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  bool last = *s_flag != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+// Reduce NV partials per block (layout partials[k * nblk + b]) in the last block.
+template <int NV, int BLOCK>
+__device__ __forceinline__ void reduce_partials(const double* partials, int nblk, double (&out)[NV],
+                                                double* smem) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += BLOCK) x += partials[k * nblk + b];
+    out[k] = x;
+  }
+  block_sum<NV, BLOCK>(out, smem);
+}
+
+// beta of utils.h:17-25
+template <typename T>
+__device__ __forceinline__ T beta_fn(T xi, T delta, T dx) {
+  T h = dx / T(2);
+  if (xi <= delta - h) return T(1);
+  if (xi > delta - h && xi <= delta + h) return (delta + h - xi) / dx;
+  return T(0);
+}
+
+}  // namespace nnpp
+
+#endif  // NNPP_COMMON_CUH

@@ -1,0 +1,65 @@
+"""Build recipe of the oracle (test infrastructure).
+
+Compiles
+  oracle/nnpp_oracle.cpp  -> oracle/liboracle.so        (always; g++ with OpenMP)
+  oracle/ref_shim.cpp     -> oracle/_ref/libnnpp_ref.so (only where the reference's
+                             sources are present, i.e. REFERENCE_ROOT exists)
+The reference shim is compiled from the reference's own headers where they lie; nothing of
+the reference is copied into this repository.  Both libraries are checkers for the tests,
+never part of the product.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE_ROOT = os.environ.get("NNPP_REFERENCE_ROOT", "/root/reference")
+
+# -ffp-contract=off: the reference is built without FMA contraction on x86-64 (-msse2,
+# CMakeLists.txt:51-54); keeping products and sums separate makes the restatement give the
+# same roundings on aarch64 hosts, where GCC would otherwise fuse them.
+CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17"]
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_oracle(force=False, verbose=False):
+    out = os.path.join(HERE, "liboracle.so")
+    srcs = [os.path.join(HERE, "nnpp_oracle.cpp"),
+            os.path.join(HERE, "..", "include", "nnpp_gb300.h")]
+    if force or not _newer(out, srcs):
+        cmd = ["g++"] + CXXFLAGS + [srcs[0], "-o", out]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+    return out
+
+
+def build_reference_shim(force=False, verbose=False):
+    """Returns the path of the shim, or None when the reference is not present."""
+    helpers = os.path.join(REFERENCE_ROOT, "src", "helpers")
+    eigen = os.path.join(REFERENCE_ROOT, "eigen")
+    if not (os.path.isdir(helpers) and os.path.isdir(eigen)):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libnnpp_ref.so")
+    src = os.path.join(HERE, "ref_shim.cpp")
+    deps = [src, os.path.join(helpers, "grid.h"), os.path.join(helpers, "utils.h")]
+    if force or not _newer(out, deps):
+        cmd = ["g++"] + CXXFLAGS + ["-w", "-I", helpers, "-I", eigen, src, "-o", out]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+    return out
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_oracle(force, True))
+    print(build_reference_shim(force, True))

@@ -1,0 +1,677 @@
+// nnpp_oracle.cpp -- FP64 CPU oracle of the nonlocal Nernst-Planck-Poisson hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker: tests, the smoke check and the
+// CPU-baseline leg of the benchmark call it; the product library never links or calls
+// it.  It restates, in plain C++ with OpenMP, the reference's algorithm for the path:
+//
+//   neighbour build   grid.h:22-204          (build_clouds_hash, sphere_cube_intersects)
+//   influence factor  utils.h:17-25          (Beta)
+//   bond sums         utils.h:72-178 (Mg), utils.h:181-257 (generic species)
+//   potential         utils.h:798-841 (F11), utils.h:1794-1848 (K11)
+//   step / front      main.cpp:556-640, 676-712 (Dirichlet), 805-837 (clamp),
+//                     914-922 (phase flip), 472-480 and 944-949 (volume)
+//
+// turned into the explicit step:  c^{n+1} = c^n - dt * (sum_KR1 + sum_KR2 - R)  with the
+// potential phi^n solved from c^n (Jacobi-preconditioned CG, FP64) before the transport,
+// and the Mg source R_0 = -k_diss * S(c_0 - CSat/CSolid) on solid interface nodes
+// (the position of the reference's Mg rate terms, utils.h:162-167).
+//
+// Parity is pinned against the reference itself: ref_shim.cpp compiles grid.h and utils.h
+// from the reference's sources and the tests compare this restatement with them (neighbour
+// lists bit for bit, residuals and K11 to rounding); golden fixtures made from those runs
+// are committed under tests/golden/.  Operation order inside each bond term follows the
+// reference's expressions so that the FP64 residuals agree bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <utility>
+#include <vector>
+
+#include <omp.h>
+
+#include "../include/nnpp_gb300.h"
+
+namespace {
+
+const int S = NNPP_NSPECIES;
+
+inline double sqr(double x) { return x * x; }
+
+// grid.h:27-41
+bool sphere_cube(double cx, double cy, double cz, double r, double bx, double by, double bz,
+                 double w, double h, double d) {
+  const double bmin[3] = {bx, by, bz};
+  const double bmax[3] = {bx + w, by + h, bz + d};
+  const double c[3] = {cx, cy, cz};
+  const double r2 = sqr(r);
+  double dmin = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    if (c[i] < bmin[i])
+      dmin += sqr(c[i] - bmin[i]);
+    else if (c[i] > bmax[i])
+      dmin += sqr(c[i] - bmax[i]);
+  }
+  return dmin <= r2;
+}
+
+// utils.h:17-25
+double beta_fn(double xi, double delta, double dx) {
+  if (xi <= delta - dx / 2.0) return 1.0;
+  if ((xi > delta - dx / 2.0) && (xi <= delta + dx / 2.0)) return (delta + dx / 2.0 - xi) / (dx);
+  return 0.0;
+}
+
+struct Oracle {
+  nnpp_params p;
+  int N = 0;
+  std::vector<double> x, y, z;
+  std::vector<int> bctypes;
+  std::vector<double> bcv;  // (S+1)*N
+  std::vector<unsigned char> dir;  // (S+1)*N Dirichlet flags
+  // neighbour lists, reference format: row i = cols[row_ptr[i] .. row_ptr[i+1]), slot 0 self
+  std::vector<int64_t> row_ptr;
+  std::vector<int> cols;
+  bool have_nb = false;
+  // state
+  std::vector<double> c;  // S*N
+  std::vector<double> phi;  // N
+  std::vector<int> phase;
+  std::vector<int> flip_step;
+  std::vector<double> c0_init;  // Mg at t = 0
+  double vol0rel = 0.0, voln1rel = 0.0;
+  int64_t steps_done = 0;
+  int64_t solid_count = 0;
+  double dissolved_total = 0.0;
+  int64_t cg_iters_total = 0, cg_solves = 0, cg_nc = 0;
+  double last_relres = 0.0;
+  double tol = 1e-12;
+  int max_iter = 20000;
+  // potential operator cache (rebuilt when the phase changes)
+  std::vector<double> wphi;  // per bond, w of the potential (K11 form), 0 if not LL
+  std::vector<double> diag;
+  std::vector<unsigned char> freev;
+  bool op_valid = false;
+  // adjoint checkpoints
+  struct Ckpt {
+    std::vector<double> c, phi;
+    std::vector<int> phase;
+    double voln1rel;
+  };
+  std::vector<Ckpt> ckpts;
+  int ck_every = 0, sample_every = 0, fwd_steps = 0;
+  std::vector<double> curve;
+};
+
+double mg_source_switch(const nnpp_params& p, double c0) {
+  double cs = p.CSat / p.CSolid;
+  if (p.switch_width > 0.0) return 1.0 / (1.0 + std::exp(-(c0 - cs) / p.switch_width));
+  return c0 > cs ? 1.0 : 0.0;
+}
+
+double mg_source_switch_deriv(const nnpp_params& p, double c0) {
+  if (p.switch_width <= 0.0) return 0.0;
+  double cs = p.CSat / p.CSolid;
+  double s = 1.0 / (1.0 + std::exp(-(c0 - cs) / p.switch_width));
+  return s * (1.0 - s) / p.switch_width;
+}
+
+// ---------------------------------------------------------------- neighbour build --------
+// grid.h:43-204.  Step 5 of the reference tests every cell against the sphere; here the
+// scan is limited to the cells within one cell of the sphere's bounding box, which contains
+// every cell the exact test can accept, and the accepted cells are visited in the same
+// ascending-hash order, so the lists are identical.
+int build_clouds(int max_node_no, double r, double cx, double cy, double cz, int N,
+                 const double* X, const double* Y, const double* Z, std::vector<int64_t>& row_ptr,
+                 std::vector<int>& cols, int* max_len) {
+  if (N <= 0) return 1;
+  double x0 = X[0], x1 = X[0], y0 = Y[0], y1 = Y[0], z0 = Z[0], z1 = Z[0];
+  for (int i = 0; i < N; ++i) {
+    x0 = std::min(x0, X[i]);
+    x1 = std::max(x1, X[i]);
+    y0 = std::min(y0, Y[i]);
+    y1 = std::max(y1, Y[i]);
+    z0 = std::min(z0, Z[i]);
+    z1 = std::max(z1, Z[i]);
+  }
+  const int mx = static_cast<int>((x1 - x0) / cx) + 1;
+  const int my = static_cast<int>((y1 - y0) / cy) + 1;
+  std::vector<std::pair<int, int> > hashes(N);
+#pragma omp parallel for
+  for (int i = 0; i < N; ++i) {
+    hashes[i].first = i;
+    hashes[i].second = static_cast<int>((X[i] - x0) / cx) + mx * static_cast<int>((Y[i] - y0) / cy) +
+                       mx * my * static_cast<int>((Z[i] - z0) / cz);
+  }
+  std::sort(hashes.begin(), hashes.end(),
+            [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.second < b.second; });
+  const int max_hash = hashes[N - 1].second + 1;
+  std::vector<int> start(max_hash + 1, 0), count(max_hash, 0);
+  for (int k = 0; k < N; ++k) count[hashes[k].second]++;
+  {
+    int acc = 0;
+    for (int h = 0; h < max_hash; ++h) {
+      start[h] = acc;
+      acc += count[h];
+    }
+    start[max_hash] = acc;
+  }
+  std::vector<int> len(N);
+  std::vector<std::vector<int> > rows(N);
+  int err = 0;
+  const double r2 = sqr(r);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < N; ++i) {
+    const double px = X[i], py = Y[i], pz = Z[i];
+    int lo[3], hi[3];
+    const double o[3] = {x0, y0, z0}, w[3] = {cx, cy, cz}, q[3] = {px, py, pz};
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = (int)std::floor((q[d] - r - o[d]) / w[d]) - 1;
+      hi[d] = (int)std::floor((q[d] + r - o[d]) / w[d]) + 1;
+      if (lo[d] < 0) lo[d] = 0;
+    }
+    if (hi[0] > mx - 1) hi[0] = mx - 1;
+    if (hi[1] > my - 1) hi[1] = my - 1;
+    std::vector<int>& row = rows[i];
+    row.clear();
+    row.push_back(i);
+    int fill = 1;
+    for (int kz = lo[2]; kz <= hi[2]; ++kz)
+      for (int ky = lo[1]; ky <= hi[1]; ++ky)
+        for (int kx = lo[0]; kx <= hi[0]; ++kx) {
+          int m = kx + mx * ky + mx * my * kz;
+          if (m >= max_hash) continue;
+          // corner as grid.h:129-140
+          int rr = (m % (mx * my)) % mx;
+          int cc = (m % (mx * my)) / mx;
+          int pp = m / (mx * my);
+          double bx = x0 + rr * cx, by = y0 + cc * cy, bz = z0 + pp * cz;
+          if (!sphere_cube(px, py, pz, r, bx, by, bz, cx, cy, cz)) continue;
+          if (count[m] == 0) continue;
+          for (int k = start[m]; k < start[m] + count[m]; ++k) {
+            int cand = hashes[k].first;
+            if (sqr(px - X[cand]) + sqr(py - Y[cand]) + sqr(pz - Z[cand]) <= r2 && cand != i) {
+              if (fill == max_node_no) {
+#pragma omp atomic write
+                err = 1;
+                break;
+              }
+              row.push_back(cand);
+              fill++;
+            }
+          }
+        }
+    len[i] = fill;
+  }
+  if (err) return 2;
+  row_ptr.assign(N + 1, 0);
+  for (int i = 0; i < N; ++i) row_ptr[i + 1] = row_ptr[i] + len[i];
+  cols.resize(row_ptr[N]);
+  int ml = 0;
+#pragma omp parallel for reduction(max : ml)
+  for (int i = 0; i < N; ++i) {
+    std::copy(rows[i].begin(), rows[i].end(), cols.begin() + row_ptr[i]);
+    ml = std::max(ml, len[i]);
+  }
+  *max_len = ml;
+  return 0;
+}
+
+// ---------------------------------------------------------------- bond sums --------------
+// Residual F_k (utils.h:72-178 for k = 0, utils.h:181-257 for k >= 1) with U^{n+1} = U^n
+// and the reference's operation order; R_k is the dissolution source of species 0.
+// Optional outputs: transport part per species (sum_KR1 + sum_KR2) and the interface flag.
+void residuals(const Oracle& o, const double* c, const double* phi, const int* phase,
+               double voln1rel, double* F, double* transport, unsigned char* iface_out) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  const double BVmix = std::pow(10., -p.vol_red * (1. - voln1rel));
+  const double csat = p.CSat / p.CSolid;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    const int64_t b = o.row_ptr[i], e = o.row_ptr[i + 1];
+    int iface = 0;
+    if (phase[i] == 1)
+      for (int64_t j = b + 1; j < e; ++j)
+        if (phase[o.cols[j]] == 0) {
+          iface = 1;
+          break;
+        }
+    if (iface_out) iface_out[i] = (unsigned char)iface;
+    for (int k = 0; k < S; ++k) {
+      const double* ck = c + (int64_t)k * N;
+      double s1 = 0.0, s2 = 0.0;
+      for (int64_t j = b + 1; j < e; ++j) {
+        const int n = o.cols[j];
+        const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+        const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+        const int pi = phase[i], pn = phase[n];
+        double a1, a2;  // K*D(*BV) prefixes, in the reference's multiplication order
+        if (k == 0) {
+          double BV = ((pi == 1 && pn == 0) || (pn == 1 && pi == 0)) ? BVmix : 1.0;
+          if (pi == 0 && pn == 0) {
+            a1 = p.K1[0] * p.D_liquid[0];
+            a2 = p.K2[0] * p.D_liquid[0];
+          } else {
+            a1 = p.K1[0] * p.D_solid[0] * BV;
+            a2 = p.K2[0] * p.D_solid[0] * BV;
+          }
+        } else {
+          if (pi == 1 && pn == 1) continue;
+          if (pi == 0 && pn == 0) {
+            a1 = p.K1[k] * p.D_liquid[k];
+            a2 = p.K2[k] * p.D_liquid[k];
+          } else {
+            a1 = p.K1[k] * p.D_solid[k];
+            a2 = p.K2[k] * p.D_solid[k];
+          }
+        }
+        const double bt = beta_fn(xi, p.delta, p.dx);
+        s1 += -(a1 * (ck[n] - ck[i]) / std::pow(xi, 3.0 + 2.0 * p.s1[k])) * bt * p.dx * p.dy * p.dz;
+        s2 += -(a2 * p.z[k] * p.F * ck[n] * (phi[n] - phi[i]) /
+                (p.R * p.T * std::pow(xi, 3.0 + 2.0 * p.s2[k]))) *
+              bt * p.dx * p.dy * p.dz;
+      }
+      double R = 0.0;
+      if (k == 0 && iface == 1) R = -p.k_diss * mg_source_switch(p, ck[i]);
+      if (transport) transport[(int64_t)k * N + i] = s1 + s2;
+      F[(int64_t)k * N + i] = ((ck[i] - ck[i]) / p.dt) + s1 + s2 - R;
+    }
+    // potential residual utils.h:798-841
+    double sp = 0.0;
+    int flag = 0;
+    for (int64_t j = b + 1; j < e; ++j) {
+      const int n = o.cols[j];
+      const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+      const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+      if (phase[i] == 0 && phase[n] == 0) {
+        sp += -(p.K_phi * p.sigma * (phi[n] - phi[i]) / std::pow(xi, 3.0 + 2.0 * p.s_phi)) *
+              beta_fn(xi, p.delta, p.dx) * p.dx * p.dy * p.dz;
+        flag = 1;
+      }
+    }
+    double f11 = 0.0;
+    if (flag == 1) {
+      double R11 = 0.0;
+      for (int k = 0; k < S; ++k) R11 += p.z[k] * c[(int64_t)k * N + i];
+      f11 = (1. / (p.K_phi * p.sigma)) * sp - (1. / (p.K_phi * p.sigma)) * p.F * p.CSolid * R11;
+    }
+    F[(int64_t)S * N + i] = f11;
+  }
+}
+
+// ---------------------------------------------------------------- potential --------------
+// K11 (utils.h:1797-1848): off-diagonal -(1/(K sigma)) (K sigma / xi^(3+2s)) beta dV on
+// liquid-liquid bonds, diagonal the negated row sum (same expression), identity rows on
+// Dirichlet nodes and on nodes without liquid-liquid bonds.
+void build_operator(Oracle& o, const int* phase) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  o.wphi.assign(o.cols.size(), 0.0);
+  o.diag.assign(N, 1.0);
+  o.freev.assign(N, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    const int64_t b = o.row_ptr[i], e = o.row_ptr[i + 1];
+    if (o.dir[(int64_t)S * N + i]) continue;
+    double sumK = 0.0;
+    int flag = 0;
+    for (int64_t j = b + 1; j < e; ++j) {
+      const int n = o.cols[j];
+      if (!(phase[i] == 0 && phase[n] == 0)) continue;
+      const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+      const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+      const double bt = beta_fn(xi, p.delta, p.dx);
+      sumK += -(p.K_phi * p.sigma / std::pow(xi, 3.0 + 2.0 * p.s_phi)) * bt * p.dx * p.dy * p.dz;
+      double off = -(1. / (p.K_phi * p.sigma)) * (p.K_phi * p.sigma / std::pow(xi, 3.0 + 2.0 * p.s_phi)) *
+                   bt * p.dx * p.dy * p.dz;
+      o.wphi[j] = -off;  // store w >= 0; the matrix entry is -w
+      flag = 1;
+    }
+    if (flag) {
+      o.diag[i] = -(1. / (p.K_phi * p.sigma)) * sumK;
+      o.freev[i] = 1;
+    }
+  }
+  o.op_valid = true;
+}
+
+double dot(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0.0;
+  const int n = (int)a.size();
+#pragma omp parallel for reduction(+ : s)
+  for (int i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// y = A x on free rows (x must vanish off the free set except where couplings are wanted)
+void apply_A(const Oracle& o, const std::vector<double>& xv, std::vector<double>& yv) {
+  const int N = o.N;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    if (!o.freev[i]) {
+      yv[i] = 0.0;
+      continue;
+    }
+    double s = o.diag[i] * xv[i];
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) s -= o.wphi[j] * xv[o.cols[j]];
+    yv[i] = s;
+  }
+}
+
+// Solve the potential for concentrations c and phase (phi: warm start in, solution out).
+// Free rows: sum_LL w (phi_i - phi_n) = (1/(K sigma)) F CSolid sum_k z_k c_k  (F11 = 0);
+// Dirichlet rows phi = bc (main.cpp:710-711); other rows keep their value.
+int solve_potential(Oracle& o, const double* c, const int* phase, double* phi, int* iters,
+                    double* relres) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  build_operator(o, phase);
+  std::vector<double> xv(phi, phi + N);
+  for (int i = 0; i < N; ++i)
+    if (o.dir[(int64_t)S * N + i]) xv[i] = o.bcv[(int64_t)S * N + i];
+  const double lam = (1. / (p.K_phi * p.sigma)) * p.F * p.CSolid;
+  std::vector<double> bvec(N, 0.0), beff(N, 0.0);
+  for (int i = 0; i < N; ++i) {
+    if (!o.freev[i]) continue;
+    double R11 = 0.0;
+    for (int k = 0; k < S; ++k) R11 += p.z[k] * c[(int64_t)k * N + i];
+    bvec[i] = lam * R11;
+    double cpl = 0.0;
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) {
+      int n = o.cols[j];
+      if (o.wphi[j] != 0.0 && !o.freev[n]) cpl += o.wphi[j] * xv[n];
+    }
+    beff[i] = bvec[i] + cpl;
+  }
+  double bnorm = std::sqrt(dot(beff, beff));
+  if (bnorm == 0.0) bnorm = 1.0;
+  std::vector<double> r(N), zv(N), pv(N), q(N), tmp(N);
+  int it_total = 0;
+  double rel = 0.0;
+  for (int restart = 0; restart < 20; ++restart) {
+    // true residual with the full vector (fixed values included)
+    {
+      std::vector<double> xf(N);
+      for (int i = 0; i < N; ++i) xf[i] = xv[i];
+#pragma omp parallel for schedule(dynamic, 256)
+      for (int i = 0; i < N; ++i) {
+        if (!o.freev[i]) {
+          r[i] = 0.0;
+          continue;
+        }
+        double s = o.diag[i] * xf[i];
+        for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) s -= o.wphi[j] * xf[o.cols[j]];
+        r[i] = bvec[i] - s;
+      }
+    }
+    rel = std::sqrt(dot(r, r)) / bnorm;
+    if (rel <= o.tol || it_total >= o.max_iter) break;
+    for (int i = 0; i < N; ++i) zv[i] = o.freev[i] ? r[i] / o.diag[i] : 0.0;
+    pv = zv;
+    double rz = dot(r, zv);
+    for (int it = 0; it < o.max_iter - it_total; ++it) {
+      apply_A(o, pv, q);
+      double pq = dot(pv, q);
+      if (pq <= 0.0) break;
+      double alpha = rz / pq;
+      for (int i = 0; i < N; ++i) {
+        if (!o.freev[i]) continue;
+        xv[i] += alpha * pv[i];
+        r[i] -= alpha * q[i];
+      }
+      ++it_total;
+      double rn = std::sqrt(dot(r, r)) / bnorm;
+      if (rn <= 0.5 * o.tol) break;
+      for (int i = 0; i < N; ++i) zv[i] = o.freev[i] ? r[i] / o.diag[i] : 0.0;
+      double rz2 = dot(r, zv);
+      double bta = rz2 / rz;
+      rz = rz2;
+      for (int i = 0; i < N; ++i) pv[i] = zv[i] + bta * pv[i];
+    }
+  }
+  for (int i = 0; i < N; ++i) phi[i] = xv[i];
+  if (iters) *iters = it_total;
+  if (relres) *relres = rel;
+  return rel <= o.tol ? 0 : 4;
+}
+
+// ---------------------------------------------------------------- explicit step ----------
+// One step with the reference's order of the per-step operations (main.cpp:547-1025):
+// potential from c^n, transport with the Dirichlet override and the clamp, phase flip,
+// volume every sub_step_no steps.  Optionally records what the adjoint needs.
+struct StepRecord {
+  std::vector<unsigned char> clamped;  // S*N
+};
+
+int step(Oracle& o, StepRecord* rec) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  int it = 0;
+  double rel = 0.0;
+  int st = solve_potential(o, o.c.data(), o.phase.data(), o.phi.data(), &it, &rel);
+  o.cg_iters_total += it;
+  o.cg_solves += 1;
+  o.last_relres = rel;
+  if (st != 0) o.cg_nc += 1;
+  std::vector<double> F((int64_t)(S + 1) * N);
+  std::vector<unsigned char> iface(N);
+  residuals(o, o.c.data(), o.phi.data(), o.phase.data(), o.voln1rel, F.data(), nullptr, iface.data());
+  std::vector<double> cn((int64_t)S * N);
+  double diss = 0.0;
+  if (rec) rec->clamped.assign((int64_t)S * N, 0);
+#pragma omp parallel for reduction(+ : diss)
+  for (int i = 0; i < N; ++i) {
+    for (int k = 0; k < S; ++k) {
+      const int64_t a = (int64_t)k * N + i;
+      double v;
+      if (o.dir[a])
+        v = o.bcv[a] / p.CSolid;
+      else
+        v = o.c[a] - p.dt * F[a];
+      if (v < p.c_floor) {
+        v = p.c_floor;
+        if (rec) rec->clamped[a] = 1;
+      }
+      cn[a] = v;
+    }
+    if (iface[i] && !o.dir[i]) diss += p.k_diss * mg_source_switch(p, o.c[i]);
+  }
+  o.dissolved_total += diss * p.dt * p.dx * p.dy * p.dz;
+  o.c.swap(cn);
+  const double csat = p.CSat / p.CSolid;
+  const int64_t s = o.steps_done + 1;
+  int64_t flips = 0;
+  for (int i = 0; i < N; ++i) {
+    if (o.phase[i] == 1 && o.c[i] <= csat) {
+      o.phase[i] = 0;
+      o.flip_step[i] = (int)s;
+      ++flips;
+    }
+  }
+  o.solid_count -= flips;
+  if (p.sub_step_no > 0 && s % p.sub_step_no == 0) {
+    double v = 0.0;
+    for (int i = 0; i < N; ++i)
+      if (o.phase[i] == 1) v += (o.c[i] - csat);
+    o.voln1rel = (o.vol0rel != 0.0) ? v / o.vol0rel : 0.0;
+  }
+  o.steps_done = s;
+  return st;
+}
+
+double mg_mass_lost(const Oracle& o) {
+  double m = 0.0;
+  for (int i = 0; i < o.N; ++i) m += o.c0_init[i] - o.c[i];
+  return m * o.p.dx * o.p.dy * o.p.dz;
+}
+
+}  // namespace
+
+// ================================================================ C interface =============
+extern "C" {
+
+void* orc_create(const nnpp_params* p, int N, const double* xyz, const int* bctypes,
+                 const double* bcvalues, const double* icvalues, const int* phase0) {
+  Oracle* o = new Oracle();
+  o->p = *p;
+  o->N = N;
+  o->x.assign(xyz, xyz + N);
+  o->y.assign(xyz + N, xyz + 2 * N);
+  o->z.assign(xyz + 2 * N, xyz + 3 * N);
+  o->bctypes.assign(bctypes, bctypes + N);
+  o->bcv.assign(bcvalues, bcvalues + (int64_t)(S + 1) * N);
+  o->dir.assign((int64_t)(S + 1) * N, 0);
+  for (int f = 0; f <= S; ++f)
+    for (int i = 0; i < N; ++i)
+      o->dir[(int64_t)f * N + i] = (bctypes[i] == 0 && bcvalues[(int64_t)f * N + i] != -1) ? 1 : 0;
+  o->c.assign(icvalues, icvalues + (int64_t)S * N);
+  o->phi.assign(icvalues + (int64_t)S * N, icvalues + (int64_t)(S + 1) * N);
+  o->phase.resize(N);
+  for (int i = 0; i < N; ++i) o->phase[i] = phase0 ? phase0[i] : (icvalues[i] > 0.0 + 10E-6 ? 1 : 0);
+  o->flip_step.assign(N, -1);
+  o->c0_init.assign(o->c.begin(), o->c.begin() + N);
+  const double csat = p->CSat / p->CSolid;
+  o->solid_count = 0;
+  o->vol0rel = 0.0;
+  for (int i = 0; i < N; ++i)
+    if (o->phase[i] == 1) {
+      o->solid_count++;
+      o->vol0rel += (o->c[i] - csat);
+    }
+  o->voln1rel = 0.0;
+  return o;
+}
+
+void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+void orc_set_solver(void* h, double tol, int max_iter) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->tol = tol;
+  o->max_iter = max_iter;
+}
+
+int orc_set_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+}
+
+// build_clouds_hash restated; lists kept in the handle
+int orc_build_neighbours(void* h, int max_node_no, double r, double cx, double cy, double cz,
+                         int* max_len) {
+  Oracle* o = static_cast<Oracle*>(h);
+  int st = build_clouds(max_node_no, r, cx, cy, cz, o->N, o->x.data(), o->y.data(), o->z.data(),
+                        o->row_ptr, o->cols, max_len);
+  o->have_nb = (st == 0);
+  o->op_valid = false;
+  return st;
+}
+
+int64_t orc_nnz(void* h) {
+  Oracle* o = static_cast<Oracle*>(h);
+  return o->have_nb ? o->row_ptr[o->N] : -1;
+}
+
+// reference-format lists: lengths (self included), row_ptr (N+1), cols (self first)
+int orc_get_clouds(void* h, int* lengths, int64_t* row_ptr, int* cols) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  for (int i = 0; i < o->N; ++i) {
+    if (lengths) lengths[i] = (int)(o->row_ptr[i + 1] - o->row_ptr[i]);
+  }
+  if (row_ptr) std::copy(o->row_ptr.begin(), o->row_ptr.end(), row_ptr);
+  if (cols) std::copy(o->cols.begin(), o->cols.end(), cols);
+  return 0;
+}
+
+int orc_set_clouds(void* h, const int64_t* row_ptr, const int* cols) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->row_ptr.assign(row_ptr, row_ptr + o->N + 1);
+  o->cols.assign(cols, cols + row_ptr[o->N]);
+  o->have_nb = true;
+  o->op_valid = false;
+  return 0;
+}
+
+int orc_residuals(void* h, const double* c, const double* phi, const int* phase, double voln1rel,
+                  double* F) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  residuals(*o, c, phi, phase, voln1rel, F, nullptr, nullptr);
+  return 0;
+}
+
+// K11 entries in CSR over the reference-format rows: diag[N], off[nnz] (-w, 0 if not LL),
+// free[N].  Rows without liquid-liquid bonds and Dirichlet rows are identity.
+int orc_poisson_matrix(void* h, const int* phase, double* diag, double* off, unsigned char* freev) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  build_operator(*o, phase);
+  for (int i = 0; i < o->N; ++i) {
+    diag[i] = o->diag[i];
+    freev[i] = o->freev[i];
+  }
+  for (size_t j = 0; j < o->wphi.size(); ++j) off[j] = -o->wphi[j];
+  return 0;
+}
+
+int orc_solve_potential(void* h, const double* c, const int* phase, double* phi, int* iters,
+                        double* relres) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  return solve_potential(*o, c, phase, phi, iters, relres);
+}
+
+int orc_forward(void* h, int n_steps) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  int worst = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    int st = step(*o, nullptr);
+    if (st) worst = st;
+  }
+  return worst;
+}
+
+int orc_get_state(void* h, double* c, double* phi, int* phase, int* flip_step) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (c) std::copy(o->c.begin(), o->c.end(), c);
+  if (phi) std::copy(o->phi.begin(), o->phi.end(), phi);
+  if (phase) std::copy(o->phase.begin(), o->phase.end(), phase);
+  if (flip_step) std::copy(o->flip_step.begin(), o->flip_step.end(), flip_step);
+  return 0;
+}
+
+int orc_set_state(void* h, const double* c, const double* phi, const int* phase) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (c) o->c.assign(c, c + (int64_t)S * o->N);
+  if (phi) o->phi.assign(phi, phi + o->N);
+  if (phase) o->phase.assign(phase, phase + o->N);
+  return 0;
+}
+
+// diag layout: [steps, solid_count, voln1rel, vol0rel, mass0..3, mg_mass_lost,
+//               dissolved_total, cg_iters, cg_solves, cg_nc, last_relres]
+int orc_get_diag(void* h, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const double dV = o->p.dx * o->p.dy * o->p.dz;
+  out[0] = (double)o->steps_done;
+  out[1] = (double)o->solid_count;
+  out[2] = o->voln1rel;
+  out[3] = o->vol0rel;
+  for (int k = 0; k < S; ++k) {
+    double m = 0.0;
+    for (int i = 0; i < o->N; ++i) m += o->c[(int64_t)k * o->N + i];
+    out[4 + k] = m * dV;
+  }
+  out[8] = mg_mass_lost(*o);
+  out[9] = o->dissolved_total;
+  out[10] = (double)o->cg_iters_total;
+  out[11] = (double)o->cg_solves;
+  out[12] = (double)o->cg_nc;
+  out[13] = o->last_relres;
+  return 0;
+}
+
+}  // extern "C"

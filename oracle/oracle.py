@@ -1,0 +1,290 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+liboracle.so is the FP64 CPU restatement of the reference's hot path (nnpp_oracle.cpp);
+_ref/libnnpp_ref.so wraps the reference's own grid.h/utils.h (built only where the
+reference's sources are present).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg use this module, as the checker.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+NSPECIES = 4
+
+_orc = None
+_ref = None
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+_LP = C.POINTER(C.c_int64)
+_P = C.c_void_p
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP) if a is not None else None
+
+
+def _lp(a):
+    return a.ctypes.data_as(_LP) if a is not None else None
+
+
+def load_oracle():
+    global _orc
+    if _orc is None:
+        from build_oracle import build_oracle  # noqa: E402 (same directory)
+        path = build_oracle()
+        L = C.CDLL(path)
+        sig = {
+            "orc_create": (_P, [_P, C.c_int, _DP, _IP, _DP, _DP, _IP]),
+            "orc_destroy": (None, [_P]),
+            "orc_set_solver": (None, [_P, C.c_double, C.c_int]),
+            "orc_set_threads": (C.c_int, [C.c_int]),
+            "orc_build_neighbours": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_double,
+                                               C.c_double, _IP]),
+            "orc_nnz": (C.c_int64, [_P]),
+            "orc_get_clouds": (C.c_int, [_P, _IP, _LP, _IP]),
+            "orc_set_clouds": (C.c_int, [_P, _LP, _IP]),
+            "orc_residuals": (C.c_int, [_P, _DP, _DP, _IP, C.c_double, _DP]),
+            "orc_poisson_matrix": (C.c_int, [_P, _IP, _DP, _DP, C.POINTER(C.c_ubyte)]),
+            "orc_solve_potential": (C.c_int, [_P, _DP, _IP, _DP, _IP, _DP]),
+            "orc_forward": (C.c_int, [_P, C.c_int]),
+            "orc_get_state": (C.c_int, [_P, _DP, _DP, _IP, _IP]),
+            "orc_set_state": (C.c_int, [_P, _DP, _DP, _IP]),
+            "orc_get_diag": (C.c_int, [_P, _DP]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _orc = L
+    return _orc
+
+
+def load_reference():
+    """The reference's own code, or None where its sources are absent."""
+    global _ref
+    if _ref is None:
+        from build_oracle import build_reference_shim
+        path = build_reference_shim()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        L.ref_build_clouds_hash.restype = C.c_int
+        L.ref_build_clouds_hash.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double,
+                                            C.c_double, C.c_int, _DP, _IP, _LP]
+        L.ref_get_clouds.argtypes = [_IP, _LP, _IP]
+        L.ref_residuals.argtypes = [C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
+                                    _DP, _DP, _DP, _DP]
+        L.ref_newton_k11.argtypes = [C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
+                                     _DP, _DP, _DP, _LP, _IP, _IP, _DP]
+        _ref = L
+    return _ref
+
+
+DIAG_KEYS = ["steps", "solid_count", "voln1rel", "vol0rel", "mass0", "mass1", "mass2", "mass3",
+             "mg_mass_lost", "dissolved_total", "cg_iters", "cg_solves", "cg_nc", "last_relres"]
+
+
+class Oracle:
+    """FP64 CPU restatement of the explicit step (nnpp_oracle.cpp)."""
+
+    def __init__(self, params, nodes, bctypes, bcvalues, icvalues, phase0=None):
+        L = load_oracle()
+        self.params = params
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.N = self.nodes.shape[1]
+        self._keep = [np.ascontiguousarray(bctypes, dtype=np.int32),
+                      np.ascontiguousarray(bcvalues, dtype=np.float64),
+                      np.ascontiguousarray(icvalues, dtype=np.float64),
+                      None if phase0 is None else np.ascontiguousarray(phase0, dtype=np.int32)]
+        self._h = L.orc_create(C.byref(params), self.N, _dp(self.nodes), _ip(self._keep[0]),
+                               _dp(self._keep[1]), _dp(self._keep[2]), _ip(self._keep[3]))
+
+    @classmethod
+    def from_synth(cls, inp):
+        return cls(inp["params"], inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"],
+                   inp["phase0"])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load_oracle().orc_destroy(self._h)
+            self._h = None
+
+    def set_solver(self, tol=1e-12, max_iter=20000):
+        load_oracle().orc_set_solver(self._h, tol, max_iter)
+
+    def build_neighbours(self, max_node_no=1024, r=None, cell=None):
+        p = self.params
+        r = p.delta * (1.0 + 1e-5) if r is None else r
+        cell = (p.dx * 10.0, p.dy * 10.0, p.dz * 10.0) if cell is None else cell
+        ml = C.c_int(0)
+        st = load_oracle().orc_build_neighbours(self._h, max_node_no, r, cell[0], cell[1],
+                                                cell[2], C.byref(ml))
+        if st != 0:
+            raise RuntimeError("oracle neighbour build failed with status %d" % st)
+        return ml.value
+
+    def clouds(self):
+        """(lengths incl. self, row_ptr int64, cols incl. self at slot 0)"""
+        L = load_oracle()
+        nnz = L.orc_nnz(self._h)
+        lengths = np.empty(self.N, dtype=np.int32)
+        ptr = np.empty(self.N + 1, dtype=np.int64)
+        cols = np.empty(nnz, dtype=np.int32)
+        L.orc_get_clouds(self._h, _ip(lengths), _lp(ptr), _ip(cols))
+        return lengths, ptr, cols
+
+    def set_clouds(self, ptr, cols):
+        ptr = np.ascontiguousarray(ptr, dtype=np.int64)
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        self._keep += [ptr, cols]
+        load_oracle().orc_set_clouds(self._h, _lp(ptr), _ip(cols))
+
+    def residuals(self, c, phi, phase, voln1rel=0.0):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        F = np.empty((NSPECIES + 1, self.N))
+        load_oracle().orc_residuals(self._h, _dp(c), _dp(phi), _ip(phase), voln1rel, _dp(F))
+        return F
+
+    def poisson_matrix(self, phase):
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        nnz = load_oracle().orc_nnz(self._h)
+        diag = np.empty(self.N)
+        off = np.empty(nnz)
+        free = np.empty(self.N, dtype=np.uint8)
+        load_oracle().orc_poisson_matrix(self._h, _ip(phase), _dp(diag), _dp(off),
+                                         free.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        return diag, off, free
+
+    def solve_potential(self, c, phase, phi0=None):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        phi = np.zeros(self.N) if phi0 is None else np.array(phi0, dtype=np.float64)
+        it = C.c_int(0)
+        rel = C.c_double(0)
+        load_oracle().orc_solve_potential(self._h, _dp(c), _ip(phase), _dp(phi), C.byref(it),
+                                          C.byref(rel))
+        return phi, it.value, rel.value
+
+    def forward(self, n_steps):
+        return load_oracle().orc_forward(self._h, n_steps)
+
+    def state(self):
+        c = np.empty((NSPECIES, self.N))
+        phi = np.empty(self.N)
+        ph = np.empty(self.N, dtype=np.int32)
+        fs = np.empty(self.N, dtype=np.int32)
+        load_oracle().orc_get_state(self._h, _dp(c), _dp(phi), _ip(ph), _ip(fs))
+        return c, phi, ph, fs
+
+    def set_state(self, c, phi=None, phase=None):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        phi = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
+        phase = None if phase is None else np.ascontiguousarray(phase, dtype=np.int32)
+        load_oracle().orc_set_state(self._h, _dp(c), _dp(phi), _ip(phase))
+
+    def diagnostics(self):
+        out = np.empty(len(DIAG_KEYS))
+        load_oracle().orc_get_diag(self._h, _dp(out))
+        return dict(zip(DIAG_KEYS, out.tolist()))
+
+
+def set_threads(n):
+    return load_oracle().orc_set_threads(n)
+
+
+# ---------------------------------------------------------------- reference shim --------
+def reference_params_vectors(p):
+    """data2 (51), datac (10x7), datac11 (4) for the reference's parameter object, from an
+    nnpp Params: the hot-path fields, every reaction constant zero (utils.h:2343-2484)."""
+    d2 = np.zeros(51)
+    d2[2], d2[3], d2[4], d2[5], d2[6] = p.dt, p.dx, p.dy, p.dz, p.delta
+    d2[7], d2[8] = p.CSolid, p.CSat
+    d2[47], d2[48], d2[49], d2[50] = p.T, p.R, p.F, p.vol_red
+    dc = np.zeros((10, 7))
+    for k in range(NSPECIES):
+        dc[k] = [p.z[k], p.D_solid[k], p.D_liquid[k], p.s1[k], p.s2[k], p.K1[k], p.K2[k]]
+    d11 = np.array([p.sigma, p.sigma, p.s_phi, p.K_phi])
+    return d2, dc, d11
+
+
+def ref_build_clouds_hash(max_node_no, r, dx, dy, dz, nodes):
+    """(lengths incl. self, row_ptr int64, cols incl. self, max_len) from the reference."""
+    L = load_reference()
+    if L is None:
+        return None
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    N = nodes.shape[1]
+    ml = C.c_int(0)
+    nnz = C.c_int64(0)
+    st = L.ref_build_clouds_hash(max_node_no, r, dx, dy, dz, N, _dp(nodes), C.byref(ml),
+                                 C.byref(nnz))
+    if st != 0:
+        raise RuntimeError("reference build_clouds_hash failed (status %d)" % st)
+    lengths = np.empty(N, dtype=np.int32)
+    ptr = np.empty(N + 1, dtype=np.int64)
+    cols = np.empty(nnz.value, dtype=np.int32)
+    L.ref_get_clouds(_ip(lengths), _lp(ptr), _ip(cols))
+    return lengths, ptr, cols, ml.value
+
+
+def _u11(c, phi, N):
+    U = np.zeros((11, N))
+    U[:NSPECIES] = c
+    U[10] = phi
+    return U
+
+
+def _bc11(bctypes, bcvalues, N):
+    B = -np.ones((11, N))
+    B[:NSPECIES] = bcvalues[:NSPECIES]
+    B[10] = bcvalues[NSPECIES]
+    return B
+
+
+def ref_residuals(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel=0.0):
+    """utils::Residuals of the reference; returns F (11, N)."""
+    L = load_reference()
+    if L is None:
+        return None
+    N = nodes.shape[1]
+    d2, dc, d11 = reference_params_vectors(p)
+    U = _u11(c, phi, N)
+    B = _bc11(bctypes, bcvalues, N)
+    F = np.zeros((11, N))
+    L.ref_residuals(N, _dp(np.ascontiguousarray(nodes)), _lp(np.ascontiguousarray(ptr, dtype=np.int64)),
+                    _ip(np.ascontiguousarray(cols, dtype=np.int32)), _dp(U),
+                    _ip(np.ascontiguousarray(phase, dtype=np.int32)),
+                    _ip(np.ascontiguousarray(bctypes, dtype=np.int32)), _dp(B), voln1rel,
+                    _dp(d2), _dp(np.ascontiguousarray(dc)), _dp(d11), _dp(F))
+    return F
+
+
+def ref_k11(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel=0.0):
+    """K11 of utils::NewtonMatrices as COO (rows, cols, values)."""
+    L = load_reference()
+    if L is None:
+        return None
+    N = nodes.shape[1]
+    d2, dc, d11 = reference_params_vectors(p)
+    U = _u11(c, phi, N)
+    B = _bc11(bctypes, bcvalues, N)
+    args = [N, _dp(np.ascontiguousarray(nodes)), _lp(np.ascontiguousarray(ptr, dtype=np.int64)),
+            _ip(np.ascontiguousarray(cols, dtype=np.int32)), _dp(U),
+            _ip(np.ascontiguousarray(phase, dtype=np.int32)),
+            _ip(np.ascontiguousarray(bctypes, dtype=np.int32)), _dp(B), voln1rel, _dp(d2),
+            _dp(np.ascontiguousarray(dc)), _dp(d11)]
+    nnz = C.c_int64(0)
+    L.ref_newton_k11(*args, C.byref(nnz), None, None, None)
+    ri = np.empty(nnz.value, dtype=np.int32)
+    ci = np.empty(nnz.value, dtype=np.int32)
+    val = np.empty(nnz.value)
+    L.ref_newton_k11(*args, C.byref(nnz), _ip(ri), _ip(ci), _dp(val))
+    return ri, ci, val
