@@ -1,0 +1,359 @@
+"""Benchmark of the NNPP hot path on GB300.
+
+Workload (default): a jittered 80^3 lattice (512,000 nodes, dx = 1/80, delta = 3.015 dx)
+with a perturbed solid Mg sphere, four species and the potential; one "step" is one
+explicit time step (potential solve + bond sums + front update) of the whole lattice.
+Metric: node-steps/s of the mixed-precision path; the FP64 GPU path is timed on the same
+workload (ratio and relative L2 error reported), and the reference's CPU path (the FP64
+oracle restatement, all host threads) is timed on a bounded sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on stdout.  Data are synthetic (seeded); nothing is read from disk
+except MEASURED_PEAKS.json and profiles/traffic.json (ncu-measured DRAM bytes per launch).
+"""
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "nnpp-mg-implant-corrosion-3d_gb300")
+
+METRIC = "node-steps/s @512k nodes, mixed vs FP64 GPU at rel err<=1e-5; adjoint/fwd ratio"
+WORKLOAD = dict(kind=1, n_side=80, seed=1)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def load_package():
+    if "nnpp_gb300" in sys.modules:
+        return sys.modules["nnpp_gb300"]
+    spec = importlib.util.spec_from_file_location(
+        "nnpp_gb300", os.path.join(PKG_DIR, "__init__.py"), submodule_search_locations=[PKG_DIR])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["nnpp_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_table():
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(inp, max_seconds=25.0):
+    """FP64 oracle (the reference's algorithm restated, OpenMP, all host threads) on the same
+    512k workload; a bounded sample of whole steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cores = O.set_threads(os.cpu_count() or 1)
+    o = O.Oracle.from_synth(inp)
+    t0 = time.perf_counter()
+    o.build_neighbours()
+    t_build = time.perf_counter() - t0
+    o.set_solver(1e-10)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        o.forward(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or steps >= 50:
+            break
+    value = inp["N"] * steps / el
+    return {"value": value, "unit": "node-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d whole explicit steps of the 512k workload from t=0 (FP64 CG to 1e-10); "
+                      "neighbour build %.2f s" % (steps, t_build)}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    nn = load_package()
+    inp = nn.synth(WORKLOAD["kind"], WORKLOAD["n_side"], WORKLOAD["seed"])
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cores = O.set_threads(os.cpu_count() or 1)
+    o = O.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-10)
+    # bounded sample: one untimed step (the cold first solve), then whole steps until
+    # args.steps are done or about a minute has passed
+    o.forward(1)
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < args.steps:
+        o.forward(1)
+        steps += 1
+        if time.perf_counter() - t0 > 60.0:
+            break
+    el = time.perf_counter() - t0
+    args.steps = steps
+    value = inp["N"] * args.steps / el
+    line = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "jittered 80^3 lattice, perturbed sphere, 4 species + potential",
+                       "n_nodes": inp["N"], "precision": "fp64 (oracle restatement of the "
+                       "reference's explicit step, OpenMP)"},
+            "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d explicit steps of the 512k workload after 1 untimed step (bounded to ~60 s)" % steps},
+            "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run_ours(args):
+    rank, world, local = dist_info()
+    nn = load_package()
+    if nn.device_count() < 1:
+        raise SystemExit("no CUDA device")
+    nn.set_device(local % nn.device_count())
+    inp = nn.synth(WORKLOAD["kind"], WORKLOAD["n_side"], WORKLOAD["seed"] + rank)
+    N = inp["N"]
+    p = inp["params"]
+    sim = nn.Simulation.from_synth(inp)
+    t0 = time.perf_counter()
+    sim.build_neighbours()
+    t_build = time.perf_counter() - t0
+    ptr, _ = sim.neighbours_csr()
+    nnz = int(ptr[-1])
+    sim64 = nn.Simulation.from_synth(inp)
+    sim64.build_neighbours()
+    log("N=%d nnz=%d neighbour build %.3f s" % (N, nnz, t_build))
+
+    # warm-up (the first solve starts from phi = 0)
+    sim.forward(args.warmup, nn.MIXED)
+    sim64.forward(args.warmup, nn.FP64)
+    d0 = sim.diagnostics()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ms = sim.forward_timed(args.steps, nn.MIXED)
+    clk = clocks.stop()
+    d1 = sim.diagnostics()
+    ms64 = sim64.forward_timed(args.steps, nn.FP64)
+    d64 = sim64.diagnostics()
+
+    # max over ranks
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * args.steps * world / (ms / 1e3)
+    value64 = N * args.steps / (ms64 / 1e3)
+
+    # accuracy of the mixed path against the FP64 path after the same steps
+    c_m, phi_m, ph_m = sim.state()
+    c_d, phi_d, ph_d = sim64.state()
+    acc = {"rel_l2_c": rel_l2(c_m, c_d), "rel_l2_phi": rel_l2(phi_m, phi_d),
+           "mask_mismatch": int((ph_m != ph_d).sum()),
+           "front_dx": float(((3 * (ph_m.sum() - ph_d.sum()) * p.dx * p.dy * p.dz / (4 * np.pi))
+                              ** (1 / 3) if ph_m.sum() != ph_d.sum() else 0.0) / p.dx),
+           "mg_mass_lost_rel": abs(d1["mg_mass_lost"] - d64["mg_mass_lost"]) /
+                               max(abs(d64["mg_mass_lost"]), 1e-300)}
+
+    inner = d1["cg_iterations_total"] - d0["cg_iterations_total"]
+    outer = d1["outer_iterations_total"] - d0["outer_iterations_total"]
+    solves = d1["cg_solves"] - d0["cg_solves"]
+    launches = solves + 2 * outer + 2 * inner + args.steps
+
+    # kernel roofline: CG SpMV vs transport, CUDA-event timed on the library's stream
+    t_spmv = sim.time_kernel(1, nn.MIXED, reps=50)
+    t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
+    t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
+    spmv_per_step = inner / args.steps
+    ir_per_step = outer / args.steps
+    shares = {"cg_spmv": t_spmv * spmv_per_step, "transport": t_tr, "ir_residual": t_ir * ir_per_step}
+    ms_step = ms / args.steps
+    # algorithmic bytes per launch (FP32 values, 4-byte indices)
+    b = 4
+    bytes_spmv = 4 * nnz + 4 * (N + 1) + N * (b + b) + 3 * N * b
+    bytes_tr = 4 * nnz + 4 * (N + 1) + N * (4 * b + b + 1 + 3 * 8 + 4 * b)
+    bytes_ir = 4 * nnz + 4 * (N + 1) + N * (b + 8 + 8 + 8)
+    dom = max(shares, key=shares.get)
+    alg = {"cg_spmv": (bytes_spmv, t_spmv), "transport": (bytes_tr, t_tr), "ir_residual": (bytes_ir, t_ir)}
+    peak, peak_src = measured_peak()
+    tt = traffic_table()
+
+    def roof(name):
+        by, t = alg[name]
+        ach = by / (t / 1e3) / 1e9
+        tr = tt.get(name, {}).get("dram_bytes_per_launch")
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": tr, "kernel": name, "ms_per_launch": t, "algorithmic_bytes": by,
+                "peak_source": peak_src}
+
+    roofline = roof(dom)
+    roofline["others"] = {k: {kk: v for kk, v in roof(k).items() if kk in ("achieved", "frac", "ms_per_launch", "traffic")}
+                          for k in alg if k != dom}
+    roofline["share_of_step"] = {k: v / ms_step for k, v in shares.items()}
+
+    # end to end through the public API with host buffers (nnpp_step_host)
+    e2e = None
+    if rank == 0:
+        try:
+            import torch
+            cin = torch.empty((4, N), dtype=torch.float64, pin_memory=True).numpy()
+            phin = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+            cout = torch.empty((4, N), dtype=torch.float64, pin_memory=True).numpy()
+            phiout = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+            phout = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+            pinned = True
+        except Exception:
+            cin, phin = np.empty((4, N)), np.empty(N, dtype=np.int32)
+            cout, phiout, phout = np.empty((4, N)), np.empty(N), np.empty(N, dtype=np.int32)
+            pinned = False
+        c0, _, ph0 = sim.state()
+        cin[:] = c0
+        phin[:] = ph0
+        ke = max(3, min(args.steps, 10))
+        sim.step_host(cin, phin, nn.MIXED, out=(cout, phiout, phout))
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            sim.step_host(cin, phin, nn.MIXED, out=(cout, phiout, phout))
+            cin[:] = cout
+            phin[:] = phout
+        el = time.perf_counter() - t0
+        e2e = {"value": N * ke / el, "unit": "node-steps/s", "h2d_bytes_per_step": 4 * N * 8 + N * 4,
+               "d2h_bytes_per_step": 4 * N * 8 + N * 8 + N * 4, "steps": ke, "pinned": pinned,
+               "api": "nnpp_step_host"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(inp)
+
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "jittered 80^3 lattice (512,000 nodes), perturbed solid sphere r=0.3, "
+                                   "4 species + potential, delta=3.015dx, mixed precision",
+                       "n_nodes": N, "bonds": nnz, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "not flushed: per-bond arrays (%.2f GB) exceed the 129 MB L2" % ((4 + 4 + 8) * nnz / 1e9),
+                       "potential_tol": 1e-10},
+            "fp64_gpu": {"value": value64, "ms_per_step": ms64 / args.steps,
+                         "mixed_over_fp64": value / world / value64},
+            "accuracy_vs_fp64_gpu": acc,
+            "solver": {"inner_cg_per_step": inner / args.steps, "outer_per_step": outer / args.steps,
+                       "fp64_cg_per_step": (d64["cg_iterations_total"]) / (args.steps + args.warmup)},
+            "adjoint_over_forward": None,
+            "neighbour_build_s": t_build,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -113,6 +113,8 @@ const char* nnpp_last_error(void);
 int nnpp_abi_version(void);
 /* Number of CUDA devices visible (0 on a machine without a GPU); never fails. */
 int nnpp_device_count(void);
+/* Device on which the calling thread's next nnpp_create allocates (cudaSetDevice). */
+nnpp_status nnpp_set_device(int device);
 
 /* Fill nnpp_params from the reference's positional control vectors: data2 (51 values,
  * utils.h:2343-2395), datac1..datac4 (7 values each, utils.h:2397-2423) and datac11
@@ -200,6 +202,19 @@ nnpp_status nnpp_residuals(nnpp_handle* h, int precision, const double* c, const
 nnpp_status nnpp_solve_potential(nnpp_handle* h, int precision, const double* c,
                                  const int* phase, double* phi, int* iterations,
                                  double* rel_residual);
+
+/* ---- measurement (no counterpart in the reference) ------------------------------------ */
+
+/* nnpp_forward, timed with CUDA events recorded on the handle's stream around the graph
+ * launches (graphs are built before the first event). */
+nnpp_status nnpp_forward_timed(nnpp_handle* h, int n_steps, int precision, double* ms);
+
+/* Average duration of one launch of a single step kernel on the current state, CUDA-event
+ * timed on the handle's stream over `reps` launches after 3 warm-up launches; the state is
+ * restored afterwards.  kernel_id: 0 transport (bond sums), 1 CG matrix-vector product,
+ * 2 FP64 refinement residual. */
+nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int reps,
+                             double* ms_per_launch);
 
 /* ---- differentiation ------------------------------------------------------------------ */
 

@@ -75,6 +75,7 @@ _SIGS = {
     "nnpp_last_error": (C.c_char_p, []),
     "nnpp_abi_version": (C.c_int, []),
     "nnpp_device_count": (C.c_int, []),
+    "nnpp_set_device": (C.c_int, [C.c_int]),
     "nnpp_params_from_reference": (C.c_int, [_DP, _DP, _DP, _DP, _DP, _DP, C.c_double, C.c_double,
                                              C.POINTER(Params)]),
     "nnpp_build_clouds_hash": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -93,6 +94,8 @@ _SIGS = {
     "nnpp_step_host": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _DP, _IP]),
     "nnpp_residuals": (C.c_int, [_P, C.c_int, _DP, _DP, _IP, C.c_double, _DP]),
     "nnpp_solve_potential": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _IP, _DP]),
+    "nnpp_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    "nnpp_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -139,6 +142,10 @@ def _ip(a):
 
 def device_count():
     return lib().nnpp_device_count()
+
+
+def set_device(device):
+    _check(lib().nnpp_set_device(device))
 
 
 # ------------------------------------------------------------------ inputs -------------
@@ -265,6 +272,19 @@ class Simulation:
 
     def forward(self, n_steps, precision=MIXED):
         _check(lib().nnpp_forward(self._h, n_steps, precision))
+
+    def forward_timed(self, n_steps, precision=MIXED):
+        """forward() timed with CUDA events on the handle's stream; returns milliseconds."""
+        ms = C.c_double(0.0)
+        _check(lib().nnpp_forward_timed(self._h, n_steps, precision, C.byref(ms)))
+        return ms.value
+
+    def time_kernel(self, kernel_id, precision=MIXED, reps=20):
+        """Average milliseconds per launch of one step kernel (0 transport, 1 CG SpMV,
+        2 FP64 refinement residual)."""
+        ms = C.c_double(0.0)
+        _check(lib().nnpp_time_kernel(self._h, kernel_id, precision, reps, C.byref(ms)))
+        return ms.value
 
     def state(self):
         c = np.empty((NSPECIES, self.N), dtype=np.float64)

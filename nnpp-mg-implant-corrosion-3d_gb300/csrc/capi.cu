@@ -227,7 +227,8 @@ nnpp_status restore(Handle& h, StateBackup& b) {
 
 // Upload user-order c (S*N), phi (N, may be NULL), phase (N, may be NULL) into the current
 // buffers in precision prec.
-nnpp_status upload_state(Handle& h, const double* c, const double* phi, const int* phase, int prec) {
+nnpp_status upload_state(Handle& h, const double* c, const double* phi, const int* phase, int prec,
+                         bool dirichlet_phi = true) {
   const size_t N = h.N;
   NNPP_CUDA(cudaMemcpyAsync(h.user_stage.get(), c, sizeof(double) * S * N, cudaMemcpyHostToDevice, h.st));
   if (phi)
@@ -236,7 +237,7 @@ nnpp_status upload_state(Handle& h, const double* c, const double* phi, const in
     NNPP_CUDA(cudaMemcpyAsync(h.user_stage_i.get(), phase, sizeof(int) * N, cudaMemcpyHostToDevice, h.st));
   if (prec != h.state_prec && !phase) NNPP_TRY(convert_state(h, prec));
   return load_state(h, h.user_stage.get(), phi ? h.user_stage.get() + S * N : nullptr,
-                    phase ? h.user_stage_i.get() : nullptr, prec);
+                    phase ? h.user_stage_i.get() : nullptr, prec, dirichlet_phi);
 }
 
 }  // namespace
@@ -251,6 +252,13 @@ int nnpp_device_count(void) {
     return 0;
   }
   return n;
+}
+
+nnpp_status nnpp_set_device(int device) {
+  clear_error();
+  if (device < 0 || device >= nnpp_device_count()) return set_error(NNPP_ERR_INVALID, "no such device");
+  NNPP_CUDA(cudaSetDevice(device));
+  return NNPP_OK;
 }
 
 nnpp_status nnpp_params_from_reference(const double* data2, const double* datac1, const double* datac2,
@@ -555,7 +563,7 @@ nnpp_status nnpp_residuals(nnpp_handle* hp, int precision, const double* c, cons
   StateBackup b;
   NNPP_TRY(backup(h, b));
   h.cur ^= 1;
-  nnpp_status st = upload_state(h, c, phi, phase, precision);
+  nnpp_status st = upload_state(h, c, phi, phase, precision, false);
   DBuf<double> Fd;
   if (st == NNPP_OK && !Fd.alloc((S + 1) * (size_t)h.N)) st = set_error(NNPP_ERR_NOMEM, "residual output");
   if (st == NNPP_OK) {
@@ -606,6 +614,91 @@ nnpp_status nnpp_solve_potential(nnpp_handle* hp, int precision, const double* c
     if (st == NNPP_OK && h.strict && ds1.cg_nc > ds0.cg_nc)
       st = set_error(NNPP_ERR_CG_NO_CONVERGE, "potential solve hit its iteration cap");
   }
+  nnpp_status st2 = restore(h, b);
+  return st != NNPP_OK ? st : st2;
+}
+
+nnpp_status nnpp_forward_timed(nnpp_handle* hp, int n_steps, int precision, double* ms) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (n_steps < 0 || !ms) return set_error(NNPP_ERR_INVALID, "forward_timed: bad argument");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  Handle& h = hp->h;
+  DevState before;
+  NNPP_TRY(read_state(h, &before));
+  NNPP_TRY(convert_state(h, precision));
+  NNPP_TRY(push_settings(h));
+  // build the graphs first so that the timed region holds only graph launches
+  NNPP_TRY(build_graph(h, kGraphStep2, precision, h.cur));
+  NNPP_TRY(build_graph(h, kGraphStep1, precision, h.cur));
+  NNPP_TRY(build_graph(h, kGraphStep2, precision, h.cur ^ 1));
+  NNPP_TRY(build_graph(h, kGraphStep1, precision, h.cur ^ 1));
+  cudaEvent_t e0, e1;
+  NNPP_CUDA(cudaEventCreate(&e0));
+  NNPP_CUDA(cudaEventCreate(&e1));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  cudaEventRecord(e0, h.st);
+  nnpp_status st = run_steps(h, n_steps, precision);
+  cudaEventRecord(e1, h.st);
+  cudaEventSynchronize(e1);
+  float f = 0.0f;
+  cudaEventElapsedTime(&f, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = f;
+  NNPP_TRY(st);
+  return check_after(h, before.cg_nc);
+}
+
+// kernel_id: 0 transport (bond sums), 1 CG SpMV (FP32/FP64 matrix-vector product on the
+// liquid-liquid graph), 2 FP64 refinement residual.  The state is restored afterwards.
+nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int reps,
+                             double* ms_per_launch) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (reps < 1 || !ms_per_launch || kernel_id < 0 || kernel_id > 2)
+    return set_error(NNPP_ERR_INVALID, "time_kernel: bad argument");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  Handle& h = hp->h;
+  NNPP_TRY(convert_state(h, precision));
+  NNPP_TRY(push_settings(h));
+  const size_t N = h.N;
+  StateBackup b;
+  NNPP_TRY(backup(h, b));
+  DBuf<Rec32> rec32b;
+  DBuf<Rec64> rec64b;
+  DBuf<int> flipb;
+  if (!rec32b.alloc(N) || !rec64b.alloc(N) || !flipb.alloc(N)) return set_error(NNPP_ERR_NOMEM, "time_kernel backup");
+  NNPP_CUDA(cudaMemcpyAsync(rec32b.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(rec64b.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(flipb.get(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
+  KParams kp = make_kparams(h, h.cur);
+  kp.in_graph = 0;
+  nnpp_status st = launch_prep(h, kp, precision, h.st, 0, nullptr);
+  if (st == NNPP_OK) st = launch_cg_init(h, kp, precision, h.st, 0);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto one = [&]() -> nnpp_status {
+    if (kernel_id == 0) return launch_transport(h, kp, precision, h.st, nullptr);
+    if (kernel_id == 1) return launch_cg_spmv(h, kp, precision, h.st);
+    return launch_ir_update(h, kp, precision, h.st, 0);
+  };
+  for (int w = 0; w < 3 && st == NNPP_OK; ++w) st = one();  // warm-up
+  if (st == NNPP_OK) {
+    cudaEventRecord(e0, h.st);
+    for (int r = 0; r < reps && st == NNPP_OK; ++r) st = one();
+    cudaEventRecord(e1, h.st);
+    cudaEventSynchronize(e1);
+    float f = 0.0f;
+    cudaEventElapsedTime(&f, e0, e1);
+    *ms_per_launch = (double)f / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemcpyAsync(h.rec32[b.cur].get(), rec32b.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st);
+  cudaMemcpyAsync(h.rec64[b.cur].get(), rec64b.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st);
+  cudaMemcpyAsync(h.flip_step.get(), flipb.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st);
   nnpp_status st2 = restore(h, b);
   return st != NNPP_OK ? st : st2;
 }

@@ -46,6 +46,7 @@ struct KParams {
   double K1[S], K2zF[S], DL[S], DSo[S], z[S];
   int sub_step_no;
   int dissolve_count;           // 1: count the dissolution source into the diagnostics
+  int in_graph;                 // 1: kernels set the conditional handles of the graph
 };
 
 enum GraphKind { kGraphStep2 = 0, kGraphStep1 = 1, kGraphSolve = 2, kGraphKinds = 3 };
@@ -120,12 +121,15 @@ nnpp_status launch_cg_init(Handle& h, const KParams& kp, int prec, cudaStream_t 
                            cudaGraphConditionalHandle hc);
 nnpp_status launch_cg_iter(Handle& h, const KParams& kp, int prec, cudaStream_t st,
                            cudaGraphConditionalHandle hc);
+nnpp_status launch_cg_spmv(Handle& h, const KParams& kp, int prec, cudaStream_t st);
 nnpp_status launch_ir_update(Handle& h, const KParams& kp, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc);
 nnpp_status launch_transport(Handle& h, const KParams& kp, int prec, cudaStream_t st,
                              double* F_out);
+// dirichlet_phi: put the boundary values of the potential on its Dirichlet nodes (state
+// for stepping); false keeps the given values (inputs of the residual entry point).
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
-                       const int* d_phase_user, int prec);
+                       const int* d_phase_user, int prec, bool dirichlet_phi);
 nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_phase_user);
 nnpp_status convert_state(Handle& h, int to_prec);
 nnpp_status init_diag(Handle& h);

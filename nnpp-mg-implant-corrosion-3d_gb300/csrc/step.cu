@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(KParams k, cudaGraphConditional
       ds->cg_solves += 1;
       ds->last_relres = sqrt(tot[1] / bn);
     }
-    cudaGraphSetConditional(hc, go ? 1u : 0u);
+    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
   }
 }
 
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(KParams k, cudaGraphConditio
     const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
                                : ds->inner_rel * ds->inner_rel * tot[1];
     ds->inner_target = target;
-    cudaGraphSetConditional(hc, (tot[1] > target && ds->max_iter > 0) ? 1u : 0u);
+    if (k.in_graph) cudaGraphSetConditional(hc, (tot[1] > target && ds->max_iter > 0) ? 1u : 0u);
   }
 }
 
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(KParams k, cudaGraphCondit
     ds->cg_iters += 1;
     const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
                     ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
-    cudaGraphSetConditional(hc, go ? 1u : 0u);
+    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
   }
 }
 
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kBlock) k_ir_update(KParams k, cudaGraphCondit
       ds->last_relres = sqrt(tot[0] / ds->bnorm2);
       if (!conv) ds->cg_nc += 1;
     }
-    cudaGraphSetConditional(hc, go ? 1u : 0u);
+    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
   }
 }
 
@@ -636,14 +636,14 @@ __global__ void __launch_bounds__(kBlock) k_transport64(KParams k, double* F_out
 
 // ------------------------------------------------------------------- state transfer -----
 __global__ void k_load_state(KParams k, const int* perm, const double* c_user, const double* phi_user,
-                             const int* phase_user, int mixed) {
+                             const int* phase_user, int mixed, int dirichlet_phi) {
   const int N = k.N;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
     const int u = perm[a];
     double c[S];
     for (int s = 0; s < S; ++s) c[s] = c_user[(size_t)s * N + u];
     double phi = phi_user ? phi_user[u] : k.phi64[a];
-    if ((k.dirmask[a] >> S) & 1) phi = k.bcval[(size_t)S * N + a];
+    if (dirichlet_phi && ((k.dirmask[a] >> S) & 1)) phi = k.bcval[(size_t)S * N + a];
     float ph;
     if (phase_user)
       ph = phase_user[u] != 0 ? 1.0f : 0.0f;
@@ -865,6 +865,7 @@ KParams make_kparams(Handle& h, int cur) {
   }
   k.sub_step_no = p.sub_step_no;
   k.dissolve_count = 1;
+  k.in_graph = 1;
   return k;
 }
 
@@ -908,6 +909,18 @@ nnpp_status launch_cg_iter(Handle& h, const KParams& kp, int prec, cudaStream_t 
   });
 }
 
+nnpp_status launch_cg_spmv(Handle& h, const KParams& kp, int prec, cudaStream_t st) {
+  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    if (prec == NNPP_MIXED)
+      k_cg_spmv<float, W><<<kp.grid, kBlock, 0, st>>>(kp);
+    else
+      k_cg_spmv<double, W><<<kp.grid, kBlock, 0, st>>>(kp);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
+
 nnpp_status launch_ir_update(Handle& h, const KParams& kp, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc) {
   return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
@@ -942,10 +955,11 @@ nnpp_status launch_transport(Handle& h, const KParams& kp, int prec, cudaStream_
 }
 
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
-                       const int* d_phase_user, int prec) {
+                       const int* d_phase_user, int prec, bool dirichlet_phi) {
   KParams kp = make_kparams(h, h.cur);
   k_load_state<<<kp.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user,
-                                             d_phase_user, prec == NNPP_MIXED ? 1 : 0);
+                                             d_phase_user, prec == NNPP_MIXED ? 1 : 0,
+                                             dirichlet_phi ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = prec;
   return NNPP_OK;

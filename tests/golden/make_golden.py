@@ -1,0 +1,130 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own code.
+
+Runs the reference's build_clouds_hash (grid.h:43-204), utils::Residuals (utils.h:29-842)
+and utils::NewtonMatrices' K11 (utils.h:1794-1848), compiled from the reference's sources
+by oracle/build_oracle.py, on the synthetic workloads of nnpp_synth_fill, and stores:
+  clouds.json     SHA-256 of the reference's neighbour lists (lengths and padded rows) for
+                  small cases of every geometry kind and for the full 8k, 512k and 2M
+                  workloads, with the max cloud length and the bond count
+  residuals.npz   F1..F4, F11 of the reference for a seeded state on small cases
+  k11.json        SHA-256 and sums of the reference's K11 entries on a small case
+  synth.json      SHA-256 of the generated node coordinates (cross-platform determinism)
+  params.json     the reference's control vectors of data/NNPP.data2, .datac1-4, .datac11
+Needs the reference's sources (REFERENCE_ROOT); run:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+REFERENCE_ROOT = os.environ.get("NNPP_REFERENCE_ROOT", "/root/reference")
+
+SMALL = [(0, 20, 11), (1, 16, 11), (2, 14, 11), (3, 20, 11), (4, 15, 11)]
+FULL = [("lattice_block_20", 0, 20, 0), ("jittered_sphere_80", 1, 80, 1),
+        ("screw_permuted_126", 2, 126, 1)]
+RESID = [(0, 12, 3), (1, 12, 3), (2, 12, 3)]
+
+
+def clouds_digest(lengths, ptr, cols):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(lengths, dtype=np.int32).tobytes())
+    h.update(np.ascontiguousarray(cols, dtype=np.int32).tobytes())
+    return h.hexdigest()
+
+
+def nodes_digest(nodes):
+    return hashlib.sha256(np.ascontiguousarray(nodes, dtype=np.float64).tobytes()).hexdigest()
+
+
+def residual_state(N, seed):
+    rng = np.random.default_rng(seed)
+    c = 0.05 + rng.random((4, N))
+    phi = rng.standard_normal(N) * 0.3
+    return c, phi
+
+
+def main():
+    from conftest import load_package
+    import oracle as O
+    nn = load_package()
+    if O.load_reference() is None:
+        raise SystemExit("reference sources not found at %s" % REFERENCE_ROOT)
+    clouds = {}
+    synth = {}
+    for kind, n, seed in SMALL:
+        inp = nn.synth(kind, n, seed)
+        p = inp["params"]
+        lo, po, co, ml = O.ref_build_clouds_hash(1024, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10,
+                                                 p.dz * 10, inp["nodes"])
+        key = "kind%d_n%d_seed%d" % (kind, n, seed)
+        clouds[key] = {"sha256": clouds_digest(lo, po, co), "max_len": int(ml), "nnz": int(po[-1])}
+        synth[key] = nodes_digest(inp["nodes"])
+        print(key, clouds[key], flush=True)
+    for name, kind, n, seed in FULL:
+        inp = nn.synth(kind, n, seed)
+        p = inp["params"]
+        lo, po, co, ml = O.ref_build_clouds_hash(1024, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10,
+                                                 p.dz * 10, inp["nodes"])
+        clouds[name] = {"kind": kind, "n_side": n, "seed": seed, "sha256": clouds_digest(lo, po, co),
+                        "max_len": int(ml), "nnz": int(po[-1]), "N": int(inp["N"])}
+        synth[name] = nodes_digest(inp["nodes"])
+        print(name, clouds[name], flush=True)
+    with open(os.path.join(HERE, "clouds.json"), "w") as f:
+        json.dump(clouds, f, indent=1, sort_keys=True)
+    with open(os.path.join(HERE, "synth.json"), "w") as f:
+        json.dump(synth, f, indent=1, sort_keys=True)
+
+    arrays = {}
+    for kind, n, seed in RESID:
+        inp = nn.synth(kind, n, seed)
+        p = inp["params"].copy()
+        p.k_diss = 0.0
+        p.vol_red = 0.5
+        N = inp["N"]
+        lo, po, co, ml = O.ref_build_clouds_hash(1024, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10,
+                                                 p.dz * 10, inp["nodes"])
+        c, phi = residual_state(N, 100 + kind)
+        F = O.ref_residuals(p, inp["nodes"], po, co, c, phi, inp["phase0"], inp["bctypes"],
+                            inp["bcvalues"], voln1rel=0.25)
+        key = "kind%d_n%d_seed%d" % (kind, n, seed)
+        arrays[key + "_F"] = np.concatenate([F[:4], F[10:11]])
+    np.savez_compressed(os.path.join(HERE, "residuals.npz"), **arrays)
+
+    kind, n, seed = RESID[1]
+    inp = nn.synth(kind, n, seed)
+    p = inp["params"]
+    lo, po, co, ml = O.ref_build_clouds_hash(1024, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10,
+                                             p.dz * 10, inp["nodes"])
+    c, phi = residual_state(inp["N"], 100 + kind)
+    ri, ci, val = O.ref_k11(p, inp["nodes"], po, co, c, phi, inp["phase0"], inp["bctypes"],
+                            inp["bcvalues"])
+    order = np.lexsort((ci, ri))
+    h = hashlib.sha256()
+    h.update(ri[order].astype(np.int32).tobytes())
+    h.update(ci[order].astype(np.int32).tobytes())
+    h.update(val[order].astype(np.float64).tobytes())
+    k11 = {"case": "kind%d_n%d_seed%d" % (kind, n, seed), "nnz": int(len(val)),
+           "sha256": h.hexdigest(), "sum": float(val.sum()), "abs_sum": float(np.abs(val).sum())}
+    with open(os.path.join(HERE, "k11.json"), "w") as f:
+        json.dump(k11, f, indent=1)
+
+    data = os.path.join(REFERENCE_ROOT, "data")
+    params = {}
+    for name, size in [("NNPP.data2", 51), ("NNPP.datac1", 7), ("NNPP.datac2", 7),
+                       ("NNPP.datac3", 7), ("NNPP.datac4", 7), ("NNPP.datac11", 4)]:
+        with open(os.path.join(data, name)) as f:
+            vals = [float(t) for t in f.read().split()][:size]
+        params[name] = vals
+    with open(os.path.join(HERE, "params.json"), "w") as f:
+        json.dump(params, f, indent=1)
+    print("fixtures written", flush=True)
+
+
+if __name__ == "__main__":
+    main()

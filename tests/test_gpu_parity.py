@@ -1,0 +1,259 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle (which is
+itself pinned to the reference's grid.h/utils.h, see test_oracle_pin.py)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# geometry kinds of nnpp_synth_fill with small sides
+SMALL_CASES = [(0, 20), (1, 16), (2, 14), (3, 20), (4, 15)]
+
+
+def _ref_rows_without_self(po, co, N):
+    return [co[po[i] + 1:po[i + 1]] for i in range(N)]
+
+
+@pytest.fixture(scope="module")
+def gpu(nn):
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    return nn
+
+
+@pytest.mark.parametrize("kind,n", SMALL_CASES)
+def test_build_clouds_hash_reference_order_bit_exact(gpu, orc, kind, n):
+    nn = gpu
+    inp = nn.synth(kind, n, seed=11)
+    p = inp["params"]
+    r = p.delta * (1 + 1e-5)
+    clouds, lengths, ml = nn.build_clouds_hash(1024, r, p.dx * 10, p.dy * 10, p.dz * 10, inp["nodes"])
+    o = orc.Oracle.from_synth(inp)
+    ml_o = o.build_neighbours()
+    lo, po, co = o.clouds()
+    assert ml == ml_o
+    assert np.array_equal(lengths, lo)
+    # padded column-major matrix exactly as the reference's Eigen::MatrixXi
+    expect = -np.ones((inp["N"], 1024), dtype=np.int32)
+    for i in range(inp["N"]):
+        expect[i, :lo[i]] = co[po[i]:po[i + 1]]
+    assert np.array_equal(clouds, expect)
+
+
+@pytest.mark.parametrize("name", ["lattice_block_20", "jittered_sphere_80", "screw_permuted_126"])
+def test_full_size_clouds_bit_exact_vs_reference_digest(gpu, name):
+    """8k, 512k and 2M workloads (the last randomly permuted): the GPU lists, neighbour
+    order included, hash to the digest of the reference's own build_clouds_hash."""
+    import hashlib
+    import json
+    import os
+    from conftest import GOLDEN_DIR
+    nn = gpu
+    with open(os.path.join(GOLDEN_DIR, "clouds.json")) as f:
+        g = json.load(f)[name]
+    inp = nn.synth(g["kind"], g["n_side"], g["seed"])
+    sim = nn.Simulation.from_synth(inp)
+    _, lengths, ml = sim.build_neighbours()
+    ptr, cols = sim.neighbours_csr()
+    N = inp["N"]
+    full = np.empty(len(cols) + N, dtype=np.int32)
+    self_pos = ptr[:-1] + np.arange(N)
+    full[self_pos] = np.arange(N, dtype=np.int32)
+    mask = np.ones(len(full), dtype=bool)
+    mask[self_pos] = False
+    full[mask] = cols
+    h = hashlib.sha256()
+    h.update(lengths.astype(np.int32).tobytes())
+    h.update(full.tobytes())
+    assert ml == g["max_len"] and len(cols) + N == g["nnz"]
+    assert h.hexdigest() == g["sha256"]
+
+
+@pytest.mark.parametrize("cell_factor", [10.0, 1.0, 0.7])
+def test_build_other_cell_sizes(gpu, orc, cell_factor):
+    """Cells smaller than the horizon exercise the multi-cell scan (grid.h:157-167)."""
+    nn = gpu
+    inp = nn.synth(1, 14, seed=2)
+    p = inp["params"]
+    r = p.delta * (1 + 1e-5)
+    cell = p.dx * cell_factor
+    _, lengths, ml = nn.build_clouds_hash(1024, r, cell, cell, cell, inp["nodes"], want_clouds=False)
+    o = orc.Oracle.from_synth(inp)
+    ml_o = o.build_neighbours(1024, r, (cell, cell, cell))
+    lo, po, co = o.clouds()
+    assert ml == ml_o and np.array_equal(lengths, lo)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours(1024, r, (cell, cell, cell))
+    ptr, cols = sim.neighbours_csr()
+    rows = _ref_rows_without_self(po, co, inp["N"])
+    assert np.array_equal(cols, np.concatenate(rows))
+
+
+def test_canonical_order_same_sets(gpu, orc):
+    nn = gpu
+    inp = nn.synth(2, 14, seed=5)
+    sim_r = nn.Simulation.from_synth(inp)
+    sim_r.build_neighbours(order_mode=nn.ORDER_REFERENCE)
+    sim_c = nn.Simulation.from_synth(inp)
+    sim_c.build_neighbours(order_mode=nn.ORDER_CANONICAL)
+    pr, cr = sim_r.neighbours_csr()
+    pc, cc = sim_c.neighbours_csr()
+    assert np.array_equal(pr, pc)
+    for i in range(inp["N"]):
+        a, b = cr[pr[i]:pr[i + 1]], cc[pc[i]:pc[i + 1]]
+        assert np.array_equal(np.sort(a), np.sort(b))
+
+
+def test_capacity_error_matches_reference(gpu, orc):
+    """grid.h:187-189 throws when a list does not fit; the C ABI returns NNPP_ERR_CAPACITY."""
+    nn = gpu
+    inp = nn.synth(0, 12, seed=1)
+    p = inp["params"]
+    with pytest.raises(nn.NNPPError) as ei:
+        nn.build_clouds_hash(64, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10, p.dz * 10, inp["nodes"])
+    assert ei.value.status == 2
+    o = orc.Oracle.from_synth(inp)
+    with pytest.raises(RuntimeError):
+        o.build_neighbours(64)
+    # exactly enough room passes
+    _, lengths, ml = nn.build_clouds_hash(123, p.delta * (1 + 1e-5), p.dx * 10, p.dy * 10, p.dz * 10,
+                                          inp["nodes"], want_clouds=False)
+    assert ml == 123
+
+
+def _random_state(rng, inp, scale_phi=0.3):
+    N = inp["N"]
+    c = 0.05 + rng.random((4, N))
+    phi = rng.standard_normal(N) * scale_phi
+    ph = inp["phase0"].copy()
+    return c, phi, ph
+
+
+@pytest.mark.parametrize("kind,n", [(0, 16), (1, 16), (2, 14)])
+def test_residuals_fp64_and_mixed(gpu, orc, kind, n):
+    nn = gpu
+    rng = np.random.default_rng(kind)
+    inp = nn.synth(kind, n, seed=3)
+    p = inp["params"].copy()
+    p.vol_red = 0.5
+    sim = nn.Simulation(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    sim.build_neighbours()
+    o = orc.Oracle(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    o.build_neighbours()
+    c, phi, ph = _random_state(rng, inp)
+    Fo = o.residuals(c, phi, ph, voln1rel=0.25)
+    F64 = sim.residuals(c, phi, ph, voln1rel=0.25, precision=nn.FP64)
+    F32 = sim.residuals(c, phi, ph, voln1rel=0.25, precision=nn.MIXED)
+    for k in range(5):
+        scale = np.abs(Fo[k]).max()
+        assert np.abs(F64[k] - Fo[k]).max() <= 1e-12 * scale, k
+    # FP32 bond sums with compensated reduction: per-node error relative to the row scale
+    for k in range(4):
+        scale = np.abs(Fo[k]).max()
+        assert np.abs(F32[k] - Fo[k]).max() <= 2e-5 * scale, k
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_solve_potential(gpu, orc, prec):
+    nn = gpu
+    rng = np.random.default_rng(7)
+    inp = nn.synth(1, 18, seed=4)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    sim.set_solver(1e-10)
+    o = orc.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    c, _, ph = _random_state(rng, inp)
+    phi_o, it_o, rel_o = o.solve_potential(c, ph)
+    phi_g, it_g, rel_g = sim.solve_potential(c, ph, precision=prec)
+    assert rel_g <= 1e-10
+    err = np.linalg.norm(phi_g - phi_o) / np.linalg.norm(phi_o)
+    assert err < 1e-8, err
+    # the reference's F11 (utils.h:798-841), evaluated by the oracle at the GPU solution,
+    # vanishes on the unknowns (non-Dirichlet liquid rows) to the solve's tolerance
+    F = o.residuals(c, phi_g, ph)
+    rows = (inp["bctypes"] == 1) & (ph == 0)
+    lam = (1.0 / (inp["params"].K_phi * inp["params"].sigma)) * inp["params"].F * inp["params"].CSolid
+    b = lam * (np.array(list(inp["params"].z)) @ c)
+    assert np.linalg.norm(F[4][rows]) <= 2e-10 * np.linalg.norm(b[rows])
+
+
+def test_forward_fp64_lattice_block_masks_bit_exact(gpu, orc):
+    """Plain FP64 lattice workload, 1000 steps: final mask and every flip step identical to
+    the oracle; fields to rounding."""
+    nn = gpu
+    inp = nn.synth(0, 20, seed=0)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    sim.set_solver(1e-12)
+    o = orc.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    for _ in range(4):
+        sim.forward(250, nn.FP64)
+        o.forward(250)
+    c_g, phi_g, ph_g = sim.state()
+    c_o, phi_o, ph_o, fs_o = o.state()
+    assert np.array_equal(ph_g, ph_o)
+    assert np.array_equal(sim.flip_steps(), fs_o)
+    assert (fs_o > 0).sum() == 1000  # the block dissolves completely
+    assert np.linalg.norm(c_g - c_o) / np.linalg.norm(c_o) < 1e-10
+    assert np.linalg.norm(phi_g - phi_o) / np.linalg.norm(phi_o) < 1e-8
+    dg = sim.diagnostics()
+    do = o.diagnostics()
+    assert dg["solid_count"] == do["solid_count"] == 0
+    assert abs(dg["mg_mass_lost"] - do["mg_mass_lost"]) <= 1e-10 * abs(do["mg_mass_lost"])
+
+
+def test_forward_mixed_vs_oracle(gpu, orc):
+    nn = gpu
+    inp = nn.synth(1, 20, seed=9)
+    o = orc.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    sim.forward(200, nn.MIXED)
+    o.forward(200)
+    c_g, phi_g, ph_g = sim.state()
+    c_o, phi_o, ph_o, _ = o.state()
+    assert np.linalg.norm(c_g - c_o) / np.linalg.norm(c_o) <= 1e-5
+    assert np.linalg.norm(phi_g - phi_o) / np.linalg.norm(phi_o) <= 1e-5
+    assert np.array_equal(ph_g, ph_o)
+
+
+def test_step_host_matches_forward(gpu):
+    nn = gpu
+    inp = nn.synth(1, 14, seed=1)
+    a = nn.Simulation.from_synth(inp)
+    a.build_neighbours()
+    b = nn.Simulation.from_synth(inp)
+    b.build_neighbours()
+    c, phi, ph = b.state()
+    for _ in range(5):
+        c, phi, ph = b.step_host(c, ph, precision=nn.FP64)
+    a.forward(5, nn.FP64)
+    ca, phia, pha = a.state()
+    assert np.array_equal(ph, pha)
+    assert np.abs(c - ca).max() <= 1e-13 * np.abs(ca).max()
+    assert np.abs(phi - phia).max() <= 1e-10 * max(np.abs(phia).max(), 1e-300)
+
+
+def test_state_roundtrip_and_errors(gpu):
+    nn = gpu
+    inp = nn.synth(0, 10, seed=1)
+    sim = nn.Simulation.from_synth(inp)
+    with pytest.raises(nn.NNPPError) as ei:
+        sim.forward(1)
+    assert ei.value.status == 7  # steps before the neighbour build
+    sim.build_neighbours()
+    c, phi, ph = sim.state()
+    sim.set_state(c * 1.5, phi, ph)
+    c2, phi2, ph2 = sim.state()
+    assert np.array_equal(c2, c * 1.5) and np.array_equal(ph2, ph)
+    c3 = c.copy()
+    c3[0, int(np.argmax(inp["bctypes"] == 1))] = np.nan
+    sim.set_state(c3, phi, ph)
+    with pytest.raises(nn.NNPPError) as ei:
+        sim.forward(2, nn.FP64)
+    assert ei.value.status == 3
