@@ -137,6 +137,25 @@ nnpp_status nnpp_build_clouds_hash(int max_node_no, double r, double dx, double 
                                    int* clouds_colmajor, int* cloud_lengths,
                                    int* max_cloud_length);
 
+/* No counterpart in the reference.  For callers that cannot allocate device memory (a host
+ * framework that owns every device allocation, a real-time loop that must not touch the
+ * allocator, an application already at its memory cap): the canonical-order build
+ * (NNPP_ORDER_CANONICAL) into caller-owned DEVICE buffers -- d_nodes_colmajor (3*N
+ * doubles), d_clouds_colmajor (N*max_node_no ints, written -1 padded with self at column
+ * 0) and d_cloud_lengths (N ints) -- on `stream` (a cudaStream_t; NULL for the legacy
+ * default stream).  It calls no cudaMalloc/cudaFree: every temporary lives in one
+ * fixed-size device array (about 6.3 MB) that each GPU loading this library holds until
+ * the process exits.  N is limited to 262,144 nodes and the hash grid to 262,144 cells;
+ * larger inputs return NNPP_ERR_INVALID.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller.  The call synchronises `stream` three times
+ * to read the bounding box, the grid size and the capacity flag. */
+nnpp_status nnpp_build_clouds_hash_noalloc(int max_node_no, double r, double dx, double dy,
+                                           double dz, int n_nodes, const double* d_nodes_colmajor,
+                                           int* d_clouds_colmajor, int* d_cloud_lengths,
+                                           int* max_cloud_length, void* stream);
+
 /* ---- simulation handle ---------------------------------------------------------------- */
 
 /* Create a handle for N nodes.  bcvalues/icvalues hold (S+1)*N doubles in the reference's

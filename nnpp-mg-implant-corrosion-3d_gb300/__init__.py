@@ -80,6 +80,9 @@ _SIGS = {
                                              C.POINTER(Params)]),
     "nnpp_build_clouds_hash": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                          C.c_int, _DP, C.c_int, _IP, _IP, _IP]),
+    "nnpp_build_clouds_hash_noalloc": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double,
+                                                 C.c_double, C.c_int, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p, _IP, C.c_void_p]),
     "nnpp_create": (C.c_int, [C.POINTER(_P), C.POINTER(Params), C.c_int, _DP, _IP, _DP, _DP, _IP]),
     "nnpp_destroy": (C.c_int, [_P]),
     "nnpp_build_neighbours": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -194,6 +197,17 @@ def build_clouds_hash(max_node_no, r, dx, dy, dz, nodes, order_mode=ORDER_REFERE
     _check(lib().nnpp_build_clouds_hash(max_node_no, r, dx, dy, dz, N, _dp(xyz), order_mode,
                                         _ip(clouds), _ip(lengths), C.byref(ml)))
     return (clouds.T if want_clouds else None), lengths, ml.value
+
+
+def build_clouds_hash_noalloc(max_node_no, r, dx, dy, dz, n_nodes, d_nodes, d_clouds,
+                              d_lengths, stream=0):
+    """nnpp_build_clouds_hash_noalloc: canonical-order build between caller-owned DEVICE
+    buffers given as integer addresses (3*N doubles in, N*max_node_no and N ints out).
+    Allocates nothing; returns max_cloud_length."""
+    ml = C.c_int(0)
+    _check(lib().nnpp_build_clouds_hash_noalloc(max_node_no, r, dx, dy, dz, n_nodes, d_nodes,
+                                                d_clouds, d_lengths, C.byref(ml), stream))
+    return ml.value
 
 
 def _colmajor_nodes(nodes):

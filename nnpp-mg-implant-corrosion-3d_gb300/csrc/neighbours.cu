@@ -302,6 +302,74 @@ __global__ void k_cell_scan(int n, const double* __restrict__ x, const double* _
   }
 }
 
+// Variant of k_cell_scan for the allocation-free build: one pass that writes the padded
+// column-major output directly (self at column 0, grid.h:170-171), the lengths (self
+// included) and the running maximum length; raises the capacity flag where grid.h:187-189
+// throws.
+__global__ void k_cell_scan_padded(int n, const double* __restrict__ x, const double* __restrict__ y,
+                                   const double* __restrict__ z, double x0, double y0, double z0,
+                                   double cx, double cy, double cz, int mx, int my, int max_hash,
+                                   double r, const int* __restrict__ start,
+                                   const int* __restrict__ order, int max_node_no, int* clouds,
+                                   int* lengths, int* misc) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const double r2 = __dmul_rn(r, r);
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const double px = x[i], py = y[i], pz = z[i];
+    int lo[3], hi[3];
+    const double q[3] = {px, py, pz}, o[3] = {x0, y0, z0}, w[3] = {cx, cy, cz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = (int)floor((q[d] - r - o[d]) / w[d]) - 1;
+      hi[d] = (int)floor((q[d] + r - o[d]) / w[d]) + 1;
+      if (lo[d] < 0) lo[d] = 0;
+    }
+    if (hi[0] > mx - 1) hi[0] = mx - 1;
+    if (hi[1] > my - 1) hi[1] = my - 1;
+    int fill = 0;
+    const int cap = max_node_no - 1;
+    for (int kz = lo[2]; kz <= hi[2]; ++kz) {
+      const int mzo = mx * my * kz;
+      if (mzo >= max_hash) break;
+      for (int ky = lo[1]; ky <= hi[1]; ++ky)
+        for (int kx = lo[0]; kx <= hi[0]; ++kx) {
+          const int m = kx + mx * ky + mzo;
+          if (m >= max_hash) continue;
+          const double bx = __dadd_rn(x0, __dmul_rn((double)kx, cx));
+          const double by = __dadd_rn(y0, __dmul_rn((double)ky, cy));
+          const double bz = __dadd_rn(z0, __dmul_rn((double)kz, cz));
+          if (!sphere_cube_rn(px, py, pz, r2, bx, by, bz, cx, cy, cz)) continue;
+          const int s = start[m], e = start[m + 1];
+          for (int base = s; base < e; base += 32) {
+            const int k = base + lane;
+            bool pass = false;
+            int cand = -1;
+            if (k < e) {
+              cand = order[k];
+              const double d2 = __dadd_rn(__dadd_rn(sqr_rn(__dsub_rn(px, x[cand])),
+                                                    sqr_rn(__dsub_rn(py, y[cand]))),
+                                          sqr_rn(__dsub_rn(pz, z[cand])));
+              pass = (d2 <= r2) && (cand != i);
+            }
+            const unsigned int bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+              const int pos = fill + __popc(bal & ((1u << lane) - 1u));
+              if (pos < cap) clouds[(int64_t)(pos + 1) * n + i] = cand;
+            }
+            fill += __popc(bal);
+          }
+        }
+    }
+    if (lane == 0) {
+      clouds[i] = i;
+      lengths[i] = fill + 1 <= max_node_no ? fill + 1 : max_node_no;
+      if (fill + 1 > max_node_no) atomicExch(&misc[1], 1);
+      atomicMax(&misc[2], fill + 1);
+    }
+  }
+}
+
 __global__ void k_max_int(const int* v, int n, int* out) {
   int m = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -515,6 +583,73 @@ nnpp_status build_ref_lists(cudaStream_t st, int N, const double* x, const doubl
   NNPP_CUDA(cudaStreamSynchronize(st));
   out.nnz = nnz;
   out.max_len = ml + 1;  // self included, grid.h:198-203
+  return NNPP_OK;
+}
+
+// exclusive scan of n <= 1024*1024 ints with the block sums in `sums` (3072 ints)
+static nnpp_status scan_into(cudaStream_t st, const int* in, int* out, int n, int* sums) {
+  const int nb = (n + kScanBlock - 1) / kScanBlock;
+  if (nb > kScanBlock) return set_error(NNPP_ERR_UNSUPPORTED, "scan: too many elements");
+  k_scan_block<int><<<nb, kScanBlock, 0, st>>>(in, out, sums, n);
+  if (nb > 1) {
+    k_scan_block<int><<<1, kScanBlock, 0, st>>>(sums, sums + 1024, sums + 2048, nb);
+    k_scan_add<int><<<nb, kScanBlock, 0, st>>>(out, sums + 1024, n);
+  }
+  k_scan_tail<int><<<1, 1, 0, st>>>(in, out, n);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status build_canonical_into(cudaStream_t st, int N, const double* x, const double* y,
+                                 const double* z, int max_node_no, double r, double cx,
+                                 double cy, double cz, const BuildScratch& sc, int* clouds,
+                                 int* lengths, int* max_len) {
+  if (N <= 0 || N > sc.max_nodes)
+    return set_error(NNPP_ERR_INVALID, "allocation-free build: node count beyond the scratch maximum");
+  if (!(r > 0.0) || !(cx > 0.0) || !(cy > 0.0) || !(cz > 0.0) || max_node_no < 1)
+    return set_error(NNPP_ERR_INVALID, "build: r, cell sizes and max_node_no must be positive");
+  // bounding box (grid.h:49-71)
+  k_bbox_partial<<<kBboxBlocks, 256, 0, st>>>(x, y, z, N, sc.bbox_part);
+  k_bbox_final<<<1, 32, 0, st>>>(sc.bbox_part, kBboxBlocks, sc.bbox);
+  NNPP_CUDA(cudaGetLastError());
+  double bb[6];
+  NNPP_CUDA(cudaMemcpyAsync(bb, sc.bbox, sizeof(bb), cudaMemcpyDeviceToHost, st));
+  NNPP_CUDA(cudaStreamSynchronize(st));
+  const int mx = static_cast<int>((bb[1] - bb[0]) / cx) + 1;
+  const int my = static_cast<int>((bb[3] - bb[2]) / cy) + 1;
+  // hashes (grid.h:81-85)
+  NNPP_CUDA(cudaMemsetAsync(sc.misc, 0, 16 * sizeof(int), st));
+  NNPP_CUDA(cudaMemsetAsync(sc.misc, 0xff, sizeof(int), st));
+  k_hash<<<grid_for(N, 256), 256, 0, st>>>(x, y, z, N, bb[0], bb[2], bb[4], cx, cy, cz, mx, my,
+                                           sc.hash, sc.misc);
+  NNPP_CUDA(cudaGetLastError());
+  int hmax = -1;
+  NNPP_CUDA(cudaMemcpyAsync(&hmax, sc.misc, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NNPP_CUDA(cudaStreamSynchronize(st));
+  if (hmax < 0) return set_error(NNPP_ERR_INVALID, "build: negative hash (non-finite coordinates?)");
+  const int max_hash = hmax + 1;
+  if (max_hash > sc.max_cells)
+    return set_error(NNPP_ERR_INVALID, "allocation-free build: cell count beyond the scratch maximum");
+  // counting sort by cell, members by node index (the canonical order)
+  NNPP_CUDA(cudaMemsetAsync(sc.count, 0, sizeof(int) * max_hash, st));
+  k_count<<<grid_for(N, 256), 256, 0, st>>>(sc.hash, N, sc.count);
+  NNPP_TRY(scan_into(st, sc.count, sc.start, max_hash, sc.scan_sums));
+  NNPP_CUDA(cudaMemcpyAsync(sc.cursor, sc.start, sizeof(int) * (max_hash + 1), cudaMemcpyDeviceToDevice, st));
+  k_scatter<<<grid_for(N, 256), 256, 0, st>>>(sc.hash, N, sc.cursor, sc.order_tmp);
+  k_sort_segments<<<grid_for(max_hash, 1, 65535), 128, 0, st>>>(sc.start, max_hash, sc.order_tmp, sc.order);
+  NNPP_CUDA(cudaGetLastError());
+  // padded output: -1 everywhere, then self and neighbours (grid.h:145-196)
+  NNPP_CUDA(cudaMemsetAsync(clouds, 0xff, sizeof(int) * (size_t)N * (size_t)max_node_no, st));
+  k_cell_scan_padded<<<grid_for((long long)N * 32, 256, 152 * 64), 256, 0, st>>>(
+      N, x, y, z, bb[0], bb[2], bb[4], cx, cy, cz, mx, my, max_hash, r, sc.start, sc.order,
+      max_node_no, clouds, lengths, sc.misc);
+  NNPP_CUDA(cudaGetLastError());
+  int misc[3];
+  NNPP_CUDA(cudaMemcpyAsync(misc, sc.misc, sizeof(misc), cudaMemcpyDeviceToHost, st));
+  NNPP_CUDA(cudaStreamSynchronize(st));
+  if (misc[1])
+    return set_error(NNPP_ERR_CAPACITY, "Not enough room to store clouds. Increase max_node_no.");
+  if (max_len) *max_len = misc[2];
   return NNPP_OK;
 }
 

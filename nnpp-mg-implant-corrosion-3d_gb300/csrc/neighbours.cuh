@@ -48,6 +48,31 @@ nnpp_status build_ref_lists(cudaStream_t st, int N, const double* x, const doubl
 nnpp_status emit_padded(cudaStream_t st, const RefLists& L, int max_node_no, int* host_clouds,
                         int* host_lengths);
 
+// Device scratch for the allocation-free build (every pointer provided by the caller).
+struct BuildScratch {
+  double* bbox_part;   // 6 * kBboxBlocks
+  double* bbox;        // 6
+  int* hash;           // max_nodes
+  int* order_tmp;      // max_nodes
+  int* order;          // max_nodes
+  int* count;          // max_cells
+  int* start;          // max_cells + 1
+  int* cursor;         // max_cells + 1
+  int* scan_sums;      // 4096
+  int* misc;           // 16: [0] hash max, [1] capacity flag, [2] max length
+  int max_nodes;
+  int max_cells;
+};
+constexpr int kBboxBlocks = 128;
+
+// Canonical-order build into caller device buffers (padded column-major clouds, lengths)
+// without allocating: all temporaries live in `sc`.  Same kernels and decisions as the
+// allocating path with NNPP_ORDER_CANONICAL.
+nnpp_status build_canonical_into(cudaStream_t st, int N, const double* x, const double* y,
+                                 const double* z, int max_node_no, double r, double cx,
+                                 double cy, double cz, const BuildScratch& sc, int* clouds,
+                                 int* lengths, int* max_len);
+
 // Internal layout from the reference lists and user-order coordinates.
 nnpp_status build_layout(cudaStream_t st, const RefLists& L, const double* x, const double* y,
                          const double* z, double bin_side, double delta, double dx,
