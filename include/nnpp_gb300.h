@@ -256,12 +256,20 @@ nnpp_status nnpp_backward(nnpp_handle* h, const double* dL_dmass, double* grad_D
 
 typedef struct nnpp_ensemble nnpp_ensemble;
 
-/* Group handles (each already built) into one batched launch: every step of every member
- * runs inside one CUDA graph with work lists over all members' nodes.  Members must use
- * the same precision in nnpp_ensemble_forward.  tile and warps_per_node of 0 select the
- * autotuned configuration. */
+/* Group handles (each already built, on one device) into batched launches: each step of
+ * every member -- of any size, with its own parameters, time step and solver iteration
+ * count -- runs in one CUDA graph whose kernels walk work lists of tiles and node chunks
+ * over all members (persistent grids); a member whose potential solve has converged drops
+ * out of the loop while the others continue.  The bins per tile and lanes per node come
+ * from the library's autotuner on the first run.  The members keep their own state and
+ * can still be used alone; a handle may belong to one ensemble at a time. */
 nnpp_status nnpp_ensemble_create(nnpp_ensemble** out, nnpp_handle* const* members, int n);
 nnpp_status nnpp_ensemble_forward(nnpp_ensemble* e, int n_steps, int precision);
+/* nnpp_ensemble_forward timed with CUDA events on the ensemble's stream (milliseconds). */
+nnpp_status nnpp_ensemble_forward_timed(nnpp_ensemble* e, int n_steps, int precision,
+                                        double* ms);
+/* The autotuned configuration: bins per tile and lanes per node. */
+nnpp_status nnpp_ensemble_tuning(nnpp_ensemble* e, int* bins_per_tile, int* lanes_per_node);
 nnpp_status nnpp_ensemble_destroy(nnpp_ensemble* e);
 
 /* ---- synthetic inputs --------------------------------------------------------------------- */

@@ -103,6 +103,8 @@ _SIGS = {
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
     "nnpp_ensemble_forward": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nnpp_ensemble_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    "nnpp_ensemble_tuning": (C.c_int, [_P, _IP, _IP]),
     "nnpp_ensemble_destroy": (C.c_int, [_P]),
     "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
     "nnpp_synth_fill": (C.c_int, [C.c_int, C.c_int, C.c_uint64, _DP, _IP, _DP, _DP, _IP,
@@ -352,3 +354,38 @@ class Simulation:
         _check(lib().nnpp_solve_potential(self._h, precision, _dp(c), _ip(phase), _dp(phi),
                                           C.byref(it), C.byref(rel)))
         return phi, it.value, rel.value
+
+
+class Ensemble:
+    """Many Simulations stepped together in batched launches (nnpp_ensemble_*)."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s.handle for s in self.sims])
+        e = C.c_void_p()
+        _check(lib().nnpp_ensemble_create(C.byref(e), arr, len(self.sims)))
+        self._e = e
+
+    def forward(self, n_steps, precision=MIXED):
+        _check(lib().nnpp_ensemble_forward(self._e, n_steps, precision))
+
+    def forward_timed(self, n_steps, precision=MIXED):
+        ms = C.c_double(0.0)
+        _check(lib().nnpp_ensemble_forward_timed(self._e, n_steps, precision, C.byref(ms)))
+        return ms.value
+
+    def tuning(self):
+        t, w = C.c_int(0), C.c_int(0)
+        _check(lib().nnpp_ensemble_tuning(self._e, C.byref(t), C.byref(w)))
+        return t.value, w.value
+
+    def close(self):
+        if getattr(self, "_e", None):
+            lib().nnpp_ensemble_destroy(self._e)
+            self._e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,184 @@
+// adjoint.cu -- forward/backward pair of the explicit step (checkpointed adjoint).
+//
+// nnpp_forward_ckpt runs the forward with a full-state checkpoint every ck steps and samples
+// the cumulative Mg mass loss.  nnpp_backward walks the checkpoint segments from last to
+// first: it restores a checkpoint, recomputes the segment's steps (the step kernels are
+// deterministic, so the recomputed states are the forward's bit for bit) keeping an FP64
+// snapshot (c, phi, phase) per step, then runs the adjoint of each step backwards: the
+// transposed bond sums (k_adj_transport), the adjoint potential solve A psi = nu through the
+// same batched solver (right-hand side overridden) and the combination
+// lambda^n = mu + (1/(K sigma)) F CSolid z_k psi.  Memory: (ck + 1) snapshots of 64 bytes per
+// node plus one checkpoint per segment.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine.cuh"
+
+using namespace nnpp;
+
+struct nnpp_handle {
+  Handle h;
+};
+
+namespace {
+
+nnpp_status save_ckpt(Handle& h, Handle::Ckpt& c) {
+  const size_t N = h.N;
+  if (!c.rec32.alloc(N) || !c.clo.alloc(N) || !c.rec64.alloc(N) || !c.phi.alloc(N) ||
+      !c.phi_prev.alloc(N) || !c.flip.alloc(N))
+    return set_error(NNPP_ERR_NOMEM, "checkpoint");
+  c.cur = h.cur;
+  c.prec = h.state_prec;
+  NNPP_CUDA(cudaMemcpyAsync(c.rec32.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(c.clo.get(), h.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(c.rec64.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(c.phi.get(), h.phi64.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(c.phi_prev.get(), h.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(c.flip.get(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(&c.ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+nnpp_status load_ckpt(Handle& h, const Handle::Ckpt& c) {
+  const size_t N = h.N;
+  h.cur = c.cur;
+  h.state_prec = c.prec;
+  NNPP_CUDA(cudaMemcpyAsync(h.rec32[h.cur].get(), c.rec32.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.clo.get(), c.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.rec64[h.cur].get(), c.rec64.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.phi64.get(), c.phi.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.phi_prev.get(), c.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), c.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &c.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  if (h.engine) NNPP_TRY(engine_params(*h.engine));
+  return NNPP_OK;
+}
+
+nnpp_status read_ds(Handle& h, DevState* ds) {
+  NNPP_CUDA(cudaMemcpyAsync(ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int ckpt_every,
+                              int sample_every, double* mass_curve) {
+  clear_error();
+  if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
+  Handle& h = hp->h;
+  if (!h.built) return set_error(NNPP_ERR_STATE, "neighbour lists not built");
+  if (n_steps < 1 || ckpt_every < 1 || sample_every < 1 || !mass_curve)
+    return set_error(NNPP_ERR_INVALID, "forward_ckpt: bad argument");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  if (h.p.vol_red != 0.0)
+    return set_error(NNPP_ERR_UNSUPPORTED, "the adjoint needs vol_red = 0 (BV = 1 on mixed bonds)");
+  NNPP_CUDA(cudaSetDevice(h.device));
+  NNPP_TRY(engine_warm(*h.engine, precision));
+  h.fwd_steps = n_steps;
+  h.ck_every = ckpt_every;
+  h.sample_every = sample_every;
+  h.fwd_prec = precision;
+  h.ckpts.clear();
+  h.ckpts.resize((n_steps + ckpt_every - 1) / ckpt_every);
+  double m0 = 0.0;
+  NNPP_TRY(launch_sum_c0(h, h.scratch_d.get() + 8));
+  NNPP_CUDA(cudaMemcpyAsync(&m0, h.scratch_d.get() + 8, sizeof(double), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.curve.assign(n_steps / sample_every, 0.0);
+  const double dV = h.p.dx * h.p.dy * h.p.dz;
+  int s = 0;
+  while (s < n_steps) {
+    if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
+    int next = std::min(n_steps, (s / ckpt_every + 1) * ckpt_every);
+    next = std::min(next, (s / sample_every + 1) * sample_every);
+    NNPP_TRY(engine_run(*h.engine, next - s, precision));
+    s = next;
+    if (s % sample_every == 0) {
+      DevState ds;
+      NNPP_TRY(read_ds(h, &ds));
+      if (ds.nonfinite) return set_error(NNPP_ERR_NONFINITE, "non-finite concentration in the state");
+      h.curve[s / sample_every - 1] = dV * (m0 - ds.mg_mass_now);
+    }
+  }
+  NNPP_TRY(save_ckpt(h, h.fwd_end));
+  std::copy(h.curve.begin(), h.curve.end(), mass_curve);
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_D, double* grad_k) {
+  clear_error();
+  if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
+  Handle& h = hp->h;
+  if (h.fwd_steps < 1 || h.ckpts.empty()) return set_error(NNPP_ERR_STATE, "backward without forward_ckpt");
+  if (!dL_dmass || !grad_D || !grad_k) return set_error(NNPP_ERR_INVALID, "backward: NULL argument");
+  NNPP_CUDA(cudaSetDevice(h.device));
+  const int n_steps = h.fwd_steps, ck = h.ck_every, se = h.sample_every, prec = h.fwd_prec;
+  const size_t N = h.N;
+  const double dV = h.p.dx * h.p.dy * h.p.dz;
+  DBuf<Rec64> snap;
+  DBuf<double> lam, mu, nu, psi, acc;
+  if (!snap.alloc((size_t)(ck + 1) * N) || !lam.alloc(S * N) || !mu.alloc(S * N) || !nu.alloc(N) ||
+      !psi.alloc(N) || !acc.alloc(8))
+    return set_error(NNPP_ERR_NOMEM, "adjoint buffers");
+  NNPP_CUDA(cudaMemsetAsync(snap.get(), 0, sizeof(Rec64) * (size_t)(ck + 1) * N, h.st));
+  NNPP_CUDA(cudaMemsetAsync(lam.get(), 0, sizeof(double) * S * N, h.st));
+  NNPP_CUDA(cudaMemsetAsync(psi.get(), 0, sizeof(double) * N, h.st));
+  NNPP_CUDA(cudaMemsetAsync(acc.get(), 0, sizeof(double) * 8, h.st));
+  nnpp_status st = NNPP_OK;
+  // lambda^{n_steps}: the sample at the last step
+  if (n_steps % se == 0) {
+    NNPP_CUDA(cudaMemsetAsync(mu.get(), 0, sizeof(double) * S * N, h.st));
+    h.b_override = nullptr;
+    NNPP_TRY(engine_params(*h.engine));
+    // freem / phi64 are irrelevant here: mu = 0, and psi is masked by freem; zero phi64
+    NNPP_CUDA(cudaMemsetAsync(h.phi64.get(), 0, sizeof(double) * N, h.st));
+    NNPP_TRY(launch_adj_combine(h, mu.get(), lam.get(), -dV * dL_dmass[n_steps / se - 1]));
+  }
+  Engine& e = *h.engine;
+  const int nseg = (int)h.ckpts.size();
+  for (int g = nseg - 1; g >= 0 && st == NNPP_OK; --g) {
+    const int s0 = g * ck, s1 = std::min(n_steps, s0 + ck);
+    NNPP_TRY(load_ckpt(h, h.ckpts[g]));
+    NNPP_TRY(launch_snap_state(h, snap.get()));
+    for (int n = s0; n < s1; ++n) {
+      NNPP_TRY(engine_run(e, 1, prec));
+      NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
+      NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
+    }
+    for (int n = s1 - 1; n >= s0; --n) {
+      const Rec64* sn = snap.get() + (size_t)(n - s0) * N;
+      const Rec64* sn1 = snap.get() + (size_t)(n - s0 + 1) * N;
+      NNPP_TRY(engine_params(e));
+      EngineView v = make_view(e, 0, 0);
+      NNPP_TRY(launch_adj_transport(e, v, sn, sn1, lam.get(), mu.get(), nu.get(), acc.get(), h.st));
+      // adjoint potential solve on the unknowns of step n
+      NNPP_TRY(launch_adj_solve_setup(h, sn, psi.get()));
+      h.b_override = nu.get();
+      const int save_ex = h.extrapolate;
+      h.extrapolate = 0;
+      st = engine_solve(e, prec);
+      h.b_override = nullptr;
+      h.extrapolate = save_ex;
+      if (st != NNPP_OK) break;
+      NNPP_CUDA(cudaMemcpyAsync(psi.get(), h.phi64.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+      const double inject = (n > 0 && n % se == 0) ? -dV * dL_dmass[n / se - 1] : 0.0;
+      NNPP_TRY(launch_adj_combine(h, mu.get(), lam.get(), inject));
+    }
+  }
+  double g5[8];
+  NNPP_CUDA(cudaMemcpyAsync(g5, acc.get(), sizeof(double) * 8, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  nnpp_status st2 = load_ckpt(h, h.fwd_end);
+  if (st != NNPP_OK) return st;
+  for (int k = 0; k < S; ++k) grad_D[k] = g5[k];
+  *grad_k = g5[4];
+  return st2;
+}
+
+}  // extern "C"

@@ -1,17 +1,23 @@
-// capi.cu -- the C ABI (include/nnpp_gb300.h): handles, neighbour build, CUDA-graph step
-// loop, state transfer, drop-in residual/solve entry points.
+// capi.cu -- the C ABI (include/nnpp_gb300.h): handles, neighbour build, stepping through
+// the batched engine (one instance per handle, many per ensemble), state transfer, the
+// drop-in residual/solve entry points and measurement.
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
 #include <vector>
 
-#include "handle.cuh"
+#include "engine.cuh"
 
 using namespace nnpp;
 
 struct nnpp_handle {
   Handle h;
+};
+
+struct nnpp_ensemble {
+  Engine e;
+  std::vector<nnpp_handle*> members;
 };
 
 namespace {
@@ -39,128 +45,9 @@ nnpp_status check_params(const nnpp_params* p) {
   return NNPP_OK;
 }
 
-nnpp_status push_settings(Handle& h) {
-  DevState ds;
-  NNPP_CUDA(cudaMemcpyAsync(&ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
-  NNPP_CUDA(cudaStreamSynchronize(h.st));
-  ds.tol = h.tol;
-  ds.max_iter = h.max_iter;
-  ds.max_outer = h.max_outer;
-  ds.inner_rel = h.inner_rel;
-  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
-  return NNPP_OK;
-}
-
 nnpp_status read_state(Handle& h, DevState* ds) {
   NNPP_CUDA(cudaMemcpyAsync(ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
-  return NNPP_OK;
-}
-
-void destroy_graphs(Handle& h) {
-  for (int k = 0; k < kGraphKinds; ++k)
-    for (int p = 0; p < 2; ++p)
-      for (int c = 0; c < 2; ++c) {
-        if (h.gexec[k][p][c]) cudaGraphExecDestroy(h.gexec[k][p][c]);
-        if (h.graph[k][p][c]) cudaGraphDestroy(h.graph[k][p][c]);
-        h.gexec[k][p][c] = nullptr;
-        h.graph[k][p][c] = nullptr;
-      }
-}
-
-// Adds a while node after the current capture position of `st`; returns its body graph.
-nnpp_status add_while(cudaStream_t st, cudaGraphConditionalHandle hc, cudaGraph_t* body) {
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t g = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t nd = 0;
-  NNPP_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
-  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
-  np.conditional.handle = hc;
-  np.conditional.type = cudaGraphCondTypeWhile;
-  np.conditional.size = 1;
-  cudaGraphNode_t node;
-  NNPP_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
-  *body = np.conditional.phGraph_out[0];
-  NNPP_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
-                                                cudaStreamSetCaptureDependencies));
-  return NNPP_OK;
-}
-
-// prep; while(outer) { cg_init; while(inner) { spmv; update } ; ir_update }
-nnpp_status capture_solve(Handle& h, const KParams& kp, int prec) {
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t g = nullptr;
-  NNPP_CUDA(cudaStreamGetCaptureInfo(h.st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
-  cudaGraphConditionalHandle hout;
-  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 0, 0));
-  NNPP_TRY(launch_prep(h, kp, prec, h.st, hout, nullptr));
-  cudaGraph_t body_out;
-  NNPP_TRY(add_while(h.st, hout, &body_out));
-  NNPP_CUDA(cudaStreamBeginCaptureToGraph(h.st_b1, body_out, nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeRelaxed));
-  cudaGraphConditionalHandle hin;
-  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hin, body_out, 0, 0));
-  NNPP_TRY(launch_cg_init(h, kp, prec, h.st_b1, hin));
-  cudaGraph_t body_in;
-  NNPP_TRY(add_while(h.st_b1, hin, &body_in));
-  NNPP_CUDA(cudaStreamBeginCaptureToGraph(h.st_b2, body_in, nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeRelaxed));
-  NNPP_TRY(launch_cg_iter(h, kp, prec, h.st_b2, hin));
-  cudaGraph_t tmp;
-  NNPP_CUDA(cudaStreamEndCapture(h.st_b2, &tmp));
-  NNPP_TRY(launch_ir_update(h, kp, prec, h.st_b1, hout));
-  NNPP_CUDA(cudaStreamEndCapture(h.st_b1, &tmp));
-  return NNPP_OK;
-}
-
-nnpp_status build_graph(Handle& h, int kind, int prec, int cur) {
-  if (h.gexec[kind][prec][cur]) return NNPP_OK;
-  NNPP_CUDA(cudaStreamBeginCapture(h.st, cudaStreamCaptureModeThreadLocal));
-  nnpp_status st = NNPP_OK;
-  int c = cur;
-  const int nsteps = kind == kGraphStep2 ? 2 : 1;
-  for (int s = 0; s < nsteps && st == NNPP_OK; ++s) {
-    KParams kp = make_kparams(h, c);
-    st = capture_solve(h, kp, prec);
-    if (st == NNPP_OK && kind != kGraphSolve) {
-      st = launch_transport(h, kp, prec, h.st, nullptr);
-      c ^= 1;
-    }
-  }
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(h.st, &g);
-  if (st != NNPP_OK) {
-    if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    return st;
-  }
-  if (e != cudaSuccess) return set_error(NNPP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  cudaGraphExec_t ex = nullptr;
-  e = cudaGraphInstantiate(&ex, g, 0);
-  if (e != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return set_error(NNPP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  }
-  h.graph[kind][prec][cur] = g;
-  h.gexec[kind][prec][cur] = ex;
-  return NNPP_OK;
-}
-
-nnpp_status run_steps(Handle& h, int n_steps, int prec) {
-  NNPP_TRY(convert_state(h, prec));
-  NNPP_TRY(push_settings(h));
-  int done = 0;
-  while (n_steps - done >= 2) {
-    NNPP_TRY(build_graph(h, kGraphStep2, prec, h.cur));
-    NNPP_CUDA(cudaGraphLaunch(h.gexec[kGraphStep2][prec][h.cur], h.st));
-    done += 2;
-  }
-  if (n_steps - done == 1) {
-    NNPP_TRY(build_graph(h, kGraphStep1, prec, h.cur));
-    NNPP_CUDA(cudaGraphLaunch(h.gexec[kGraphStep1][prec][h.cur], h.st));
-    h.cur ^= 1;
-  }
   return NNPP_OK;
 }
 
@@ -198,30 +85,47 @@ bool have_gpu() {
       return set_error(NNPP_ERR_STATE, "neighbour lists not built (call nnpp_build_neighbours)"); \
   } while (0)
 
+// Everything a one-off evaluation on scratch inputs changes, so that it can be undone.
 struct StateBackup {
   int cur, prec;
-  DBuf<double> phi;
+  DBuf<double> phi, phi_prev;
   DBuf<float4> clo;
+  DBuf<Rec32> rec32;
+  DBuf<Rec64> rec64;
+  DBuf<int> flip;
   DevState ds;
 };
 
 nnpp_status backup(Handle& h, StateBackup& b) {
+  const size_t N = h.N;
   b.cur = h.cur;
   b.prec = h.state_prec;
-  if (!b.phi.alloc(h.N) || !b.clo.alloc(h.N)) return set_error(NNPP_ERR_NOMEM, "backup");
-  NNPP_CUDA(cudaMemcpyAsync(b.phi.get(), h.phi64.get(), sizeof(double) * h.N, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(b.clo.get(), h.clo.get(), sizeof(float4) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  if (!b.phi.alloc(N) || !b.phi_prev.alloc(N) || !b.clo.alloc(N) || !b.rec32.alloc(N) ||
+      !b.rec64.alloc(N) || !b.flip.alloc(N))
+    return set_error(NNPP_ERR_NOMEM, "backup");
+  NNPP_CUDA(cudaMemcpyAsync(b.phi.get(), h.phi64.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.phi_prev.get(), h.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.clo.get(), h.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.rec32.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.rec64.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(b.flip.get(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_TRY(read_state(h, &b.ds));
   return NNPP_OK;
 }
 
 nnpp_status restore(Handle& h, StateBackup& b) {
+  const size_t N = h.N;
   h.cur = b.cur;
   h.state_prec = b.prec;
-  NNPP_CUDA(cudaMemcpyAsync(h.phi64.get(), b.phi.get(), sizeof(double) * h.N, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(h.clo.get(), b.clo.get(), sizeof(float4) * h.N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.phi64.get(), b.phi.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.phi_prev.get(), b.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.clo.get(), b.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.rec32[h.cur].get(), b.rec32.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.rec64[h.cur].get(), b.rec64.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), b.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &b.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
+  if (h.engine) NNPP_TRY(engine_params(*h.engine));
   return NNPP_OK;
 }
 
@@ -238,6 +142,20 @@ nnpp_status upload_state(Handle& h, const double* c, const double* phi, const in
   if (prec != h.state_prec && !phase) NNPP_TRY(convert_state(h, prec));
   return load_state(h, h.user_stage.get(), phi ? h.user_stage.get() + S * N : nullptr,
                     phase ? h.user_stage_i.get() : nullptr, prec, dirichlet_phi);
+}
+
+// single-instance view of h's engine with a private KParams block (in_graph = 0)
+struct OneView {
+  DBuf<KParams> kp;
+  EngineView v;
+};
+
+nnpp_status one_view(Handle& h, const KParams& k, OneView& ov) {
+  if (!ov.kp.alloc(1)) return set_error(NNPP_ERR_NOMEM, "view");
+  NNPP_CUDA(cudaMemcpyAsync(ov.kp.get(), &k, sizeof(KParams), cudaMemcpyHostToDevice, h.st));
+  ov.v = make_view(*h.engine, 0, 0);
+  ov.v.inst = ov.kp.get();
+  return NNPP_OK;
 }
 
 }  // namespace
@@ -339,6 +257,8 @@ nnpp_status nnpp_create(nnpp_handle** out, const nnpp_params* p, int n_nodes,
   if (n_nodes <= 0 || !nodes_colmajor || !bctypes || !bcvalues || !icvalues)
     return set_error(NNPP_ERR_INVALID, "create: missing inputs");
   if (!have_gpu()) return set_error(NNPP_ERR_CUDA, "no CUDA device");
+  for (size_t i = 0; i < 3 * (size_t)n_nodes; ++i)
+    if (!std::isfinite(nodes_colmajor[i])) return set_error(NNPP_ERR_INVALID, "non-finite node coordinate");
   nnpp_handle* hp = new nnpp_handle();
   Handle& h = hp->h;
   h.p = *p;
@@ -348,9 +268,7 @@ nnpp_status nnpp_create(nnpp_handle** out, const nnpp_params* p, int n_nodes,
     nnpp_destroy(hp);
     return st;
   };
-  if (cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h.st_b1, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h.st_b2, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_error(NNPP_ERR_CUDA, "stream creation"));
   const size_t N = n_nodes;
   if (!h.ux.alloc(N) || !h.uy.alloc(N) || !h.uz.alloc(N)) return fail(set_error(NNPP_ERR_NOMEM, "nodes"));
@@ -359,8 +277,6 @@ nnpp_status nnpp_create(nnpp_handle** out, const nnpp_params* p, int n_nodes,
       cudaMemcpyAsync(h.uz.get(), nodes_colmajor + 2 * N, sizeof(double) * N, cudaMemcpyHostToDevice, h.st) ||
       cudaStreamSynchronize(h.st))
     return fail(set_error(NNPP_ERR_CUDA, "node upload"));
-  for (size_t i = 0; i < 3 * N; ++i)
-    if (!std::isfinite(nodes_colmajor[i])) return fail(set_error(NNPP_ERR_INVALID, "non-finite node coordinate"));
   h.h_bctypes.assign(bctypes, bctypes + N);
   h.h_bcv.assign(bcvalues, bcvalues + (S + 1) * N);
   h.h_ic.assign(icvalues, icvalues + (S + 1) * N);
@@ -376,11 +292,13 @@ nnpp_status nnpp_destroy(nnpp_handle* hp) {
   Handle& h = hp->h;
   cudaSetDevice(h.device);
   if (h.st) cudaStreamSynchronize(h.st);
-  destroy_graphs(h);
-  if (h.st) cudaStreamDestroy(h.st);
-  if (h.st_b1) cudaStreamDestroy(h.st_b1);
-  if (h.st_b2) cudaStreamDestroy(h.st_b2);
+  if (h.engine) {
+    delete h.engine;
+    h.engine = nullptr;
+  }
+  cudaStream_t st = h.st;
   delete hp;
+  if (st) cudaStreamDestroy(st);
   return NNPP_OK;
 }
 
@@ -389,7 +307,10 @@ nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, do
                                   int* max_cloud_length) {
   NNPP_GUARD(hp);
   Handle& h = hp->h;
-  destroy_graphs(h);
+  if (h.engine) {
+    delete h.engine;
+    h.engine = nullptr;
+  }
   h.built = false;
   NNPP_TRY(build_ref_lists(h.st, h.N, h.ux.get(), h.uy.get(), h.uz.get(), max_node_no, r, cx, cy, cz,
                            order_mode, h.ref));
@@ -397,7 +318,13 @@ nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, do
   NNPP_TRY(emit_padded(h.st, h.ref, max_node_no, clouds_colmajor, cloud_lengths));
   if (max_cloud_length) *max_cloud_length = h.ref.max_len;
   const nnpp_params& p = h.p;
-  NNPP_TRY(build_layout(h.st, h.ref, h.ux.get(), h.uy.get(), h.uz.get(), r, p.delta, p.dx,
+  // bins of side h32 >= r (an FP32 value, so that tile-relative FP32 coordinates are exact
+  // multiples of it): every neighbour lies in an adjacent bin
+  const double want = r * (1.0 + 1e-7);
+  float h32 = (float)want;
+  while ((double)h32 < want) h32 = nextafterf(h32, INFINITY);
+  h.h32 = h32;
+  NNPP_TRY(build_layout(h.st, h.ref, h.ux.get(), h.uy.get(), h.uz.get(), (double)h32, p.delta, p.dx,
                         p.dx * p.dy * p.dz, p.s_phi, h.lay));
   NNPP_TRY(step_alloc(h));
   // per-node constants in internal order (main.cpp:676-712: Dirichlet where bctypes == 0
@@ -423,14 +350,25 @@ nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, do
   // initial state (main.cpp:398-420 with the given phase)
   DevState ds;
   std::memset(&ds, 0, sizeof(ds));
+  ds.tol = h.tol;
+  ds.max_iter = h.max_iter;
+  ds.max_outer = h.max_outer;
+  ds.inner_rel = h.inner_rel;
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
   h.cur = 0;
   NNPP_TRY(upload_state(h, h.h_ic.data(), h.h_ic.data() + S * N, h.h_phase0.data(), NNPP_FP64));
   NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, sizeof(int) * N, h.st));
   NNPP_TRY(init_diag(h));
-  NNPP_TRY(push_settings(h));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   h.built = true;
+  h.engine = new Engine();
+  h.engine->members.push_back(&h);
+  h.engine->st = h.st;
+  nnpp_status st = engine_build(*h.engine);
+  if (st != NNPP_OK) {
+    h.built = false;
+    return st;
+  }
   return NNPP_OK;
 }
 
@@ -454,7 +392,6 @@ nnpp_status nnpp_set_solver(nnpp_handle* hp, double tol, int max_iter, int stric
   h.tol = tol;
   h.max_iter = max_iter;
   h.strict = strict;
-  if (h.built) NNPP_TRY(push_settings(h));
   return NNPP_OK;
 }
 
@@ -466,7 +403,7 @@ nnpp_status nnpp_forward(nnpp_handle* hp, int n_steps, int precision) {
   Handle& h = hp->h;
   DevState before;
   NNPP_TRY(read_state(h, &before));
-  NNPP_TRY(run_steps(h, n_steps, precision));
+  NNPP_TRY(engine_run(*h.engine, n_steps, precision));
   return check_after(h, before.cg_nc);
 }
 
@@ -542,7 +479,7 @@ nnpp_status nnpp_step_host(nnpp_handle* hp, int precision, const double* c_in, c
   DevState before;
   NNPP_TRY(read_state(h, &before));
   NNPP_TRY(upload_state(h, c_in, nullptr, phase_in, precision));
-  NNPP_TRY(run_steps(h, 1, precision));
+  NNPP_TRY(engine_run(*h.engine, 1, precision));
   const size_t N = h.N;
   NNPP_TRY(store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get()));
   if (c_out) NNPP_CUDA(cudaMemcpyAsync(c_out, h.user_stage.get(), sizeof(double) * S * N, cudaMemcpyDeviceToHost, h.st));
@@ -560,18 +497,20 @@ nnpp_status nnpp_residuals(nnpp_handle* hp, int precision, const double* c, cons
   if (!c || !phi || !phase || !F) return set_error(NNPP_ERR_INVALID, "residuals: NULL argument");
   if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
   Handle& h = hp->h;
+  NNPP_TRY(engine_warm(*h.engine, precision));
   StateBackup b;
   NNPP_TRY(backup(h, b));
-  h.cur ^= 1;
   nnpp_status st = upload_state(h, c, phi, phase, precision, false);
   DBuf<double> Fd;
+  OneView ov;
   if (st == NNPP_OK && !Fd.alloc((S + 1) * (size_t)h.N)) st = set_error(NNPP_ERR_NOMEM, "residual output");
   if (st == NNPP_OK) {
     NNPP_CUDA(cudaMemcpyAsync(h.scratch_d.get(), &voln1rel, sizeof(double), cudaMemcpyHostToDevice, h.st));
     KParams kp = make_kparams(h, h.cur);
     kp.voln1rel_ptr = h.scratch_d.get();
-    st = launch_transport(h, kp, precision, h.st, Fd.get());
-    if (st == NNPP_OK) st = launch_prep(h, kp, precision, h.st, 0, Fd.get() + (size_t)S * h.N);
+    st = one_view(h, kp, ov);
+    if (st == NNPP_OK) st = launch_transport_b(*h.engine, ov.v, precision, h.st, Fd.get());
+    if (st == NNPP_OK) st = launch_prep_b(*h.engine, ov.v, precision, h.st, 0, Fd.get() + (size_t)S * h.N);
     if (st == NNPP_OK) {
       k_unpermute<<<h.grid, kBlockHost, 0, h.st>>>(h.lay.perm.get(), h.N, S + 1, Fd.get(), h.user_stage.get());
       if (cudaGetLastError() != cudaSuccess) st = set_error(NNPP_ERR_CUDA, "unpermute");
@@ -593,20 +532,16 @@ nnpp_status nnpp_solve_potential(nnpp_handle* hp, int precision, const double* c
   Handle& h = hp->h;
   StateBackup b;
   NNPP_TRY(backup(h, b));
-  h.cur ^= 1;
   nnpp_status st = upload_state(h, c, phi, phase, precision);
-  if (st == NNPP_OK) st = push_settings(h);
-  if (st == NNPP_OK) st = build_graph(h, kGraphSolve, precision, h.cur);
   DevState ds0, ds1;
   if (st == NNPP_OK) st = read_state(h, &ds0);
-  if (st == NNPP_OK && cudaGraphLaunch(h.gexec[kGraphSolve][precision][h.cur], h.st) != cudaSuccess)
-    st = set_error(NNPP_ERR_CUDA, "graph launch");
+  if (st == NNPP_OK) st = engine_solve(*h.engine, precision);
   if (st == NNPP_OK) st = read_state(h, &ds1);
   if (st == NNPP_OK) {
-    const size_t N = h.N;
-    st = store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get());
+    k_unpermute<<<h.grid, kBlockHost, 0, h.st>>>(h.lay.perm.get(), h.N, 1, h.phi64.get(), h.user_stage.get());
+    if (cudaGetLastError() != cudaSuccess) st = set_error(NNPP_ERR_CUDA, "unpermute");
     if (st == NNPP_OK) {
-      NNPP_CUDA(cudaMemcpyAsync(phi, h.user_stage.get() + S * N, sizeof(double) * N, cudaMemcpyDeviceToHost, h.st));
+      NNPP_CUDA(cudaMemcpyAsync(phi, h.user_stage.get(), sizeof(double) * h.N, cudaMemcpyDeviceToHost, h.st));
       NNPP_CUDA(cudaStreamSynchronize(h.st));
     }
     if (iterations) *iterations = (int)(ds1.cg_iters - ds0.cg_iters);
@@ -626,19 +561,13 @@ nnpp_status nnpp_forward_timed(nnpp_handle* hp, int n_steps, int precision, doub
   Handle& h = hp->h;
   DevState before;
   NNPP_TRY(read_state(h, &before));
-  NNPP_TRY(convert_state(h, precision));
-  NNPP_TRY(push_settings(h));
-  // build the graphs first so that the timed region holds only graph launches
-  NNPP_TRY(build_graph(h, kGraphStep2, precision, h.cur));
-  NNPP_TRY(build_graph(h, kGraphStep1, precision, h.cur));
-  NNPP_TRY(build_graph(h, kGraphStep2, precision, h.cur ^ 1));
-  NNPP_TRY(build_graph(h, kGraphStep1, precision, h.cur ^ 1));
+  NNPP_TRY(engine_warm(*h.engine, precision));
   cudaEvent_t e0, e1;
   NNPP_CUDA(cudaEventCreate(&e0));
   NNPP_CUDA(cudaEventCreate(&e1));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   cudaEventRecord(e0, h.st);
-  nnpp_status st = run_steps(h, n_steps, precision);
+  nnpp_status st = engine_run(*h.engine, n_steps, precision, true);
   cudaEventRecord(e1, h.st);
   cudaEventSynchronize(e1);
   float f = 0.0f;
@@ -650,7 +579,7 @@ nnpp_status nnpp_forward_timed(nnpp_handle* hp, int n_steps, int precision, doub
   return check_after(h, before.cg_nc);
 }
 
-// kernel_id: 0 transport (bond sums), 1 CG SpMV (FP32/FP64 matrix-vector product on the
+// kernel_id: 0 transport (bond sums), 1 CG SpMV (matrix-vector product on the
 // liquid-liquid graph), 2 FP64 refinement residual.  The state is restored afterwards.
 nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int reps,
                              double* ms_per_launch) {
@@ -660,32 +589,39 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
     return set_error(NNPP_ERR_INVALID, "time_kernel: bad argument");
   if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
   Handle& h = hp->h;
-  NNPP_TRY(convert_state(h, precision));
-  NNPP_TRY(push_settings(h));
-  const size_t N = h.N;
+  NNPP_TRY(engine_warm(*h.engine, precision));
   StateBackup b;
   NNPP_TRY(backup(h, b));
-  DBuf<Rec32> rec32b;
-  DBuf<Rec64> rec64b;
-  DBuf<int> flipb;
-  if (!rec32b.alloc(N) || !rec64b.alloc(N) || !flipb.alloc(N)) return set_error(NNPP_ERR_NOMEM, "time_kernel backup");
-  NNPP_CUDA(cudaMemcpyAsync(rec32b.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(rec64b.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(flipb.get(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
-  KParams kp = make_kparams(h, h.cur);
-  kp.in_graph = 0;
-  nnpp_status st = launch_prep(h, kp, precision, h.st, 0, nullptr);
-  if (st == NNPP_OK) st = launch_cg_init(h, kp, precision, h.st, 0);
+  Engine& e = *h.engine;
+  EngineView v = make_view(e, 0, 0);
+  nnpp_status st = launch_prep_b(e, v, precision, h.st, 0, nullptr);
+  // every instance active so that the timed kernels do their full work
+  DevState ds;
+  if (st == NNPP_OK) st = read_state(h, &ds);
+  ds.outer_active = 1;
+  ds.inner_active = 1;
+  ds.tol = 0.0;            // keep the refinement kernel's instance active across repetitions
+  ds.max_outer = 1 << 30;
+  if (st == NNPP_OK) {
+    cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st);
+    st = launch_cg_init_b(e, v, precision, h.st, 0);
+  }
+  if (st == NNPP_OK) {
+    ds.outer_active = 1;
+    ds.inner_active = 1;
+    cudaMemcpyAsync(&h.dstate.get()->outer_active, &ds.outer_active, 2 * sizeof(int), cudaMemcpyHostToDevice, h.st);
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   auto one = [&]() -> nnpp_status {
-    if (kernel_id == 0) return launch_transport(h, kp, precision, h.st, nullptr);
-    if (kernel_id == 1) return launch_cg_spmv(h, kp, precision, h.st);
-    return launch_ir_update(h, kp, precision, h.st, 0);
+    if (kernel_id == 0) return launch_transport_b(e, v, precision, h.st, nullptr);
+    if (kernel_id == 1) return launch_cg_spmv_b(e, v, precision, h.st);
+    return launch_ir_update_b(e, v, precision, h.st, 0);
   };
-  for (int w = 0; w < 3 && st == NNPP_OK; ++w) st = one();  // warm-up
+  for (int w = 0; w < 3 && st == NNPP_OK; ++w) st = one();
   if (st == NNPP_OK) {
+    cudaMemcpyAsync(&h.dstate.get()->outer_active, &ds.outer_active, 2 * sizeof(int), cudaMemcpyHostToDevice, h.st);
     cudaEventRecord(e0, h.st);
     for (int r = 0; r < reps && st == NNPP_OK; ++r) st = one();
     cudaEventRecord(e1, h.st);
@@ -696,11 +632,104 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaMemcpyAsync(h.rec32[b.cur].get(), rec32b.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st);
-  cudaMemcpyAsync(h.rec64[b.cur].get(), rec64b.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st);
-  cudaMemcpyAsync(h.flip_step.get(), flipb.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st);
   nnpp_status st2 = restore(h, b);
   return st != NNPP_OK ? st : st2;
+}
+
+// ---- ensembles ------------------------------------------------------------------------------
+nnpp_status nnpp_ensemble_create(nnpp_ensemble** out, nnpp_handle* const* members, int n) {
+  clear_error();
+  if (!out || !members || n < 1) return set_error(NNPP_ERR_INVALID, "ensemble: no members");
+  *out = nullptr;
+  nnpp_ensemble* es = new nnpp_ensemble();
+  for (int i = 0; i < n; ++i) {
+    if (!members[i] || !members[i]->h.built) {
+      delete es;
+      return set_error(NNPP_ERR_STATE, "ensemble member without neighbour lists");
+    }
+    for (int j = 0; j < i; ++j)
+      if (members[j] == members[i]) {
+        delete es;
+        return set_error(NNPP_ERR_INVALID, "ensemble: a handle appears twice");
+      }
+    es->members.push_back(members[i]);
+    es->e.members.push_back(&members[i]->h);
+  }
+  if (cudaSetDevice(es->e.members[0]->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&es->e.st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete es;
+    return set_error(NNPP_ERR_CUDA, "ensemble stream");
+  }
+  nnpp_status st = engine_build(es->e);
+  if (st != NNPP_OK) {
+    nnpp_ensemble_destroy(es);
+    return st;
+  }
+  *out = es;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_ensemble_forward(nnpp_ensemble* es, int n_steps, int precision) {
+  clear_error();
+  if (!es) return set_error(NNPP_ERR_INVALID, "ensemble is NULL");
+  if (n_steps < 0) return set_error(NNPP_ERR_INVALID, "n_steps < 0");
+  if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
+  NNPP_CUDA(cudaSetDevice(es->e.device));
+  std::vector<long long> nc(es->members.size());
+  for (size_t i = 0; i < es->members.size(); ++i) {
+    DevState ds;
+    NNPP_TRY(read_state(es->members[i]->h, &ds));
+    nc[i] = ds.cg_nc;
+  }
+  NNPP_TRY(engine_run(es->e, n_steps, precision));
+  for (size_t i = 0; i < es->members.size(); ++i) {
+    Handle& h = es->members[i]->h;
+    NNPP_TRY(check_after(h, nc[i]));
+    if (h.engine) NNPP_TRY(engine_params(*h.engine));
+  }
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_ensemble_forward_timed(nnpp_ensemble* es, int n_steps, int precision, double* ms) {
+  clear_error();
+  if (!es || !ms) return set_error(NNPP_ERR_INVALID, "ensemble_forward_timed: bad argument");
+  NNPP_CUDA(cudaSetDevice(es->e.device));
+  NNPP_TRY(engine_warm(es->e, precision));
+  cudaEvent_t e0, e1;
+  NNPP_CUDA(cudaEventCreate(&e0));
+  NNPP_CUDA(cudaEventCreate(&e1));
+  NNPP_CUDA(cudaStreamSynchronize(es->e.st));
+  cudaEventRecord(e0, es->e.st);
+  nnpp_status st = engine_run(es->e, n_steps, precision, true);
+  cudaEventRecord(e1, es->e.st);
+  cudaEventSynchronize(e1);
+  float f = 0.0f;
+  cudaEventElapsedTime(&f, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = f;
+  NNPP_TRY(st);
+  for (auto* m : es->members)
+    if (m->h.engine) NNPP_TRY(engine_params(*m->h.engine));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_ensemble_tuning(nnpp_ensemble* es, int* bins_per_tile, int* lanes_per_node) {
+  clear_error();
+  if (!es) return set_error(NNPP_ERR_INVALID, "ensemble is NULL");
+  if (bins_per_tile) *bins_per_tile = es->e.T;
+  if (lanes_per_node) *lanes_per_node = es->e.W;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_ensemble_destroy(nnpp_ensemble* es) {
+  if (!es) return NNPP_OK;
+  cudaSetDevice(es->e.device);
+  cudaStream_t st = es->e.st;
+  if (st) cudaStreamSynchronize(st);
+  delete es;
+  if (st) cudaStreamDestroy(st);
+  return NNPP_OK;
 }
 
 }  // extern "C"

@@ -81,9 +81,13 @@ struct DevState {
   int max_iter;
   int max_outer;
   int solve_iters;    // inner iterations of the current solve
+  int outer_active;   // this instance still refines its potential
+  int inner_active;   // this instance still iterates its inner CG
   int pad1;
   // per-step mass-curve sampling (adjoint forward)
   double mg_mass_now;
+  // adjoint accumulators: dL/dD_liquid[0..3], dL/dk_diss
+  double adj_g[5];
   // block tickets for last-block reductions
   unsigned int ticket[8];
 };

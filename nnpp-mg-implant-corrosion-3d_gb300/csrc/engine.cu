@@ -1,0 +1,347 @@
+// engine.cu -- batched execution: work lists over one or many instances, the autotuner
+// (bins per tile T, lanes per node W), CUDA-graph capture of the step with device-side loop
+// control (conditional while nodes) and the run loop.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace nnpp {
+
+namespace {
+
+nnpp_status push_settings(Handle& h) {
+  DevState ds;
+  NNPP_CUDA(cudaMemcpyAsync(&ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  ds.tol = h.tol;
+  ds.max_iter = h.max_iter;
+  ds.max_outer = h.max_outer;
+  ds.inner_rel = h.inner_rel;
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  return NNPP_OK;
+}
+
+// KParams of every member for the current record parity (block 0) and the flipped one.
+nnpp_status refresh_params(Engine& e) {
+  const int M = (int)e.members.size();
+  std::vector<KParams> k0(M), k1(M);
+  for (int i = 0; i < M; ++i) {
+    k0[i] = make_kparams(*e.members[i], e.members[i]->cur);
+    k1[i] = make_kparams(*e.members[i], e.members[i]->cur ^ 1);
+  }
+  NNPP_CUDA(cudaMemcpyAsync(e.d_inst[0].get(), k0.data(), sizeof(KParams) * M, cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaMemcpyAsync(e.d_inst[1].get(), k1.data(), sizeof(KParams) * M, cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  return NNPP_OK;
+}
+
+nnpp_status sync_members(Engine& e) {
+  for (Handle* h : e.members)
+    if (h->st != e.st) NNPP_CUDA(cudaStreamSynchronize(h->st));
+  return NNPP_OK;
+}
+
+// Work lists for bins-per-tile T (rebuilds every member's slots).
+nnpp_status build_lists(Engine& e, int T) {
+  const int M = (int)e.members.size();
+  std::vector<TileDesc> tiles;
+  std::vector<Chunk> chunks;
+  std::vector<int> meta(4 * M);
+  int hm = 0;
+  for (int i = 0; i < M; ++i) {
+    Handle& h = *e.members[i];
+    meta[i] = (int)tiles.size();
+    int hmi = 0;
+    NNPP_TRY(build_tiles(h, T, tiles, i, &hmi));
+    meta[M + i] = (int)tiles.size() - meta[i];
+    hm = std::max(hm, hmi);
+    meta[2 * M + i] = (int)chunks.size();
+    for (int b = 0; b < h.N; b += kChunk) {
+      Chunk c;
+      c.inst = i;
+      c.begin = b;
+      c.end = std::min(h.N, b + kChunk);
+      c.pad = 0;
+      chunks.push_back(c);
+    }
+    meta[3 * M + i] = (int)chunks.size() - meta[2 * M + i];
+  }
+  e.ntiles = (int)tiles.size();
+  e.nchunks = (int)chunks.size();
+  e.halo_max = hm;
+  e.T = T;
+  if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
+      !e.d_ticket.alloc(M + 1) || !e.d_partials.alloc((size_t)kReduceSlots * std::max(e.ntiles, e.nchunks)) ||
+      !e.d_inst[0].alloc(M) || !e.d_inst[1].alloc(M))
+    return set_error(NNPP_ERR_NOMEM, "engine work lists");
+  NNPP_CUDA(cudaMemcpyAsync(e.d_tiles.get(), tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaMemcpyAsync(e.d_chunks.get(), chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaMemcpyAsync(e.d_meta.get(), meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, sizeof(unsigned int) * (M + 1), e.st));
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  engine_destroy_graphs(e);
+  return NNPP_OK;
+}
+
+nnpp_status set_active(Engine& e, int outer, int inner) {
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  for (Handle* h : e.members) {
+    DevState ds;
+    NNPP_CUDA(cudaMemcpyAsync(&ds, h->dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, e.st));
+    NNPP_CUDA(cudaStreamSynchronize(e.st));
+    ds.outer_active = outer;
+    ds.inner_active = inner;
+    NNPP_CUDA(cudaMemcpyAsync(h->dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, e.st));
+  }
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  return NNPP_OK;
+}
+
+// Autotuner: bins per tile T and lanes per node W that minimise the FP32 CG operator on the
+// current state (the kernel run ~100 times per step).
+nnpp_status tune(Engine& e, int prec) {
+  std::vector<DevState> saved(e.members.size());
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  for (size_t i = 0; i < e.members.size(); ++i)
+    NNPP_CUDA(cudaMemcpy(&saved[i], e.members[i]->dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost));
+  const int Ts[3] = {2, 4, 8};
+  const int Ws[3] = {4, 8, 16};
+  float best = 1e30f;
+  int bT = 4, bW = 8;
+  cudaEvent_t e0, e1;
+  NNPP_CUDA(cudaEventCreate(&e0));
+  NNPP_CUDA(cudaEventCreate(&e1));
+  for (int T : Ts) {
+    NNPP_TRY(build_lists(e, T));
+    NNPP_TRY(refresh_params(e));
+    for (int W : Ws) {
+      e.W = W;
+      if (prepare_kernels(e.halo_max, W) != NNPP_OK) continue;
+      EngineView v = make_view(e, 0, 0);
+      NNPP_TRY(set_active(e, 1, 1));
+      NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
+      NNPP_TRY(set_active(e, 1, 1));
+      NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+      cudaEventRecord(e0, e.st);
+      for (int r = 0; r < 5; ++r) NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+      cudaEventRecord(e1, e.st);
+      NNPP_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        bT = T;
+        bW = W;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  for (size_t i = 0; i < e.members.size(); ++i)
+    NNPP_CUDA(cudaMemcpy(e.members[i]->dstate.get(), &saved[i], sizeof(DevState), cudaMemcpyHostToDevice));
+  NNPP_TRY(build_lists(e, bT));
+  e.W = bW;
+  NNPP_TRY(prepare_kernels(e.halo_max, bW));
+  e.tuned = true;
+  return NNPP_OK;
+}
+
+// ---------------------------------------------------------------- graph capture --------
+nnpp_status add_while(cudaStream_t st, cudaGraphConditionalHandle hc, cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  NNPP_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = hc;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  NNPP_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+  *body = np.conditional.phGraph_out[0];
+  NNPP_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return NNPP_OK;
+}
+
+// prep; while(outer) { cg_init; while(inner) { spmv; update }; ir_update }
+nnpp_status capture_solve(Engine& e, const EngineView& v, int prec) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  NNPP_CUDA(cudaStreamGetCaptureInfo(e.st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle hout;
+  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 0, 0));
+  NNPP_TRY(launch_prep_b(e, v, prec, e.st, hout, nullptr));
+  cudaGraph_t body_out;
+  NNPP_TRY(add_while(e.st, hout, &body_out));
+  NNPP_CUDA(cudaStreamBeginCaptureToGraph(e.st_b1, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  cudaGraphConditionalHandle hin;
+  NNPP_CUDA(cudaGraphConditionalHandleCreate(&hin, body_out, 0, 0));
+  NNPP_TRY(launch_cg_init_b(e, v, prec, e.st_b1, hin));
+  cudaGraph_t body_in;
+  NNPP_TRY(add_while(e.st_b1, hin, &body_in));
+  NNPP_CUDA(cudaStreamBeginCaptureToGraph(e.st_b2, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st_b2));
+  NNPP_TRY(launch_cg_update_b(e, v, prec, e.st_b2, hin));
+  cudaGraph_t tmp;
+  NNPP_CUDA(cudaStreamEndCapture(e.st_b2, &tmp));
+  NNPP_TRY(launch_ir_update_b(e, v, prec, e.st_b1, hout));
+  NNPP_CUDA(cudaStreamEndCapture(e.st_b1, &tmp));
+  return NNPP_OK;
+}
+
+nnpp_status build_graph(Engine& e, int kind, int prec) {
+  if (e.gexec[kind][prec][0]) return NNPP_OK;
+  NNPP_CUDA(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
+  nnpp_status st = NNPP_OK;
+  const int nsteps = kind == kGraphStep2 ? 2 : 1;
+  for (int s = 0; s < nsteps && st == NNPP_OK; ++s) {
+    EngineView v = make_view(e, s & 1, 1);
+    st = capture_solve(e, v, prec);
+    if (st == NNPP_OK && kind != kGraphSolve) st = launch_transport_b(e, v, prec, e.st, nullptr);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t err = cudaStreamEndCapture(e.st, &g);
+  if (st != NNPP_OK) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return st;
+  }
+  if (err != cudaSuccess) return set_error(NNPP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+  cudaGraphExec_t ex = nullptr;
+  err = cudaGraphInstantiate(&ex, g, 0);
+  if (err != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return set_error(NNPP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+  }
+  e.graph[kind][prec][0] = g;
+  e.gexec[kind][prec][0] = ex;
+  return NNPP_OK;
+}
+
+nnpp_status prepare_run(Engine& e, int prec) {
+  NNPP_TRY(sync_members(e));
+  for (Handle* h : e.members) {
+    NNPP_TRY(convert_state(*h, prec));
+    NNPP_TRY(push_settings(*h));
+  }
+  if (!e.tuned || e.ntiles == 0) {
+    NNPP_TRY(refresh_params(e));
+    NNPP_TRY(tune(e, prec));
+  } else {
+    for (Handle* h : e.members)
+      if (h->tiles_T != e.T) {
+        NNPP_TRY(build_lists(e, e.T));
+        NNPP_TRY(prepare_kernels(e.halo_max, e.W));
+        break;
+      }
+  }
+  NNPP_TRY(refresh_params(e));
+  return NNPP_OK;
+}
+
+}  // namespace
+
+Engine::~Engine() {
+  engine_destroy_graphs(*this);
+  if (st_b1) cudaStreamDestroy(st_b1);
+  if (st_b2) cudaStreamDestroy(st_b2);
+}
+
+void engine_destroy_graphs(Engine& e) {
+  for (int k = 0; k < kGraphKinds; ++k)
+    for (int p = 0; p < 2; ++p)
+      for (int c = 0; c < 2; ++c) {
+        if (e.gexec[k][p][c]) cudaGraphExecDestroy(e.gexec[k][p][c]);
+        if (e.graph[k][p][c]) cudaGraphDestroy(e.graph[k][p][c]);
+        e.gexec[k][p][c] = nullptr;
+        e.graph[k][p][c] = nullptr;
+      }
+}
+
+EngineView make_view(Engine& e, int parity, int in_graph) {
+  EngineView v;
+  const int M = (int)e.members.size();
+  v.inst = e.d_inst[parity].get();
+  v.tiles = e.d_tiles.get();
+  v.chunks = e.d_chunks.get();
+  v.tile_first = e.d_meta.get();
+  v.tile_count = e.d_meta.get() + M;
+  v.chunk_first = e.d_meta.get() + 2 * M;
+  v.chunk_count = e.d_meta.get() + 3 * M;
+  v.ticket = e.d_ticket.get();
+  v.partials = e.d_partials.get();
+  v.ntiles = e.ntiles;
+  v.nchunks = e.nchunks;
+  v.M = M;
+  v.in_graph = in_graph;
+  v.stride = std::max(e.ntiles, e.nchunks);
+  v.halo_max = e.halo_max;
+  return v;
+}
+
+nnpp_status engine_build(Engine& e) {
+  if (e.members.empty()) return set_error(NNPP_ERR_INVALID, "engine without members");
+  e.device = e.members[0]->device;
+  for (Handle* h : e.members) {
+    if (!h->built) return set_error(NNPP_ERR_STATE, "engine member without neighbour lists");
+    if (h->device != e.device) return set_error(NNPP_ERR_INVALID, "engine members on different devices");
+  }
+  if (!e.st_b1) NNPP_CUDA(cudaStreamCreateWithFlags(&e.st_b1, cudaStreamNonBlocking));
+  if (!e.st_b2) NNPP_CUDA(cudaStreamCreateWithFlags(&e.st_b2, cudaStreamNonBlocking));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e.device);
+  if (sms <= 0) sms = 152;
+  e.grid = sms * 4;
+  NNPP_TRY(build_lists(e, e.T));
+  NNPP_TRY(prepare_kernels(e.halo_max, e.W));
+  return NNPP_OK;
+}
+
+nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
+  if (!prepared) NNPP_TRY(prepare_run(e, prec));
+  int done = 0;
+  if (n_steps >= 2) NNPP_TRY(build_graph(e, kGraphStep2, prec));
+  if (n_steps % 2) NNPP_TRY(build_graph(e, kGraphStep1, prec));
+  while (n_steps - done >= 2) {
+    NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphStep2][prec][0], e.st));
+    done += 2;
+  }
+  if (n_steps - done == 1) {
+    NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphStep1][prec][0], e.st));
+    for (Handle* h : e.members) h->cur ^= 1;
+    NNPP_TRY(refresh_params(e));
+  }
+  if (e.members.size() > 1 || e.members[0]->st != e.st) NNPP_CUDA(cudaStreamSynchronize(e.st));
+  return NNPP_OK;
+}
+
+nnpp_status engine_warm(Engine& e, int prec) {
+  NNPP_TRY(prepare_run(e, prec));
+  NNPP_TRY(build_graph(e, kGraphStep2, prec));
+  NNPP_TRY(build_graph(e, kGraphStep1, prec));
+  return NNPP_OK;
+}
+
+nnpp_status engine_params(Engine& e) { return refresh_params(e); }
+
+nnpp_status engine_solve(Engine& e, int prec) {
+  NNPP_TRY(prepare_run(e, prec));
+  NNPP_TRY(build_graph(e, kGraphSolve, prec));
+  NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphSolve][prec][0], e.st));
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  return NNPP_OK;
+}
+
+Handle::~Handle() {
+  if (engine) {
+    delete engine;
+    engine = nullptr;
+  }
+}
+
+}  // namespace nnpp

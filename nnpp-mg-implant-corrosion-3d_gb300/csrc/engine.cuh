@@ -1,0 +1,111 @@
+// engine.cuh -- batched execution of one or many instances: tile and chunk work lists,
+// per-instance reductions, the CUDA graph of a step.
+#ifndef NNPP_ENGINE_CUH
+#define NNPP_ENGINE_CUH
+
+#include <vector>
+
+#include "handle.cuh"
+
+namespace nnpp {
+
+// A tile: T consecutive bins along x of one instance (its "own" nodes) and the 3x3 rows of
+// bins around them (its halo).  Bins have side >= the horizon radius, so every neighbour of
+// an own node lies in the halo; halo rows are contiguous node ranges in the internal order.
+struct TileDesc {
+  int inst;
+  int own_begin, own_end;  // own nodes (internal indices of the instance)
+  int hb[9];               // halo row r: nodes [hb[r], hb[r] + hl[r])
+  int hl[9];
+  int halo;                // total halo nodes (sum of hl)
+  int cb[3];               // centre bin (coordinates are staged relative to it)
+  int pad;
+};
+
+// An elementwise work item: nodes [begin, end) of one instance.
+struct Chunk {
+  int inst;
+  int begin, end;
+  int pad;
+};
+
+// What every batched kernel receives.
+struct EngineView {
+  const KParams* inst;      // per instance
+  const TileDesc* tiles;    // grouped by instance
+  const Chunk* chunks;      // grouped by instance
+  const int* tile_first;    // per instance: first tile index
+  const int* tile_count;    // per instance: number of tiles
+  const int* chunk_first;
+  const int* chunk_count;
+  unsigned int* ticket;     // per instance completion counters, + [M] global
+  double* partials;         // kReduceSlots * max(ntiles, nchunks)
+  int ntiles, nchunks, M, in_graph;
+  int stride;               // max(ntiles, nchunks): slot stride of partials
+  int halo_max;             // largest halo (dynamic shared memory sizing)
+};
+
+constexpr int kChunk = 4096;  // nodes per elementwise work item
+
+struct Engine {
+  std::vector<Handle*> members;
+  int T = 4;                // bins per tile (autotuned)
+  int W = 8;                // lanes per node (autotuned)
+  bool tuned = false;
+  int grid = 0;
+  int halo_max = 0;
+  DBuf<KParams> d_inst[2];  // indexed by the parity of the current record buffer
+  DBuf<TileDesc> d_tiles;
+  DBuf<Chunk> d_chunks;
+  DBuf<int> d_meta;         // tile_first, tile_count, chunk_first, chunk_count (4*M)
+  DBuf<unsigned int> d_ticket;
+  DBuf<double> d_partials;
+  int ntiles = 0, nchunks = 0;
+  cudaStream_t st = nullptr, st_b1 = nullptr, st_b2 = nullptr;
+  int device = 0;
+  int cur = 0;              // record parity shared by all members
+  cudaGraphExec_t gexec[kGraphKinds][2][2] = {};
+  cudaGraph_t graph[kGraphKinds][2][2] = {};
+  ~Engine();
+};
+
+EngineView make_view(Engine& e, int parity, int in_graph);
+
+// engine.cu
+nnpp_status engine_build(Engine& e);             // tiles, work lists, autotune
+nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared = false);
+nnpp_status engine_solve(Engine& e, int prec);   // potential solve only (current state)
+nnpp_status engine_warm(Engine& e, int prec);    // tune, upload parameters, build graphs
+nnpp_status engine_params(Engine& e);            // re-upload the members' KParams
+void engine_destroy_graphs(Engine& e);
+
+// tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max);
+
+// step.cu launchers (batched)
+nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                          cudaGraphConditionalHandle hc, double* F11_out);
+nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                             cudaGraphConditionalHandle hc);
+nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
+nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               cudaGraphConditionalHandle hc);
+nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               cudaGraphConditionalHandle hc);
+nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               double* F_out);
+nnpp_status prepare_kernels(int halo_max, int W);
+
+// adjoint (step.cu)
+nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec64* snap,
+                                 const Rec64* snap1, const double* lam, double* mu, double* nu,
+                                 double* acc, cudaStream_t st);
+nnpp_status launch_adj_combine(Handle& h, const double* mu, double* lam, double inject);
+nnpp_status launch_snap_state(Handle& h, Rec64* dst);
+nnpp_status launch_snap_phi(Handle& h, Rec64* dst);
+nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev);
+nnpp_status launch_sum_c0(Handle& h, double* out);
+
+}  // namespace nnpp
+
+#endif  // NNPP_ENGINE_CUH

@@ -10,53 +10,62 @@
 
 namespace nnpp {
 
-// Everything a step kernel reads or writes, passed by value.  Pointers are device pointers
-// into the handle's buffers (internal node order).
+// Everything a step kernel reads or writes for one instance; stored in device memory, one
+// per instance of a batched launch.  Pointers are device pointers into the instance's
+// buffers (internal node order).
 struct KParams {
   int N;
-  int grid;                     // CTAs of every step kernel (layout of `partials`)
+  int pad0;
   const int* row;
   const int* col;
+  const unsigned short* slot16;  // per bond: halo slot of the neighbour within its tile
+  const float4* posrec;          // per node: {x, y, z offsets within its bin, packed bin}
   const double* w64;
   const float* w32;
   const unsigned char* dirmask;  // bit k: species k Dirichlet, bit S: potential Dirichlet
-  const double* bcval;          // (S+1)*N: species values already divided by CSolid
+  const double* bcval;           // (S+1)*N: species values already divided by CSolid
   Rec32* rec32_cur;
   Rec32* rec32_nxt;
-  float4* clo;                  // compensation words of the FP32 concentrations
+  float4* clo;                   // compensation words of the FP32 concentrations
   Rec64* rec64_cur;
   Rec64* rec64_nxt;
-  double* phi64;                // potential (FP64, both precisions)
+  double* phi64;                 // potential (FP64, both precisions)
+  double* phi_prev;              // potential of the previous step (linear extrapolation)
   int* flip_step;
   // potential solve
   double* b64;
   double* r64;
-  double* dsum64;               // sum of liquid-liquid weights (K11 diagonal)
-  unsigned char* freem;         // unknown of the potential solve
+  double* dsum64;                // sum of liquid-liquid weights (K11 diagonal)
+  unsigned char* freem;          // unknown of the potential solve
   float* d32;
   float* dinv32;
   double* dinv64;
   float *rin32, *z32, *p32, *q32, *e32;
   double *rin64, *z64, *p64, *q64, *e64;
-  double* partials;             // kReduceSlots * grid
   DevState* ds;
-  const double* voln1rel_ptr;   // value entering BV (ds->voln1rel, or an override)
+  const double* voln1rel_ptr;    // value entering BV (ds->voln1rel, or an override)
+  const double* b_override;      // right-hand side of the potential solve instead of
+                                 // (1/(K sigma)) F CSolid sum_k z_k c_k (adjoint solves)
   // physics
   double dt, csat, c_floor, k_diss, sw, vol_red, lam;
   double K1[S], K2zF[S], DL[S], DSo[S], z[S];
+  float h32;                     // bin side
+  float delta_lo, delta_hi, inv_dx, dVf;  // FP32 weight recompute: beta and dV
   int sub_step_no;
-  int dissolve_count;           // 1: count the dissolution source into the diagnostics
-  int in_graph;                 // 1: kernels set the conditional handles of the graph
+  int dissolve_count;            // 1: count the dissolution source into the diagnostics
+  int extrapolate;               // 1: warm start phi = 2 phi^n - phi^{n-1}
+  int pad1;
 };
 
 enum GraphKind { kGraphStep2 = 0, kGraphStep1 = 1, kGraphSolve = 2, kGraphKinds = 3 };
+
+struct Engine;
 
 struct Handle {
   nnpp_params p;
   int N = 0;
   int device = 0;
   cudaStream_t st = nullptr;
-  cudaStream_t st_b1 = nullptr, st_b2 = nullptr;  // capture streams for conditional bodies
   // user-order inputs
   DBuf<double> ux, uy, uz;
   std::vector<int> h_bctypes;
@@ -67,6 +76,11 @@ struct Handle {
   Layout lay;
   bool built = false;
   int max_node_no = 0;
+  // tiles (built for tiles_T bins per tile)
+  DBuf<unsigned short> slot16;
+  DBuf<float4> posrec;
+  float h32 = 0.f;
+  int tiles_T = 0;
   // per-node constants, internal order
   DBuf<unsigned char> dirmask;
   DBuf<double> bcval;
@@ -76,13 +90,12 @@ struct Handle {
   DBuf<Rec64> rec64[2];
   int cur = 0;
   int state_prec = NNPP_FP64;
-  DBuf<double> phi64;
+  DBuf<double> phi64, phi_prev;
   DBuf<int> flip_step;
   // solver
   DBuf<double> b64, r64, dsum64, dinv64, rin64, z64, p64, q64, e64;
   DBuf<float> d32, dinv32, rin32, z32, p32, q32, e32;
   DBuf<unsigned char> freem;
-  DBuf<double> partials;
   DBuf<DevState> dstate;
   DBuf<double> scratch_d;       // small device scratch (voln1rel override, ...)
   DBuf<double> user_stage;      // (S+1)*N FP64 staging for host transfers
@@ -92,40 +105,30 @@ struct Handle {
   int max_outer = 30;
   double inner_rel = 1e-4;
   int strict = 0;
-  int grid = 0;
-  int lanes = 8;                // lanes per node of the bond kernels (autotuned)
-  // graphs [kind][precision][cur]
-  cudaGraphExec_t gexec[kGraphKinds][2][2] = {};
-  cudaGraph_t graph[kGraphKinds][2][2] = {};
-  // adjoint checkpoints (host-owned device buffers)
+  int extrapolate = 1;
+  const double* b_override = nullptr;  // set during adjoint solves
+  int grid = 0;                 // CTAs of the per-handle elementwise kernels
+  Engine* engine = nullptr;     // single-instance engine (owned)
+  // adjoint checkpoints: the full device state at a step
   struct Ckpt {
-    DBuf<Rec64> rec;
-    DBuf<double> phi;
+    DBuf<Rec32> rec32;
+    DBuf<float4> clo;
+    DBuf<Rec64> rec64;
+    DBuf<double> phi, phi_prev;
+    DBuf<int> flip;
     DevState ds;
+    int cur = 0, prec = 0;
   };
   std::vector<Ckpt> ckpts;
+  Ckpt fwd_end;
   int fwd_steps = 0, ck_every = 0, sample_every = 0, fwd_prec = NNPP_FP64;
   std::vector<double> curve;
-  DevState ds_start;
-  DBuf<Rec64> rec_start;
-  DBuf<double> phi_start;
-  DBuf<int> flip_start;
+  ~Handle();
 };
 
 // step.cu
 nnpp_status step_alloc(Handle& h);
 KParams make_kparams(Handle& h, int cur);
-nnpp_status launch_prep(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                        cudaGraphConditionalHandle hc, double* F11_out);
-nnpp_status launch_cg_init(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                           cudaGraphConditionalHandle hc);
-nnpp_status launch_cg_iter(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                           cudaGraphConditionalHandle hc);
-nnpp_status launch_cg_spmv(Handle& h, const KParams& kp, int prec, cudaStream_t st);
-nnpp_status launch_ir_update(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                             cudaGraphConditionalHandle hc);
-nnpp_status launch_transport(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                             double* F_out);
 // dirichlet_phi: put the boundary values of the potential on its Dirichlet nodes (state
 // for stepping); false keeps the given values (inputs of the residual entry point).
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,

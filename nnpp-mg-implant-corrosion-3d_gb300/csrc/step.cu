@@ -1,21 +1,29 @@
-// step.cu -- the explicit NNPP step on the GPU: potential solve (K11, utils.h:1794-1848 /
-// F11, utils.h:798-841) and transport (bond sums utils.h:72-257, Dirichlet main.cpp:676-712,
-// clamp main.cpp:805-837, phase flip main.cpp:914-922, volume main.cpp:944-949).
+// step.cu -- the explicit NNPP step on the GPU for one or many instances: potential solve
+// (K11, utils.h:1794-1848 / F11, utils.h:798-841) and transport (bond sums utils.h:72-257,
+// Dirichlet main.cpp:676-712, clamp main.cpp:805-837, phase flip main.cpp:914-922, volume
+// main.cpp:944-949).
 //
-// Two precisions share one structure:
-//   FP64  : FP64 records and weights, FP64 Jacobi-preconditioned CG.
-//   mixed : FP32 bond sums over 32-byte records with FP64-computed FP32 weights, per-lane
-//           FP32 accumulation and a compensated (TwoSum) cross-lane reduction per node;
-//           concentrations kept as compensated FP32 pairs (hi + lo) so that the time
-//           accumulation and the FP64 saturation test see ~48 significant bits; the
-//           potential is refined in FP64 (FP64 residual b - A phi on FP64 weights) with
-//           FP32 CG for the corrections.
+// Work is a list of tiles (bond kernels) or node chunks (vector kernels) over all instances
+// of a batch; each CTA loops over the list (persistent grid).  A tile kernel stages the
+// tile's halo into shared memory and reaches every neighbour through a 16-bit slot, so the
+// per-bond stream is 2 bytes (+ the stored weight where one is used).
 //
-// Every kernel that reduces writes one partial per block; the block that takes the last
-// ticket reduces them in block order, so results are bitwise reproducible.
+// Precision:
+//   FP64  : FP64 records and stored FP64 weights, FP64 Jacobi-preconditioned CG.
+//   mixed : transport in FP32 with stored FP32 weights (computed in FP64), per-lane FP32
+//           accumulation and a compensated (TwoSum) cross-lane reduction per node;
+//           concentrations kept as compensated FP32 pairs (hi + lo), the saturation test on
+//           hi + lo in FP64; potential: FP64 residual b - A phi (stored FP64 weights) with
+//           FP32 CG corrections whose operator recomputes the weights in FP32 from
+//           tile-relative coordinates.
+//
+// Reductions: every work item writes one partial per value; the CTA that completes an
+// instance's last item reduces that instance's partials in item order (deterministic), and
+// the last instance to finish sets the graph's loop condition (any instance still active).
 #include <cmath>
+#include <cstring>
 
-#include "handle.cuh"
+#include "engine.cuh"
 
 namespace nnpp {
 
@@ -23,10 +31,88 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ void node_range(int N, int& beg, int& end) {
-  const int chunk = (N + gridDim.x - 1) / gridDim.x;
-  beg = blockIdx.x * chunk;
-  end = min(N, beg + chunk);
+// ---------------------------------------------------------------- work-item plumbing ----
+struct TileSmem {
+  int off[10];  // prefix offsets of the 9 halo rows, off[9] = halo size
+  int hb[9];
+  int flag;
+};
+
+__device__ __forceinline__ void load_tile(const TileDesc& t, TileSmem& ts) {
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int r = 0; r < 9; ++r) {
+      ts.off[r] = acc;
+      ts.hb[r] = t.hb[r];
+      acc += t.hl[r];
+    }
+    ts.off[9] = acc;
+  }
+  __syncthreads();
+}
+
+// node of halo index s
+__device__ __forceinline__ int halo_node(const TileSmem& ts, int s) {
+  int r = 0;
+#pragma unroll
+  for (int q = 1; q < 9; ++q) r += (s >= ts.off[q]) ? 1 : 0;
+  return ts.hb[r] + (s - ts.off[r]);
+}
+
+// Records that an item of an instance is done; true in the CTA that completed the
+// instance's last one (all threads).  `count` = number of items of the instance.
+__device__ __forceinline__ bool item_done(unsigned int* ticket, int count, int* s_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(ticket, 1u);
+    *s_flag = (t == (unsigned int)(count - 1)) ? 1 : 0;
+  }
+  __syncthreads();
+  const bool last = *s_flag != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+// thread 0 of an instance's finishing CTA: reset its ticket, count the instance as done and,
+// in the last instance, set the loop condition to "any instance active".
+__device__ __forceinline__ void instance_finished(const EngineView& v, int inst, int which,
+                                                  cudaGraphConditionalHandle hc) {
+  v.ticket[inst] = 0;
+  __threadfence();
+  const unsigned int g = atomicAdd(&v.ticket[v.M], 1u);
+  if (g == (unsigned int)(v.M - 1)) {
+    __threadfence();
+    v.ticket[v.M] = 0;
+    int any = 0;
+    for (int i = 0; i < v.M; ++i) {
+      const DevState* ds = v.inst[i].ds;
+      any |= (which == 0) ? *((volatile const int*)&ds->outer_active)
+                          : *((volatile const int*)&ds->inner_active);
+    }
+    if (v.in_graph) cudaGraphSetConditional(hc, any ? 1u : 0u);
+  }
+}
+
+// reduce NV partials of items [first, first+count) (layout partials[k*stride + item])
+template <int NV>
+__device__ __forceinline__ void reduce_items(const double* partials, int stride, int first, int count,
+                                             double (&out)[NV], double* sm) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = 0.0;
+    for (int b = threadIdx.x; b < count; b += kBlock) x += partials[(size_t)k * stride + first + b];
+    out[k] = x;
+  }
+  block_sum<NV, kBlock>(out, sm);
+}
+
+template <int NV>
+__device__ __forceinline__ void write_partials(const EngineView& v, int item, double (&part)[NV], double* sm) {
+  block_sum<NV, kBlock>(part, sm);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v.partials[(size_t)k * v.stride + item] = part[k];
 }
 
 template <typename P>
@@ -39,7 +125,6 @@ struct VecSel<float> {
   __device__ static float* q(const KParams& k) { return k.q32; }
   __device__ static float* e(const KParams& k) { return k.e32; }
   __device__ static const float* dinv(const KParams& k) { return k.dinv32; }
-  __device__ static const float* w(const KParams& k) { return k.w32; }
 };
 template <>
 struct VecSel<double> {
@@ -49,7 +134,6 @@ struct VecSel<double> {
   __device__ static double* q(const KParams& k) { return k.q64; }
   __device__ static double* e(const KParams& k) { return k.e64; }
   __device__ static const double* dinv(const KParams& k) { return k.dinv64; }
-  __device__ static const double* w(const KParams& k) { return k.w64; }
 };
 
 template <typename P>
@@ -63,7 +147,6 @@ __device__ __forceinline__ float phase_of<double>(const KParams& k, int a) {
   return (float)k.rec64_cur[a].phase;
 }
 
-// FP64 concentration of species s at node a in the current state
 template <typename P>
 __device__ __forceinline__ double conc_of(const KParams& k, int a, int s);
 template <>
@@ -87,89 +170,120 @@ __device__ __forceinline__ void set_phi_rec(const KParams& k, int a, double phi,
   }
 }
 
+__device__ __forceinline__ float sel4(const float4& v, int s) {
+  return s == 0 ? v.x : s == 1 ? v.y : s == 2 ? v.z : v.w;
+}
+
 // ------------------------------------------------------------------- potential: prep ----
-// Per node: diagonal of K11 (sum of liquid-liquid weights), unknown mask, right-hand side
-// b = (1/(K sigma)) F CSolid sum_k z_k c_k, FP64 residual r = b - A phi.  With F11_out set,
-// writes the reference's F11 (utils.h:798-841) for every node instead and changes nothing.
+// Per node: K11 diagonal (sum of liquid-liquid weights), unknown mask, right-hand side
+// b = (1/(K sigma)) F CSolid sum_k z_k c_k and the FP64 residual r = b - A phi.  With F11_out
+// (single instance), writes the reference's F11 (utils.h:798-841) for every node instead.
 template <typename P, int W>
-__global__ void __launch_bounds__(kBlock) k_prep(KParams k, cudaGraphConditionalHandle hc,
+__global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditionalHandle hc,
                                                  double* F11_out) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
   const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
-  int beg, end;
-  node_range(k.N, beg, end);
-  double part[2] = {0.0, 0.0};  // ||b_eff||^2, ||r||^2
-  for (int a0 = beg; a0 < end; a0 += nseg) {
-    const int a = a0 + seg;
-    const bool act = a < end;
-    const float pa = act ? phase_of<P>(k, a) : 1.0f;
-    const bool dirp = act && ((k.dirmask[a] >> S) & 1);
-    const bool scan = act && pa == 0.0f && (F11_out != nullptr || !dirp);
-    double dsum = 0.0, swphi = 0.0, cpl = 0.0;
-    int anyll = 0;
-    if (scan) {
-      for (int j = k.row[a] + sub; j < k.row[a + 1]; j += W) {
-        const int n = k.col[j];
-        if (phase_of<P>(k, n) == 0.0f) {
-          const double w = k.w64[j];
-          const double ph = k.phi64[n];
-          dsum += w;
-          swphi += w * ph;
-          anyll = 1;
-          if ((k.dirmask[n] >> S) & 1) cpl += w * ph;
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    load_tile(t, ts);
+    double* sphi = reinterpret_cast<double*>(dsm);
+    unsigned char* sfl = dsm + sizeof(double) * (size_t)t.halo;
+    const double* phi64 = k.phi64;
+    const unsigned char* dm = k.dirmask;
+    for (int s = threadIdx.x; s < t.halo; s += kBlock) {
+      const int n = halo_node(ts, s);
+      sphi[s] = phi64[n];
+      sfl[s] = (unsigned char)((phase_of<P>(k, n) == 0.0f ? 1 : 0) | (((dm[n] >> S) & 1) ? 2 : 0));
+    }
+    __syncthreads();
+    double part[2] = {0.0, 0.0};
+    const int* row = k.row;
+    const unsigned short* slot = k.slot16;
+    const double* w64 = k.w64;
+    const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+    for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+      const int a = a0 + seg;
+      const bool act = a < t.own_end;
+      const int so = own0 + (a - t.own_begin);
+      const unsigned char fa = act ? sfl[so] : 0;
+      const bool scan = act && (fa & 1) && (F11_out != nullptr || !(fa & 2));
+      double dsum = 0.0, swphi = 0.0, cpl = 0.0;
+      int anyll = 0;
+      if (scan) {
+        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+          const int s = slot[j];
+          const unsigned char f = sfl[s];
+          if (f & 1) {
+            const double w = w64[j];
+            const double ph = sphi[s];
+            dsum += w;
+            swphi += w * ph;
+            anyll = 1;
+            if (f & 2) cpl += w * ph;
+          }
+        }
+      }
+      dsum = seg_reduce_d<W>(dsum);
+      swphi = seg_reduce_d<W>(swphi);
+      cpl = seg_reduce_d<W>(cpl);
+      anyll = seg_or<W>(anyll);
+      if (act && sub == 0) {
+        double b;
+        if (k.b_override) {
+          b = k.b_override[a];
+        } else {
+          double R11 = 0.0;
+          for (int s = 0; s < S; ++s) R11 += k.z[s] * conc_of<P>(k, a, s);
+          b = k.lam * R11;
+        }
+        const double pha = sphi[so];
+        if (F11_out) {
+          F11_out[a] = anyll ? (dsum * pha - swphi) - b : 0.0;
+        } else {
+          const bool fr = !(fa & 2) && (fa & 1) && anyll;
+          k.freem[a] = fr ? 1 : 0;
+          k.dsum64[a] = fr ? dsum : 1.0;
+          k.dinv64[a] = fr ? 1.0 / dsum : 0.0;
+          k.d32[a] = fr ? (float)dsum : 1.0f;
+          k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
+          const double bb = fr ? b : 0.0;
+          const double r = fr ? bb - (dsum * pha - swphi) : 0.0;
+          k.b64[a] = bb;
+          k.r64[a] = r;
+          const double be = bb + (fr ? cpl : 0.0);
+          part[0] += be * be;
+          part[1] += r * r;
         }
       }
     }
-    dsum = seg_reduce_d<W>(dsum);
-    swphi = seg_reduce_d<W>(swphi);
-    cpl = seg_reduce_d<W>(cpl);
-    anyll = seg_or<W>(anyll);
-    if (act && sub == 0) {
-      double R11 = 0.0;
-      for (int s = 0; s < S; ++s) R11 += k.z[s] * conc_of<P>(k, a, s);
-      const double b = k.lam * R11;
-      if (F11_out) {
-        F11_out[a] = anyll ? (dsum * k.phi64[a] - swphi) - b : 0.0;
-      } else {
-        const bool fr = !dirp && pa == 0.0f && anyll;
-        k.freem[a] = fr ? 1 : 0;
-        k.dsum64[a] = fr ? dsum : 1.0;
-        k.dinv64[a] = fr ? 1.0 / dsum : 0.0;
-        k.d32[a] = fr ? (float)dsum : 1.0f;
-        k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
-        const double bb = fr ? b : 0.0;
-        const double r = fr ? bb - (dsum * k.phi64[a] - swphi) : 0.0;
-        k.b64[a] = bb;
-        k.r64[a] = r;
-        part[0] += (bb + (fr ? cpl : 0.0)) * (bb + (fr ? cpl : 0.0));
-        part[1] += r * r;
+    if (!F11_out) {
+      write_partials<2>(v, item, part, sm);
+      if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+        double tot[2];
+        reduce_items<2>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+        if (threadIdx.x == 0) {
+          DevState* ds = k.ds;
+          const double bn = tot[0] > 0.0 ? tot[0] : 1.0;
+          ds->bnorm2 = bn;
+          ds->rnorm2 = tot[1];
+          ds->outer_it = 0;
+          ds->solve_iters = 0;
+          const bool go = tot[1] > ds->tol * ds->tol * bn && ds->max_outer > 0;
+          if (!go) {
+            ds->cg_solves += 1;
+            ds->last_relres = sqrt(tot[1] / bn);
+          }
+          ds->outer_active = go ? 1 : 0;
+          ds->inner_active = 0;
+          instance_finished(v, t.inst, 0, hc);
+        }
       }
     }
-  }
-  if (F11_out) return;
-  block_sum<2, kBlock>(part, sm);
-  if (threadIdx.x == 0) {
-    k.partials[0 * gridDim.x + blockIdx.x] = part[0];
-    k.partials[1 * gridDim.x + blockIdx.x] = part[1];
-  }
-  if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
-  double tot[2];
-  reduce_partials<2, kBlock>(k.partials, gridDim.x, tot, sm);
-  if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    double bn = tot[0] > 0.0 ? tot[0] : 1.0;
-    ds->bnorm2 = bn;
-    ds->rnorm2 = tot[1];
-    ds->outer_it = 0;
-    ds->solve_iters = 0;
-    const bool go = tot[1] > ds->tol * ds->tol * bn && ds->max_outer > 0;
-    if (!go) {
-      ds->cg_solves += 1;
-      ds->last_relres = sqrt(tot[1] / bn);
-    }
-    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
+    __syncthreads();
   }
 }
 
@@ -177,223 +291,349 @@ __global__ void __launch_bounds__(kBlock) k_prep(KParams k, cudaGraphConditional
 // Inner PCG on A e = r (r: FP64 outer residual rounded to P).  Jacobi preconditioner
 // (the reference's Eigen::DiagonalPreconditioner, main.cpp:714-768).
 template <typename P>
-__global__ void __launch_bounds__(kBlock) k_cg_init(KParams k, cudaGraphConditionalHandle hc,
+__global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphConditionalHandle hc,
                                                     int fp64) {
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
-  P* rin = VecSel<P>::rin(k);
-  P* z = VecSel<P>::z(k);
-  P* p = VecSel<P>::p(k);
-  P* q = VecSel<P>::q(k);
-  P* e = VecSel<P>::e(k);
-  const P* dinv = VecSel<P>::dinv(k);
-  double part[2] = {0.0, 0.0};
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
-    const P r = (P)k.r64[a];
-    const P zz = r * dinv[a];
-    rin[a] = r;
-    z[a] = zz;
-    p[a] = P(0);
-    q[a] = P(0);
-    e[a] = P(0);
-    part[0] += (double)r * (double)zz;
-    part[1] += (double)r * (double)r;
-  }
-  block_sum<2, kBlock>(part, sm);
-  if (threadIdx.x == 0) {
-    k.partials[0 * gridDim.x + blockIdx.x] = part[0];
-    k.partials[1 * gridDim.x + blockIdx.x] = part[1];
-  }
-  if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
-  double tot[2];
-  reduce_partials<2, kBlock>(k.partials, gridDim.x, tot, sm);
-  if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    ds->rz = tot[0];
-    ds->rr0 = tot[1];
-    ds->rr = tot[1];
-    ds->beta = 0.0;
-    ds->alpha = 0.0;
-    ds->inner_it = 0;
-    // FP64: solve to the final tolerance in one sweep; mixed: reduce by inner_rel
-    const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
-                               : ds->inner_rel * ds->inner_rel * tot[1];
-    ds->inner_target = target;
-    if (k.in_graph) cudaGraphSetConditional(hc, (tot[1] > target && ds->max_iter > 0) ? 1u : 0u);
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const bool active = *((volatile int*)&k.ds->outer_active) != 0;
+    double part[2] = {0.0, 0.0};
+    if (active) {
+      P* rin = VecSel<P>::rin(k);
+      P* z = VecSel<P>::z(k);
+      P* p = VecSel<P>::p(k);
+      P* q = VecSel<P>::q(k);
+      P* e = VecSel<P>::e(k);
+      const P* dinv = VecSel<P>::dinv(k);
+      for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+        const P r = (P)k.r64[a];
+        const P zz = r * dinv[a];
+        rin[a] = r;
+        z[a] = zz;
+        p[a] = P(0);
+        q[a] = P(0);
+        e[a] = P(0);
+        part[0] += (double)r * (double)zz;
+        part[1] += (double)r * (double)r;
+      }
+    }
+    write_partials<2>(v, item, part, sm);
+    if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
+      double tot[2];
+      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->outer_active) {
+          ds->rz = tot[0];
+          ds->rr = tot[1];
+          ds->beta = 0.0;
+          ds->alpha = 0.0;
+          ds->inner_it = 0;
+          // FP64: solve to the final tolerance in one sweep; mixed: reduce by inner_rel
+          const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
+                                     : ds->inner_rel * ds->inner_rel * tot[1];
+          ds->inner_target = target;
+          ds->inner_active = (tot[1] > target && ds->max_iter > 0) ? 1 : 0;
+        } else {
+          ds->inner_active = 0;
+        }
+        instance_finished(v, c.inst, 1, hc);
+      }
+    }
+    __syncthreads();
   }
 }
 
-// q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha
-template <typename P, int W>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(KParams k) {
+// q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
+// FP32: the weights are recomputed from the staged tile-relative coordinates.
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
-  const P* z = VecSel<P>::z(k);
-  P* p = VecSel<P>::p(k);
-  P* q = VecSel<P>::q(k);
-  const P* w = VecSel<P>::w(k);
-  const P beta = (P)k.ds->beta;
-  int beg, end;
-  node_range(k.N, beg, end);
-  double part[1] = {0.0};
-  for (int a0 = beg; a0 < end; a0 += nseg) {
-    const int a = a0 + seg;
-    const bool act = a < end && k.freem[a];
-    P acc = P(0);
-    if (act)
-      for (int j = k.row[a] + sub; j < k.row[a + 1]; j += W) acc += w[j] * z[k.col[j]];
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
+    double part[1] = {0.0};
+    if (active) {
+      load_tile(t, ts);
+      float4* hs = reinterpret_cast<float4*>(dsm);
+      const float4* posrec = k.posrec;
+      const float* z = k.z32;
+      const float h = k.h32;
+      for (int s = threadIdx.x; s < t.halo; s += kBlock) {
+        const int n = halo_node(ts, s);
+        const float4 pr = posrec[n];
+        const int pb = __float_as_int(pr.w);
+        float4 o;
+        o.x = fmaf((float)((pb & 1023) - t.cb[0]), h, pr.x);
+        o.y = fmaf((float)(((pb >> 10) & 1023) - t.cb[1]), h, pr.y);
+        o.z = fmaf((float)(((pb >> 20) & 1023) - t.cb[2]), h, pr.z);
+        o.w = z[n];
+        hs[s] = o;
+      }
+      __syncthreads();
+      const int* row = k.row;
+      const unsigned short* slot = k.slot16;
+      const unsigned char* freem = k.freem;
+      float* p = k.p32;
+      float* q = k.q32;
+      const float beta = (float)k.ds->beta;
+      const float dlo = k.delta_lo, dhi = k.delta_hi, idx = k.inv_dx, dV = k.dVf;
+      const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+      for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+        const int a = a0 + seg;
+        const bool act = a < t.own_end && freem[a];
+        float acc = 0.0f;
+        float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act) {
+          me = hs[own0 + (a - t.own_begin)];
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+            const float4 o = hs[slot[j]];
+            const float dx = o.x - me.x, dy = o.y - me.y, dz = o.z - me.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float ri = rsqrtf(r2);
+            const float xi = r2 * ri;
+            const float bt = xi <= dlo ? 1.0f : (xi <= dhi ? (dhi - xi) * idx : 0.0f);
+            const float w = bt * dV * ri * ri * ri;
+            acc = fmaf(w, o.w, acc);
+          }
+        }
 #pragma unroll
-    for (int off = W / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, W);
-    if (act && sub == 0) {
-      const P dg = sizeof(P) == 4 ? (P)k.d32[a] : (P)k.dsum64[a];
-      const P s = dg * z[a] - acc;
-      const P qn = s + beta * q[a];
-      const P pn = z[a] + beta * p[a];
-      q[a] = qn;
-      p[a] = pn;
-      part[0] += (double)pn * (double)qn;
+        for (int off = W / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, W);
+        if (act && sub == 0) {
+          const float s = k.d32[a] * me.w - acc;
+          const float qn = s + beta * q[a];
+          const float pn = me.w + beta * p[a];
+          q[a] = qn;
+          p[a] = pn;
+          part[0] += (double)pn * (double)qn;
+        }
+      }
     }
+    write_partials<1>(v, item, part, sm);
+    if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+      double tot[1];
+      reduce_items<1>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+        v.ticket[t.inst] = 0;
+      }
+    }
+    __syncthreads();
   }
-  block_sum<1, kBlock>(part, sm);
-  if (threadIdx.x == 0) k.partials[blockIdx.x] = part[0];
-  if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
-  double tot[1];
-  reduce_partials<1, kBlock>(k.partials, gridDim.x, tot, sm);
-  if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+}
+
+// FP64 operator: stored FP64 weights, staged FP64 vector values
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
+  __shared__ double sm[kBlock / 32];
+  __shared__ int s_last;
+  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
+    double part[1] = {0.0};
+    if (active) {
+      load_tile(t, ts);
+      double* hs = reinterpret_cast<double*>(dsm);
+      const double* z = k.z64;
+      for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = z[halo_node(ts, s)];
+      __syncthreads();
+      const int* row = k.row;
+      const unsigned short* slot = k.slot16;
+      const double* w64 = k.w64;
+      const unsigned char* freem = k.freem;
+      double* p = k.p64;
+      double* q = k.q64;
+      const double beta = k.ds->beta;
+      const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+      for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+        const int a = a0 + seg;
+        const bool act = a < t.own_end && freem[a];
+        double acc = 0.0;
+        if (act)
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[slot[j]], acc);
+        acc = seg_reduce_d<W>(acc);
+        if (act && sub == 0) {
+          const double za = hs[own0 + (a - t.own_begin)];
+          const double s = k.dsum64[a] * za - acc;
+          const double qn = s + beta * q[a];
+          const double pn = za + beta * p[a];
+          q[a] = qn;
+          p[a] = pn;
+          part[0] += pn * qn;
+        }
+      }
+    }
+    write_partials<1>(v, item, part, sm);
+    if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+      double tot[1];
+      reduce_items<1>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+        v.ticket[t.inst] = 0;
+      }
+    }
+    __syncthreads();
   }
 }
 
 // e += alpha p, r -= alpha q, z = D^-1 r, partial r.z and r.r -> beta, stop test
 template <typename P>
-__global__ void __launch_bounds__(kBlock) k_cg_update(KParams k, cudaGraphConditionalHandle hc) {
+__global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphConditionalHandle hc) {
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
-  P* rin = VecSel<P>::rin(k);
-  P* z = VecSel<P>::z(k);
-  const P* p = VecSel<P>::p(k);
-  const P* q = VecSel<P>::q(k);
-  P* e = VecSel<P>::e(k);
-  const P* dinv = VecSel<P>::dinv(k);
-  const double alpha_d = k.ds->alpha;
-  const P alpha = (P)alpha_d;
-  double part[2] = {0.0, 0.0};
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
-    const P di = dinv[a];
-    if (di == P(0)) continue;
-    const P ee = e[a] + alpha * p[a];
-    const P r = rin[a] - alpha * q[a];
-    const P zz = r * di;
-    e[a] = ee;
-    rin[a] = r;
-    z[a] = zz;
-    part[0] += (double)r * (double)zz;
-    part[1] += (double)r * (double)r;
-  }
-  block_sum<2, kBlock>(part, sm);
-  if (threadIdx.x == 0) {
-    k.partials[0 * gridDim.x + blockIdx.x] = part[0];
-    k.partials[1 * gridDim.x + blockIdx.x] = part[1];
-  }
-  if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
-  double tot[2];
-  reduce_partials<2, kBlock>(k.partials, gridDim.x, tot, sm);
-  if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    ds->beta = ds->rz != 0.0 ? tot[0] / ds->rz : 0.0;
-    ds->rz = tot[0];
-    ds->rr = tot[1];
-    ds->inner_it += 1;
-    ds->solve_iters += 1;
-    ds->cg_iters += 1;
-    const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
-                    ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
-    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
+    double part[2] = {0.0, 0.0};
+    if (active) {
+      P* rin = VecSel<P>::rin(k);
+      P* z = VecSel<P>::z(k);
+      const P* p = VecSel<P>::p(k);
+      const P* q = VecSel<P>::q(k);
+      P* e = VecSel<P>::e(k);
+      const P* dinv = VecSel<P>::dinv(k);
+      const P alpha = (P)k.ds->alpha;
+      for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+        const P di = dinv[a];
+        if (di == P(0)) continue;
+        const P ee = e[a] + alpha * p[a];
+        const P r = rin[a] - alpha * q[a];
+        const P zz = r * di;
+        e[a] = ee;
+        rin[a] = r;
+        z[a] = zz;
+        part[0] += (double)r * (double)zz;
+        part[1] += (double)r * (double)r;
+      }
+    }
+    write_partials<2>(v, item, part, sm);
+    if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
+      double tot[2];
+      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->inner_active) {
+          const double alpha_d = ds->alpha;
+          ds->beta = ds->rz != 0.0 ? tot[0] / ds->rz : 0.0;
+          ds->rz = tot[0];
+          ds->rr = tot[1];
+          ds->inner_it += 1;
+          ds->solve_iters += 1;
+          ds->cg_iters += 1;
+          const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
+                          ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
+          ds->inner_active = go ? 1 : 0;
+        }
+        instance_finished(v, c.inst, 1, hc);
+      }
+    }
+    __syncthreads();
   }
 }
 
 // phi += e on the unknowns; FP64 residual r -= A e (FP64 weights); outer stop test.
 template <typename P, int W>
-__global__ void __launch_bounds__(kBlock) k_ir_update(KParams k, cudaGraphConditionalHandle hc) {
+__global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphConditionalHandle hc) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
-  const P* e = VecSel<P>::e(k);
   const bool mixed = sizeof(P) == 4;
-  int beg, end;
-  node_range(k.N, beg, end);
-  double part[1] = {0.0};
-  for (int a0 = beg; a0 < end; a0 += nseg) {
-    const int a = a0 + seg;
-    const bool act = a < end && k.freem[a];
-    double acc = 0.0;
-    if (act)
-      for (int j = k.row[a] + sub; j < k.row[a + 1]; j += W) acc += k.w64[j] * (double)e[k.col[j]];
-    acc = seg_reduce_d<W>(acc);
-    if (act && sub == 0) {
-      const double ea = (double)e[a];
-      const double r = k.r64[a] - (k.dsum64[a] * ea - acc);
-      k.r64[a] = r;
-      const double ph = k.phi64[a] + ea;
-      k.phi64[a] = ph;
-      set_phi_rec(k, a, ph, mixed);
-      part[0] += r * r;
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    const bool active = *((volatile int*)&k.ds->outer_active) != 0;
+    double part[1] = {0.0};
+    if (active) {
+      load_tile(t, ts);
+      double* hs = reinterpret_cast<double*>(dsm);
+      const P* e = VecSel<P>::e(k);
+      for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = (double)e[halo_node(ts, s)];
+      __syncthreads();
+      const int* row = k.row;
+      const unsigned short* slot = k.slot16;
+      const double* w64 = k.w64;
+      const unsigned char* freem = k.freem;
+      const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+      for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+        const int a = a0 + seg;
+        const bool act = a < t.own_end && freem[a];
+        double acc = 0.0;
+        if (act)
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[slot[j]], acc);
+        acc = seg_reduce_d<W>(acc);
+        if (act && sub == 0) {
+          const double ea = hs[own0 + (a - t.own_begin)];
+          const double r = k.r64[a] - (k.dsum64[a] * ea - acc);
+          k.r64[a] = r;
+          const double ph = k.phi64[a] + ea;
+          k.phi64[a] = ph;
+          set_phi_rec(k, a, ph, mixed);
+          part[0] += r * r;
+        }
+      }
     }
-  }
-  block_sum<1, kBlock>(part, sm);
-  if (threadIdx.x == 0) k.partials[blockIdx.x] = part[0];
-  if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
-  double tot[1];
-  reduce_partials<1, kBlock>(k.partials, gridDim.x, tot, sm);
-  if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    ds->rnorm2 = tot[0];
-    ds->outer_it += 1;
-    ds->outer_total += 1;
-    const bool conv = tot[0] <= ds->tol * ds->tol * ds->bnorm2;
-    const bool go = !conv && ds->outer_it < ds->max_outer && ds->solve_iters < ds->max_iter &&
-                    isfinite(tot[0]);
-    if (!go) {
-      ds->cg_solves += 1;
-      ds->last_relres = sqrt(tot[0] / ds->bnorm2);
-      if (!conv) ds->cg_nc += 1;
+    write_partials<1>(v, item, part, sm);
+    if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+      double tot[1];
+      reduce_items<1>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->outer_active) {
+          ds->rnorm2 = tot[0];
+          ds->outer_it += 1;
+          ds->outer_total += 1;
+          const bool conv = tot[0] <= ds->tol * ds->tol * ds->bnorm2;
+          const bool go = !conv && ds->outer_it < ds->max_outer && ds->solve_iters < ds->max_iter &&
+                          isfinite(tot[0]);
+          if (!go) {
+            ds->cg_solves += 1;
+            ds->last_relres = sqrt(tot[0] / ds->bnorm2);
+            if (!conv) ds->cg_nc += 1;
+          }
+          ds->outer_active = go ? 1 : 0;
+        }
+        instance_finished(v, t.inst, 0, hc);
+      }
     }
-    if (k.in_graph) cudaGraphSetConditional(hc, go ? 1u : 0u);
+    __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------- transport -----------
-__device__ __forceinline__ float sel4(const float4& v, int s) {
-  return s == 0 ? v.x : s == 1 ? v.y : s == 2 ? v.z : v.w;
-}
-
 __device__ __forceinline__ double dissolve_switch(double c0, double csat, double sw) {
   if (sw > 0.0) return 1.0 / (1.0 + exp(-(c0 - csat) / sw));
   return c0 > csat ? 1.0 : 0.0;
 }
 
-constexpr int kDiagSlots = 9;  // mass[4], solid, vol, dissolved, nonfinite, mg
+constexpr int kDiagSlots = 9;  // mass[4], solid, vol, dissolved, nonfinite, spare
 
-// Finishes a transport launch: block partials -> DevState (last block).
-__device__ __forceinline__ void transport_epilogue(const KParams& k, double (&part)[kDiagSlots],
-                                                   double* sm, int* s_last) {
-  block_sum<kDiagSlots, kBlock>(part, sm);
-  if (threadIdx.x == 0)
-    for (int v = 0; v < kDiagSlots; ++v) k.partials[v * gridDim.x + blockIdx.x] = part[v];
-  if (!take_last_ticket(&k.ds->ticket[0], s_last)) return;
+__device__ __forceinline__ void transport_finish(const EngineView& v, const TileDesc& t,
+                                                 const KParams& k, int item,
+                                                 double (&part)[kDiagSlots], double* sm,
+                                                 int* s_last) {
+  write_partials<kDiagSlots>(v, item, part, sm);
+  if (!item_done(&v.ticket[t.inst], v.tile_count[t.inst], s_last)) return;
   double tot[kDiagSlots];
-  reduce_partials<kDiagSlots, kBlock>(k.partials, gridDim.x, tot, sm);
+  reduce_items<kDiagSlots>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
   if (threadIdx.x == 0) {
     DevState* ds = k.ds;
-    ds->ticket[0] = 0;
-    const double dV = 1.0;  // multiplied on the host
-    (void)dV;
+    v.ticket[t.inst] = 0;
     for (int s = 0; s < S; ++s) ds->mass[s] = tot[s];
     ds->solid_count = (long long)tot[4];
     ds->steps += 1;
@@ -405,233 +645,297 @@ __device__ __forceinline__ void transport_epilogue(const KParams& k, double (&pa
   }
 }
 
-// Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
-// and change nothing; otherwise advance the state into rec32_nxt / clo.
-template <int W, bool RESID>
-__global__ void __launch_bounds__(kBlock) k_transport32(KParams k, double* F_out) {
-  __shared__ double sm[kDiagSlots * kBlock / 32];
-  __shared__ int s_last;
-  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
-  const double voln1rel = *k.voln1rel_ptr;
-  const double BV = pow(10., -k.vol_red * (1. - voln1rel));
-  float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    cLL[s] = (float)k.DL[s];
-    cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
-    cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
-    K1f[s] = (float)k.K1[s];
-    K2f[s] = (float)k.K2zF[s];
+// Warm start of the next solve: phi = 2 phi^n - phi^{n-1} on the unknowns (phi_prev keeps
+// phi^n); the returned value also goes into the next record so that both agree.
+__device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
+  const double ph = k.phi64[a];
+  if (!k.extrapolate || !k.freem[a]) {
+    k.phi_prev[a] = ph;
+    return ph;
   }
-  const float dtf = (float)k.dt;
-  const long long step_no = k.ds->steps + 1;
-  int beg, end;
-  node_range(k.N, beg, end);
-  double part[kDiagSlots];
-#pragma unroll
-  for (int v = 0; v < kDiagSlots; ++v) part[v] = 0.0;
-  for (int a0 = beg; a0 < end; a0 += nseg) {
-    const int a = a0 + seg;
-    const bool act = a < end;
-    Rec32 ra;
-    if (act) ra = k.rec32_cur[a];
-    const float pa = act ? ra.phase : 0.0f;
-    float a1[S], a2[S];
-#pragma unroll
-    for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
-    int iface = 0;
-    if (act) {
-      const int jb = k.row[a], je = k.row[a + 1];
-      for (int j = jb + sub; j < je; j += W) {
-        const int n = k.col[j];
-        const float w = k.w32[j];
-        const Rec32 rn = k.rec32_cur[n];
-        const float pn = rn.phase;
-        const float dphi = (rn.phi_hi - ra.phi_hi) + (rn.phi_lo - ra.phi_lo);
-        const bool ll = (pa == 0.0f) && (pn == 0.0f);
-        const bool ss = (pa != 0.0f) && (pn != 0.0f);
-        iface |= (pa != 0.0f && pn == 0.0f) ? 1 : 0;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const float coef = ll ? cLL[s] : (ss ? cSS[s] : cX[s]);
-          const float cw = coef * w;
-          a1[s] = fmaf(cw, rn.c[s] - ra.c[s], a1[s]);
-          a2[s] = fmaf(cw * rn.c[s], dphi, a2[s]);
-        }
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      a1[s] = comp_reduce<W>(a1[s]);
-      a2[s] = comp_reduce<W>(a2[s]);
-    }
-    iface = seg_or<W>(iface);
-    if (!act || sub != 0) continue;
-    const unsigned char dm = k.dirmask[a];
-    const float4 lo4 = k.clo[a];
-    const double c0old = (double)ra.c[0] + (double)lo4.x;
-    const bool src_on = iface && !(dm & 1);
-    const double sw = src_on ? dissolve_switch(c0old, k.csat, k.sw) : 0.0;
-    const float Rmg = src_on ? (float)(-k.k_diss * sw) : 0.0f;
-    if (RESID) {
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const double f = -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
-        F_out[(size_t)s * k.N + a] = f;
-      }
-      continue;
-    }
-    float hi[S], lo[S];
-    double v[S];
-    bool bad = false;
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
-      float t, e1, sh;
-      two_sum(sel4(lo4, s), inc, t, e1);
-      float e2;
-      two_sum(ra.c[s], t, sh, e2);
-      float sl = e1 + e2;
-      float h2 = sh + sl;  // renormalise
-      sl = sl - (h2 - sh);
-      double val = (double)h2 + (double)sl;
-      if ((dm >> s) & 1) val = k.bcval[(size_t)s * k.N + a];
-      if (val < k.c_floor) val = k.c_floor;
-      if (!isfinite(val)) bad = true;
-      const float vh = (float)val;
-      hi[s] = vh;
-      lo[s] = (float)(val - (double)vh);
-      v[s] = val;
-    }
-    float pnew = pa;
-    if (pa != 0.0f && v[0] <= k.csat) {
-      pnew = 0.0f;
-      k.flip_step[a] = (int)step_no;
-    }
-    Rec32 out;
-#pragma unroll
-    for (int s = 0; s < S; ++s) out.c[s] = hi[s];
-    out.phi_hi = ra.phi_hi;
-    out.phi_lo = ra.phi_lo;
-    out.phase = pnew;
-    out.pad = 0.0f;
-    k.rec32_nxt[a] = out;
-    k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
-#pragma unroll
-    for (int s = 0; s < S; ++s) part[s] += v[s];
-    if (pnew != 0.0f) {
-      part[4] += 1.0;
-      part[5] += v[0] - k.csat;
-    }
-    part[6] += k.k_diss * sw;
-    part[7] += bad ? 1.0 : 0.0;
-  }
-  if (RESID) return;
-  transport_epilogue(k, part, sm, &s_last);
+  const double g = 2.0 * ph - k.phi_prev[a];
+  k.phi_prev[a] = ph;
+  k.phi64[a] = g;
+  return g;
 }
 
-// FP64 transport, same structure.
+// Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
+// (single instance) and change nothing; otherwise advance the state into rec32_nxt / clo.
 template <int W, bool RESID>
-__global__ void __launch_bounds__(kBlock) k_transport64(KParams k, double* F_out) {
+__global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_out) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
   const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
-  const double voln1rel = *k.voln1rel_ptr;
-  const double BV = pow(10., -k.vol_red * (1. - voln1rel));
-  double cLL[S], cX[S], cSS[S];
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    load_tile(t, ts);
+    float4* hc = reinterpret_cast<float4*>(dsm);
+    float2* hp = reinterpret_cast<float2*>(hc + t.halo);
+    float* hph = reinterpret_cast<float*>(hp + t.halo);
+    const Rec32* rc = k.rec32_cur;
+    for (int s = threadIdx.x; s < t.halo; s += kBlock) {
+      const int n = halo_node(ts, s);
+      const float4* src = reinterpret_cast<const float4*>(rc + n);
+      const float4 a = src[0], b = src[1];
+      hc[s] = a;
+      hp[s] = make_float2(b.x, b.y);
+      hph[s] = b.z;
+    }
+    __syncthreads();
+    const double voln1rel = *k.voln1rel_ptr;
+    const double BV = pow(10., -k.vol_red * (1. - voln1rel));
+    float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
 #pragma unroll
-  for (int s = 0; s < S; ++s) {
-    cLL[s] = k.DL[s];
-    cX[s] = s == 0 ? k.DSo[0] * BV : k.DSo[s];
-    cSS[s] = s == 0 ? k.DSo[0] : 0.0;
-  }
-  const long long step_no = k.ds->steps + 1;
-  int beg, end;
-  node_range(k.N, beg, end);
-  double part[kDiagSlots];
+    for (int s = 0; s < S; ++s) {
+      cLL[s] = (float)k.DL[s];
+      cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
+      cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
+      K1f[s] = (float)k.K1[s];
+      K2f[s] = (float)k.K2zF[s];
+    }
+    const float dtf = (float)k.dt;
+    const long long step_no = k.ds->steps + 1;
+    const int* row = k.row;
+    const unsigned short* slot = k.slot16;
+    const float* w32 = k.w32;
+    const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+    double part[kDiagSlots];
 #pragma unroll
-  for (int v = 0; v < kDiagSlots; ++v) part[v] = 0.0;
-  for (int a0 = beg; a0 < end; a0 += nseg) {
-    const int a = a0 + seg;
-    const bool act = a < end;
-    Rec64 ra;
-    if (act) ra = k.rec64_cur[a];
-    const double pa = act ? ra.phase : 0.0;
-    double a1[S], a2[S];
+    for (int q = 0; q < kDiagSlots; ++q) part[q] = 0.0;
+    for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+      const int a = a0 + seg;
+      const bool act = a < t.own_end;
+      const int so = own0 + (a - t.own_begin);
+      float4 ca = make_float4(0.f, 0.f, 0.f, 0.f);
+      float2 pha = make_float2(0.f, 0.f);
+      float pa = 0.0f;
+      if (act) {
+        ca = hc[so];
+        pha = hp[so];
+        pa = hph[so];
+      }
+      float a1[S], a2[S];
 #pragma unroll
-    for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0;
-    int iface = 0;
-    if (act) {
-      const int jb = k.row[a], je = k.row[a + 1];
-      for (int j = jb + sub; j < je; j += W) {
-        const int n = k.col[j];
-        const double w = k.w64[j];
-        const Rec64 rn = k.rec64_cur[n];
-        const double pn = rn.phase;
-        const double dphi = rn.phi - ra.phi;
-        const bool ll = (pa == 0.0) && (pn == 0.0);
-        const bool ss = (pa != 0.0) && (pn != 0.0);
-        iface |= (pa != 0.0 && pn == 0.0) ? 1 : 0;
+      for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
+      int iface = 0;
+      if (act) {
+        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+          const int sl = slot[j];
+          const float w = w32[j];
+          const float4 cn = hc[sl];
+          const float2 pn2 = hp[sl];
+          const float pn = hph[sl];
+          const float dphi = (pn2.x - pha.x) + (pn2.y - pha.y);
+          const bool ll = (pa == 0.0f) && (pn == 0.0f);
+          const bool ss = (pa != 0.0f) && (pn != 0.0f);
+          iface |= (pa != 0.0f && pn == 0.0f) ? 1 : 0;
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const double coef = ll ? cLL[s] : (ss ? cSS[s] : cX[s]);
-          const double cw = coef * w;
-          a1[s] += cw * (rn.c[s] - ra.c[s]);
-          a2[s] += cw * rn.c[s] * dphi;
+          for (int s = 0; s < S; ++s) {
+            const float coef = ll ? cLL[s] : (ss ? cSS[s] : cX[s]);
+            const float cw = coef * w;
+            const float cns = sel4(cn, s);
+            a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
+            a2[s] = fmaf(cw * cns, dphi, a2[s]);
+          }
         }
       }
-    }
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      a1[s] = seg_reduce_d<W>(a1[s]);
-      a2[s] = seg_reduce_d<W>(a2[s]);
-    }
-    iface = seg_or<W>(iface);
-    if (!act || sub != 0) continue;
-    const unsigned char dm = k.dirmask[a];
-    const bool src_on = iface && !(dm & 1);
-    const double sw = src_on ? dissolve_switch(ra.c[0], k.csat, k.sw) : 0.0;
-    const double Rmg = src_on ? -k.k_diss * sw : 0.0;
-    if (RESID) {
+      for (int s = 0; s < S; ++s) {
+        a1[s] = comp_reduce<W>(a1[s]);
+        a2[s] = comp_reduce<W>(a2[s]);
+      }
+      iface = seg_or<W>(iface);
+      if (!act || sub != 0) continue;
+      const unsigned char dm = k.dirmask[a];
+      const float4 lo4 = k.clo[a];
+      const double c0old = (double)ca.x + (double)lo4.x;
+      const bool src_on = iface && !(dm & 1);
+      const double swv = src_on ? dissolve_switch(c0old, k.csat, k.sw) : 0.0;
+      const float Rmg = src_on ? (float)(-k.k_diss * swv) : 0.0f;
+      if (RESID) {
 #pragma unroll
-      for (int s = 0; s < S; ++s)
-        F_out[(size_t)s * k.N + a] = -k.K1[s] * a1[s] - k.K2zF[s] * a2[s] - (s == 0 ? Rmg : 0.0);
-      continue;
-    }
-    double v[S];
-    bool bad = false;
+        for (int s = 0; s < S; ++s)
+          F_out[(size_t)s * k.N + a] =
+              -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
+        continue;
+      }
+      float hi[S], lo[S];
+      double val[S];
+      bool bad = false;
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
-      const double F = -k.K1[s] * a1[s] - k.K2zF[s] * a2[s] - (s == 0 ? Rmg : 0.0);
-      double val = ra.c[s] - k.dt * F;
-      if ((dm >> s) & 1) val = k.bcval[(size_t)s * k.N + a];
-      if (val < k.c_floor) val = k.c_floor;
-      if (!isfinite(val)) bad = true;
-      v[s] = val;
-    }
-    double pnew = pa;
-    if (pa != 0.0 && v[0] <= k.csat) {
-      pnew = 0.0;
-      k.flip_step[a] = (int)step_no;
-    }
-    Rec64 out;
+      for (int s = 0; s < S; ++s) {
+        const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
+        float tt, e1, sh, e2;
+        two_sum(sel4(lo4, s), inc, tt, e1);
+        two_sum(sel4(ca, s), tt, sh, e2);
+        double x = (double)sh + (double)(e1 + e2);
+        if ((dm >> s) & 1) x = k.bcval[(size_t)s * k.N + a];
+        if (x < k.c_floor) x = k.c_floor;
+        if (!isfinite(x)) bad = true;
+        const float xh = (float)x;
+        hi[s] = xh;
+        lo[s] = (float)(x - (double)xh);
+        val[s] = x;
+      }
+      float pnew = pa;
+      if (pa != 0.0f && val[0] <= k.csat) {
+        pnew = 0.0f;
+        k.flip_step[a] = (int)step_no;
+      }
+      const double g = next_phi_guess(k, a);
+      Rec32 out;
 #pragma unroll
-    for (int s = 0; s < S; ++s) out.c[s] = v[s];
-    out.phi = ra.phi;
-    out.phase = pnew;
-    out.pad[0] = out.pad[1] = 0.0;
-    k.rec64_nxt[a] = out;
+      for (int s = 0; s < S; ++s) out.c[s] = hi[s];
+      out.phi_hi = (float)g;
+      out.phi_lo = (float)(g - (double)out.phi_hi);
+      out.phase = pnew;
+      out.pad = 0.0f;
+      k.rec32_nxt[a] = out;
+      k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
 #pragma unroll
-    for (int s = 0; s < S; ++s) part[s] += v[s];
-    if (pnew != 0.0) {
-      part[4] += 1.0;
-      part[5] += v[0] - k.csat;
+      for (int s = 0; s < S; ++s) part[s] += val[s];
+      if (pnew != 0.0f) {
+        part[4] += 1.0;
+        part[5] += val[0] - k.csat;
+      }
+      part[6] += k.k_diss * swv;
+      part[7] += bad ? 1.0 : 0.0;
     }
-    part[6] += k.k_diss * sw;
-    part[7] += bad ? 1.0 : 0.0;
+    if (!RESID) transport_finish(v, t, k, item, part, sm, &s_last);
+    __syncthreads();
   }
-  if (RESID) return;
-  transport_epilogue(k, part, sm, &s_last);
+}
+
+// FP64 transport, same structure (stored FP64 weights, FP64 records).
+template <int W, bool RESID>
+__global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_out) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
+  __shared__ double sm[kDiagSlots * kBlock / 32];
+  __shared__ int s_last;
+  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    load_tile(t, ts);
+    double* hrec = reinterpret_cast<double*>(dsm);  // 6 doubles per halo node (SoA)
+    const Rec64* rc = k.rec64_cur;
+    const int H = t.halo;
+    for (int s = threadIdx.x; s < H; s += kBlock) {
+      const Rec64 r = rc[halo_node(ts, s)];
+#pragma unroll
+      for (int q = 0; q < S; ++q) hrec[(size_t)q * H + s] = r.c[q];
+      hrec[(size_t)S * H + s] = r.phi;
+      hrec[(size_t)(S + 1) * H + s] = r.phase;
+    }
+    __syncthreads();
+    const double voln1rel = *k.voln1rel_ptr;
+    const double BV = pow(10., -k.vol_red * (1. - voln1rel));
+    double cLL[S], cX[S], cSS[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      cLL[s] = k.DL[s];
+      cX[s] = s == 0 ? k.DSo[0] * BV : k.DSo[s];
+      cSS[s] = s == 0 ? k.DSo[0] : 0.0;
+    }
+    const long long step_no = k.ds->steps + 1;
+    const int* row = k.row;
+    const unsigned short* slot = k.slot16;
+    const double* w64 = k.w64;
+    const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+    double part[kDiagSlots];
+#pragma unroll
+    for (int q = 0; q < kDiagSlots; ++q) part[q] = 0.0;
+    for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+      const int a = a0 + seg;
+      const bool act = a < t.own_end;
+      const int so = own0 + (a - t.own_begin);
+      double ca[S], pha = 0.0, pa = 0.0;
+#pragma unroll
+      for (int s = 0; s < S; ++s) ca[s] = act ? hrec[(size_t)s * H + so] : 0.0;
+      if (act) {
+        pha = hrec[(size_t)S * H + so];
+        pa = hrec[(size_t)(S + 1) * H + so];
+      }
+      double a1[S], a2[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0;
+      int iface = 0;
+      if (act) {
+        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+          const int sl = slot[j];
+          const double w = w64[j];
+          const double pn = hrec[(size_t)(S + 1) * H + sl];
+          const double dphi = hrec[(size_t)S * H + sl] - pha;
+          const bool ll = (pa == 0.0) && (pn == 0.0);
+          const bool ss = (pa != 0.0) && (pn != 0.0);
+          iface |= (pa != 0.0 && pn == 0.0) ? 1 : 0;
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            const double coef = ll ? cLL[s] : (ss ? cSS[s] : cX[s]);
+            const double cw = coef * w;
+            const double cns = hrec[(size_t)s * H + sl];
+            a1[s] += cw * (cns - ca[s]);
+            a2[s] += cw * cns * dphi;
+          }
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        a1[s] = seg_reduce_d<W>(a1[s]);
+        a2[s] = seg_reduce_d<W>(a2[s]);
+      }
+      iface = seg_or<W>(iface);
+      if (!act || sub != 0) continue;
+      const unsigned char dm = k.dirmask[a];
+      const bool src_on = iface && !(dm & 1);
+      const double swv = src_on ? dissolve_switch(ca[0], k.csat, k.sw) : 0.0;
+      const double Rmg = src_on ? -k.k_diss * swv : 0.0;
+      if (RESID) {
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+          F_out[(size_t)s * k.N + a] = -k.K1[s] * a1[s] - k.K2zF[s] * a2[s] - (s == 0 ? Rmg : 0.0);
+        continue;
+      }
+      double val[S];
+      bool bad = false;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const double F = -k.K1[s] * a1[s] - k.K2zF[s] * a2[s] - (s == 0 ? Rmg : 0.0);
+        double x = ca[s] - k.dt * F;
+        if ((dm >> s) & 1) x = k.bcval[(size_t)s * k.N + a];
+        if (x < k.c_floor) x = k.c_floor;
+        if (!isfinite(x)) bad = true;
+        val[s] = x;
+      }
+      double pnew = pa;
+      if (pa != 0.0 && val[0] <= k.csat) {
+        pnew = 0.0;
+        k.flip_step[a] = (int)step_no;
+      }
+      const double g = next_phi_guess(k, a);
+      Rec64 out;
+#pragma unroll
+      for (int s = 0; s < S; ++s) out.c[s] = val[s];
+      out.phi = g;
+      out.phase = pnew;
+      out.pad[0] = out.pad[1] = 0.0;
+      k.rec64_nxt[a] = out;
+#pragma unroll
+      for (int s = 0; s < S; ++s) part[s] += val[s];
+      if (pnew != 0.0) {
+        part[4] += 1.0;
+        part[5] += val[0] - k.csat;
+      }
+      part[6] += k.k_diss * swv;
+      part[7] += bad ? 1.0 : 0.0;
+    }
+    if (!RESID) transport_finish(v, t, k, item, part, sm, &s_last);
+    __syncthreads();
+  }
 }
 
 // ------------------------------------------------------------------- state transfer -----
@@ -642,7 +946,7 @@ __global__ void k_load_state(KParams k, const int* perm, const double* c_user, c
     const int u = perm[a];
     double c[S];
     for (int s = 0; s < S; ++s) c[s] = c_user[(size_t)s * N + u];
-    double phi = phi_user ? phi_user[u] : k.phi64[a];
+    double phi = phi_user ? phi_user[u] : k.phi_prev[a];
     if (dirichlet_phi && ((k.dirmask[a] >> S) & 1)) phi = k.bcval[(size_t)S * N + a];
     float ph;
     if (phase_user)
@@ -650,6 +954,7 @@ __global__ void k_load_state(KParams k, const int* perm, const double* c_user, c
     else
       ph = mixed ? k.rec32_cur[a].phase : (float)k.rec64_cur[a].phase;
     k.phi64[a] = phi;
+    k.phi_prev[a] = phi;
     if (mixed) {
       Rec32 r;
       float lo[S];
@@ -674,6 +979,8 @@ __global__ void k_load_state(KParams k, const int* perm, const double* c_user, c
   }
 }
 
+// The potential of the last solve is phi_prev (after a step phi64 holds the next warm
+// start; before any step both agree).
 __global__ void k_store_state(KParams k, const int* perm, double* c_user, double* phi_user,
                               int* phase_user, int mixed) {
   const int N = k.N;
@@ -691,14 +998,13 @@ __global__ void k_store_state(KParams k, const int* perm, double* c_user, double
         for (int s = 0; s < S; ++s) c_user[(size_t)s * N + u] = r.c[s];
       if (phase_user) phase_user[u] = r.phase != 0.0 ? 1 : 0;
     }
-    if (phi_user) phi_user[u] = k.phi64[a];
+    if (phi_user) phi_user[u] = k.phi_prev[a];
   }
 }
 
 // convert the current state between the two representations
 __global__ void k_convert(KParams k, int to_mixed) {
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
-    const double phi = k.phi64[a];
     if (to_mixed) {
       const Rec64 s64 = k.rec64_cur[a];
       Rec32 r;
@@ -707,8 +1013,8 @@ __global__ void k_convert(KParams k, int to_mixed) {
         r.c[s] = (float)s64.c[s];
         lo[s] = (float)(s64.c[s] - (double)r.c[s]);
       }
-      r.phi_hi = (float)phi;
-      r.phi_lo = (float)(phi - (double)r.phi_hi);
+      r.phi_hi = (float)s64.phi;
+      r.phi_lo = (float)(s64.phi - (double)r.phi_hi);
       r.phase = (float)s64.phase;
       r.pad = 0.0f;
       k.rec32_cur[a] = r;
@@ -718,7 +1024,7 @@ __global__ void k_convert(KParams k, int to_mixed) {
       const float4 lo = k.clo[a];
       Rec64 r;
       for (int s = 0; s < S; ++s) r.c[s] = (double)s32.c[s] + (double)sel4(lo, s);
-      r.phi = phi;
+      r.phi = (double)s32.phi_hi + (double)s32.phi_lo;
       r.phase = (double)s32.phase;
       r.pad[0] = r.pad[1] = 0.0;
       k.rec64_cur[a] = r;
@@ -727,7 +1033,7 @@ __global__ void k_convert(KParams k, int to_mixed) {
 }
 
 // initial diagnostics (main.cpp:472-480): solid count, vol0rel, masses
-__global__ void k_init_diag(KParams k, int mixed) {
+__global__ void k_init_diag(KParams k, int mixed, double* partials) {
   __shared__ double sm[7 * kBlock / 32];
   __shared__ int s_last;
   double part[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -752,10 +1058,10 @@ __global__ void k_init_diag(KParams k, int mixed) {
   }
   block_sum<7, kBlock>(part, sm);
   if (threadIdx.x == 0)
-    for (int v = 0; v < 7; ++v) k.partials[v * gridDim.x + blockIdx.x] = part[v];
+    for (int q = 0; q < 7; ++q) partials[q * gridDim.x + blockIdx.x] = part[q];
   if (!take_last_ticket(&k.ds->ticket[0], &s_last)) return;
   double tot[7];
-  reduce_partials<7, kBlock>(k.partials, gridDim.x, tot, sm);
+  reduce_partials<7, kBlock>(partials, gridDim.x, tot, sm);
   if (threadIdx.x == 0) {
     DevState* ds = k.ds;
     ds->ticket[0] = 0;
@@ -774,38 +1080,411 @@ nnpp_status dispatch_lanes(int lanes, F&& f) {
     case 4: return f(std::integral_constant<int, 4>());
     case 8: return f(std::integral_constant<int, 8>());
     case 16: return f(std::integral_constant<int, 16>());
-    case 32: return f(std::integral_constant<int, 32>());
-    default: return set_error(NNPP_ERR_INVALID, "lanes per node must be 4, 8, 16 or 32");
+    default: return set_error(NNPP_ERR_INVALID, "lanes per node must be 4, 8 or 16");
   }
 }
 
+size_t smem_prep(int H) { return (size_t)H * (sizeof(double) + 1) + 16; }
+size_t smem_spmv32(int H) { return (size_t)H * sizeof(float4); }
+size_t smem_vec64(int H) { return (size_t)H * sizeof(double); }
+size_t smem_tr32(int H) { return (size_t)H * (sizeof(float4) + sizeof(float2) + sizeof(float)); }
+size_t smem_tr64(int H) { return (size_t)H * 6 * sizeof(double); }
+
+template <typename K>
+nnpp_status allow_smem(K kern, size_t bytes) {
+  if (bytes > 48 * 1024)
+    NNPP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return NNPP_OK;
+}
+
+// ------------------------------------------------------------------- adjoint -------------
+// Transpose of one explicit step (FP64).  For node m, with lh = lambda^{n+1} masked to zero
+// on Dirichlet and clamped entries, a = dt K1 D w and b = dt K2 z F/(RT) D w:
+//   mu_k,m = lh_k,m + sum_i a (lh_k,i - lh_k,m) + sum_i lh_k,i b (phi_m - phi_i)
+//            [+ lh_0,m (-dt k S'(c_0,m)) on interface nodes]
+//   nu_m   = sum_k dt K2zF_k (c_k,m sum_i D w lh_k,i - lh_k,m sum_i D w c_k,i)   (d/dphi)
+// and the parameter sensitivities dL/dD_k = sum_m lh_k,m (transport increment)/D_k,
+// dL/dk = sum_m lh_0,m (-dt S(c_0,m)) over interface nodes.  The bond terms are the
+// off-diagonal weights of the reference's tangent (utils.h:955-963), applied transposed.
+struct AdjArgs {
+  const Rec64* snap;   // c^n, phi^n, phase^n
+  const Rec64* snap1;  // c^{n+1} (clamp mask)
+  const double* lam;   // lambda^{n+1}, S*N
+  double* mu;          // S*N
+  double* nu;          // N
+  double* acc;         // 5 accumulators (dL/dD_k, dL/dk)
+};
+
+__device__ __forceinline__ double pair_D(const KParams& k, int s, bool pm, bool pi) {
+  if (!pm && !pi) return k.DL[s];
+  if (s == 0) return k.DSo[0];  // BV = 1: the adjoint requires vol_red = 0
+  if (pm && pi) return 0.0;
+  return k.DSo[s];
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock) k_adj_transport(EngineView v, AdjArgs ad) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
+  __shared__ double sm[5 * kBlock / 32];
+  __shared__ int s_last;
+  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    load_tile(t, ts);
+    const int H = t.halo;
+    const int N = k.N;
+    double* hc = reinterpret_cast<double*>(dsm);  // c: S*H
+    double* hl = hc + (size_t)S * H;              // masked lambda: S*H
+    double* hphi = hl + (size_t)S * H;            // H
+    unsigned char* hph = reinterpret_cast<unsigned char*>(hphi + H);
+    for (int s = threadIdx.x; s < H; s += kBlock) {
+      const int n = halo_node(ts, s);
+      const Rec64 r = ad.snap[n];
+      const Rec64 r1 = ad.snap1[n];
+      const unsigned char dm = k.dirmask[n];
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        hc[(size_t)q * H + s] = r.c[q];
+        const bool zero = ((dm >> q) & 1) || r1.c[q] == k.c_floor;
+        hl[(size_t)q * H + s] = zero ? 0.0 : ad.lam[(size_t)q * N + n];
+      }
+      hphi[s] = r.phi;
+      hph[s] = r.phase != 0.0 ? 1 : 0;
+    }
+    __syncthreads();
+    const int* row = k.row;
+    const unsigned short* slot = k.slot16;
+    const double* w64 = k.w64;
+    const double dt = k.dt;
+    const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+    double part[5] = {0, 0, 0, 0, 0};
+    for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
+      const int a = a0 + seg;
+      const bool act = a < t.own_end;
+      const int so = own0 + (a - t.own_begin);
+      double cm[S], lm[S];
+      double phm = 0.0;
+      bool pm = false;
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        cm[q] = act ? hc[(size_t)q * H + so] : 0.0;
+        lm[q] = act ? hl[(size_t)q * H + so] : 0.0;
+      }
+      if (act) {
+        phm = hphi[so];
+        pm = hph[so] != 0;
+      }
+      double acc[S], a1[S], a2[S], sl[S], sc[S];
+#pragma unroll
+      for (int q = 0; q < S; ++q) acc[q] = a1[q] = a2[q] = sl[q] = sc[q] = 0.0;
+      int iface = 0;
+      if (act) {
+        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+          const int si = slot[j];
+          const double w = w64[j];
+          const bool pi = hph[si] != 0;
+          const double phi_i = hphi[si];
+          iface |= (pm && !pi) ? 1 : 0;
+#pragma unroll
+          for (int q = 0; q < S; ++q) {
+            const double Dw = pair_D(k, q, pm, pi) * w;
+            const double li = hl[(size_t)q * H + si];
+            const double ci = hc[(size_t)q * H + si];
+            acc[q] += dt * k.K1[q] * Dw * (li - lm[q]) + li * dt * k.K2zF[q] * Dw * (phm - phi_i);
+            a1[q] += Dw * (ci - cm[q]);
+            a2[q] += Dw * ci * (phi_i - phm);
+            sl[q] += Dw * li;
+            sc[q] += Dw * ci;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        acc[q] = seg_reduce_d<W>(acc[q]);
+        a1[q] = seg_reduce_d<W>(a1[q]);
+        a2[q] = seg_reduce_d<W>(a2[q]);
+        sl[q] = seg_reduce_d<W>(sl[q]);
+        sc[q] = seg_reduce_d<W>(sc[q]);
+      }
+      iface = seg_or<W>(iface);
+      if (!act || sub != 0) continue;
+      const bool src = iface && !(k.dirmask[a] & 1);
+      double nu = 0.0;
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        double m = lm[q] + acc[q];
+        if (q == 0 && src) {
+          const double sw = dissolve_switch(cm[0], k.csat, k.sw);
+          const double dsw = k.sw > 0.0 ? sw * (1.0 - sw) / k.sw : 0.0;
+          m += lm[0] * (-dt * k.k_diss * dsw);
+          part[4] += lm[0] * (-dt * sw);
+        }
+        ad.mu[(size_t)q * N + a] = m;
+        nu += dt * k.K2zF[q] * (cm[q] * sl[q] - lm[q] * sc[q]);
+        part[q] += lm[q] * dt * (k.K1[q] * a1[q] + k.K2zF[q] * a2[q]) / k.DL[q];
+      }
+      ad.nu[a] = nu;
+    }
+    write_partials<5>(v, item, part, sm);
+    if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+      double tot[5];
+      reduce_items<5>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        for (int q = 0; q < 5; ++q) ad.acc[q] += tot[q];
+        v.ticket[t.inst] = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// lambda^n = mu + (1/(K sigma)) F CSolid z_k psi on the unknowns, + the loss injection on
+// species 0 (d(mass loss)/dc_0 = -dV times dL/d(sample))
+__global__ void k_adj_combine(KParams k, const double* mu, double* lam, double inject) {
+  const int N = k.N;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
+    const double psi = k.freem[a] ? k.phi64[a] : 0.0;
+    for (int s = 0; s < S; ++s)
+      lam[(size_t)s * N + a] = mu[(size_t)s * N + a] + k.lam * k.z[s] * psi + (s == 0 ? inject : 0.0);
+  }
+}
+
+// snapshot c and phase of the current state (either representation)
+__global__ void k_snap_state(KParams k, Rec64* dst, int mixed) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    Rec64 r = dst[a];
+    if (mixed) {
+      const Rec32 s32 = k.rec32_cur[a];
+      const float4 lo = k.clo[a];
+      for (int s = 0; s < S; ++s) r.c[s] = (double)s32.c[s] + (double)sel4(lo, s);
+      r.phase = (double)s32.phase;
+    } else {
+      const Rec64 s64 = k.rec64_cur[a];
+      for (int s = 0; s < S; ++s) r.c[s] = s64.c[s];
+      r.phase = s64.phase;
+    }
+    dst[a] = r;
+  }
+}
+
+// phi^n (the last solve's potential) into a snapshot
+__global__ void k_snap_phi(KParams k, Rec64* dst) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x)
+    dst[a].phi = k.phi_prev[a];
+}
+
+// adjoint solve set-up: phase^n into the current records, warm start psi (0 on Dirichlet
+// and solid nodes)
+__global__ void k_adj_solve_setup(KParams k, const Rec64* snap, const double* psi_prev) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    const double ph = snap[a].phase;
+    k.rec32_cur[a].phase = (float)ph;
+    k.rec64_cur[a].phase = ph;
+    const bool zero = ph != 0.0 || ((k.dirmask[a] >> S) & 1);
+    const double x = zero ? 0.0 : psi_prev[a];
+    k.phi64[a] = x;
+    k.phi_prev[a] = x;
+    k.rec32_cur[a].phi_hi = (float)x;
+    k.rec32_cur[a].phi_lo = (float)(x - (double)(float)x);
+    k.rec64_cur[a].phi = x;
+  }
+}
+
+__global__ void k_sum_c0(KParams k, int mixed, double* out) {
+  __shared__ double sm[kBlock / 32];
+  double part[1] = {0.0};
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    if (mixed)
+      part[0] += (double)k.rec32_cur[a].c[0] + (double)k.clo[a].x;
+    else
+      part[0] += k.rec64_cur[a].c[0];
+  }
+  block_sum<1, kBlock>(part, sm);
+  if (threadIdx.x == 0) atomicAdd(out, part[0]);
+}
+
 }  // namespace
+
+nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec64* snap,
+                                 const Rec64* snap1, const double* lam, double* mu, double* nu,
+                                 double* acc, cudaStream_t st) {
+  AdjArgs ad{snap, snap1, lam, mu, nu, acc};
+  const size_t sh = (size_t)v.halo_max * (9 * sizeof(double) + 1) + 16;
+  if (sh > 227 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "adjoint: tile halo too large");
+  return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    NNPP_TRY(allow_smem(k_adj_transport<W>, sh));
+    k_adj_transport<W><<<e.grid, kBlock, sh, st>>>(v, ad);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
+
+nnpp_status launch_adj_combine(Handle& h, const double* mu, double* lam, double inject) {
+  KParams kp = make_kparams(h, h.cur);
+  k_adj_combine<<<h.grid, kBlock, 0, h.st>>>(kp, mu, lam, inject);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_snap_state(Handle& h, Rec64* dst) {
+  KParams kp = make_kparams(h, h.cur);
+  k_snap_state<<<h.grid, kBlock, 0, h.st>>>(kp, dst, h.state_prec == NNPP_MIXED ? 1 : 0);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_snap_phi(Handle& h, Rec64* dst) {
+  KParams kp = make_kparams(h, h.cur);
+  k_snap_phi<<<h.grid, kBlock, 0, h.st>>>(kp, dst);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev) {
+  KParams kp = make_kparams(h, h.cur);
+  k_adj_solve_setup<<<h.grid, kBlock, 0, h.st>>>(kp, snap, psi_prev);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_sum_c0(Handle& h, double* out) {
+  KParams kp = make_kparams(h, h.cur);
+  NNPP_CUDA(cudaMemsetAsync(out, 0, sizeof(double), h.st));
+  k_sum_c0<<<h.grid, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0, out);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+nnpp_status prepare_kernels(int H, int lanes) {
+  if (smem_tr64(H) > 200 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
+  return dispatch_lanes(lanes, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H)));
+    NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H)));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W>, smem_spmv32(H)));
+    NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H)));
+    NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H)));
+    NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H)));
+    NNPP_TRY(allow_smem(k_transport32<W, false>, smem_tr32(H)));
+    NNPP_TRY(allow_smem(k_transport32<W, true>, smem_tr32(H)));
+    NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H)));
+    NNPP_TRY(allow_smem(k_transport64<W, true>, smem_tr64(H)));
+    return NNPP_OK;
+  });
+}
+
+nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                          cudaGraphConditionalHandle hc, double* F11_out) {
+  return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    const size_t sh = smem_prep(v.halo_max);
+    if (prec == NNPP_MIXED)
+      k_prep<float, W><<<e.grid, kBlock, sh, st>>>(v, hc, F11_out);
+    else
+      k_prep<double, W><<<e.grid, kBlock, sh, st>>>(v, hc, F11_out);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
+
+nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                             cudaGraphConditionalHandle hc) {
+  if (prec == NNPP_MIXED)
+    k_cg_init<float><<<e.grid, kBlock, 0, st>>>(v, hc, 0);
+  else
+    k_cg_init<double><<<e.grid, kBlock, 0, st>>>(v, hc, 1);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
+  return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    if (prec == NNPP_MIXED)
+      k_cg_spmv32<W><<<e.grid, kBlock, smem_spmv32(v.halo_max), st>>>(v);
+    else
+      k_cg_spmv64<W><<<e.grid, kBlock, smem_vec64(v.halo_max), st>>>(v);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
+
+nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               cudaGraphConditionalHandle hc) {
+  if (prec == NNPP_MIXED)
+    k_cg_update<float><<<e.grid, kBlock, 0, st>>>(v, hc);
+  else
+    k_cg_update<double><<<e.grid, kBlock, 0, st>>>(v, hc);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               cudaGraphConditionalHandle hc) {
+  return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    const size_t sh = smem_vec64(v.halo_max);
+    if (prec == NNPP_MIXED)
+      k_ir_update<float, W><<<e.grid, kBlock, sh, st>>>(v, hc);
+    else
+      k_ir_update<double, W><<<e.grid, kBlock, sh, st>>>(v, hc);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
+
+nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
+                               double* F_out) {
+  return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
+    constexpr int W = decltype(wc)::value;
+    if (prec == NNPP_MIXED) {
+      const size_t sh = smem_tr32(v.halo_max);
+      if (F_out)
+        k_transport32<W, true><<<e.grid, kBlock, sh, st>>>(v, F_out);
+      else
+        k_transport32<W, false><<<e.grid, kBlock, sh, st>>>(v, nullptr);
+    } else {
+      const size_t sh = smem_tr64(v.halo_max);
+      if (F_out)
+        k_transport64<W, true><<<e.grid, kBlock, sh, st>>>(v, F_out);
+      else
+        k_transport64<W, false><<<e.grid, kBlock, sh, st>>>(v, nullptr);
+    }
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  });
+}
 
 // ---------------------------------------------------------------------------------------
 nnpp_status step_alloc(Handle& h) {
   const size_t N = (size_t)h.N;
   bool ok = h.dirmask.alloc(N) && h.bcval.alloc((S + 1) * N) && h.rec32[0].alloc(N) &&
             h.rec32[1].alloc(N) && h.clo.alloc(N) && h.rec64[0].alloc(N) && h.rec64[1].alloc(N) &&
-            h.phi64.alloc(N) && h.flip_step.alloc(N) && h.b64.alloc(N) && h.r64.alloc(N) &&
-            h.dsum64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) && h.z64.alloc(N) &&
-            h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
+            h.phi64.alloc(N) && h.phi_prev.alloc(N) && h.flip_step.alloc(N) && h.b64.alloc(N) &&
+            h.r64.alloc(N) && h.dsum64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
+            h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
             h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N) && h.p32.alloc(N) &&
-            h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) &&
-            h.partials.alloc((size_t)kReduceSlots * kMaxPartialBlocks) && h.dstate.alloc(1) &&
-            h.scratch_d.alloc(16) && h.user_stage.alloc((S + 1) * N) && h.user_stage_i.alloc(N);
+            h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.dstate.alloc(1) &&
+            h.scratch_d.alloc(16 + 7 * 4096) && h.user_stage.alloc((S + 1) * N) &&
+            h.user_stage_i.alloc(N);
   if (!ok) return set_error(NNPP_ERR_NOMEM, "device state allocation");
   NNPP_CUDA(cudaMemsetAsync(h.freem.get(), 0, N, h.st));
   NNPP_CUDA(cudaMemsetAsync(h.rec32[1].get(), 0, N * sizeof(Rec32), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.rec64[1].get(), 0, N * sizeof(Rec64), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.e32.get(), 0, N * sizeof(float), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.e64.get(), 0, N * sizeof(double), h.st));
+  NNPP_CUDA(cudaMemsetAsync(h.z32.get(), 0, N * sizeof(float), h.st));
+  NNPP_CUDA(cudaMemsetAsync(h.z64.get(), 0, N * sizeof(double), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, N * sizeof(int), h.st));
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h.device);
   if (sms <= 0) sms = 152;
-  long long want = ((long long)h.N + 63) / 64;
-  long long g = std::min<long long>(want, (long long)sms * 8);
-  if (g > kMaxPartialBlocks) g = kMaxPartialBlocks;
+  long long g = std::min<long long>(((long long)h.N + 255) / 256, (long long)sms * 8);
+  if (g > 4096) g = 4096;
   if (g < 1) g = 1;
   h.grid = (int)g;
   return NNPP_OK;
@@ -813,11 +1492,13 @@ nnpp_status step_alloc(Handle& h) {
 
 KParams make_kparams(Handle& h, int cur) {
   KParams k;
+  std::memset(&k, 0, sizeof(k));
   const nnpp_params& p = h.p;
   k.N = h.N;
-  k.grid = h.grid;
   k.row = h.lay.row.get();
   k.col = h.lay.col.get();
+  k.slot16 = h.slot16.get();
+  k.posrec = h.posrec.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
   k.dirmask = h.dirmask.get();
@@ -828,6 +1509,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.rec64_cur = h.rec64[cur].get();
   k.rec64_nxt = h.rec64[cur ^ 1].get();
   k.phi64 = h.phi64.get();
+  k.phi_prev = h.phi_prev.get();
   k.flip_step = h.flip_step.get();
   k.b64 = h.b64.get();
   k.r64 = h.r64.get();
@@ -846,9 +1528,9 @@ KParams make_kparams(Handle& h, int cur) {
   k.p64 = h.p64.get();
   k.q64 = h.q64.get();
   k.e64 = h.e64.get();
-  k.partials = h.partials.get();
   k.ds = h.dstate.get();
   k.voln1rel_ptr = &h.dstate.get()->voln1rel;
+  k.b_override = h.b_override;
   k.dt = p.dt;
   k.csat = p.CSat / p.CSolid;
   k.c_floor = p.c_floor;
@@ -863,103 +1545,22 @@ KParams make_kparams(Handle& h, int cur) {
     k.DSo[s] = p.D_solid[s];
     k.z[s] = p.z[s];
   }
+  k.h32 = h.h32;
+  k.delta_lo = (float)(p.delta - p.dx / 2.0);
+  k.delta_hi = (float)(p.delta + p.dx / 2.0);
+  k.inv_dx = (float)(1.0 / p.dx);
+  k.dVf = (float)(p.dx * p.dy * p.dz);
   k.sub_step_no = p.sub_step_no;
   k.dissolve_count = 1;
-  k.in_graph = 1;
+  k.extrapolate = h.extrapolate;
   return k;
-}
-
-nnpp_status launch_prep(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                        cudaGraphConditionalHandle hc, double* F11_out) {
-  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
-    constexpr int W = decltype(wc)::value;
-    if (prec == NNPP_MIXED)
-      k_prep<float, W><<<kp.grid, kBlock, 0, st>>>(kp, hc, F11_out);
-    else
-      k_prep<double, W><<<kp.grid, kBlock, 0, st>>>(kp, hc, F11_out);
-    NNPP_CUDA(cudaGetLastError());
-    return NNPP_OK;
-  });
-}
-
-nnpp_status launch_cg_init(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                           cudaGraphConditionalHandle hc) {
-  (void)h;
-  if (prec == NNPP_MIXED)
-    k_cg_init<float><<<kp.grid, kBlock, 0, st>>>(kp, hc, 0);
-  else
-    k_cg_init<double><<<kp.grid, kBlock, 0, st>>>(kp, hc, 1);
-  NNPP_CUDA(cudaGetLastError());
-  return NNPP_OK;
-}
-
-nnpp_status launch_cg_iter(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                           cudaGraphConditionalHandle hc) {
-  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
-    constexpr int W = decltype(wc)::value;
-    if (prec == NNPP_MIXED) {
-      k_cg_spmv<float, W><<<kp.grid, kBlock, 0, st>>>(kp);
-      k_cg_update<float><<<kp.grid, kBlock, 0, st>>>(kp, hc);
-    } else {
-      k_cg_spmv<double, W><<<kp.grid, kBlock, 0, st>>>(kp);
-      k_cg_update<double><<<kp.grid, kBlock, 0, st>>>(kp, hc);
-    }
-    NNPP_CUDA(cudaGetLastError());
-    return NNPP_OK;
-  });
-}
-
-nnpp_status launch_cg_spmv(Handle& h, const KParams& kp, int prec, cudaStream_t st) {
-  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
-    constexpr int W = decltype(wc)::value;
-    if (prec == NNPP_MIXED)
-      k_cg_spmv<float, W><<<kp.grid, kBlock, 0, st>>>(kp);
-    else
-      k_cg_spmv<double, W><<<kp.grid, kBlock, 0, st>>>(kp);
-    NNPP_CUDA(cudaGetLastError());
-    return NNPP_OK;
-  });
-}
-
-nnpp_status launch_ir_update(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                             cudaGraphConditionalHandle hc) {
-  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
-    constexpr int W = decltype(wc)::value;
-    if (prec == NNPP_MIXED)
-      k_ir_update<float, W><<<kp.grid, kBlock, 0, st>>>(kp, hc);
-    else
-      k_ir_update<double, W><<<kp.grid, kBlock, 0, st>>>(kp, hc);
-    NNPP_CUDA(cudaGetLastError());
-    return NNPP_OK;
-  });
-}
-
-nnpp_status launch_transport(Handle& h, const KParams& kp, int prec, cudaStream_t st,
-                             double* F_out) {
-  return dispatch_lanes(h.lanes, [&](auto wc) -> nnpp_status {
-    constexpr int W = decltype(wc)::value;
-    if (prec == NNPP_MIXED) {
-      if (F_out)
-        k_transport32<W, true><<<kp.grid, kBlock, 0, st>>>(kp, F_out);
-      else
-        k_transport32<W, false><<<kp.grid, kBlock, 0, st>>>(kp, nullptr);
-    } else {
-      if (F_out)
-        k_transport64<W, true><<<kp.grid, kBlock, 0, st>>>(kp, F_out);
-      else
-        k_transport64<W, false><<<kp.grid, kBlock, 0, st>>>(kp, nullptr);
-    }
-    NNPP_CUDA(cudaGetLastError());
-    return NNPP_OK;
-  });
 }
 
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
                        const int* d_phase_user, int prec, bool dirichlet_phi) {
   KParams kp = make_kparams(h, h.cur);
-  k_load_state<<<kp.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user,
-                                             d_phase_user, prec == NNPP_MIXED ? 1 : 0,
-                                             dirichlet_phi ? 1 : 0);
+  k_load_state<<<h.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user, d_phase_user,
+                                            prec == NNPP_MIXED ? 1 : 0, dirichlet_phi ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = prec;
   return NNPP_OK;
@@ -967,8 +1568,8 @@ nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_us
 
 nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_phase_user) {
   KParams kp = make_kparams(h, h.cur);
-  k_store_state<<<kp.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user,
-                                              d_phase_user, h.state_prec == NNPP_MIXED ? 1 : 0);
+  k_store_state<<<h.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user, d_phase_user,
+                                             h.state_prec == NNPP_MIXED ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
@@ -976,7 +1577,7 @@ nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_
 nnpp_status convert_state(Handle& h, int to_prec) {
   if (h.state_prec == to_prec) return NNPP_OK;
   KParams kp = make_kparams(h, h.cur);
-  k_convert<<<kp.grid, kBlock, 0, h.st>>>(kp, to_prec == NNPP_MIXED ? 1 : 0);
+  k_convert<<<h.grid, kBlock, 0, h.st>>>(kp, to_prec == NNPP_MIXED ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = to_prec;
   return NNPP_OK;
@@ -984,7 +1585,8 @@ nnpp_status convert_state(Handle& h, int to_prec) {
 
 nnpp_status init_diag(Handle& h) {
   KParams kp = make_kparams(h, h.cur);
-  k_init_diag<<<kp.grid, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0);
+  k_init_diag<<<h.grid, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0,
+                                           h.scratch_d.get() + 16);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }

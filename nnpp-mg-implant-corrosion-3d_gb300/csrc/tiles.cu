@@ -1,0 +1,154 @@
+// tiles.cu -- tile work items of one instance, 16-bit halo slots of every bond and FP32
+// position records.
+//
+// A tile is T consecutive bins along x (bins of side >= the horizon radius, x-fastest
+// order, so the tile's own nodes and each of its 3x3 halo rows are contiguous node
+// ranges).  A kernel stages a tile's halo into shared memory and reaches a neighbour through
+// its slot: the neighbour's position in the concatenation of the halo rows.
+#include <algorithm>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace nnpp {
+
+namespace {
+
+struct Grid3 {
+  int nb[3];
+  int T;
+};
+
+// halo rows r = (dy+1) + 3 (dz+1) of tile (tx, by, bz): node ranges [hb, hb+hl)
+__host__ __device__ inline void tile_rows(const int* bin_start, Grid3 g, int tx, int by, int bz,
+                                          int* hb, int* hl) {
+  const int lo = max(tx * g.T - 1, 0);
+  const int hi = min(tx * g.T + g.T, g.nb[0] - 1);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int r = (dy + 1) + 3 * (dz + 1);
+      const int yy = by + dy, zz = bz + dz;
+      if (yy < 0 || yy >= g.nb[1] || zz < 0 || zz >= g.nb[2]) {
+        hb[r] = 0;
+        hl[r] = 0;
+        continue;
+      }
+      const int b0 = lo + g.nb[0] * (yy + g.nb[1] * zz);
+      const int b1 = hi + g.nb[0] * (yy + g.nb[1] * zz);
+      hb[r] = bin_start[b0];
+      hl[r] = bin_start[b1 + 1] - bin_start[b0];
+    }
+}
+
+__global__ void k_posrec(int n, const double* pos, double ox, double oy, double oz, double hb,
+                         int nbx, int nby, int nbz, float4* rec) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const double x = pos[a], y = pos[n + a], z = pos[2 * n + a];
+    int bx = (int)((x - ox) / hb), by = (int)((y - oy) / hb), bz = (int)((z - oz) / hb);
+    bx = min(max(bx, 0), nbx - 1);
+    by = min(max(by, 0), nby - 1);
+    bz = min(max(bz, 0), nbz - 1);
+    float4 r;
+    r.x = (float)(x - (ox + (double)bx * hb));
+    r.y = (float)(y - (oy + (double)by * hb));
+    r.z = (float)(z - (oz + (double)bz * hb));
+    r.w = __int_as_float(bx | (by << 10) | (bz << 20));
+    rec[a] = r;
+  }
+}
+
+// warp per node: slot of every neighbour within the halo of the node's tile
+__global__ void k_slots(int n, const int* row, const int* col, const float4* posrec,
+                        const int* bin_start, Grid3 g, unsigned short* slot, int* err) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < n; a += warps) {
+    const int pb = __float_as_int(posrec[a].w);
+    const int bx = pb & 1023, by = (pb >> 10) & 1023, bz = (pb >> 20) & 1023;
+    int hb[9], hl[9], off[9];
+    tile_rows(bin_start, g, bx / g.T, by, bz, hb, hl);
+    int acc = 0;
+    for (int r = 0; r < 9; ++r) {
+      off[r] = acc;
+      acc += hl[r];
+    }
+    for (int j = row[a] + lane; j < row[a + 1]; j += 32) {
+      const int nn = col[j];
+      const int q = __float_as_int(posrec[nn].w);
+      const int dy = ((q >> 10) & 1023) - by, dz = ((q >> 20) & 1023) - bz;
+      int s = -1;
+      if (dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1) {
+        const int r = (dy + 1) + 3 * (dz + 1);
+        if (nn >= hb[r] && nn < hb[r] + hl[r]) s = off[r] + (nn - hb[r]);
+      }
+      if (s < 0 || s > 65535) {
+        atomicExch(err, 1);
+        s = 0;
+      }
+      slot[j] = (unsigned short)s;
+    }
+  }
+}
+
+}  // namespace
+
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max) {
+  const Layout& L = h.lay;
+  const int N = h.N;
+  if (L.nb[0] > 1024 || L.nb[1] > 1024 || L.nb[2] > 1024)
+    return set_error(NNPP_ERR_UNSUPPORTED, "tiles: more than 1024 bins per axis");
+  Grid3 g;
+  g.nb[0] = L.nb[0];
+  g.nb[1] = L.nb[1];
+  g.nb[2] = L.nb[2];
+  g.T = T;
+  const double hb = (double)h.h32;
+  if (!h.posrec.alloc(N) || !h.slot16.alloc(L.nnz > 0 ? (size_t)L.nnz : 1))
+    return set_error(NNPP_ERR_NOMEM, "tile arrays");
+  const int blocks = std::max(1, std::min((N + 255) / 256, 152 * 16));
+  k_posrec<<<blocks, 256, 0, h.st>>>(N, L.pos.get(), h.ref.bbox[0], h.ref.bbox[2], h.ref.bbox[4], hb,
+                                     g.nb[0], g.nb[1], g.nb[2], h.posrec.get());
+  DBuf<int> err;
+  if (!err.alloc(1)) return set_error(NNPP_ERR_NOMEM, "tile flag");
+  NNPP_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(int), h.st));
+  const int wblocks = std::max(1, std::min((int)(((long long)N * 32 + 255) / 256), 152 * 64));
+  k_slots<<<wblocks, 256, 0, h.st>>>(N, L.row.get(), L.col.get(), h.posrec.get(), L.bin_start.get(), g,
+                                     h.slot16.get(), err.get());
+  NNPP_CUDA(cudaGetLastError());
+  std::vector<int> bs(L.nbins + 1);
+  int herr = 0;
+  NNPP_CUDA(cudaMemcpyAsync(bs.data(), L.bin_start.get(), sizeof(int) * (L.nbins + 1), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  if (herr) return set_error(NNPP_ERR_INVALID, "tiles: a neighbour outside its tile's halo");
+  const int ntx = (g.nb[0] + T - 1) / T;
+  int hm = 0;
+  for (int bz = 0; bz < g.nb[2]; ++bz)
+    for (int by = 0; by < g.nb[1]; ++by)
+      for (int tx = 0; tx < ntx; ++tx) {
+        const int bx0 = tx * T, bx1 = std::min(tx * T + T, g.nb[0]) - 1;
+        const int o0 = bs[bx0 + g.nb[0] * (by + g.nb[1] * bz)];
+        const int o1 = bs[bx1 + g.nb[0] * (by + g.nb[1] * bz) + 1];
+        if (o1 <= o0) continue;
+        TileDesc t;
+        t.inst = inst;
+        t.own_begin = o0;
+        t.own_end = o1;
+        tile_rows(bs.data(), g, tx, by, bz, t.hb, t.hl);
+        int tot = 0;
+        for (int r = 0; r < 9; ++r) tot += t.hl[r];
+        if (tot > 65536) return set_error(NNPP_ERR_UNSUPPORTED, "tiles: halo larger than 65536 nodes");
+        t.halo = tot;
+        t.cb[0] = bx0 + T / 2;
+        t.cb[1] = by;
+        t.cb[2] = bz;
+        t.pad = 0;
+        hm = std::max(hm, tot);
+        tiles.push_back(t);
+      }
+  *halo_max = hm;
+  h.tiles_T = T;
+  return NNPP_OK;
+}
+
+}  // namespace nnpp

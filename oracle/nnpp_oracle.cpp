@@ -501,6 +501,134 @@ int step(Oracle& o, StepRecord* rec) {
   return st;
 }
 
+// ---------------------------------------------------------------- adjoint ----------------
+// Forward with every step recorded (small cases), then the exact adjoint of the explicit
+// step: the transposed bond sums (the weights of the reference's tangent, utils.h:955-963),
+// the adjoint potential solve (K11 is symmetric on the unknowns) and the smoothed
+// dissolution switch.  Phase flips, interface flags and the unknown set are piecewise
+// constant in the parameters; clamped and Dirichlet values have zero derivative.
+struct Record {
+  std::vector<std::vector<double> > c, phi;            // c^n (S*N), phi^n (N)
+  std::vector<std::vector<int> > phase;                // phase^n
+  std::vector<std::vector<unsigned char> > clamped;    // clamp of c^{n+1}
+  std::vector<double> c0;                              // c_0 at t = 0
+  int steps = 0, sample_every = 0;
+};
+
+Record g_rec;
+
+// A psi = nu on the unknowns of `phase` (Dirichlet and frozen values 0), FP64 CG.
+void adjoint_solve(Oracle& o, const int* phase, const std::vector<double>& nu, std::vector<double>& psi) {
+  const int N = o.N;
+  build_operator(o, phase);
+  std::vector<double> b(N, 0.0);
+  for (int i = 0; i < N; ++i) b[i] = o.freev[i] ? nu[i] : 0.0;
+  double bn = std::sqrt(dot(b, b));
+  psi.assign(N, 0.0);
+  if (bn == 0.0) return;
+  std::vector<double> r(b), z(N), p(N), q(N);
+  for (int i = 0; i < N; ++i) z[i] = o.freev[i] ? r[i] / o.diag[i] : 0.0;
+  p = z;
+  double rz = dot(r, z);
+  for (int it = 0; it < o.max_iter; ++it) {
+    apply_A(o, p, q);
+    const double pq = dot(p, q);
+    if (pq <= 0.0) break;
+    const double alpha = rz / pq;
+    for (int i = 0; i < N; ++i) {
+      psi[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+    }
+    if (std::sqrt(dot(r, r)) <= 0.1 * o.tol * bn) break;
+    for (int i = 0; i < N; ++i) z[i] = o.freev[i] ? r[i] / o.diag[i] : 0.0;
+    const double rz2 = dot(r, z);
+    const double bt = rz2 / rz;
+    rz = rz2;
+    for (int i = 0; i < N; ++i) p[i] = z[i] + bt * p[i];
+  }
+}
+
+// bond weight beta dV / xi^(3+2s)
+inline double bond_w(const Oracle& o, int i, int n) {
+  const nnpp_params& p = o.p;
+  const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+  const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+  return beta_fn(xi, p.delta, p.dx) * p.dx * p.dy * p.dz / std::pow(xi, 3.0 + 2.0 * p.s_phi);
+}
+
+// D of species k on a bond between phases pi, pn (with BV = 10^(-vol_red (1 - voln1rel)))
+inline double pair_D(const nnpp_params& p, int k, int pi, int pn, double BVmix) {
+  if (pi == 0 && pn == 0) return p.D_liquid[k];
+  if (k == 0) return (pi == 1 && pn == 1) ? p.D_solid[0] : p.D_solid[0] * BVmix;
+  if (pi == 1 && pn == 1) return 0.0;
+  return p.D_solid[k];
+}
+
+void adjoint_step(Oracle& o, int n, std::vector<double>& lam, double* gD, double* gk) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  const std::vector<double>& c = g_rec.c[n];
+  const std::vector<double>& phi = g_rec.phi[n];
+  const std::vector<int>& ph = g_rec.phase[n];
+  const std::vector<unsigned char>& cl = g_rec.clamped[n];
+  const double BV = std::pow(10., -p.vol_red * (1. - 0.0));
+  const double csat = p.CSat / p.CSolid;
+  std::vector<double> lh((int64_t)S * N);
+  for (int k = 0; k < S; ++k)
+    for (int i = 0; i < N; ++i) {
+      const int64_t a = (int64_t)k * N + i;
+      lh[a] = (o.dir[a] || cl[a]) ? 0.0 : lam[a];
+    }
+  std::vector<double> mu((int64_t)S * N, 0.0), nu(N, 0.0);
+  double gDl[S] = {0, 0, 0, 0}, gkl = 0.0;
+  for (int m = 0; m < N; ++m) {
+    int iface = 0;
+    if (ph[m] == 1)
+      for (int64_t j = o.row_ptr[m] + 1; j < o.row_ptr[m + 1]; ++j)
+        if (ph[o.cols[j]] == 0) {
+          iface = 1;
+          break;
+        }
+    double nul = 0.0;
+    for (int k = 0; k < S; ++k) {
+      const double* ck = c.data() + (int64_t)k * N;
+      const double* lk = lh.data() + (int64_t)k * N;
+      const double K2zF = p.K2[k] * p.z[k] * p.F / (p.R * p.T);
+      double acc = lk[m], a1 = 0.0, a2 = 0.0, sl = 0.0, sc = 0.0;
+      for (int64_t j = o.row_ptr[m] + 1; j < o.row_ptr[m + 1]; ++j) {
+        const int i = o.cols[j];
+        const double D = pair_D(p, k, ph[m], ph[i], BV);
+        if (D == 0.0) continue;
+        const double w = bond_w(o, m, i);
+        acc += p.dt * p.K1[k] * D * w * (lk[i] - lk[m]);
+        acc += lk[i] * p.dt * K2zF * D * w * (phi[m] - phi[i]);
+        a1 += D * w * (ck[i] - ck[m]);
+        a2 += D * w * ck[i] * (phi[i] - phi[m]);
+        sl += D * w * lk[i];
+        sc += D * w * ck[i];
+      }
+      const bool src = (k == 0) && iface && !o.dir[m];
+      if (src) {
+        acc += lk[m] * (-p.dt * p.k_diss * mg_source_switch_deriv(p, ck[m]));
+        gkl += lk[m] * (-p.dt * mg_source_switch(p, ck[m]));
+      }
+      mu[(int64_t)k * N + m] = acc;
+      nul += p.dt * K2zF * (ck[m] * sl - lk[m] * sc);
+      gDl[k] += lk[m] * p.dt * (p.K1[k] * a1 + K2zF * a2) / p.D_liquid[k];
+    }
+    nu[m] = nul;
+  }
+  std::vector<double> psi;
+  adjoint_solve(o, ph.data(), nu, psi);
+  const double lamp = (1. / (p.K_phi * p.sigma)) * p.F * p.CSolid;
+  for (int k = 0; k < S; ++k)
+    for (int i = 0; i < N; ++i)
+      if (o.freev[i]) mu[(int64_t)k * N + i] += lamp * p.z[k] * psi[i];
+  lam.swap(mu);
+  for (int k = 0; k < S; ++k) gD[k] += gDl[k];
+  *gk += gkl;
+}
+
 double mg_mass_lost(const Oracle& o) {
   double m = 0.0;
   for (int i = 0; i < o.N; ++i) m += o.c0_init[i] - o.c[i];
@@ -648,6 +776,56 @@ int orc_set_state(void* h, const double* c, const double* phi, const int* phase)
   if (c) o->c.assign(c, c + (int64_t)S * o->N);
   if (phi) o->phi.assign(phi, phi + o->N);
   if (phase) o->phase.assign(phase, phase + o->N);
+  return 0;
+}
+
+// Forward n_steps recording every step; curve[m] = mass loss dV sum_i (c_0,i(0) - c_0,i(t))
+// at t = (m+1) sample_every.  Needs vol_red == 0 (BV = 1) for the adjoint.
+int orc_forward_record(void* h, int n_steps, int sample_every, double* curve) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb || sample_every < 1) return 1;
+  if (o->p.vol_red != 0.0) return 6;
+  const int N = o->N;
+  g_rec = Record();
+  g_rec.steps = n_steps;
+  g_rec.sample_every = sample_every;
+  g_rec.c0.assign(o->c.begin(), o->c.begin() + N);
+  const double dV = o->p.dx * o->p.dy * o->p.dz;
+  int worst = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    g_rec.c.push_back(o->c);
+    g_rec.phase.push_back(o->phase);
+    StepRecord rec;
+    int st = step(*o, &rec);
+    if (st) worst = st;
+    g_rec.phi.push_back(o->phi);
+    g_rec.clamped.push_back(rec.clamped);
+    if ((s + 1) % sample_every == 0) {
+      double m = 0.0;
+      for (int i = 0; i < N; ++i) m += g_rec.c0[i] - o->c[i];
+      curve[(s + 1) / sample_every - 1] = m * dV;
+    }
+  }
+  return worst;
+}
+
+// dL/d(D_liquid[k]) and dL/dk_diss for dL/d(curve) given, by the adjoint of the recorded run.
+int orc_backward(void* h, const double* dL_dcurve, double* grad_D, double* grad_k) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const int N = o->N;
+  const int se = g_rec.sample_every;
+  if (g_rec.steps <= 0 || se < 1) return 7;
+  const double dV = o->p.dx * o->p.dy * o->p.dz;
+  std::vector<double> lam((int64_t)S * N, 0.0);
+  for (int k = 0; k < S; ++k) grad_D[k] = 0.0;
+  *grad_k = 0.0;
+  for (int n = g_rec.steps - 1; n >= 0; --n) {
+    if ((n + 1) % se == 0) {
+      const double g = dL_dcurve[(n + 1) / se - 1];
+      for (int i = 0; i < N; ++i) lam[i] += -dV * g;
+    }
+    adjoint_step(*o, n, lam, grad_D, grad_k);
+  }
   return 0;
 }
 

@@ -257,3 +257,36 @@ def test_state_roundtrip_and_errors(gpu):
     with pytest.raises(nn.NNPPError) as ei:
         sim.forward(2, nn.FP64)
     assert ei.value.status == 3
+
+
+def test_ensemble_matches_individual_runs(gpu):
+    """Uneven instances with their own parameters in one batched launch give the same
+    states as each instance run alone."""
+    nn = gpu
+    cases = [nn.synth(4, 14, 1), nn.synth(4, 20, 2), nn.synth(4, 17, 3), nn.synth(1, 12, 4)]
+    sims = []
+    for inp in cases:
+        s = nn.Simulation.from_synth(inp)
+        s.build_neighbours()
+        s.set_solver(1e-12)
+        sims.append(s)
+    ens = nn.Ensemble(sims)
+    ens.forward(30, nn.FP64)
+    T, W = ens.tuning()
+    assert T in (2, 4, 8) and W in (4, 8, 16)
+    for inp, s in zip(cases, sims):
+        alone = nn.Simulation.from_synth(inp)
+        alone.build_neighbours()
+        alone.set_solver(1e-12)
+        alone.forward(30, nn.FP64)
+        c_e, phi_e, ph_e = s.state()
+        c_a, phi_a, ph_a = alone.state()
+        assert np.array_equal(ph_e, ph_a)
+        assert np.abs(c_e - c_a).max() <= 1e-11 * np.abs(c_a).max()
+        assert np.abs(phi_e - phi_a).max() <= 1e-8 * max(np.abs(phi_a).max(), 1e-30)
+        assert s.diagnostics()["steps_done"] == 30
+    # mixed precision through the same ensemble, then continue one member alone
+    ens.forward(10, nn.MIXED)
+    sims[0].forward(2, nn.MIXED)
+    assert sims[0].diagnostics()["steps_done"] == 42
+    ens.close()
