@@ -189,6 +189,62 @@ def run_reference(args):
     return 0
 
 
+def adjoint_cost(nn, steps, ck=50, se=20):
+    """Cost of one gradient of the mass-loss misfit on the calibration workload (jittered
+    64^3 lattice minus an 8-node shell, solid cylinder r=0.25, sigmoid switch of width
+    0.01): forward with checkpoints + backward, against the plain forward of the same steps."""
+    inp = nn.synth(3, 64, 1)
+    base = inp["params"].copy()
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    pert = base.copy()
+    for k in range(4):
+        pert.D_liquid[k] *= 1.2
+        pert.D_solid[k] *= 1.2
+    pert.k_diss = 0.06
+    sim.set_params(pert)
+    target = sim.forward_ckpt(steps, nn.MIXED, ck, se)
+    sim.set_params(base)
+    sim.reset()
+    t0 = time.perf_counter()
+    curve = sim.forward_ckpt(steps, nn.MIXED, ck, se)
+    t1 = time.perf_counter()
+    gD, gk = sim.backward(2.0 * (curve - target))
+    t2 = time.perf_counter()
+    sim.reset()
+    ms_fwd = sim.forward_timed(steps, nn.MIXED)
+    fwd_ckpt, bwd = 1e3 * (t1 - t0), 1e3 * (t2 - t1)
+    return {"workload": "jittered 64^3 lattice minus 8-node shell (%d nodes), solid cylinder "
+                        "r=0.25, loss = L2 misfit of the Mg mass-loss curve" % inp["N"],
+            "steps": steps, "ckpt_every": ck, "sample_every": se,
+            "precision": "mixed forward, FP64 adjoint bond sums, mixed adjoint potential solve",
+            "forward_ms": ms_fwd, "forward_ckpt_ms": fwd_ckpt, "backward_ms": bwd,
+            "gradient_over_forward": (fwd_ckpt + bwd) / ms_fwd,
+            "backward_over_forward": bwd / ms_fwd,
+            "grad_D": [float(x) for x in gD], "grad_k": float(gk),
+            "loss": float(((curve - target) ** 2).sum())}
+
+
+class ProfileRange:
+    """cudaProfilerStart/Stop around one region of the run, for `ncu --profile-from-start off`;
+    NNPP_PROFILE=timed selects the timed steps, NNPP_PROFILE=kernels the per-kernel timings."""
+
+    def __init__(self, name):
+        self.on = os.environ.get("NNPP_PROFILE") == name
+
+    def __enter__(self):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
@@ -219,7 +275,8 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    ms = sim.forward_timed(args.steps, nn.MIXED)
+    with ProfileRange("timed"):
+        ms = sim.forward_timed(args.steps, nn.MIXED)
     clk = clocks.stop()
     d1 = sim.diagnostics()
     ms64 = sim64.forward_timed(args.steps, nn.FP64)
@@ -252,9 +309,10 @@ def run_ours(args):
     launches = solves + 2 * outer + 2 * inner + args.steps
 
     # kernel roofline: CG SpMV vs transport, CUDA-event timed on the library's stream
-    t_spmv = sim.time_kernel(1, nn.MIXED, reps=50)
-    t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
-    t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
+    with ProfileRange("kernels"):
+        t_spmv = sim.time_kernel(1, nn.MIXED, reps=50)
+        t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
+        t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
     spmv_per_step = inner / args.steps
     ir_per_step = outer / args.steps
     shares = {"cg_spmv": t_spmv * spmv_per_step, "transport": t_tr, "ir_residual": t_ir * ir_per_step}
@@ -312,6 +370,11 @@ def run_ours(args):
                "d2h_bytes_per_step": 4 * N * 8 + N * 8 + N * 4, "steps": ke, "pinned": pinned,
                "api": "nnpp_step_host"}
 
+    adj = None
+    if rank == 0 and args.adjoint_steps > 0:
+        adj = adjoint_cost(nn, args.adjoint_steps)
+        log("adjoint: %s" % json.dumps(adj))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(inp)
@@ -332,7 +395,8 @@ def run_ours(args):
             "accuracy_vs_fp64_gpu": acc,
             "solver": {"inner_cg_per_step": inner / args.steps, "outer_per_step": outer / args.steps,
                        "fp64_cg_per_step": (d64["cg_iterations_total"]) / (args.steps + args.warmup)},
-            "adjoint_over_forward": None,
+            "adjoint_over_forward": adj["gradient_over_forward"] if adj else None,
+            "adjoint": adj,
             "neighbour_build_s": t_build,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -347,6 +411,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=400,
+                    help="steps of the gradient-cost measurement (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -186,6 +186,21 @@ nnpp_status nnpp_get_neighbours_csr(nnpp_handle* h, int* row_ptr, int* cols, int
  * diagnostics.  The step sequence is captured once into a CUDA graph per precision. */
 nnpp_status nnpp_forward(nnpp_handle* h, int n_steps, int precision);
 
+/* Return to the initial state of nnpp_build_neighbours (initial values, phase0, zeroed
+ * counters and diagnostics, no flipped node), keeping the lists, solver settings and tuning.
+ * The reference starts each run from its .icvalues files (main.cpp:398-420). */
+nnpp_status nnpp_reset(nnpp_handle* h);
+
+/* Replace the model parameters of a handle (diffusivities, rate constant, time step,
+ * charges, constants) without rebuilding its neighbour lists, e.g. between the iterations of
+ * a calibration loop.  The geometry fields (dx, dy, dz, delta, the kernel exponents) and
+ * CSolid must equal the handle's, since the bond weights and the scaled Dirichlet values
+ * depend on them (NNPP_ERR_INVALID otherwise).
+ * Discards a recorded forward_ckpt run.  The reference fixes its utils::parameter object
+ * once per run (main.cpp:224-230, from the .data2/.datac* files); this entry point lets one
+ * handle serve many parameter sets. */
+nnpp_status nnpp_set_params(nnpp_handle* h, const nnpp_params* p);
+
 /* Solver settings: relative tolerance of the potential (default 1e-10), iteration cap of
  * the CG (default 2000), strict != 0 turns a capped solve into NNPP_ERR_CG_NO_CONVERGE. */
 nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict);
@@ -234,6 +249,10 @@ nnpp_status nnpp_forward_timed(nnpp_handle* h, int n_steps, int precision, doubl
  * 2 FP64 refinement residual. */
 nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int reps,
                              double* ms_per_launch);
+
+/* Autotuned configuration of the handle's kernels: bins per tile and lanes per node (both 0
+ * before the first step). */
+nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node);
 
 /* ---- differentiation ------------------------------------------------------------------ */
 

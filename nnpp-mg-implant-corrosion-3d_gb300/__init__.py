@@ -99,6 +99,9 @@ _SIGS = {
     "nnpp_solve_potential": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _IP, _DP]),
     "nnpp_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
     "nnpp_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
+    "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP]),
+    "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
+    "nnpp_reset": (C.c_int, [_P]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -283,6 +286,16 @@ class Simulation:
         _check(lib().nnpp_get_neighbours_csr(self._h, _ip(ptr), _ip(cols), C.byref(nnz)))
         return ptr, cols[:nnz.value]
 
+    def reset(self):
+        """Back to the initial state of build_neighbours (lists and tuning kept)."""
+        _check(lib().nnpp_reset(self._h))
+
+    def set_params(self, params):
+        """New model parameters with the same geometry (no neighbour rebuild)."""
+        p = params.copy()
+        _check(lib().nnpp_set_params(self._h, C.byref(p)))
+        self.params = p
+
     def set_solver(self, tol=1e-10, max_iter=2000, strict=False):
         _check(lib().nnpp_set_solver(self._h, tol, max_iter, 1 if strict else 0))
 
@@ -301,6 +314,27 @@ class Simulation:
         ms = C.c_double(0.0)
         _check(lib().nnpp_time_kernel(self._h, kernel_id, precision, reps, C.byref(ms)))
         return ms.value
+
+    def forward_ckpt(self, n_steps, precision=MIXED, ckpt_every=50, sample_every=20):
+        """Forward half of the adjoint pair: returns the cumulative Mg mass-loss curve
+        sampled every `sample_every` steps (checkpoints every `ckpt_every` steps)."""
+        curve = np.empty(n_steps // sample_every, dtype=np.float64)
+        _check(lib().nnpp_forward_ckpt(self._h, n_steps, precision, ckpt_every, sample_every,
+                                       _dp(curve)))
+        return curve
+
+    def backward(self, dL_dcurve):
+        """Backward half: dL/dD_liquid (4,) and dL/dk_diss for dL/d(curve)."""
+        g = np.ascontiguousarray(dL_dcurve, dtype=np.float64)
+        gD = np.zeros(NSPECIES)
+        gk = C.c_double(0.0)
+        _check(lib().nnpp_backward(self._h, _dp(g), _dp(gD), C.byref(gk)))
+        return gD, gk.value
+
+    def tuning(self):
+        t, w = C.c_int(0), C.c_int(0)
+        _check(lib().nnpp_get_tuning(self._h, C.byref(t), C.byref(w)))
+        return t.value, w.value
 
     def state(self):
         c = np.empty((NSPECIES, self.N), dtype=np.float64)

@@ -144,6 +144,28 @@ nnpp_status upload_state(Handle& h, const double* c, const double* phi, const in
                     phase ? h.user_stage_i.get() : nullptr, prec, dirichlet_phi);
 }
 
+// The initial state (main.cpp:398-420 with the given phase): concentrations and potential
+// from the initial values, counters and diagnostics zeroed, no flipped node, no recorded run.
+nnpp_status reset_initial(Handle& h) {
+  const size_t N = h.N;
+  DevState ds;
+  std::memset(&ds, 0, sizeof(ds));
+  ds.tol = h.tol;
+  ds.max_iter = h.max_iter;
+  ds.max_outer = h.max_outer;
+  ds.inner_rel = h.inner_rel;
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  h.cur = 0;
+  NNPP_TRY(upload_state(h, h.h_ic.data(), h.h_ic.data() + S * N, h.h_phase0.data(), NNPP_FP64));
+  NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, sizeof(int) * N, h.st));
+  NNPP_TRY(init_diag(h));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.fwd_steps = 0;
+  h.ckpts.clear();
+  if (h.engine) NNPP_TRY(engine_params(*h.engine));
+  return NNPP_OK;
+}
+
 // single-instance view of h's engine with a private KParams block (in_graph = 0)
 struct OneView {
   DBuf<KParams> kp;
@@ -347,19 +369,7 @@ nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, do
   }
   NNPP_CUDA(cudaMemcpyAsync(h.dirmask.get(), dm.data(), N, cudaMemcpyHostToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.bcval.get(), bcv.data(), sizeof(double) * (S + 1) * N, cudaMemcpyHostToDevice, h.st));
-  // initial state (main.cpp:398-420 with the given phase)
-  DevState ds;
-  std::memset(&ds, 0, sizeof(ds));
-  ds.tol = h.tol;
-  ds.max_iter = h.max_iter;
-  ds.max_outer = h.max_outer;
-  ds.inner_rel = h.inner_rel;
-  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
-  h.cur = 0;
-  NNPP_TRY(upload_state(h, h.h_ic.data(), h.h_ic.data() + S * N, h.h_phase0.data(), NNPP_FP64));
-  NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, sizeof(int) * N, h.st));
-  NNPP_TRY(init_diag(h));
-  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  NNPP_TRY(reset_initial(h));
   h.built = true;
   h.engine = new Engine();
   h.engine->members.push_back(&h);
@@ -634,6 +644,40 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
   cudaEventDestroy(e1);
   nnpp_status st2 = restore(h, b);
   return st != NNPP_OK ? st : st2;
+}
+
+nnpp_status nnpp_reset(nnpp_handle* hp) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  return reset_initial(hp->h);
+}
+
+nnpp_status nnpp_set_params(nnpp_handle* hp, const nnpp_params* p) {
+  NNPP_GUARD(hp);
+  NNPP_TRY(check_params(p));
+  Handle& h = hp->h;
+  const nnpp_params& o = h.p;
+  bool same = p->dx == o.dx && p->dy == o.dy && p->dz == o.dz && p->delta == o.delta &&
+              p->s_phi == o.s_phi && p->CSolid == o.CSolid;
+  for (int s = 0; s < S; ++s) same = same && p->s1[s] == o.s1[s] && p->s2[s] == o.s2[s];
+  if (!same)
+    return set_error(NNPP_ERR_INVALID, "set_params: geometry fields or CSolid differ from the handle's");
+  NNPP_CUDA(cudaSetDevice(h.device));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.p = *p;
+  h.fwd_steps = 0;
+  h.ckpts.clear();
+  if (h.engine) NNPP_TRY(engine_params(*h.engine));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_tuning(nnpp_handle* hp, int* bins_per_tile, int* lanes_per_node) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  const Engine& e = *hp->h.engine;
+  if (bins_per_tile) *bins_per_tile = e.tuned ? e.T : 0;
+  if (lanes_per_node) *lanes_per_node = e.tuned ? e.W : 0;
+  return NNPP_OK;
 }
 
 // ---- ensembles ------------------------------------------------------------------------------

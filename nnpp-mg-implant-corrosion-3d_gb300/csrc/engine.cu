@@ -50,14 +50,15 @@ nnpp_status build_lists(Engine& e, int T) {
   std::vector<TileDesc> tiles;
   std::vector<Chunk> chunks;
   std::vector<int> meta(4 * M);
-  int hm = 0;
+  int hm = 0, bmax = 0;
   for (int i = 0; i < M; ++i) {
     Handle& h = *e.members[i];
     meta[i] = (int)tiles.size();
-    int hmi = 0;
-    NNPP_TRY(build_tiles(h, T, tiles, i, &hmi));
+    int hmi = 0, bmi = 0;
+    NNPP_TRY(build_tiles(h, T, tiles, i, &hmi, &bmi));
     meta[M + i] = (int)tiles.size() - meta[i];
     hm = std::max(hm, hmi);
+    bmax = std::max(bmax, bmi);
     meta[2 * M + i] = (int)chunks.size();
     for (int b = 0; b < h.N; b += kChunk) {
       Chunk c;
@@ -72,6 +73,7 @@ nnpp_status build_lists(Engine& e, int T) {
   e.ntiles = (int)tiles.size();
   e.nchunks = (int)chunks.size();
   e.halo_max = hm;
+  e.bond_max = bmax;
   e.T = T;
   if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
       !e.d_ticket.alloc(M + 1) || !e.d_partials.alloc((size_t)kReduceSlots * std::max(e.ntiles, e.nchunks)) ||
@@ -119,7 +121,7 @@ nnpp_status tune(Engine& e, int prec) {
     NNPP_TRY(refresh_params(e));
     for (int W : Ws) {
       e.W = W;
-      if (prepare_kernels(e.halo_max, W) != NNPP_OK) continue;
+      if (prepare_kernels(e.halo_max, e.bond_max, W) != NNPP_OK) continue;
       EngineView v = make_view(e, 0, 0);
       NNPP_TRY(set_active(e, 1, 1));
       NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
@@ -145,7 +147,7 @@ nnpp_status tune(Engine& e, int prec) {
     NNPP_CUDA(cudaMemcpy(e.members[i]->dstate.get(), &saved[i], sizeof(DevState), cudaMemcpyHostToDevice));
   NNPP_TRY(build_lists(e, bT));
   e.W = bW;
-  NNPP_TRY(prepare_kernels(e.halo_max, bW));
+  NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, bW));
   e.tuned = true;
   return NNPP_OK;
 }
@@ -236,7 +238,7 @@ nnpp_status prepare_run(Engine& e, int prec) {
     for (Handle* h : e.members)
       if (h->tiles_T != e.T) {
         NNPP_TRY(build_lists(e, e.T));
-        NNPP_TRY(prepare_kernels(e.halo_max, e.W));
+        NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, e.W));
         break;
       }
   }
@@ -281,6 +283,7 @@ EngineView make_view(Engine& e, int parity, int in_graph) {
   v.in_graph = in_graph;
   v.stride = std::max(e.ntiles, e.nchunks);
   v.halo_max = e.halo_max;
+  v.bond_max = e.bond_max;
   return v;
 }
 
@@ -296,9 +299,10 @@ nnpp_status engine_build(Engine& e) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e.device);
   if (sms <= 0) sms = 152;
+  e.sms = sms;
   e.grid = sms * 4;
   NNPP_TRY(build_lists(e, e.T));
-  NNPP_TRY(prepare_kernels(e.halo_max, e.W));
+  NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, e.W));
   return NNPP_OK;
 }
 

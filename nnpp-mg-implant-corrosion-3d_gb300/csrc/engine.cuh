@@ -19,7 +19,8 @@ struct TileDesc {
   int hl[9];
   int halo;                // total halo nodes (sum of hl)
   int cb[3];               // centre bin (coordinates are staged relative to it)
-  int pad;
+  int bond0;               // first bond of the own nodes, rounded down to a multiple of 8
+  int bond1;               // one past the last bond of the own nodes
 };
 
 // An elementwise work item: nodes [begin, end) of one instance.
@@ -43,6 +44,7 @@ struct EngineView {
   int ntiles, nchunks, M, in_graph;
   int stride;               // max(ntiles, nchunks): slot stride of partials
   int halo_max;             // largest halo (dynamic shared memory sizing)
+  int bond_max;             // largest staged bond range of a tile (bond1 - bond0)
 };
 
 constexpr int kChunk = 4096;  // nodes per elementwise work item
@@ -53,7 +55,9 @@ struct Engine {
   int W = 8;                // lanes per node (autotuned)
   bool tuned = false;
   int grid = 0;
+  int sms = 152;
   int halo_max = 0;
+  int bond_max = 0;
   DBuf<KParams> d_inst[2];  // indexed by the parity of the current record buffer
   DBuf<TileDesc> d_tiles;
   DBuf<Chunk> d_chunks;
@@ -80,7 +84,8 @@ nnpp_status engine_params(Engine& e);            // re-upload the members' KPara
 void engine_destroy_graphs(Engine& e);
 
 // tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
-nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max);
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max,
+                        int* bond_max);
 
 // step.cu launchers (batched)
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
@@ -94,7 +99,7 @@ nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, c
                                cudaGraphConditionalHandle hc);
 nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                double* F_out);
-nnpp_status prepare_kernels(int halo_max, int W);
+nnpp_status prepare_kernels(int halo_max, int bond_max, int W);
 
 // adjoint (step.cu)
 nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec64* snap,

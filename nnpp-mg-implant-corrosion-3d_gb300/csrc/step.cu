@@ -51,6 +51,19 @@ __device__ __forceinline__ void load_tile(const TileDesc& t, TileSmem& ts) {
   __syncthreads();
 }
 
+__host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// Copy the tile's bond slots [bond0, bond1) into shared memory with 16-byte loads (bond0 is
+// a multiple of 8, the slot array is padded); bond j is then at dst[j - bond0].
+__device__ __forceinline__ const unsigned short* stage_slots(const unsigned short* slot16,
+                                                             const TileDesc& t, unsigned char* dst) {
+  const int n = (t.bond1 - t.bond0 + 7) >> 3;
+  const uint4* src = reinterpret_cast<const uint4*>(slot16 + t.bond0);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = src[i];
+  return reinterpret_cast<const unsigned short*>(dst);
+}
+
 // node of halo index s
 __device__ __forceinline__ int halo_node(const TileSmem& ts, int s) {
   int r = 0;
@@ -192,6 +205,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
     load_tile(t, ts);
     double* sphi = reinterpret_cast<double*>(dsm);
     unsigned char* sfl = dsm + sizeof(double) * (size_t)t.halo;
+    const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(double) * (size_t)t.halo + t.halo));
     const double* phi64 = k.phi64;
     const unsigned char* dm = k.dirmask;
     for (int s = threadIdx.x; s < t.halo; s += kBlock) {
@@ -202,7 +216,6 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
     __syncthreads();
     double part[2] = {0.0, 0.0};
     const int* row = k.row;
-    const unsigned short* slot = k.slot16;
     const double* w64 = k.w64;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
     for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
@@ -215,7 +228,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
       int anyll = 0;
       if (scan) {
         for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int s = slot[j];
+          const int s = sslot[j - t.bond0];
           const unsigned char f = sfl[s];
           if (f & 1) {
             const double w = w64[j];
@@ -363,6 +376,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
     if (active) {
       load_tile(t, ts);
       float4* hs = reinterpret_cast<float4*>(dsm);
+      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + sizeof(float4) * (size_t)t.halo);
       const float4* posrec = k.posrec;
       const float* z = k.z32;
       const float h = k.h32;
@@ -379,7 +393,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
       }
       __syncthreads();
       const int* row = k.row;
-      const unsigned short* slot = k.slot16;
       const unsigned char* freem = k.freem;
       float* p = k.p32;
       float* q = k.q32;
@@ -394,7 +407,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
         if (act) {
           me = hs[own0 + (a - t.own_begin)];
           for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-            const float4 o = hs[slot[j]];
+            const float4 o = hs[sslot[j - t.bond0]];
             const float dx = o.x - me.x, dy = o.y - me.y, dz = o.z - me.z;
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const float ri = rsqrtf(r2);
@@ -446,11 +459,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
     if (active) {
       load_tile(t, ts);
       double* hs = reinterpret_cast<double*>(dsm);
+      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(double) * (size_t)t.halo));
       const double* z = k.z64;
       for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = z[halo_node(ts, s)];
       __syncthreads();
       const int* row = k.row;
-      const unsigned short* slot = k.slot16;
       const double* w64 = k.w64;
       const unsigned char* freem = k.freem;
       double* p = k.p64;
@@ -462,7 +475,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
         const bool act = a < t.own_end && freem[a];
         double acc = 0.0;
         if (act)
-          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[slot[j]], acc);
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[sslot[j - t.bond0]], acc);
         acc = seg_reduce_d<W>(acc);
         if (act && sub == 0) {
           const double za = hs[own0 + (a - t.own_begin)];
@@ -562,11 +575,11 @@ __global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphCon
     if (active) {
       load_tile(t, ts);
       double* hs = reinterpret_cast<double*>(dsm);
+      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(double) * (size_t)t.halo));
       const P* e = VecSel<P>::e(k);
       for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = (double)e[halo_node(ts, s)];
       __syncthreads();
       const int* row = k.row;
-      const unsigned short* slot = k.slot16;
       const double* w64 = k.w64;
       const unsigned char* freem = k.freem;
       const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
@@ -575,7 +588,7 @@ __global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphCon
         const bool act = a < t.own_end && freem[a];
         double acc = 0.0;
         if (act)
-          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[slot[j]], acc);
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[sslot[j - t.bond0]], acc);
         acc = seg_reduce_d<W>(acc);
         if (act && sub == 0) {
           const double ea = hs[own0 + (a - t.own_begin)];
@@ -675,6 +688,7 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     float4* hc = reinterpret_cast<float4*>(dsm);
     float2* hp = reinterpret_cast<float2*>(hc + t.halo);
     float* hph = reinterpret_cast<float*>(hp + t.halo);
+    const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16((size_t)28 * t.halo));
     const Rec32* rc = k.rec32_cur;
     for (int s = threadIdx.x; s < t.halo; s += kBlock) {
       const int n = halo_node(ts, s);
@@ -699,7 +713,6 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     const float dtf = (float)k.dt;
     const long long step_no = k.ds->steps + 1;
     const int* row = k.row;
-    const unsigned short* slot = k.slot16;
     const float* w32 = k.w32;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
     double part[kDiagSlots];
@@ -723,7 +736,7 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
       int iface = 0;
       if (act) {
         for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int sl = slot[j];
+          const int sl = sslot[j - t.bond0];
           const float w = w32[j];
           const float4 cn = hc[sl];
           const float2 pn2 = hp[sl];
@@ -822,6 +835,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
     const KParams& k = v.inst[t.inst];
     load_tile(t, ts);
     double* hrec = reinterpret_cast<double*>(dsm);  // 6 doubles per halo node (SoA)
+    const unsigned short* sslot = stage_slots(k.slot16, t, dsm + (size_t)6 * t.halo * sizeof(double));
     const Rec64* rc = k.rec64_cur;
     const int H = t.halo;
     for (int s = threadIdx.x; s < H; s += kBlock) {
@@ -843,7 +857,6 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
     }
     const long long step_no = k.ds->steps + 1;
     const int* row = k.row;
-    const unsigned short* slot = k.slot16;
     const double* w64 = k.w64;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
     double part[kDiagSlots];
@@ -866,7 +879,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
       int iface = 0;
       if (act) {
         for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int sl = slot[j];
+          const int sl = sslot[j - t.bond0];
           const double w = w64[j];
           const double pn = hrec[(size_t)(S + 1) * H + sl];
           const double dphi = hrec[(size_t)S * H + sl] - pha;
@@ -1084,11 +1097,25 @@ nnpp_status dispatch_lanes(int lanes, F&& f) {
   }
 }
 
-size_t smem_prep(int H) { return (size_t)H * (sizeof(double) + 1) + 16; }
-size_t smem_spmv32(int H) { return (size_t)H * sizeof(float4); }
-size_t smem_vec64(int H) { return (size_t)H * sizeof(double); }
-size_t smem_tr32(int H) { return (size_t)H * (sizeof(float4) + sizeof(float2) + sizeof(float)); }
-size_t smem_tr64(int H) { return (size_t)H * 6 * sizeof(double); }
+// Persistent grid: as many CTAs as fit on the device at once (at most one per item).
+template <typename K>
+int occ_grid(K kern, size_t smem, int sms, int items) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, smem) != cudaSuccess) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  if (nb < 1) nb = 1;
+  const int g = sms * nb;
+  return items < g ? (items > 0 ? items : 1) : g;
+}
+
+size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
+size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
+size_t smem_spmv32(int H, int B) { return (size_t)H * sizeof(float4) + smem_slots(B); }
+size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
+size_t smem_tr32(int H, int B) { return align16((size_t)28 * H) + smem_slots(B); }
+size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 
 template <typename K>
 nnpp_status allow_smem(K kern, size_t bytes) {
@@ -1139,6 +1166,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_transport(EngineView v, AdjArgs 
     double* hl = hc + (size_t)S * H;              // masked lambda: S*H
     double* hphi = hl + (size_t)S * H;            // H
     unsigned char* hph = reinterpret_cast<unsigned char*>(hphi + H);
+    const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16((size_t)9 * H * sizeof(double) + H));
     for (int s = threadIdx.x; s < H; s += kBlock) {
       const int n = halo_node(ts, s);
       const Rec64 r = ad.snap[n];
@@ -1155,7 +1183,6 @@ __global__ void __launch_bounds__(kBlock) k_adj_transport(EngineView v, AdjArgs 
     }
     __syncthreads();
     const int* row = k.row;
-    const unsigned short* slot = k.slot16;
     const double* w64 = k.w64;
     const double dt = k.dt;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
@@ -1182,7 +1209,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_transport(EngineView v, AdjArgs 
       int iface = 0;
       if (act) {
         for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int si = slot[j];
+          const int si = sslot[j - t.bond0];
           const double w = w64[j];
           const bool pi = hph[si] != 0;
           const double phi_i = hphi[si];
@@ -1302,7 +1329,7 @@ __global__ void k_sum_c0(KParams k, int mixed, double* out) {
       part[0] += k.rec64_cur[a].c[0];
   }
   block_sum<1, kBlock>(part, sm);
-  if (threadIdx.x == 0) atomicAdd(out, part[0]);
+  if (threadIdx.x == 0) *out = part[0];
 }
 
 }  // namespace
@@ -1311,12 +1338,12 @@ nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec
                                  const Rec64* snap1, const double* lam, double* mu, double* nu,
                                  double* acc, cudaStream_t st) {
   AdjArgs ad{snap, snap1, lam, mu, nu, acc};
-  const size_t sh = (size_t)v.halo_max * (9 * sizeof(double) + 1) + 16;
+  const size_t sh = align16((size_t)v.halo_max * (9 * sizeof(double) + 1)) + (size_t)(v.bond_max + 16) * 2 + 16;
   if (sh > 227 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "adjoint: tile halo too large");
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     NNPP_TRY(allow_smem(k_adj_transport<W>, sh));
-    k_adj_transport<W><<<e.grid, kBlock, sh, st>>>(v, ad);
+    k_adj_transport<W><<<occ_grid(k_adj_transport<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, ad);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   });
@@ -1352,27 +1379,27 @@ nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* p
 
 nnpp_status launch_sum_c0(Handle& h, double* out) {
   KParams kp = make_kparams(h, h.cur);
-  NNPP_CUDA(cudaMemsetAsync(out, 0, sizeof(double), h.st));
-  k_sum_c0<<<h.grid, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0, out);
+  // one block: a fixed summation order, so repeated runs give the same mass to the bit
+  k_sum_c0<<<1, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0, out);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
 
 // ---------------------------------------------------------------------------------------
-nnpp_status prepare_kernels(int H, int lanes) {
-  if (smem_tr64(H) > 200 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
+nnpp_status prepare_kernels(int H, int B, int lanes) {
+  if (smem_tr64(H, B) > 220 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
   return dispatch_lanes(lanes, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
-    NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H)));
-    NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H)));
-    NNPP_TRY(allow_smem(k_cg_spmv32<W>, smem_spmv32(H)));
-    NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H)));
-    NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H)));
-    NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H)));
-    NNPP_TRY(allow_smem(k_transport32<W, false>, smem_tr32(H)));
-    NNPP_TRY(allow_smem(k_transport32<W, true>, smem_tr32(H)));
-    NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H)));
-    NNPP_TRY(allow_smem(k_transport64<W, true>, smem_tr64(H)));
+    NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
+    NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W>, smem_spmv32(H, B)));
+    NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
+    NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
+    NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
+    NNPP_TRY(allow_smem(k_transport32<W, false>, smem_tr32(H, B)));
+    NNPP_TRY(allow_smem(k_transport32<W, true>, smem_tr32(H, B)));
+    NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
+    NNPP_TRY(allow_smem(k_transport64<W, true>, smem_tr64(H, B)));
     return NNPP_OK;
   });
 }
@@ -1381,11 +1408,11 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
                           cudaGraphConditionalHandle hc, double* F11_out) {
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
-    const size_t sh = smem_prep(v.halo_max);
+    const size_t sh = smem_prep(v.halo_max, v.bond_max);
     if (prec == NNPP_MIXED)
-      k_prep<float, W><<<e.grid, kBlock, sh, st>>>(v, hc, F11_out);
+      k_prep<float, W><<<occ_grid(k_prep<float, W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, hc, F11_out);
     else
-      k_prep<double, W><<<e.grid, kBlock, sh, st>>>(v, hc, F11_out);
+      k_prep<double, W><<<occ_grid(k_prep<double, W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, hc, F11_out);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   });
@@ -1394,9 +1421,9 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc) {
   if (prec == NNPP_MIXED)
-    k_cg_init<float><<<e.grid, kBlock, 0, st>>>(v, hc, 0);
+    k_cg_init<float><<<occ_grid(k_cg_init<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0);
   else
-    k_cg_init<double><<<e.grid, kBlock, 0, st>>>(v, hc, 1);
+    k_cg_init<double><<<occ_grid(k_cg_init<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 1);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
@@ -1405,9 +1432,9 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      k_cg_spmv32<W><<<e.grid, kBlock, smem_spmv32(v.halo_max), st>>>(v);
+      { const size_t sh = smem_spmv32(v.halo_max, v.bond_max); k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }
     else
-      k_cg_spmv64<W><<<e.grid, kBlock, smem_vec64(v.halo_max), st>>>(v);
+      { const size_t sh = smem_vec64(v.halo_max, v.bond_max); k_cg_spmv64<W><<<occ_grid(k_cg_spmv64<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   });
@@ -1416,9 +1443,9 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
   if (prec == NNPP_MIXED)
-    k_cg_update<float><<<e.grid, kBlock, 0, st>>>(v, hc);
+    k_cg_update<float><<<occ_grid(k_cg_update<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
   else
-    k_cg_update<double><<<e.grid, kBlock, 0, st>>>(v, hc);
+    k_cg_update<double><<<occ_grid(k_cg_update<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
@@ -1427,11 +1454,11 @@ nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, c
                                cudaGraphConditionalHandle hc) {
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
-    const size_t sh = smem_vec64(v.halo_max);
+    const size_t sh = smem_vec64(v.halo_max, v.bond_max);
     if (prec == NNPP_MIXED)
-      k_ir_update<float, W><<<e.grid, kBlock, sh, st>>>(v, hc);
+      k_ir_update<float, W><<<occ_grid(k_ir_update<float, W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, hc);
     else
-      k_ir_update<double, W><<<e.grid, kBlock, sh, st>>>(v, hc);
+      k_ir_update<double, W><<<occ_grid(k_ir_update<double, W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, hc);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   });
@@ -1442,17 +1469,17 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED) {
-      const size_t sh = smem_tr32(v.halo_max);
+      const size_t sh = smem_tr32(v.halo_max, v.bond_max);
       if (F_out)
-        k_transport32<W, true><<<e.grid, kBlock, sh, st>>>(v, F_out);
+        k_transport32<W, true><<<occ_grid(k_transport32<W, true>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, F_out);
       else
-        k_transport32<W, false><<<e.grid, kBlock, sh, st>>>(v, nullptr);
+        k_transport32<W, false><<<occ_grid(k_transport32<W, false>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, nullptr);
     } else {
-      const size_t sh = smem_tr64(v.halo_max);
+      const size_t sh = smem_tr64(v.halo_max, v.bond_max);
       if (F_out)
-        k_transport64<W, true><<<e.grid, kBlock, sh, st>>>(v, F_out);
+        k_transport64<W, true><<<occ_grid(k_transport64<W, true>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, F_out);
       else
-        k_transport64<W, false><<<e.grid, kBlock, sh, st>>>(v, nullptr);
+        k_transport64<W, false><<<occ_grid(k_transport64<W, false>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, nullptr);
     }
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;

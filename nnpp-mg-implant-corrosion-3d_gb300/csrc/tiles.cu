@@ -92,7 +92,8 @@ __global__ void k_slots(int n, const int* row, const int* col, const float4* pos
 
 }  // namespace
 
-nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max) {
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max,
+                        int* bond_max) {
   const Layout& L = h.lay;
   const int N = h.N;
   if (L.nb[0] > 1024 || L.nb[1] > 1024 || L.nb[2] > 1024)
@@ -103,8 +104,10 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
   g.nb[2] = L.nb[2];
   g.T = T;
   const double hb = (double)h.h32;
-  if (!h.posrec.alloc(N) || !h.slot16.alloc(L.nnz > 0 ? (size_t)L.nnz : 1))
+  // slots are staged per tile with 16-byte loads from a multiple of 8: pad the array
+  if (!h.posrec.alloc(N) || !h.slot16.alloc((size_t)L.nnz + 16))
     return set_error(NNPP_ERR_NOMEM, "tile arrays");
+  NNPP_CUDA(cudaMemsetAsync(h.slot16.get(), 0, sizeof(unsigned short) * ((size_t)L.nnz + 16), h.st));
   const int blocks = std::max(1, std::min((N + 255) / 256, 152 * 16));
   k_posrec<<<blocks, 256, 0, h.st>>>(N, L.pos.get(), h.ref.bbox[0], h.ref.bbox[2], h.ref.bbox[4], hb,
                                      g.nb[0], g.nb[1], g.nb[2], h.posrec.get());
@@ -115,14 +118,15 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
   k_slots<<<wblocks, 256, 0, h.st>>>(N, L.row.get(), L.col.get(), h.posrec.get(), L.bin_start.get(), g,
                                      h.slot16.get(), err.get());
   NNPP_CUDA(cudaGetLastError());
-  std::vector<int> bs(L.nbins + 1);
+  std::vector<int> bs(L.nbins + 1), rows(N + 1);
   int herr = 0;
   NNPP_CUDA(cudaMemcpyAsync(bs.data(), L.bin_start.get(), sizeof(int) * (L.nbins + 1), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(rows.data(), L.row.get(), sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (herr) return set_error(NNPP_ERR_INVALID, "tiles: a neighbour outside its tile's halo");
   const int ntx = (g.nb[0] + T - 1) / T;
-  int hm = 0;
+  int hm = 0, bm = 0;
   for (int bz = 0; bz < g.nb[2]; ++bz)
     for (int by = 0; by < g.nb[1]; ++by)
       for (int tx = 0; tx < ntx; ++tx) {
@@ -142,11 +146,14 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
         t.cb[0] = bx0 + T / 2;
         t.cb[1] = by;
         t.cb[2] = bz;
-        t.pad = 0;
+        t.bond0 = rows[o0] & ~7;
+        t.bond1 = rows[o1];
         hm = std::max(hm, tot);
+        bm = std::max(bm, t.bond1 - t.bond0);
         tiles.push_back(t);
       }
   *halo_max = hm;
+  *bond_max = bm;
   h.tiles_T = T;
   return NNPP_OK;
 }

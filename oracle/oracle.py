@@ -288,3 +288,34 @@ def ref_k11(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel=0.0)
     val = np.empty(nnz.value)
     L.ref_newton_k11(*args, C.byref(nnz), _ip(ri), _ip(ci), _dp(val))
     return ri, ci, val
+
+
+def _adjoint_sigs():
+    L = load_oracle()
+    if not getattr(L, "_adj", False):
+        L.orc_forward_record.restype = C.c_int
+        L.orc_forward_record.argtypes = [_P, C.c_int, C.c_int, _DP]
+        L.orc_backward.restype = C.c_int
+        L.orc_backward.argtypes = [_P, _DP, _DP, _DP]
+        L._adj = True
+    return L
+
+
+def oracle_forward_record(o, n_steps, sample_every):
+    """FP64 forward recording every step; returns the mass-loss curve."""
+    L = _adjoint_sigs()
+    curve = np.zeros(n_steps // sample_every)
+    st = L.orc_forward_record(o._h, n_steps, sample_every, _dp(curve))
+    if st not in (0, 4):
+        raise RuntimeError("oracle forward_record failed (%d)" % st)
+    return curve
+
+
+def oracle_backward(o, dL_dcurve):
+    """Adjoint of the last recorded run: (dL/dD_liquid (4,), dL/dk_diss)."""
+    L = _adjoint_sigs()
+    g = np.ascontiguousarray(dL_dcurve, dtype=np.float64)
+    gD = np.zeros(NSPECIES)
+    gk = np.zeros(1)
+    L.orc_backward(o._h, _dp(g), _dp(gD), _dp(gk))
+    return gD, float(gk[0])

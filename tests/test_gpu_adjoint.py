@@ -1,0 +1,175 @@
+"""GPU checkpointed adjoint (nnpp_forward_ckpt / nnpp_backward) against the oracle's FP64
+adjoint, against central finite differences of the GPU forward, across checkpoint intervals
+and precisions, and through the torch.autograd binding."""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N_STEPS, SE = 60, 20
+
+
+@pytest.fixture(scope="module")
+def gpu(nn):
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    return nn
+
+
+def _params(inp, scale_D=1.0, k=0.05):
+    p = inp["params"].copy()
+    p.switch_width = 0.01
+    p.k_diss = k
+    for s in range(4):
+        p.D_liquid[s] *= scale_D
+        p.D_solid[s] *= scale_D
+    return p
+
+
+@pytest.fixture(scope="module")
+def case(gpu, orc):
+    inp = gpu.synth(1, 12, 5)
+    o = orc.Oracle(_params(inp, 1.2, 0.06), inp["nodes"], inp["bctypes"], inp["bcvalues"],
+                   inp["icvalues"], inp["phase0"])
+    o.build_neighbours()
+    o.set_solver(1e-14)
+    target = orc.oracle_forward_record(o, N_STEPS, SE)
+    return inp, target
+
+
+def _sim(nn, inp, p, tol=1e-13):
+    sim = nn.Simulation(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"],
+                        inp["phase0"])
+    sim.build_neighbours()
+    sim.set_solver(tol, 4000)
+    return sim
+
+
+def test_adjoint_fp64_matches_oracle(gpu, orc, case):
+    inp, target = case
+    p = _params(inp)
+    o = orc.Oracle(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    o.build_neighbours()
+    o.set_solver(1e-14)
+    curve_o = orc.oracle_forward_record(o, N_STEPS, SE)
+    gD_o, gk_o = orc.oracle_backward(o, 2.0 * (curve_o - target))
+    sim = _sim(gpu, inp, p)
+    curve = sim.forward_ckpt(N_STEPS, gpu.FP64, 25, SE)
+    np.testing.assert_allclose(curve, curve_o, rtol=1e-10)
+    gD, gk = sim.backward(2.0 * (curve - target))
+    # species 0 and the rate constant to 1e-8; species 1-3 act through the potential only
+    # (gradients 100-1000x smaller) and carry the solves' 1e-13 tolerance
+    assert abs(gD[0] - gD_o[0]) <= 1e-8 * abs(gD_o[0]), (gD, gD_o)
+    for k in range(1, 4):
+        assert abs(gD[k] - gD_o[k]) <= 1e-5 * abs(gD_o[k]), (k, gD, gD_o)
+    assert abs(gk - gk_o) <= 1e-8 * abs(gk_o), (gk, gk_o)
+
+
+def test_adjoint_fp64_matches_central_differences(gpu, case):
+    inp, target = case
+    base = _params(inp)
+    sim = _sim(gpu, inp, base)
+    curve = sim.forward_ckpt(N_STEPS, gpu.FP64, 25, SE)
+    gD, gk = sim.backward(2.0 * (curve - target))
+
+    def loss(p):
+        sim.set_params(p)
+        sim.reset()
+        c = sim.forward_ckpt(N_STEPS, gpu.FP64, 25, SE)
+        return float(((c - target) ** 2).sum())
+
+    h = 1e-5
+    tol = (1e-7, 1e-4, 1e-4, 1e-4)
+    for k in range(4):
+        pp, pm = base.copy(), base.copy()
+        v = base.D_liquid[k]
+        for q, f in ((pp, 1 + h), (pm, 1 - h)):
+            q.D_liquid[k] = v * f
+            q.D_solid[k] = base.D_solid[k] * f
+        fd = (loss(pp) - loss(pm)) / (2 * h * v)
+        assert abs(gD[k] - fd) <= tol[k] * abs(fd), (k, gD[k], fd)
+    pp, pm = base.copy(), base.copy()
+    pp.k_diss = base.k_diss * (1 + h)
+    pm.k_diss = base.k_diss * (1 - h)
+    fd = (loss(pp) - loss(pm)) / (2 * h * base.k_diss)
+    assert abs(gk - fd) <= 1e-8 * abs(fd), (gk, fd)
+
+
+def test_checkpoint_interval_does_not_change_result(gpu, case):
+    """Segments are recomputed from checkpoints by the same deterministic kernels, so the
+    gradients do not depend on the checkpoint interval."""
+    inp, target = case
+    out = []
+    for ck in (7, 25, 60):
+        sim = _sim(gpu, inp, _params(inp))
+        curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
+        gD, gk = sim.backward(2.0 * (curve - target))
+        out.append((curve, gD, gk))
+    for curve, gD, gk in out[1:]:
+        assert np.array_equal(curve, out[0][0])
+        assert np.array_equal(gD, out[0][1])
+        assert gk == out[0][2]
+
+
+def test_backward_restores_end_state(gpu, case):
+    inp, target = case
+    sim = _sim(gpu, inp, _params(inp))
+    curve = sim.forward_ckpt(N_STEPS, gpu.FP64, 25, SE)
+    c0, phi0, ph0 = sim.state()
+    sim.backward(2.0 * (curve - target))
+    c1, phi1, ph1 = sim.state()
+    assert np.array_equal(c0, c1) and np.array_equal(phi0, phi1) and np.array_equal(ph0, ph1)
+
+
+def test_adjoint_mixed_close_to_fp64(gpu, case):
+    inp, target = case
+    g = {}
+    for prec in (gpu.FP64, gpu.MIXED):
+        sim = _sim(gpu, inp, _params(inp), tol=1e-12)
+        curve = sim.forward_ckpt(N_STEPS, prec, 25, SE)
+        g[prec] = sim.backward(2.0 * (curve - target))
+    (gD64, gk64), (gD32, gk32) = g[gpu.FP64], g[gpu.MIXED]
+    assert abs(gD32[0] - gD64[0]) <= 1e-5 * abs(gD64[0])
+    assert abs(gk32 - gk64) <= 1e-5 * abs(gk64)
+    assert np.linalg.norm(gD32 - gD64) <= 1e-3 * np.linalg.norm(gD64)
+
+
+def test_backward_errors(gpu, case):
+    inp, _ = case
+    sim = _sim(gpu, inp, _params(inp))
+    with pytest.raises(gpu.NNPPError) as e:
+        sim.backward(np.zeros(3))
+    assert e.value.status == 7  # NNPP_ERR_STATE: no recorded forward
+    sim.forward_ckpt(N_STEPS, gpu.FP64, 25, SE)
+    p = _params(inp)
+    p.delta *= 1.01
+    with pytest.raises(gpu.NNPPError) as e:
+        sim.set_params(p)
+    assert e.value.status == 1
+
+
+def test_torch_autograd_binding(gpu, orc, case):
+    torch = pytest.importorskip("torch")
+    ag = importlib.import_module("nnpp_gb300.autograd")
+    inp, target = case
+    base = _params(inp)
+    sim = _sim(gpu, inp, base)
+    theta = torch.tensor(list(base.D_liquid) + [base.k_diss], dtype=torch.float64,
+                         requires_grad=True)
+    curve = ag.mass_loss_curve(theta, sim, base, N_STEPS, gpu.FP64, 25, SE)
+    loss = ((curve - torch.from_numpy(target)) ** 2).sum()
+    loss.backward()
+    o = orc.Oracle(base, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    o.build_neighbours()
+    o.set_solver(1e-14)
+    curve_o = orc.oracle_forward_record(o, N_STEPS, SE)
+    gD_o, gk_o = orc.oracle_backward(o, 2.0 * (curve_o - target))
+    ref = np.concatenate([gD_o, [gk_o]])
+    got = theta.grad.numpy()
+    assert abs(got[0] - ref[0]) <= 1e-8 * abs(ref[0])
+    assert abs(got[4] - ref[4]) <= 1e-8 * abs(ref[4])
+    # a second call from the reset state gives the same curve
+    curve2 = ag.mass_loss_curve(theta.detach(), sim, base, N_STEPS, gpu.FP64, 25, SE)
+    assert torch.equal(curve.detach(), curve2)
