@@ -308,22 +308,31 @@ def run_ours(args):
     solves = d1["cg_solves"] - d0["cg_solves"]
     launches = solves + 2 * outer + 2 * inner + args.steps
 
-    # kernel roofline: CG SpMV vs transport, CUDA-event timed on the library's stream
+    # kernel roofline: CUDA-event timed launches on the library's stream (state restored)
     with ProfileRange("kernels"):
         t_spmv = sim.time_kernel(1, nn.MIXED, reps=50)
         t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
         t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
+        t_upd = sim.time_kernel(3, nn.MIXED, reps=50)
+    k64 = {"cg_spmv": sim64.time_kernel(1, nn.FP64, reps=20),
+           "transport": sim64.time_kernel(0, nn.FP64, reps=10),
+           "cg_update": sim64.time_kernel(3, nn.FP64, reps=20)}
     spmv_per_step = inner / args.steps
     ir_per_step = outer / args.steps
-    shares = {"cg_spmv": t_spmv * spmv_per_step, "transport": t_tr, "ir_residual": t_ir * ir_per_step}
+    shares = {"cg_spmv": t_spmv * spmv_per_step, "cg_update": t_upd * spmv_per_step,
+              "transport": t_tr, "ir_residual": t_ir * ir_per_step}
     ms_step = ms / args.steps
-    # algorithmic bytes per launch (FP32 values, 4-byte indices)
+    # algorithmic bytes per launch (FP32 values, 4-byte indices; stored per-bond weights are
+    # not algorithmic and are reported separately)
     b = 4
     bytes_spmv = 4 * nnz + 4 * (N + 1) + N * (b + b) + 3 * N * b
     bytes_tr = 4 * nnz + 4 * (N + 1) + N * (4 * b + b + 1 + 3 * 8 + 4 * b)
     bytes_ir = 4 * nnz + 4 * (N + 1) + N * (b + 8 + 8 + 8)
+    bytes_upd = N * b * 6 + N * b
     dom = max(shares, key=shares.get)
-    alg = {"cg_spmv": (bytes_spmv, t_spmv), "transport": (bytes_tr, t_tr), "ir_residual": (bytes_ir, t_ir)}
+    alg = {"cg_spmv": (bytes_spmv, t_spmv), "transport": (bytes_tr, t_tr), "ir_residual": (bytes_ir, t_ir),
+           "cg_update": (bytes_upd, t_upd)}
+    stored = {"cg_spmv": 4 * nnz, "transport": 4 * nnz, "ir_residual": 8 * nnz, "cg_update": 0}
     peak, peak_src = measured_peak()
     tt = traffic_table()
 
@@ -333,12 +342,13 @@ def run_ours(args):
         tr = tt.get(name, {}).get("dram_bytes_per_launch")
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": tr, "kernel": name, "ms_per_launch": t, "algorithmic_bytes": by,
-                "peak_source": peak_src}
+                "stored_weight_bytes": stored[name], "peak_source": peak_src}
 
     roofline = roof(dom)
     roofline["others"] = {k: {kk: v for kk, v in roof(k).items() if kk in ("achieved", "frac", "ms_per_launch", "traffic")}
                           for k in alg if k != dom}
     roofline["share_of_step"] = {k: v / ms_step for k, v in shares.items()}
+    roofline["fp64_path_ms_per_launch"] = k64
 
     # end to end through the public API with host buffers (nnpp_step_host)
     e2e = None

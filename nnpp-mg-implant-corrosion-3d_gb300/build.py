@@ -82,7 +82,26 @@ def build(verbose=False, force=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed\n%s\n%s" % (r.stdout, r.stderr))
+    _build_driver(verbose)
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "driver", "nnpp_run.cpp")
+DRIVER = os.path.join(HERE, "nnpp_run")
+
+
+def _build_driver(verbose):
+    """The C++ job-file driver, linked against the library (rpath $ORIGIN)."""
+    if not _stale(DRIVER, [DRIVER_SRC, LIB, os.path.join(INCLUDE, "nnpp_gb300.h")]):
+        return DRIVER
+    cmd = ["g++"] + CXX_FLAGS + [DRIVER_SRC, "-o", DRIVER, "-L", HERE, "-lnnpp_gb300",
+                                 "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed\n%s\n%s" % (r.stdout, r.stderr))
+    return DRIVER
 
 
 if __name__ == "__main__":

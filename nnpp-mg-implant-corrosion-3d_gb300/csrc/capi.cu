@@ -515,9 +515,10 @@ nnpp_status nnpp_residuals(nnpp_handle* hp, int precision, const double* c, cons
   OneView ov;
   if (st == NNPP_OK && !Fd.alloc((S + 1) * (size_t)h.N)) st = set_error(NNPP_ERR_NOMEM, "residual output");
   if (st == NNPP_OK) {
-    NNPP_CUDA(cudaMemcpyAsync(h.scratch_d.get(), &voln1rel, sizeof(double), cudaMemcpyHostToDevice, h.st));
+    const double bv = std::pow(10., -h.p.vol_red * (1. - voln1rel));  // utils.h:100-116
+    NNPP_CUDA(cudaMemcpyAsync(h.scratch_d.get(), &bv, sizeof(double), cudaMemcpyHostToDevice, h.st));
     KParams kp = make_kparams(h, h.cur);
-    kp.voln1rel_ptr = h.scratch_d.get();
+    kp.bv_ptr = h.scratch_d.get();
     st = one_view(h, kp, ov);
     if (st == NNPP_OK) st = launch_transport_b(*h.engine, ov.v, precision, h.st, Fd.get());
     if (st == NNPP_OK) st = launch_prep_b(*h.engine, ov.v, precision, h.st, 0, Fd.get() + (size_t)S * h.N);
@@ -595,7 +596,7 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
                              double* ms_per_launch) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
-  if (reps < 1 || !ms_per_launch || kernel_id < 0 || kernel_id > 2)
+  if (reps < 1 || !ms_per_launch || kernel_id < 0 || kernel_id > 3)
     return set_error(NNPP_ERR_INVALID, "time_kernel: bad argument");
   if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
   Handle& h = hp->h;
@@ -620,6 +621,8 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
     ds.outer_active = 1;
     ds.inner_active = 1;
     cudaMemcpyAsync(&h.dstate.get()->outer_active, &ds.outer_active, 2 * sizeof(int), cudaMemcpyHostToDevice, h.st);
+    static const double zero = 0.0;  // the CG update's stop test must not end the repetitions
+    cudaMemcpyAsync(&h.dstate.get()->inner_target, &zero, sizeof(double), cudaMemcpyHostToDevice, h.st);
   }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -627,6 +630,7 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
   auto one = [&]() -> nnpp_status {
     if (kernel_id == 0) return launch_transport_b(e, v, precision, h.st, nullptr);
     if (kernel_id == 1) return launch_cg_spmv_b(e, v, precision, h.st);
+    if (kernel_id == 3) return launch_cg_update_b(e, v, precision, h.st, 0);
     return launch_ir_update_b(e, v, precision, h.st, 0);
   };
   for (int w = 0; w < 3 && st == NNPP_OK; ++w) st = one();

@@ -56,6 +56,7 @@ struct DevState {
   long long solid_count;
   double voln1rel;
   double vol0rel;
+  double BV;  // 10^(-vol_red (1 - voln1rel)), refreshed with voln1rel
   double mass[S];
   double mg_mass_t0;
   double dissolved;

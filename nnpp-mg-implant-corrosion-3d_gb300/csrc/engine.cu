@@ -2,6 +2,7 @@
 // (bins per tile T, lanes per node W), CUDA-graph capture of the step with device-side loop
 // control (conditional while nodes) and the run loop.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -196,6 +197,38 @@ nnpp_status capture_solve(Engine& e, const EngineView& v, int prec) {
   return NNPP_OK;
 }
 
+// Eager form of capture_solve for profilers that cannot see into graphs with conditional
+// nodes: the same kernels launched one at a time, the two loops driven by the host from the
+// members' active flags.
+nnpp_status any_active(Engine& e, int which, bool* any) {
+  *any = false;
+  std::vector<int> f(2 * e.members.size());
+  for (size_t i = 0; i < e.members.size(); ++i)
+    NNPP_CUDA(cudaMemcpyAsync(&f[2 * i], &e.members[i]->dstate.get()->outer_active, 2 * sizeof(int),
+                              cudaMemcpyDeviceToHost, e.st));
+  NNPP_CUDA(cudaStreamSynchronize(e.st));
+  for (size_t i = 0; i < e.members.size(); ++i) *any = *any || f[2 * i + which] != 0;
+  return NNPP_OK;
+}
+
+nnpp_status eager_solve(Engine& e, const EngineView& v, int prec) {
+  NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
+  bool go = false;
+  for (int outer = 0; outer < (1 << 20); ++outer) {
+    NNPP_TRY(any_active(e, 0, &go));
+    if (!go) break;
+    NNPP_TRY(launch_cg_init_b(e, v, prec, e.st, 0));
+    for (int inner = 0; inner < (1 << 24); ++inner) {
+      NNPP_TRY(any_active(e, 1, &go));
+      if (!go) break;
+      NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+      NNPP_TRY(launch_cg_update_b(e, v, prec, e.st, 0));
+    }
+    NNPP_TRY(launch_ir_update_b(e, v, prec, e.st, 0));
+  }
+  return NNPP_OK;
+}
+
 nnpp_status build_graph(Engine& e, int kind, int prec) {
   if (e.gexec[kind][prec][0]) return NNPP_OK;
   NNPP_CUDA(cudaStreamBeginCapture(e.st, cudaStreamCaptureModeThreadLocal));
@@ -301,6 +334,8 @@ nnpp_status engine_build(Engine& e) {
   if (sms <= 0) sms = 152;
   e.sms = sms;
   e.grid = sms * 4;
+  const char* eager = std::getenv("NNPP_EAGER");
+  e.eager = eager && std::atoi(eager) != 0;
   NNPP_TRY(build_lists(e, e.T));
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, e.W));
   return NNPP_OK;
@@ -308,6 +343,17 @@ nnpp_status engine_build(Engine& e) {
 
 nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
   if (!prepared) NNPP_TRY(prepare_run(e, prec));
+  if (e.eager) {
+    for (int s = 0; s < n_steps; ++s) {
+      EngineView v = make_view(e, 0, 0);
+      NNPP_TRY(eager_solve(e, v, prec));
+      NNPP_TRY(launch_transport_b(e, v, prec, e.st, nullptr));
+      for (Handle* h : e.members) h->cur ^= 1;
+      NNPP_TRY(refresh_params(e));
+    }
+    NNPP_CUDA(cudaStreamSynchronize(e.st));
+    return NNPP_OK;
+  }
   int done = 0;
   if (n_steps >= 2) NNPP_TRY(build_graph(e, kGraphStep2, prec));
   if (n_steps % 2) NNPP_TRY(build_graph(e, kGraphStep1, prec));
@@ -326,6 +372,7 @@ nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
 
 nnpp_status engine_warm(Engine& e, int prec) {
   NNPP_TRY(prepare_run(e, prec));
+  if (e.eager) return NNPP_OK;
   NNPP_TRY(build_graph(e, kGraphStep2, prec));
   NNPP_TRY(build_graph(e, kGraphStep1, prec));
   return NNPP_OK;
@@ -335,6 +382,11 @@ nnpp_status engine_params(Engine& e) { return refresh_params(e); }
 
 nnpp_status engine_solve(Engine& e, int prec) {
   NNPP_TRY(prepare_run(e, prec));
+  if (e.eager) {
+    NNPP_TRY(eager_solve(e, make_view(e, 0, 0), prec));
+    NNPP_CUDA(cudaStreamSynchronize(e.st));
+    return NNPP_OK;
+  }
   NNPP_TRY(build_graph(e, kGraphSolve, prec));
   NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphSolve][prec][0], e.st));
   NNPP_CUDA(cudaStreamSynchronize(e.st));

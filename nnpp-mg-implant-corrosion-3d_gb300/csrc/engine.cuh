@@ -54,6 +54,7 @@ struct Engine {
   int T = 4;                // bins per tile (autotuned)
   int W = 8;                // lanes per node (autotuned)
   bool tuned = false;
+  bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
   int grid = 0;
   int sms = 152;
   int halo_max = 0;

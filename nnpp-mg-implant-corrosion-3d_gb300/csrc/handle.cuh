@@ -43,7 +43,7 @@ struct KParams {
   float *rin32, *z32, *p32, *q32, *e32;
   double *rin64, *z64, *p64, *q64, *e64;
   DevState* ds;
-  const double* voln1rel_ptr;    // value entering BV (ds->voln1rel, or an override)
+  const double* bv_ptr;          // interface factor BV (ds->BV, or an override)
   const double* b_override;      // right-hand side of the potential solve instead of
                                  // (1/(K sigma)) F CSolid sum_k z_k c_k (adjoint solves)
   // physics

@@ -375,54 +375,33 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
     double part[1] = {0.0};
     if (active) {
       load_tile(t, ts);
-      float4* hs = reinterpret_cast<float4*>(dsm);
-      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + sizeof(float4) * (size_t)t.halo);
-      const float4* posrec = k.posrec;
+      float* hs = reinterpret_cast<float*>(dsm);
+      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(float) * (size_t)t.halo));
       const float* z = k.z32;
-      const float h = k.h32;
-      for (int s = threadIdx.x; s < t.halo; s += kBlock) {
-        const int n = halo_node(ts, s);
-        const float4 pr = posrec[n];
-        const int pb = __float_as_int(pr.w);
-        float4 o;
-        o.x = fmaf((float)((pb & 1023) - t.cb[0]), h, pr.x);
-        o.y = fmaf((float)(((pb >> 10) & 1023) - t.cb[1]), h, pr.y);
-        o.z = fmaf((float)(((pb >> 20) & 1023) - t.cb[2]), h, pr.z);
-        o.w = z[n];
-        hs[s] = o;
-      }
+      for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = z[halo_node(ts, s)];
       __syncthreads();
       const int* row = k.row;
       const unsigned char* freem = k.freem;
+      const float* w32 = k.w32;
       float* p = k.p32;
       float* q = k.q32;
       const float beta = (float)k.ds->beta;
-      const float dlo = k.delta_lo, dhi = k.delta_hi, idx = k.inv_dx, dV = k.dVf;
       const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
       for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
         const int a = a0 + seg;
         const bool act = a < t.own_end && freem[a];
-        float acc = 0.0f;
-        float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+        float acc = 0.0f, za = 0.0f;
         if (act) {
-          me = hs[own0 + (a - t.own_begin)];
-          for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-            const float4 o = hs[sslot[j - t.bond0]];
-            const float dx = o.x - me.x, dy = o.y - me.y, dz = o.z - me.z;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float ri = rsqrtf(r2);
-            const float xi = r2 * ri;
-            const float bt = xi <= dlo ? 1.0f : (xi <= dhi ? (dhi - xi) * idx : 0.0f);
-            const float w = bt * dV * ri * ri * ri;
-            acc = fmaf(w, o.w, acc);
-          }
+          za = hs[own0 + (a - t.own_begin)];
+          const int j1 = row[a + 1];
+          for (int j = row[a] + sub; j < j1; j += W) acc = fmaf(__ldg(w32 + j), hs[sslot[j - t.bond0]], acc);
         }
 #pragma unroll
         for (int off = W / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, W);
         if (act && sub == 0) {
-          const float s = k.d32[a] * me.w - acc;
+          const float s = k.d32[a] * za - acc;
           const float qn = s + beta * q[a];
-          const float pn = me.w + beta * p[a];
+          const float pn = za + beta * p[a];
           q[a] = qn;
           p[a] = pn;
           part[0] += (double)pn * (double)qn;
@@ -653,8 +632,10 @@ __device__ __forceinline__ void transport_finish(const EngineView& v, const Tile
     if (k.dissolve_count) ds->dissolved += tot[6];
     if (tot[7] != 0.0) ds->nonfinite = 1;
     ds->mg_mass_now = tot[0];
-    if (k.sub_step_no > 0 && ds->steps % k.sub_step_no == 0)
+    if (k.sub_step_no > 0 && ds->steps % k.sub_step_no == 0) {
       ds->voln1rel = ds->vol0rel != 0.0 ? tot[5] / ds->vol0rel : 0.0;
+      ds->BV = pow(10., -k.vol_red * (1. - ds->voln1rel));  // utils.h:100-116
+    }
   }
 }
 
@@ -699,8 +680,7 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
       hph[s] = b.z;
     }
     __syncthreads();
-    const double voln1rel = *k.voln1rel_ptr;
-    const double BV = pow(10., -k.vol_red * (1. - voln1rel));
+    const double BV = *k.bv_ptr;
     float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) {
@@ -846,8 +826,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
       hrec[(size_t)(S + 1) * H + s] = r.phase;
     }
     __syncthreads();
-    const double voln1rel = *k.voln1rel_ptr;
-    const double BV = pow(10., -k.vol_red * (1. - voln1rel));
+    const double BV = *k.bv_ptr;
     double cLL[S], cX[S], cSS[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) {
@@ -1084,6 +1063,7 @@ __global__ void k_init_diag(KParams k, int mixed, double* partials) {
     ds->solid_count = (long long)tot[4];
     ds->vol0rel = tot[5];
     ds->voln1rel = 0.0;
+    ds->BV = pow(10., -k.vol_red);
   }
 }
 
@@ -1112,7 +1092,7 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
 
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
-size_t smem_spmv32(int H, int B) { return (size_t)H * sizeof(float4) + smem_slots(B); }
+size_t smem_spmv32(int H, int B) { return align16((size_t)H * sizeof(float)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
 size_t smem_tr32(int H, int B) { return align16((size_t)28 * H) + smem_slots(B); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
@@ -1556,7 +1536,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.q64 = h.q64.get();
   k.e64 = h.e64.get();
   k.ds = h.dstate.get();
-  k.voln1rel_ptr = &h.dstate.get()->voln1rel;
+  k.bv_ptr = &h.dstate.get()->BV;
   k.b_override = h.b_override;
   k.dt = p.dt;
   k.csat = p.CSat / p.CSolid;

@@ -1,0 +1,104 @@
+"""The C++ job-file driver (nnpp_run): synthetic jobs written in the reference's input layout
+read back exactly (CPU), and a run of the driver on such a job matches the FP64 oracle (GPU)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import PKG_DIR
+
+DRIVER = os.path.join(PKG_DIR, "nnpp_run")
+
+
+def _driver():
+    if not os.path.exists(DRIVER):
+        pytest.fail("nnpp_run has not been built (build.py builds it with the library)")
+    return DRIVER
+
+
+def _load(path, dtype=float):
+    return np.loadtxt(path, dtype=dtype)
+
+
+def _write(job, kind, n, seed, steps):
+    r = subprocess.run([_driver(), "--write-synth", str(kind), str(n), str(seed), job,
+                        "--steps", str(steps)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+
+
+def test_write_synth_reads_back_exactly(nn, tmp_path):
+    job = str(tmp_path / "SYN")
+    _write(job, 1, 8, 3, 40)
+    inp = nn.synth(1, 8, 3)
+    N = inp["N"]
+    d1 = _load(job + ".data1", int)
+    assert d1[0] == N and d1[1] == 40 and d1[3] == 0
+    assert d1[2] == int((inp["bctypes"] == 0).sum())
+    nodes = _load(job + ".nodes")
+    assert nodes.shape == (N, 3)
+    assert np.array_equal(nodes, np.asarray(inp["nodes"]).reshape(3, N).T)
+    assert np.array_equal(_load(job + ".bctypes", int), inp["bctypes"])
+    assert np.array_equal(_load(job + ".phase0", int), inp["phase0"])
+    bcv = np.asarray(inp["bcvalues"]).reshape(5, N)
+    icv = np.asarray(inp["icvalues"]).reshape(5, N)
+    for f in range(1, 12):
+        src = f - 1 if f <= 4 else (4 if f == 11 else None)
+        b = _load(job + ".bcvalues%d" % f)
+        i = _load(job + ".icvalues%d" % f)
+        if src is None:
+            assert np.all(b == -1) and np.all(i == 0)
+        else:
+            assert np.array_equal(b, bcv[src]) and np.array_equal(i, icv[src])
+    # the parameter files give back the same parameters through the reference-vector entry point
+    d2 = _load(job + ".data2")
+    dc = [_load(job + ".datac%d" % c) for c in range(1, 5)]
+    d11 = _load(job + ".datac11")
+    p = nn.params_from_reference(d2, np.array(dc), d11)
+    q = inp["params"]
+    for name in ("dt", "dx", "dy", "dz", "delta", "CSolid", "CSat", "F", "R", "T", "vol_red",
+                 "sigma", "s_phi", "K_phi"):
+        assert getattr(p, name) == getattr(q, name), name
+    for name in ("z", "D_solid", "D_liquid", "s1", "s2", "K1", "K2"):
+        assert list(getattr(p, name)) == list(getattr(q, name)), name
+
+
+def test_usage_errors():
+    r = subprocess.run([_driver()], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr
+    r = subprocess.run([_driver(), "--write-synth", "9", "8", "1", "/nonexistent/x"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0
+
+
+@pytest.mark.gpu
+def test_driver_run_matches_oracle(nn, orc, tmp_path):
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    job = str(tmp_path / "SYN")
+    steps = 40
+    _write(job, 1, 12, 7, steps)
+    r = subprocess.run([_driver(), "-fp64", job, "--precision", "fp64", "--tol", "1e-12"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    inp = nn.synth(1, 12, 7)
+    p = inp["params"].copy()
+    p.k_diss = 0.05
+    p.switch_width = 0.0
+    o = orc.Oracle(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    o.forward(steps)
+    c, phi, ph, _ = o.state()
+    out = np.loadtxt(job + "-fp64-%d.output.csv" % steps, delimiter=",", skiprows=1)
+    with open(job + "-fp64-%d.output.csv" % steps) as f:
+        assert f.readline().strip().split(",")[:4] == ["X", "Y", "Z", "Mg++"]
+    N = inp["N"]
+    assert out.shape == (N, 15)
+    assert np.array_equal(out[:, 14].astype(int), ph)
+    for k in range(4):
+        assert np.linalg.norm(out[:, 3 + k] - c[k]) <= 1e-10 * np.linalg.norm(c[k])
+    assert np.linalg.norm(out[:, 13] - phi) <= 1e-9 * np.linalg.norm(phi)
+    vol = [float(x.strip().rstrip(",")) for x in open(job + "-fp64.volume") if x.strip()]
+    assert len(vol) == steps // 8
+    assert len(open(job + "-fp64.energy").read().split()) == steps // 8
