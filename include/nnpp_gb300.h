@@ -205,6 +205,15 @@ nnpp_status nnpp_set_params(nnpp_handle* h, const nnpp_params* p);
  * the CG (default 2000), strict != 0 turns a capped solve into NNPP_ERR_CG_NO_CONVERGE. */
 nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict);
 
+/* Initial guess of each potential solve.  history 0: the previous potential (the
+ * reference's warm start, main.cpp:764-779); 1 or 2: linear extrapolation 2 phi^n -
+ * phi^{n-1}; 3..6 (default 6): the combination of the last `history` potentials and their
+ * divided differences that minimises the energy-norm error (a Galerkin projection onto the
+ * history, using the stored images A phi = b - r of earlier solves; no extra operator
+ * application).  Only the iteration count depends on it: every solve still runs to the
+ * solver tolerance.  Discards a recorded forward_ckpt run. */
+nnpp_status nnpp_set_warm_start(nnpp_handle* h, int history);
+
 /* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
  * NULL. */
 nnpp_status nnpp_get_state(nnpp_handle* h, double* c, double* phi, int* phase);

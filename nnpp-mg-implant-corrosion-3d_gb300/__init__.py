@@ -102,6 +102,7 @@ _SIGS = {
     "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP]),
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
+    "nnpp_set_warm_start": (C.c_int, [_P, C.c_int]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -285,6 +286,11 @@ class Simulation:
         cols = np.empty(max(nnz.value, 1), dtype=np.int32)
         _check(lib().nnpp_get_neighbours_csr(self._h, _ip(ptr), _ip(cols), C.byref(nnz)))
         return ptr, cols[:nnz.value]
+
+    def set_warm_start(self, history):
+        """Initial guess of the potential solves: 0 previous potential, 1-2 linear
+        extrapolation, 3-6 energy-norm-optimal combination of that many past potentials."""
+        _check(lib().nnpp_set_warm_start(self._h, history))
 
     def reset(self):
         """Back to the initial state of build_neighbours (lists and tuning kept)."""

@@ -8,7 +8,8 @@
 // transposed bond sums (k_adj_transport), the adjoint potential solve A psi = nu through the
 // same batched solver (right-hand side overridden) and the combination
 // lambda^n = mu + (1/(K sigma)) F CSolid z_k psi.  Memory: (ck + 1) snapshots of 64 bytes per
-// node plus one checkpoint per segment.
+// node plus one checkpoint per segment (state, and the warm-start history so that the
+// recomputed solves start from the same guesses).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -28,8 +29,14 @@ nnpp_status save_ckpt(Handle& h, Handle::Ckpt& c) {
   if (!c.rec32.alloc(N) || !c.clo.alloc(N) || !c.rec64.alloc(N) || !c.phi.alloc(N) ||
       !c.phi_prev.alloc(N) || !c.flip.alloc(N))
     return set_error(NNPP_ERR_NOMEM, "checkpoint");
+  const size_t HN = h.xh.get() ? (size_t)h.warm_hist * N : 0;
+  if (HN && (!c.xh.alloc(HN) || !c.bh.alloc(HN))) return set_error(NNPP_ERR_NOMEM, "checkpoint history");
   c.cur = h.cur;
   c.prec = h.state_prec;
+  if (HN) {
+    NNPP_CUDA(cudaMemcpyAsync(c.xh.get(), h.xh.get(), sizeof(double) * HN, cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(c.bh.get(), h.bh.get(), sizeof(double) * HN, cudaMemcpyDeviceToDevice, h.st));
+  }
   NNPP_CUDA(cudaMemcpyAsync(c.rec32.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(c.clo.get(), h.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(c.rec64.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
@@ -45,6 +52,11 @@ nnpp_status load_ckpt(Handle& h, const Handle::Ckpt& c) {
   const size_t N = h.N;
   h.cur = c.cur;
   h.state_prec = c.prec;
+  const size_t HN = h.xh.get() ? (size_t)h.warm_hist * N : 0;
+  if (HN && c.xh.get()) {
+    NNPP_CUDA(cudaMemcpyAsync(h.xh.get(), c.xh.get(), sizeof(double) * HN, cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(h.bh.get(), c.bh.get(), sizeof(double) * HN, cudaMemcpyDeviceToDevice, h.st));
+  }
   NNPP_CUDA(cudaMemcpyAsync(h.rec32[h.cur].get(), c.rec32.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.clo.get(), c.clo.get(), sizeof(float4) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.rec64[h.cur].get(), c.rec64.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));

@@ -650,6 +650,35 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
   return st != NNPP_OK ? st : st2;
 }
 
+nnpp_status nnpp_set_warm_start(nnpp_handle* hp, int history) {
+  NNPP_GUARD(hp);
+  if (history < 0 || history > kHistMax)
+    return set_error(NNPP_ERR_INVALID, "warm start history must be in [0, 6]");
+  Handle& h = hp->h;
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.extrapolate = history >= 1 ? 1 : 0;
+  h.warm_hist = history >= 3 ? history : 0;
+  h.xh.reset();
+  h.bh.reset();
+  if (h.warm_hist && h.built) {
+    const size_t HN = (size_t)h.warm_hist * h.N;
+    if (!h.xh.alloc(HN) || !h.bh.alloc(HN)) return set_error(NNPP_ERR_NOMEM, "warm-start history");
+  }
+  h.fwd_steps = 0;
+  h.ckpts.clear();
+  if (h.built) {
+    static const int zero = 0;
+    NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->hist_n, &zero, sizeof(int), cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->hist_head, &zero, sizeof(int), cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+  }
+  if (h.engine) {
+    engine_destroy_graphs(*h.engine);
+    NNPP_TRY(engine_params(*h.engine));
+  }
+  return NNPP_OK;
+}
+
 nnpp_status nnpp_reset(nnpp_handle* hp) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);

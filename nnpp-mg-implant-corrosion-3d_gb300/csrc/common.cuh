@@ -13,7 +13,8 @@
 namespace nnpp {
 
 constexpr int S = NNPP_NSPECIES;
-constexpr int kReduceSlots = 16;   // values reduced per block by the step kernels
+constexpr int kReduceSlots = 24;   // values reduced per block by the step kernels
+constexpr int kHistMax = 6;        // potentials kept for the warm start of the solve
 constexpr int kMaxPartialBlocks = 4096;
 
 // CUDA call check inside functions returning nnpp_status.
@@ -89,6 +90,13 @@ struct DevState {
   double mg_mass_now;
   // adjoint accumulators: dL/dD_liquid[0..3], dL/dk_diss
   double adj_g[5];
+  // warm start of the potential solve from the last hist_n solutions (ring, newest at
+  // hist_head): coefficients of their divided differences for the next initial guess
+  int hist_n;
+  int hist_head;
+  int warm_nd;        // differences used by the next guess (0: keep the extrapolation)
+  int pad2;
+  double warm_coef[kHistMax];
   // block tickets for last-block reductions
   unsigned int ticket[8];
 };

@@ -171,13 +171,14 @@ nnpp_status add_while(cudaStream_t st, cudaGraphConditionalHandle hc, cudaGraph_
   return NNPP_OK;
 }
 
-// prep; while(outer) { cg_init; while(inner) { spmv; update }; ir_update }
+// warm start; prep; while(outer) { cg_init; while(inner) { spmv; update }; ir_update }
 nnpp_status capture_solve(Engine& e, const EngineView& v, int prec) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t g = nullptr;
   NNPP_CUDA(cudaStreamGetCaptureInfo(e.st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
   cudaGraphConditionalHandle hout;
   NNPP_CUDA(cudaGraphConditionalHandleCreate(&hout, g, 0, 0));
+  NNPP_TRY(launch_warm_b(e, v, prec, e.st));
   NNPP_TRY(launch_prep_b(e, v, prec, e.st, hout, nullptr));
   cudaGraph_t body_out;
   NNPP_TRY(add_while(e.st, hout, &body_out));
@@ -212,6 +213,7 @@ nnpp_status any_active(Engine& e, int which, bool* any) {
 }
 
 nnpp_status eager_solve(Engine& e, const EngineView& v, int prec) {
+  NNPP_TRY(launch_warm_b(e, v, prec, e.st));
   NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
   bool go = false;
   for (int outer = 0; outer < (1 << 20); ++outer) {

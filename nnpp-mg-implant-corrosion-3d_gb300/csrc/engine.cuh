@@ -47,7 +47,7 @@ struct EngineView {
   int bond_max;             // largest staged bond range of a tile (bond1 - bond0)
 };
 
-constexpr int kChunk = 4096;  // nodes per elementwise work item
+constexpr int kChunk = 1024;  // nodes per elementwise work item
 
 struct Engine {
   std::vector<Handle*> members;
@@ -89,6 +89,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
                         int* bond_max);
 
 // step.cu launchers (batched)
+nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out);
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,

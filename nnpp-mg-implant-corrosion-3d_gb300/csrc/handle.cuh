@@ -19,7 +19,6 @@ struct KParams {
   const int* row;
   const int* col;
   const unsigned short* slot16;  // per bond: halo slot of the neighbour within its tile
-  const float4* posrec;          // per node: {x, y, z offsets within its bin, packed bin}
   const double* w64;
   const float* w32;
   const unsigned char* dirmask;  // bit k: species k Dirichlet, bit S: potential Dirichlet
@@ -49,12 +48,13 @@ struct KParams {
   // physics
   double dt, csat, c_floor, k_diss, sw, vol_red, lam;
   double K1[S], K2zF[S], DL[S], DSo[S], z[S];
-  float h32;                     // bin side
-  float delta_lo, delta_hi, inv_dx, dVf;  // FP32 weight recompute: beta and dV
   int sub_step_no;
   int dissolve_count;            // 1: count the dissolution source into the diagnostics
   int extrapolate;               // 1: warm start phi = 2 phi^n - phi^{n-1}
-  int pad1;
+  int hist_m;                    // >= 3: A-norm-optimal warm start from the last hist_m
+                                 // solutions (history ring xh, bh = A xh); 0: off
+  double* xh;                    // hist_m * N potentials of previous solves
+  double* bh;                    // hist_m * N: A x of those (b - r at convergence)
 };
 
 enum GraphKind { kGraphStep2 = 0, kGraphStep1 = 1, kGraphSolve = 2, kGraphKinds = 3 };
@@ -106,6 +106,8 @@ struct Handle {
   double inner_rel = 1e-4;
   int strict = 0;
   int extrapolate = 1;
+  int warm_hist = kHistMax;     // history length of the warm start (0: extrapolation only)
+  DBuf<double> xh, bh;          // warm-start history, warm_hist * N each
   const double* b_override = nullptr;  // set during adjoint solves
   int grid = 0;                 // CTAs of the per-handle elementwise kernels
   Engine* engine = nullptr;     // single-instance engine (owned)
@@ -116,6 +118,7 @@ struct Handle {
     DBuf<Rec64> rec64;
     DBuf<double> phi, phi_prev;
     DBuf<int> flip;
+    DBuf<double> xh, bh;
     DevState ds;
     int cur = 0, prec = 0;
   };

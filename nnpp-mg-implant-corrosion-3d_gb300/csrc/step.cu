@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
 }
 
 // q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
-// FP32: the weights are recomputed from the staged tile-relative coordinates.
+// FP32: weights stored per bond (w32), z staged per tile in shared memory.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -537,6 +537,169 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
   }
 }
 
+// ------------------------------------------------------------------- warm start ---------
+// Initial guess of the potential solve from the last H solutions x_n, ..., x_{n-H+1} and
+// their images A x (the ring xh, bh; bh = b - r at the end of each solve):
+//   x0 = x_n + sum_l a_l D^l x_n,   D^l: l-th backward difference at the newest solution,
+// with the coefficients minimising the A-norm error of x0 over that affine space
+// (Galerkin condition  (D^i x)^T A (D^j x) a_j = (D^i x)^T (b_new - A x_n)); A D^l x is the
+// same difference of bh.  The differences are the well-conditioned basis of the span of
+// the history; the linear extrapolation 2 x_n - x_{n-1} is the member a = (1, 0, ...).
+constexpr int kWarmD = kHistMax - 1;                         // differences
+constexpr int kWarmSlots = kWarmD * (kWarmD + 1) / 2 + kWarmD + 1;  // G (upper), rhs, x.Ax
+static_assert(kWarmSlots <= kReduceSlots, "warm-start partials exceed the reduction buffer");
+
+__device__ __forceinline__ int warm_history(const KParams& k) {
+  if (k.hist_m < 3 || !k.extrapolate || k.b_override) return 0;
+  const int n = k.ds->hist_n;
+  return n < k.hist_m ? n : k.hist_m;
+}
+
+// backward differences D^1..D^{H-1} of t[0..H-1] (newest first) into d; t is consumed
+__device__ __forceinline__ void warm_diffs(double (&t)[kHistMax], int H, double (&d)[kWarmD]) {
+#pragma unroll
+  for (int l = 1; l < kHistMax; ++l) {
+#pragma unroll
+    for (int j = 0; j + 1 < kHistMax; ++j)
+      if (j + l < H) t[j] -= t[j + 1];
+    d[l - 1] = l < H ? t[0] : 0.0;
+  }
+}
+
+// Solve the scaled Galerkin system by Cholesky; differences whose pivot falls below 1e-12
+// (near-dependent) or whose A-norm is below 1e-12 of the solution's (rounding level) end
+// the basis.  Thread 0 of one CTA.
+__device__ void warm_solve(const double (&tot)[kWarmSlots], int nd, DevState* ds) {
+  double G[kWarmD][kWarmD], r[kWarmD], d[kWarmD], L[kWarmD][kWarmD], y[kWarmD];
+  int q = 0;
+  for (int i = 0; i < kWarmD; ++i)
+    for (int j = i; j < kWarmD; ++j) G[i][j] = G[j][i] = tot[q++];
+  for (int i = 0; i < kWarmD; ++i) r[i] = tot[q++];
+  const double xax = tot[q];
+  int n = 0;
+  for (int i = 0; i < nd; ++i) {
+    if (!(G[i][i] > 1e-24 * xax) || !isfinite(G[i][i])) break;
+    d[i] = sqrt(G[i][i]);
+    n = i + 1;
+  }
+  int m = 0;
+  for (int j = 0; j < n; ++j) {
+    double sj = 1.0;
+    for (int k2 = 0; k2 < j; ++k2) sj -= L[j][k2] * L[j][k2];
+    if (!(sj > 1e-12)) break;
+    L[j][j] = sqrt(sj);
+    for (int i = j + 1; i < n; ++i) {
+      double si = G[i][j] / (d[i] * d[j]);
+      for (int k2 = 0; k2 < j; ++k2) si -= L[i][k2] * L[j][k2];
+      L[i][j] = si / L[j][j];
+    }
+    m = j + 1;
+  }
+  for (int i = 0; i < m; ++i) {
+    double si = r[i] / d[i];
+    for (int k2 = 0; k2 < i; ++k2) si -= L[i][k2] * y[k2];
+    y[i] = si / L[i][i];
+  }
+  bool ok = m > 0;
+  for (int i = m - 1; i >= 0; --i) {
+    double si = y[i];
+    for (int k2 = i + 1; k2 < m; ++k2) si -= L[k2][i] * y[k2];
+    y[i] = si / L[i][i];
+    ok = ok && isfinite(y[i]);
+  }
+  for (int i = 0; i < kWarmD; ++i) ds->warm_coef[i] = (ok && i < m) ? y[i] / d[i] : 0.0;
+  ds->warm_nd = ok ? m : 0;
+}
+
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
+  __shared__ double sm[kWarmSlots * kBlock / 32];
+  __shared__ int s_last;
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const int H = warm_history(k);
+    double part[kWarmSlots];
+#pragma unroll
+    for (int q = 0; q < kWarmSlots; ++q) part[q] = 0.0;
+    if (H >= 3) {
+      const int head = k.ds->hist_head, m = k.hist_m;
+      const size_t N = (size_t)k.N;
+      for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+        if (!k.freem[a]) continue;
+        double tx[kHistMax], tb[kHistMax];
+#pragma unroll
+        for (int j = 0; j < kHistMax; ++j) {
+          const size_t o = (size_t)((head - j + 2 * m) % m) * N + a;
+          tx[j] = j < H ? k.xh[o] : 0.0;
+          tb[j] = j < H ? k.bh[o] : 0.0;
+        }
+        double R11 = 0.0;
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) R11 += k.z[s2] * conc_of<P>(k, a, s2);
+        const double g = k.lam * R11 - tb[0];
+        const double xax = tx[0] * tb[0];
+        double dx[kWarmD], db[kWarmD];
+        warm_diffs(tx, H, dx);
+        warm_diffs(tb, H, db);
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < kWarmD; ++i)
+#pragma unroll
+          for (int j = i; j < kWarmD; ++j) part[q++] += dx[i] * db[j];
+#pragma unroll
+        for (int i = 0; i < kWarmD; ++i) part[q++] += dx[i] * g;
+        part[q] += xax;
+      }
+    }
+    write_partials<kWarmSlots>(v, item, part, sm);
+    if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
+      double tot[kWarmSlots];
+      reduce_items<kWarmSlots>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        ds->warm_nd = 0;
+        if (H >= 3) warm_solve(tot, H - 1, ds);
+        v.ticket[c.inst] = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// x0 = x_n + sum_l a_l D^l x_n on the unknowns, into phi64 and the state's potential
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_warm_apply(EngineView v) {
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const int H = warm_history(k);
+    if (H < 3) continue;
+    const int nd = k.ds->warm_nd;
+    if (nd <= 0) continue;
+    double coef[kWarmD];
+#pragma unroll
+    for (int i = 0; i < kWarmD; ++i) coef[i] = k.ds->warm_coef[i];
+    const int head = k.ds->hist_head, m = k.hist_m;
+    const size_t N = (size_t)k.N;
+    for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+      if (!k.freem[a]) continue;
+      double tx[kHistMax];
+#pragma unroll
+      for (int j = 0; j < kHistMax; ++j)
+        tx[j] = j < H ? k.xh[(size_t)((head - j + 2 * m) % m) * N + a] : 0.0;
+      const double x = tx[0];
+      double dx[kWarmD];
+      warm_diffs(tx, H, dx);
+      double x0 = x;
+#pragma unroll
+      for (int i = 0; i < kWarmD; ++i) x0 += coef[i] * dx[i];
+      k.phi64[a] = x0;
+      set_phi_rec(k, a, x0, sizeof(P) == 4);
+    }
+  }
+}
+
 // phi += e on the unknowns; FP64 residual r -= A e (FP64 weights); outer stop test.
 template <typename P, int W>
 __global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphConditionalHandle hc) {
@@ -632,11 +795,23 @@ __device__ __forceinline__ void transport_finish(const EngineView& v, const Tile
     if (k.dissolve_count) ds->dissolved += tot[6];
     if (tot[7] != 0.0) ds->nonfinite = 1;
     ds->mg_mass_now = tot[0];
+    if (k.hist_m >= 3) {
+      ds->hist_head = (ds->hist_head + 1) % k.hist_m;
+      ds->hist_n = ds->hist_n < k.hist_m ? ds->hist_n + 1 : k.hist_m;
+    }
     if (k.sub_step_no > 0 && ds->steps % k.sub_step_no == 0) {
       ds->voln1rel = ds->vol0rel != 0.0 ? tot[5] / ds->vol0rel : 0.0;
       ds->BV = pow(10., -k.vol_red * (1. - ds->voln1rel));  // utils.h:100-116
     }
   }
+}
+
+// The solution of this step's solve and its image A x = b - r into the warm-start ring.
+__device__ __forceinline__ void record_history(const KParams& k, int a, int hslot) {
+  if (k.hist_m < 3) return;
+  const size_t o = (size_t)hslot * k.N + a;
+  k.xh[o] = k.phi64[a];
+  k.bh[o] = k.freem[a] ? k.b64[a] - k.r64[a] : 0.0;
 }
 
 // Warm start of the next solve: phi = 2 phi^n - phi^{n-1} on the unknowns (phi_prev keeps
@@ -692,6 +867,7 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     }
     const float dtf = (float)k.dt;
     const long long step_no = k.ds->steps + 1;
+    const int hslot = k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0;
     const int* row = k.row;
     const float* w32 = k.w32;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
@@ -778,6 +954,7 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
         pnew = 0.0f;
         k.flip_step[a] = (int)step_no;
       }
+      record_history(k, a, hslot);
       const double g = next_phi_guess(k, a);
       Rec32 out;
 #pragma unroll
@@ -835,6 +1012,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
       cSS[s] = s == 0 ? k.DSo[0] : 0.0;
     }
     const long long step_no = k.ds->steps + 1;
+    const int hslot = k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0;
     const int* row = k.row;
     const double* w64 = k.w64;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
@@ -908,6 +1086,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
         pnew = 0.0;
         k.flip_step[a] = (int)step_no;
       }
+      record_history(k, a, hslot);
       const double g = next_phi_guess(k, a);
       Rec64 out;
 #pragma unroll
@@ -934,6 +1113,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
 __global__ void k_load_state(KParams k, const int* perm, const double* c_user, const double* phi_user,
                              const int* phase_user, int mixed, int dirichlet_phi) {
   const int N = k.N;
+  if (blockIdx.x == 0 && threadIdx.x == 0) k.ds->hist_n = 0;  // a new state: no history
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
     const int u = perm[a];
     double c[S];
@@ -1384,6 +1564,18 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
   });
 }
 
+nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
+  if (prec == NNPP_MIXED) {
+    k_warm_dots<float><<<occ_grid(k_warm_dots<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+    k_warm_apply<float><<<occ_grid(k_warm_apply<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+  } else {
+    k_warm_dots<double><<<occ_grid(k_warm_dots<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+    k_warm_apply<double><<<occ_grid(k_warm_apply<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+  }
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out) {
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
@@ -1478,6 +1670,7 @@ nnpp_status step_alloc(Handle& h) {
             h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.dstate.alloc(1) &&
             h.scratch_d.alloc(16 + 7 * 4096) && h.user_stage.alloc((S + 1) * N) &&
             h.user_stage_i.alloc(N);
+  if (ok && h.warm_hist >= 3) ok = h.xh.alloc((size_t)h.warm_hist * N) && h.bh.alloc((size_t)h.warm_hist * N);
   if (!ok) return set_error(NNPP_ERR_NOMEM, "device state allocation");
   NNPP_CUDA(cudaMemsetAsync(h.freem.get(), 0, N, h.st));
   NNPP_CUDA(cudaMemsetAsync(h.rec32[1].get(), 0, N * sizeof(Rec32), h.st));
@@ -1505,7 +1698,6 @@ KParams make_kparams(Handle& h, int cur) {
   k.row = h.lay.row.get();
   k.col = h.lay.col.get();
   k.slot16 = h.slot16.get();
-  k.posrec = h.posrec.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
   k.dirmask = h.dirmask.get();
@@ -1552,14 +1744,12 @@ KParams make_kparams(Handle& h, int cur) {
     k.DSo[s] = p.D_solid[s];
     k.z[s] = p.z[s];
   }
-  k.h32 = h.h32;
-  k.delta_lo = (float)(p.delta - p.dx / 2.0);
-  k.delta_hi = (float)(p.delta + p.dx / 2.0);
-  k.inv_dx = (float)(1.0 / p.dx);
-  k.dVf = (float)(p.dx * p.dy * p.dz);
   k.sub_step_no = p.sub_step_no;
   k.dissolve_count = 1;
   k.extrapolate = h.extrapolate;
+  k.hist_m = (h.extrapolate && h.warm_hist >= 3 && h.xh.get()) ? h.warm_hist : 0;
+  k.xh = h.xh.get();
+  k.bh = h.bh.get();
   return k;
 }
 

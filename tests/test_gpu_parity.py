@@ -290,3 +290,38 @@ def test_ensemble_matches_individual_runs(gpu):
     sims[0].forward(2, nn.MIXED)
     assert sims[0].diagnostics()["steps_done"] == 42
     ens.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_warm_start_modes_agree_and_history_saves_iterations(gpu, prec):
+    """The warm start changes only the iteration count: after 60 steps every mode gives the
+    same state to the solver tolerance, and the history projection needs fewer CG
+    iterations than the linear extrapolation."""
+    nn = gpu
+    inp = nn.synth(1, 24, seed=4)
+    out = {}
+    for mode in (0, 1, 6):
+        sim = nn.Simulation.from_synth(inp)
+        sim.build_neighbours()
+        sim.set_warm_start(mode)
+        sim.set_solver(1e-11)
+        sim.forward(60, prec)
+        out[mode] = (sim.state(), sim.diagnostics())
+    (c1, phi1, ph1), d1 = out[1]
+    for mode in (0, 6):
+        (c, phi, ph), d = out[mode]
+        assert np.array_equal(ph, ph1)
+        assert np.linalg.norm(c - c1) <= 1e-8 * np.linalg.norm(c1)
+        assert np.linalg.norm(phi - phi1) <= 1e-8 * np.linalg.norm(phi1)
+        assert d["cg_not_converged"] == 0
+    assert out[6][1]["cg_iterations_total"] < 0.8 * out[1][1]["cg_iterations_total"]
+    assert out[1][1]["cg_iterations_total"] < out[0][1]["cg_iterations_total"]
+
+
+def test_warm_start_rejects_bad_history(gpu):
+    nn = gpu
+    inp = nn.synth(1, 12, seed=4)
+    sim = nn.Simulation.from_synth(inp)
+    with pytest.raises(nn.NNPPError) as e:
+        sim.set_warm_start(7)
+    assert e.value.status == 1
