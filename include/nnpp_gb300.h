@@ -225,8 +225,8 @@ nnpp_status nnpp_get_diagnostics(nnpp_handle* h, nnpp_diag* out);
 nnpp_status nnpp_get_flip_steps(nnpp_handle* h, int* flip_step);
 
 /* Host-buffer step, the call a host-side time loop makes: upload c (S*N) and phase (N),
- * run one step with the handle's potential as warm start, download c, phi and phase.
- * in and out buffers may alias. */
+ * run one step with the handle's potential (and its warm-start history) as the initial
+ * guess of the potential solve, download c, phi and phase.  in and out buffers may alias. */
 nnpp_status nnpp_step_host(nnpp_handle* h, int precision, const double* c_in,
                            const int* phase_in, double* c_out, double* phi_out,
                            int* phase_out);

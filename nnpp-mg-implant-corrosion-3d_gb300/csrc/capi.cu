@@ -132,7 +132,7 @@ nnpp_status restore(Handle& h, StateBackup& b) {
 // Upload user-order c (S*N), phi (N, may be NULL), phase (N, may be NULL) into the current
 // buffers in precision prec.
 nnpp_status upload_state(Handle& h, const double* c, const double* phi, const int* phase, int prec,
-                         bool dirichlet_phi = true) {
+                         bool dirichlet_phi = true, bool keep_history = false) {
   const size_t N = h.N;
   NNPP_CUDA(cudaMemcpyAsync(h.user_stage.get(), c, sizeof(double) * S * N, cudaMemcpyHostToDevice, h.st));
   if (phi)
@@ -141,7 +141,7 @@ nnpp_status upload_state(Handle& h, const double* c, const double* phi, const in
     NNPP_CUDA(cudaMemcpyAsync(h.user_stage_i.get(), phase, sizeof(int) * N, cudaMemcpyHostToDevice, h.st));
   if (prec != h.state_prec && !phase) NNPP_TRY(convert_state(h, prec));
   return load_state(h, h.user_stage.get(), phi ? h.user_stage.get() + S * N : nullptr,
-                    phase ? h.user_stage_i.get() : nullptr, prec, dirichlet_phi);
+                    phase ? h.user_stage_i.get() : nullptr, prec, dirichlet_phi, keep_history);
 }
 
 // The initial state (main.cpp:398-420 with the given phase): concentrations and potential
@@ -488,7 +488,7 @@ nnpp_status nnpp_step_host(nnpp_handle* hp, int precision, const double* c_in, c
   Handle& h = hp->h;
   DevState before;
   NNPP_TRY(read_state(h, &before));
-  NNPP_TRY(upload_state(h, c_in, nullptr, phase_in, precision));
+  NNPP_TRY(upload_state(h, c_in, nullptr, phase_in, precision, true, true));
   NNPP_TRY(engine_run(*h.engine, 1, precision));
   const size_t N = h.N;
   NNPP_TRY(store_state(h, h.user_stage.get(), h.user_stage.get() + S * N, h.user_stage_i.get()));

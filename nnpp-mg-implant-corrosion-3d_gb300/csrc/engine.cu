@@ -110,7 +110,7 @@ nnpp_status tune(Engine& e, int prec) {
   NNPP_CUDA(cudaStreamSynchronize(e.st));
   for (size_t i = 0; i < e.members.size(); ++i)
     NNPP_CUDA(cudaMemcpy(&saved[i], e.members[i]->dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost));
-  const int Ts[3] = {2, 4, 8};
+  const int Ts[4] = {2, 4, 8, 16};
   const int Ws[3] = {4, 8, 16};
   float best = 1e30f;
   int bT = 4, bW = 8;

@@ -18,7 +18,8 @@ struct TileDesc {
   int hb[9];               // halo row r: nodes [hb[r], hb[r] + hl[r])
   int hl[9];
   int halo;                // total halo nodes (sum of hl)
-  int cb[3];               // centre bin (coordinates are staged relative to it)
+  int slice0;              // first 32-row slice of the own nodes (instance's sliced arrays)
+  int pad[2];
   int bond0;               // first bond of the own nodes, rounded down to a multiple of 8
   int bond1;               // one past the last bond of the own nodes
 };

@@ -19,6 +19,11 @@ struct KParams {
   const int* row;
   const int* col;
   const unsigned short* slot16;  // per bond: halo slot of the neighbour within its tile
+  // sliced layout (32 consecutive rows of a tile per slice, bonds column-major within a
+  // slice, rows padded to the slice's longest): {offset, width} per slice, slots, weights
+  const int2* sell_meta;
+  const unsigned short* sell_slot;
+  const float* sell_w;
   const double* w64;
   const float* w32;
   const unsigned char* dirmask;  // bit k: species k Dirichlet, bit S: potential Dirichlet
@@ -78,6 +83,9 @@ struct Handle {
   int max_node_no = 0;
   // tiles (built for tiles_T bins per tile)
   DBuf<unsigned short> slot16;
+  DBuf<int2> sell_meta;
+  DBuf<unsigned short> sell_slot;
+  DBuf<float> sell_w;
   DBuf<float4> posrec;
   float h32 = 0.f;
   int tiles_T = 0;
@@ -135,7 +143,8 @@ KParams make_kparams(Handle& h, int cur);
 // dirichlet_phi: put the boundary values of the potential on its Dirichlet nodes (state
 // for stepping); false keeps the given values (inputs of the residual entry point).
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
-                       const int* d_phase_user, int prec, bool dirichlet_phi);
+                       const int* d_phase_user, int prec, bool dirichlet_phi,
+                       bool keep_history = false);
 nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_phase_user);
 nnpp_status convert_state(Handle& h, int to_prec);
 nnpp_status init_diag(Handle& h);

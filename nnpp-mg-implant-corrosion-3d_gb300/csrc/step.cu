@@ -360,14 +360,15 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
 }
 
 // q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
-// FP32: weights stored per bond (w32), z staged per tile in shared memory.
+// FP32: z of the tile's halo staged in shared memory; each warp streams one 32-row slice of
+// the sliced operator (slots and weights column-major, one coalesced load per bond column).
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ TileSmem ts;
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
-  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
     const TileDesc t = v.tiles[item];
     const KParams& k = v.inst[t.inst];
@@ -376,36 +377,37 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
     if (active) {
       load_tile(t, ts);
       float* hs = reinterpret_cast<float*>(dsm);
-      const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(float) * (size_t)t.halo));
       const float* z = k.z32;
       for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = z[halo_node(ts, s)];
       __syncthreads();
-      const int* row = k.row;
       const unsigned char* freem = k.freem;
-      const float* w32 = k.w32;
       float* p = k.p32;
       float* q = k.q32;
       const float beta = (float)k.ds->beta;
       const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
-      for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
-        const int a = a0 + seg;
-        const bool act = a < t.own_end && freem[a];
-        float acc = 0.0f, za = 0.0f;
-        if (act) {
-          za = hs[own0 + (a - t.own_begin)];
-          const int j1 = row[a + 1];
-          for (int j = row[a] + sub; j < j1; j += W) acc = fmaf(__ldg(w32 + j), hs[sslot[j - t.bond0]], acc);
+      const int nsl = (t.own_end - t.own_begin + 31) >> 5;
+      for (int sl = warp; sl < nsl; sl += kBlock / 32) {
+        const int a = t.own_begin + sl * 32 + lane;
+        if (a >= t.own_end || !freem[a]) continue;
+        const int2 md = k.sell_meta[t.slice0 + sl];
+        const unsigned short* cs = k.sell_slot + md.x + lane;
+        const float* ws = k.sell_w + md.x + lane;
+        float acc0 = 0.0f, acc1 = 0.0f;
+        int c = 0;
+        for (; c + 1 < md.y; c += 2) {
+          const float w0 = __ldg(ws + 32 * c), w1 = __ldg(ws + 32 * c + 32);
+          const int s0 = __ldg(cs + 32 * c), s1 = __ldg(cs + 32 * c + 32);
+          acc0 = fmaf(w0, hs[s0], acc0);
+          acc1 = fmaf(w1, hs[s1], acc1);
         }
-#pragma unroll
-        for (int off = W / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, W);
-        if (act && sub == 0) {
-          const float s = k.d32[a] * za - acc;
-          const float qn = s + beta * q[a];
-          const float pn = za + beta * p[a];
-          q[a] = qn;
-          p[a] = pn;
-          part[0] += (double)pn * (double)qn;
-        }
+        if (c < md.y) acc0 = fmaf(__ldg(ws + 32 * c), hs[__ldg(cs + 32 * c)], acc0);
+        const float za = hs[own0 + (a - t.own_begin)];
+        const float sa = k.d32[a] * za - (acc0 + acc1);
+        const float qn = sa + beta * q[a];
+        const float pn = za + beta * p[a];
+        q[a] = qn;
+        p[a] = pn;
+        part[0] += (double)pn * (double)qn;
       }
     }
     write_partials<1>(v, item, part, sm);
@@ -830,13 +832,15 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
 
 // Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
 // (single instance) and change nothing; otherwise advance the state into rec32_nxt / clo.
+// The tile's halo records are staged in shared memory; each warp streams one 32-row slice
+// of the sliced operator, one lane per node, so the per-node update runs on full warps.
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_out) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ TileSmem ts;
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
-  const int sub = threadIdx.x % W, seg = threadIdx.x / W, nseg = kBlock / W;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
     const TileDesc t = v.tiles[item];
     const KParams& k = v.inst[t.inst];
@@ -844,7 +848,6 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     float4* hc = reinterpret_cast<float4*>(dsm);
     float2* hp = reinterpret_cast<float2*>(hc + t.halo);
     float* hph = reinterpret_cast<float*>(hp + t.halo);
-    const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16((size_t)28 * t.halo));
     const Rec32* rc = k.rec32_cur;
     for (int s = threadIdx.x; s < t.halo; s += kBlock) {
       const int n = halo_node(ts, s);
@@ -868,56 +871,49 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     const float dtf = (float)k.dt;
     const long long step_no = k.ds->steps + 1;
     const int hslot = k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0;
-    const int* row = k.row;
-    const float* w32 = k.w32;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
     double part[kDiagSlots];
 #pragma unroll
     for (int q = 0; q < kDiagSlots; ++q) part[q] = 0.0;
-    for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
-      const int a = a0 + seg;
-      const bool act = a < t.own_end;
+    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
+    for (int sl = warp; sl < nsl; sl += kBlock / 32) {
+      const int a = t.own_begin + sl * 32 + lane;
+      if (a >= t.own_end) continue;
       const int so = own0 + (a - t.own_begin);
-      float4 ca = make_float4(0.f, 0.f, 0.f, 0.f);
-      float2 pha = make_float2(0.f, 0.f);
-      float pa = 0.0f;
-      if (act) {
-        ca = hc[so];
-        pha = hp[so];
-        pa = hph[so];
+      const float4 ca = hc[so];
+      const float2 pha = hp[so];
+      const float pa = hph[so];
+      // bond coefficient by the neighbour's phase (utils.h:100-153): liquid-liquid D_liquid,
+      // mixed D_solid (BV for Mg), solid-solid D_solid for Mg only
+      float cfL[S], cfS[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        cfL[s] = pa == 0.0f ? cLL[s] : cX[s];
+        cfS[s] = pa == 0.0f ? cX[s] : cSS[s];
       }
       float a1[S], a2[S];
 #pragma unroll
       for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
       int iface = 0;
-      if (act) {
-        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int sl = sslot[j - t.bond0];
-          const float w = w32[j];
-          const float4 cn = hc[sl];
-          const float2 pn2 = hp[sl];
-          const float pn = hph[sl];
-          const float dphi = (pn2.x - pha.x) + (pn2.y - pha.y);
-          const bool ll = (pa == 0.0f) && (pn == 0.0f);
-          const bool ss = (pa != 0.0f) && (pn != 0.0f);
-          iface |= (pa != 0.0f && pn == 0.0f) ? 1 : 0;
+      const int2 md = k.sell_meta[t.slice0 + sl];
+      const unsigned short* cs = k.sell_slot + md.x + lane;
+      const float* ws = k.sell_w + md.x + lane;
+      for (int c = 0; c < md.y; ++c) {
+        const float w = __ldg(ws + 32 * c);
+        const int sn = __ldg(cs + 32 * c);
+        const float4 cn = hc[sn];
+        const float2 pn2 = hp[sn];
+        const bool nsol = hph[sn] != 0.0f;
+        const float dphi = (pn2.x - pha.x) + (pn2.y - pha.y);
+        iface |= (w != 0.0f && pa != 0.0f && !nsol) ? 1 : 0;  // padding has w = 0
 #pragma unroll
-          for (int s = 0; s < S; ++s) {
-            const float coef = ll ? cLL[s] : (ss ? cSS[s] : cX[s]);
-            const float cw = coef * w;
-            const float cns = sel4(cn, s);
-            a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
-            a2[s] = fmaf(cw * cns, dphi, a2[s]);
-          }
+        for (int s = 0; s < S; ++s) {
+          const float cw = (nsol ? cfS[s] : cfL[s]) * w;
+          const float cns = sel4(cn, s);
+          a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
+          a2[s] = fmaf(cw * cns, dphi, a2[s]);
         }
       }
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        a1[s] = comp_reduce<W>(a1[s]);
-        a2[s] = comp_reduce<W>(a2[s]);
-      }
-      iface = seg_or<W>(iface);
-      if (!act || sub != 0) continue;
       const unsigned char dm = k.dirmask[a];
       const float4 lo4 = k.clo[a];
       const double c0old = (double)ca.x + (double)lo4.x;
@@ -1111,9 +1107,11 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
 
 // ------------------------------------------------------------------- state transfer -----
 __global__ void k_load_state(KParams k, const int* perm, const double* c_user, const double* phi_user,
-                             const int* phase_user, int mixed, int dirichlet_phi) {
+                             const int* phase_user, int mixed, int dirichlet_phi, int keep_history) {
   const int N = k.N;
-  if (blockIdx.x == 0 && threadIdx.x == 0) k.ds->hist_n = 0;  // a new state: no history
+  // the history pairs (x, A x) stay valid guesses for the same operator; a new state
+  // starts without them unless the caller continues a run (nnpp_step_host)
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !keep_history) k.ds->hist_n = 0;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += gridDim.x * blockDim.x) {
     const int u = perm[a];
     double c[S];
@@ -1272,9 +1270,9 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
 
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
-size_t smem_spmv32(int H, int B) { return align16((size_t)H * sizeof(float)) + smem_slots(B); }
+size_t smem_spmv32(int H, int B) { return align16((size_t)H * sizeof(float)); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
-size_t smem_tr32(int H, int B) { return align16((size_t)28 * H) + smem_slots(B); }
+size_t smem_tr32(int H, int B) { return align16((size_t)28 * H); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 
 template <typename K>
@@ -1698,6 +1696,9 @@ KParams make_kparams(Handle& h, int cur) {
   k.row = h.lay.row.get();
   k.col = h.lay.col.get();
   k.slot16 = h.slot16.get();
+  k.sell_meta = h.sell_meta.get();
+  k.sell_slot = h.sell_slot.get();
+  k.sell_w = h.sell_w.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
   k.dirmask = h.dirmask.get();
@@ -1754,10 +1755,12 @@ KParams make_kparams(Handle& h, int cur) {
 }
 
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
-                       const int* d_phase_user, int prec, bool dirichlet_phi) {
+                       const int* d_phase_user, int prec, bool dirichlet_phi,
+                       bool keep_history) {
   KParams kp = make_kparams(h, h.cur);
   k_load_state<<<h.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user, d_phase_user,
-                                            prec == NNPP_MIXED ? 1 : 0, dirichlet_phi ? 1 : 0);
+                                            prec == NNPP_MIXED ? 1 : 0, dirichlet_phi ? 1 : 0,
+                                            keep_history ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = prec;
   return NNPP_OK;

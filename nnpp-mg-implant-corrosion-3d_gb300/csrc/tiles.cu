@@ -1,5 +1,6 @@
-// tiles.cu -- tile work items of one instance, 16-bit halo slots of every bond and FP32
-// position records.
+// tiles.cu -- tile work items of one instance, 16-bit halo slots of every bond, FP32
+// position records and the sliced (32 rows per slice, column-major) copy of the slots and
+// FP32 weights that the CG operator streams.
 //
 // A tile is T consecutive bins along x (bins of side >= the horizon radius, x-fastest
 // order, so the tile's own nodes and each of its 3x3 halo rows are contiguous node
@@ -90,6 +91,26 @@ __global__ void k_slots(int n, const int* row, const int* col, const float4* pos
   }
 }
 
+// warp per slice: bond k of lane l (row row0 + l) at off + 32 k + l; padding: slot 0,
+// weight 0
+__global__ void k_sell_fill(int nslices, const int4* sl, const int* row, const unsigned short* slot,
+                            const float* w32, unsigned short* oslot, float* ow) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
+    const int4 d = sl[s];  // {off, width, row0, nrows}
+    const bool live = lane < d.w;
+    const int j0 = live ? row[d.z + lane] : 0;
+    const int len = live ? row[d.z + lane + 1] - j0 : 0;
+    for (int k = 0; k < d.y; ++k) {
+      const size_t o = (size_t)d.x + (size_t)k * 32 + lane;
+      const bool in = k < len;
+      oslot[o] = in ? slot[j0 + k] : (unsigned short)0;
+      ow[o] = in ? w32[j0 + k] : 0.0f;
+    }
+  }
+}
+
 }  // namespace
 
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max,
@@ -127,6 +148,9 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
   if (herr) return set_error(NNPP_ERR_INVALID, "tiles: a neighbour outside its tile's halo");
   const int ntx = (g.nb[0] + T - 1) / T;
   int hm = 0, bm = 0;
+  std::vector<int4> slices;  // {off, width, row0, nrows}
+  std::vector<int2> smeta;
+  long long soff = 0;
   for (int bz = 0; bz < g.nb[2]; ++bz)
     for (int by = 0; by < g.nb[1]; ++by)
       for (int tx = 0; tx < ntx; ++tx) {
@@ -143,15 +167,38 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
         for (int r = 0; r < 9; ++r) tot += t.hl[r];
         if (tot > 65536) return set_error(NNPP_ERR_UNSUPPORTED, "tiles: halo larger than 65536 nodes");
         t.halo = tot;
-        t.cb[0] = bx0 + T / 2;
-        t.cb[1] = by;
-        t.cb[2] = bz;
+        t.slice0 = (int)slices.size();
+        t.pad[0] = t.pad[1] = 0;
+        for (int r0 = o0; r0 < o1; r0 += 32) {
+          const int nr = std::min(32, o1 - r0);
+          int wd = 0;
+          for (int l = 0; l < nr; ++l) wd = std::max(wd, rows[r0 + l + 1] - rows[r0 + l]);
+          slices.push_back(make_int4((int)soff, wd, r0, nr));
+          smeta.push_back(make_int2((int)soff, wd));
+          soff += 32LL * wd;
+          if (soff > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "sliced operator above 2^31 entries");
+        }
         t.bond0 = rows[o0] & ~7;
         t.bond1 = rows[o1];
         hm = std::max(hm, tot);
         bm = std::max(bm, t.bond1 - t.bond0);
         tiles.push_back(t);
       }
+  // sliced copy of the slots and FP32 weights for the CG operator
+  const size_t ns = slices.size();
+  if (!h.sell_meta.alloc(ns + 1) || !h.sell_slot.alloc((size_t)soff + 32) || !h.sell_w.alloc((size_t)soff + 32))
+    return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  DBuf<int4> dsl;
+  if (ns && !dsl.alloc(ns)) return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  if (ns) {
+    NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(h.sell_meta.get(), smeta.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, h.st));
+    const int sb = std::max(1, std::min((int)((ns * 32 + 255) / 256), 152 * 32));
+    k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), L.row.get(), h.slot16.get(), L.w32.get(),
+                                      h.sell_slot.get(), h.sell_w.get());
+    NNPP_CUDA(cudaGetLastError());
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+  }
   *halo_max = hm;
   *bond_max = bm;
   h.tiles_T = T;
