@@ -50,13 +50,16 @@ nnpp_status build_lists(Engine& e, int T) {
   const int M = (int)e.members.size();
   std::vector<TileDesc> tiles;
   std::vector<Chunk> chunks;
-  std::vector<int> meta(4 * M);
+  std::vector<SliceDesc> slices;
+  std::vector<int> meta(6 * M);
   int hm = 0, bmax = 0;
   for (int i = 0; i < M; ++i) {
     Handle& h = *e.members[i];
     meta[i] = (int)tiles.size();
     int hmi = 0, bmi = 0;
-    NNPP_TRY(build_tiles(h, T, tiles, i, &hmi, &bmi));
+    meta[4 * M + i] = (int)slices.size();
+    NNPP_TRY(build_tiles(h, T, tiles, slices, i, &hmi, &bmi));
+    meta[5 * M + i] = (int)slices.size() - meta[4 * M + i];
     meta[M + i] = (int)tiles.size() - meta[i];
     hm = std::max(hm, hmi);
     bmax = std::max(bmax, bmi);
@@ -73,17 +76,22 @@ nnpp_status build_lists(Engine& e, int T) {
   }
   e.ntiles = (int)tiles.size();
   e.nchunks = (int)chunks.size();
+  e.nslices = (int)slices.size();
   e.halo_max = hm;
   e.bond_max = bmax;
   e.T = T;
+  const int stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
   if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
-      !e.d_ticket.alloc(M + 1) || !e.d_partials.alloc((size_t)kReduceSlots * std::max(e.ntiles, e.nchunks)) ||
+      !e.d_slices.alloc(std::max<size_t>(slices.size(), 1)) || !e.d_ticket.alloc(M + 2) ||
+      !e.d_partials.alloc((size_t)kReduceSlots * stride) ||
       !e.d_inst[0].alloc(M) || !e.d_inst[1].alloc(M))
     return set_error(NNPP_ERR_NOMEM, "engine work lists");
   NNPP_CUDA(cudaMemcpyAsync(e.d_tiles.get(), tiles.data(), sizeof(TileDesc) * tiles.size(), cudaMemcpyHostToDevice, e.st));
   NNPP_CUDA(cudaMemcpyAsync(e.d_chunks.get(), chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice, e.st));
   NNPP_CUDA(cudaMemcpyAsync(e.d_meta.get(), meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, e.st));
-  NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, sizeof(unsigned int) * (M + 1), e.st));
+  if (!slices.empty())
+    NNPP_CUDA(cudaMemcpyAsync(e.d_slices.get(), slices.data(), sizeof(SliceDesc) * slices.size(), cudaMemcpyHostToDevice, e.st));
+  NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, sizeof(unsigned int) * (M + 2), e.st));
   NNPP_CUDA(cudaStreamSynchronize(e.st));
   engine_destroy_graphs(e);
   return NNPP_OK;
@@ -103,8 +111,9 @@ nnpp_status set_active(Engine& e, int outer, int inner) {
   return NNPP_OK;
 }
 
-// Autotuner: bins per tile T and lanes per node W that minimise the FP32 CG operator on the
-// current state (the kernel run ~100 times per step).
+// Autotuner: bins per tile T and lanes per node W that minimise the CG operator on the
+// current state (run tens of times per step) plus, for the mixed path, one FP64 tile
+// operator (the refinement residual and the prep use the W lanes per node).
 nnpp_status tune(Engine& e, int prec) {
   std::vector<DevState> saved(e.members.size());
   NNPP_CUDA(cudaStreamSynchronize(e.st));
@@ -118,7 +127,12 @@ nnpp_status tune(Engine& e, int prec) {
   NNPP_CUDA(cudaEventCreate(&e0));
   NNPP_CUDA(cudaEventCreate(&e1));
   for (int T : Ts) {
-    NNPP_TRY(build_lists(e, T));
+    const nnpp_status bs = build_lists(e, T);
+    if (bs == NNPP_ERR_UNSUPPORTED) {
+      clear_error();
+      continue;
+    }
+    NNPP_TRY(bs);
     NNPP_TRY(refresh_params(e));
     for (int W : Ws) {
       e.W = W;
@@ -129,7 +143,9 @@ nnpp_status tune(Engine& e, int prec) {
       NNPP_TRY(set_active(e, 1, 1));
       NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
       cudaEventRecord(e0, e.st);
+      // the CG operator dominates; the FP64 tile kernels (residual, prep) follow the lanes
       for (int r = 0; r < 5; ++r) NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+      if (prec == NNPP_MIXED) NNPP_TRY(launch_cg_spmv_b(e, v, NNPP_FP64, e.st));
       cudaEventRecord(e1, e.st);
       NNPP_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -310,13 +326,17 @@ EngineView make_view(Engine& e, int parity, int in_graph) {
   v.tile_count = e.d_meta.get() + M;
   v.chunk_first = e.d_meta.get() + 2 * M;
   v.chunk_count = e.d_meta.get() + 3 * M;
+  v.slice_first = e.d_meta.get() + 4 * M;
+  v.slice_count = e.d_meta.get() + 5 * M;
+  v.slices = e.d_slices.get();
+  v.nslices = e.nslices;
   v.ticket = e.d_ticket.get();
   v.partials = e.d_partials.get();
   v.ntiles = e.ntiles;
   v.nchunks = e.nchunks;
   v.M = M;
   v.in_graph = in_graph;
-  v.stride = std::max(e.ntiles, e.nchunks);
+  v.stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
   v.halo_max = e.halo_max;
   v.bond_max = e.bond_max;
   return v;

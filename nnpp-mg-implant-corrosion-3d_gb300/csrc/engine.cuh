@@ -31,6 +31,18 @@ struct Chunk {
   int pad;
 };
 
+// 32 consecutive rows of one tile in the sliced operator layout (bond c of row row0 + l at
+// off + 32 c + l of the instance's sliced arrays; slot code = halo row << 12 | offset in it).
+struct SliceDesc {
+  int inst;
+  int tile;    // global tile index: its halo rows decode the slot codes
+  int row0;    // first row (internal node index of the instance)
+  int nrows;   // rows in the slice (<= 32)
+  int off;     // offset in the instance's sliced arrays
+  int width;   // columns (longest row of the slice)
+  int pad[2];
+};
+
 // What every batched kernel receives.
 struct EngineView {
   const KParams* inst;      // per instance
@@ -40,10 +52,14 @@ struct EngineView {
   const int* tile_count;    // per instance: number of tiles
   const int* chunk_first;
   const int* chunk_count;
-  unsigned int* ticket;     // per instance completion counters, + [M] global
-  double* partials;         // kReduceSlots * max(ntiles, nchunks)
+  const SliceDesc* slices;  // grouped by instance, tiles in order
+  const int* slice_first;
+  const int* slice_count;
+  unsigned int* ticket;     // per instance completion counters, + [M] global, + [M+1] grid
+  double* partials;         // kReduceSlots * stride
   int ntiles, nchunks, M, in_graph;
-  int stride;               // max(ntiles, nchunks): slot stride of partials
+  int nslices;
+  int stride;               // max(ntiles, nchunks, nslices): slot stride of partials
   int halo_max;             // largest halo (dynamic shared memory sizing)
   int bond_max;             // largest staged bond range of a tile (bond1 - bond0)
 };
@@ -63,10 +79,11 @@ struct Engine {
   DBuf<KParams> d_inst[2];  // indexed by the parity of the current record buffer
   DBuf<TileDesc> d_tiles;
   DBuf<Chunk> d_chunks;
-  DBuf<int> d_meta;         // tile_first, tile_count, chunk_first, chunk_count (4*M)
+  DBuf<int> d_meta;         // tile/chunk/slice first and count (6*M)
+  DBuf<SliceDesc> d_slices;
   DBuf<unsigned int> d_ticket;
   DBuf<double> d_partials;
-  int ntiles = 0, nchunks = 0;
+  int ntiles = 0, nchunks = 0, nslices = 0;
   cudaStream_t st = nullptr, st_b1 = nullptr, st_b2 = nullptr;
   int device = 0;
   int cur = 0;              // record parity shared by all members
@@ -86,8 +103,8 @@ nnpp_status engine_params(Engine& e);            // re-upload the members' KPara
 void engine_destroy_graphs(Engine& e);
 
 // tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
-nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max,
-                        int* bond_max);
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& slices,
+                        int inst, int* halo_max, int* bond_max);
 
 // step.cu launchers (batched)
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);

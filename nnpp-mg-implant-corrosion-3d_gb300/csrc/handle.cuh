@@ -20,8 +20,7 @@ struct KParams {
   const int* col;
   const unsigned short* slot16;  // per bond: halo slot of the neighbour within its tile
   // sliced layout (32 consecutive rows of a tile per slice, bonds column-major within a
-  // slice, rows padded to the slice's longest): {offset, width} per slice, slots, weights
-  const int2* sell_meta;
+  // slice, rows padded to the slice's longest): slot codes (halo row << 12 | offset), weights
   const unsigned short* sell_slot;
   const float* sell_w;
   const double* w64;
@@ -83,7 +82,6 @@ struct Handle {
   int max_node_no = 0;
   // tiles (built for tiles_T bins per tile)
   DBuf<unsigned short> slot16;
-  DBuf<int2> sell_meta;
   DBuf<unsigned short> sell_slot;
   DBuf<float> sell_w;
   DBuf<float4> posrec;

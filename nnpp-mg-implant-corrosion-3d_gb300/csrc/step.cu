@@ -359,68 +359,90 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
   }
 }
 
+// Work split of the slice list: warp gw of nw takes the contiguous range [s0, s1), so the
+// warps of one CTA walk neighbouring slices and share their neighbours in L1.
+__device__ __forceinline__ void warp_slices(const EngineView& v, int* s0, int* s1) {
+  const long long nw = (long long)gridDim.x * (kBlock / 32);
+  const long long gw = (long long)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+  *s0 = (int)(((long long)v.nslices * gw) / nw);
+  *s1 = (int)(((long long)v.nslices * (gw + 1)) / nw);
+}
+
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+  return x;
+}
+
+// node of a slot code: halo row start (per-warp table of the slice's tile) + offset
+__device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
+  return hb[code >> 12] + (int)(code & 4095u);
+}
+
 // q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
-// FP32: z of the tile's halo staged in shared memory; each warp streams one 32-row slice of
-// the sliced operator (slots and weights column-major, one coalesced load per bond column).
+// FP32, sliced operator: each warp streams 32-row slices (slot codes and weights
+// column-major: one coalesced load per bond column), gathers z from L1/L2, one lane per row.
+// Slice partials are reduced per instance by the last CTA.
 template <int W>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ TileSmem ts;
+  __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
-    const TileDesc t = v.tiles[item];
-    const KParams& k = v.inst[t.inst];
-    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
-    double part[1] = {0.0};
-    if (active) {
-      load_tile(t, ts);
-      float* hs = reinterpret_cast<float*>(dsm);
-      const float* z = k.z32;
-      for (int s = threadIdx.x; s < t.halo; s += kBlock) hs[s] = z[halo_node(ts, s)];
-      __syncthreads();
-      const unsigned char* freem = k.freem;
-      float* p = k.p32;
-      float* q = k.q32;
-      const float beta = (float)k.ds->beta;
-      const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
-      const int nsl = (t.own_end - t.own_begin + 31) >> 5;
-      for (int sl = warp; sl < nsl; sl += kBlock / 32) {
-        const int a = t.own_begin + sl * 32 + lane;
-        if (a >= t.own_end || !freem[a]) continue;
-        const int2 md = k.sell_meta[t.slice0 + sl];
-        const unsigned short* cs = k.sell_slot + md.x + lane;
-        const float* ws = k.sell_w + md.x + lane;
-        float acc0 = 0.0f, acc1 = 0.0f;
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    double part = 0.0;
+    if (*((volatile int*)&k.ds->inner_active) != 0) {
+      if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+      __syncwarp();
+      const int a = d.row0 + lane;
+      if (lane < d.nrows && k.freem[a]) {
+        const int* hb = s_hb[warp];
+        const unsigned short* cs = k.sell_slot + d.off + lane;
+        const float* ws = k.sell_w + d.off + lane;
+        const float* z = k.z32;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         int c = 0;
-        for (; c + 1 < md.y; c += 2) {
-          const float w0 = __ldg(ws + 32 * c), w1 = __ldg(ws + 32 * c + 32);
-          const int s0 = __ldg(cs + 32 * c), s1 = __ldg(cs + 32 * c + 32);
-          acc0 = fmaf(w0, hs[s0], acc0);
-          acc1 = fmaf(w1, hs[s1], acc1);
+        for (; c + 8 <= d.width; c += 8) {
+          float w[8];
+          unsigned int code[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            w[u] = __ldcs(ws + 32 * (c + u));
+            code[u] = __ldcs(cs + 32 * (c + u));
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[u & 3] = fmaf(w[u], __ldg(z + code_node(hb, code[u])), acc[u & 3]);
         }
-        if (c < md.y) acc0 = fmaf(__ldg(ws + 32 * c), hs[__ldg(cs + 32 * c)], acc0);
-        const float za = hs[own0 + (a - t.own_begin)];
-        const float sa = k.d32[a] * za - (acc0 + acc1);
-        const float qn = sa + beta * q[a];
-        const float pn = za + beta * p[a];
-        q[a] = qn;
-        p[a] = pn;
-        part[0] += (double)pn * (double)qn;
+        for (; c < d.width; ++c)
+          acc[0] = fmaf(__ldcs(ws + 32 * c), __ldg(z + code_node(hb, __ldcs(cs + 32 * c))), acc[0]);
+        const float za = z[a];
+        const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+        const float beta = (float)k.ds->beta;
+        const float qn = sa + beta * k.q32[a];
+        const float pn = za + beta * k.p32[a];
+        k.q32[a] = qn;
+        k.p32[a] = pn;
+        part = (double)pn * (double)qn;
       }
+      __syncwarp();
     }
-    write_partials<1>(v, item, part, sm);
-    if (item_done(&v.ticket[t.inst], v.tile_count[t.inst], &s_last)) {
+    part = warp_sum_d(part);
+    if (lane == 0) v.partials[sg] = part;
+  }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_items<1>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
+      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
-        DevState* ds = k.ds;
+        DevState* ds = v.inst[i].ds;
         if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
-        v.ticket[t.inst] = 0;
       }
     }
-    __syncthreads();
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
   }
 }
 
@@ -780,6 +802,25 @@ __device__ __forceinline__ double dissolve_switch(double c0, double csat, double
 
 constexpr int kDiagSlots = 9;  // mass[4], solid, vol, dissolved, nonfinite, spare
 
+// Per-step diagnostics of one instance from its reduced transport partials (thread 0).
+__device__ __forceinline__ void finish_instance(const KParams& k, const double (&tot)[kDiagSlots]) {
+  DevState* ds = k.ds;
+  for (int s = 0; s < S; ++s) ds->mass[s] = tot[s];
+  ds->solid_count = (long long)tot[4];
+  ds->steps += 1;
+  if (k.dissolve_count) ds->dissolved += tot[6];
+  if (tot[7] != 0.0) ds->nonfinite = 1;
+  ds->mg_mass_now = tot[0];
+  if (k.hist_m >= 3) {
+    ds->hist_head = (ds->hist_head + 1) % k.hist_m;
+    ds->hist_n = ds->hist_n < k.hist_m ? ds->hist_n + 1 : k.hist_m;
+  }
+  if (k.sub_step_no > 0 && ds->steps % k.sub_step_no == 0) {
+    ds->voln1rel = ds->vol0rel != 0.0 ? tot[5] / ds->vol0rel : 0.0;
+    ds->BV = pow(10., -k.vol_red * (1. - ds->voln1rel));  // utils.h:100-116
+  }
+}
+
 __device__ __forceinline__ void transport_finish(const EngineView& v, const TileDesc& t,
                                                  const KParams& k, int item,
                                                  double (&part)[kDiagSlots], double* sm,
@@ -789,22 +830,8 @@ __device__ __forceinline__ void transport_finish(const EngineView& v, const Tile
   double tot[kDiagSlots];
   reduce_items<kDiagSlots>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
   if (threadIdx.x == 0) {
-    DevState* ds = k.ds;
     v.ticket[t.inst] = 0;
-    for (int s = 0; s < S; ++s) ds->mass[s] = tot[s];
-    ds->solid_count = (long long)tot[4];
-    ds->steps += 1;
-    if (k.dissolve_count) ds->dissolved += tot[6];
-    if (tot[7] != 0.0) ds->nonfinite = 1;
-    ds->mg_mass_now = tot[0];
-    if (k.hist_m >= 3) {
-      ds->hist_head = (ds->hist_head + 1) % k.hist_m;
-      ds->hist_n = ds->hist_n < k.hist_m ? ds->hist_n + 1 : k.hist_m;
-    }
-    if (k.sub_step_no > 0 && ds->steps % k.sub_step_no == 0) {
-      ds->voln1rel = ds->vol0rel != 0.0 ? tot[5] / ds->vol0rel : 0.0;
-      ds->BV = pow(10., -k.vol_red * (1. - ds->voln1rel));  // utils.h:100-116
-    }
+    finish_instance(k, tot);
   }
 }
 
@@ -832,57 +859,42 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
 
 // Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
 // (single instance) and change nothing; otherwise advance the state into rec32_nxt / clo.
-// The tile's halo records are staged in shared memory; each warp streams one 32-row slice
-// of the sliced operator, one lane per node, so the per-node update runs on full warps.
+// Each warp streams 32-row slices of the sliced operator, one lane per node, gathering the
+// neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
+// partials of the diagnostics are reduced per instance by the last CTA.
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_out) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ TileSmem ts;
+  __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
-    const TileDesc t = v.tiles[item];
-    const KParams& k = v.inst[t.inst];
-    load_tile(t, ts);
-    float4* hc = reinterpret_cast<float4*>(dsm);
-    float2* hp = reinterpret_cast<float2*>(hc + t.halo);
-    float* hph = reinterpret_cast<float*>(hp + t.halo);
-    const Rec32* rc = k.rec32_cur;
-    for (int s = threadIdx.x; s < t.halo; s += kBlock) {
-      const int n = halo_node(ts, s);
-      const float4* src = reinterpret_cast<const float4*>(rc + n);
-      const float4 a = src[0], b = src[1];
-      hc[s] = a;
-      hp[s] = make_float2(b.x, b.y);
-      hph[s] = b.z;
-    }
-    __syncthreads();
-    const double BV = *k.bv_ptr;
-    float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-      cLL[s] = (float)k.DL[s];
-      cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
-      cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
-      K1f[s] = (float)k.K1[s];
-      K2f[s] = (float)k.K2zF[s];
-    }
-    const float dtf = (float)k.dt;
-    const long long step_no = k.ds->steps + 1;
-    const int hslot = k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0;
-    const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+    __syncwarp();
     double part[kDiagSlots];
 #pragma unroll
     for (int q = 0; q < kDiagSlots; ++q) part[q] = 0.0;
-    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
-    for (int sl = warp; sl < nsl; sl += kBlock / 32) {
-      const int a = t.own_begin + sl * 32 + lane;
-      if (a >= t.own_end) continue;
-      const int so = own0 + (a - t.own_begin);
-      const float4 ca = hc[so];
-      const float2 pha = hp[so];
-      const float pa = hph[so];
+    const int a = d.row0 + lane;
+    if (lane < d.nrows) {
+      const int* hb = s_hb[warp];
+      const float4* rc = reinterpret_cast<const float4*>(k.rec32_cur);
+      const double BV = *k.bv_ptr;
+      float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        cLL[s] = (float)k.DL[s];
+        cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
+        cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
+        K1f[s] = (float)k.K1[s];
+        K2f[s] = (float)k.K2zF[s];
+      }
+      const float4 ca = rc[2 * a];
+      const float4 cb = rc[2 * a + 1];  // phi_hi, phi_lo, phase, pad
+      const float pa = cb.z;
       // bond coefficient by the neighbour's phase (utils.h:100-153): liquid-liquid D_liquid,
       // mixed D_solid (BV for Mg), solid-solid D_solid for Mg only
       float cfL[S], cfS[S];
@@ -895,17 +907,18 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
 #pragma unroll
       for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
       int iface = 0;
-      const int2 md = k.sell_meta[t.slice0 + sl];
-      const unsigned short* cs = k.sell_slot + md.x + lane;
-      const float* ws = k.sell_w + md.x + lane;
-      for (int c = 0; c < md.y; ++c) {
-        const float w = __ldg(ws + 32 * c);
-        const int sn = __ldg(cs + 32 * c);
-        const float4 cn = hc[sn];
-        const float2 pn2 = hp[sn];
-        const bool nsol = hph[sn] != 0.0f;
-        const float dphi = (pn2.x - pha.x) + (pn2.y - pha.y);
-        iface |= (w != 0.0f && pa != 0.0f && !nsol) ? 1 : 0;  // padding has w = 0
+      const unsigned short* cs = k.sell_slot + d.off + lane;
+      const float* ws = k.sell_w + d.off + lane;
+      const int len = k.row[a + 1] - k.row[a];
+#pragma unroll 2
+      for (int c = 0; c < len; ++c) {
+        const float w = __ldcs(ws + 32 * c);
+        const int n = code_node(hb, __ldcs(cs + 32 * c));
+        const float4 cn = __ldg(rc + 2 * n);
+        const float4 nb = __ldg(rc + 2 * n + 1);
+        const bool nsol = nb.z != 0.0f;
+        const float dphi = (nb.x - cb.x) + (nb.y - cb.y);
+        iface |= (pa != 0.0f && !nsol) ? 1 : 0;
 #pragma unroll
         for (int s = 0; s < S; ++s) {
           const float cw = (nsol ? cfS[s] : cfL[s]) * w;
@@ -925,57 +938,74 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
         for (int s = 0; s < S; ++s)
           F_out[(size_t)s * k.N + a] =
               -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
-        continue;
-      }
-      float hi[S], lo[S];
-      double val[S];
-      bool bad = false;
+      } else {
+        const float dtf = (float)k.dt;
+        float hi[S], lo[S];
+        double val[S];
+        bool bad = false;
 #pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
-        float tt, e1, sh, e2;
-        two_sum(sel4(lo4, s), inc, tt, e1);
-        two_sum(sel4(ca, s), tt, sh, e2);
-        double x = (double)sh + (double)(e1 + e2);
-        if ((dm >> s) & 1) x = k.bcval[(size_t)s * k.N + a];
-        if (x < k.c_floor) x = k.c_floor;
-        if (!isfinite(x)) bad = true;
-        const float xh = (float)x;
-        hi[s] = xh;
-        lo[s] = (float)(x - (double)xh);
-        val[s] = x;
-      }
-      float pnew = pa;
-      if (pa != 0.0f && val[0] <= k.csat) {
-        pnew = 0.0f;
-        k.flip_step[a] = (int)step_no;
-      }
-      record_history(k, a, hslot);
-      const double g = next_phi_guess(k, a);
-      Rec32 out;
+        for (int s = 0; s < S; ++s) {
+          const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
+          float tt, e1, sh, e2;
+          two_sum(sel4(lo4, s), inc, tt, e1);
+          two_sum(sel4(ca, s), tt, sh, e2);
+          double x = (double)sh + (double)(e1 + e2);
+          if ((dm >> s) & 1) x = k.bcval[(size_t)s * k.N + a];
+          if (x < k.c_floor) x = k.c_floor;
+          if (!isfinite(x)) bad = true;
+          const float xh = (float)x;
+          hi[s] = xh;
+          lo[s] = (float)(x - (double)xh);
+          val[s] = x;
+        }
+        float pnew = pa;
+        if (pa != 0.0f && val[0] <= k.csat) {
+          pnew = 0.0f;
+          k.flip_step[a] = (int)(k.ds->steps + 1);
+        }
+        record_history(k, a, k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0);
+        const double g = next_phi_guess(k, a);
+        Rec32 out;
 #pragma unroll
-      for (int s = 0; s < S; ++s) out.c[s] = hi[s];
-      out.phi_hi = (float)g;
-      out.phi_lo = (float)(g - (double)out.phi_hi);
-      out.phase = pnew;
-      out.pad = 0.0f;
-      k.rec32_nxt[a] = out;
-      k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        for (int s = 0; s < S; ++s) out.c[s] = hi[s];
+        out.phi_hi = (float)g;
+        out.phi_lo = (float)(g - (double)out.phi_hi);
+        out.phase = pnew;
+        out.pad = 0.0f;
+        k.rec32_nxt[a] = out;
+        k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
 #pragma unroll
-      for (int s = 0; s < S; ++s) part[s] += val[s];
-      if (pnew != 0.0f) {
-        part[4] += 1.0;
-        part[5] += val[0] - k.csat;
+        for (int s = 0; s < S; ++s) part[s] = val[s];
+        if (pnew != 0.0f) {
+          part[4] = 1.0;
+          part[5] = val[0] - k.csat;
+        }
+        part[6] = k.k_diss * swv;
+        part[7] = bad ? 1.0 : 0.0;
       }
-      part[6] += k.k_diss * swv;
-      part[7] += bad ? 1.0 : 0.0;
     }
-    if (!RESID) transport_finish(v, t, k, item, part, sm, &s_last);
-    __syncthreads();
+    __syncwarp();
+    if (!RESID) {
+#pragma unroll
+      for (int q = 0; q < kDiagSlots; ++q) part[q] = warp_sum_d(part[q]);
+      if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < kDiagSlots; ++q) v.partials[(size_t)q * v.stride + sg] = part[q];
+    }
+  }
+  if (RESID) return;
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[kDiagSlots];
+      reduce_items<kDiagSlots>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      if (threadIdx.x == 0) finish_instance(v.inst[i], tot);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
   }
 }
 
-// FP64 transport, same structure (stored FP64 weights, FP64 records).
+// FP64 transport (the plain FP64 path)
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_out) {
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -1270,10 +1300,9 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
 
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
-size_t smem_spmv32(int H, int B) { return align16((size_t)H * sizeof(float)); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
-size_t smem_tr32(int H, int B) { return align16((size_t)28 * H); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
+size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) + 1)) + smem_slots(B) + 16; }
 
 template <typename K>
 nnpp_status allow_smem(K kern, size_t bytes) {
@@ -1496,7 +1525,7 @@ nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec
                                  const Rec64* snap1, const double* lam, double* mu, double* nu,
                                  double* acc, cudaStream_t st) {
   AdjArgs ad{snap, snap1, lam, mu, nu, acc};
-  const size_t sh = align16((size_t)v.halo_max * (9 * sizeof(double) + 1)) + (size_t)(v.bond_max + 16) * 2 + 16;
+  const size_t sh = smem_adj(v.halo_max, v.bond_max);
   if (sh > 227 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "adjoint: tile halo too large");
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
@@ -1545,17 +1574,16 @@ nnpp_status launch_sum_c0(Handle& h, double* out) {
 
 // ---------------------------------------------------------------------------------------
 nnpp_status prepare_kernels(int H, int B, int lanes) {
-  if (smem_tr64(H, B) > 220 * 1024) return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
+  // every tile kernel, the adjoint's included, must fit its staged halo
+  if (smem_tr64(H, B) > 220 * 1024 || smem_adj(H, B) > 220 * 1024)
+    return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
   return dispatch_lanes(lanes, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
-    NNPP_TRY(allow_smem(k_cg_spmv32<W>, smem_spmv32(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
-    NNPP_TRY(allow_smem(k_transport32<W, false>, smem_tr32(H, B)));
-    NNPP_TRY(allow_smem(k_transport32<W, true>, smem_tr32(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, true>, smem_tr64(H, B)));
     return NNPP_OK;
@@ -1602,7 +1630,7 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      { const size_t sh = smem_spmv32(v.halo_max, v.bond_max); k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }
+      k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v);
     else
       { const size_t sh = smem_vec64(v.halo_max, v.bond_max); k_cg_spmv64<W><<<occ_grid(k_cg_spmv64<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }
     NNPP_CUDA(cudaGetLastError());
@@ -1639,11 +1667,10 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED) {
-      const size_t sh = smem_tr32(v.halo_max, v.bond_max);
       if (F_out)
-        k_transport32<W, true><<<occ_grid(k_transport32<W, true>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, F_out);
+        k_transport32<W, true><<<occ_grid(k_transport32<W, true>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v, F_out);
       else
-        k_transport32<W, false><<<occ_grid(k_transport32<W, false>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, nullptr);
+        k_transport32<W, false><<<occ_grid(k_transport32<W, false>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v, nullptr);
     } else {
       const size_t sh = smem_tr64(v.halo_max, v.bond_max);
       if (F_out)
@@ -1696,7 +1723,6 @@ KParams make_kparams(Handle& h, int cur) {
   k.row = h.lay.row.get();
   k.col = h.lay.col.get();
   k.slot16 = h.slot16.get();
-  k.sell_meta = h.sell_meta.get();
   k.sell_slot = h.sell_slot.get();
   k.sell_w = h.sell_w.get();
   k.w64 = h.lay.w64.get();

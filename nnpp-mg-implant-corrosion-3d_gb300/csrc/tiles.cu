@@ -91,30 +91,41 @@ __global__ void k_slots(int n, const int* row, const int* col, const float4* pos
   }
 }
 
-// warp per slice: bond k of lane l (row row0 + l) at off + 32 k + l; padding: slot 0,
-// weight 0
-__global__ void k_sell_fill(int nslices, const int4* sl, const int* row, const unsigned short* slot,
-                            const float* w32, unsigned short* oslot, float* ow) {
+// warp per slice: bond c of lane l (row row0 + l) at off + 32 c + l as (halo row << 12 |
+// offset within the row) and its FP32 weight; padding: code 0, weight 0.  pre: the tile's
+// halo row starts within the concatenated halo (9 per slice).
+__global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre, const int* row,
+                            const unsigned short* slot, const float* w32, unsigned short* ocode,
+                            float* ow) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
-    const int4 d = sl[s];  // {off, width, row0, nrows}
-    const bool live = lane < d.w;
-    const int j0 = live ? row[d.z + lane] : 0;
-    const int len = live ? row[d.z + lane + 1] - j0 : 0;
-    for (int k = 0; k < d.y; ++k) {
-      const size_t o = (size_t)d.x + (size_t)k * 32 + lane;
-      const bool in = k < len;
-      oslot[o] = in ? slot[j0 + k] : (unsigned short)0;
-      ow[o] = in ? w32[j0 + k] : 0.0f;
+    const SliceDesc d = sl[s];
+    const int* p9 = pre + 9 * s;
+    const bool live = lane < d.nrows;
+    const int j0 = live ? row[d.row0 + lane] : 0;
+    const int len = live ? row[d.row0 + lane + 1] - j0 : 0;
+    for (int c = 0; c < d.width; ++c) {
+      const size_t o = (size_t)d.off + (size_t)c * 32 + lane;
+      unsigned short code = 0;
+      float w = 0.0f;
+      if (c < len) {
+        const int sv = slot[j0 + c];
+        int r = 0;
+        while (r < 8 && sv >= p9[r + 1]) ++r;
+        code = (unsigned short)((r << 12) | (sv - p9[r]));
+        w = w32[j0 + c];
+      }
+      ocode[o] = code;
+      ow[o] = w;
     }
   }
 }
 
 }  // namespace
 
-nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst, int* halo_max,
-                        int* bond_max) {
+nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& gslices,
+                        int inst, int* halo_max, int* bond_max) {
   const Layout& L = h.lay;
   const int N = h.N;
   if (L.nb[0] > 1024 || L.nb[1] > 1024 || L.nb[2] > 1024)
@@ -148,8 +159,8 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
   if (herr) return set_error(NNPP_ERR_INVALID, "tiles: a neighbour outside its tile's halo");
   const int ntx = (g.nb[0] + T - 1) / T;
   int hm = 0, bm = 0;
-  std::vector<int4> slices;  // {off, width, row0, nrows}
-  std::vector<int2> smeta;
+  std::vector<SliceDesc> slices;  // this instance's, offsets local to its sliced arrays
+  std::vector<int> pre;            // per slice: starts of the 9 halo rows in the halo
   long long soff = 0;
   for (int bz = 0; bz < g.nb[2]; ++bz)
     for (int by = 0; by < g.nb[1]; ++by)
@@ -167,15 +178,27 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
         for (int r = 0; r < 9; ++r) tot += t.hl[r];
         if (tot > 65536) return set_error(NNPP_ERR_UNSUPPORTED, "tiles: halo larger than 65536 nodes");
         t.halo = tot;
-        t.slice0 = (int)slices.size();
+        t.slice0 = (int)(gslices.size() + slices.size());
         t.pad[0] = t.pad[1] = 0;
+        for (int r = 0; r < 9; ++r)
+          if (t.hl[r] > 4096) return set_error(NNPP_ERR_UNSUPPORTED, "tiles: halo row longer than 4096 nodes");
         for (int r0 = o0; r0 < o1; r0 += 32) {
-          const int nr = std::min(32, o1 - r0);
-          int wd = 0;
-          for (int l = 0; l < nr; ++l) wd = std::max(wd, rows[r0 + l + 1] - rows[r0 + l]);
-          slices.push_back(make_int4((int)soff, wd, r0, nr));
-          smeta.push_back(make_int2((int)soff, wd));
-          soff += 32LL * wd;
+          SliceDesc d;
+          d.inst = inst;
+          d.tile = (int)tiles.size();
+          d.row0 = r0;
+          d.nrows = std::min(32, o1 - r0);
+          d.off = (int)soff;
+          d.width = 0;
+          d.pad[0] = d.pad[1] = 0;
+          for (int l = 0; l < d.nrows; ++l) d.width = std::max(d.width, rows[r0 + l + 1] - rows[r0 + l]);
+          slices.push_back(d);
+          int acc = 0;
+          for (int r = 0; r < 9; ++r) {
+            pre.push_back(acc);
+            acc += t.hl[r];
+          }
+          soff += 32LL * d.width;
           if (soff > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "sliced operator above 2^31 entries");
         }
         t.bond0 = rows[o0] & ~7;
@@ -184,21 +207,23 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, int inst
         bm = std::max(bm, t.bond1 - t.bond0);
         tiles.push_back(t);
       }
-  // sliced copy of the slots and FP32 weights for the CG operator
+  // sliced copy of the slot codes and FP32 weights for the CG operator and the transport
   const size_t ns = slices.size();
-  if (!h.sell_meta.alloc(ns + 1) || !h.sell_slot.alloc((size_t)soff + 32) || !h.sell_w.alloc((size_t)soff + 32))
+  if (!h.sell_slot.alloc((size_t)soff + 32) || !h.sell_w.alloc((size_t)soff + 32))
     return set_error(NNPP_ERR_NOMEM, "sliced operator");
-  DBuf<int4> dsl;
-  if (ns && !dsl.alloc(ns)) return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  DBuf<SliceDesc> dsl;
+  DBuf<int> dpre;
+  if (ns && (!dsl.alloc(ns) || !dpre.alloc(9 * ns))) return set_error(NNPP_ERR_NOMEM, "sliced operator");
   if (ns) {
-    NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice, h.st));
-    NNPP_CUDA(cudaMemcpyAsync(h.sell_meta.get(), smeta.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(dpre.get(), pre.data(), sizeof(int) * 9 * ns, cudaMemcpyHostToDevice, h.st));
     const int sb = std::max(1, std::min((int)((ns * 32 + 255) / 256), 152 * 32));
-    k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), L.row.get(), h.slot16.get(), L.w32.get(),
+    k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), dpre.get(), L.row.get(), h.slot16.get(), L.w32.get(),
                                       h.sell_slot.get(), h.sell_w.get());
     NNPP_CUDA(cudaGetLastError());
     NNPP_CUDA(cudaStreamSynchronize(h.st));
   }
+  gslices.insert(gslices.end(), slices.begin(), slices.end());
   *halo_max = hm;
   *bond_max = bm;
   h.tiles_T = T;
