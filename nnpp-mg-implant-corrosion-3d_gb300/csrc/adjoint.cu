@@ -14,9 +14,14 @@
 #include <cstring>
 #include <vector>
 
+#include <cstddef>
+
 #include "engine.cuh"
 
 using namespace nnpp;
+
+static_assert(offsetof(DevState, hist_head) == offsetof(DevState, hist_n) + sizeof(int),
+              "hist_n and hist_head are written together");
 
 struct nnpp_handle {
   Handle h;
@@ -134,7 +139,12 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
   const size_t N = h.N;
   const double dV = h.p.dx * h.p.dy * h.p.dz;
   DBuf<Rec64> snap;
-  DBuf<double> lam, mu, nu, psi, acc;
+  DBuf<double> lam, mu, nu, psi, acc, xa, ba;
+  // warm-start ring of the adjoint potential solves (host-tracked fill and head)
+  const int hm = (h.extrapolate && h.warm_hist >= 3 && h.xh.get()) ? h.warm_hist : 0;
+  int an = 0, ahead = hm ? hm - 1 : 0;
+  if (hm && (!xa.alloc((size_t)hm * N) || !ba.alloc((size_t)hm * N)))
+    return set_error(NNPP_ERR_NOMEM, "adjoint warm-start ring");
   if (!snap.alloc((size_t)(ck + 1) * N) || !lam.alloc(S * N) || !mu.alloc(S * N) || !nu.alloc(N) ||
       !psi.alloc(N) || !acc.alloc(8))
     return set_error(NNPP_ERR_NOMEM, "adjoint buffers");
@@ -172,11 +182,21 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       // adjoint potential solve on the unknowns of step n
       NNPP_TRY(launch_adj_solve_setup(h, sn, psi.get()));
       h.b_override = nu.get();
-      const int save_ex = h.extrapolate;
-      h.extrapolate = 0;
+      if (hm >= 3) {
+        // the adjoint potentials form their own warm-start ring
+        h.warm_x_alt = xa.get();
+        h.warm_b_alt = ba.get();
+        const int hs[2] = {an, ahead};
+        NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->hist_n, hs, sizeof(hs), cudaMemcpyHostToDevice, h.st));
+      }
       st = engine_solve(e, prec);
+      if (st == NNPP_OK && hm >= 3) {
+        ahead = (ahead + 1) % hm;
+        an = an < hm ? an + 1 : hm;
+        st = launch_record_solve(h, ahead);
+      }
       h.b_override = nullptr;
-      h.extrapolate = save_ex;
+      h.warm_x_alt = h.warm_b_alt = nullptr;
       if (st != NNPP_OK) break;
       NNPP_CUDA(cudaMemcpyAsync(psi.get(), h.phi64.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
       const double inject = (n > 0 && n % se == 0) ? -dV * dL_dmass[n / se - 1] : 0.0;

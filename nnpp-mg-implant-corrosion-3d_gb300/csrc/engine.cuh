@@ -129,6 +129,7 @@ nnpp_status launch_adj_combine(Handle& h, const double* mu, double* lam, double 
 nnpp_status launch_snap_state(Handle& h, Rec64* dst);
 nnpp_status launch_snap_phi(Handle& h, Rec64* dst);
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev);
+nnpp_status launch_record_solve(Handle& h, int slot);
 nnpp_status launch_sum_c0(Handle& h, double* out);
 
 }  // namespace nnpp

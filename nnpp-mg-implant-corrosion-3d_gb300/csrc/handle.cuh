@@ -51,6 +51,7 @@ struct KParams {
                                  // (1/(K sigma)) F CSolid sum_k z_k c_k (adjoint solves)
   // physics
   double dt, csat, c_floor, k_diss, sw, vol_red, lam;
+  float csat_hi, csat_lo, cfl_hi, cfl_lo;  // CSat/CSolid and c_floor as FP32 pairs
   double K1[S], K2zF[S], DL[S], DSo[S], z[S];
   int sub_step_no;
   int dissolve_count;            // 1: count the dissolution source into the diagnostics
@@ -114,6 +115,8 @@ struct Handle {
   int extrapolate = 1;
   int warm_hist = kHistMax;     // history length of the warm start (0: extrapolation only)
   DBuf<double> xh, bh;          // warm-start history, warm_hist * N each
+  double* warm_x_alt = nullptr; // another ring in place of xh, bh (the adjoint's solves)
+  double* warm_b_alt = nullptr;
   const double* b_override = nullptr;  // set during adjoint solves
   int grid = 0;                 // CTAs of the per-handle elementwise kernels
   Engine* engine = nullptr;     // single-instance engine (owned)

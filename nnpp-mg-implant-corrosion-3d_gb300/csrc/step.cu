@@ -374,6 +374,20 @@ __device__ __forceinline__ double warp_sum_d(double x) {
   return x;
 }
 
+// warp sum of FP32 pairs (hi, lo) with TwoSum at each level; lane 0 holds the pair sum to
+// ~2^-48 relative (as good as an FP64 sum of 32 terms, on the FP32 pipes)
+__device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, hi, off);
+    const float ol = __shfl_down_sync(0xffffffffu, lo, off);
+    float sum, err;
+    two_sum(hi, oh, sum, err);
+    hi = sum;
+    lo = lo + ol + err;
+  }
+}
+
 // node of a slot code: halo row start (per-warp table of the slice's tile) + offset
 __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
   return hb[code >> 12] + (int)(code & 4095u);
@@ -384,7 +398,7 @@ __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
 // column-major: one coalesced load per bond column), gathers z from L1/L2, one lane per row.
 // Slice partials are reduced per instance by the last CTA.
 template <int W>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
+__global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
@@ -404,20 +418,39 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv32(EngineView v) {
         const unsigned short* cs = k.sell_slot + d.off + lane;
         const float* ws = k.sell_w + d.off + lane;
         const float* z = k.z32;
+        // software pipeline: the next batch of streamed columns is in flight while the
+        // current batch's neighbour values are gathered
+        constexpr int B = 8;
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        int c = 0;
-        for (; c + 8 <= d.width; c += 8) {
-          float w[8];
-          unsigned int code[8];
+        const int nb = d.width / B;
+        float w[B];
+        unsigned int code[B];
+        if (nb > 0) {
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            w[u] = __ldcs(ws + 32 * (c + u));
-            code[u] = __ldcs(cs + 32 * (c + u));
+          for (int u = 0; u < B; ++u) {
+            w[u] = __ldcs(ws + 32 * u);
+            code[u] = __ldcs(cs + 32 * u);
+          }
+        }
+        for (int b = 0; b < nb; ++b) {
+          float zv[B];
+#pragma unroll
+          for (int u = 0; u < B; ++u) zv[u] = __ldg(z + code_node(hb, code[u]));
+          float wc[B];
+#pragma unroll
+          for (int u = 0; u < B; ++u) wc[u] = w[u];
+          if (b + 1 < nb) {
+            const int c1 = (b + 1) * B;
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+              w[u] = __ldcs(ws + 32 * (c1 + u));
+              code[u] = __ldcs(cs + 32 * (c1 + u));
+            }
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) acc[u & 3] = fmaf(w[u], __ldg(z + code_node(hb, code[u])), acc[u & 3]);
+          for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
-        for (; c < d.width; ++c)
+        for (int c = nb * B; c < d.width; ++c)
           acc[0] = fmaf(__ldcs(ws + 32 * c), __ldg(z + code_node(hb, __ldcs(cs + 32 * c))), acc[0]);
         const float za = z[a];
         const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
@@ -574,7 +607,7 @@ constexpr int kWarmSlots = kWarmD * (kWarmD + 1) / 2 + kWarmD + 1;  // G (upper)
 static_assert(kWarmSlots <= kReduceSlots, "warm-start partials exceed the reduction buffer");
 
 __device__ __forceinline__ int warm_history(const KParams& k) {
-  if (k.hist_m < 3 || !k.extrapolate || k.b_override) return 0;
+  if (k.hist_m < 3 || !k.extrapolate) return 0;
   const int n = k.ds->hist_n;
   return n < k.hist_m ? n : k.hist_m;
 }
@@ -658,10 +691,16 @@ __global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
           tx[j] = j < H ? k.xh[o] : 0.0;
           tb[j] = j < H ? k.bh[o] : 0.0;
         }
-        double R11 = 0.0;
+        double bn;
+        if (k.b_override) {
+          bn = k.b_override[a];  // adjoint solves: the given right-hand side
+        } else {
+          double R11 = 0.0;
 #pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) R11 += k.z[s2] * conc_of<P>(k, a, s2);
-        const double g = k.lam * R11 - tb[0];
+          for (int s2 = 0; s2 < S; ++s2) R11 += k.z[s2] * conc_of<P>(k, a, s2);
+          bn = k.lam * R11;
+        }
+        const double g = bn - tb[0];
         const double xax = tx[0] * tb[0];
         double dx[kWarmD], db[kWarmD];
         warm_diffs(tx, H, dx);
@@ -688,6 +727,15 @@ __global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
       }
     }
     __syncthreads();
+  }
+}
+
+// the solution of a solve run outside a step (adjoint) and A x = b - r into ring slot `slot`
+__global__ void k_record_solve(KParams k, int slot) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    const size_t o = (size_t)slot * k.N + a;
+    k.xh[o] = k.phi64[a];
+    k.bh[o] = k.freem[a] ? k.b64[a] - k.r64[a] : 0.0;
   }
 }
 
@@ -863,7 +911,7 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
 // neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
 // partials of the diagnostics are reduced per instance by the last CTA.
 template <int W, bool RESID>
-__global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_out) {
+__global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double* F_out) {
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
@@ -875,9 +923,10 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
     const KParams& k = v.inst[d.inst];
     if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
     __syncwarp();
-    double part[kDiagSlots];
+    float ph_hi[6], ph_lo[6];  // masses[4], solid volume sum, dissolved (FP32 pairs)
 #pragma unroll
-    for (int q = 0; q < kDiagSlots; ++q) part[q] = 0.0;
+    for (int q = 0; q < 6; ++q) ph_hi[q] = ph_lo[q] = 0.0f;
+    int n_solid = 0, n_bad = 0;
     const int a = d.row0 + lane;
     if (lane < d.nrows) {
       const int* hb = s_hb[warp];
@@ -910,10 +959,17 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
       const unsigned short* cs = k.sell_slot + d.off + lane;
       const float* ws = k.sell_w + d.off + lane;
       const int len = k.row[a + 1] - k.row[a];
+      // the next streamed column is in flight while this one's neighbour record is gathered
+      float wn = len > 0 ? __ldcs(ws) : 0.0f;
+      unsigned int cn_code = len > 0 ? __ldcs(cs) : 0u;
 #pragma unroll 2
       for (int c = 0; c < len; ++c) {
-        const float w = __ldcs(ws + 32 * c);
-        const int n = code_node(hb, __ldcs(cs + 32 * c));
+        const float w = wn;
+        const int n = code_node(hb, cn_code);
+        if (c + 1 < len) {
+          wn = __ldcs(ws + 32 * (c + 1));
+          cn_code = __ldcs(cs + 32 * (c + 1));
+        }
         const float4 cn = __ldg(rc + 2 * n);
         const float4 nb = __ldg(rc + 2 * n + 1);
         const bool nsol = nb.z != 0.0f;
@@ -929,9 +985,8 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
       }
       const unsigned char dm = k.dirmask[a];
       const float4 lo4 = k.clo[a];
-      const double c0old = (double)ca.x + (double)lo4.x;
       const bool src_on = iface && !(dm & 1);
-      const double swv = src_on ? dissolve_switch(c0old, k.csat, k.sw) : 0.0;
+      const double swv = src_on ? dissolve_switch((double)ca.x + (double)lo4.x, k.csat, k.sw) : 0.0;
       const float Rmg = src_on ? (float)(-k.k_diss * swv) : 0.0f;
       if (RESID) {
 #pragma unroll
@@ -939,9 +994,10 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
           F_out[(size_t)s * k.N + a] =
               -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
       } else {
+        // c + dt (K1 a1 + K2 a2 + R) on the compensated pair (hi, lo), renormalised: hi is
+        // the FP32 rounding of the exact pair sum and lo its exact remainder
         const float dtf = (float)k.dt;
         float hi[S], lo[S];
-        double val[S];
         bool bad = false;
 #pragma unroll
         for (int s = 0; s < S; ++s) {
@@ -949,17 +1005,22 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
           float tt, e1, sh, e2;
           two_sum(sel4(lo4, s), inc, tt, e1);
           two_sum(sel4(ca, s), tt, sh, e2);
-          double x = (double)sh + (double)(e1 + e2);
-          if ((dm >> s) & 1) x = k.bcval[(size_t)s * k.N + a];
-          if (x < k.c_floor) x = k.c_floor;
-          if (!isfinite(x)) bad = true;
-          const float xh = (float)x;
-          hi[s] = xh;
-          lo[s] = (float)(x - (double)xh);
-          val[s] = x;
+          two_sum(sh, e1 + e2, hi[s], lo[s]);
+          if ((dm >> s) & 1) {
+            const double x = k.bcval[(size_t)s * k.N + a];
+            hi[s] = (float)x;
+            lo[s] = (float)(x - (double)hi[s]);
+          }
+          // clamp c >= c_floor (main.cpp:805-837), compared on the normalised pairs
+          if (hi[s] < k.cfl_hi || (hi[s] == k.cfl_hi && lo[s] < k.cfl_lo)) {
+            hi[s] = k.cfl_hi;
+            lo[s] = k.cfl_lo;
+          }
+          bad = bad || !isfinite(hi[s]);
         }
         float pnew = pa;
-        if (pa != 0.0f && val[0] <= k.csat) {
+        // saturation test in FP64 (main.cpp:914-922)
+        if (pa != 0.0f && (double)hi[0] + (double)lo[0] <= k.csat) {
           pnew = 0.0f;
           k.flip_step[a] = (int)(k.ds->steps + 1);
         }
@@ -974,23 +1035,44 @@ __global__ void __launch_bounds__(kBlock) k_transport32(EngineView v, double* F_
         out.pad = 0.0f;
         k.rec32_nxt[a] = out;
         k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        // diagnostics as FP32 pairs: masses, solid volume sum (c_0 - CSat/CSolid), dissolved
 #pragma unroll
-        for (int s = 0; s < S; ++s) part[s] = val[s];
-        if (pnew != 0.0f) {
-          part[4] = 1.0;
-          part[5] = val[0] - k.csat;
+        for (int s = 0; s < S; ++s) {
+          ph_hi[s] = hi[s];
+          ph_lo[s] = lo[s];
         }
-        part[6] = k.k_diss * swv;
-        part[7] = bad ? 1.0 : 0.0;
+        if (pnew != 0.0f) {
+          n_solid = 1;
+          float vs, ve;
+          two_sum(hi[0], -k.csat_hi, vs, ve);
+          ph_hi[4] = vs;
+          ph_lo[4] = ve + (lo[0] - k.csat_lo);
+        }
+        if (src_on) {
+          const double dv = k.k_diss * swv;
+          ph_hi[5] = (float)dv;
+          ph_lo[5] = (float)(dv - (double)ph_hi[5]);
+        }
+        n_bad = bad ? 1 : 0;
       }
     }
     __syncwarp();
     if (!RESID) {
 #pragma unroll
-      for (int q = 0; q < kDiagSlots; ++q) part[q] = warp_sum_d(part[q]);
-      if (lane == 0)
+      for (int q = 0; q < 6; ++q) pair_warp_sum(ph_hi[q], ph_lo[q]);
+      n_solid = __reduce_add_sync(0xffffffffu, n_solid);
+      n_bad = __reduce_add_sync(0xffffffffu, n_bad);
+      if (lane == 0) {
+        double* pp = v.partials + sg;
+        const size_t st = v.stride;
 #pragma unroll
-        for (int q = 0; q < kDiagSlots; ++q) v.partials[(size_t)q * v.stride + sg] = part[q];
+        for (int s = 0; s < S; ++s) pp[s * st] = (double)ph_hi[s] + (double)ph_lo[s];
+        pp[4 * st] = (double)n_solid;
+        pp[5 * st] = (double)ph_hi[4] + (double)ph_lo[4];
+        pp[6 * st] = (double)ph_hi[5] + (double)ph_lo[5];
+        pp[7 * st] = (double)n_bad;
+        pp[8 * st] = 0.0;
+      }
     }
   }
   if (RESID) return;
@@ -1557,6 +1639,13 @@ nnpp_status launch_snap_phi(Handle& h, Rec64* dst) {
   return NNPP_OK;
 }
 
+nnpp_status launch_record_solve(Handle& h, int slot) {
+  KParams kp = make_kparams(h, h.cur);
+  k_record_solve<<<h.grid, kBlock, 0, h.st>>>(kp, slot);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev) {
   KParams kp = make_kparams(h, h.cur);
   k_adj_solve_setup<<<h.grid, kBlock, 0, h.st>>>(kp, snap, psi_prev);
@@ -1760,6 +1849,10 @@ KParams make_kparams(Handle& h, int cur) {
   k.dt = p.dt;
   k.csat = p.CSat / p.CSolid;
   k.c_floor = p.c_floor;
+  k.csat_hi = (float)k.csat;
+  k.csat_lo = (float)(k.csat - (double)k.csat_hi);
+  k.cfl_hi = (float)k.c_floor;
+  k.cfl_lo = (float)(k.c_floor - (double)k.cfl_hi);
   k.k_diss = p.k_diss;
   k.sw = p.switch_width;
   k.vol_red = p.vol_red;
@@ -1775,8 +1868,8 @@ KParams make_kparams(Handle& h, int cur) {
   k.dissolve_count = 1;
   k.extrapolate = h.extrapolate;
   k.hist_m = (h.extrapolate && h.warm_hist >= 3 && h.xh.get()) ? h.warm_hist : 0;
-  k.xh = h.xh.get();
-  k.bh = h.bh.get();
+  k.xh = h.warm_x_alt ? h.warm_x_alt : h.xh.get();
+  k.bh = h.warm_b_alt ? h.warm_b_alt : h.bh.get();
   return k;
 }
 
