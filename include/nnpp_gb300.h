@@ -259,9 +259,15 @@ nnpp_status nnpp_forward_timed(nnpp_handle* h, int n_steps, int precision, doubl
 nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int reps,
                              double* ms_per_launch);
 
-/* Autotuned configuration of the handle's kernels: bins per tile and lanes per node (both 0
- * before the first step). */
-nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node);
+/* The execution configuration of the handle's kernels: bins per tile, lanes per node of the
+ * FP64 tile kernels, and whether the FP32 CG operator streams its slices through
+ * bulk-copy-staged shared memory (1) or gathers from L1/L2 (0).  Chosen by the autotuner on
+ * the first run (all 0 / -1 before); nnpp_set_tuning pins a configuration instead (bins in
+ * {2,4,8,16}, lanes in {4,8,16}; NNPP_ERR_UNSUPPORTED when a tile halo does not fit). */
+nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node,
+                            int* staged_operator);
+nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_node,
+                            int staged_operator);
 
 /* ---- differentiation ------------------------------------------------------------------ */
 

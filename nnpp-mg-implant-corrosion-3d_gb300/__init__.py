@@ -99,7 +99,8 @@ _SIGS = {
     "nnpp_solve_potential": (C.c_int, [_P, C.c_int, _DP, _IP, _DP, _IP, _DP]),
     "nnpp_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
     "nnpp_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
-    "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP]),
+    "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP, _IP]),
+    "nnpp_set_tuning": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
     "nnpp_set_warm_start": (C.c_int, [_P, C.c_int]),
@@ -338,9 +339,14 @@ class Simulation:
         return gD, gk.value
 
     def tuning(self):
-        t, w = C.c_int(0), C.c_int(0)
-        _check(lib().nnpp_get_tuning(self._h, C.byref(t), C.byref(w)))
-        return t.value, w.value
+        """(bins per tile, lanes per node, staged CG operator) of the autotuned engine."""
+        t, w, g = C.c_int(0), C.c_int(0), C.c_int(0)
+        _check(lib().nnpp_get_tuning(self._h, C.byref(t), C.byref(w), C.byref(g)))
+        return t.value, w.value, g.value
+
+    def set_tuning(self, bins_per_tile, lanes_per_node, staged_operator):
+        """Pin the execution configuration instead of autotuning it."""
+        _check(lib().nnpp_set_tuning(self._h, bins_per_tile, lanes_per_node, int(staged_operator)))
 
     def state(self):
         c = np.empty((NSPECIES, self.N), dtype=np.float64)

@@ -119,6 +119,7 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
     if (s % sample_every == 0) {
       DevState ds;
       NNPP_TRY(read_ds(h, &ds));
+      if (ds.wait_timeout) return set_error(NNPP_ERR_CUDA, "a bounded device wait timed out");
       if (ds.nonfinite) return set_error(NNPP_ERR_NONFINITE, "non-finite concentration in the state");
       h.curve[s / sample_every - 1] = dV * (m0 - ds.mg_mass_now);
     }
@@ -140,6 +141,8 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
   const double dV = h.p.dx * h.p.dy * h.p.dz;
   DBuf<Rec64> snap;
   DBuf<double> lam, mu, nu, psi, acc, xa, ba;
+  DBuf<float4> arec;  // FP32 adjoint records (mixed precision)
+  if (prec == NNPP_MIXED && !arec.alloc(3 * N)) return set_error(NNPP_ERR_NOMEM, "adjoint records");
   // warm-start ring of the adjoint potential solves (host-tracked fill and head)
   const int hm = (h.extrapolate && h.warm_hist >= 3 && h.xh.get()) ? h.warm_hist : 0;
   int an = 0, ahead = hm ? hm - 1 : 0;
@@ -178,7 +181,10 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       const Rec64* sn1 = snap.get() + (size_t)(n - s0 + 1) * N;
       NNPP_TRY(engine_params(e));
       EngineView v = make_view(e, 0, 0);
-      NNPP_TRY(launch_adj_transport(e, v, sn, sn1, lam.get(), mu.get(), nu.get(), acc.get(), h.st));
+      if (prec == NNPP_MIXED)
+        NNPP_TRY(launch_adj_transport32(e, v, h, sn, sn1, lam.get(), arec.get(), mu.get(), nu.get(), acc.get(), h.st));
+      else
+        NNPP_TRY(launch_adj_transport(e, v, sn, sn1, lam.get(), mu.get(), nu.get(), acc.get(), h.st));
       // adjoint potential solve on the unknowns of step n
       NNPP_TRY(launch_adj_solve_setup(h, sn, psi.get()));
       h.b_override = nu.get();

@@ -67,7 +67,7 @@ struct DevState {
   double last_relres;
   long long outer_total;
   int nonfinite;
-  int pad0;
+  int wait_timeout;   // a bounded device wait gave up (the step's results are invalid)
   // potential solve
   double bnorm2;      // ||b_eff||^2
   double rnorm2;      // ||r||^2 of the outer (FP64) residual

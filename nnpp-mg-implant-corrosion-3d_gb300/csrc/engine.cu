@@ -123,6 +123,7 @@ nnpp_status tune(Engine& e, int prec) {
   const int Ws[3] = {4, 8, 16};
   float best = 1e30f;
   int bT = 4, bW = 8;
+  bool bS = false;
   cudaEvent_t e0, e1;
   NNPP_CUDA(cudaEventCreate(&e0));
   NNPP_CUDA(cudaEventCreate(&e1));
@@ -140,20 +141,25 @@ nnpp_status tune(Engine& e, int prec) {
       EngineView v = make_view(e, 0, 0);
       NNPP_TRY(set_active(e, 1, 1));
       NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
-      NNPP_TRY(set_active(e, 1, 1));
-      NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
-      cudaEventRecord(e0, e.st);
-      // the CG operator dominates; the FP64 tile kernels (residual, prep) follow the lanes
-      for (int r = 0; r < 5; ++r) NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
-      if (prec == NNPP_MIXED) NNPP_TRY(launch_cg_spmv_b(e, v, NNPP_FP64, e.st));
-      cudaEventRecord(e1, e.st);
-      NNPP_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best) {
-        best = ms;
-        bT = T;
-        bW = W;
+      const int nvar = (prec == NNPP_MIXED && spmv_staged_fits(e.halo_max)) ? 2 : 1;
+      for (int var = 0; var < nvar; ++var) {
+        e.spmv_staged = var == 1;
+        NNPP_TRY(set_active(e, 1, 1));
+        NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+        cudaEventRecord(e0, e.st);
+        // the CG operator dominates; the FP64 tile kernels (residual, prep) follow the lanes
+        for (int r = 0; r < 5; ++r) NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
+        if (prec == NNPP_MIXED) NNPP_TRY(launch_cg_spmv_b(e, v, NNPP_FP64, e.st));
+        cudaEventRecord(e1, e.st);
+        NNPP_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+          best = ms;
+          bT = T;
+          bW = W;
+          bS = e.spmv_staged;
+        }
       }
     }
   }
@@ -164,6 +170,7 @@ nnpp_status tune(Engine& e, int prec) {
     NNPP_CUDA(cudaMemcpy(e.members[i]->dstate.get(), &saved[i], sizeof(DevState), cudaMemcpyHostToDevice));
   NNPP_TRY(build_lists(e, bT));
   e.W = bW;
+  e.spmv_staged = bS;
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, bW));
   e.tuned = true;
   return NNPP_OK;
@@ -401,6 +408,8 @@ nnpp_status engine_warm(Engine& e, int prec) {
 }
 
 nnpp_status engine_params(Engine& e) { return refresh_params(e); }
+
+nnpp_status engine_set_tiles(Engine& e, int T) { return build_lists(e, T); }
 
 nnpp_status engine_solve(Engine& e, int prec) {
   NNPP_TRY(prepare_run(e, prec));

@@ -72,6 +72,7 @@ struct Engine {
   int W = 8;                // lanes per node (autotuned)
   bool tuned = false;
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
+  bool spmv_staged = false; // FP32 CG operator: bulk-copy staged (true) or L1/L2 gathers
   int grid = 0;
   int sms = 152;
   int halo_max = 0;
@@ -108,6 +109,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
 
 // step.cu launchers (batched)
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
+bool spmv_staged_fits(int halo_max);
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out);
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
@@ -120,6 +122,7 @@ nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, c
 nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                double* F_out);
 nnpp_status prepare_kernels(int halo_max, int bond_max, int W);
+nnpp_status engine_set_tiles(Engine& e, int T);  // work lists for T bins per tile
 
 // adjoint (step.cu)
 nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec64* snap,
@@ -130,6 +133,9 @@ nnpp_status launch_snap_state(Handle& h, Rec64* dst);
 nnpp_status launch_snap_phi(Handle& h, Rec64* dst);
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev);
 nnpp_status launch_record_solve(Handle& h, int slot);
+nnpp_status launch_adj_transport32(const Engine& e, const EngineView& v, Handle& h, const Rec64* snap,
+                                   const Rec64* snap1, const double* lam, float4* rec, double* mu,
+                                   double* nu, double* acc, cudaStream_t st);
 nnpp_status launch_sum_c0(Handle& h, double* out);
 
 }  // namespace nnpp

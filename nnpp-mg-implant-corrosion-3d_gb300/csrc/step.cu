@@ -24,6 +24,7 @@
 #include <cstring>
 
 #include "engine.cuh"
+#include "tma.cuh"
 
 namespace nnpp {
 
@@ -466,6 +467,158 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
     part = warp_sum_d(part);
     if (lane == 0) v.partials[sg] = part;
   }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[1];
+      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = v.inst[i].ds;
+        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+      }
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
+// Staged FP32 CG operator (the same product as k_cg_spmv32): a CTA walks tiles, stages the
+// tile's halo of z in shared memory, and its 8 warps take the tile's 32-row slices.  Each
+// warp streams its slices' slot codes and weights through a private ring of kTmaStages
+// shared-memory stages (kTmaCol bond columns each) filled by cp.async.bulk and completed on
+// one mbarrier per stage: lane 0 refills a stage as soon as the warp has consumed it, so
+// kTmaStages columns blocks are always in flight and the gathers hit shared memory only.
+constexpr int kTmaCol = 32;
+constexpr int kTmaStages = 4;
+constexpr int kStageW = kTmaCol * 32 * 4;  // weights of one stage (bytes)
+constexpr int kStageC = kTmaCol * 32 * 2;  // slot codes of one stage (bytes)
+constexpr int kStageBytes = kStageW + kStageC;
+constexpr int kWarpsCta = kBlock / 32;
+constexpr size_t kTmaRingBytes = (size_t)kWarpsCta * kTmaStages * kStageBytes;
+constexpr size_t kTmaBarBytes = (size_t)kWarpsCta * kTmaStages * sizeof(uint64_t);
+constexpr unsigned kWaitPolls = 1u << 22;
+
+__device__ __forceinline__ int tma_chunks(int width) { return width > 0 ? (width + kTmaCol - 1) / kTmaCol : 1; }
+
+// position of a warp's producer in its sequence (tile item, slice, chunk)
+struct TmaCursor {
+  int item, sl, ch;
+};
+
+__device__ __forceinline__ bool tma_seek(const EngineView& v, TmaCursor& c, int warp) {
+  while (c.item < v.ntiles) {
+    const TileDesc& t = v.tiles[c.item];
+    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
+    const bool act = *((volatile int*)&v.inst[t.inst].ds->inner_active) != 0;
+    if (act && c.sl < nsl) return true;
+    c.item += gridDim.x;
+    c.sl = warp;
+    c.ch = 0;
+  }
+  return false;
+}
+
+// lane 0: issue the cursor's chunk into stage `stage` and advance; false when exhausted
+__device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, int warp, int stage,
+                                            unsigned char* ring, uint64_t* bars) {
+  if (!tma_seek(v, c, warp)) return false;
+  const TileDesc& t = v.tiles[c.item];
+  const KParams& k = v.inst[t.inst];
+  const SliceDesc& d = v.slices[t.slice0 + c.sl];
+  const int c0 = c.ch * kTmaCol;
+  const int cc = min(kTmaCol, max(d.width - c0, 0));
+  unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
+  uint64_t* bar = bars + warp * kTmaStages + stage;
+  fence_proxy_async_smem();
+  mbar_arrive_expect_tx(bar, (unsigned)(cc * 32 * 6));
+  if (cc > 0) {
+    const size_t e0 = (size_t)d.off + (size_t)c0 * 32;
+    bulk_g2s(buf, k.sell_w + e0, (unsigned)(cc * 32 * 4), bar);
+    bulk_g2s(buf + kStageW, k.sell_slot + e0, (unsigned)(cc * 32 * 2), bar);
+  }
+  if (++c.ch >= tma_chunks(d.width)) {
+    c.ch = 0;
+    c.sl += kWarpsCta;
+  }
+  return true;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ TileSmem ts;
+  __shared__ double sm[kBlock / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* ring = dsm;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dsm + kTmaRingBytes);
+  float* hs = reinterpret_cast<float*>(dsm + kTmaRingBytes + kTmaBarBytes);
+  if (threadIdx.x < kWarpsCta * kTmaStages) mbar_init(bars + threadIdx.x, 1);
+  fence_mbar_init();
+  __syncthreads();
+  TmaCursor pc{(int)blockIdx.x, warp, 0};
+  if (lane == 0)
+    for (int st = 0; st < kTmaStages; ++st)
+      if (!tma_produce(v, pc, warp, st, ring, bars)) break;
+  __syncwarp();
+  int stage = 0;
+  unsigned phases = 0u;
+  int timed_out = -1;  // instance whose wait gave up
+  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
+    const TileDesc t = v.tiles[item];
+    const KParams& k = v.inst[t.inst];
+    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
+    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
+    if (active) {
+      load_tile(t, ts);
+      const float* z = k.z32;
+      for (int s2 = threadIdx.x; s2 < t.halo; s2 += kBlock) hs[s2] = z[halo_node(ts, s2)];
+    }
+    __syncthreads();
+    for (int sl = warp; sl < nsl; sl += kWarpsCta) {
+      double part = 0.0;
+      if (active) {
+        const SliceDesc d = v.slices[t.slice0 + sl];
+        float acc0 = 0.0f, acc1 = 0.0f;
+        const int nch = tma_chunks(d.width);
+        for (int ch = 0; ch < nch; ++ch) {
+          uint64_t* bar = bars + warp * kTmaStages + stage;
+          if (!mbar_wait_bounded(bar, (phases >> stage) & 1u, kWaitPolls)) timed_out = t.inst;
+          phases ^= 1u << stage;
+          const unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
+          const float* sw = reinterpret_cast<const float*>(buf) + lane;
+          const unsigned short* sc = reinterpret_cast<const unsigned short*>(buf + kStageW) + lane;
+          const int cc = min(kTmaCol, d.width - ch * kTmaCol);
+          int c = 0;
+          for (; c + 1 < cc; c += 2) {
+            const unsigned q0 = sc[32 * c], q1 = sc[32 * c + 32];
+            acc0 = fmaf(sw[32 * c], hs[ts.off[q0 >> 12] + (int)(q0 & 4095u)], acc0);
+            acc1 = fmaf(sw[32 * c + 32], hs[ts.off[q1 >> 12] + (int)(q1 & 4095u)], acc1);
+          }
+          if (c < cc) {
+            const unsigned q0 = sc[32 * c];
+            acc0 = fmaf(sw[32 * c], hs[ts.off[q0 >> 12] + (int)(q0 & 4095u)], acc0);
+          }
+          __syncwarp();
+          if (lane == 0) tma_produce(v, pc, warp, stage, ring, bars);
+          stage = stage + 1 == kTmaStages ? 0 : stage + 1;
+        }
+        const int a = d.row0 + lane;
+        if (lane < d.nrows && k.freem[a]) {
+          const float za = hs[ts.off[4] + (a - t.hb[4])];
+          const float sa = k.d32[a] * za - (acc0 + acc1);
+          const float beta = (float)k.ds->beta;
+          const float qn = sa + beta * k.q32[a];
+          const float pn = za + beta * k.p32[a];
+          k.q32[a] = qn;
+          k.p32[a] = pn;
+          part = (double)pn * (double)qn;
+        }
+      }
+      part = warp_sum_d(part);
+      if (lane == 0) v.partials[t.slice0 + sl] = part;
+    }
+    __syncthreads();
+  }
+  if (timed_out >= 0 && lane == 0) v.inst[timed_out].ds->wait_timeout = 1;
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
@@ -1383,6 +1536,7 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
+size_t smem_spmv_staged(int H) { return kTmaRingBytes + kTmaBarBytes + align16((size_t)H * sizeof(float)); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) + 1)) + smem_slots(B) + 16; }
 
@@ -1536,6 +1690,132 @@ __global__ void __launch_bounds__(kBlock) k_adj_transport(EngineView v, AdjArgs 
   }
 }
 
+// Mixed adjoint transport: the same transpose in FP32 on the sliced operator.  k_adj_pack
+// writes per node the 48-byte record {c[4], masked lambda[4], phi_hi, phi_lo, phase, 0};
+// k_adj_transport32 streams the slices (one lane per node), gathers the neighbours' records
+// from L1/L2, forms the differences directly (no cancellation of large sums) and
+// accumulates the parameter sensitivities as FP32 pairs.
+__global__ void k_adj_pack(KParams k, const Rec64* snap, const Rec64* snap1, const double* lam,
+                           float4* rec) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    const Rec64 r = snap[a];
+    const Rec64 r1 = snap1[a];
+    const unsigned char dm = k.dirmask[a];
+    float lh[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+      const bool zero = ((dm >> q) & 1) || r1.c[q] == k.c_floor;
+      lh[q] = zero ? 0.0f : (float)lam[(size_t)q * k.N + a];
+    }
+    const float ph = (float)r.phi;
+    rec[3 * a] = make_float4((float)r.c[0], (float)r.c[1], (float)r.c[2], (float)r.c[3]);
+    rec[3 * a + 1] = make_float4(lh[0], lh[1], lh[2], lh[3]);
+    rec[3 * a + 2] = make_float4(ph, (float)(r.phi - (double)ph), r.phase != 0.0 ? 1.0f : 0.0f, 0.0f);
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, const float4* rec,
+                                                               double* mu, double* nu, double* acc) {
+  __shared__ int s_hb[kBlock / 32][12];
+  __shared__ double sm[5 * kBlock / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+    __syncwarp();
+    float gh[5], gl[5];  // dL/dD_k (4), dL/dk as FP32 pairs
+#pragma unroll
+    for (int q = 0; q < 5; ++q) gh[q] = gl[q] = 0.0f;
+    const int a = d.row0 + lane;
+    if (lane < d.nrows) {
+      const int* hb = s_hb[warp];
+      const float4 cm4 = rec[3 * a], lm4 = rec[3 * a + 1], pm4 = rec[3 * a + 2];
+      const bool pm = pm4.z != 0.0f;
+      float cfL[S], cfS[S];  // pair coefficient for a liquid / solid neighbour (BV = 1)
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const float dl = (float)k.DL[q], ds = (float)k.DSo[q];
+        cfL[q] = pm ? ds : dl;
+        cfS[q] = pm ? (q == 0 ? ds : 0.0f) : ds;
+      }
+      float A1[S], A2[S], a1[S], a2[S], sl[S], sc[S];
+#pragma unroll
+      for (int q = 0; q < S; ++q) A1[q] = A2[q] = a1[q] = a2[q] = sl[q] = sc[q] = 0.0f;
+      int iface = 0;
+      const unsigned short* cs = k.sell_slot + d.off + lane;
+      const float* ws = k.sell_w + d.off + lane;
+      const int len = k.row[a + 1] - k.row[a];
+      for (int c = 0; c < len; ++c) {
+        const float w = __ldcs(ws + 32 * c);
+        const int n = code_node(hb, __ldcs(cs + 32 * c));
+        const float4 cn = __ldg(rec + 3 * n), ln = __ldg(rec + 3 * n + 1), pn = __ldg(rec + 3 * n + 2);
+        const bool nsol = pn.z != 0.0f;
+        iface |= (pm && !nsol) ? 1 : 0;
+        const float dphi = (pm4.x - pn.x) + (pm4.y - pn.y);  // phi_m - phi_i
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+          const float Dw = (nsol ? cfS[q] : cfL[q]) * w;
+          const float li = sel4(ln, q), ci = sel4(cn, q);
+          A1[q] = fmaf(Dw, li - sel4(lm4, q), A1[q]);
+          a1[q] = fmaf(Dw, ci - sel4(cm4, q), a1[q]);
+          const float tl = Dw * li, tc = Dw * ci;
+          A2[q] = fmaf(tl, dphi, A2[q]);
+          a2[q] = fmaf(-tc, dphi, a2[q]);
+          sl[q] += tl;
+          sc[q] += tc;
+        }
+      }
+      const unsigned char dm = k.dirmask[a];
+      const bool src = iface && !(dm & 1);
+      const float dt = (float)k.dt;
+      float nu_a = 0.0f;
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const float K1 = (float)k.K1[q], K2 = (float)k.K2zF[q];
+        const float lmq = sel4(lm4, q), cmq = sel4(cm4, q);
+        float m = lmq + dt * (K1 * A1[q] + K2 * A2[q]);
+        if (q == 0 && src) {
+          const double swd = dissolve_switch((double)cm4.x, k.csat, k.sw);
+          const double dsw = k.sw > 0.0 ? swd * (1.0 - swd) / k.sw : 0.0;
+          m += lmq * (float)(-k.dt * k.k_diss * dsw);
+          const float gk = lmq * (float)(-k.dt * swd);
+          float ek;
+          two_sum(gh[4], gk, gh[4], ek);
+          gl[4] += ek;
+        }
+        mu[(size_t)q * k.N + a] = (double)m;
+        nu_a = fmaf(dt * K2, cmq * sl[q] - lmq * sc[q], nu_a);
+        const float gq = lmq * dt * (K1 * a1[q] + K2 * a2[q]) / (float)k.DL[q];
+        float e;
+        two_sum(gh[q], gq, gh[q], e);
+        gl[q] += e;
+      }
+      nu[a] = (double)nu_a;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 5; ++q) pair_warp_sum(gh[q], gl[q]);
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) v.partials[(size_t)q * v.stride + sg] = (double)gh[q] + (double)gl[q];
+  }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[5];
+      reduce_items<5>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      if (threadIdx.x == 0)
+        for (int q = 0; q < 5; ++q) acc[q] += tot[q];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
 // lambda^n = mu + (1/(K sigma)) F CSolid z_k psi on the unknowns, + the loss injection on
 // species 0 (d(mass loss)/dc_0 = -dV times dL/d(sample))
 __global__ void k_adj_combine(KParams k, const double* mu, double* lam, double inject) {
@@ -1618,6 +1898,18 @@ nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec
   });
 }
 
+nnpp_status launch_adj_transport32(const Engine& e, const EngineView& v, Handle& h, const Rec64* snap,
+                                   const Rec64* snap1, const double* lam, float4* rec, double* mu,
+                                   double* nu, double* acc, cudaStream_t st) {
+  KParams kp = make_kparams(h, h.cur);
+  k_adj_pack<<<h.grid, kBlock, 0, st>>>(kp, snap, snap1, lam, rec);
+  NNPP_CUDA(cudaGetLastError());
+  k_adj_transport32<4><<<occ_grid(k_adj_transport32<4>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(
+      v, rec, mu, nu, acc);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_adj_combine(Handle& h, const double* mu, double* lam, double inject) {
   KParams kp = make_kparams(h, h.cur);
   k_adj_combine<<<h.grid, kBlock, 0, h.st>>>(kp, mu, lam, inject);
@@ -1671,6 +1963,7 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
+    if (smem_spmv_staged(H) <= 227 * 1024) NNPP_TRY(allow_smem(k_cg_spmv32t<W>, smem_spmv_staged(H)));
     NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
@@ -1678,6 +1971,8 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     return NNPP_OK;
   });
 }
+
+bool spmv_staged_fits(int halo_max) { return smem_spmv_staged(halo_max) <= 227 * 1024; }
 
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
   if (prec == NNPP_MIXED) {
@@ -1719,7 +2014,12 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v);
+      if (e.spmv_staged) {
+        const size_t sh = smem_spmv_staged(v.halo_max);
+        k_cg_spmv32t<W><<<occ_grid(k_cg_spmv32t<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v);
+      } else {
+        k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v);
+      }
     else
       { const size_t sh = smem_vec64(v.halo_max, v.bond_max); k_cg_spmv64<W><<<occ_grid(k_cg_spmv64<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }
     NNPP_CUDA(cudaGetLastError());

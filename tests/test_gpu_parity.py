@@ -325,3 +325,37 @@ def test_warm_start_rejects_bad_history(gpu):
     with pytest.raises(nn.NNPPError) as e:
         sim.set_warm_start(7)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("staged", [0, 1])
+def test_cg_operator_variants_vs_oracle(gpu, orc, staged):
+    """Both FP32 CG operators (L1/L2 gathers; bulk-copy-staged slices) reach the oracle's
+    state to the mixed-precision tolerance, with the configuration pinned."""
+    nn = gpu
+    inp = nn.synth(1, 20, seed=11)
+    o = orc.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    o.forward(100)
+    c_o, phi_o, ph_o, _ = o.state()
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    sim.set_tuning(8, 8, staged)
+    sim.forward(100, nn.MIXED)
+    assert sim.tuning() == (8, 8, staged)
+    c_g, phi_g, ph_g = sim.state()
+    assert np.array_equal(ph_g, ph_o)
+    assert np.linalg.norm(c_g - c_o) / np.linalg.norm(c_o) <= 1e-5
+    assert np.linalg.norm(phi_g - phi_o) / np.linalg.norm(phi_o) <= 1e-5
+    assert sim.diagnostics()["cg_not_converged"] == 0
+
+
+def test_set_tuning_rejects_bad_configuration(gpu):
+    nn = gpu
+    inp = nn.synth(1, 12, seed=4)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 2)):
+        with pytest.raises(nn.NNPPError) as e:
+            sim.set_tuning(*bad)
+        assert e.value.status == 1
