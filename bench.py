@@ -314,6 +314,17 @@ def run_ours(args):
         t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
         t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
         t_upd = sim.time_kernel(3, nn.MIXED, reps=50)
+    tuned = sim.tuning()
+    variants = {}
+    with ProfileRange("variants"):
+        for staged in (0, 1):
+            key = "staged" if staged else "gather"
+            try:
+                sim.set_tuning(tuned[0], tuned[1], staged)
+                variants[key] = sim.time_kernel(1, nn.MIXED, reps=50)
+            except nn.NNPPError as ex:
+                variants[key] = "unsupported: %s" % ex
+    sim.set_tuning(*tuned)
     k64 = {"cg_spmv": sim64.time_kernel(1, nn.FP64, reps=20),
            "transport": sim64.time_kernel(0, nn.FP64, reps=10),
            "cg_update": sim64.time_kernel(3, nn.FP64, reps=20)}
@@ -349,6 +360,7 @@ def run_ours(args):
                           for k in alg if k != dom}
     roofline["share_of_step"] = {k: v / ms_step for k, v in shares.items()}
     roofline["fp64_path_ms_per_launch"] = k64
+    roofline["cg_operator_variants_ms"] = variants
 
     # end to end through the public API with host buffers (nnpp_step_host)
     e2e = None
@@ -399,7 +411,9 @@ def run_ours(args):
                                    "4 species + potential, delta=3.015dx, mixed precision",
                        "n_nodes": N, "bonds": nnz, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "not flushed: per-bond arrays (%.2f GB) exceed the 129 MB L2" % ((4 + 4 + 8) * nnz / 1e9),
-                       "potential_tol": 1e-10},
+                       "potential_tol": 1e-10,
+                       "tuning": {"bins_per_tile": tuned[0], "lanes_per_node": tuned[1],
+                                  "staged_cg_operator": tuned[2]}},
             "fp64_gpu": {"value": value64, "ms_per_step": ms64 / args.steps,
                          "mixed_over_fp64": value / world / value64},
             "accuracy_vs_fp64_gpu": acc,

@@ -728,8 +728,8 @@ nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_no
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   NNPP_TRY(engine_set_tiles(e, T));
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, W));
-  if (staged_operator && !spmv_staged_fits(e.halo_max))
-    return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: the staged operator's tile halo does not fit shared memory");
+  if (staged_operator && !spmv_staged_fits(e))
+    return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: a slice window of the staged operator exceeds its capacity");
   e.W = W;
   e.spmv_staged = staged_operator != 0;
   e.tuned = true;

@@ -52,13 +52,16 @@ nnpp_status build_lists(Engine& e, int T) {
   std::vector<Chunk> chunks;
   std::vector<SliceDesc> slices;
   std::vector<int> meta(6 * M);
+  bool fit = true;
   int hm = 0, bmax = 0;
   for (int i = 0; i < M; ++i) {
     Handle& h = *e.members[i];
     meta[i] = (int)tiles.size();
     int hmi = 0, bmi = 0;
     meta[4 * M + i] = (int)slices.size();
-    NNPP_TRY(build_tiles(h, T, tiles, slices, i, &hmi, &bmi));
+    bool wf = false;
+    NNPP_TRY(build_tiles(h, T, tiles, slices, i, &hmi, &bmi, &wf));
+    fit = fit && wf;
     meta[5 * M + i] = (int)slices.size() - meta[4 * M + i];
     meta[M + i] = (int)tiles.size() - meta[i];
     hm = std::max(hm, hmi);
@@ -77,6 +80,7 @@ nnpp_status build_lists(Engine& e, int T) {
   e.ntiles = (int)tiles.size();
   e.nchunks = (int)chunks.size();
   e.nslices = (int)slices.size();
+  e.windows_fit = fit;
   e.halo_max = hm;
   e.bond_max = bmax;
   e.T = T;
@@ -141,7 +145,7 @@ nnpp_status tune(Engine& e, int prec) {
       EngineView v = make_view(e, 0, 0);
       NNPP_TRY(set_active(e, 1, 1));
       NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
-      const int nvar = (prec == NNPP_MIXED && spmv_staged_fits(e.halo_max)) ? 2 : 1;
+      const int nvar = (prec == NNPP_MIXED && spmv_staged_fits(e)) ? 2 : 1;
       for (int var = 0; var < nvar; ++var) {
         e.spmv_staged = var == 1;
         NNPP_TRY(set_active(e, 1, 1));

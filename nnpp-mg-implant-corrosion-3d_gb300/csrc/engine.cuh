@@ -32,15 +32,24 @@ struct Chunk {
 };
 
 // 32 consecutive rows of one tile in the sliced operator layout (bond c of row row0 + l at
-// off + 32 c + l of the instance's sliced arrays; slot code = halo row << 12 | offset in it).
+// off + 32 c + l of the instance's sliced arrays).  The neighbours of a slice lie in 9 node
+// ranges (its window rows, within the tile's 3x3 halo rows); a slot code is
+// (window row r << 12 | node - lo[r]).  The window is what the staged kernels copy to shared
+// memory: row r is wlen[r] nodes from lo[r] (both multiples of 4) at woff[r].
+constexpr int kWinCap = 2048;  // nodes of one staged window
 struct SliceDesc {
   int inst;
-  int tile;    // global tile index: its halo rows decode the slot codes
+  int tile;    // global tile index
   int row0;    // first row (internal node index of the instance)
   int nrows;   // rows in the slice (<= 32)
   int off;     // offset in the instance's sliced arrays
   int width;   // columns (longest row of the slice)
-  int pad[2];
+  int wtotal;  // nodes of the window (sum of wlen)
+  int pad;
+  int lo[9];
+  int woff[9];
+  int wlen[9];
+  int pad2;
 };
 
 // What every batched kernel receives.
@@ -73,6 +82,7 @@ struct Engine {
   bool tuned = false;
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
   bool spmv_staged = false; // FP32 CG operator: bulk-copy staged (true) or L1/L2 gathers
+  bool windows_fit = false; // every slice window fits kWinCap (the staged operator runs)
   int grid = 0;
   int sms = 152;
   int halo_max = 0;
@@ -105,11 +115,11 @@ void engine_destroy_graphs(Engine& e);
 
 // tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& slices,
-                        int inst, int* halo_max, int* bond_max);
+                        int inst, int* halo_max, int* bond_max, bool* windows_fit);
 
 // step.cu launchers (batched)
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
-bool spmv_staged_fits(int halo_max);
+bool spmv_staged_fits(const Engine& e);
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out);
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,

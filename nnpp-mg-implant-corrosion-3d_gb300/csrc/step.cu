@@ -389,7 +389,7 @@ __device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
   }
 }
 
-// node of a slot code: halo row start (per-warp table of the slice's tile) + offset
+// node of a slot code: window row start (per-warp table of the slice's lo[]) + offset
 __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
   return hb[code >> 12] + (int)(code & 4095u);
 }
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
     if (*((volatile int*)&k.ds->inner_active) != 0) {
-      if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+      if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
       __syncwarp();
       const int a = d.row0 + lane;
       if (lane < d.nrows && k.freem[a]) {
@@ -480,49 +480,47 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
   }
 }
 
-// Staged FP32 CG operator (the same product as k_cg_spmv32): a CTA walks tiles, stages the
-// tile's halo of z in shared memory, and its 8 warps take the tile's 32-row slices.  Each
-// warp streams its slices' slot codes and weights through a private ring of kTmaStages
-// shared-memory stages (kTmaCol bond columns each) filled by cp.async.bulk and completed on
-// one mbarrier per stage: lane 0 refills a stage as soon as the warp has consumed it, so
-// kTmaStages columns blocks are always in flight and the gathers hit shared memory only.
-constexpr int kTmaCol = 32;
-constexpr int kTmaStages = 4;
+// Staged FP32 CG operator (the same product as k_cg_spmv32, same work split).  Every warp
+// owns, in shared memory,
+//   - a ring of kTmaStages stages of kTmaCol bond columns (slot codes + weights) of its
+//     slices, refilled by cp.async.bulk as soon as a stage is consumed, and
+//   - two window buffers: the z values of the current slice's 9 window rows (the only nodes
+//     its bonds reach) and, in flight, the next slice's,
+// each completed on an mbarrier.  The gathers are shared-memory loads; HBM only sees the
+// streamed operator and the windows.  Waits are bounded: a timeout is recorded in the
+// instance's state (reported as NNPP_ERR_CUDA).
+constexpr int kTmaCol = 16;
+constexpr int kTmaStages = 3;
 constexpr int kStageW = kTmaCol * 32 * 4;  // weights of one stage (bytes)
 constexpr int kStageC = kTmaCol * 32 * 2;  // slot codes of one stage (bytes)
 constexpr int kStageBytes = kStageW + kStageC;
 constexpr int kWarpsCta = kBlock / 32;
 constexpr size_t kTmaRingBytes = (size_t)kWarpsCta * kTmaStages * kStageBytes;
-constexpr size_t kTmaBarBytes = (size_t)kWarpsCta * kTmaStages * sizeof(uint64_t);
+constexpr size_t kTmaWinBytes = (size_t)kWarpsCta * 2 * kWinCap * sizeof(float);
+constexpr size_t kTmaBarBytes = (size_t)kWarpsCta * (kTmaStages + 2) * sizeof(uint64_t);
 constexpr unsigned kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ int tma_chunks(int width) { return width > 0 ? (width + kTmaCol - 1) / kTmaCol : 1; }
 
-// position of a warp's producer in its sequence (tile item, slice, chunk)
-struct TmaCursor {
-  int item, sl, ch;
-};
-
-__device__ __forceinline__ bool tma_seek(const EngineView& v, TmaCursor& c, int warp) {
-  while (c.item < v.ntiles) {
-    const TileDesc& t = v.tiles[c.item];
-    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
-    const bool act = *((volatile int*)&v.inst[t.inst].ds->inner_active) != 0;
-    if (act && c.sl < nsl) return true;
-    c.item += gridDim.x;
-    c.sl = warp;
-    c.ch = 0;
-  }
-  return false;
+__device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
+  return *((volatile int*)&v.inst[v.slices[sg].inst].ds->inner_active) != 0;
 }
 
-// lane 0: issue the cursor's chunk into stage `stage` and advance; false when exhausted
-__device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, int warp, int stage,
+// position of a warp's operator producer in its slice range: slice, chunk
+struct TmaCursor {
+  int sg, ch;
+};
+
+// lane 0: issue the cursor's chunk into `stage` and advance; false when the range is done
+__device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, int s1, int warp, int stage,
                                             unsigned char* ring, uint64_t* bars) {
-  if (!tma_seek(v, c, warp)) return false;
-  const TileDesc& t = v.tiles[c.item];
-  const KParams& k = v.inst[t.inst];
-  const SliceDesc& d = v.slices[t.slice0 + c.sl];
+  while (c.sg < s1 && !slice_active(v, c.sg)) {
+    ++c.sg;  // inactive instance: the consumer skips its slices too
+    c.ch = 0;
+  }
+  if (c.sg >= s1) return false;
+  const SliceDesc& d = v.slices[c.sg];
+  const KParams& k = v.inst[d.inst];
   const int c0 = c.ch * kTmaCol;
   const int cc = min(kTmaCol, max(d.width - c0, 0));
   unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
@@ -536,87 +534,111 @@ __device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, i
   }
   if (++c.ch >= tma_chunks(d.width)) {
     c.ch = 0;
-    c.sl += kWarpsCta;
+    ++c.sg;
   }
+  return true;
+}
+
+// lane 0: copy the window of the next active slice at or after *ws into window buffer wb;
+// advances *ws past it; false when none is left
+__device__ __forceinline__ bool win_produce(const EngineView& v, int* ws, int s1, float* win, uint64_t* bar) {
+  while (*ws < s1 && !slice_active(v, *ws)) ++*ws;
+  if (*ws >= s1) return false;
+  const SliceDesc& d = v.slices[*ws];
+  const float* z = v.inst[d.inst].z32;
+  fence_proxy_async_smem();
+  mbar_arrive_expect_tx(bar, (unsigned)(d.wtotal * 4));
+  for (int r = 0; r < 9; ++r)
+    if (d.wlen[r] > 0) bulk_g2s(win + d.woff[r], z + d.lo[r], (unsigned)(d.wlen[r] * 4), bar);
+  ++*ws;
   return true;
 }
 
 template <int W>
 __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ TileSmem ts;
+  __shared__ int s_woff[kBlock / 32][12];
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* ring = dsm;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(dsm + kTmaRingBytes);
-  float* hs = reinterpret_cast<float*>(dsm + kTmaRingBytes + kTmaBarBytes);
-  if (threadIdx.x < kWarpsCta * kTmaStages) mbar_init(bars + threadIdx.x, 1);
+  float* wins = reinterpret_cast<float*>(dsm + kTmaRingBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dsm + kTmaRingBytes + kTmaWinBytes);
+  uint64_t* wbars = bars + kWarpsCta * kTmaStages;
+  if (threadIdx.x < kWarpsCta * (kTmaStages + 2)) mbar_init(bars + threadIdx.x, 1);
   fence_mbar_init();
   __syncthreads();
-  TmaCursor pc{(int)blockIdx.x, warp, 0};
-  if (lane == 0)
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  float* mywin = wins + (size_t)warp * 2 * kWinCap;
+  TmaCursor pc{s0, 0};
+  int wsrc = s0;  // next slice whose window is to be copied
+  if (lane == 0) {
     for (int st = 0; st < kTmaStages; ++st)
-      if (!tma_produce(v, pc, warp, st, ring, bars)) break;
+      if (!tma_produce(v, pc, s1, warp, st, ring, bars)) break;
+    win_produce(v, &wsrc, s1, mywin, wbars + warp * 2);
+  }
   __syncwarp();
-  int stage = 0;
-  unsigned phases = 0u;
+  int stage = 0, wb = 0;
+  unsigned phases = 0u, wphases = 0u;
   int timed_out = -1;  // instance whose wait gave up
-  for (int item = blockIdx.x; item < v.ntiles; item += gridDim.x) {
-    const TileDesc t = v.tiles[item];
-    const KParams& k = v.inst[t.inst];
-    const bool active = *((volatile int*)&k.ds->inner_active) != 0;
-    const int nsl = (t.own_end - t.own_begin + 31) >> 5;
-    if (active) {
-      load_tile(t, ts);
-      const float* z = k.z32;
-      for (int s2 = threadIdx.x; s2 < t.halo; s2 += kBlock) hs[s2] = z[halo_node(ts, s2)];
-    }
-    __syncthreads();
-    for (int sl = warp; sl < nsl; sl += kWarpsCta) {
-      double part = 0.0;
-      if (active) {
-        const SliceDesc d = v.slices[t.slice0 + sl];
-        float acc0 = 0.0f, acc1 = 0.0f;
-        const int nch = tma_chunks(d.width);
-        for (int ch = 0; ch < nch; ++ch) {
-          uint64_t* bar = bars + warp * kTmaStages + stage;
-          if (!mbar_wait_bounded(bar, (phases >> stage) & 1u, kWaitPolls)) timed_out = t.inst;
-          phases ^= 1u << stage;
-          const unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
-          const float* sw = reinterpret_cast<const float*>(buf) + lane;
-          const unsigned short* sc = reinterpret_cast<const unsigned short*>(buf + kStageW) + lane;
-          const int cc = min(kTmaCol, d.width - ch * kTmaCol);
-          int c = 0;
-          for (; c + 1 < cc; c += 2) {
-            const unsigned q0 = sc[32 * c], q1 = sc[32 * c + 32];
-            acc0 = fmaf(sw[32 * c], hs[ts.off[q0 >> 12] + (int)(q0 & 4095u)], acc0);
-            acc1 = fmaf(sw[32 * c + 32], hs[ts.off[q1 >> 12] + (int)(q1 & 4095u)], acc1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc& d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    double part = 0.0;
+    if (*((volatile int*)&k.ds->inner_active) != 0) {
+      // the next slice's window goes to the other buffer (free: its slice is done)
+      if (lane == 0) win_produce(v, &wsrc, s1, mywin + (wb ^ 1) * kWinCap, wbars + warp * 2 + (wb ^ 1));
+      if (lane < 9) s_woff[warp][lane] = d.woff[lane];
+      const int width = d.width;
+      __syncwarp();
+      if (!mbar_wait_bounded(wbars + warp * 2 + wb, (wphases >> wb) & 1u, kWaitPolls)) timed_out = d.inst;
+      wphases ^= 1u << wb;
+      const float* zw = mywin + wb * kWinCap;
+      const int* wo = s_woff[warp];
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const int nch = tma_chunks(width);
+      for (int ch = 0; ch < nch; ++ch) {
+        uint64_t* bar = bars + warp * kTmaStages + stage;
+        if (!mbar_wait_bounded(bar, (phases >> stage) & 1u, kWaitPolls)) timed_out = d.inst;
+        phases ^= 1u << stage;
+        const unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
+        const float* sw = reinterpret_cast<const float*>(buf) + lane;
+        const unsigned short* sc = reinterpret_cast<const unsigned short*>(buf + kStageW) + lane;
+        const int cc = min(kTmaCol, width - ch * kTmaCol);
+        if (cc == kTmaCol) {
+#pragma unroll
+          for (int c = 0; c < kTmaCol; ++c) {
+            const unsigned q = sc[32 * c];
+            acc[c & 3] = fmaf(sw[32 * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
           }
-          if (c < cc) {
-            const unsigned q0 = sc[32 * c];
-            acc0 = fmaf(sw[32 * c], hs[ts.off[q0 >> 12] + (int)(q0 & 4095u)], acc0);
+        } else {
+          for (int c = 0; c < cc; ++c) {
+            const unsigned q = sc[32 * c];
+            acc[c & 3] = fmaf(sw[32 * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
           }
-          __syncwarp();
-          if (lane == 0) tma_produce(v, pc, warp, stage, ring, bars);
-          stage = stage + 1 == kTmaStages ? 0 : stage + 1;
         }
-        const int a = d.row0 + lane;
-        if (lane < d.nrows && k.freem[a]) {
-          const float za = hs[ts.off[4] + (a - t.hb[4])];
-          const float sa = k.d32[a] * za - (acc0 + acc1);
-          const float beta = (float)k.ds->beta;
-          const float qn = sa + beta * k.q32[a];
-          const float pn = za + beta * k.p32[a];
-          k.q32[a] = qn;
-          k.p32[a] = pn;
-          part = (double)pn * (double)qn;
-        }
+        __syncwarp();
+        if (lane == 0) tma_produce(v, pc, s1, warp, stage, ring, bars);
+        stage = stage + 1 == kTmaStages ? 0 : stage + 1;
       }
-      part = warp_sum_d(part);
-      if (lane == 0) v.partials[t.slice0 + sl] = part;
+      const int a = d.row0 + lane;
+      if (lane < d.nrows && k.freem[a]) {
+        const float* z = k.z32;
+        const float za = z[a];
+        const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+        const float beta = (float)k.ds->beta;
+        const float qn = sa + beta * k.q32[a];
+        const float pn = za + beta * k.p32[a];
+        k.q32[a] = qn;
+        k.p32[a] = pn;
+        part = (double)pn * (double)qn;
+      }
+      __syncwarp();
+      wb ^= 1;
     }
-    __syncthreads();
+    part = warp_sum_d(part);
+    if (lane == 0) v.partials[sg] = part;
   }
   if (timed_out >= 0 && lane == 0) v.inst[timed_out].ds->wait_timeout = 1;
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
@@ -1074,7 +1096,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+    if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
     __syncwarp();
     float ph_hi[6], ph_lo[6];  // masses[4], solid volume sum, dissolved (FP32 pairs)
 #pragma unroll
@@ -1536,7 +1558,7 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
-size_t smem_spmv_staged(int H) { return kTmaRingBytes + kTmaBarBytes + align16((size_t)H * sizeof(float)); }
+size_t smem_spmv_staged() { return kTmaRingBytes + kTmaWinBytes + kTmaBarBytes; }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) + 1)) + smem_slots(B) + 16; }
 
@@ -1726,7 +1748,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, con
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    if (lane < 9) s_hb[warp][lane] = v.tiles[d.tile].hb[lane];
+    if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
     __syncwarp();
     float gh[5], gl[5];  // dL/dD_k (4), dL/dk as FP32 pairs
 #pragma unroll
@@ -1963,7 +1985,7 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
-    if (smem_spmv_staged(H) <= 227 * 1024) NNPP_TRY(allow_smem(k_cg_spmv32t<W>, smem_spmv_staged(H)));
+    NNPP_TRY(allow_smem(k_cg_spmv32t<W>, smem_spmv_staged()));
     NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
@@ -1972,7 +1994,7 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
   });
 }
 
-bool spmv_staged_fits(int halo_max) { return smem_spmv_staged(halo_max) <= 227 * 1024; }
+bool spmv_staged_fits(const Engine& e) { return e.windows_fit && smem_spmv_staged() <= 227 * 1024; }
 
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
   if (prec == NNPP_MIXED) {
@@ -2015,8 +2037,8 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
       if (e.spmv_staged) {
-        const size_t sh = smem_spmv_staged(v.halo_max);
-        k_cg_spmv32t<W><<<occ_grid(k_cg_spmv32t<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v);
+        const size_t sh = smem_spmv_staged();
+        k_cg_spmv32t<W><<<occ_grid(k_cg_spmv32t<W>, sh, e.sms, (v.nslices + 7) / 8), kBlock, sh, st>>>(v);
       } else {
         k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v);
       }
@@ -2080,7 +2102,7 @@ nnpp_status step_alloc(Handle& h) {
             h.phi64.alloc(N) && h.phi_prev.alloc(N) && h.flip_step.alloc(N) && h.b64.alloc(N) &&
             h.r64.alloc(N) && h.dsum64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
             h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
-            h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N) && h.p32.alloc(N) &&
+            h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N + 16) && h.p32.alloc(N) &&
             h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.dstate.alloc(1) &&
             h.scratch_d.alloc(16 + 7 * 4096) && h.user_stage.alloc((S + 1) * N) &&
             h.user_stage_i.alloc(N);
@@ -2091,7 +2113,8 @@ nnpp_status step_alloc(Handle& h) {
   NNPP_CUDA(cudaMemsetAsync(h.rec64[1].get(), 0, N * sizeof(Rec64), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.e32.get(), 0, N * sizeof(float), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.e64.get(), 0, N * sizeof(double), h.st));
-  NNPP_CUDA(cudaMemsetAsync(h.z32.get(), 0, N * sizeof(float), h.st));
+  // z32 is padded by 16 (read, never used) elements: window copies round their rows up to 4
+  NNPP_CUDA(cudaMemsetAsync(h.z32.get(), 0, (N + 16) * sizeof(float), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.z64.get(), 0, N * sizeof(double), h.st));
   NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, N * sizeof(int), h.st));
   int sms = 0;

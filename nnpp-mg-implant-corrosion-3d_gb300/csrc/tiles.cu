@@ -91,17 +91,68 @@ __global__ void k_slots(int n, const int* row, const int* col, const float4* pos
   }
 }
 
-// warp per slice: bond c of lane l (row row0 + l) at off + 32 c + l as (halo row << 12 |
-// offset within the row) and its FP32 weight; padding: code 0, weight 0.  pre: the tile's
-// halo row starts within the concatenated halo (9 per slice).
-__global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre, const int* row,
+// node of a tile-halo slot: pre = starts of the tile's 9 halo rows in its halo, hb = their
+// first nodes
+__device__ __forceinline__ void slot_node(int sv, const int* pre, const int* hb, int* r, int* node) {
+  int q = 0;
+  while (q < 8 && sv >= pre[q + 1]) ++q;
+  *r = q;
+  *node = hb[q] + (sv - pre[q]);
+}
+
+// warp per slice: the node range [lo, hi) each of the 9 halo rows contributes to the slice
+__global__ void k_slice_windows(int nslices, const SliceDesc* sl, const int* pre_hb, const int* row,
+                                const unsigned short* slot, int* lohi) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
+    const SliceDesc d = sl[s];
+    const int* pre = pre_hb + 18 * s;
+    const int* hb = pre + 9;
+    int lo[9], hi[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      lo[q] = 0x7fffffff;
+      hi[q] = -1;
+    }
+    if (lane < d.nrows) {
+      const int j1 = row[d.row0 + lane + 1];
+      for (int j = row[d.row0 + lane]; j < j1; ++j) {
+        int r, node;
+        slot_node(slot[j], pre, hb, &r, &node);
+#pragma unroll
+        for (int q = 0; q < 9; ++q)
+          if (q == r) {
+            lo[q] = min(lo[q], node);
+            hi[q] = max(hi[q], node + 1);
+          }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      lo[q] = __reduce_min_sync(0xffffffffu, lo[q]);
+      hi[q] = __reduce_max_sync(0xffffffffu, hi[q]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        lohi[18 * s + q] = lo[q];
+        lohi[18 * s + 9 + q] = hi[q];
+      }
+  }
+}
+
+// warp per slice: bond c of lane l (row row0 + l) at off + 32 c + l as (window row << 12 |
+// node - lo[row]) and its FP32 weight; padding: code 0, weight 0
+__global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb, const int* row,
                             const unsigned short* slot, const float* w32, unsigned short* ocode,
                             float* ow) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
-    const SliceDesc d = sl[s];
-    const int* p9 = pre + 9 * s;
+    const SliceDesc& d = sl[s];
+    const int* pre = pre_hb + 18 * s;
+    const int* hb = pre + 9;
     const bool live = lane < d.nrows;
     const int j0 = live ? row[d.row0 + lane] : 0;
     const int len = live ? row[d.row0 + lane + 1] - j0 : 0;
@@ -110,10 +161,9 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre, co
       unsigned short code = 0;
       float w = 0.0f;
       if (c < len) {
-        const int sv = slot[j0 + c];
-        int r = 0;
-        while (r < 8 && sv >= p9[r + 1]) ++r;
-        code = (unsigned short)((r << 12) | (sv - p9[r]));
+        int r, node;
+        slot_node(slot[j0 + c], pre, hb, &r, &node);
+        code = (unsigned short)((r << 12) | (node - d.lo[r]));
         w = w32[j0 + c];
       }
       ocode[o] = code;
@@ -125,7 +175,7 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre, co
 }  // namespace
 
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& gslices,
-                        int inst, int* halo_max, int* bond_max) {
+                        int inst, int* halo_max, int* bond_max, bool* windows_fit) {
   const Layout& L = h.lay;
   const int N = h.N;
   if (L.nb[0] > 1024 || L.nb[1] > 1024 || L.nb[2] > 1024)
@@ -160,7 +210,8 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
   const int ntx = (g.nb[0] + T - 1) / T;
   int hm = 0, bm = 0;
   std::vector<SliceDesc> slices;  // this instance's, offsets local to its sliced arrays
-  std::vector<int> pre;            // per slice: starts of the 9 halo rows in the halo
+  std::vector<int> pre;            // per slice: starts of the 9 halo rows in the halo, then
+                                   // their first nodes (18 ints)
   long long soff = 0;
   for (int bz = 0; bz < g.nb[2]; ++bz)
     for (int by = 0; by < g.nb[1]; ++by)
@@ -190,7 +241,8 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
           d.nrows = std::min(32, o1 - r0);
           d.off = (int)soff;
           d.width = 0;
-          d.pad[0] = d.pad[1] = 0;
+          d.wtotal = d.pad = d.pad2 = 0;
+          for (int r = 0; r < 9; ++r) d.lo[r] = d.woff[r] = d.wlen[r] = 0;
           for (int l = 0; l < d.nrows; ++l) d.width = std::max(d.width, rows[r0 + l + 1] - rows[r0 + l]);
           slices.push_back(d);
           int acc = 0;
@@ -198,6 +250,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
             pre.push_back(acc);
             acc += t.hl[r];
           }
+          for (int r = 0; r < 9; ++r) pre.push_back(t.hb[r]);
           soff += 32LL * d.width;
           if (soff > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "sliced operator above 2^31 entries");
         }
@@ -212,17 +265,47 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
   if (!h.sell_slot.alloc((size_t)soff + 32) || !h.sell_w.alloc((size_t)soff + 32))
     return set_error(NNPP_ERR_NOMEM, "sliced operator");
   DBuf<SliceDesc> dsl;
-  DBuf<int> dpre;
-  if (ns && (!dsl.alloc(ns) || !dpre.alloc(9 * ns))) return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  DBuf<int> dpre, dlohi;
+  bool fit = true;
+  if (ns && (!dsl.alloc(ns) || !dpre.alloc(18 * ns) || !dlohi.alloc(18 * ns)))
+    return set_error(NNPP_ERR_NOMEM, "sliced operator");
   if (ns) {
     NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
-    NNPP_CUDA(cudaMemcpyAsync(dpre.get(), pre.data(), sizeof(int) * 9 * ns, cudaMemcpyHostToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(dpre.get(), pre.data(), sizeof(int) * 18 * ns, cudaMemcpyHostToDevice, h.st));
     const int sb = std::max(1, std::min((int)((ns * 32 + 255) / 256), 152 * 32));
+    k_slice_windows<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), dpre.get(), L.row.get(), h.slot16.get(), dlohi.get());
+    NNPP_CUDA(cudaGetLastError());
+    std::vector<int> lohi(18 * ns);
+    NNPP_CUDA(cudaMemcpyAsync(lohi.data(), dlohi.get(), sizeof(int) * 18 * ns, cudaMemcpyDeviceToHost, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+    // window rows: [lo, hi) rounded out to multiples of 4 nodes (16-byte bulk copies); the
+    // codes' 12-bit offsets must reach hi - 1
+    for (size_t q = 0; q < ns; ++q) {
+      SliceDesc& d = slices[q];
+      int acc = 0;
+      for (int r = 0; r < 9; ++r) {
+        const int lo = lohi[18 * q + r], hi = lohi[18 * q + 9 + r];
+        if (hi <= lo) {
+          d.lo[r] = 0;
+          d.wlen[r] = 0;
+        } else {
+          d.lo[r] = lo & ~3;
+          d.wlen[r] = (hi - d.lo[r] + 3) & ~3;
+          if (hi - 1 - d.lo[r] > 4095) return set_error(NNPP_ERR_UNSUPPORTED, "tiles: slice window row wider than 4096 nodes");
+        }
+        d.woff[r] = acc;
+        acc += d.wlen[r];
+      }
+      d.wtotal = acc;
+      fit = fit && acc <= kWinCap;
+    }
+    NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
     k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), dpre.get(), L.row.get(), h.slot16.get(), L.w32.get(),
                                       h.sell_slot.get(), h.sell_w.get());
     NNPP_CUDA(cudaGetLastError());
     NNPP_CUDA(cudaStreamSynchronize(h.st));
   }
+  *windows_fit = fit;
   gslices.insert(gslices.end(), slices.begin(), slices.end());
   *halo_max = hm;
   *bond_max = bm;
