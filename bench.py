@@ -317,10 +317,10 @@ def run_ours(args):
     tuned = sim.tuning()
     variants = {}
     with ProfileRange("variants"):
-        for staged in (0, 1):
-            key = "staged" if staged else "gather"
+        for var, key in ((0, "gather8"), (1, "bulk_staged"), (2, "smem_window8"), (3, "gather16"),
+                         (4, "smem_window16")):
             try:
-                sim.set_tuning(tuned[0], tuned[1], staged)
+                sim.set_tuning(tuned[0], tuned[1], var)
                 variants[key] = sim.time_kernel(1, nn.MIXED, reps=50)
             except nn.NNPPError as ex:
                 variants[key] = "unsupported: %s" % ex
@@ -413,7 +413,7 @@ def run_ours(args):
                        "l2": "not flushed: per-bond arrays (%.2f GB) exceed the 129 MB L2" % ((4 + 4 + 8) * nnz / 1e9),
                        "potential_tol": 1e-10,
                        "tuning": {"bins_per_tile": tuned[0], "lanes_per_node": tuned[1],
-                                  "staged_cg_operator": tuned[2]}},
+                                  "cg_operator": tuned[2]}},
             "fp64_gpu": {"value": value64, "ms_per_step": ms64 / args.steps,
                          "mixed_over_fp64": value / world / value64},
             "accuracy_vs_fp64_gpu": acc,

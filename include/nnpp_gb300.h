@@ -260,14 +260,15 @@ nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int r
                              double* ms_per_launch);
 
 /* The execution configuration of the handle's kernels: bins per tile, lanes per node of the
- * FP64 tile kernels, and whether the FP32 CG operator streams its slices through
- * bulk-copy-staged shared memory (1) or gathers from L1/L2 (0).  Chosen by the autotuner on
- * the first run (all 0 / -1 before); nnpp_set_tuning pins a configuration instead (bins in
- * {2,4,8,16}, lanes in {4,8,16}; NNPP_ERR_UNSUPPORTED when a tile halo does not fit). */
+ * FP64 tile kernels, and the FP32 CG operator's variant: 0 / 3 gathers from L1/L2 (batches
+ * of 8 / 16 bond columns), 1 operator and slice windows streamed by bulk copies into shared
+ * memory, 2 / 4 slice windows copied into shared memory by the warp (batches of 8 / 16).  Chosen by the autotuner on the first run (0 / -1 before);
+ * nnpp_set_tuning pins a configuration instead (bins in {2,4,8,16}, lanes in {4,8,16};
+ * NNPP_ERR_UNSUPPORTED when a tile halo or a slice window does not fit). */
 nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node,
-                            int* staged_operator);
+                            int* cg_operator);
 nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_node,
-                            int staged_operator);
+                            int cg_operator);
 
 /* ---- differentiation ------------------------------------------------------------------ */
 

@@ -339,14 +339,15 @@ class Simulation:
         return gD, gk.value
 
     def tuning(self):
-        """(bins per tile, lanes per node, staged CG operator) of the autotuned engine."""
+        """(bins per tile, lanes per node, CG operator variant) of the autotuned engine."""
         t, w, g = C.c_int(0), C.c_int(0), C.c_int(0)
         _check(lib().nnpp_get_tuning(self._h, C.byref(t), C.byref(w), C.byref(g)))
         return t.value, w.value, g.value
 
-    def set_tuning(self, bins_per_tile, lanes_per_node, staged_operator):
-        """Pin the execution configuration instead of autotuning it."""
-        _check(lib().nnpp_set_tuning(self._h, bins_per_tile, lanes_per_node, int(staged_operator)))
+    def set_tuning(self, bins_per_tile, lanes_per_node, cg_operator):
+        """Pin the execution configuration instead of autotuning it (cg_operator: 0 L1/L2
+        gathers, 1 bulk-copy staged, 2 shared-memory windows)."""
+        _check(lib().nnpp_set_tuning(self._h, bins_per_tile, lanes_per_node, int(cg_operator)))
 
     def state(self):
         c = np.empty((NSPECIES, self.N), dtype=np.float64)

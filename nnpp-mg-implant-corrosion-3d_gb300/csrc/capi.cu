@@ -706,32 +706,32 @@ nnpp_status nnpp_set_params(nnpp_handle* hp, const nnpp_params* p) {
 }
 
 nnpp_status nnpp_get_tuning(nnpp_handle* hp, int* bins_per_tile, int* lanes_per_node,
-                            int* staged_operator) {
+                            int* cg_operator) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   const Engine& e = *hp->h.engine;
   if (bins_per_tile) *bins_per_tile = e.tuned ? e.T : 0;
   if (lanes_per_node) *lanes_per_node = e.tuned ? e.W : 0;
-  if (staged_operator) *staged_operator = e.tuned ? (e.spmv_staged ? 1 : 0) : -1;
+  if (cg_operator) *cg_operator = e.tuned ? e.spmv_variant : -1;
   return NNPP_OK;
 }
 
-nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_node, int staged_operator) {
+nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_node, int cg_operator) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   const int T = bins_per_tile, W = lanes_per_node;
   if ((T != 2 && T != 4 && T != 8 && T != 16) || (W != 4 && W != 8 && W != 16) ||
-      (staged_operator != 0 && staged_operator != 1))
-    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, staged 0/1");
+      cg_operator < 0 || cg_operator >= kSpmvVariants)
+    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, operator 0..4");
   Handle& h = hp->h;
   Engine& e = *h.engine;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   NNPP_TRY(engine_set_tiles(e, T));
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, W));
-  if (staged_operator && !spmv_staged_fits(e))
-    return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: a slice window of the staged operator exceeds its capacity");
+  if ((cg_operator == 1 || cg_operator == 2 || cg_operator == 4) && !spmv_staged_fits(e))
+    return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: a slice window exceeds the staged operators' capacity");
   e.W = W;
-  e.spmv_staged = staged_operator != 0;
+  e.spmv_variant = cg_operator;
   e.tuned = true;
   NNPP_TRY(engine_params(e));
   return NNPP_OK;

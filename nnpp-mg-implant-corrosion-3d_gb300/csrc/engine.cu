@@ -127,7 +127,7 @@ nnpp_status tune(Engine& e, int prec) {
   const int Ws[3] = {4, 8, 16};
   float best = 1e30f;
   int bT = 4, bW = 8;
-  bool bS = false;
+  int bS = 0;
   cudaEvent_t e0, e1;
   NNPP_CUDA(cudaEventCreate(&e0));
   NNPP_CUDA(cudaEventCreate(&e1));
@@ -145,9 +145,11 @@ nnpp_status tune(Engine& e, int prec) {
       EngineView v = make_view(e, 0, 0);
       NNPP_TRY(set_active(e, 1, 1));
       NNPP_TRY(launch_prep_b(e, v, prec, e.st, 0, nullptr));
-      const int nvar = (prec == NNPP_MIXED && spmv_staged_fits(e)) ? 2 : 1;
+      const bool win = prec == NNPP_MIXED && spmv_staged_fits(e);
+      const int nvar = prec == NNPP_MIXED ? kSpmvVariants : 1;
       for (int var = 0; var < nvar; ++var) {
-        e.spmv_staged = var == 1;
+        if (!win && (var == 1 || var == 2 || var == 4)) continue;
+        e.spmv_variant = var;
         NNPP_TRY(set_active(e, 1, 1));
         NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
         cudaEventRecord(e0, e.st);
@@ -162,7 +164,7 @@ nnpp_status tune(Engine& e, int prec) {
           best = ms;
           bT = T;
           bW = W;
-          bS = e.spmv_staged;
+          bS = e.spmv_variant;
         }
       }
     }
@@ -174,7 +176,7 @@ nnpp_status tune(Engine& e, int prec) {
     NNPP_CUDA(cudaMemcpy(e.members[i]->dstate.get(), &saved[i], sizeof(DevState), cudaMemcpyHostToDevice));
   NNPP_TRY(build_lists(e, bT));
   e.W = bW;
-  e.spmv_staged = bS;
+  e.spmv_variant = bS;
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, bW));
   e.tuned = true;
   return NNPP_OK;

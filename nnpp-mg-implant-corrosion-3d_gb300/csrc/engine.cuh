@@ -74,6 +74,7 @@ struct EngineView {
 };
 
 constexpr int kChunk = 1024;  // nodes per elementwise work item
+constexpr int kSpmvVariants = 5;  // FP32 CG operator variants the autotuner times
 
 struct Engine {
   std::vector<Handle*> members;
@@ -81,7 +82,8 @@ struct Engine {
   int W = 8;                // lanes per node (autotuned)
   bool tuned = false;
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
-  bool spmv_staged = false; // FP32 CG operator: bulk-copy staged (true) or L1/L2 gathers
+  int spmv_variant = 0;     // FP32 CG operator: 0, 3 L1/L2 gathers (batches of 8, 16),
+                            // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16)
   bool windows_fit = false; // every slice window fits kWinCap (the staged operator runs)
   int grid = 0;
   int sms = 152;

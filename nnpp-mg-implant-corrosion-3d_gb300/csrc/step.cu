@@ -389,6 +389,11 @@ __device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
   }
 }
 
+// the inner-loop flag of a slice's instance (constant while the operator runs)
+__device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
+  return __ldg(&v.inst[__ldg(&v.slices[sg].inst)].ds->inner_active) != 0;
+}
+
 // node of a slot code: window row start (per-warp table of the slice's lo[]) + offset
 __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
   return hb[code >> 12] + (int)(code & 4095u);
@@ -396,22 +401,37 @@ __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
 
 // q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
 // FP32, sliced operator: each warp streams 32-row slices (slot codes and weights
-// column-major: one coalesced load per bond column), gathers z from L1/L2, one lane per row.
+// column-major: one coalesced load per bond column), one lane per row.  WIN: the warp first
+// copies the slice's window (the z values of its 9 window rows) into its shared-memory
+// buffer with coalesced loads and gathers from there; otherwise it gathers from L1/L2.
 // Slice partials are reduced per instance by the last CTA.
-template <int W>
-__global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
+template <int W, bool WIN, int B, bool PIPE, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
+  extern __shared__ __align__(16) float zwin[];
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int s0, s1;
   warp_slices(v, &s0, &s1);
+  float* zw = zwin + (WIN ? (size_t)warp * kWinCap : 0);
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
-    if (*((volatile int*)&k.ds->inner_active) != 0) {
-      if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
+    if (slice_active(v, sg)) {
+      if (WIN) {
+        const SliceDesc& dg = v.slices[sg];
+        if (lane < 9) s_hb[warp][lane] = dg.woff[lane];
+        const float* zg = k.z32;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+          const int n = dg.wlen[r], lo = dg.lo[r], wo = dg.woff[r];
+          for (int i = lane; i < n; i += 32) zw[wo + i] = __ldg(zg + lo + i);
+        }
+      } else if (lane < 9) {
+        s_hb[warp][lane] = v.slices[sg].lo[lane];
+      }
       __syncwarp();
       const int a = d.row0 + lane;
       if (lane < d.nrows && k.freem[a]) {
@@ -419,14 +439,13 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
         const unsigned short* cs = k.sell_slot + d.off + lane;
         const float* ws = k.sell_w + d.off + lane;
         const float* z = k.z32;
-        // software pipeline: the next batch of streamed columns is in flight while the
-        // current batch's neighbour values are gathered
-        constexpr int B = 8;
+        // B columns per batch; PIPE: the next batch of streamed columns is in flight while
+        // the current batch's neighbour values are gathered (more registers, fewer warps)
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         const int nb = d.width / B;
         float w[B];
         unsigned int code[B];
-        if (nb > 0) {
+        if (PIPE && nb > 0) {
 #pragma unroll
           for (int u = 0; u < B; ++u) {
             w[u] = __ldcs(ws + 32 * u);
@@ -434,13 +453,20 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
           }
         }
         for (int b = 0; b < nb; ++b) {
+          if (!PIPE) {
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+              w[u] = __ldcs(ws + 32 * (b * B + u));
+              code[u] = __ldcs(cs + 32 * (b * B + u));
+            }
+          }
           float zv[B];
 #pragma unroll
-          for (int u = 0; u < B; ++u) zv[u] = __ldg(z + code_node(hb, code[u]));
+          for (int u = 0; u < B; ++u) zv[u] = WIN ? zw[code_node(hb, code[u])] : __ldg(z + code_node(hb, code[u]));
           float wc[B];
 #pragma unroll
           for (int u = 0; u < B; ++u) wc[u] = w[u];
-          if (b + 1 < nb) {
+          if (PIPE && b + 1 < nb) {
             const int c1 = (b + 1) * B;
 #pragma unroll
             for (int u = 0; u < B; ++u) {
@@ -451,8 +477,10 @@ __global__ void __launch_bounds__(kBlock, 5) k_cg_spmv32(EngineView v) {
 #pragma unroll
           for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
-        for (int c = nb * B; c < d.width; ++c)
-          acc[0] = fmaf(__ldcs(ws + 32 * c), __ldg(z + code_node(hb, __ldcs(cs + 32 * c))), acc[0]);
+        for (int c = nb * B; c < d.width; ++c) {
+          const int q = code_node(hb, __ldcs(cs + 32 * c));
+          acc[0] = fmaf(__ldcs(ws + 32 * c), WIN ? zw[q] : __ldg(z + q), acc[0]);
+        }
         const float za = z[a];
         const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
         const float beta = (float)k.ds->beta;
@@ -502,37 +530,45 @@ constexpr unsigned kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ int tma_chunks(int width) { return width > 0 ? (width + kTmaCol - 1) / kTmaCol : 1; }
 
-__device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
-  return *((volatile int*)&v.inst[v.slices[sg].inst].ds->inner_active) != 0;
-}
-
-// position of a warp's operator producer in its slice range: slice, chunk
+// a warp's operator producer (lane 0): position in its slice range and the current slice's
+// descriptors, loaded once per slice so that issuing a chunk costs no dependent loads
 struct TmaCursor {
   int sg, ch;
+  int loaded;  // slice whose fields below are valid (-1: none)
+  int width, nch;
+  const float* w;
+  const unsigned short* code;
 };
 
 // lane 0: issue the cursor's chunk into `stage` and advance; false when the range is done
 __device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, int s1, int warp, int stage,
-                                            unsigned char* ring, uint64_t* bars) {
-  while (c.sg < s1 && !slice_active(v, c.sg)) {
-    ++c.sg;  // inactive instance: the consumer skips its slices too
-    c.ch = 0;
+                                            unsigned char* ring, uint64_t* bars, uint64_t pol) {
+  if (c.loaded != c.sg) {
+    while (c.sg < s1 && !slice_active(v, c.sg)) {
+      ++c.sg;  // inactive instance: the consumer skips its slices too
+      c.ch = 0;
+    }
+    if (c.sg >= s1) return false;
+    const SliceDesc& d = v.slices[c.sg];
+    const KParams& k = v.inst[d.inst];
+    c.width = d.width;
+    c.nch = tma_chunks(c.width);
+    c.w = k.sell_w + d.off;
+    c.code = k.sell_slot + d.off;
+    c.loaded = c.sg;
   }
-  if (c.sg >= s1) return false;
-  const SliceDesc& d = v.slices[c.sg];
-  const KParams& k = v.inst[d.inst];
   const int c0 = c.ch * kTmaCol;
-  const int cc = min(kTmaCol, max(d.width - c0, 0));
+  const int cc = min(kTmaCol, max(c.width - c0, 0));
   unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
   uint64_t* bar = bars + warp * kTmaStages + stage;
   fence_proxy_async_smem();
   mbar_arrive_expect_tx(bar, (unsigned)(cc * 32 * 6));
   if (cc > 0) {
-    const size_t e0 = (size_t)d.off + (size_t)c0 * 32;
-    bulk_g2s(buf, k.sell_w + e0, (unsigned)(cc * 32 * 4), bar);
-    bulk_g2s(buf + kStageW, k.sell_slot + e0, (unsigned)(cc * 32 * 2), bar);
+    const size_t e0 = (size_t)c0 * 32;
+    bulk_g2s_hint(buf, c.w + e0, (unsigned)(cc * 32 * 4), bar, pol);
+    bulk_g2s_hint(buf + kStageW, c.code + e0, (unsigned)(cc * 32 * 2), bar, pol);
   }
-  if (++c.ch >= tma_chunks(d.width)) {
+  if (++c.ch >= c.nch) {
     c.ch = 0;
     ++c.sg;
   }
@@ -571,11 +607,12 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
   int s0, s1;
   warp_slices(v, &s0, &s1);
   float* mywin = wins + (size_t)warp * 2 * kWinCap;
-  TmaCursor pc{s0, 0};
+  TmaCursor pc{s0, 0, -1, 0, 0, nullptr, nullptr};
   int wsrc = s0;  // next slice whose window is to be copied
+  const uint64_t pol = l2_evict_first_policy();  // the operator is read once per launch
   if (lane == 0) {
     for (int st = 0; st < kTmaStages; ++st)
-      if (!tma_produce(v, pc, s1, warp, st, ring, bars)) break;
+      if (!tma_produce(v, pc, s1, warp, st, ring, bars, pol)) break;
     win_produce(v, &wsrc, s1, mywin, wbars + warp * 2);
   }
   __syncwarp();
@@ -586,11 +623,21 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
-    if (*((volatile int*)&k.ds->inner_active) != 0) {
+    if (slice_active(v, sg)) {
       // the next slice's window goes to the other buffer (free: its slice is done)
       if (lane == 0) win_produce(v, &wsrc, s1, mywin + (wb ^ 1) * kWinCap, wbars + warp * 2 + (wb ^ 1));
       if (lane < 9) s_woff[warp][lane] = d.woff[lane];
       const int width = d.width;
+      // the row's own values are loaded now and arrive while the slice streams
+      const int a = d.row0 + lane;
+      const bool live = lane < d.nrows && k.freem[a];
+      float za = 0.0f, da = 0.0f, qa = 0.0f, pa = 0.0f;
+      if (live) {
+        za = k.z32[a];
+        da = k.d32[a];
+        qa = k.q32[a];
+        pa = k.p32[a];
+      }
       __syncwarp();
       if (!mbar_wait_bounded(wbars + warp * 2 + wb, (wphases >> wb) & 1u, kWaitPolls)) timed_out = d.inst;
       wphases ^= 1u << wb;
@@ -619,17 +666,14 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
           }
         }
         __syncwarp();
-        if (lane == 0) tma_produce(v, pc, s1, warp, stage, ring, bars);
+        if (lane == 0) tma_produce(v, pc, s1, warp, stage, ring, bars, pol);
         stage = stage + 1 == kTmaStages ? 0 : stage + 1;
       }
-      const int a = d.row0 + lane;
-      if (lane < d.nrows && k.freem[a]) {
-        const float* z = k.z32;
-        const float za = z[a];
-        const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+      if (live) {
+        const float sa = da * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
         const float beta = (float)k.ds->beta;
-        const float qn = sa + beta * k.q32[a];
-        const float pn = za + beta * k.p32[a];
+        const float qn = sa + beta * qa;
+        const float pn = za + beta * pa;
         k.q32[a] = qn;
         k.p32[a] = pn;
         part = (double)pn * (double)qn;
@@ -1559,6 +1603,7 @@ size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
 size_t smem_spmv_staged() { return kTmaRingBytes + kTmaWinBytes + kTmaBarBytes; }
+size_t smem_spmv_win() { return (size_t)(kBlock / 32) * kWinCap * sizeof(float); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) + 1)) + smem_slots(B) + 16; }
 
@@ -1986,12 +2031,40 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv32t<W>, smem_spmv_staged()));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 8, true, 3>, smem_spmv_win()));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 16, false, 3>, smem_spmv_win()));
     NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, true>, smem_tr64(H, B)));
     return NNPP_OK;
   });
+}
+
+// FP32 CG operator variants without bulk copies (the autotuner's list): 0 L1/L2 gathers in
+// batches of 8, 32 registers (64 warps per SM); 2 shared-memory windows, pipelined batches of
+// 8; 3 L1/L2 gathers in batches of 16 (40 warps per SM); 4 shared-memory windows, batches
+// of 16
+template <int W>
+void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t st) {
+  const int items = (v.nslices + 7) / 8;
+  switch (variant) {
+    case 2: {
+      const size_t sh = smem_spmv_win();
+      k_cg_spmv32<W, true, 8, true, 3><<<occ_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      break;
+    }
+    case 3:
+      k_cg_spmv32<W, false, 16, false, 5><<<occ_grid(k_cg_spmv32<W, false, 16, false, 5>, 0, sms, items), kBlock, 0, st>>>(v);
+      break;
+    case 4: {
+      const size_t sh = smem_spmv_win();
+      k_cg_spmv32<W, true, 16, false, 3><<<occ_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      break;
+    }
+    default:
+      k_cg_spmv32<W, false, 8, false, 8><<<occ_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, items), kBlock, 0, st>>>(v);
+  }
 }
 
 bool spmv_staged_fits(const Engine& e) { return e.windows_fit && smem_spmv_staged() <= 227 * 1024; }
@@ -2036,11 +2109,11 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      if (e.spmv_staged) {
+      if (e.spmv_variant == 1) {
         const size_t sh = smem_spmv_staged();
         k_cg_spmv32t<W><<<occ_grid(k_cg_spmv32t<W>, sh, e.sms, (v.nslices + 7) / 8), kBlock, sh, st>>>(v);
       } else {
-        k_cg_spmv32<W><<<occ_grid(k_cg_spmv32<W>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v);
+        launch_spmv_gather<W>(e.spmv_variant, v, e.sms, st);
       }
     else
       { const size_t sh = smem_vec64(v.halo_max, v.bond_max); k_cg_spmv64<W><<<occ_grid(k_cg_spmv64<W>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v); }

@@ -327,10 +327,10 @@ def test_warm_start_rejects_bad_history(gpu):
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("staged", [0, 1])
-def test_cg_operator_variants_vs_oracle(gpu, orc, staged):
-    """Both FP32 CG operators (L1/L2 gathers; bulk-copy-staged slices) reach the oracle's
-    state to the mixed-precision tolerance, with the configuration pinned."""
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+def test_cg_operator_variants_vs_oracle(gpu, orc, variant):
+    """Every FP32 CG operator (L1/L2 gathers; bulk-copy staged; shared-memory windows)
+    reaches the oracle's state to the mixed-precision tolerance, configuration pinned."""
     nn = gpu
     inp = nn.synth(1, 20, seed=11)
     o = orc.Oracle.from_synth(inp)
@@ -340,9 +340,9 @@ def test_cg_operator_variants_vs_oracle(gpu, orc, staged):
     c_o, phi_o, ph_o, _ = o.state()
     sim = nn.Simulation.from_synth(inp)
     sim.build_neighbours()
-    sim.set_tuning(8, 8, staged)
+    sim.set_tuning(8, 8, variant)
     sim.forward(100, nn.MIXED)
-    assert sim.tuning() == (8, 8, staged)
+    assert sim.tuning() == (8, 8, variant)
     c_g, phi_g, ph_g = sim.state()
     assert np.array_equal(ph_g, ph_o)
     assert np.linalg.norm(c_g - c_o) / np.linalg.norm(c_o) <= 1e-5
@@ -355,7 +355,7 @@ def test_set_tuning_rejects_bad_configuration(gpu):
     inp = nn.synth(1, 12, seed=4)
     sim = nn.Simulation.from_synth(inp)
     sim.build_neighbours()
-    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 2)):
+    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 5)):
         with pytest.raises(nn.NNPPError) as e:
             sim.set_tuning(*bad)
         assert e.value.status == 1
