@@ -245,6 +245,50 @@ class ProfileRange:
             torch.cuda.profiler.stop()
 
 
+def ensemble_cost(nn, steps, members=64, seed=4):
+    """Batched ensemble: `members` instances with node counts log-uniform in [20k, 200k]
+    (each its own inclusion, diffusivities and rate), all advanced by one graph launch per
+    step, against the same instances run one after another with the single-instance path."""
+    rng = np.random.default_rng(seed)
+    sides = [int(round(np.exp(rng.uniform(np.log(20000), np.log(200000))) ** (1 / 3)))
+             for _ in range(members)]
+    sims = []
+    for i, n in enumerate(sides):
+        sim = nn.Simulation.from_synth(nn.synth(4, n, seed + i))
+        sim.build_neighbours()
+        sims.append(sim)
+    total = sum(sm.N for sm in sims)
+    seq_ms = 0.0
+    for sm in sims:
+        sm.forward(3, nn.MIXED)
+        seq_ms += sm.forward_timed(steps, nn.MIXED)
+    ens = nn.Ensemble(sims)
+    ens.forward(3, nn.MIXED)
+    ms = ens.forward_timed(steps, nn.MIXED)
+    out = {"workload": "%d instances, %d nodes in total (log-uniform 20k-200k), own inclusion, "
+                       "D x U(0.5,2), k in U(0.02,0.08)" % (members, total),
+           "steps": steps, "value": total * steps / (ms / 1e3), "unit": "node-steps/s",
+           "sequential_value": total * steps / (seq_ms / 1e3),
+           "batched_over_sequential": seq_ms / ms, "tuning": list(ens.tuning())}
+    ens.close()
+    return out
+
+
+def large_cost(nn, steps):
+    """The 2M-node screw: neighbour build in the reference's order (bit-exact) and the mixed
+    step throughput."""
+    inp = nn.synth(2, 126, 1)
+    sim = nn.Simulation.from_synth(inp)
+    t0 = time.perf_counter()
+    sim.build_neighbours()
+    t_build = time.perf_counter() - t0
+    sim.forward(3, nn.MIXED)
+    ms = sim.forward_timed(steps, nn.MIXED)
+    return {"workload": "jittered, randomly permuted 126^3 lattice (%d nodes), screw implant" % inp["N"],
+            "neighbour_build_s": t_build, "steps": steps,
+            "value": inp["N"] * steps / (ms / 1e3), "unit": "node-steps/s"}
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
@@ -396,6 +440,14 @@ def run_ours(args):
     if rank == 0 and args.adjoint_steps > 0:
         adj = adjoint_cost(nn, args.adjoint_steps)
         log("adjoint: %s" % json.dumps(adj))
+    ensemble = None
+    if rank == 0 and args.ensemble_steps > 0:
+        ensemble = ensemble_cost(nn, args.ensemble_steps)
+        log("ensemble: %s" % json.dumps(ensemble))
+    large = None
+    if rank == 0 and args.large_steps > 0:
+        large = large_cost(nn, args.large_steps)
+        log("large: %s" % json.dumps(large))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -421,6 +473,8 @@ def run_ours(args):
                        "fp64_cg_per_step": (d64["cg_iterations_total"]) / (args.steps + args.warmup)},
             "adjoint_over_forward": adj["gradient_over_forward"] if adj else None,
             "adjoint": adj,
+            "ensemble": ensemble,
+            "large_2m": large,
             "neighbour_build_s": t_build,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -437,6 +491,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=400,
                     help="steps of the gradient-cost measurement (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=20,
+                    help="steps of the 64-instance ensemble measurement (0: skip)")
+    ap.add_argument("--large-steps", type=int, default=10,
+                    help="steps of the 2M-node measurement (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
