@@ -69,6 +69,7 @@ nnpp_status load_ckpt(Handle& h, const Handle::Ckpt& c) {
   NNPP_CUDA(cudaMemcpyAsync(h.phi_prev.get(), c.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), c.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &c.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  h.settings_pushed = false;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (h.engine) NNPP_TRY(engine_params(*h.engine));
   return NNPP_OK;

@@ -125,6 +125,7 @@ nnpp_status restore(Handle& h, StateBackup& b) {
   NNPP_CUDA(cudaMemcpyAsync(h.rec64[h.cur].get(), b.rec64.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), b.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &b.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  h.settings_pushed = false;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (h.engine) NNPP_TRY(engine_params(*h.engine));
   return NNPP_OK;
@@ -156,6 +157,7 @@ nnpp_status reset_initial(Handle& h) {
   ds.max_outer = h.max_outer;
   ds.inner_rel = h.inner_rel;
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  h.settings_pushed = false;
   h.cur = 0;
   NNPP_TRY(upload_state(h, h.h_ic.data(), h.h_ic.data() + S * N, h.h_phase0.data(), NNPP_FP64));
   NNPP_CUDA(cudaMemsetAsync(h.flip_step.get(), 0xff, sizeof(int) * N, h.st));
@@ -403,6 +405,7 @@ nnpp_status nnpp_set_solver(nnpp_handle* hp, double tol, int max_iter, int stric
   h.tol = tol;
   h.max_iter = max_iter;
   h.strict = strict;
+  h.settings_pushed = false;
   return NNPP_OK;
 }
 

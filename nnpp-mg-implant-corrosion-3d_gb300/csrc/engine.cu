@@ -13,6 +13,7 @@ namespace nnpp {
 namespace {
 
 nnpp_status push_settings(Handle& h) {
+  if (h.settings_pushed) return NNPP_OK;
   DevState ds;
   NNPP_CUDA(cudaMemcpyAsync(&ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
@@ -22,6 +23,7 @@ nnpp_status push_settings(Handle& h) {
   ds.inner_rel = h.inner_rel;
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.settings_pushed = true;
   return NNPP_OK;
 }
 
@@ -33,9 +35,10 @@ nnpp_status refresh_params(Engine& e) {
     k0[i] = make_kparams(*e.members[i], e.members[i]->cur);
     k1[i] = make_kparams(*e.members[i], e.members[i]->cur ^ 1);
   }
+  // pageable sources: the copies are staged before the calls return, and the kernels that
+  // read the blocks are ordered after them on e.st
   NNPP_CUDA(cudaMemcpyAsync(e.d_inst[0].get(), k0.data(), sizeof(KParams) * M, cudaMemcpyHostToDevice, e.st));
   NNPP_CUDA(cudaMemcpyAsync(e.d_inst[1].get(), k1.data(), sizeof(KParams) * M, cudaMemcpyHostToDevice, e.st));
-  NNPP_CUDA(cudaStreamSynchronize(e.st));
   return NNPP_OK;
 }
 
@@ -426,7 +429,6 @@ nnpp_status engine_solve(Engine& e, int prec) {
   }
   NNPP_TRY(build_graph(e, kGraphSolve, prec));
   NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphSolve][prec][0], e.st));
-  NNPP_CUDA(cudaStreamSynchronize(e.st));
   return NNPP_OK;
 }
 

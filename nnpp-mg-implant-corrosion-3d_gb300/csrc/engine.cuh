@@ -36,7 +36,7 @@ struct Chunk {
 // ranges (its window rows, within the tile's 3x3 halo rows); a slot code is
 // (window row r << 12 | node - lo[r]).  The window is what the staged kernels copy to shared
 // memory: row r is wlen[r] nodes from lo[r] (both multiples of 4) at woff[r].
-constexpr int kWinCap = 2048;  // nodes of one staged window
+constexpr int kWinCap = 1536;  // nodes of one staged window
 struct SliceDesc {
   int inst;
   int tile;    // global tile index

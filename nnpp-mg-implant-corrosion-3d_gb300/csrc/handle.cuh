@@ -20,9 +20,9 @@ struct KParams {
   const int* col;
   const unsigned short* slot16;  // per bond: halo slot of the neighbour within its tile
   // sliced layout (32 consecutive rows of a tile per slice, bonds column-major within a
-  // slice, rows padded to the slice's longest): slot codes (halo row << 12 | offset), weights
-  const unsigned short* sell_slot;
-  const float* sell_w;
+  // slice, rows padded to the slice's longest): per bond column 32 FP32 weights then 32
+  // 16-bit slot codes (window row << 12 | offset)
+  const float* sell;
   const double* w64;
   const float* w32;
   const unsigned char* dirmask;  // bit k: species k Dirichlet, bit S: potential Dirichlet
@@ -83,8 +83,7 @@ struct Handle {
   int max_node_no = 0;
   // tiles (built for tiles_T bins per tile)
   DBuf<unsigned short> slot16;
-  DBuf<unsigned short> sell_slot;
-  DBuf<float> sell_w;
+  DBuf<float> sell;
   DBuf<float4> posrec;
   float h32 = 0.f;
   int tiles_T = 0;
@@ -112,6 +111,7 @@ struct Handle {
   int max_outer = 30;
   double inner_rel = 1e-4;
   int strict = 0;
+  bool settings_pushed = false; // tol, max_iter, ... already in the device state
   int extrapolate = 1;
   int warm_hist = kHistMax;     // history length of the warm start (0: extrapolation only)
   DBuf<double> xh, bh;          // warm-start history, warm_hist * N each

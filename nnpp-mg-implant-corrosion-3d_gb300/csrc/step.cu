@@ -389,6 +389,17 @@ __device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
   }
 }
 
+// Interleaved sliced operator: bond column c of a slice holds 32 FP32 weights then 32 16-bit
+// slot codes (kSellW floats = 192 bytes), so one contiguous copy moves both.
+constexpr int kSellW = 48;      // stride of a column in floats
+constexpr int kSellC = 96;      // stride of a column in 16-bit codes
+__device__ __forceinline__ const float* sell_w(const KParams& k, const SliceDesc& d) {
+  return k.sell + (size_t)(d.off >> 5) * kSellW;
+}
+__device__ __forceinline__ const unsigned short* sell_code(const KParams& k, const SliceDesc& d) {
+  return reinterpret_cast<const unsigned short*>(sell_w(k, d) + 32);
+}
+
 // the inner-loop flag of a slice's instance (constant while the operator runs)
 __device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
   return __ldg(&v.inst[__ldg(&v.slices[sg].inst)].ds->inner_active) != 0;
@@ -436,8 +447,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
       const int a = d.row0 + lane;
       if (lane < d.nrows && k.freem[a]) {
         const int* hb = s_hb[warp];
-        const unsigned short* cs = k.sell_slot + d.off + lane;
-        const float* ws = k.sell_w + d.off + lane;
+        const float* ws = sell_w(k, d) + lane;
+        const unsigned short* cs = sell_code(k, d) + lane;
         const float* z = k.z32;
         // B columns per batch; PIPE: the next batch of streamed columns is in flight while
         // the current batch's neighbour values are gathered (more registers, fewer warps)
@@ -448,16 +459,16 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
         if (PIPE && nb > 0) {
 #pragma unroll
           for (int u = 0; u < B; ++u) {
-            w[u] = __ldcs(ws + 32 * u);
-            code[u] = __ldcs(cs + 32 * u);
+            w[u] = __ldcs(ws + kSellW * u);
+            code[u] = __ldcs(cs + kSellC * u);
           }
         }
         for (int b = 0; b < nb; ++b) {
           if (!PIPE) {
 #pragma unroll
             for (int u = 0; u < B; ++u) {
-              w[u] = __ldcs(ws + 32 * (b * B + u));
-              code[u] = __ldcs(cs + 32 * (b * B + u));
+              w[u] = __ldcs(ws + kSellW * (b * B + u));
+              code[u] = __ldcs(cs + kSellC * (b * B + u));
             }
           }
           float zv[B];
@@ -470,16 +481,16 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
             const int c1 = (b + 1) * B;
 #pragma unroll
             for (int u = 0; u < B; ++u) {
-              w[u] = __ldcs(ws + 32 * (c1 + u));
-              code[u] = __ldcs(cs + 32 * (c1 + u));
+              w[u] = __ldcs(ws + kSellW * (c1 + u));
+              code[u] = __ldcs(cs + kSellC * (c1 + u));
             }
           }
 #pragma unroll
           for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
         for (int c = nb * B; c < d.width; ++c) {
-          const int q = code_node(hb, __ldcs(cs + 32 * c));
-          acc[0] = fmaf(__ldcs(ws + 32 * c), WIN ? zw[q] : __ldg(z + q), acc[0]);
+          const int q = code_node(hb, __ldcs(cs + kSellC * c));
+          acc[0] = fmaf(__ldcs(ws + kSellW * c), WIN ? zw[q] : __ldg(z + q), acc[0]);
         }
         const float za = z[a];
         const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
@@ -510,22 +521,21 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
 
 // Staged FP32 CG operator (the same product as k_cg_spmv32, same work split).  Every warp
 // owns, in shared memory,
-//   - a ring of kTmaStages stages of kTmaCol bond columns (slot codes + weights) of its
-//     slices, refilled by cp.async.bulk as soon as a stage is consumed, and
+//   - a ring of kTmaStages stages of kTmaCol interleaved bond columns of its slices (one
+//     cp.async.bulk per stage, completed on an mbarrier), refilled by lane 0 as soon as the
+//     warp has consumed the stage, and
 //   - two window buffers: the z values of the current slice's 9 window rows (the only nodes
-//     its bonds reach) and, in flight, the next slice's,
-// each completed on an mbarrier.  The gathers are shared-memory loads; HBM only sees the
-// streamed operator and the windows.  Waits are bounded: a timeout is recorded in the
-// instance's state (reported as NNPP_ERR_CUDA).
-constexpr int kTmaCol = 16;
-constexpr int kTmaStages = 3;
-constexpr int kStageW = kTmaCol * 32 * 4;  // weights of one stage (bytes)
-constexpr int kStageC = kTmaCol * 32 * 2;  // slot codes of one stage (bytes)
-constexpr int kStageBytes = kStageW + kStageC;
+//     its bonds reach) and, in flight, the next slice's, copied by the lanes with 16-byte
+//     cp.async.
+// The gathers are shared-memory loads; HBM only sees the streamed operator.  Waits are
+// bounded: a timeout is recorded in the instance's state (reported as NNPP_ERR_CUDA).
+constexpr int kTmaCol = 32;
+constexpr int kTmaStages = 2;
+constexpr int kStageBytes = kTmaCol * kSellW * 4;  // 6 KB
 constexpr int kWarpsCta = kBlock / 32;
 constexpr size_t kTmaRingBytes = (size_t)kWarpsCta * kTmaStages * kStageBytes;
 constexpr size_t kTmaWinBytes = (size_t)kWarpsCta * 2 * kWinCap * sizeof(float);
-constexpr size_t kTmaBarBytes = (size_t)kWarpsCta * (kTmaStages + 2) * sizeof(uint64_t);
+constexpr size_t kTmaBarBytes = (size_t)kWarpsCta * kTmaStages * sizeof(uint64_t);
 constexpr unsigned kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ int tma_chunks(int width) { return width > 0 ? (width + kTmaCol - 1) / kTmaCol : 1; }
@@ -536,8 +546,7 @@ struct TmaCursor {
   int sg, ch;
   int loaded;  // slice whose fields below are valid (-1: none)
   int width, nch;
-  const float* w;
-  const unsigned short* code;
+  const float* base;
 };
 
 // lane 0: issue the cursor's chunk into `stage` and advance; false when the range is done
@@ -550,11 +559,9 @@ __device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, i
     }
     if (c.sg >= s1) return false;
     const SliceDesc& d = v.slices[c.sg];
-    const KParams& k = v.inst[d.inst];
     c.width = d.width;
     c.nch = tma_chunks(c.width);
-    c.w = k.sell_w + d.off;
-    c.code = k.sell_slot + d.off;
+    c.base = sell_w(v.inst[d.inst], d);
     c.loaded = c.sg;
   }
   const int c0 = c.ch * kTmaCol;
@@ -562,12 +569,8 @@ __device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, i
   unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
   uint64_t* bar = bars + warp * kTmaStages + stage;
   fence_proxy_async_smem();
-  mbar_arrive_expect_tx(bar, (unsigned)(cc * 32 * 6));
-  if (cc > 0) {
-    const size_t e0 = (size_t)c0 * 32;
-    bulk_g2s_hint(buf, c.w + e0, (unsigned)(cc * 32 * 4), bar, pol);
-    bulk_g2s_hint(buf + kStageW, c.code + e0, (unsigned)(cc * 32 * 2), bar, pol);
-  }
+  mbar_arrive_expect_tx(bar, (unsigned)(cc * kSellW * 4));
+  if (cc > 0) bulk_g2s_hint(buf, c.base + (size_t)c0 * kSellW, (unsigned)(cc * kSellW * 4), bar, pol);
   if (++c.ch >= c.nch) {
     c.ch = 0;
     ++c.sg;
@@ -575,19 +578,23 @@ __device__ __forceinline__ bool tma_produce(const EngineView& v, TmaCursor& c, i
   return true;
 }
 
-// lane 0: copy the window of the next active slice at or after *ws into window buffer wb;
-// advances *ws past it; false when none is left
-__device__ __forceinline__ bool win_produce(const EngineView& v, int* ws, int s1, float* win, uint64_t* bar) {
+// all lanes: 16-byte cp.async copies of the window of the next active slice at or after *ws
+// into zw, then one commit group (empty when no slice is left); advances *ws past it
+__device__ __forceinline__ void win_copy(const EngineView& v, int* ws, int s1, float* zw, int lane) {
   while (*ws < s1 && !slice_active(v, *ws)) ++*ws;
-  if (*ws >= s1) return false;
-  const SliceDesc& d = v.slices[*ws];
-  const float* z = v.inst[d.inst].z32;
-  fence_proxy_async_smem();
-  mbar_arrive_expect_tx(bar, (unsigned)(d.wtotal * 4));
-  for (int r = 0; r < 9; ++r)
-    if (d.wlen[r] > 0) bulk_g2s(win + d.woff[r], z + d.lo[r], (unsigned)(d.wlen[r] * 4), bar);
-  ++*ws;
-  return true;
+  if (*ws < s1) {
+    const SliceDesc& d = v.slices[*ws];
+    const float* z = v.inst[d.inst].z32;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+      const int n = d.wlen[r], lo = d.lo[r], wo = d.woff[r];
+      for (int i = 4 * lane; i < n; i += 128)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(zw + wo + i)), "l"(z + lo + i)
+                     : "memory");
+    }
+    ++*ws;
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 template <int W>
@@ -600,35 +607,32 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
   unsigned char* ring = dsm;
   float* wins = reinterpret_cast<float*>(dsm + kTmaRingBytes);
   uint64_t* bars = reinterpret_cast<uint64_t*>(dsm + kTmaRingBytes + kTmaWinBytes);
-  uint64_t* wbars = bars + kWarpsCta * kTmaStages;
-  if (threadIdx.x < kWarpsCta * (kTmaStages + 2)) mbar_init(bars + threadIdx.x, 1);
+  if (threadIdx.x < kWarpsCta * kTmaStages) mbar_init(bars + threadIdx.x, 1);
   fence_mbar_init();
   __syncthreads();
   int s0, s1;
   warp_slices(v, &s0, &s1);
   float* mywin = wins + (size_t)warp * 2 * kWinCap;
-  TmaCursor pc{s0, 0, -1, 0, 0, nullptr, nullptr};
+  TmaCursor pc{s0, 0, -1, 0, 0, nullptr};
   int wsrc = s0;  // next slice whose window is to be copied
   const uint64_t pol = l2_evict_first_policy();  // the operator is read once per launch
-  if (lane == 0) {
+  if (lane == 0)
     for (int st = 0; st < kTmaStages; ++st)
       if (!tma_produce(v, pc, s1, warp, st, ring, bars, pol)) break;
-    win_produce(v, &wsrc, s1, mywin, wbars + warp * 2);
-  }
-  __syncwarp();
+  win_copy(v, &wsrc, s1, mywin, lane);
   int stage = 0, wb = 0;
-  unsigned phases = 0u, wphases = 0u;
+  unsigned phases = 0u;
   int timed_out = -1;  // instance whose wait gave up
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
     if (slice_active(v, sg)) {
-      // the next slice's window goes to the other buffer (free: its slice is done)
-      if (lane == 0) win_produce(v, &wsrc, s1, mywin + (wb ^ 1) * kWinCap, wbars + warp * 2 + (wb ^ 1));
+      // the next slice's window goes to the other buffer (free: its slice is done), then
+      // this slice's window (the older commit group) is waited for
+      win_copy(v, &wsrc, s1, mywin + (wb ^ 1) * kWinCap, lane);
       if (lane < 9) s_woff[warp][lane] = d.woff[lane];
       const int width = d.width;
-      // the row's own values are loaded now and arrive while the slice streams
       const int a = d.row0 + lane;
       const bool live = lane < d.nrows && k.freem[a];
       float za = 0.0f, da = 0.0f, qa = 0.0f, pa = 0.0f;
@@ -638,9 +642,8 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
         qa = k.q32[a];
         pa = k.p32[a];
       }
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
       __syncwarp();
-      if (!mbar_wait_bounded(wbars + warp * 2 + wb, (wphases >> wb) & 1u, kWaitPolls)) timed_out = d.inst;
-      wphases ^= 1u << wb;
       const float* zw = mywin + wb * kWinCap;
       const int* wo = s_woff[warp];
       float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -649,20 +652,19 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
         uint64_t* bar = bars + warp * kTmaStages + stage;
         if (!mbar_wait_bounded(bar, (phases >> stage) & 1u, kWaitPolls)) timed_out = d.inst;
         phases ^= 1u << stage;
-        const unsigned char* buf = ring + (size_t)(warp * kTmaStages + stage) * kStageBytes;
-        const float* sw = reinterpret_cast<const float*>(buf) + lane;
-        const unsigned short* sc = reinterpret_cast<const unsigned short*>(buf + kStageW) + lane;
+        const float* sw = reinterpret_cast<const float*>(ring + (size_t)(warp * kTmaStages + stage) * kStageBytes) + lane;
+        const unsigned short* sc = reinterpret_cast<const unsigned short*>(sw - lane + 32) + lane;
         const int cc = min(kTmaCol, width - ch * kTmaCol);
         if (cc == kTmaCol) {
-#pragma unroll
+#pragma unroll 8
           for (int c = 0; c < kTmaCol; ++c) {
-            const unsigned q = sc[32 * c];
-            acc[c & 3] = fmaf(sw[32 * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
+            const unsigned q = sc[kSellC * c];
+            acc[c & 3] = fmaf(sw[kSellW * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
           }
         } else {
           for (int c = 0; c < cc; ++c) {
-            const unsigned q = sc[32 * c];
-            acc[c & 3] = fmaf(sw[32 * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
+            const unsigned q = sc[kSellC * c];
+            acc[c & 3] = fmaf(sw[kSellW * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
           }
         }
         __syncwarp();
@@ -684,6 +686,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
     part = warp_sum_d(part);
     if (lane == 0) v.partials[sg] = part;
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   if (timed_out >= 0 && lane == 0) v.inst[timed_out].ds->wait_timeout = 1;
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
@@ -1175,8 +1178,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
 #pragma unroll
       for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
       int iface = 0;
-      const unsigned short* cs = k.sell_slot + d.off + lane;
-      const float* ws = k.sell_w + d.off + lane;
+      const float* ws = sell_w(k, d) + lane;
+      const unsigned short* cs = sell_code(k, d) + lane;
       const int len = k.row[a + 1] - k.row[a];
       // the next streamed column is in flight while this one's neighbour record is gathered
       float wn = len > 0 ? __ldcs(ws) : 0.0f;
@@ -1186,8 +1189,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
         const float w = wn;
         const int n = code_node(hb, cn_code);
         if (c + 1 < len) {
-          wn = __ldcs(ws + 32 * (c + 1));
-          cn_code = __ldcs(cs + 32 * (c + 1));
+          wn = __ldcs(ws + kSellW * (c + 1));
+          cn_code = __ldcs(cs + kSellC * (c + 1));
         }
         const float4 cn = __ldg(rc + 2 * n);
         const float4 nb = __ldg(rc + 2 * n + 1);
@@ -1609,7 +1612,7 @@ size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) +
 
 template <typename K>
 nnpp_status allow_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024)
+  if (bytes > 32 * 1024)  // the default limit counts static shared memory too
     NNPP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return NNPP_OK;
 }
@@ -1814,12 +1817,12 @@ __global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, con
 #pragma unroll
       for (int q = 0; q < S; ++q) A1[q] = A2[q] = a1[q] = a2[q] = sl[q] = sc[q] = 0.0f;
       int iface = 0;
-      const unsigned short* cs = k.sell_slot + d.off + lane;
-      const float* ws = k.sell_w + d.off + lane;
+      const float* ws = sell_w(k, d) + lane;
+      const unsigned short* cs = sell_code(k, d) + lane;
       const int len = k.row[a + 1] - k.row[a];
       for (int c = 0; c < len; ++c) {
-        const float w = __ldcs(ws + 32 * c);
-        const int n = code_node(hb, __ldcs(cs + 32 * c));
+        const float w = __ldcs(ws + kSellW * c);
+        const int n = code_node(hb, __ldcs(cs + kSellC * c));
         const float4 cn = __ldg(rec + 3 * n), ln = __ldg(rec + 3 * n + 1), pn = __ldg(rec + 3 * n + 2);
         const bool nsol = pn.z != 0.0f;
         iface |= (pm && !nsol) ? 1 : 0;
@@ -2208,8 +2211,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.row = h.lay.row.get();
   k.col = h.lay.col.get();
   k.slot16 = h.slot16.get();
-  k.sell_slot = h.sell_slot.get();
-  k.sell_w = h.sell_w.get();
+  k.sell = h.sell.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
   k.dirmask = h.dirmask.get();

@@ -1,6 +1,6 @@
 // tiles.cu -- tile work items of one instance, 16-bit halo slots of every bond, FP32
-// position records and the sliced (32 rows per slice, column-major) copy of the slots and
-// FP32 weights that the CG operator streams.
+// position records and the sliced operator (32 rows per slice, column-major, each bond
+// column 32 FP32 weights + 32 16-bit codes) that the FP32 kernels stream.
 //
 // A tile is T consecutive bins along x (bins of side >= the horizon radius, x-fastest
 // order, so the tile's own nodes and each of its 3x3 halo rows are contiguous node
@@ -142,11 +142,11 @@ __global__ void k_slice_windows(int nslices, const SliceDesc* sl, const int* pre
   }
 }
 
-// warp per slice: bond c of lane l (row row0 + l) at off + 32 c + l as (window row << 12 |
-// node - lo[row]) and its FP32 weight; padding: code 0, weight 0
+// warp per slice: bond c of lane l (row row0 + l): its FP32 weight at float 48 (off/32 + c)
+// + l of the interleaved array, its code (window row << 12 | node - lo[row]) at 16-bit
+// element 96 (off/32 + c) + 64 + l; padding: code 0, weight 0
 __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb, const int* row,
-                            const unsigned short* slot, const float* w32, unsigned short* ocode,
-                            float* ow) {
+                            const unsigned short* slot, const float* w32, float* sell) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
@@ -157,7 +157,7 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
     const int j0 = live ? row[d.row0 + lane] : 0;
     const int len = live ? row[d.row0 + lane + 1] - j0 : 0;
     for (int c = 0; c < d.width; ++c) {
-      const size_t o = (size_t)d.off + (size_t)c * 32 + lane;
+      float* col = sell + ((size_t)(d.off >> 5) + c) * 48;
       unsigned short code = 0;
       float w = 0.0f;
       if (c < len) {
@@ -166,8 +166,8 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
         code = (unsigned short)((r << 12) | (node - d.lo[r]));
         w = w32[j0 + c];
       }
-      ocode[o] = code;
-      ow[o] = w;
+      col[lane] = w;
+      reinterpret_cast<unsigned short*>(col + 32)[lane] = code;
     }
   }
 }
@@ -262,8 +262,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
       }
   // sliced copy of the slot codes and FP32 weights for the CG operator and the transport
   const size_t ns = slices.size();
-  if (!h.sell_slot.alloc((size_t)soff + 32) || !h.sell_w.alloc((size_t)soff + 32))
-    return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48)) return set_error(NNPP_ERR_NOMEM, "sliced operator");
   DBuf<SliceDesc> dsl;
   DBuf<int> dpre, dlohi;
   bool fit = true;
@@ -301,7 +300,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
     }
     NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
     k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), dpre.get(), L.row.get(), h.slot16.get(), L.w32.get(),
-                                      h.sell_slot.get(), h.sell_w.get());
+                                      h.sell.get());
     NNPP_CUDA(cudaGetLastError());
     NNPP_CUDA(cudaStreamSynchronize(h.st));
   }
