@@ -25,6 +25,7 @@ struct KParams {
   const float* sell;
   const double* w64;
   const float* w32;
+  const float* wlo32;            // w64 - w32: the FP32 pair (w32, wlo32) carries w64
   const unsigned char* dirmask;  // bit k: species k Dirichlet, bit S: potential Dirichlet
   const double* bcval;           // (S+1)*N: species values already divided by CSolid
   Rec32* rec32_cur;

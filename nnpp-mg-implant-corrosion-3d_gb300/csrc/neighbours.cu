@@ -438,7 +438,7 @@ __global__ void k_gather_pos(const int* perm, const double* x, const double* y, 
 // w = beta(xi) dV / xi^(3+2s), FP64; same expression as the reference's bond terms
 // (utils.h:122-124) without the K D factors.
 __global__ void k_weights(int n, const int* row, const int* col, const double* pos, double delta,
-                          double dx, double dV, double s_exp, double* w64, float* w32) {
+                          double dx, double dV, double s_exp, double* w64, float* w32, float* wlo32) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   const double ex = 3.0 + 2.0 * s_exp;
@@ -451,6 +451,7 @@ __global__ void k_weights(int n, const int* row, const int* col, const double* p
       const double w = beta_fn<double>(xi, delta, dx) * dV / (s_exp == 0.0 ? xi * xi * xi : pow(xi, ex));
       w64[j] = w;
       w32[j] = (float)w;
+      wlo32[j] = (float)(w - (double)w32[j]);  // w = w32 + wlo32 to ~2^-48
     }
   }
 }
@@ -708,6 +709,7 @@ nnpp_status build_layout(cudaStream_t st, const RefLists& L, const double* x, co
   out.nnz = nnz;
   const size_t nz = nnz > 0 ? (size_t)nnz : 1;
   if (!tmpcol.alloc(nz) || !out.col.alloc(nz) || !out.w64.alloc(nz) || !out.w32.alloc(nz) ||
+      !out.wlo32.alloc(nz) ||
       !out.pos.alloc(3 * (size_t)N))
     return set_error(NNPP_ERR_NOMEM, "layout bonds");
   const int wg = grid_for((long long)N * 32, 256, 152 * 64);
@@ -716,7 +718,7 @@ nnpp_status build_layout(cudaStream_t st, const RefLists& L, const double* x, co
   k_sort_segments<<<grid_for(N, 1, 65535), 128, 0, st>>>(out.row.get(), N, tmpcol.get(), out.col.get());
   k_gather_pos<<<grid_for(N, 256), 256, 0, st>>>(out.perm.get(), x, y, z, N, out.pos.get());
   k_weights<<<wg, 256, 0, st>>>(N, out.row.get(), out.col.get(), out.pos.get(), delta, dx, dV, s_exp,
-                                out.w64.get(), out.w32.get());
+                                out.w64.get(), out.w32.get(), out.wlo32.get());
   NNPP_CUDA(cudaGetLastError());
   NNPP_CUDA(cudaStreamSynchronize(st));
   out.max_row = L.max_len - 1;

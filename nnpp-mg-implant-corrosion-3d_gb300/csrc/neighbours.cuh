@@ -34,6 +34,7 @@ struct Layout {
   DBuf<double> pos;      // 3N SoA, internal order
   DBuf<double> w64;      // nnz
   DBuf<float> w32;       // nnz
+  DBuf<float> wlo32;     // nnz: w64 - w32 (so that w32 + wlo32 carries w64 to ~2^-48)
 };
 
 // GPU exclusive scan of n ints into out[0..n] (out[n] = total).  Returns the total.

@@ -188,6 +188,30 @@ __device__ __forceinline__ float sel4(const float4& v, int s) {
   return s == 0 ? v.x : s == 1 ? v.y : s == 2 ? v.z : v.w;
 }
 
+// FP32 pairs (hi, lo) standing in for FP64 where GB300's FP64 rate would bound a bond pass:
+// products by FMA-based TwoProd, sums by TwoSum; ~2^-46 relative per operation.
+__device__ __forceinline__ void pair_add(float& sh, float& sl, float ah, float al) {
+  float s, e;
+  two_sum(sh, ah, s, e);
+  sh = s;
+  sl += e + al;
+}
+__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+  ph = ah * bh;
+  pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
+}
+// sum of pairs over the W lanes of a node's segment (lane 0 of the segment holds it)
+template <int WIDTH>
+__device__ __forceinline__ double seg_reduce_pair(float h, float l) {
+#pragma unroll
+  for (int off = WIDTH / 2; off > 0; off >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, h, off, WIDTH);
+    const float ol = __shfl_down_sync(0xffffffffu, l, off, WIDTH);
+    pair_add(h, l, oh, ol);
+  }
+  return (double)h + (double)l;
+}
+
 // ------------------------------------------------------------------- potential: prep ----
 // Per node: K11 diagonal (sum of liquid-liquid weights), unknown mask, right-hand side
 // b = (1/(K sigma)) F CSolid sum_k z_k c_k and the FP64 residual r = b - A phi.  With F11_out
@@ -204,14 +228,22 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
     const TileDesc t = v.tiles[item];
     const KParams& k = v.inst[t.inst];
     load_tile(t, ts);
+    constexpr bool kPair = sizeof(P) == 4;  // mixed path: FP32-pair arithmetic on the bonds
     double* sphi = reinterpret_cast<double*>(dsm);
+    float2* sphi2 = reinterpret_cast<float2*>(dsm);
     unsigned char* sfl = dsm + sizeof(double) * (size_t)t.halo;
     const unsigned short* sslot = stage_slots(k.slot16, t, dsm + align16(sizeof(double) * (size_t)t.halo + t.halo));
     const double* phi64 = k.phi64;
     const unsigned char* dm = k.dirmask;
     for (int s = threadIdx.x; s < t.halo; s += kBlock) {
       const int n = halo_node(ts, s);
-      sphi[s] = phi64[n];
+      const double ph = phi64[n];
+      if (kPair) {
+        const float hi = (float)ph;
+        sphi2[s] = make_float2(hi, (float)(ph - (double)hi));
+      } else {
+        sphi[s] = ph;
+      }
       sfl[s] = (unsigned char)((phase_of<P>(k, n) == 0.0f ? 1 : 0) | (((dm[n] >> S) & 1) ? 2 : 0));
     }
     __syncthreads();
@@ -227,23 +259,46 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
       const bool scan = act && (fa & 1) && (F11_out != nullptr || !(fa & 2));
       double dsum = 0.0, swphi = 0.0, cpl = 0.0;
       int anyll = 0;
-      if (scan) {
-        for (int j = row[a] + sub; j < row[a + 1]; j += W) {
-          const int s = sslot[j - t.bond0];
-          const unsigned char f = sfl[s];
-          if (f & 1) {
-            const double w = w64[j];
-            const double ph = sphi[s];
-            dsum += w;
-            swphi += w * ph;
-            anyll = 1;
-            if (f & 2) cpl += w * ph;
+      if (kPair) {
+        float dh = 0.f, dl = 0.f, sh = 0.f, sl = 0.f, ch = 0.f, cl = 0.f;
+        if (scan) {
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+            const int s = sslot[j - t.bond0];
+            const unsigned char f = sfl[s];
+            if (f & 1) {
+              const float wh = k.w32[j], wl = k.wlo32[j];
+              const float2 ph = sphi2[s];
+              float ph_, pl_;
+              pair_mul(wh, wl, ph.x, ph.y, ph_, pl_);
+              pair_add(dh, dl, wh, wl);
+              pair_add(sh, sl, ph_, pl_);
+              anyll = 1;
+              if (f & 2) pair_add(ch, cl, ph_, pl_);
+            }
           }
         }
+        dsum = seg_reduce_pair<W>(dh, dl);
+        swphi = seg_reduce_pair<W>(sh, sl);
+        cpl = seg_reduce_pair<W>(ch, cl);
+      } else {
+        if (scan) {
+          for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+            const int s = sslot[j - t.bond0];
+            const unsigned char f = sfl[s];
+            if (f & 1) {
+              const double w = w64[j];
+              const double ph = sphi[s];
+              dsum += w;
+              swphi += w * ph;
+              anyll = 1;
+              if (f & 2) cpl += w * ph;
+            }
+          }
+        }
+        dsum = seg_reduce_d<W>(dsum);
+        swphi = seg_reduce_d<W>(swphi);
+        cpl = seg_reduce_d<W>(cpl);
       }
-      dsum = seg_reduce_d<W>(dsum);
-      swphi = seg_reduce_d<W>(swphi);
-      cpl = seg_reduce_d<W>(cpl);
       anyll = seg_or<W>(anyll);
       if (act && sub == 0) {
         double b;
@@ -254,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
           for (int s = 0; s < S; ++s) R11 += k.z[s] * conc_of<P>(k, a, s);
           b = k.lam * R11;
         }
-        const double pha = sphi[so];
+        const double pha = kPair ? (double)sphi2[so].x + (double)sphi2[so].y : sphi[so];
         if (F11_out) {
           F11_out[a] = anyll ? (dsum * pha - swphi) - b : 0.0;
         } else {
@@ -1023,9 +1078,23 @@ __global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphCon
         const int a = a0 + seg;
         const bool act = a < t.own_end && freem[a];
         double acc = 0.0;
-        if (act)
-          for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[sslot[j - t.bond0]], acc);
-        acc = seg_reduce_d<W>(acc);
+        if (mixed) {
+          // A e with the FP32 pair (w32, wlo32) and the FP32 correction e: exact products
+          // (TwoProd), TwoSum accumulation
+          float sh = 0.f, sl = 0.f;
+          if (act)
+            for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+              const float ev = (float)hs[sslot[j - t.bond0]];
+              float ph, pl;
+              pair_mul(k.w32[j], k.wlo32[j], ev, 0.0f, ph, pl);
+              pair_add(sh, sl, ph, pl);
+            }
+          acc = seg_reduce_pair<W>(sh, sl);
+        } else {
+          if (act)
+            for (int j = row[a] + sub; j < row[a + 1]; j += W) acc = fma(w64[j], hs[sslot[j - t.bond0]], acc);
+          acc = seg_reduce_d<W>(acc);
+        }
         if (act && sub == 0) {
           const double ea = hs[own0 + (a - t.own_begin)];
           const double r = k.r64[a] - (k.dsum64[a] * ea - acc);
@@ -2214,6 +2283,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.sell = h.sell.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
+  k.wlo32 = h.lay.wlo32.get();
   k.dirmask = h.dirmask.get();
   k.bcval = h.bcval.get();
   k.rec32_cur = h.rec32[cur].get();
