@@ -325,6 +325,16 @@ def run_ours(args):
     d1 = sim.diagnostics()
     ms64 = sim64.forward_timed(args.steps, nn.FP64)
     d64 = sim64.diagnostics()
+    # the same run with the diagonal (Jacobi) preconditioner alone, for comparison
+    pk, cn = sim.preconditioner()
+    simj = nn.Simulation.from_synth(inp)
+    simj.build_neighbours()
+    simj.set_preconditioner(nn.PRECOND_JACOBI)
+    simj.forward(args.warmup, nn.MIXED)
+    dj0 = simj.diagnostics()
+    msj = simj.forward_timed(args.steps, nn.MIXED)
+    dj1 = simj.diagnostics()
+    del simj
 
     # max over ranks
     if world > 1:
@@ -350,7 +360,10 @@ def run_ours(args):
     inner = d1["cg_iterations_total"] - d0["cg_iterations_total"]
     outer = d1["outer_iterations_total"] - d0["outer_iterations_total"]
     solves = d1["cg_solves"] - d0["cg_solves"]
-    launches = solves + 2 * outer + 2 * inner + args.steps
+    # per solve: warm-start dots + apply + prep; per outer iteration cg_init + ir_update; per CG
+    # iteration spmv + update; with the coarse correction restrict + coarse product + z/dots
+    # after every cg_init and update; per step the transport
+    launches = 3 * solves + 2 * outer + 2 * inner + args.steps + (3 * (inner + outer) if cn else 0)
 
     # kernel roofline: CUDA-event timed launches on the library's stream (state restored)
     with ProfileRange("kernels"):
@@ -384,6 +397,9 @@ def run_ours(args):
     bytes_tr = 4 * nnz + 4 * (N + 1) + N * (4 * b + b + 1 + 3 * 8 + 4 * b)
     bytes_ir = 4 * nnz + 4 * (N + 1) + N * (b + 8 + 8 + 8)
     bytes_upd = N * b * 6 + N * b
+    if cn:
+        # restriction (r), coarse product (the n x n inverse), z = D^-1 r + x_c[agg] (r, dinv, agg, z)
+        bytes_upd += N * b + 4 * cn * cn + N * (b + b + 4 + b)
     dom = max(shares, key=shares.get)
     alg = {"cg_spmv": (bytes_spmv, t_spmv), "transport": (bytes_tr, t_tr), "ir_residual": (bytes_ir, t_ir),
            "cg_update": (bytes_upd, t_upd)}
@@ -470,7 +486,12 @@ def run_ours(args):
                          "mixed_over_fp64": value / world / value64},
             "accuracy_vs_fp64_gpu": acc,
             "solver": {"inner_cg_per_step": inner / args.steps, "outer_per_step": outer / args.steps,
-                       "fp64_cg_per_step": (d64["cg_iterations_total"]) / (args.steps + args.warmup)},
+                       "fp64_cg_per_step": (d64["cg_iterations_total"]) / (args.steps + args.warmup),
+                       "preconditioner": "two-level (Jacobi + coarse aggregates)" if pk else "jacobi",
+                       "coarse_unknowns": cn,
+                       "jacobi_only": {"ms_per_step": msj / args.steps,
+                                       "inner_cg_per_step": (dj1["cg_iterations_total"] -
+                                                             dj0["cg_iterations_total"]) / args.steps}},
             "adjoint_over_forward": adj["gradient_over_forward"] if adj else None,
             "adjoint": adj,
             "ensemble": ensemble,

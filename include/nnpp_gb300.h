@@ -53,6 +53,11 @@ typedef enum nnpp_precision {
   NNPP_MIXED = 1    /* FP32 bond sums (compensated), FP32 inner CG + FP64 refinement */
 } nnpp_precision;
 
+typedef enum nnpp_preconditioner {
+  NNPP_PRECOND_JACOBI = 0,     /* z = D^-1 r (the reference's diagonal scaling)            */
+  NNPP_PRECOND_TWO_LEVEL = 1   /* z = D^-1 r + P A_c^-1 P^T r, aggregates of bin blocks     */
+} nnpp_preconditioner;
+
 typedef enum nnpp_order_mode {
   NNPP_ORDER_REFERENCE = 0,  /* within-cell order of std::sort as in grid.h:90 (bit-exact) */
   NNPP_ORDER_CANONICAL = 1   /* within-cell order by node index (stable counting sort)   */
@@ -213,6 +218,18 @@ nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict
  * application).  Only the iteration count depends on it: every solve still runs to the
  * solver tolerance.  Discards a recorded forward_ckpt run. */
 nnpp_status nnpp_set_warm_start(nnpp_handle* h, int history);
+
+/* Preconditioner of the potential CG (both precisions).  NNPP_PRECOND_TWO_LEVEL (the
+ * default) adds to the Jacobi scaling a coarse correction on aggregates of f x f x f hash
+ * bins (at most 3000 aggregates): the Galerkin coarse operator P^T A P of the current
+ * phases, inverted once per state (nnpp_set_state / nnpp_reset) on the GPU, applied as one
+ * dense product per iteration.  Single-instance runs only (ensembles use Jacobi).  Only the
+ * iteration count depends on it: every solve still runs to the solver tolerance.  Discards a
+ * recorded forward_ckpt run.  The reference's solve of K11 is diagonally preconditioned
+ * (Eigen::GMRES with DiagonalPreconditioner, main.cpp:764-766, solved at main.cpp:779). */
+nnpp_status nnpp_set_preconditioner(nnpp_handle* h, int kind);
+/* Current preconditioner and the number of coarse unknowns (0 for Jacobi). */
+nnpp_status nnpp_get_preconditioner(nnpp_handle* h, int* kind, int* coarse_unknowns);
 
 /* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
  * NULL. */

@@ -22,6 +22,8 @@ FP64 = 0
 MIXED = 1
 ORDER_REFERENCE = 0
 ORDER_CANONICAL = 1
+PRECOND_JACOBI = 0
+PRECOND_TWO_LEVEL = 1
 
 STATUS = {0: "NNPP_OK", 1: "NNPP_ERR_INVALID", 2: "NNPP_ERR_CAPACITY", 3: "NNPP_ERR_NONFINITE",
           4: "NNPP_ERR_CG_NO_CONVERGE", 5: "NNPP_ERR_CUDA", 6: "NNPP_ERR_UNSUPPORTED",
@@ -104,6 +106,8 @@ _SIGS = {
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
     "nnpp_set_warm_start": (C.c_int, [_P, C.c_int]),
+    "nnpp_set_preconditioner": (C.c_int, [_P, C.c_int]),
+    "nnpp_get_preconditioner": (C.c_int, [_P, _IP, _IP]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -292,6 +296,17 @@ class Simulation:
         """Initial guess of the potential solves: 0 previous potential, 1-2 linear
         extrapolation, 3-6 energy-norm-optimal combination of that many past potentials."""
         _check(lib().nnpp_set_warm_start(self._h, history))
+
+    def set_preconditioner(self, kind):
+        """Preconditioner of the potential CG: PRECOND_JACOBI (diagonal) or
+        PRECOND_TWO_LEVEL (diagonal + coarse correction on aggregates of hash bins)."""
+        _check(lib().nnpp_set_preconditioner(self._h, kind))
+
+    def preconditioner(self):
+        """(kind, coarse unknowns) of the potential CG's preconditioner."""
+        k, n = C.c_int(), C.c_int()
+        _check(lib().nnpp_get_preconditioner(self._h, C.byref(k), C.byref(n)))
+        return k.value, n.value
 
     def reset(self):
         """Back to the initial state of build_neighbours (lists and tuning kept)."""

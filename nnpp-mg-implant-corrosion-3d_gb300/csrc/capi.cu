@@ -378,6 +378,7 @@ nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, do
   h.engine->members.push_back(&h);
   h.engine->st = h.st;
   nnpp_status st = engine_build(*h.engine);
+  if (st == NNPP_OK) st = coarse_build(h);
   if (st != NNPP_OK) {
     h.built = false;
     return st;
@@ -441,6 +442,7 @@ nnpp_status nnpp_set_state(nnpp_handle* hp, const double* c, const double* phi, 
   if (!c) return set_error(NNPP_ERR_INVALID, "c is NULL");
   Handle& h = hp->h;
   NNPP_TRY(upload_state(h, c, phi, phase, h.state_prec));
+  h.coarse.stale = true;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   return NNPP_OK;
 }
@@ -686,7 +688,38 @@ nnpp_status nnpp_set_warm_start(nnpp_handle* hp, int history) {
 nnpp_status nnpp_reset(nnpp_handle* hp) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
-  return reset_initial(hp->h);
+  NNPP_TRY(reset_initial(hp->h));
+  hp->h.coarse.stale = true;
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_set_preconditioner(nnpp_handle* hp, int kind) {
+  NNPP_GUARD(hp);
+  if (kind != NNPP_PRECOND_JACOBI && kind != NNPP_PRECOND_TWO_LEVEL)
+    return set_error(NNPP_ERR_INVALID, "preconditioner: 0 (Jacobi) or 1 (two-level)");
+  Handle& h = hp->h;
+  NNPP_CUDA(cudaSetDevice(h.device));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  const bool want = kind == NNPP_PRECOND_TWO_LEVEL;
+  if (want == h.coarse_enabled) return NNPP_OK;
+  h.coarse_enabled = want;
+  h.coarse.valid = false;
+  h.coarse.stale = true;
+  h.fwd_steps = 0;
+  h.ckpts.clear();
+  if (h.built) {
+    if (want && h.coarse.n == 0) NNPP_TRY(coarse_build(h));
+    if (h.engine) NNPP_TRY(engine_params(*h.engine));
+  }
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_preconditioner(nnpp_handle* hp, int* kind, int* coarse_unknowns) {
+  NNPP_GUARD(hp);
+  const Handle& h = hp->h;
+  if (kind) *kind = h.coarse_enabled ? NNPP_PRECOND_TWO_LEVEL : NNPP_PRECOND_JACOBI;
+  if (coarse_unknowns) *coarse_unknowns = h.coarse_enabled ? h.coarse.n : 0;
+  return NNPP_OK;
 }
 
 nnpp_status nnpp_set_params(nnpp_handle* hp, const nnpp_params* p) {

@@ -1,0 +1,225 @@
+// coarse.cu -- the coarse space of the two-level preconditioner of the potential solve.
+//
+// Aggregates are blocks of f x f x f bins (bins of side >= the horizon radius, so every bond
+// joins the same or an adjacent aggregate).  The preconditioner is
+//   M^-1 r = D^-1 r + P A_c^-1 P^T r,   P = the aggregate indicator of the unknowns,
+// A_c = P^T A P the Galerkin coarse operator (27 nonzeros per row), stored with its inverse
+// as dense n x n FP32 matrices (n <= kCoarseMax).  The inverse comes from the Newton-Schulz
+// iteration X <- X (2I - A_c X), X_0 = I / ||A_c||_inf (every iterate is a positive
+// polynomial of A_c, so the preconditioner stays symmetric positive definite even when the
+// iteration is stopped early), on cuBLAS SGEMM.  The coarse operator is rebuilt when the
+// phases have changed (a stale one is still a valid preconditioner).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include <cublas_v2.h>
+
+#include "engine.cuh"
+
+namespace nnpp {
+
+namespace {
+
+constexpr int kNsIterations = 18;
+
+// aggregate of every node (internal order), from the bins' node ranges
+__global__ void k_agg_fill(const int* bin_start, int nb0, int nb1, int nb2, int f, int na0, int na1,
+                           int* agg) {
+  const int nbins = nb0 * nb1 * nb2;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
+    const int bx = b % nb0, by = (b / nb0) % nb1, bz = b / (nb0 * nb1);
+    const int I = bx / f + na0 * (by / f + na1 * (bz / f));
+    for (int i = bin_start[b]; i < bin_start[b + 1]; ++i) agg[i] = I;
+  }
+}
+
+__device__ __forceinline__ bool node_liquid(const KParams& k, int i, int mixed) {
+  return (mixed ? k.rec32_cur[i].phase : (float)k.rec64_cur[i].phase) == 0.0f;
+}
+
+// Warp per aggregate row I: the 27 entries of A_c = P^T A P from the current phases (an
+// unknown is a liquid node off the potential's Dirichlet set with a liquid neighbour; its
+// diagonal is the sum of its liquid bonds, its off-diagonals -w to unknown neighbours).
+// Lanes own fixed node subsets and reduce in a fixed order, so the matrix is reproducible.
+__global__ void k_coarse_assemble(KParams k, const int* bin_start, int nb0, int nb1, int nb2, int f,
+                                  int na0, int na1, int na2, int mixed, float* mat, float* rowabs) {
+  const int lane = threadIdx.x & 31;
+  const int n = na0 * na1 * na2;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < n; I += warps) {
+    const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
+    float acc[27];
+#pragma unroll
+    for (int q = 0; q < 27; ++q) acc[q] = 0.0f;
+    int unknowns = 0;
+    for (int bz = az * f; bz < min(az * f + f, nb2); ++bz)
+      for (int by = ay * f; by < min(ay * f + f, nb1); ++by)
+        for (int bx = ax * f; bx < min(ax * f + f, nb0); ++bx) {
+          const int b = bx + nb0 * (by + nb1 * bz);
+          for (int i = bin_start[b] + lane; i < bin_start[b + 1]; i += 32) {
+            if (!node_liquid(k, i, mixed) || ((k.dirmask[i] >> S) & 1)) continue;
+            float d = 0.0f;
+            bool ll = false;
+            for (int j = k.row[i]; j < k.row[i + 1]; ++j) {
+              const int m = k.col[j];
+              if (!node_liquid(k, m, mixed)) continue;
+              const float w = k.w32[j];
+              d += w;
+              ll = true;
+              if ((k.dirmask[m] >> S) & 1) continue;
+              const int J = k.agg[m];
+              const int jx = J % na0, jy = (J / na0) % na1, jz = J / (na0 * na1);
+              const int q = (jx - ax + 1) + 3 * ((jy - ay + 1) + 3 * (jz - az + 1));
+#pragma unroll
+              for (int t = 0; t < 27; ++t)
+                if (t == q) acc[t] -= w;
+            }
+            if (ll) {
+              acc[13] += d;
+              ++unknowns;
+            }
+          }
+        }
+    unknowns = __reduce_add_sync(0xffffffffu, unknowns);
+    float ra = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+      float x = acc[q];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      acc[q] = x;
+      ra += fabsf(x);
+    }
+    if (lane == 0) {
+      // no unknown in the aggregate: an identity row keeps A_c regular
+      if (unknowns == 0) {
+        mat[(size_t)I * n + I] = 1.0f;
+        ra = 1.0f;
+      } else {
+        for (int q = 0; q < 27; ++q) {
+          const int jx = ax + q % 3 - 1, jy = ay + (q / 3) % 3 - 1, jz = az + q / 9 - 1;
+          if (jx < 0 || jy < 0 || jz < 0 || jx >= na0 || jy >= na1 || jz >= na2) continue;
+          mat[(size_t)I * n + (jx + na0 * (jy + na1 * jz))] = acc[q];
+        }
+      }
+      rowabs[I] = ra;
+    }
+  }
+}
+
+// X = I / max_i rowabs[i]  (column-major n x n)
+__global__ void k_ns_init(int n, const float* rowabs, float* X) {
+  __shared__ float smax;
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int i = 0; i < n; ++i) m = fmaxf(m, rowabs[i]);
+    smax = m > 0.0f ? m : 1.0f;
+  }
+  __syncthreads();
+  const float inv = 1.0f / smax;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x)
+    X[e] = (e / n == e % n) ? inv : 0.0f;
+}
+
+// T = 2I - T
+__global__ void k_two_i_minus(int n, float* T) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x)
+    T[e] = ((e / n == e % n) ? 2.0f : 0.0f) - T[e];
+}
+
+// Y = (X + X^T) / 2
+__global__ void k_symmetrize(int n, const float* X, float* Y) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = e / n, j = e % n;
+    Y[e] = 0.5f * (X[e] + X[j * n + i]);
+  }
+}
+
+}  // namespace
+
+Coarse::~Coarse() {
+  if (cublas) cublasDestroy(static_cast<cublasHandle_t>(cublas));
+}
+
+nnpp_status coarse_build(Handle& h) {
+  Coarse& c = h.coarse;
+  c.valid = false;
+  c.n = 0;
+  if (!h.coarse_enabled) return NNPP_OK;
+  const Layout& L = h.lay;
+  int f = 1;
+  auto count = [&](int ff) {
+    long long n = 1;
+    for (int d = 0; d < 3; ++d) n *= (L.nb[d] + ff - 1) / ff;
+    return n;
+  };
+  while (count(f) > kCoarseMax) ++f;
+  c.f = f;
+  for (int d = 0; d < 3; ++d) c.na[d] = (L.nb[d] + f - 1) / f;
+  c.n = (int)count(f);
+  const size_t nn = (size_t)c.n * c.n;
+  if (!c.agg.alloc(h.N) || !c.inv.alloc(nn) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) || !c.rowabs.alloc(c.n))
+    return set_error(NNPP_ERR_NOMEM, "coarse space");
+  k_agg_fill<<<std::max(1, std::min((L.nbins + 255) / 256, 4096)), 256, 0, h.st>>>(
+      L.bin_start.get(), L.nb[0], L.nb[1], L.nb[2], f, c.na[0], c.na[1], c.agg.get());
+  NNPP_CUDA(cudaGetLastError());
+  if (!c.cublas) {
+    cublasHandle_t hb = nullptr;
+    if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasCreate");
+    c.cublas = hb;
+  }
+  c.stale = true;
+  return NNPP_OK;
+}
+
+nnpp_status coarse_refresh(Handle& h) {
+  Coarse& c = h.coarse;
+  if (!h.coarse_enabled || c.n == 0) return NNPP_OK;
+  const Layout& L = h.lay;
+  const int n = c.n;
+  const size_t nn = (size_t)n * n;
+  // work matrices on first use (ensemble members never refresh and never hold them)
+  if (!c.a.alloc(nn) || !c.t.alloc(nn) || !c.x.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "coarse inverse");
+  DBuf<float>& A = c.a;
+  DBuf<float>& T = c.t;
+  DBuf<float>& X = c.x;
+  NNPP_CUDA(cudaMemsetAsync(A.get(), 0, sizeof(float) * nn, h.st));
+  KParams kp = make_kparams(h, h.cur);
+  k_coarse_assemble<<<std::max(1, std::min((n * 32 + 255) / 256, 152 * 32)), 256, 0, h.st>>>(
+      kp, L.bin_start.get(), L.nb[0], L.nb[1], L.nb[2], c.f, c.na[0], c.na[1], c.na[2],
+      h.state_prec == NNPP_MIXED ? 1 : 0, A.get(), c.rowabs.get());
+  NNPP_CUDA(cudaGetLastError());
+  const int eg = (int)std::min<size_t>((nn + 255) / 256, 152 * 64);
+  k_ns_init<<<eg, 256, 0, h.st>>>(n, c.rowabs.get(), X.get());
+  NNPP_CUDA(cudaGetLastError());
+  cublasHandle_t hb = static_cast<cublasHandle_t>(c.cublas);
+  if (cublasSetStream(hb, h.st) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasSetStream");
+  const float one = 1.0f, zero = 0.0f;
+  float* x = X.get();
+  float* y = c.inv.get();  // scratch until the final symmetrisation
+  for (int it = 0; it < kNsIterations; ++it) {
+    // T = A X ; T = 2I - T ; X <- X T
+    if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
+        CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    k_two_i_minus<<<eg, 256, 0, h.st>>>(n, T.get());
+    NNPP_CUDA(cudaGetLastError());
+    if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, x, n, T.get(), n, &zero, y, n) !=
+        CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    std::swap(x, y);
+  }
+  // x holds the last iterate; the symmetrised copy goes to c.inv (through T when x is c.inv)
+  if (x == c.inv.get()) {
+    NNPP_CUDA(cudaMemcpyAsync(T.get(), x, sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
+    x = T.get();
+  }
+  k_symmetrize<<<eg, 256, 0, h.st>>>(n, x, c.inv.get());
+  NNPP_CUDA(cudaGetLastError());
+  c.valid = true;
+  c.stale = false;
+  return NNPP_OK;
+}
+
+}  // namespace nnpp

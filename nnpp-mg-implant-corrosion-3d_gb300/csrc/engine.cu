@@ -309,6 +309,17 @@ nnpp_status prepare_run(Engine& e, int prec) {
         break;
       }
   }
+  // two-level preconditioner of single-instance engines: recompute the coarse inverse when the
+  // state was replaced; the captured graphs follow whether the coarse correction is applied
+  if (e.members.size() == 1) {
+    Handle& h = *e.members[0];
+    if (h.coarse_enabled && h.coarse.n > 0 && (h.coarse.stale || !h.coarse.valid)) NNPP_TRY(coarse_refresh(h));
+  }
+  const bool split = engine_coarse(e);
+  if (split != e.coarse_graphs) {
+    engine_destroy_graphs(e);
+    e.coarse_graphs = split;
+  }
   NNPP_TRY(refresh_params(e));
   return NNPP_OK;
 }

@@ -100,6 +100,7 @@ struct Engine {
   cudaStream_t st = nullptr, st_b1 = nullptr, st_b2 = nullptr;
   int device = 0;
   int cur = 0;              // record parity shared by all members
+  bool coarse_graphs = false;  // graphs captured with the two-level preconditioner
   cudaGraphExec_t gexec[kGraphKinds][2][2] = {};
   cudaGraph_t graph[kGraphKinds][2][2] = {};
   ~Engine();
@@ -129,6 +130,7 @@ nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cud
 nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc);
+bool engine_coarse(const Engine& e);  // the two-level preconditioner applies (one member, inverse ready)
 nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc);
 nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,

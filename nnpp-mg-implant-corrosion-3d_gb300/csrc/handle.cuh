@@ -61,11 +61,37 @@ struct KParams {
                                  // solutions (history ring xh, bh = A xh); 0: off
   double* xh;                    // hist_m * N potentials of previous solves
   double* bh;                    // hist_m * N: A x of those (b - r at convergence)
+  // two-level preconditioner (single-instance engines): node -> aggregate, the coarse
+  // inverse (n x n), the restricted residual and the coarse correction
+  const int* agg;
+  const float* cinv;
+  float* rc;
+  float* xc;
+  const int* bin_start;
+  int coarse;                    // 1: z = D^-1 r + P A_c^-1 P^T r
+  int cn;                        // coarse unknowns
+  int cf, cna0, cna1, cna2, nb0, nb1, nb2;
 };
 
 enum GraphKind { kGraphStep2 = 0, kGraphStep1 = 1, kGraphSolve = 2, kGraphKinds = 3 };
 
 struct Engine;
+
+constexpr int kCoarseMax = 3000;  // aggregates of the coarse space (dense inverse n^2 floats)
+
+struct Coarse {
+  int f = 0, n = 0, na[3] = {0, 0, 0};
+  DBuf<int> agg;      // N: aggregate of each node
+  DBuf<float> inv;    // n x n: the coarse inverse
+  DBuf<float> rc, xc; // n: restricted residual, coarse correction
+  DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
+  DBuf<float> a, t, x; // n x n: A_c and the Newton-Schulz work matrices
+  void* cublas = nullptr;
+  bool valid = false; // inv holds an inverse
+  bool stale = true;  // the phases changed since inv was computed
+  long long solid_at = -1;
+  ~Coarse();
+};
 
 struct Handle {
   nnpp_params p;
@@ -115,6 +141,8 @@ struct Handle {
   bool settings_pushed = false; // tol, max_iter, ... already in the device state
   int extrapolate = 1;
   int warm_hist = kHistMax;     // history length of the warm start (0: extrapolation only)
+  bool coarse_enabled = true;   // two-level preconditioner (single-instance runs)
+  Coarse coarse;
   DBuf<double> xh, bh;          // warm-start history, warm_hist * N each
   double* warm_x_alt = nullptr; // another ring in place of xh, bh (the adjoint's solves)
   double* warm_b_alt = nullptr;
@@ -138,6 +166,10 @@ struct Handle {
   std::vector<double> curve;
   ~Handle();
 };
+
+// coarse.cu
+nnpp_status coarse_build(Handle& h);
+nnpp_status coarse_refresh(Handle& h);
 
 // step.cu
 nnpp_status step_alloc(Handle& h);

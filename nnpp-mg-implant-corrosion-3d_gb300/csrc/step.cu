@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
 // (the reference's Eigen::DiagonalPreconditioner, main.cpp:714-768).
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphConditionalHandle hc,
-                                                    int fp64) {
+                                                    int fp64, int split) {
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
@@ -369,6 +369,22 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
     const KParams& k = v.inst[c.inst];
     const bool active = *((volatile int*)&k.ds->outer_active) != 0;
     double part[2] = {0.0, 0.0};
+    if (split) {
+      // two-level preconditioner: r, p, q, e here; z and the dots after the coarse solve
+      if (active) {
+        P* rin = VecSel<P>::rin(k);
+        P* p = VecSel<P>::p(k);
+        P* q = VecSel<P>::q(k);
+        P* e = VecSel<P>::e(k);
+        for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+          rin[a] = (P)k.r64[a];
+          p[a] = P(0);
+          q[a] = P(0);
+          e[a] = P(0);
+        }
+      }
+      continue;
+    }
     if (active) {
       P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
@@ -817,7 +833,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
 
 // e += alpha p, r -= alpha q, z = D^-1 r, partial r.z and r.r -> beta, stop test
 template <typename P>
-__global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphConditionalHandle hc) {
+__global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphConditionalHandle hc, int split) {
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
@@ -825,6 +841,23 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
     const KParams& k = v.inst[c.inst];
     const bool active = *((volatile int*)&k.ds->inner_active) != 0;
     double part[2] = {0.0, 0.0};
+    if (split) {
+      // two-level preconditioner: e and r here; z and the dots after the coarse solve
+      if (active) {
+        P* rin = VecSel<P>::rin(k);
+        const P* p = VecSel<P>::p(k);
+        const P* q = VecSel<P>::q(k);
+        P* e = VecSel<P>::e(k);
+        const P* dinv = VecSel<P>::dinv(k);
+        const P alpha = (P)k.ds->alpha;
+        for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+          if (dinv[a] == P(0)) continue;
+          e[a] = e[a] + alpha * p[a];
+          rin[a] = rin[a] - alpha * q[a];
+        }
+      }
+      continue;
+    }
     if (active) {
       P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
@@ -853,6 +886,118 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (ds->inner_active) {
+          const double alpha_d = ds->alpha;
+          ds->beta = ds->rz != 0.0 ? tot[0] / ds->rz : 0.0;
+          ds->rz = tot[0];
+          ds->rr = tot[1];
+          ds->inner_it += 1;
+          ds->solve_iters += 1;
+          ds->cg_iters += 1;
+          const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
+                          ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
+          ds->inner_active = go ? 1 : 0;
+        }
+        instance_finished(v, c.inst, 1, hc);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ two-level preconditioner ----
+// Applied as z = D^-1 r + P A_c^-1 P^T r (single-instance engines; the coarse space and its
+// inverse come from coarse.cu): the restriction sums r over each aggregate, the coarse solve
+// is one product with the dense inverse, and k_cg_zdots forms z with the CG's dots and
+// decisions.  All reductions run in a fixed order (reproducible iterates).
+__device__ __forceinline__ bool coarse_active(const KParams& k, int which) {
+  return (which ? *((volatile int*)&k.ds->inner_active) : *((volatile int*)&k.ds->outer_active)) != 0;
+}
+
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int which) {
+  const KParams& k = v.inst[0];
+  if (!coarse_active(k, which)) return;
+  const P* r = VecSel<P>::rin(k);
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < k.cn; I += warps) {
+    const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
+    float acc = 0.0f;
+    for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
+      for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by)
+        for (int bx = ax * k.cf; bx < min(ax * k.cf + k.cf, k.nb0); ++bx) {
+          const int b = bx + k.nb0 * (by + k.nb1 * bz);
+          for (int i = k.bin_start[b] + lane; i < k.bin_start[b + 1]; i += 32) acc += (float)r[i];
+        }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) k.rc[I] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which) {
+  extern __shared__ __align__(16) float srv[];
+  const KParams& k = v.inst[0];
+  if (!coarse_active(k, which)) return;
+  const int n = k.cn;
+  for (int i = threadIdx.x; i < n; i += kBlock) srv[i] = k.rc[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < n; I += warps) {
+    const float* row = k.cinv + (size_t)I * n;
+    float acc = 0.0f;
+    for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(row + j), srv[j], acc);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) k.xc[I] = acc;
+  }
+}
+
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphConditionalHandle hc, int init,
+                                                     int fp64) {
+  __shared__ double sm[2 * kBlock / 32];
+  __shared__ int s_last;
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const bool active = coarse_active(k, init ? 0 : 1);
+    double part[2] = {0.0, 0.0};
+    if (active) {
+      const P* rin = VecSel<P>::rin(k);
+      P* z = VecSel<P>::z(k);
+      const P* dinv = VecSel<P>::dinv(k);
+      for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+        const P di = dinv[a];
+        const P r = rin[a];
+        const P zz = di == P(0) ? P(0) : r * di + (P)k.xc[k.agg[a]];
+        z[a] = zz;
+        part[0] += (double)r * (double)zz;
+        part[1] += (double)r * (double)r;
+      }
+    }
+    write_partials<2>(v, item, part, sm);
+    if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
+      double tot[2];
+      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (init) {
+          if (ds->outer_active) {
+            ds->rz = tot[0];
+            ds->rr = tot[1];
+            ds->beta = 0.0;
+            ds->alpha = 0.0;
+            ds->inner_it = 0;
+            const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
+                                       : ds->inner_rel * ds->inner_rel * tot[1];
+            ds->inner_target = target;
+            ds->inner_active = (tot[1] > target && ds->max_iter > 0) ? 1 : 0;
+          } else {
+            ds->inner_active = 0;
+          }
+        } else if (ds->inner_active) {
           const double alpha_d = ds->alpha;
           ds->beta = ds->rz != 0.0 ? tot[0] / ds->rz : 0.0;
           ds->rz = tot[0];
@@ -2167,13 +2312,32 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
   });
 }
 
+// z = M^-1 r with the two-level preconditioner: restriction, coarse solve, z and the dots
+template <typename P>
+nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t st, cudaGraphConditionalHandle hc,
+                            int init) {
+  const Coarse& c = e.members[0]->coarse;
+  const int which = init ? 0 : 1;
+  const int rg = std::max(1, std::min((c.n * 32 + kBlock - 1) / kBlock, e.sms * 8));
+  k_coarse_restrict<P><<<rg, kBlock, 0, st>>>(v, which);
+  k_coarse_gemv<<<rg, kBlock, (size_t)c.n * sizeof(float), st>>>(v, which);
+  k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, init,
+                                                                               sizeof(P) == 8 ? 1 : 0);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+bool engine_coarse(const Engine& e) { return e.members.size() == 1 && e.members[0]->coarse.valid; }
+
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc) {
+  const int split = engine_coarse(e) ? 1 : 0;
   if (prec == NNPP_MIXED)
-    k_cg_init<float><<<occ_grid(k_cg_init<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0);
+    k_cg_init<float><<<occ_grid(k_cg_init<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, 0, split);
   else
-    k_cg_init<double><<<occ_grid(k_cg_init<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 1);
+    k_cg_init<double><<<occ_grid(k_cg_init<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, 1, split);
   NNPP_CUDA(cudaGetLastError());
+  if (split) return prec == NNPP_MIXED ? launch_coarse_z<float>(e, v, st, hc, 1) : launch_coarse_z<double>(e, v, st, hc, 1);
   return NNPP_OK;
 }
 
@@ -2196,11 +2360,13 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
 
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
+  const int split = engine_coarse(e) ? 1 : 0;
   if (prec == NNPP_MIXED)
-    k_cg_update<float><<<occ_grid(k_cg_update<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
+    k_cg_update<float><<<occ_grid(k_cg_update<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, split);
   else
-    k_cg_update<double><<<occ_grid(k_cg_update<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
+    k_cg_update<double><<<occ_grid(k_cg_update<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, split);
   NNPP_CUDA(cudaGetLastError());
+  if (split) return prec == NNPP_MIXED ? launch_coarse_z<float>(e, v, st, hc, 0) : launch_coarse_z<double>(e, v, st, hc, 0);
   return NNPP_OK;
 }
 
@@ -2338,6 +2504,21 @@ KParams make_kparams(Handle& h, int cur) {
   k.hist_m = (h.extrapolate && h.warm_hist >= 3 && h.xh.get()) ? h.warm_hist : 0;
   k.xh = h.warm_x_alt ? h.warm_x_alt : h.xh.get();
   k.bh = h.warm_b_alt ? h.warm_b_alt : h.bh.get();
+  const Coarse& co = h.coarse;
+  k.coarse = co.valid ? 1 : 0;
+  k.agg = co.agg.get();
+  k.cinv = co.inv.get();
+  k.rc = const_cast<float*>(co.rc.get());
+  k.xc = const_cast<float*>(co.xc.get());
+  k.bin_start = h.lay.bin_start.get();
+  k.cn = co.n;
+  k.cf = co.f;
+  k.cna0 = co.na[0];
+  k.cna1 = co.na[1];
+  k.cna2 = co.na[2];
+  k.nb0 = h.lay.nb[0];
+  k.nb1 = h.lay.nb[1];
+  k.nb2 = h.lay.nb[2];
   return k;
 }
 

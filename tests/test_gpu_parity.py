@@ -318,6 +318,81 @@ def test_warm_start_modes_agree_and_history_saves_iterations(gpu, prec):
     assert out[1][1]["cg_iterations_total"] < out[0][1]["cg_iterations_total"]
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("n", [24, 48])
+def test_preconditioners_agree_and_two_level_saves_iterations(gpu, orc, prec, n):
+    """The two-level preconditioner changes only the iteration count: both preconditioners
+    reach the oracle's state (to 1e-9 in FP64, the mixed tolerance in mixed precision), and
+    the coarse correction needs fewer CG iterations.  n = 48 has more bins than coarse
+    unknowns, so aggregates of 2 x 2 x 2 bins are formed."""
+    nn = gpu
+    inp = nn.synth(1, n, seed=9)
+    o = orc.Oracle.from_synth(inp)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    o.forward(30)
+    c_o, phi_o, ph_o, _ = o.state()
+    out = {}
+    for kind in (nn.PRECOND_JACOBI, nn.PRECOND_TWO_LEVEL):
+        sim = nn.Simulation.from_synth(inp)
+        sim.build_neighbours()
+        sim.set_preconditioner(kind)
+        k, cn = sim.preconditioner()
+        assert k == kind and (cn > 0) == (kind == nn.PRECOND_TWO_LEVEL)
+        sim.forward(30, prec)
+        out[kind] = (sim.state(), sim.diagnostics(), cn)
+    tol = 1e-9 if prec == nn.FP64 else 1e-5
+    for kind, ((c, phi, ph), d, cn) in out.items():
+        assert np.array_equal(ph, ph_o)
+        assert np.linalg.norm(c - c_o) <= tol * np.linalg.norm(c_o)
+        assert np.linalg.norm(phi - phi_o) <= tol * np.linalg.norm(phi_o)
+        assert d["cg_not_converged"] == 0
+    it_j = out[nn.PRECOND_JACOBI][1]["cg_iterations_total"]
+    it_c = out[nn.PRECOND_TWO_LEVEL][1]["cg_iterations_total"]
+    assert it_c < 0.8 * it_j, (it_c, it_j)
+
+
+def test_two_level_is_reproducible_and_follows_set_state(gpu):
+    """Two runs from the same state give identical bits; a new state (set_state) rebuilds
+    the coarse operator, so a run after set_state equals a run of a fresh handle.  The
+    configuration is pinned (the autotuner's choice changes the summation order)."""
+    nn = gpu
+    inp = nn.synth(1, 32, seed=5)
+
+    def make():
+        s = nn.Simulation.from_synth(inp)
+        s.build_neighbours()
+        s.set_tuning(4, 8, 0)
+        return s
+
+    sims = []
+    for _ in range(2):
+        sim = make()
+        sim.forward(20, nn.MIXED)
+        sims.append(sim.state())
+    for a, b in zip(*sims):
+        assert np.array_equal(a, b)
+    sim = make()
+    sim.forward(20, nn.MIXED)
+    c, phi, ph = sim.state()
+    fresh = make()
+    fresh.set_state(c, phi, ph)
+    fresh.forward(10, nn.MIXED)
+    sim.set_state(c, phi, ph)
+    sim.forward(10, nn.MIXED)
+    for a, b in zip(sim.state(), fresh.state()):
+        assert np.array_equal(a, b)
+
+
+def test_preconditioner_rejects_bad_kind(gpu):
+    nn = gpu
+    inp = nn.synth(1, 12, seed=4)
+    sim = nn.Simulation.from_synth(inp)
+    with pytest.raises(nn.NNPPError) as e:
+        sim.set_preconditioner(2)
+    assert e.value.status == 1
+
+
 def test_warm_start_rejects_bad_history(gpu):
     nn = gpu
     inp = nn.synth(1, 12, seed=4)
