@@ -227,7 +227,8 @@ def adjoint_cost(nn, steps, ck=50, se=20):
 
 class ProfileRange:
     """cudaProfilerStart/Stop around one region of the run, for `ncu --profile-from-start off`;
-    NNPP_PROFILE=timed selects the timed steps, NNPP_PROFILE=kernels the per-kernel timings."""
+    NNPP_PROFILE=timed selects the timed steps, NNPP_PROFILE=kernels the per-kernel timings,
+    NNPP_PROFILE=variant<k> the timing of CG operator variant k."""
 
     def __init__(self, name):
         self.on = os.environ.get("NNPP_PROFILE") == name
@@ -326,7 +327,7 @@ def run_ours(args):
     ms64 = sim64.forward_timed(args.steps, nn.FP64)
     d64 = sim64.diagnostics()
     # the same run with the diagonal (Jacobi) preconditioner alone, for comparison
-    pk, cn = sim.preconditioner()
+    pk, cn, _, _ = sim.preconditioner()
     simj = nn.Simulation.from_synth(inp)
     simj.build_neighbours()
     simj.set_preconditioner(nn.PRECOND_JACOBI)
@@ -375,10 +376,12 @@ def run_ours(args):
     variants = {}
     with ProfileRange("variants"):
         for var, key in ((0, "gather8"), (1, "bulk_staged"), (2, "smem_window8"), (3, "gather16"),
-                         (4, "smem_window16")):
+                         (4, "smem_window16"), (5, "smem_window16_l2pf"), (6, "gather16_l2pf"),
+                         (7, "smem_window8_l2pf")):
             try:
                 sim.set_tuning(tuned[0], tuned[1], var)
-                variants[key] = sim.time_kernel(1, nn.MIXED, reps=50)
+                with ProfileRange("variant%d" % var):
+                    variants[key] = sim.time_kernel(1, nn.MIXED, reps=50)
             except nn.NNPPError as ex:
                 variants[key] = "unsupported: %s" % ex
     sim.set_tuning(*tuned)

@@ -221,15 +221,20 @@ nnpp_status nnpp_set_warm_start(nnpp_handle* h, int history);
 
 /* Preconditioner of the potential CG (both precisions).  NNPP_PRECOND_TWO_LEVEL (the
  * default) adds to the Jacobi scaling a coarse correction on aggregates of f x f x f hash
- * bins (at most 3000 aggregates): the Galerkin coarse operator P^T A P of the current
- * phases, inverted once per state (nnpp_set_state / nnpp_reset) on the GPU, applied as one
- * dense product per iteration.  Single-instance runs only (ensembles use Jacobi).  Only the
- * iteration count depends on it: every solve still runs to the solver tolerance.  Discards a
- * recorded forward_ckpt run.  The reference's solve of K11 is diagonally preconditioned
- * (Eigen::GMRES with DiagonalPreconditioner, main.cpp:764-766, solved at main.cpp:779). */
-nnpp_status nnpp_set_preconditioner(nnpp_handle* h, int kind);
-/* Current preconditioner and the number of coarse unknowns (0 for Jacobi). */
-nnpp_status nnpp_get_preconditioner(nnpp_handle* h, int* kind, int* coarse_unknowns);
+ * bins (at most 3000 aggregates): the Galerkin coarse operator P^T A P of the phases,
+ * inverted on the GPU and applied as one dense product per iteration.  It is rebuilt when
+ * the state is replaced (nnpp_set_state, nnpp_reset) and, when refresh_every > 0 (default
+ * 64), after every refresh_every steps counted from then if a phase has changed; backward
+ * replays the rebuilds of forward_ckpt.  Single-instance runs only (ensembles use Jacobi).
+ * Only the iteration count depends on it: every solve still runs to the solver tolerance.
+ * A change discards a recorded forward_ckpt run.  The reference's solve of K11 is
+ * diagonally preconditioned (Eigen::GMRES with DiagonalPreconditioner, main.cpp:764-766,
+ * solved at main.cpp:779). */
+nnpp_status nnpp_set_preconditioner(nnpp_handle* h, int kind, int refresh_every);
+/* Current preconditioner, its number of coarse unknowns (0 for Jacobi), refresh period and
+ * the number of coarse inverses computed so far; any pointer may be NULL. */
+nnpp_status nnpp_get_preconditioner(nnpp_handle* h, int* kind, int* coarse_unknowns, int* refresh_every,
+                                    int64_t* rebuilds);
 
 /* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
  * NULL. */
@@ -279,9 +284,11 @@ nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int r
 /* The execution configuration of the handle's kernels: bins per tile, lanes per node of the
  * FP64 tile kernels, and the FP32 CG operator's variant: 0 / 3 gathers from L1/L2 (batches
  * of 8 / 16 bond columns), 1 operator and slice windows streamed by bulk copies into shared
- * memory, 2 / 4 slice windows copied into shared memory by the warp (batches of 8 / 16).  Chosen by the autotuner on the first run (0 / -1 before);
- * nnpp_set_tuning pins a configuration instead (bins in {2,4,8,16}, lanes in {4,8,16};
- * NNPP_ERR_UNSUPPORTED when a tile halo or a slice window does not fit). */
+ * memory, 2 / 4 slice windows copied into shared memory by asynchronous copies (batches of
+ * 8 / 16), 5 / 6 / 7 the variants 4 / 3 / 2 with bulk L2 prefetches of the operator stream
+ * a few batches ahead.  Chosen by the autotuner on the first run (0 / -1 before);
+ * nnpp_set_tuning pins a configuration instead (bins in {2,4,8,16}, lanes in {4,8,16},
+ * operator 0..7; NNPP_ERR_UNSUPPORTED when a tile halo or a slice window does not fit). */
 nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node,
                             int* cg_operator);
 nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_node,

@@ -106,8 +106,8 @@ _SIGS = {
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
     "nnpp_set_warm_start": (C.c_int, [_P, C.c_int]),
-    "nnpp_set_preconditioner": (C.c_int, [_P, C.c_int]),
-    "nnpp_get_preconditioner": (C.c_int, [_P, _IP, _IP]),
+    "nnpp_set_preconditioner": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nnpp_get_preconditioner": (C.c_int, [_P, _IP, _IP, _IP, C.POINTER(C.c_int64)]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -297,16 +297,18 @@ class Simulation:
         extrapolation, 3-6 energy-norm-optimal combination of that many past potentials."""
         _check(lib().nnpp_set_warm_start(self._h, history))
 
-    def set_preconditioner(self, kind):
+    def set_preconditioner(self, kind, refresh_every=64):
         """Preconditioner of the potential CG: PRECOND_JACOBI (diagonal) or
-        PRECOND_TWO_LEVEL (diagonal + coarse correction on aggregates of hash bins)."""
-        _check(lib().nnpp_set_preconditioner(self._h, kind))
+        PRECOND_TWO_LEVEL (diagonal + coarse correction on aggregates of hash bins, rebuilt
+        every refresh_every steps when the phases changed; 0: only on set_state/reset)."""
+        _check(lib().nnpp_set_preconditioner(self._h, kind, refresh_every))
 
     def preconditioner(self):
-        """(kind, coarse unknowns) of the potential CG's preconditioner."""
-        k, n = C.c_int(), C.c_int()
-        _check(lib().nnpp_get_preconditioner(self._h, C.byref(k), C.byref(n)))
-        return k.value, n.value
+        """(kind, coarse unknowns, refresh period, coarse inverses computed so far) of the
+        potential CG's preconditioner."""
+        k, n, r, b = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        _check(lib().nnpp_get_preconditioner(self._h, C.byref(k), C.byref(n), C.byref(r), C.byref(b)))
+        return k.value, n.value, r.value, b.value
 
     def reset(self):
         """Back to the initial state of build_neighbours (lists and tuning kept)."""

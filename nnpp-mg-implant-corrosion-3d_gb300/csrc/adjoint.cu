@@ -98,6 +98,23 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
     return set_error(NNPP_ERR_UNSUPPORTED, "the adjoint needs vol_red = 0 (BV = 1 on mixed bonds)");
   NNPP_CUDA(cudaSetDevice(h.device));
   NNPP_TRY(engine_warm(*h.engine, precision));
+  // coarse inverses used along the run: the current one from step 0, then each rebuild
+  h.coarse_events.clear();
+  h.coarse_event_cur = -1;
+  h.coarse_record = false;
+  if (engine_coarse(*h.engine)) {
+    h.coarse_events.emplace_back();
+    const size_t nn = (size_t)h.coarse.n * h.coarse.n;
+    if (!h.coarse_events[0].inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
+    NNPP_CUDA(cudaMemcpyAsync(h.coarse_events[0].inv.get(), h.coarse.inv.get(), sizeof(float) * nn,
+                              cudaMemcpyDeviceToDevice, h.st));
+    h.coarse_base = h.nstep;
+    h.coarse_record = true;
+  }
+  struct RecordOff {
+    Handle& h;
+    ~RecordOff() { h.coarse_record = false; }
+  } record_off{h};
   h.fwd_steps = n_steps;
   h.ck_every = ckpt_every;
   h.sample_every = sample_every;
@@ -126,6 +143,8 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
     }
   }
   NNPP_TRY(save_ckpt(h, h.fwd_end));
+  h.fwd_nstep_end = h.nstep;
+  h.coarse_event_cur = (int)h.coarse_events.size() - 1;
   std::copy(h.curve.begin(), h.curve.end(), mass_curve);
   return NNPP_OK;
 }
@@ -167,12 +186,24 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
     NNPP_TRY(launch_adj_combine(h, mu.get(), lam.get(), -dV * dL_dmass[n_steps / se - 1]));
   }
   Engine& e = *h.engine;
+  // replay the recorded coarse inverses (no rebuilds while recomputing); afterwards the last
+  // one and the step count of the end of the forward run are back
+  h.coarse_replay = true;
+  struct ReplayOff {
+    Handle& h;
+    ~ReplayOff() {
+      coarse_select(h, h.fwd_steps);
+      h.coarse_replay = false;
+      h.nstep = h.fwd_nstep_end;
+    }
+  } replay_off{h};
   const int nseg = (int)h.ckpts.size();
   for (int g = nseg - 1; g >= 0 && st == NNPP_OK; --g) {
     const int s0 = g * ck, s1 = std::min(n_steps, s0 + ck);
     NNPP_TRY(load_ckpt(h, h.ckpts[g]));
     NNPP_TRY(launch_snap_state(h, snap.get()));
     for (int n = s0; n < s1; ++n) {
+      NNPP_TRY(coarse_select(h, n));
       NNPP_TRY(engine_run(e, 1, prec));
       NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
       NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
@@ -187,6 +218,7 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       else
         NNPP_TRY(launch_adj_transport(e, v, sn, sn1, lam.get(), mu.get(), nu.get(), acc.get(), h.st));
       // adjoint potential solve on the unknowns of step n
+      NNPP_TRY(coarse_select(h, n));
       NNPP_TRY(launch_adj_solve_setup(h, sn, psi.get()));
       h.b_override = nu.get();
       if (hm >= 3) {

@@ -165,6 +165,7 @@ nnpp_status reset_initial(Handle& h) {
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   h.fwd_steps = 0;
   h.ckpts.clear();
+  h.nstep = 0;
   if (h.engine) NNPP_TRY(engine_params(*h.engine));
   return NNPP_OK;
 }
@@ -443,6 +444,7 @@ nnpp_status nnpp_set_state(nnpp_handle* hp, const double* c, const double* phi, 
   Handle& h = hp->h;
   NNPP_TRY(upload_state(h, c, phi, phase, h.state_prec));
   h.coarse.stale = true;
+  h.nstep = 0;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   return NNPP_OK;
 }
@@ -693,14 +695,20 @@ nnpp_status nnpp_reset(nnpp_handle* hp) {
   return NNPP_OK;
 }
 
-nnpp_status nnpp_set_preconditioner(nnpp_handle* hp, int kind) {
+nnpp_status nnpp_set_preconditioner(nnpp_handle* hp, int kind, int refresh_every) {
   NNPP_GUARD(hp);
   if (kind != NNPP_PRECOND_JACOBI && kind != NNPP_PRECOND_TWO_LEVEL)
     return set_error(NNPP_ERR_INVALID, "preconditioner: 0 (Jacobi) or 1 (two-level)");
+  if (refresh_every < 0) return set_error(NNPP_ERR_INVALID, "preconditioner: refresh_every < 0");
   Handle& h = hp->h;
   NNPP_CUDA(cudaSetDevice(h.device));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   const bool want = kind == NNPP_PRECOND_TWO_LEVEL;
+  if (refresh_every != h.coarse_every) {
+    h.coarse_every = refresh_every;
+    h.fwd_steps = 0;
+    h.ckpts.clear();
+  }
   if (want == h.coarse_enabled) return NNPP_OK;
   h.coarse_enabled = want;
   h.coarse.valid = false;
@@ -714,11 +722,14 @@ nnpp_status nnpp_set_preconditioner(nnpp_handle* hp, int kind) {
   return NNPP_OK;
 }
 
-nnpp_status nnpp_get_preconditioner(nnpp_handle* hp, int* kind, int* coarse_unknowns) {
+nnpp_status nnpp_get_preconditioner(nnpp_handle* hp, int* kind, int* coarse_unknowns, int* refresh_every,
+                                    int64_t* rebuilds) {
   NNPP_GUARD(hp);
   const Handle& h = hp->h;
   if (kind) *kind = h.coarse_enabled ? NNPP_PRECOND_TWO_LEVEL : NNPP_PRECOND_JACOBI;
   if (coarse_unknowns) *coarse_unknowns = h.coarse_enabled ? h.coarse.n : 0;
+  if (refresh_every) *refresh_every = h.coarse_every;
+  if (rebuilds) *rebuilds = h.coarse.rebuilds;
   return NNPP_OK;
 }
 
@@ -758,13 +769,13 @@ nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_no
   const int T = bins_per_tile, W = lanes_per_node;
   if ((T != 2 && T != 4 && T != 8 && T != 16) || (W != 4 && W != 8 && W != 16) ||
       cg_operator < 0 || cg_operator >= kSpmvVariants)
-    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, operator 0..4");
+    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, operator 0..7");
   Handle& h = hp->h;
   Engine& e = *h.engine;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   NNPP_TRY(engine_set_tiles(e, T));
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, W));
-  if ((cg_operator == 1 || cg_operator == 2 || cg_operator == 4) && !spmv_staged_fits(e))
+  if (spmv_needs_windows(cg_operator) && !spmv_staged_fits(e))
     return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: a slice window exceeds the staged operators' capacity");
   e.W = W;
   e.spmv_variant = cg_operator;

@@ -8,7 +8,10 @@
 // iteration X <- X (2I - A_c X), X_0 = I / ||A_c||_inf (every iterate is a positive
 // polynomial of A_c, so the preconditioner stays symmetric positive definite even when the
 // iteration is stopped early), on cuBLAS SGEMM.  The coarse operator is rebuilt when the
-// phases have changed (a stale one is still a valid preconditioner).
+// state is replaced, and every `coarse_every` steps (counted from the last replacement) if a
+// phase changed since the last rebuild; in between a stale one is still a valid
+// preconditioner.  The schedule depends only on the step count and the phases, so it is
+// reproducible, and forward_ckpt records each rebuilt inverse for backward to replay.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -136,6 +139,21 @@ __global__ void k_symmetrize(int n, const float* X, float* Y) {
   }
 }
 
+// phases in internal order (1: solid) from the current records
+__global__ void k_phase_snap(KParams k, int mixed, unsigned char* snap) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.N; i += gridDim.x * blockDim.x)
+    snap[i] = node_liquid(k, i, mixed) ? 0 : 1;
+}
+
+// number of nodes whose phase differs from snap
+__global__ void k_phase_diff(KParams k, int mixed, const unsigned char* snap, int* count) {
+  int c = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.N; i += gridDim.x * blockDim.x)
+    c += (node_liquid(k, i, mixed) ? 0 : 1) != snap[i];
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
 }  // namespace
 
 Coarse::~Coarse() {
@@ -217,8 +235,50 @@ nnpp_status coarse_refresh(Handle& h) {
   }
   k_symmetrize<<<eg, 256, 0, h.st>>>(n, x, c.inv.get());
   NNPP_CUDA(cudaGetLastError());
+  if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
+  k_phase_snap<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
+      kp, h.state_prec == NNPP_MIXED ? 1 : 0, c.snap.get());
+  NNPP_CUDA(cudaGetLastError());
   c.valid = true;
   c.stale = false;
+  c.rebuilds += 1;
+  h.coarse_event_cur = -1;
+  return NNPP_OK;
+}
+
+nnpp_status coarse_check(Handle& h) {
+  Coarse& c = h.coarse;
+  if (!h.coarse_enabled || !c.valid || h.coarse_replay) return NNPP_OK;
+  KParams kp = make_kparams(h, h.cur);
+  NNPP_CUDA(cudaMemsetAsync(c.count.get(), 0, sizeof(int), h.st));
+  k_phase_diff<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
+      kp, h.state_prec == NNPP_MIXED ? 1 : 0, c.snap.get(), c.count.get());
+  NNPP_CUDA(cudaGetLastError());
+  int changed = 0;
+  NNPP_CUDA(cudaMemcpyAsync(&changed, c.count.get(), sizeof(int), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  if (changed == 0) return NNPP_OK;
+  NNPP_TRY(coarse_refresh(h));
+  if (h.coarse_record) {
+    h.coarse_events.emplace_back();
+    Handle::CoarseEvent& ev = h.coarse_events.back();
+    ev.step = h.nstep - h.coarse_base;
+    const size_t nn = (size_t)c.n * c.n;
+    if (!ev.inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
+    NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
+  }
+  return NNPP_OK;
+}
+
+nnpp_status coarse_select(Handle& h, long long step) {
+  if (h.coarse_events.empty()) return NNPP_OK;
+  int e = 0;
+  while (e + 1 < (int)h.coarse_events.size() && h.coarse_events[e + 1].step <= step) ++e;
+  if (e == h.coarse_event_cur) return NNPP_OK;
+  const size_t nn = (size_t)h.coarse.n * h.coarse.n;
+  NNPP_CUDA(cudaMemcpyAsync(h.coarse.inv.get(), h.coarse_events[e].inv.get(), sizeof(float) * nn,
+                            cudaMemcpyDeviceToDevice, h.st));
+  h.coarse_event_cur = e;
   return NNPP_OK;
 }
 

@@ -84,6 +84,9 @@ nnpp_status build_lists(Engine& e, int T) {
   e.nchunks = (int)chunks.size();
   e.nslices = (int)slices.size();
   e.windows_fit = fit;
+  int wmax = 16;
+  for (const SliceDesc& d : slices) wmax = std::max(wmax, d.wtotal);
+  e.win_cap = (wmax + 15) & ~15;
   e.halo_max = hm;
   e.bond_max = bmax;
   e.T = T;
@@ -151,7 +154,7 @@ nnpp_status tune(Engine& e, int prec) {
       const bool win = prec == NNPP_MIXED && spmv_staged_fits(e);
       const int nvar = prec == NNPP_MIXED ? kSpmvVariants : 1;
       for (int var = 0; var < nvar; ++var) {
-        if (!win && (var == 1 || var == 2 || var == 4)) continue;
+        if (!win && spmv_needs_windows(var)) continue;
         e.spmv_variant = var;
         NNPP_TRY(set_active(e, 1, 1));
         NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
@@ -390,8 +393,7 @@ nnpp_status engine_build(Engine& e) {
   return NNPP_OK;
 }
 
-nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
-  if (!prepared) NNPP_TRY(prepare_run(e, prec));
+static nnpp_status run_steps(Engine& e, int n_steps, int prec) {
   if (e.eager) {
     for (int s = 0; s < n_steps; ++s) {
       EngineView v = make_view(e, 0, 0);
@@ -414,6 +416,24 @@ nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
     NNPP_CUDA(cudaGraphLaunch(e.gexec[kGraphStep1][prec][0], e.st));
     for (Handle* h : e.members) h->cur ^= 1;
     NNPP_TRY(refresh_params(e));
+  }
+  return NNPP_OK;
+}
+
+nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
+  if (!prepared) NNPP_TRY(prepare_run(e, prec));
+  // single-instance runs with the coarse correction stop at multiples of coarse_every steps
+  // (since the state was replaced) to rebuild the coarse operator when the phases changed
+  Handle* h1 = e.members.size() == 1 ? e.members[0] : nullptr;
+  const long long R = (h1 && engine_coarse(e) && !h1->coarse_replay) ? h1->coarse_every : 0;
+  int done = 0;
+  while (done < n_steps) {
+    int seg = n_steps - done;
+    if (R > 0) seg = (int)std::min<long long>(seg, R - h1->nstep % R);
+    NNPP_TRY(run_steps(e, seg, prec));
+    for (Handle* h : e.members) h->nstep += seg;
+    done += seg;
+    if (R > 0 && h1->nstep % R == 0) NNPP_TRY(coarse_check(*h1));
   }
   if (e.members.size() > 1 || e.members[0]->st != e.st) NNPP_CUDA(cudaStreamSynchronize(e.st));
   return NNPP_OK;

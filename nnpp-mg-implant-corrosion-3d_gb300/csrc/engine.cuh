@@ -49,7 +49,12 @@ struct SliceDesc {
   int lo[9];
   int woff[9];
   int wlen[9];
-  int pad2;
+  // gather base of window row r: a bond's neighbour is gbase[code >> 12] + (code & 4095).
+  // When the window fits 4096 nodes the 12-bit part is the neighbour's position in the
+  // window (woff[r] + node - lo[r]) and gbase[r] = lo[r] - woff[r]; otherwise it is
+  // node - lo[r] and gbase[r] = lo[r].
+  int gbase[9];
+  int pad2[4];
 };
 
 // What every batched kernel receives.
@@ -74,7 +79,7 @@ struct EngineView {
 };
 
 constexpr int kChunk = 1024;  // nodes per elementwise work item
-constexpr int kSpmvVariants = 5;  // FP32 CG operator variants the autotuner times
+constexpr int kSpmvVariants = 8;  // FP32 CG operator variants the autotuner times
 
 struct Engine {
   std::vector<Handle*> members;
@@ -83,8 +88,10 @@ struct Engine {
   bool tuned = false;
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
   int spmv_variant = 0;     // FP32 CG operator: 0, 3 L1/L2 gathers (batches of 8, 16),
-                            // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16)
+                            // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16),
+                            // 5, 6, 7: 4, 3, 2 with L2 prefetch of the operator stream
   bool windows_fit = false; // every slice window fits kWinCap (the staged operator runs)
+  int win_cap = 0;          // largest slice window (nodes, multiple of 16)
   int grid = 0;
   int sms = 152;
   int halo_max = 0;
@@ -123,6 +130,10 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
 // step.cu launchers (batched)
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 bool spmv_staged_fits(const Engine& e);
+// the variant gathers from per-slice shared-memory windows (needs spmv_staged_fits)
+inline bool spmv_needs_windows(int variant) {
+  return variant == 1 || variant == 2 || variant == 4 || variant == 5 || variant == 7;
+}
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out);
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,

@@ -86,10 +86,12 @@ struct Coarse {
   DBuf<float> rc, xc; // n: restricted residual, coarse correction
   DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
   DBuf<float> a, t, x; // n x n: A_c and the Newton-Schulz work matrices
+  DBuf<unsigned char> snap;  // N: phases (internal order) the inverse was computed from
+  DBuf<int> count;           // phase changes since (coarse_check)
   void* cublas = nullptr;
   bool valid = false; // inv holds an inverse
   bool stale = true;  // the phases changed since inv was computed
-  long long solid_at = -1;
+  long long rebuilds = 0;  // inverses computed since the handle was built
   ~Coarse();
 };
 
@@ -143,6 +145,19 @@ struct Handle {
   int warm_hist = kHistMax;     // history length of the warm start (0: extrapolation only)
   bool coarse_enabled = true;   // two-level preconditioner (single-instance runs)
   Coarse coarse;
+  int coarse_every = 64;        // check for phase changes every that many steps (0: never)
+  long long nstep = 0;          // steps since the state was last replaced (refresh schedule)
+  // refreshes during forward_ckpt (step relative to its start, the inverse from then on),
+  // replayed by backward so that recomputed steps and adjoint solves see the same operator
+  struct CoarseEvent {
+    long long step = 0;
+    DBuf<float> inv;
+  };
+  std::vector<CoarseEvent> coarse_events;
+  bool coarse_record = false, coarse_replay = false;
+  long long coarse_base = 0;    // nstep at the start of forward_ckpt
+  long long fwd_nstep_end = 0;  // nstep at its end
+  int coarse_event_cur = -1;    // event whose inverse coarse.inv holds during replay
   DBuf<double> xh, bh;          // warm-start history, warm_hist * N each
   double* warm_x_alt = nullptr; // another ring in place of xh, bh (the adjoint's solves)
   double* warm_b_alt = nullptr;
@@ -170,6 +185,11 @@ struct Handle {
 // coarse.cu
 nnpp_status coarse_build(Handle& h);
 nnpp_status coarse_refresh(Handle& h);
+// at a refresh point: recompute the inverse if a phase changed since the last refresh
+nnpp_status coarse_check(Handle& h);
+// during backward: put the inverse of the last recorded refresh at or before `step`
+// (relative to the start of forward_ckpt) into coarse.inv
+nnpp_status coarse_select(Handle& h, long long step);
 
 // step.cu
 nnpp_status step_alloc(Handle& h);

@@ -112,11 +112,23 @@ __device__ __forceinline__ void instance_finished(const EngineView& v, int inst,
 template <int NV>
 __device__ __forceinline__ void reduce_items(const double* partials, int stride, int first, int count,
                                              double (&out)[NV], double* sm) {
+  // eight independent accumulators per thread (loads in flight together), combined in a
+  // fixed order: the sum does not depend on timing
+  constexpr int U = 8;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double x = 0.0;
-    for (int b = threadIdx.x; b < count; b += kBlock) x += partials[(size_t)k * stride + first + b];
-    out[k] = x;
+    const double* p = partials + (size_t)k * stride + first;
+    double x[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) x[u] = 0.0;
+    int b = threadIdx.x;
+    for (; b + (U - 1) * kBlock < count; b += U * kBlock)
+#pragma unroll
+      for (int u = 0; u < U; ++u) x[u] += p[b + u * kBlock];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (b + u * kBlock < count) x[u] += p[b + u * kBlock];
+    out[k] = ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
   }
   block_sum<NV, kBlock>(out, sm);
 }
@@ -477,6 +489,18 @@ __device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
 }
 
 // node of a slot code: window row start (per-warp table of the slice's lo[]) + offset
+// streamed operator loads that bypass L1 allocation (L1 stays with the gathered vectors)
+__device__ __forceinline__ float ld_stream(const float* p) {
+  float v;
+  asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ unsigned int ld_stream(const unsigned short* p) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(v) : "l"(p));
+  return v;
+}
+
 __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
   return hb[code >> 12] + (int)(code & 4095u);
 }
@@ -485,9 +509,12 @@ __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
 // FP32, sliced operator: each warp streams 32-row slices (slot codes and weights
 // column-major: one coalesced load per bond column), one lane per row.  WIN: the warp first
 // copies the slice's window (the z values of its 9 window rows) into its shared-memory
-// buffer with coalesced loads and gathers from there; otherwise it gathers from L1/L2.
+// buffer with asynchronous 16-byte copies and gathers from there (the code's low 12 bits
+// are the position in the window); otherwise it gathers from L1/L2.  PF > 0: lane 0 keeps
+// bulk L2 prefetches of the warp's operator stream PF batches ahead of the batch being read
+// (the warp's slices are contiguous in the sliced array), so that the batch loads hit L2.
 // Slice partials are reduced per instance by the last CTA.
-template <int W, bool WIN, int B, bool PIPE, int MINB>
+template <int W, bool WIN, int B, bool PIPE, int MINB, int PF = 0>
 __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   extern __shared__ __align__(16) float zwin[];
   __shared__ int s_hb[kBlock / 32][12];
@@ -497,26 +524,56 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   int s0, s1;
   warp_slices(v, &s0, &s1);
   float* zw = zwin + (WIN ? (size_t)warp * kWinCap : 0);
+  // prefetch window of the operator stream: [pf_next, pf_end) of the warp's byte range
+  const char* pf_next = nullptr;
+  const char* pf_end = nullptr;
+  if (PF > 0 && s0 < s1) {
+    const SliceDesc& da = v.slices[s0];
+    const SliceDesc& db = v.slices[s1 - 1];
+    pf_next = reinterpret_cast<const char*>(sell_w(v.inst[da.inst], da));
+    pf_end = reinterpret_cast<const char*>(sell_w(v.inst[db.inst], db)) + (size_t)db.width * kSellW * 4;
+    if (da.inst != db.inst) pf_end = pf_next;  // the range spans instances: no prefetch
+    if (lane == 0) {
+      const char* stop = pf_next + (size_t)PF * B * kSellW * 4;
+      if (stop > pf_end) stop = pf_end;
+      for (; pf_next < stop; pf_next += B * kSellW * 4)
+        bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
+    }
+  }
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
     if (slice_active(v, sg)) {
       if (WIN) {
+        // the window (z of the 9 window rows, 16-byte aligned row segments) by 16-byte
+        // cp.async, all copies in flight before the one wait
         const SliceDesc& dg = v.slices[sg];
-        if (lane < 9) s_hb[warp][lane] = dg.woff[lane];
         const float* zg = k.z32;
-#pragma unroll
+#pragma unroll 1
         for (int r = 0; r < 9; ++r) {
           const int n = dg.wlen[r], lo = dg.lo[r], wo = dg.woff[r];
-          for (int i = lane; i < n; i += 32) zw[wo + i] = __ldg(zg + lo + i);
+          for (int i = 4 * lane; i < n; i += 128)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(zw + wo + i)), "l"(zg + lo + i)
+                         : "memory");
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
       } else if (lane < 9) {
-        s_hb[warp][lane] = v.slices[sg].lo[lane];
+        s_hb[warp][lane] = v.slices[sg].gbase[lane];
       }
       __syncwarp();
       const int a = d.row0 + lane;
-      if (lane < d.nrows && k.freem[a]) {
+      const bool live = lane < d.nrows && k.freem[a];
+      if (PF > 0 && lane == 0) {
+        // keep the prefetches at least PF batches ahead of this slice's first column
+        const char* target = reinterpret_cast<const char*>(sell_w(k, d)) + (size_t)PF * B * kSellW * 4;
+        if (target > pf_end) target = pf_end;
+        for (; pf_next < target; pf_next += B * kSellW * 4)
+          bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
+      }
+      // every lane of a slice with a live row runs the bond loop (padding columns and rows
+      // hold code 0, weight 0), so that lane 0 can issue the prefetches
+      if (PF > 0 ? __any_sync(0xffffffffu, live) : live) {
         const int* hb = s_hb[warp];
         const float* ws = sell_w(k, d) + lane;
         const unsigned short* cs = sell_code(k, d) + lane;
@@ -530,21 +587,25 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
         if (PIPE && nb > 0) {
 #pragma unroll
           for (int u = 0; u < B; ++u) {
-            w[u] = __ldcs(ws + kSellW * u);
-            code[u] = __ldcs(cs + kSellC * u);
+            w[u] = ld_stream(ws + kSellW * u);
+            code[u] = ld_stream(cs + kSellC * u);
           }
         }
         for (int b = 0; b < nb; ++b) {
+          if (PF > 0 && lane == 0 && pf_next < pf_end) {
+            bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
+            pf_next += B * kSellW * 4;
+          }
           if (!PIPE) {
 #pragma unroll
             for (int u = 0; u < B; ++u) {
-              w[u] = __ldcs(ws + kSellW * (b * B + u));
-              code[u] = __ldcs(cs + kSellC * (b * B + u));
+              w[u] = ld_stream(ws + kSellW * (b * B + u));
+              code[u] = ld_stream(cs + kSellC * (b * B + u));
             }
           }
           float zv[B];
 #pragma unroll
-          for (int u = 0; u < B; ++u) zv[u] = WIN ? zw[code_node(hb, code[u])] : __ldg(z + code_node(hb, code[u]));
+          for (int u = 0; u < B; ++u) zv[u] = WIN ? zw[code[u] & 4095u] : __ldg(z + code_node(hb, code[u]));
           float wc[B];
 #pragma unroll
           for (int u = 0; u < B; ++u) wc[u] = w[u];
@@ -552,25 +613,27 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
             const int c1 = (b + 1) * B;
 #pragma unroll
             for (int u = 0; u < B; ++u) {
-              w[u] = __ldcs(ws + kSellW * (c1 + u));
-              code[u] = __ldcs(cs + kSellC * (c1 + u));
+              w[u] = ld_stream(ws + kSellW * (c1 + u));
+              code[u] = ld_stream(cs + kSellC * (c1 + u));
             }
           }
 #pragma unroll
           for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
         for (int c = nb * B; c < d.width; ++c) {
-          const int q = code_node(hb, __ldcs(cs + kSellC * c));
-          acc[0] = fmaf(__ldcs(ws + kSellW * c), WIN ? zw[q] : __ldg(z + q), acc[0]);
+          const unsigned int cc = ld_stream(cs + kSellC * c);
+          acc[0] = fmaf(ld_stream(ws + kSellW * c), WIN ? zw[cc & 4095u] : __ldg(z + code_node(hb, cc)), acc[0]);
         }
-        const float za = z[a];
-        const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
-        const float beta = (float)k.ds->beta;
-        const float qn = sa + beta * k.q32[a];
-        const float pn = za + beta * k.p32[a];
-        k.q32[a] = qn;
-        k.p32[a] = pn;
-        part = (double)pn * (double)qn;
+        if (live) {
+          const float za = z[a];
+          const float sa = k.d32[a] * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+          const float beta = (float)k.ds->beta;
+          const float qn = sa + beta * k.q32[a];
+          const float pn = za + beta * k.p32[a];
+          k.q32[a] = qn;
+          k.p32[a] = pn;
+          part = (double)pn * (double)qn;
+        }
       }
       __syncwarp();
     }
@@ -671,7 +734,6 @@ __device__ __forceinline__ void win_copy(const EngineView& v, int* ws, int s1, f
 template <int W>
 __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ int s_woff[kBlock / 32][12];
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -702,7 +764,6 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
       // the next slice's window goes to the other buffer (free: its slice is done), then
       // this slice's window (the older commit group) is waited for
       win_copy(v, &wsrc, s1, mywin + (wb ^ 1) * kWinCap, lane);
-      if (lane < 9) s_woff[warp][lane] = d.woff[lane];
       const int width = d.width;
       const int a = d.row0 + lane;
       const bool live = lane < d.nrows && k.freem[a];
@@ -716,7 +777,6 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
       asm volatile("cp.async.wait_group 1;" ::: "memory");
       __syncwarp();
       const float* zw = mywin + wb * kWinCap;
-      const int* wo = s_woff[warp];
       float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
       const int nch = tma_chunks(width);
       for (int ch = 0; ch < nch; ++ch) {
@@ -730,12 +790,12 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
 #pragma unroll 8
           for (int c = 0; c < kTmaCol; ++c) {
             const unsigned q = sc[kSellC * c];
-            acc[c & 3] = fmaf(sw[kSellW * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
+            acc[c & 3] = fmaf(sw[kSellW * c], zw[q & 4095u], acc[c & 3]);
           }
         } else {
           for (int c = 0; c < cc; ++c) {
             const unsigned q = sc[kSellC * c];
-            acc[c & 3] = fmaf(sw[kSellW * c], zw[wo[q >> 12] + (int)(q & 4095u)], acc[c & 3]);
+            acc[c & 3] = fmaf(sw[kSellW * c], zw[q & 4095u], acc[c & 3]);
           }
         }
         __syncwarp();
@@ -769,6 +829,189 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
       }
     }
     if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
+// Streamed FP32 CG operator for single-instance engines (the same product and work split as
+// k_cg_spmv32).  A warp's slices are consecutive in the sliced array, so its whole share of
+// the operator is one contiguous byte range: lane 0 streams it through a ring of `stages`
+// shared-memory stages of kTmaCol bond columns with cp.async.bulk (completed on mbarriers,
+// refilled as soon as a stage is consumed), independently of the slice boundaries.  The
+// lanes consume the columns slice by slice and gather from double-buffered slice windows.
+// Nothing on a slice's path waits on a dependent global load: the slice descriptors arrive
+// by cp.async three slices ahead into a shared-memory ring of four, and each slice's window
+// one slice ahead (one cp.async group per slice: the window of slice s + 1 and the
+// descriptor of slice s + 3).
+// Dynamic shared memory: ring [warps][stages][kStageBytes], windows [warps][2][win_cap]
+// floats, barriers [warps][stages], descriptors [warps][4].  Waits are bounded (timeout
+// recorded in the state).
+constexpr int kDescRing = 4;
+
+// lanes 0..11: 16-byte cp.async copies of slice sg's descriptor into dst (no-op past s1)
+__device__ __forceinline__ void desc_copy(const EngineView& v, int sg, int s1, SliceDesc* dst, int lane) {
+  static_assert(sizeof(SliceDesc) % 16 == 0, "slice descriptor copied in 16-byte pieces");
+  if (sg < s1 && lane < (int)(sizeof(SliceDesc) / 16))
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(reinterpret_cast<char*>(dst) + 16 * lane)),
+                 "l"(reinterpret_cast<const char*>(v.slices + sg) + 16 * lane)
+                 : "memory");
+}
+
+// all lanes: 16-byte cp.async copies of the window of the slice described by d into zw
+__device__ __forceinline__ void win_copy_desc(const SliceDesc& d, const float* z, float* zw, int lane) {
+#pragma unroll 1
+  for (int r = 0; r < 9; ++r) {
+    const int n = d.wlen[r], lo = d.lo[r], wo = d.woff[r];
+    for (int i = 4 * lane; i < n; i += 128)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(zw + wo + i)), "l"(z + lo + i)
+                   : "memory");
+  }
+}
+
+template <int W, int COL>
+__global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32s(EngineView v, int stages, int win_cap) {
+  constexpr int SB = COL * kSellW * 4;  // bytes of a stage
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ double sm[kBlock / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t ring_bytes = (size_t)kWarpsCta * stages * SB;
+  const size_t win_bytes = (size_t)kWarpsCta * 2 * win_cap * sizeof(float);
+  unsigned char* ring = dsm;
+  float* wins = reinterpret_cast<float*>(dsm + ring_bytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dsm + ring_bytes + win_bytes);
+  SliceDesc* descs = reinterpret_cast<SliceDesc*>(dsm + ring_bytes + win_bytes +
+                                                  (size_t)kWarpsCta * stages * sizeof(uint64_t));
+  if (threadIdx.x < kWarpsCta * stages) mbar_init(bars + threadIdx.x, 1);
+  fence_mbar_init();
+  __syncthreads();
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  const KParams& k = v.inst[0];
+  int timed_out = 0;
+  if (s0 < s1 && slice_active(v, s0)) {
+    const SliceDesc& da = v.slices[s0];
+    const SliceDesc& db = v.slices[s1 - 1];
+    const char* base = reinterpret_cast<const char*>(sell_w(k, da));
+    const size_t total = ((size_t)((db.off - da.off) >> 5) + (size_t)db.width) * kSellW * 4;
+    const uint64_t pol = l2_evict_first_policy();  // the operator is read once per launch
+    unsigned char* myring = ring + (size_t)warp * stages * SB;
+    uint64_t* mybars = bars + warp * stages;
+    SliceDesc* mydesc = descs + warp * kDescRing;
+    size_t pos = 0;  // lane 0: bytes of the range issued so far
+    if (lane == 0)
+      for (int st = 0; st < stages && pos < total; ++st) {
+        const unsigned bytes = (unsigned)min((size_t)SB, total - pos);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(mybars + st, bytes);
+        bulk_g2s_hint(myring + (size_t)st * SB, base + pos, bytes, mybars + st, pol);
+        pos += bytes;
+      }
+    const float* zg = k.z32;
+    float* mywin = wins + (size_t)warp * 2 * win_cap;
+    // descriptors of s0 and s0 + 1 now; then the window of s0 with the descriptor of s0 + 2
+    desc_copy(v, s0, s1, mydesc, lane);
+    desc_copy(v, s0 + 1, s1, mydesc + 1, lane);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncwarp();
+    win_copy_desc(mydesc[0], zg, mywin, lane);
+    desc_copy(v, s0 + 2, s1, mydesc + 2, lane);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    int stage = 0, wb = 0;
+    unsigned phases = 0u;
+    bool ready = false;
+    int cis = 0;  // column within the current stage
+    for (int sg = s0; sg < s1; ++sg) {
+      const int j = sg - s0;
+      // this slice's window and the descriptors up to sg + 2 are in
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncwarp();
+      const SliceDesc& d = mydesc[j & (kDescRing - 1)];
+      if (sg + 1 < s1) win_copy_desc(mydesc[(j + 1) & (kDescRing - 1)], zg, mywin + (wb ^ 1) * win_cap, lane);
+      desc_copy(v, sg + 3, s1, mydesc + ((j + 3) & (kDescRing - 1)), lane);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      const int width = d.width;
+      const int a = d.row0 + lane;
+      const bool row = lane < d.nrows;
+      bool live = false;
+      float za = 0.0f, dd = 0.0f, qa = 0.0f, pa = 0.0f;
+      if (row) {
+        live = k.freem[a] != 0;
+        za = k.z32[a];
+        dd = k.d32[a];
+        qa = k.q32[a];
+        pa = k.p32[a];
+      }
+      const float* zw = mywin + wb * win_cap;
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      int c = 0;
+      while (c < width) {
+        if (!ready) {
+          if (!mbar_wait_bounded(mybars + stage, (phases >> stage) & 1u, kWaitPolls)) timed_out = 1;
+          phases ^= 1u << stage;
+          ready = true;
+        }
+        const float* sw = reinterpret_cast<const float*>(myring + (size_t)stage * SB) + lane;
+        const unsigned short* sc = reinterpret_cast<const unsigned short*>(sw - lane + 32) + lane;
+        const int n = min(COL - cis, width - c);
+        if (n == COL) {
+#pragma unroll 8
+          for (int q = 0; q < COL; ++q) {
+            const unsigned code = sc[kSellC * q];
+            acc[q & 3] = fmaf(sw[kSellW * q], zw[code & 4095u], acc[q & 3]);
+          }
+        } else {
+          for (int q = cis; q < cis + n; ++q) {
+            const unsigned code = sc[kSellC * q];
+            acc[q & 3] = fmaf(sw[kSellW * q], zw[code & 4095u], acc[q & 3]);
+          }
+        }
+        c += n;
+        cis += n;
+        if (cis == COL) {
+          // stage consumed: refill it with the range's next chunk
+          __syncwarp();
+          if (lane == 0 && pos < total) {
+            const unsigned bytes = (unsigned)min((size_t)SB, total - pos);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(mybars + stage, bytes);
+            bulk_g2s_hint(myring + (size_t)stage * SB, base + pos, bytes, mybars + stage, pol);
+            pos += bytes;
+          }
+          stage = stage + 1 == stages ? 0 : stage + 1;
+          ready = false;
+          cis = 0;
+        }
+      }
+      double part = 0.0;
+      if (live) {
+        const float sa = dd * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+        const float beta = (float)k.ds->beta;
+        const float qn = sa + beta * qa;
+        const float pn = za + beta * pa;
+        k.q32[a] = qn;
+        k.p32[a] = pn;
+        part = (double)pn * (double)qn;
+      }
+      __syncwarp();
+      wb ^= 1;
+      part = warp_sum_d(part);
+      if (lane == 0) v.partials[sg] = part;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else {
+    for (int sg = s0; sg < s1; ++sg)
+      if (lane == 0) v.partials[sg] = 0.0;
+  }
+  if (timed_out && lane == 0) k.ds->wait_timeout = 1;
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    double tot[1];
+    reduce_items<1>(v.partials, v.stride, v.slice_first[0], v.slice_count[0], tot, sm);
+    if (threadIdx.x == 0) {
+      DevState* ds = k.ds;
+      if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+      v.ticket[v.M + 1] = 0;
+    }
   }
 }
 
@@ -1357,7 +1600,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
+    if (lane < 9) s_hb[warp][lane] = v.slices[sg].gbase[lane];
     __syncwarp();
     float ph_hi[6], ph_lo[6];  // masses[4], solid volume sum, dissolved (FP32 pairs)
 #pragma unroll
@@ -1820,6 +2063,19 @@ size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
 size_t smem_spmv_staged() { return kTmaRingBytes + kTmaWinBytes + kTmaBarBytes; }
+// streamed operator: the deepest ring (2..4 stages) that fits beside windows of win_cap nodes
+constexpr size_t kSmemCta = 225 * 1024;
+// stages of kStreamCol columns (2 .. kStreamMaxStages)
+constexpr int kStreamCol = 32;
+constexpr int kStreamMaxStages = 4;
+size_t smem_spmv_stream(int win_cap, int* stages) {
+  const size_t win = (size_t)kWarpsCta * 2 * win_cap * sizeof(float) + (size_t)kWarpsCta * kDescRing * sizeof(SliceDesc);
+  const size_t sb = (size_t)kStreamCol * kSellW * 4 + sizeof(uint64_t);
+  int st = kStreamMaxStages;
+  while (st > 2 && (size_t)kWarpsCta * st * sb + win > kSmemCta) --st;
+  *stages = st;
+  return (size_t)kWarpsCta * st * sb + win;
+}
 size_t smem_spmv_win() { return (size_t)(kBlock / 32) * kWinCap * sizeof(float); }
 size_t smem_tr64(int H, int B) { return (size_t)H * 6 * sizeof(double) + smem_slots(B); }
 size_t smem_adj(int H, int B) { return align16((size_t)H * (9 * sizeof(double) + 1)) + smem_slots(B) + 16; }
@@ -2010,7 +2266,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, con
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    if (lane < 9) s_hb[warp][lane] = v.slices[sg].lo[lane];
+    if (lane < 9) s_hb[warp][lane] = v.slices[sg].gbase[lane];
     __syncwarp();
     float gh[5], gl[5];  // dL/dD_k (4), dL/dk as FP32 pairs
 #pragma unroll
@@ -2248,8 +2504,11 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     NNPP_TRY(allow_smem(k_prep<double, W>, smem_prep(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv64<W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_cg_spmv32t<W>, smem_spmv_staged()));
+    NNPP_TRY(allow_smem(k_cg_spmv32s<W, kStreamCol>, kSmemCta));
     NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 8, true, 3>, smem_spmv_win()));
     NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 16, false, 3>, smem_spmv_win()));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 16, false, 3, 3>, smem_spmv_win()));
+    NNPP_TRY(allow_smem(k_cg_spmv32<W, true, 8, true, 3, 4>, smem_spmv_win()));
     NNPP_TRY(allow_smem(k_ir_update<float, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_ir_update<double, W>, smem_vec64(H, B)));
     NNPP_TRY(allow_smem(k_transport64<W, false>, smem_tr64(H, B)));
@@ -2258,10 +2517,10 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
   });
 }
 
-// FP32 CG operator variants without bulk copies (the autotuner's list): 0 L1/L2 gathers in
-// batches of 8, 32 registers (64 warps per SM); 2 shared-memory windows, pipelined batches of
-// 8; 3 L1/L2 gathers in batches of 16 (40 warps per SM); 4 shared-memory windows, batches
-// of 16
+// FP32 CG operator variants without the staged ring (the autotuner's list): 0 L1/L2 gathers
+// in batches of 8, 32 registers (64 warps per SM); 2 shared-memory windows, pipelined batches
+// of 8; 3 L1/L2 gathers in batches of 16 (40 warps per SM); 4 shared-memory windows, batches
+// of 16; 5, 6, 7: 4, 3, 2 with bulk L2 prefetches of the operator stream 3, 3, 4 batches ahead
 template <int W>
 void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t st) {
   const int items = (v.nslices + 7) / 8;
@@ -2277,6 +2536,19 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
     case 4: {
       const size_t sh = smem_spmv_win();
       k_cg_spmv32<W, true, 16, false, 3><<<occ_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      break;
+    }
+    case 5: {
+      const size_t sh = smem_spmv_win();
+      k_cg_spmv32<W, true, 16, false, 3, 3><<<occ_grid(k_cg_spmv32<W, true, 16, false, 3, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      break;
+    }
+    case 6:
+      k_cg_spmv32<W, false, 16, false, 5, 3><<<occ_grid(k_cg_spmv32<W, false, 16, false, 5, 3>, 0, sms, items), kBlock, 0, st>>>(v);
+      break;
+    case 7: {
+      const size_t sh = smem_spmv_win();
+      k_cg_spmv32<W, true, 8, true, 3, 4><<<occ_grid(k_cg_spmv32<W, true, 8, true, 3, 4>, sh, sms, items), kBlock, sh, st>>>(v);
       break;
     }
     default:
@@ -2345,7 +2617,12 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      if (e.spmv_variant == 1) {
+      if (e.spmv_variant == 1 && e.members.size() == 1) {
+        int stages = 2;
+        const size_t sh = smem_spmv_stream(e.win_cap, &stages);
+        k_cg_spmv32s<W, kStreamCol><<<occ_grid(k_cg_spmv32s<W, kStreamCol>, sh, e.sms, (v.nslices + 7) / 8), kBlock, sh, st>>>(
+            v, stages, e.win_cap);
+      } else if (e.spmv_variant == 1) {
         const size_t sh = smem_spmv_staged();
         k_cg_spmv32t<W><<<occ_grid(k_cg_spmv32t<W>, sh, e.sms, (v.nslices + 7) / 8), kBlock, sh, st>>>(v);
       } else {

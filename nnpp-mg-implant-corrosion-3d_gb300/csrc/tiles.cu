@@ -143,7 +143,7 @@ __global__ void k_slice_windows(int nslices, const SliceDesc* sl, const int* pre
 }
 
 // warp per slice: bond c of lane l (row row0 + l): its FP32 weight at float 48 (off/32 + c)
-// + l of the interleaved array, its code (window row << 12 | node - lo[row]) at 16-bit
+// + l of the interleaved array, its code (window row << 12 | node - gbase[row]) at 16-bit
 // element 96 (off/32 + c) + 64 + l; padding: code 0, weight 0
 __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb, const int* row,
                             const unsigned short* slot, const float* w32, float* sell) {
@@ -163,7 +163,7 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
       if (c < len) {
         int r, node;
         slot_node(slot[j0 + c], pre, hb, &r, &node);
-        code = (unsigned short)((r << 12) | (node - d.lo[r]));
+        code = (unsigned short)((r << 12) | (node - d.gbase[r]));
         w = w32[j0 + c];
       }
       col[lane] = w;
@@ -241,8 +241,9 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
           d.nrows = std::min(32, o1 - r0);
           d.off = (int)soff;
           d.width = 0;
-          d.wtotal = d.pad = d.pad2 = 0;
-          for (int r = 0; r < 9; ++r) d.lo[r] = d.woff[r] = d.wlen[r] = 0;
+          d.wtotal = d.pad = 0;
+          for (int q = 0; q < 4; ++q) d.pad2[q] = 0;
+          for (int r = 0; r < 9; ++r) d.lo[r] = d.woff[r] = d.wlen[r] = d.gbase[r] = 0;
           for (int l = 0; l < d.nrows; ++l) d.width = std::max(d.width, rows[r0 + l + 1] - rows[r0 + l]);
           slices.push_back(d);
           int acc = 0;
@@ -296,6 +297,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
         acc += d.wlen[r];
       }
       d.wtotal = acc;
+      for (int r = 0; r < 9; ++r) d.gbase[r] = acc <= 4096 ? d.lo[r] - d.woff[r] : d.lo[r];
       fit = fit && acc <= kWinCap;
     }
     NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));

@@ -58,6 +58,12 @@ __device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, unsign
       : "memory");
 }
 
+// asynchronous prefetch of `bytes` (multiple of 16) from a 16-byte aligned global address
+// into L2; no destination, no completion to wait for
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(

@@ -113,6 +113,34 @@ def test_checkpoint_interval_does_not_change_result(gpu, case):
         assert gk == out[0][2]
 
 
+def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
+    """The implant dissolves between steps 35 and 40 (k_diss = 0.1), so the coarse operator of
+    the two-level preconditioner is rebuilt during the forward run (refresh period 4);
+    backward replays the recorded inverses, and the gradients stay independent of the
+    checkpoint interval, and equal to a run that never rebuilds to the solver tolerance."""
+    inp, _ = case
+    p = _params(inp, 1.0, 0.1)
+    target = np.zeros(N_STEPS // SE)
+    out = []
+    for every, ck in ((4, 7), (4, 25), (4, 60), (0, 25)):
+        sim = _sim(gpu, inp, p)
+        sim.set_preconditioner(gpu.PRECOND_TWO_LEVEL, every)
+        curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
+        built = sim.preconditioner()[3]
+        assert built >= 2 if every else built == 1
+        gD, gk = sim.backward(2.0 * (curve - target))
+        assert sim.preconditioner()[3] == built
+        out.append((curve, gD, gk))
+    for curve, gD, gk in out[1:3]:
+        assert np.array_equal(curve, out[0][0])
+        assert np.array_equal(gD, out[0][1])
+        assert gk == out[0][2]
+    curve, gD, gk = out[3]
+    assert np.allclose(curve, out[0][0], rtol=1e-9, atol=0)
+    assert np.allclose(gD, out[0][1], rtol=1e-6, atol=1e-12 * np.abs(out[0][1]).max())
+    assert abs(gk - out[0][2]) <= 1e-6 * abs(out[0][2])
+
+
 def test_backward_restores_end_state(gpu, case):
     inp, target = case
     sim = _sim(gpu, inp, _params(inp))

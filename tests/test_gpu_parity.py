@@ -337,8 +337,8 @@ def test_preconditioners_agree_and_two_level_saves_iterations(gpu, orc, prec, n)
         sim = nn.Simulation.from_synth(inp)
         sim.build_neighbours()
         sim.set_preconditioner(kind)
-        k, cn = sim.preconditioner()
-        assert k == kind and (cn > 0) == (kind == nn.PRECOND_TWO_LEVEL)
+        k, cn, every, _ = sim.preconditioner()
+        assert k == kind and (cn > 0) == (kind == nn.PRECOND_TWO_LEVEL) and every == 64
         sim.forward(30, prec)
         out[kind] = (sim.state(), sim.diagnostics(), cn)
     tol = 1e-9 if prec == nn.FP64 else 1e-5
@@ -388,9 +388,45 @@ def test_preconditioner_rejects_bad_kind(gpu):
     nn = gpu
     inp = nn.synth(1, 12, seed=4)
     sim = nn.Simulation.from_synth(inp)
-    with pytest.raises(nn.NNPPError) as e:
-        sim.set_preconditioner(2)
-    assert e.value.status == 1
+    for bad in ((2, 64), (1, -1)):
+        with pytest.raises(nn.NNPPError) as e:
+            sim.set_preconditioner(*bad)
+        assert e.value.status == 1
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_coarse_rebuild_follows_dissolution(gpu, orc, prec):
+    """The implant dissolves between steps 35 and 40 (k_diss = 0.1): with a refresh period of
+    4 steps the coarse operator is rebuilt after the flip; with period 0 it keeps the initial
+    phases.  Both runs and a Jacobi run reach the oracle's state."""
+    nn = gpu
+    inp = nn.synth(1, 12, 5)
+    p = inp["params"].copy()
+    p.switch_width = 0.01
+    p.k_diss = 0.1
+    args = (p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    o = orc.Oracle(*args)
+    o.build_neighbours()
+    o.set_solver(1e-13)
+    o.forward(60)
+    c_o, phi_o, ph_o, _ = o.state()
+    assert (ph_o != inp["phase0"]).sum() > 0
+    tol = 1e-9 if prec == nn.FP64 else 1e-5
+    rebuilds = {}
+    for kind, every in ((nn.PRECOND_TWO_LEVEL, 4), (nn.PRECOND_TWO_LEVEL, 0), (nn.PRECOND_JACOBI, 4)):
+        sim = nn.Simulation(*args)
+        sim.build_neighbours()
+        sim.set_preconditioner(kind, every)
+        sim.forward(60, prec)
+        c, phi, ph = sim.state()
+        assert np.array_equal(ph, ph_o)
+        assert np.linalg.norm(c - c_o) <= tol * np.linalg.norm(c_o)
+        assert np.linalg.norm(phi - phi_o) <= tol * np.linalg.norm(phi_o)
+        assert sim.diagnostics()["cg_not_converged"] == 0
+        rebuilds[(kind, every)] = sim.preconditioner()[3]
+    assert rebuilds[(nn.PRECOND_TWO_LEVEL, 0)] == 1
+    assert rebuilds[(nn.PRECOND_TWO_LEVEL, 4)] >= 2
+    assert rebuilds[(nn.PRECOND_JACOBI, 4)] == 0
 
 
 def test_warm_start_rejects_bad_history(gpu):
@@ -402,10 +438,11 @@ def test_warm_start_rejects_bad_history(gpu):
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_cg_operator_variants_vs_oracle(gpu, orc, variant):
-    """Every FP32 CG operator (L1/L2 gathers; bulk-copy staged; shared-memory windows)
-    reaches the oracle's state to the mixed-precision tolerance, configuration pinned."""
+    """Every FP32 CG operator (L1/L2 gathers; bulk-copy staged; shared-memory windows; with
+    and without L2 prefetch of the operator stream) reaches the oracle's state to the
+    mixed-precision tolerance, configuration pinned."""
     nn = gpu
     inp = nn.synth(1, 20, seed=11)
     o = orc.Oracle.from_synth(inp)
@@ -430,7 +467,7 @@ def test_set_tuning_rejects_bad_configuration(gpu):
     inp = nn.synth(1, 12, seed=4)
     sim = nn.Simulation.from_synth(inp)
     sim.build_neighbours()
-    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 5)):
+    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 8), (8, 8, -1)):
         with pytest.raises(nn.NNPPError) as e:
             sim.set_tuning(*bad)
         assert e.value.status == 1
