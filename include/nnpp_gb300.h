@@ -225,7 +225,8 @@ nnpp_status nnpp_set_warm_start(nnpp_handle* h, int history);
  * inverted on the GPU and applied as one dense product per iteration.  It is rebuilt when
  * the state is replaced (nnpp_set_state, nnpp_reset) and, when refresh_every > 0 (default
  * 64), after every refresh_every steps counted from then if a phase has changed; backward
- * replays the rebuilds of forward_ckpt.  Single-instance runs only (ensembles use Jacobi).
+ * replays the rebuilds of forward_ckpt.  In an ensemble every member applies its own
+ * coarse correction (block diagonal).
  * Only the iteration count depends on it: every solve still runs to the solver tolerance.
  * A change discards a recorded forward_ckpt run.  The reference's solve of K11 is
  * diagonally preconditioned (Eigen::GMRES with DiagonalPreconditioner, main.cpp:764-766,

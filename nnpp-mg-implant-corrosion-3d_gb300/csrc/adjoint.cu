@@ -68,7 +68,9 @@ nnpp_status load_ckpt(Handle& h, const Handle::Ckpt& c) {
   NNPP_CUDA(cudaMemcpyAsync(h.phi64.get(), c.phi.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.phi_prev.get(), c.phi_prev.get(), sizeof(double) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), c.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &c.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
+  DevState ds = c.ds;
+  ds.op_valid = 0;  // the cached operator arrays are not part of a checkpoint
+  NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
   h.settings_pushed = false;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (h.engine) NNPP_TRY(engine_params(*h.engine));

@@ -85,7 +85,8 @@ struct DevState {
   int solve_iters;    // inner iterations of the current solve
   int outer_active;   // this instance still refines its potential
   int inner_active;   // this instance still iterates its inner CG
-  int pad1;
+  int op_valid;       // freem, dsum, dinv, d32 and the Dirichlet coupling hold the current
+                      // phases' values (cleared by a flip or a state change)
   // per-step mass-curve sampling (adjoint forward)
   double mg_mass_now;
   // adjoint accumulators: dL/dD_liquid[0..3], dL/dk_diss

@@ -314,9 +314,12 @@ nnpp_status prepare_run(Engine& e, int prec) {
   }
   // two-level preconditioner of single-instance engines: recompute the coarse inverse when the
   // state was replaced; the captured graphs follow whether the coarse correction is applied
-  if (e.members.size() == 1) {
-    Handle& h = *e.members[0];
-    if (h.coarse_enabled && h.coarse.n > 0 && (h.coarse.stale || !h.coarse.valid)) NNPP_TRY(coarse_refresh(h));
+  for (Handle* hp : e.members) {
+    Handle& h = *hp;
+    if (h.coarse_enabled && h.coarse.n > 0 && (h.coarse.stale || !h.coarse.valid)) {
+      NNPP_TRY(coarse_refresh(h));
+      if (h.st != e.st) NNPP_CUDA(cudaStreamSynchronize(h.st));  // built on the member's stream
+    }
   }
   const bool split = engine_coarse(e);
   if (split != e.coarse_graphs) {
@@ -422,10 +425,11 @@ static nnpp_status run_steps(Engine& e, int n_steps, int prec) {
 
 nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
   if (!prepared) NNPP_TRY(prepare_run(e, prec));
-  // single-instance runs with the coarse correction stop at multiples of coarse_every steps
-  // (since the state was replaced) to rebuild the coarse operator when the phases changed
-  Handle* h1 = e.members.size() == 1 ? e.members[0] : nullptr;
-  const long long R = (h1 && engine_coarse(e) && !h1->coarse_replay) ? h1->coarse_every : 0;
+  // runs with the coarse correction stop at multiples of the first member's coarse_every
+  // steps (counted since its state was replaced) to rebuild the coarse operators of members
+  // whose phases changed
+  Handle* h1 = e.members[0];
+  const long long R = (engine_coarse(e) && !h1->coarse_replay) ? h1->coarse_every : 0;
   int done = 0;
   while (done < n_steps) {
     int seg = n_steps - done;
@@ -433,7 +437,14 @@ nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
     NNPP_TRY(run_steps(e, seg, prec));
     for (Handle* h : e.members) h->nstep += seg;
     done += seg;
-    if (R > 0 && h1->nstep % R == 0) NNPP_TRY(coarse_check(*h1));
+    if (R > 0 && h1->nstep % R == 0) {
+      // the checks and rebuilds run on the members' streams
+      if (e.members.size() > 1 || h1->st != e.st) NNPP_CUDA(cudaStreamSynchronize(e.st));
+      for (Handle* h : e.members) {
+        NNPP_TRY(coarse_check(*h));
+        if (h->st != e.st) NNPP_CUDA(cudaStreamSynchronize(h->st));
+      }
+    }
   }
   if (e.members.size() > 1 || e.members[0]->st != e.st) NNPP_CUDA(cudaStreamSynchronize(e.st));
   return NNPP_OK;

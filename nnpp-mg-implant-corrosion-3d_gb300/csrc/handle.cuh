@@ -40,6 +40,7 @@ struct KParams {
   double* b64;
   double* r64;
   double* dsum64;                // sum of liquid-liquid weights (K11 diagonal)
+  double* cpl64;                 // coupling to Dirichlet neighbours sum_j w phi_j (free rows)
   unsigned char* freem;          // unknown of the potential solve
   float* d32;
   float* dinv32;
@@ -128,7 +129,7 @@ struct Handle {
   DBuf<double> phi64, phi_prev;
   DBuf<int> flip_step;
   // solver
-  DBuf<double> b64, r64, dsum64, dinv64, rin64, z64, p64, q64, e64;
+  DBuf<double> b64, r64, dsum64, cpl64, dinv64, rin64, z64, p64, q64, e64;
   DBuf<float> d32, dinv32, rin32, z32, p32, q32, e32;
   DBuf<unsigned char> freem;
   DBuf<DevState> dstate;
@@ -201,6 +202,8 @@ nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_us
                        bool keep_history = false);
 nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_phase_user);
 nnpp_status convert_state(Handle& h, int to_prec);
+// the potential operator's mask-dependent arrays must be recomputed by the next prep
+nnpp_status invalidate_operator(Handle& h);
 nnpp_status init_diag(Handle& h);
 
 }  // namespace nnpp

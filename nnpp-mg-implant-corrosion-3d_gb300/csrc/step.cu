@@ -263,6 +263,9 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
     const int* row = k.row;
     const double* w64 = k.w64;
     const int own0 = ts.off[4] + (t.own_begin - t.hb[4]);
+    // the mask-only sums (diagonal, Dirichlet coupling, unknown flag) are kept from the
+    // last prep while no phase changed: only sum_j w phi_j is formed then
+    const bool cached = F11_out == nullptr && k.ds->op_valid != 0;
     for (int a0 = t.own_begin; a0 < t.own_end; a0 += nseg) {
       const int a = a0 + seg;
       const bool act = a < t.own_end;
@@ -271,7 +274,31 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
       const bool scan = act && (fa & 1) && (F11_out != nullptr || !(fa & 2));
       double dsum = 0.0, swphi = 0.0, cpl = 0.0;
       int anyll = 0;
-      if (kPair) {
+      if (cached) {
+        if (kPair) {
+          float sh = 0.f, sl = 0.f;
+          if (scan && k.freem[a]) {
+            for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+              const int s = sslot[j - t.bond0];
+              if (sfl[s] & 1) {
+                const float2 ph = sphi2[s];
+                float ph_, pl_;
+                pair_mul(k.w32[j], k.wlo32[j], ph.x, ph.y, ph_, pl_);
+                pair_add(sh, sl, ph_, pl_);
+              }
+            }
+          }
+          swphi = seg_reduce_pair<W>(sh, sl);
+        } else {
+          if (scan && k.freem[a]) {
+            for (int j = row[a] + sub; j < row[a + 1]; j += W) {
+              const int s = sslot[j - t.bond0];
+              if (sfl[s] & 1) swphi += w64[j] * sphi[s];
+            }
+          }
+          swphi = seg_reduce_d<W>(swphi);
+        }
+      } else if (kPair) {
         float dh = 0.f, dl = 0.f, sh = 0.f, sl = 0.f, ch = 0.f, cl = 0.f;
         if (scan) {
           for (int j = row[a] + sub; j < row[a + 1]; j += W) {
@@ -325,12 +352,20 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
         if (F11_out) {
           F11_out[a] = anyll ? (dsum * pha - swphi) - b : 0.0;
         } else {
-          const bool fr = !(fa & 2) && (fa & 1) && anyll;
-          k.freem[a] = fr ? 1 : 0;
-          k.dsum64[a] = fr ? dsum : 1.0;
-          k.dinv64[a] = fr ? 1.0 / dsum : 0.0;
-          k.d32[a] = fr ? (float)dsum : 1.0f;
-          k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
+          bool fr;
+          if (cached) {
+            fr = k.freem[a] != 0;
+            dsum = k.dsum64[a];
+            cpl = k.cpl64[a];
+          } else {
+            fr = !(fa & 2) && (fa & 1) && anyll;
+            k.freem[a] = fr ? 1 : 0;
+            k.dsum64[a] = fr ? dsum : 1.0;
+            k.cpl64[a] = fr ? cpl : 0.0;
+            k.dinv64[a] = fr ? 1.0 / dsum : 0.0;
+            k.d32[a] = fr ? (float)dsum : 1.0f;
+            k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
+          }
           const double bb = fr ? b : 0.0;
           const double r = fr ? bb - (dsum * pha - swphi) : 0.0;
           k.b64[a] = bb;
@@ -348,6 +383,7 @@ __global__ void __launch_bounds__(kBlock) k_prep(EngineView v, cudaGraphConditio
         reduce_items<2>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
         if (threadIdx.x == 0) {
           DevState* ds = k.ds;
+          ds->op_valid = 1;
           const double bn = tot[0] > 0.0 ? tot[0] : 1.0;
           ds->bnorm2 = bn;
           ds->rnorm2 = tot[1];
@@ -1148,52 +1184,65 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
 }
 
 // ------------------------------------------------------------ two-level preconditioner ----
-// Applied as z = D^-1 r + P A_c^-1 P^T r (single-instance engines; the coarse space and its
-// inverse come from coarse.cu): the restriction sums r over each aggregate, the coarse solve
-// is one product with the dense inverse, and k_cg_zdots forms z with the CG's dots and
-// decisions.  All reductions run in a fixed order (reproducible iterates).
+// Applied as z = D^-1 r + P A_c^-1 P^T r per instance (block diagonal over an ensemble; the
+// coarse spaces and their inverses come from coarse.cu): the restriction sums r over each
+// aggregate, the coarse solve is one product with the dense inverse, and k_cg_zdots forms z
+// with the CG's dots and decisions.  Instances without a coarse space (k.coarse == 0) take
+// z = D^-1 r.  All reductions run in a fixed order (reproducible iterates).
 __device__ __forceinline__ bool coarse_active(const KParams& k, int which) {
   return (which ? *((volatile int*)&k.ds->inner_active) : *((volatile int*)&k.ds->outer_active)) != 0;
 }
 
+// warp per aggregate, the instances one after another
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int which) {
-  const KParams& k = v.inst[0];
-  if (!coarse_active(k, which)) return;
-  const P* r = VecSel<P>::rin(k);
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < k.cn; I += warps) {
-    const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
-    float acc = 0.0f;
-    for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
-      for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by)
-        for (int bx = ax * k.cf; bx < min(ax * k.cf + k.cf, k.nb0); ++bx) {
-          const int b = bx + k.nb0 * (by + k.nb1 * bz);
-          for (int i = k.bin_start[b] + lane; i < k.bin_start[b + 1]; i += 32) acc += (float)r[i];
-        }
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int inst = 0; inst < v.M; ++inst) {
+    const KParams& k = v.inst[inst];
+    if (!k.coarse || !coarse_active(k, which)) continue;
+    const P* r = VecSel<P>::rin(k);
+    for (int I = gw; I < k.cn; I += warps) {
+      const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
+      float acc = 0.0f;
+      for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
+        for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by)
+          for (int bx = ax * k.cf; bx < min(ax * k.cf + k.cf, k.nb0); ++bx) {
+            const int b = bx + k.nb0 * (by + k.nb1 * bz);
+            for (int i = k.bin_start[b] + lane; i < k.bin_start[b + 1]; i += 32) acc += (float)r[i];
+          }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) k.rc[I] = acc;
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+      if (lane == 0) k.rc[I] = acc;
+    }
   }
 }
 
+// warp per row of an instance's inverse: x_c = A_c^-1 r_c (four accumulators, fixed order)
 __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which) {
-  extern __shared__ __align__(16) float srv[];
-  const KParams& k = v.inst[0];
-  if (!coarse_active(k, which)) return;
-  const int n = k.cn;
-  for (int i = threadIdx.x; i < n; i += kBlock) srv[i] = k.rc[i];
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < n; I += warps) {
-    const float* row = k.cinv + (size_t)I * n;
-    float acc = 0.0f;
-    for (int j = lane; j < n; j += 32) acc = fmaf(__ldg(row + j), srv[j], acc);
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int inst = 0; inst < v.M; ++inst) {
+    const KParams& k = v.inst[inst];
+    if (!k.coarse || !coarse_active(k, which)) continue;
+    const int n = k.cn;
+    const float* rc = k.rc;
+    for (int I = gw; I < n; I += warps) {
+      const float* row = k.cinv + (size_t)I * n;
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      int j = lane;
+      for (; j + 96 < n; j += 128) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) k.xc[I] = acc;
+        for (int u = 0; u < 4; ++u) acc[u] = fmaf(__ldg(row + j + 32 * u), __ldg(rc + j + 32 * u), acc[u]);
+      }
+      for (; j < n; j += 32) acc[0] = fmaf(__ldg(row + j), __ldg(rc + j), acc[0]);
+      float x = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if (lane == 0) k.xc[I] = x;
+    }
   }
 }
 
@@ -1214,7 +1263,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
       for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
         const P di = dinv[a];
         const P r = rin[a];
-        const P zz = di == P(0) ? P(0) : r * di + (P)k.xc[k.agg[a]];
+        const P zz = di == P(0) ? P(0) : (k.coarse ? r * di + (P)k.xc[k.agg[a]] : r * di);
         z[a] = zz;
         part[0] += (double)r * (double)zz;
         part[1] += (double)r * (double)r;
@@ -1702,6 +1751,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
         if (pa != 0.0f && (double)hi[0] + (double)lo[0] <= k.csat) {
           pnew = 0.0f;
           k.flip_step[a] = (int)(k.ds->steps + 1);
+          k.ds->op_valid = 0;
         }
         record_history(k, a, k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0);
         const double g = next_phi_guess(k, a);
@@ -1872,6 +1922,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
       if (pa != 0.0 && val[0] <= k.csat) {
         pnew = 0.0;
         k.flip_step[a] = (int)step_no;
+        k.ds->op_valid = 0;
       }
       record_history(k, a, hslot);
       const double g = next_phi_guess(k, a);
@@ -1909,11 +1960,9 @@ __global__ void k_load_state(KParams k, const int* perm, const double* c_user, c
     for (int s = 0; s < S; ++s) c[s] = c_user[(size_t)s * N + u];
     double phi = phi_user ? phi_user[u] : k.phi_prev[a];
     if (dirichlet_phi && ((k.dirmask[a] >> S) & 1)) phi = k.bcval[(size_t)S * N + a];
-    float ph;
-    if (phase_user)
-      ph = phase_user[u] != 0 ? 1.0f : 0.0f;
-    else
-      ph = mixed ? k.rec32_cur[a].phase : (float)k.rec64_cur[a].phase;
+    const float ph_old = mixed ? k.rec32_cur[a].phase : (float)k.rec64_cur[a].phase;
+    const float ph = phase_user ? (phase_user[u] != 0 ? 1.0f : 0.0f) : ph_old;
+    if (ph != ph_old) k.ds->op_valid = 0;  // a new liquid mask: the prep recomputes the diagonal
     k.phi64[a] = phi;
     k.phi_prev[a] = phi;
     if (mixed) {
@@ -2479,6 +2528,7 @@ nnpp_status launch_record_solve(Handle& h, int slot) {
 }
 
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev) {
+  NNPP_TRY(invalidate_operator(h));  // the adjoint solve's unknowns are those of step n
   KParams kp = make_kparams(h, h.cur);
   k_adj_solve_setup<<<h.grid, kBlock, 0, h.st>>>(kp, snap, psi_prev);
   NNPP_CUDA(cudaGetLastError());
@@ -2588,18 +2638,23 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
 template <typename P>
 nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t st, cudaGraphConditionalHandle hc,
                             int init) {
-  const Coarse& c = e.members[0]->coarse;
+  int nmax = 1;
+  for (const Handle* h : e.members) nmax = std::max(nmax, h->coarse.valid ? h->coarse.n : 0);
   const int which = init ? 0 : 1;
-  const int rg = std::max(1, std::min((c.n * 32 + kBlock - 1) / kBlock, e.sms * 8));
+  const int rg = std::max(1, std::min((nmax * 32 + kBlock - 1) / kBlock, e.sms * 8));
   k_coarse_restrict<P><<<rg, kBlock, 0, st>>>(v, which);
-  k_coarse_gemv<<<rg, kBlock, (size_t)c.n * sizeof(float), st>>>(v, which);
+  k_coarse_gemv<<<rg, kBlock, 0, st>>>(v, which);
   k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, init,
                                                                                sizeof(P) == 8 ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
 
-bool engine_coarse(const Engine& e) { return e.members.size() == 1 && e.members[0]->coarse.valid; }
+bool engine_coarse(const Engine& e) {
+  for (const Handle* h : e.members)
+    if (h->coarse_enabled && h->coarse.valid) return true;
+  return false;
+}
 
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc) {
@@ -2688,7 +2743,7 @@ nnpp_status step_alloc(Handle& h) {
   bool ok = h.dirmask.alloc(N) && h.bcval.alloc((S + 1) * N) && h.rec32[0].alloc(N) &&
             h.rec32[1].alloc(N) && h.clo.alloc(N) && h.rec64[0].alloc(N) && h.rec64[1].alloc(N) &&
             h.phi64.alloc(N) && h.phi_prev.alloc(N) && h.flip_step.alloc(N) && h.b64.alloc(N) &&
-            h.r64.alloc(N) && h.dsum64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
+            h.r64.alloc(N) && h.dsum64.alloc(N) && h.cpl64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
             h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
             h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N + 16) && h.p32.alloc(N) &&
             h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.dstate.alloc(1) &&
@@ -2740,6 +2795,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.b64 = h.b64.get();
   k.r64 = h.r64.get();
   k.dsum64 = h.dsum64.get();
+  k.cpl64 = h.cpl64.get();
   k.freem = h.freem.get();
   k.d32 = h.d32.get();
   k.dinv32 = h.dinv32.get();
@@ -2782,7 +2838,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.xh = h.warm_x_alt ? h.warm_x_alt : h.xh.get();
   k.bh = h.warm_b_alt ? h.warm_b_alt : h.bh.get();
   const Coarse& co = h.coarse;
-  k.coarse = co.valid ? 1 : 0;
+  k.coarse = (h.coarse_enabled && co.valid) ? 1 : 0;
   k.agg = co.agg.get();
   k.cinv = co.inv.get();
   k.rc = const_cast<float*>(co.rc.get());
@@ -2802,12 +2858,20 @@ KParams make_kparams(Handle& h, int cur) {
 nnpp_status load_state(Handle& h, const double* d_c_user, const double* d_phi_user,
                        const int* d_phase_user, int prec, bool dirichlet_phi,
                        bool keep_history) {
+  // the cached operator arrays stay valid for the same phases, precision and Dirichlet
+  // potentials (a changed phase is detected by the kernel)
+  if (prec != h.state_prec || !dirichlet_phi) NNPP_TRY(invalidate_operator(h));
   KParams kp = make_kparams(h, h.cur);
   k_load_state<<<h.grid, kBlock, 0, h.st>>>(kp, h.lay.perm.get(), d_c_user, d_phi_user, d_phase_user,
                                             prec == NNPP_MIXED ? 1 : 0, dirichlet_phi ? 1 : 0,
                                             keep_history ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = prec;
+  return NNPP_OK;
+}
+
+nnpp_status invalidate_operator(Handle& h) {
+  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->op_valid, 0, sizeof(int), h.st));
   return NNPP_OK;
 }
 
@@ -2825,7 +2889,8 @@ nnpp_status convert_state(Handle& h, int to_prec) {
   k_convert<<<h.grid, kBlock, 0, h.st>>>(kp, to_prec == NNPP_MIXED ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   h.state_prec = to_prec;
-  return NNPP_OK;
+  // the two precisions form the diagonal with different arithmetic
+  return invalidate_operator(h);
 }
 
 nnpp_status init_diag(Handle& h) {
