@@ -363,8 +363,9 @@ def run_ours(args):
     solves = d1["cg_solves"] - d0["cg_solves"]
     # per solve: warm-start dots + apply + prep; per outer iteration cg_init + ir_update; per CG
     # iteration spmv + update; with the coarse correction restrict + coarse product + z/dots
-    # after every cg_init and update; per step the transport
-    launches = 3 * solves + 2 * outer + 2 * inner + args.steps + (3 * (inner + outer) if cn else 0)
+    # after every cg_init, coarse product + z/dots after every (restricting) update; per step
+    # the transport
+    launches = 3 * solves + 2 * outer + 2 * inner + args.steps + ((2 * inner + 3 * outer) if cn else 0)
 
     # kernel roofline: CUDA-event timed launches on the library's stream (state restored)
     with ProfileRange("kernels"):

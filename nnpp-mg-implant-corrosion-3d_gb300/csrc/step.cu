@@ -1112,7 +1112,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
 
 // e += alpha p, r -= alpha q, z = D^-1 r, partial r.z and r.r -> beta, stop test
 template <typename P>
-__global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphConditionalHandle hc, int split) {
+__global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphConditionalHandle hc) {
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
@@ -1120,23 +1120,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
     const KParams& k = v.inst[c.inst];
     const bool active = *((volatile int*)&k.ds->inner_active) != 0;
     double part[2] = {0.0, 0.0};
-    if (split) {
-      // two-level preconditioner: e and r here; z and the dots after the coarse solve
-      if (active) {
-        P* rin = VecSel<P>::rin(k);
-        const P* p = VecSel<P>::p(k);
-        const P* q = VecSel<P>::q(k);
-        P* e = VecSel<P>::e(k);
-        const P* dinv = VecSel<P>::dinv(k);
-        const P alpha = (P)k.ds->alpha;
-        for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
-          if (dinv[a] == P(0)) continue;
-          e[a] = e[a] + alpha * p[a];
-          rin[a] = rin[a] - alpha * q[a];
-        }
-      }
-      continue;
-    }
     if (active) {
       P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
@@ -1205,13 +1188,67 @@ __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int wh
     const P* r = VecSel<P>::rin(k);
     for (int I = gw; I < k.cn; I += warps) {
       const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
+      const int bx0 = ax * k.cf, bx1 = min(bx0 + k.cf, k.nb0);
       float acc = 0.0f;
       for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
-        for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by)
-          for (int bx = ax * k.cf; bx < min(ax * k.cf + k.cf, k.nb0); ++bx) {
-            const int b = bx + k.nb0 * (by + k.nb1 * bz);
-            for (int i = k.bin_start[b] + lane; i < k.bin_start[b + 1]; i += 32) acc += (float)r[i];
+        for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
+          // the aggregate's bins along x are one contiguous node range
+          const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
+          const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
+          for (int i = i0 + lane; i < i1; i += 32) acc += (float)r[i];
+        }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+      if (lane == 0) k.rc[I] = acc;
+    }
+  }
+}
+
+// The CG update of the split (two-level) iteration fused with the restriction: e += alpha p,
+// r -= alpha q on the unknowns, with a warp per aggregate walking its bins' node ranges, so
+// that the new residual is summed into r_c[I] as it is written.  Instances without a coarse
+// space take the plain update over their nodes.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int inst = 0; inst < v.M; ++inst) {
+    const KParams& k = v.inst[inst];
+    if (!coarse_active(k, 1)) continue;
+    P* rin = VecSel<P>::rin(k);
+    const P* p = VecSel<P>::p(k);
+    const P* q = VecSel<P>::q(k);
+    P* e = VecSel<P>::e(k);
+    const P* dinv = VecSel<P>::dinv(k);
+    const P alpha = (P)k.ds->alpha;
+    if (!k.coarse) {
+      for (int a = gw * 32 + lane; a < k.N; a += warps * 32) {
+        if (dinv[a] == P(0)) continue;
+        e[a] = e[a] + alpha * p[a];
+        rin[a] = rin[a] - alpha * q[a];
+      }
+      continue;
+    }
+    for (int I = gw; I < k.cn; I += warps) {
+      const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
+      const int bx0 = ax * k.cf, bx1 = min(bx0 + k.cf, k.nb0);
+      float acc = 0.0f;
+      for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
+        for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
+          // the aggregate's bins along x are one contiguous node range
+          const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
+          const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
+          for (int i = i0 + lane; i < i1; i += 32) {
+            P r = rin[i];
+            if (dinv[i] != P(0)) {
+              e[i] = e[i] + alpha * p[i];
+              r = r - alpha * q[i];
+              rin[i] = r;
+            }
+            acc += (float)r;
           }
+        }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
       if (lane == 0) k.rc[I] = acc;
@@ -2108,6 +2145,17 @@ int occ_grid(K kern, size_t smem, int sms, int items) {
   return items < g ? (items > 0 ? items : 1) : g;
 }
 
+// Grid of a slice kernel with several CTAs per SM: as many 8-warp CTAs as give every warp
+// the same number of slices (the fewest rounds the resident warps need), so that no warp
+// idles a whole slice at the end while the others of its CTA finish a second one.
+template <typename K>
+int slice_grid(K kern, size_t smem, int sms, int nslices) {
+  const int g = occ_grid(kern, smem, sms, (nslices + 7) / 8);
+  const int rounds = (nslices + 8 * g - 1) / (8 * g);
+  const int g2 = (nslices + 8 * rounds - 1) / (8 * rounds);
+  return g2 < 1 ? 1 : g2;
+}
+
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
@@ -2573,36 +2621,35 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
 // of 16; 5, 6, 7: 4, 3, 2 with bulk L2 prefetches of the operator stream 3, 3, 4 batches ahead
 template <int W>
 void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t st) {
-  const int items = (v.nslices + 7) / 8;
   switch (variant) {
     case 2: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 8, true, 3><<<occ_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 8, true, 3><<<slice_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     case 3:
-      k_cg_spmv32<W, false, 16, false, 5><<<occ_grid(k_cg_spmv32<W, false, 16, false, 5>, 0, sms, items), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 16, false, 5><<<slice_grid(k_cg_spmv32<W, false, 16, false, 5>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
       break;
     case 4: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 16, false, 3><<<occ_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 16, false, 3><<<slice_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     case 5: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 16, false, 3, 3><<<occ_grid(k_cg_spmv32<W, true, 16, false, 3, 3>, sh, sms, items), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 16, false, 3, 3><<<slice_grid(k_cg_spmv32<W, true, 16, false, 3, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     case 6:
-      k_cg_spmv32<W, false, 16, false, 5, 3><<<occ_grid(k_cg_spmv32<W, false, 16, false, 5, 3>, 0, sms, items), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 16, false, 5, 3><<<slice_grid(k_cg_spmv32<W, false, 16, false, 5, 3>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
       break;
     case 7: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 8, true, 3, 4><<<occ_grid(k_cg_spmv32<W, true, 8, true, 3, 4>, sh, sms, items), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 8, true, 3, 4><<<slice_grid(k_cg_spmv32<W, true, 8, true, 3, 4>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     default:
-      k_cg_spmv32<W, false, 8, false, 8><<<occ_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, items), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 8, false, 8><<<slice_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
   }
 }
 
@@ -2690,15 +2737,28 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   });
 }
 
+// update fused with the restriction, coarse product, z and the dots
+template <typename P>
+nnpp_status launch_coarse_update(const Engine& e, const EngineView& v, cudaStream_t st, cudaGraphConditionalHandle hc) {
+  int nmax = 1;
+  for (const Handle* h : e.members) nmax = std::max(nmax, h->coarse.valid ? h->coarse.n : 0);
+  const int rg = std::max(1, std::min((nmax * 32 + kBlock - 1) / kBlock, e.sms * 8));
+  k_cg_update_restrict<P><<<rg, kBlock, 0, st>>>(v);
+  k_coarse_gemv<<<rg, kBlock, 0, st>>>(v, 1);
+  k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0, sizeof(P) == 8 ? 1 : 0);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
-  const int split = engine_coarse(e) ? 1 : 0;
+  if (engine_coarse(e))
+    return prec == NNPP_MIXED ? launch_coarse_update<float>(e, v, st, hc) : launch_coarse_update<double>(e, v, st, hc);
   if (prec == NNPP_MIXED)
-    k_cg_update<float><<<occ_grid(k_cg_update<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, split);
+    k_cg_update<float><<<occ_grid(k_cg_update<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
   else
-    k_cg_update<double><<<occ_grid(k_cg_update<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, split ? 0 : hc, split);
+    k_cg_update<double><<<occ_grid(k_cg_update<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
   NNPP_CUDA(cudaGetLastError());
-  if (split) return prec == NNPP_MIXED ? launch_coarse_z<float>(e, v, st, hc, 0) : launch_coarse_z<double>(e, v, st, hc, 0);
   return NNPP_OK;
 }
 
@@ -2722,9 +2782,9 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED) {
       if (F_out)
-        k_transport32<W, true><<<occ_grid(k_transport32<W, true>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v, F_out);
+        k_transport32<W, true><<<slice_grid(k_transport32<W, true>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, F_out);
       else
-        k_transport32<W, false><<<occ_grid(k_transport32<W, false>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(v, nullptr);
+        k_transport32<W, false><<<slice_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
     } else {
       const size_t sh = smem_tr64(v.halo_max, v.bond_max);
       if (F_out)
