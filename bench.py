@@ -217,7 +217,9 @@ def adjoint_cost(nn, steps, ck=50, se=20):
     return {"workload": "jittered 64^3 lattice minus 8-node shell (%d nodes), solid cylinder "
                         "r=0.25, loss = L2 misfit of the Mg mass-loss curve" % inp["N"],
             "steps": steps, "ckpt_every": ck, "sample_every": se,
-            "precision": "mixed forward, FP64 adjoint bond sums, mixed adjoint potential solve",
+            "precision": "mixed forward, FP32 sliced adjoint bond sums, mixed adjoint potential solve",
+            "storage": "every step's FP64 snapshot kept (no recomputation) when it fits a quarter "
+                       "of the free device memory, else checkpoints every %d steps" % ck,
             "forward_ms": ms_fwd, "forward_ckpt_ms": fwd_ckpt, "backward_ms": bwd,
             "gradient_over_forward": (fwd_ckpt + bwd) / ms_fwd,
             "backward_over_forward": bwd / ms_fwd,

@@ -305,10 +305,18 @@ nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_nod
 nnpp_status nnpp_forward_ckpt(nnpp_handle* h, int n_steps, int precision, int ckpt_every,
                               int sample_every, double* mass_curve);
 
-/* Backward half: given dL/d(mass_curve) (same length), recompute each checkpoint segment
- * and run the adjoint of the explicit step backwards, returning dL/dD_liquid[k] (the solid
- * diffusivity D_solid[k] scales with D_liquid[k]) and dL/dk_diss.  The handle's state is
- * restored to the end of the forward run. */
+/* Storage of the recorded forward run.  0 (default): automatic, every step's FP64
+ * snapshot (64 bytes per node and step) when they fit a quarter of the free device memory,
+ * else checkpoints; 1: checkpoints every ckpt_every steps, backward recomputes each segment;
+ * 2: every step's snapshot, NNPP_ERR_NOMEM when they do not fit.  The gradients do not depend
+ * on the mode (bit for bit).  Discards a recorded run. */
+nnpp_status nnpp_set_adjoint_store(nnpp_handle* h, int mode);
+
+/* Backward half: given dL/d(mass_curve) (same length), run the adjoint of the explicit step
+ * backwards (recomputing each checkpoint segment when the run was recorded with
+ * checkpoints), returning dL/dD_liquid[k] (the solid diffusivity D_solid[k] scales with
+ * D_liquid[k]) and dL/dk_diss.  The handle's state is restored to the end of the forward
+ * run. */
 nnpp_status nnpp_backward(nnpp_handle* h, const double* dL_dmass, double* grad_D,
                           double* grad_k);
 

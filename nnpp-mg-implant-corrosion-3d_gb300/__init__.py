@@ -110,6 +110,7 @@ _SIGS = {
     "nnpp_get_preconditioner": (C.c_int, [_P, _IP, _IP, _IP, C.POINTER(C.c_int64)]),
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
+    "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
     "nnpp_ensemble_forward": (C.c_int, [_P, C.c_int, C.c_int]),
     "nnpp_ensemble_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
@@ -346,6 +347,11 @@ class Simulation:
         _check(lib().nnpp_forward_ckpt(self._h, n_steps, precision, ckpt_every, sample_every,
                                        _dp(curve)))
         return curve
+
+    def set_adjoint_store(self, mode):
+        """Storage of the recorded forward run: 0 automatic, 1 checkpoints (backward
+        recomputes the segments), 2 every step's snapshot."""
+        _check(lib().nnpp_set_adjoint_store(self._h, mode))
 
     def backward(self, dL_dcurve):
         """Backward half: dL/dD_liquid (4,) and dL/dk_diss for dL/d(curve)."""

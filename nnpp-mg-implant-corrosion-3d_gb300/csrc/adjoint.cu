@@ -1,15 +1,15 @@
 // adjoint.cu -- forward/backward pair of the explicit step (checkpointed adjoint).
 //
-// nnpp_forward_ckpt runs the forward with a full-state checkpoint every ck steps and samples
-// the cumulative Mg mass loss.  nnpp_backward walks the checkpoint segments from last to
-// first: it restores a checkpoint, recomputes the segment's steps (the step kernels are
-// deterministic, so the recomputed states are the forward's bit for bit) keeping an FP64
-// snapshot (c, phi, phase) per step, then runs the adjoint of each step backwards: the
-// transposed bond sums (k_adj_transport), the adjoint potential solve A psi = nu through the
-// same batched solver (right-hand side overridden) and the combination
-// lambda^n = mu + (1/(K sigma)) F CSolid z_k psi.  Memory: (ck + 1) snapshots of 64 bytes per
-// node plus one checkpoint per segment (state, and the warm-start history so that the
-// recomputed solves start from the same guesses).
+// nnpp_forward_ckpt runs the forward and samples the cumulative Mg mass loss.  When the FP64
+// snapshots (c, phi, phase; 64 bytes per node) of every step fit the storage budget it keeps
+// them all; otherwise it saves a full-state checkpoint every ck steps.  nnpp_backward runs
+// the adjoint of each step backwards: the transposed bond sums (k_adj_transport), the adjoint
+// potential solve A psi = nu through the same batched solver (right-hand side overridden) and
+// the combination lambda^n = mu + (1/(K sigma)) F CSolid z_k psi.  With checkpoints it walks
+// the segments from last to first, restoring a checkpoint and recomputing the segment's steps
+// (the step kernels are deterministic, so the recomputed states are the forward's bit for
+// bit) into (ck + 1) snapshots; a checkpoint holds the state and the warm-start history, so
+// that the recomputed solves start from the same guesses.  Both modes give the same bits.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -122,7 +122,28 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   h.sample_every = sample_every;
   h.fwd_prec = precision;
   h.ckpts.clear();
-  h.ckpts.resize((n_steps + ckpt_every - 1) / ckpt_every);
+  h.snap_all_valid = false;
+  const size_t N = h.N;
+  bool store_all = h.adjoint_store == 2;
+  if (h.adjoint_store == 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      free_b = 0;
+    }
+    const size_t need = (size_t)(n_steps + 1) * N * sizeof(Rec64);
+    store_all = need <= free_b / 4 || (h.snap_all.get() && h.snap_all.size() >= (size_t)(n_steps + 1) * N);
+  }
+  if (store_all) {
+    if (h.snap_all.size() < (size_t)(n_steps + 1) * N) {
+      h.snap_all.reset();
+      if (!h.snap_all.alloc((size_t)(n_steps + 1) * N))
+        return set_error(NNPP_ERR_NOMEM, "adjoint snapshots of every step");
+    }
+  } else {
+    h.snap_all.reset();
+    h.ckpts.resize((n_steps + ckpt_every - 1) / ckpt_every);
+  }
   double m0 = 0.0;
   NNPP_TRY(launch_sum_c0(h, h.scratch_d.get() + 8));
   NNPP_CUDA(cudaMemcpyAsync(&m0, h.scratch_d.get() + 8, sizeof(double), cudaMemcpyDeviceToHost, h.st));
@@ -130,11 +151,21 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   h.curve.assign(n_steps / sample_every, 0.0);
   const double dV = h.p.dx * h.p.dy * h.p.dz;
   int s = 0;
+  if (store_all) NNPP_TRY(launch_snap_state(h, h.snap_all.get()));
   while (s < n_steps) {
-    if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
-    int next = std::min(n_steps, (s / ckpt_every + 1) * ckpt_every);
-    next = std::min(next, (s / sample_every + 1) * sample_every);
-    NNPP_TRY(engine_run(*h.engine, next - s, precision));
+    int next;
+    if (store_all) {
+      // one step at a time: the potential it solved joins snapshot s, its result is s + 1
+      NNPP_TRY(engine_run(*h.engine, 1, precision));
+      NNPP_TRY(launch_snap_phi(h, h.snap_all.get() + (size_t)s * N));
+      NNPP_TRY(launch_snap_state(h, h.snap_all.get() + (size_t)(s + 1) * N));
+      next = s + 1;
+    } else {
+      if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
+      next = std::min(n_steps, (s / ckpt_every + 1) * ckpt_every);
+      next = std::min(next, (s / sample_every + 1) * sample_every);
+      NNPP_TRY(engine_run(*h.engine, next - s, precision));
+    }
     s = next;
     if (s % sample_every == 0) {
       DevState ds;
@@ -145,9 +176,27 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
     }
   }
   NNPP_TRY(save_ckpt(h, h.fwd_end));
+  h.snap_all_valid = store_all;
   h.fwd_nstep_end = h.nstep;
   h.coarse_event_cur = (int)h.coarse_events.size() - 1;
   std::copy(h.curve.begin(), h.curve.end(), mass_curve);
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_set_adjoint_store(nnpp_handle* hp, int mode) {
+  clear_error();
+  if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
+  if (mode < 0 || mode > 2) return set_error(NNPP_ERR_INVALID, "adjoint store: 0 automatic, 1 checkpoints, 2 every step");
+  Handle& h = hp->h;
+  h.adjoint_store = mode;
+  h.fwd_steps = 0;
+  h.ckpts.clear();
+  h.snap_all_valid = false;
+  if (mode == 1) {
+    NNPP_CUDA(cudaSetDevice(h.device));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+    h.snap_all.reset();
+  }
   return NNPP_OK;
 }
 
@@ -155,7 +204,8 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
   clear_error();
   if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
   Handle& h = hp->h;
-  if (h.fwd_steps < 1 || h.ckpts.empty()) return set_error(NNPP_ERR_STATE, "backward without forward_ckpt");
+  if (h.fwd_steps < 1 || (h.ckpts.empty() && !h.snap_all_valid))
+    return set_error(NNPP_ERR_STATE, "backward without forward_ckpt");
   if (!dL_dmass || !grad_D || !grad_k) return set_error(NNPP_ERR_INVALID, "backward: NULL argument");
   NNPP_CUDA(cudaSetDevice(h.device));
   const int n_steps = h.fwd_steps, ck = h.ck_every, se = h.sample_every, prec = h.fwd_prec;
@@ -170,10 +220,11 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
   int an = 0, ahead = hm ? hm - 1 : 0;
   if (hm && (!xa.alloc((size_t)hm * N) || !ba.alloc((size_t)hm * N)))
     return set_error(NNPP_ERR_NOMEM, "adjoint warm-start ring");
-  if (!snap.alloc((size_t)(ck + 1) * N) || !lam.alloc(S * N) || !mu.alloc(S * N) || !nu.alloc(N) ||
+  const bool all = h.snap_all_valid;
+  if ((!all && !snap.alloc((size_t)(ck + 1) * N)) || !lam.alloc(S * N) || !mu.alloc(S * N) || !nu.alloc(N) ||
       !psi.alloc(N) || !acc.alloc(8))
     return set_error(NNPP_ERR_NOMEM, "adjoint buffers");
-  NNPP_CUDA(cudaMemsetAsync(snap.get(), 0, sizeof(Rec64) * (size_t)(ck + 1) * N, h.st));
+  if (!all) NNPP_CUDA(cudaMemsetAsync(snap.get(), 0, sizeof(Rec64) * (size_t)(ck + 1) * N, h.st));
   NNPP_CUDA(cudaMemsetAsync(lam.get(), 0, sizeof(double) * S * N, h.st));
   NNPP_CUDA(cudaMemsetAsync(psi.get(), 0, sizeof(double) * N, h.st));
   NNPP_CUDA(cudaMemsetAsync(acc.get(), 0, sizeof(double) * 8, h.st));
@@ -199,20 +250,25 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       h.nstep = h.fwd_nstep_end;
     }
   } replay_off{h};
-  const int nseg = (int)h.ckpts.size();
+  // with every step's snapshot one segment covers the run and nothing is recomputed
+  const int nseg = all ? 1 : (int)h.ckpts.size();
+  const int seg_len = all ? n_steps : ck;
   for (int g = nseg - 1; g >= 0 && st == NNPP_OK; --g) {
-    const int s0 = g * ck, s1 = std::min(n_steps, s0 + ck);
-    NNPP_TRY(load_ckpt(h, h.ckpts[g]));
-    NNPP_TRY(launch_snap_state(h, snap.get()));
-    for (int n = s0; n < s1; ++n) {
-      NNPP_TRY(coarse_select(h, n));
-      NNPP_TRY(engine_run(e, 1, prec));
-      NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
-      NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
+    const int s0 = g * seg_len, s1 = std::min(n_steps, s0 + seg_len);
+    const Rec64* base = all ? h.snap_all.get() : snap.get();
+    if (!all) {
+      NNPP_TRY(load_ckpt(h, h.ckpts[g]));
+      NNPP_TRY(launch_snap_state(h, snap.get()));
+      for (int n = s0; n < s1; ++n) {
+        NNPP_TRY(coarse_select(h, n));
+        NNPP_TRY(engine_run(e, 1, prec));
+        NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
+        NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
+      }
     }
     for (int n = s1 - 1; n >= s0; --n) {
-      const Rec64* sn = snap.get() + (size_t)(n - s0) * N;
-      const Rec64* sn1 = snap.get() + (size_t)(n - s0 + 1) * N;
+      const Rec64* sn = base + (size_t)(n - s0) * N;
+      const Rec64* sn1 = base + (size_t)(n - s0 + 1) * N;
       NNPP_TRY(engine_params(e));
       EngineView v = make_view(e, 0, 0);
       if (prec == NNPP_MIXED)

@@ -178,6 +178,11 @@ struct Handle {
   };
   std::vector<Ckpt> ckpts;
   Ckpt fwd_end;
+  // adjoint storage: 0 automatic (every step's snapshot when it fits a quarter of the free
+  // device memory), 1 checkpoints and recomputation, 2 every step's snapshot
+  int adjoint_store = 0;
+  DBuf<Rec64> snap_all;         // (steps + 1) x N snapshots of the recorded forward
+  bool snap_all_valid = false;
   int fwd_steps = 0, ck_every = 0, sample_every = 0, fwd_prec = NNPP_FP64;
   std::vector<double> curve;
   ~Handle();

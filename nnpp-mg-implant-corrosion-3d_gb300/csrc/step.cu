@@ -464,9 +464,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
           ds->beta = 0.0;
           ds->alpha = 0.0;
           ds->inner_it = 0;
-          // FP64: solve to the final tolerance in one sweep; mixed: reduce by inner_rel
+          // FP64: solve to the final tolerance in one sweep; mixed: reduce by inner_rel, but
+          // not below what the outer tolerance needs (0.3 tol: the last sweep stops early)
           const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
-                                     : ds->inner_rel * ds->inner_rel * tot[1];
+                                     : fmax(ds->inner_rel * ds->inner_rel * tot[1],
+                                            0.09 * ds->tol * ds->tol * ds->bnorm2);
           ds->inner_target = target;
           ds->inner_active = (tot[1] > target && ds->max_iter > 0) ? 1 : 0;
         } else {
@@ -1320,7 +1322,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
             ds->alpha = 0.0;
             ds->inner_it = 0;
             const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
-                                       : ds->inner_rel * ds->inner_rel * tot[1];
+                                       : fmax(ds->inner_rel * ds->inner_rel * tot[1],
+                                              0.09 * ds->tol * ds->tol * ds->bnorm2);
             ds->inner_target = target;
             ds->inner_active = (tot[1] > target && ds->max_iter > 0) ? 1 : 0;
           } else {

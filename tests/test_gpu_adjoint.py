@@ -104,6 +104,7 @@ def test_checkpoint_interval_does_not_change_result(gpu, case):
     out = []
     for ck in (7, 25, 60):
         sim = _sim(gpu, inp, _params(inp))
+        sim.set_adjoint_store(1)
         curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
         gD, gk = sim.backward(2.0 * (curve - target))
         out.append((curve, gD, gk))
@@ -124,6 +125,7 @@ def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
     out = []
     for every, ck in ((4, 7), (4, 25), (4, 60), (0, 25)):
         sim = _sim(gpu, inp, p)
+        sim.set_adjoint_store(1)
         sim.set_preconditioner(gpu.PRECOND_TWO_LEVEL, every)
         curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
         built = sim.preconditioner()[3]
@@ -139,6 +141,35 @@ def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
     assert np.allclose(curve, out[0][0], rtol=1e-9, atol=0)
     assert np.allclose(gD, out[0][1], rtol=1e-6, atol=1e-12 * np.abs(out[0][1]).max())
     assert abs(gk - out[0][2]) <= 1e-6 * abs(out[0][2])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_stored_snapshots_equal_recomputation(gpu, case, prec):
+    """Keeping every step's snapshot (no recomputation) and recomputing checkpoint segments
+    give the same curve and gradients bit for bit, and the automatic mode picks one of them."""
+    inp, target = case
+    out = []
+    for mode in (1, 2, 0):
+        sim = _sim(gpu, inp, _params(inp))
+        sim.set_adjoint_store(mode)
+        curve = sim.forward_ckpt(N_STEPS, prec, 25, SE)
+        gD, gk = sim.backward(2.0 * (curve - target))
+        out.append((curve, gD, gk, sim.state()))
+    for curve, gD, gk, state in out[1:]:
+        assert np.array_equal(curve, out[0][0])
+        assert np.array_equal(gD, out[0][1])
+        assert gk == out[0][2]
+        for a, b in zip(state, out[0][3]):
+            assert np.array_equal(a, b)
+
+
+def test_adjoint_store_rejects_bad_mode(gpu, case):
+    inp, _ = case
+    sim = _sim(gpu, inp, _params(inp))
+    for bad in (-1, 3):
+        with pytest.raises(gpu.NNPPError) as e:
+            sim.set_adjoint_store(bad)
+        assert e.value.status == 1
 
 
 def test_backward_restores_end_state(gpu, case):
