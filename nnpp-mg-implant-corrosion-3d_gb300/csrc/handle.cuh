@@ -23,6 +23,8 @@ struct KParams {
   // slice, rows padded to the slice's longest): per bond column 32 FP32 weights then 32
   // 16-bit slot codes (window row << 12 | offset)
   const float* sell;
+  const float* sell_lo;          // sliced like sell's weights: wlo32 (32 floats per column)
+  float4* phi4;                  // per node {phi_hi, phi_lo} (zero on solid nodes), liquid, Dirichlet
   const double* w64;
   const float* w32;
   const float* wlo32;            // w64 - w32: the FP32 pair (w32, wlo32) carries w64
@@ -114,6 +116,8 @@ struct Handle {
   // tiles (built for tiles_T bins per tile)
   DBuf<unsigned short> slot16;
   DBuf<float> sell;
+  DBuf<float> sell_lo;
+  DBuf<float4> phi4;
   DBuf<float4> posrec;
   float h32 = 0.f;
   int tiles_T = 0;

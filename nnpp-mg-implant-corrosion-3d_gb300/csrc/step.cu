@@ -1610,6 +1610,270 @@ __global__ void __launch_bounds__(kBlock) k_ir_update(EngineView v, cudaGraphCon
   }
 }
 
+// ---------------------------------------------------- potential residuals on the slices ----
+// Mixed path: the prep and the refinement residual as slice kernels over the sliced operator
+// (one lane per row, bond columns streamed in batches of 8, neighbour values gathered through
+// L1/L2), with the FP64 weight carried as the FP32 pair (sell, sell_lo) and FP32-pair
+// arithmetic (TwoProd, TwoSum) along each row.  Slice partials, one global ticket; the last
+// CTA makes every instance's decisions.
+constexpr int kResB = 8;
+
+__device__ __forceinline__ const float* sell_lo_col(const KParams& k, const SliceDesc& d) {
+  return k.sell_lo + (size_t)(d.off >> 5) * 32;
+}
+
+// per node {phi_hi, phi_lo} (zero on solid nodes), liquid flag, potential-Dirichlet flag
+__global__ void __launch_bounds__(kBlock) k_phi4(EngineView v) {
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+      const bool liq = k.rec32_cur[a].phase == 0.0f;
+      const double ph = k.phi64[a];
+      const float hi = (float)ph;
+      const float lo = (float)(ph - (double)hi);
+      k.phi4[a] = make_float4(liq ? hi : 0.0f, liq ? lo : 0.0f, liq ? 1.0f : 0.0f,
+                              ((k.dirmask[a] >> S) & 1) ? 1.0f : 0.0f);
+    }
+  }
+}
+
+// prep: b, the FP64 residual r = b - A phi and the norms; the mask-only sums (diagonal,
+// Dirichlet coupling, unknown flag) are formed only when the phases changed (op_valid == 0)
+__global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphConditionalHandle hc) {
+  __shared__ int s_hb[kBlock / 32][12];
+  __shared__ double sm[2 * kBlock / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc& d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    const bool cached = k.ds->op_valid != 0;
+    if (lane < 9) s_hb[warp][lane] = d.gbase[lane];
+    __syncwarp();
+    const int a = d.row0 + lane;
+    const bool rowok = lane < d.nrows;
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f);
+    int len = 0;
+    if (rowok) {
+      fa = k.phi4[a];
+      len = k.row[a + 1] - k.row[a];
+    }
+    const bool scan = rowok && fa.z != 0.0f && fa.w == 0.0f;
+    const int* hb = s_hb[warp];
+    const float* ws = sell_w(k, d) + lane;
+    const float* wls = sell_lo_col(k, d) + lane;
+    const unsigned short* cs = sell_code(k, d) + lane;
+    float dh = 0.f, dl = 0.f, sh = 0.f, sl = 0.f, ch = 0.f, cl = 0.f;
+    int anyll = 0;
+    if (__any_sync(0xffffffffu, scan)) {
+      const int width = d.width;
+      for (int c0 = 0; c0 < width; c0 += kResB) {
+        const int nc = min(kResB, width - c0);
+        float w[kResB], wl[kResB];
+        unsigned int code[kResB];
+#pragma unroll
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc) {
+            w[u] = ld_stream(ws + kSellW * (c0 + u));
+            wl[u] = ld_stream(wls + 32 * (c0 + u));
+            code[u] = ld_stream(cs + kSellC * (c0 + u));
+          }
+        if (cached) {
+          float2 f[kResB];
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) f[u] = __ldg(reinterpret_cast<const float2*>(k.phi4 + code_node(hb, code[u])));
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) {
+              float ph, pl;
+              pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+              pair_add(sh, sl, ph, pl);
+            }
+        } else {
+          float4 f[kResB];
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) f[u] = __ldg(k.phi4 + code_node(hb, code[u]));
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc && c0 + u < len && f[u].z != 0.0f) {
+              float ph, pl;
+              pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+              pair_add(dh, dl, w[u], wl[u]);
+              pair_add(sh, sl, ph, pl);
+              anyll = 1;
+              if (f[u].w != 0.0f) pair_add(ch, cl, ph, pl);
+            }
+        }
+      }
+    }
+    double part0 = 0.0, part1 = 0.0;
+    if (rowok) {
+      double b;
+      if (k.b_override) {
+        b = k.b_override[a];
+      } else {
+        double R11 = 0.0;
+        for (int s = 0; s < S; ++s) R11 += k.z[s] * conc_of<float>(k, a, s);
+        b = k.lam * R11;
+      }
+      const double pha = (double)fa.x + (double)fa.y;
+      const double swphi = scan ? (double)sh + (double)sl : 0.0;
+      bool fr;
+      double dsum, cpl;
+      if (cached) {
+        fr = k.freem[a] != 0;
+        dsum = k.dsum64[a];
+        cpl = k.cpl64[a];
+      } else {
+        dsum = scan ? (double)dh + (double)dl : 0.0;
+        cpl = scan ? (double)ch + (double)cl : 0.0;
+        fr = scan && anyll;
+        k.freem[a] = fr ? 1 : 0;
+        k.dsum64[a] = fr ? dsum : 1.0;
+        k.cpl64[a] = fr ? cpl : 0.0;
+        k.dinv64[a] = fr ? 1.0 / dsum : 0.0;
+        k.d32[a] = fr ? (float)dsum : 1.0f;
+        k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
+      }
+      const double bb = fr ? b : 0.0;
+      const double r = fr ? bb - (dsum * pha - swphi) : 0.0;
+      k.b64[a] = bb;
+      k.r64[a] = r;
+      const double be = bb + (fr ? cpl : 0.0);
+      part0 = be * be;
+      part1 = r * r;
+    }
+    part0 = warp_sum_d(part0);
+    part1 = warp_sum_d(part1);
+    if (lane == 0) {
+      v.partials[sg] = part0;
+      v.partials[(size_t)v.stride + sg] = part1;
+    }
+    __syncwarp();
+  }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[2];
+      reduce_items<2>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = v.inst[i].ds;
+        ds->op_valid = 1;
+        const double bn = tot[0] > 0.0 ? tot[0] : 1.0;
+        ds->bnorm2 = bn;
+        ds->rnorm2 = tot[1];
+        ds->outer_it = 0;
+        ds->solve_iters = 0;
+        const bool go = tot[1] > ds->tol * ds->tol * bn && ds->max_outer > 0;
+        if (!go) {
+          ds->cg_solves += 1;
+          ds->last_relres = sqrt(tot[1] / bn);
+        }
+        ds->outer_active = go ? 1 : 0;
+        ds->inner_active = 0;
+        instance_finished(v, i, 0, hc);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
+// refinement: phi += e on the unknowns, r -= A e (FP32 pairs of the FP64 weights times the
+// FP32 correction), outer stop test
+__global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphConditionalHandle hc) {
+  __shared__ int s_hb[kBlock / 32][12];
+  __shared__ double sm[kBlock / 32];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int s0, s1;
+  warp_slices(v, &s0, &s1);
+  for (int sg = s0; sg < s1; ++sg) {
+    const SliceDesc& d = v.slices[sg];
+    const KParams& k = v.inst[d.inst];
+    double part = 0.0;
+    if (*((volatile int*)&k.ds->outer_active) != 0) {
+      if (lane < 9) s_hb[warp][lane] = d.gbase[lane];
+      __syncwarp();
+      const int a = d.row0 + lane;
+      const bool live = lane < d.nrows && k.freem[a];
+      const int* hb = s_hb[warp];
+      const float* ws = sell_w(k, d) + lane;
+      const float* wls = sell_lo_col(k, d) + lane;
+      const unsigned short* cs = sell_code(k, d) + lane;
+      const float* e = k.e32;
+      float sh = 0.f, sl = 0.f;
+      if (__any_sync(0xffffffffu, live)) {
+        const int width = d.width;
+        for (int c0 = 0; c0 < width; c0 += kResB) {
+          const int nc = min(kResB, width - c0);
+          float w[kResB], wl[kResB], ev[kResB];
+          unsigned int code[kResB];
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) {
+              w[u] = ld_stream(ws + kSellW * (c0 + u));
+              wl[u] = ld_stream(wls + 32 * (c0 + u));
+              code[u] = ld_stream(cs + kSellC * (c0 + u));
+            }
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) ev[u] = __ldg(e + code_node(hb, code[u]));
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) {
+              float ph, pl;
+              pair_mul(w[u], wl[u], ev[u], 0.0f, ph, pl);
+              pair_add(sh, sl, ph, pl);
+            }
+        }
+      }
+      if (live) {
+        const double ea = (double)e[a];
+        const double r = k.r64[a] - (k.dsum64[a] * ea - ((double)sh + (double)sl));
+        k.r64[a] = r;
+        const double ph = k.phi64[a] + ea;
+        k.phi64[a] = ph;
+        set_phi_rec(k, a, ph, true);
+        part = r * r;
+      }
+      __syncwarp();
+    }
+    part = warp_sum_d(part);
+    if (lane == 0) v.partials[sg] = part;
+  }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[1];
+      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = v.inst[i].ds;
+        if (ds->outer_active) {
+          ds->rnorm2 = tot[0];
+          ds->outer_it += 1;
+          ds->outer_total += 1;
+          const bool conv = tot[0] <= ds->tol * ds->tol * ds->bnorm2;
+          const bool go = !conv && ds->outer_it < ds->max_outer && ds->solve_iters < ds->max_iter &&
+                          isfinite(tot[0]);
+          if (!go) {
+            ds->cg_solves += 1;
+            ds->last_relres = sqrt(tot[0] / ds->bnorm2);
+            if (!conv) ds->cg_nc += 1;
+          }
+          ds->outer_active = go ? 1 : 0;
+        }
+        instance_finished(v, i, 0, hc);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
 // ------------------------------------------------------------------- transport -----------
 __device__ __forceinline__ double dissolve_switch(double c0, double csat, double sw) {
   if (sw > 0.0) return 1.0 / (1.0 + exp(-(c0 - csat) / sw));
@@ -2672,6 +2936,12 @@ nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaSt
 
 nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                           cudaGraphConditionalHandle hc, double* F11_out) {
+  if (prec == NNPP_MIXED && !F11_out) {
+    k_phi4<<<occ_grid(k_phi4, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+    k_prep_slices<<<slice_grid(k_prep_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  }
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     const size_t sh = smem_prep(v.halo_max, v.bond_max);
@@ -2767,6 +3037,11 @@ nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, c
 
 nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
+  if (prec == NNPP_MIXED) {
+    k_ir_slices<<<slice_grid(k_ir_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
+    NNPP_CUDA(cudaGetLastError());
+    return NNPP_OK;
+  }
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     const size_t sh = smem_vec64(v.halo_max, v.bond_max);
@@ -2809,7 +3084,7 @@ nnpp_status step_alloc(Handle& h) {
             h.r64.alloc(N) && h.dsum64.alloc(N) && h.cpl64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
             h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
             h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N + 16) && h.p32.alloc(N) &&
-            h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.dstate.alloc(1) &&
+            h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.phi4.alloc(N) && h.dstate.alloc(1) &&
             h.scratch_d.alloc(16 + 7 * 4096) && h.user_stage.alloc((S + 1) * N) &&
             h.user_stage_i.alloc(N);
   if (ok && h.warm_hist >= 3) ok = h.xh.alloc((size_t)h.warm_hist * N) && h.bh.alloc((size_t)h.warm_hist * N);
@@ -2842,6 +3117,8 @@ KParams make_kparams(Handle& h, int cur) {
   k.col = h.lay.col.get();
   k.slot16 = h.slot16.get();
   k.sell = h.sell.get();
+  k.sell_lo = h.sell_lo.get();
+  k.phi4 = h.phi4.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
   k.wlo32 = h.lay.wlo32.get();

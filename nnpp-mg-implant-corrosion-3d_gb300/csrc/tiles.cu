@@ -146,7 +146,8 @@ __global__ void k_slice_windows(int nslices, const SliceDesc* sl, const int* pre
 // + l of the interleaved array, its code (window row << 12 | node - gbase[row]) at 16-bit
 // element 96 (off/32 + c) + 64 + l; padding: code 0, weight 0
 __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb, const int* row,
-                            const unsigned short* slot, const float* w32, float* sell) {
+                            const unsigned short* slot, const float* w32, const float* wlo32, float* sell,
+                            float* sell_lo) {
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
@@ -159,15 +160,17 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
     for (int c = 0; c < d.width; ++c) {
       float* col = sell + ((size_t)(d.off >> 5) + c) * 48;
       unsigned short code = 0;
-      float w = 0.0f;
+      float w = 0.0f, wl = 0.0f;
       if (c < len) {
         int r, node;
         slot_node(slot[j0 + c], pre, hb, &r, &node);
         code = (unsigned short)((r << 12) | (node - d.gbase[r]));
         w = w32[j0 + c];
+        wl = wlo32[j0 + c];
       }
       col[lane] = w;
       reinterpret_cast<unsigned short*>(col + 32)[lane] = code;
+      sell_lo[((size_t)(d.off >> 5) + c) * 32 + lane] = wl;
     }
   }
 }
@@ -263,7 +266,8 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
       }
   // sliced copy of the slot codes and FP32 weights for the CG operator and the transport
   const size_t ns = slices.size();
-  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48)) return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48) || !h.sell_lo.alloc((size_t)(soff / 32) * 32 + 32))
+    return set_error(NNPP_ERR_NOMEM, "sliced operator");
   DBuf<SliceDesc> dsl;
   DBuf<int> dpre, dlohi;
   bool fit = true;
@@ -302,7 +306,7 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
     }
     NNPP_CUDA(cudaMemcpyAsync(dsl.get(), slices.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
     k_sell_fill<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), dpre.get(), L.row.get(), h.slot16.get(), L.w32.get(),
-                                      h.sell.get());
+                                      L.wlo32.get(), h.sell.get(), h.sell_lo.get());
     NNPP_CUDA(cudaGetLastError());
     NNPP_CUDA(cudaStreamSynchronize(h.st));
   }
