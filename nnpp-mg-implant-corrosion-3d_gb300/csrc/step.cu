@@ -1942,8 +1942,9 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
 // Each warp streams 32-row slices of the sliced operator, one lane per node, gathering the
 // neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
 // partials of the diagnostics are reduced per instance by the last CTA.
+constexpr int kTrB = 4;  // bond columns per batch of the FP32 transport
 template <int W, bool RESID>
-__global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double* F_out) {
+__global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double* F_out) {
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
@@ -1991,29 +1992,40 @@ __global__ void __launch_bounds__(kBlock, 4) k_transport32(EngineView v, double*
       const float* ws = sell_w(k, d) + lane;
       const unsigned short* cs = sell_code(k, d) + lane;
       const int len = k.row[a + 1] - k.row[a];
-      // the next streamed column is in flight while this one's neighbour record is gathered
-      float wn = len > 0 ? __ldcs(ws) : 0.0f;
-      unsigned int cn_code = len > 0 ? __ldcs(cs) : 0u;
-#pragma unroll 2
-      for (int c = 0; c < len; ++c) {
-        const float w = wn;
-        const int n = code_node(hb, cn_code);
-        if (c + 1 < len) {
-          wn = __ldcs(ws + kSellW * (c + 1));
-          cn_code = __ldcs(cs + kSellC * (c + 1));
-        }
-        const float4 cn = __ldg(rc + 2 * n);
-        const float4 nb = __ldg(rc + 2 * n + 1);
-        const bool nsol = nb.z != 0.0f;
-        const float dphi = (nb.x - cb.x) + (nb.y - cb.y);
-        iface |= (pa != 0.0f && !nsol) ? 1 : 0;
+      // bonds in batches of kTrB columns: the batch's streamed codes and weights, then its
+      // neighbour records, all in flight before the arithmetic (column order is kept, so the
+      // sums do not depend on the batch size)
+      for (int c0 = 0; c0 < len; c0 += kTrB) {
+        float w[kTrB];
+        unsigned int code[kTrB];
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const float cw = (nsol ? cfS[s] : cfL[s]) * w;
-          const float cns = sel4(cn, s);
-          a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
-          a2[s] = fmaf(cw * cns, dphi, a2[s]);
-        }
+        for (int u = 0; u < kTrB; ++u)
+          if (c0 + u < len) {
+            w[u] = ld_stream(ws + kSellW * (c0 + u));
+            code[u] = ld_stream(cs + kSellC * (c0 + u));
+          }
+        float4 cn[kTrB], nb[kTrB];
+#pragma unroll
+        for (int u = 0; u < kTrB; ++u)
+          if (c0 + u < len) {
+            const int n = code_node(hb, code[u]);
+            cn[u] = __ldg(rc + 2 * n);
+            nb[u] = __ldg(rc + 2 * n + 1);
+          }
+#pragma unroll
+        for (int u = 0; u < kTrB; ++u)
+          if (c0 + u < len) {
+            const bool nsol = nb[u].z != 0.0f;
+            const float dphi = (nb[u].x - cb.x) + (nb[u].y - cb.y);
+            iface |= (pa != 0.0f && !nsol) ? 1 : 0;
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              const float cw = (nsol ? cfS[s] : cfL[s]) * w[u];
+              const float cns = sel4(cn[u], s);
+              a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
+              a2[s] = fmaf(cw * cns, dphi, a2[s]);
+            }
+          }
       }
       const unsigned char dm = k.dirmask[a];
       const float4 lo4 = k.clo[a];
