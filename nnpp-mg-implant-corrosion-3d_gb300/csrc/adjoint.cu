@@ -106,7 +106,7 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   h.coarse_record = false;
   if (engine_coarse(*h.engine)) {
     h.coarse_events.emplace_back();
-    const size_t nn = (size_t)h.coarse.n * h.coarse.n;
+    const size_t nn = h.coarse.inv_elems();
     if (!h.coarse_events[0].inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
     NNPP_CUDA(cudaMemcpyAsync(h.coarse_events[0].inv.get(), h.coarse.inv.get(), sizeof(float) * nn,
                               cudaMemcpyDeviceToDevice, h.st));

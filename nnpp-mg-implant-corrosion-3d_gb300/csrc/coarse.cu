@@ -131,11 +131,11 @@ __global__ void k_two_i_minus(int n, float* T) {
     T[e] = ((e / n == e % n) ? 2.0f : 0.0f) - T[e];
 }
 
-// Y = (X + X^T) / 2
-__global__ void k_symmetrize(int n, const float* X, float* Y) {
+// Y = (X + X^T) / 2, Y with rows of stride ld
+__global__ void k_symmetrize(int n, int ld, const float* X, float* Y) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x) {
     const size_t i = e / n, j = e % n;
-    Y[e] = 0.5f * (X[e] + X[j * n + i]);
+    Y[i * ld + j] = 0.5f * (X[e] + X[j * n + i]);
   }
 }
 
@@ -176,9 +176,11 @@ nnpp_status coarse_build(Handle& h) {
   c.f = f;
   for (int d = 0; d < 3; ++d) c.na[d] = (L.nb[d] + f - 1) / f;
   c.n = (int)count(f);
-  const size_t nn = (size_t)c.n * c.n;
-  if (!c.agg.alloc(h.N) || !c.inv.alloc(nn) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) || !c.rowabs.alloc(c.n))
+  c.ld = (c.n + 3) & ~3;
+  if (!c.agg.alloc(h.N) || !c.inv.alloc(c.inv_elems()) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) ||
+      !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n))
     return set_error(NNPP_ERR_NOMEM, "coarse space");
+  NNPP_CUDA(cudaMemsetAsync(c.inv.get(), 0, sizeof(float) * c.inv_elems(), h.st));  // padding stays 0
   k_agg_fill<<<std::max(1, std::min((L.nbins + 255) / 256, 4096)), 256, 0, h.st>>>(
       L.bin_start.get(), L.nb[0], L.nb[1], L.nb[2], f, c.na[0], c.na[1], c.agg.get());
   NNPP_CUDA(cudaGetLastError());
@@ -198,7 +200,8 @@ nnpp_status coarse_refresh(Handle& h) {
   const int n = c.n;
   const size_t nn = (size_t)n * n;
   // work matrices on first use (ensemble members never refresh and never hold them)
-  if (!c.a.alloc(nn) || !c.t.alloc(nn) || !c.x.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "coarse inverse");
+  if (!c.a.alloc(nn) || !c.t.alloc(nn) || !c.x.alloc(nn) || !c.y.alloc(nn))
+    return set_error(NNPP_ERR_NOMEM, "coarse inverse");
   DBuf<float>& A = c.a;
   DBuf<float>& T = c.t;
   DBuf<float>& X = c.x;
@@ -215,7 +218,7 @@ nnpp_status coarse_refresh(Handle& h) {
   if (cublasSetStream(hb, h.st) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasSetStream");
   const float one = 1.0f, zero = 0.0f;
   float* x = X.get();
-  float* y = c.inv.get();  // scratch until the final symmetrisation
+  float* y = c.y.get();
   for (int it = 0; it < kNsIterations; ++it) {
     // T = A X ; T = 2I - T ; X <- X T
     if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
@@ -228,12 +231,8 @@ nnpp_status coarse_refresh(Handle& h) {
       return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
     std::swap(x, y);
   }
-  // x holds the last iterate; the symmetrised copy goes to c.inv (through T when x is c.inv)
-  if (x == c.inv.get()) {
-    NNPP_CUDA(cudaMemcpyAsync(T.get(), x, sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
-    x = T.get();
-  }
-  k_symmetrize<<<eg, 256, 0, h.st>>>(n, x, c.inv.get());
+  // x holds the last iterate; its symmetrised copy goes to c.inv (rows of stride ld)
+  k_symmetrize<<<eg, 256, 0, h.st>>>(n, c.ld, x, c.inv.get());
   NNPP_CUDA(cudaGetLastError());
   if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
   k_phase_snap<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
@@ -263,7 +262,7 @@ nnpp_status coarse_check(Handle& h) {
     h.coarse_events.emplace_back();
     Handle::CoarseEvent& ev = h.coarse_events.back();
     ev.step = h.nstep - h.coarse_base;
-    const size_t nn = (size_t)c.n * c.n;
+    const size_t nn = c.inv_elems();
     if (!ev.inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
     NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
   }
@@ -275,7 +274,7 @@ nnpp_status coarse_select(Handle& h, long long step) {
   int e = 0;
   while (e + 1 < (int)h.coarse_events.size() && h.coarse_events[e + 1].step <= step) ++e;
   if (e == h.coarse_event_cur) return NNPP_OK;
-  const size_t nn = (size_t)h.coarse.n * h.coarse.n;
+  const size_t nn = h.coarse.inv_elems();
   NNPP_CUDA(cudaMemcpyAsync(h.coarse.inv.get(), h.coarse_events[e].inv.get(), sizeof(float) * nn,
                             cudaMemcpyDeviceToDevice, h.st));
   h.coarse_event_cur = e;

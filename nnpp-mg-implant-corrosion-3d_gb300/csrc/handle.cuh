@@ -73,6 +73,8 @@ struct KParams {
   const int* bin_start;
   int coarse;                    // 1: z = D^-1 r + P A_c^-1 P^T r
   int cn;                        // coarse unknowns
+  int cld;                       // row stride of cinv
+  double* cdots;                 // 3 cn: per-aggregate dot contributions
   int cf, cna0, cna1, cna2, nb0, nb1, nb2;
 };
 
@@ -84,11 +86,14 @@ constexpr int kCoarseMax = 3000;  // aggregates of the coarse space (dense inver
 
 struct Coarse {
   int f = 0, n = 0, na[3] = {0, 0, 0};
+  int ld = 0;         // row stride of inv: n rounded up to 4 (16-byte rows, zero padding)
   DBuf<int> agg;      // N: aggregate of each node
-  DBuf<float> inv;    // n x n: the coarse inverse
+  DBuf<float> inv;    // n x ld: the coarse inverse (symmetric: row I = column I)
   DBuf<float> rc, xc; // n: restricted residual, coarse correction
+  DBuf<double> dots;  // 3n: per aggregate r.D^-1 r and r.r of the update, r_c x_c of the product
   DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
-  DBuf<float> a, t, x; // n x n: A_c and the Newton-Schulz work matrices
+  DBuf<float> a, t, x, y; // n x n: A_c and the Newton-Schulz work matrices
+  size_t inv_elems() const { return (size_t)n * ld; }
   DBuf<unsigned char> snap;  // N: phases (internal order) the inverse was computed from
   DBuf<int> count;           // phase changes since (coarse_check)
   void* cublas = nullptr;

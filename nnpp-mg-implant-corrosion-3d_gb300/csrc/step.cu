@@ -527,15 +527,22 @@ __device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
 }
 
 // node of a slot code: window row start (per-warp table of the slice's lo[]) + offset
-// streamed operator loads that bypass L1 allocation (L1 stays with the gathered vectors)
+// streamed operator loads: no L1 allocation (L1 stays with the gathered vectors) and L2
+// evict-first (the operator is read once per pass; the vectors and the coarse inverse the
+// other kernels of the iteration read stay in L2)
+__device__ __forceinline__ uint64_t stream_policy() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
 __device__ __forceinline__ float ld_stream(const float* p) {
   float v;
-  asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(stream_policy()));
   return v;
 }
 __device__ __forceinline__ unsigned int ld_stream(const unsigned short* p) {
   unsigned short v;
-  asm volatile("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(v) : "l"(p));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(stream_policy()));
   return v;
 }
 
@@ -1208,8 +1215,8 @@ __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int wh
 
 // The CG update of the split (two-level) iteration fused with the restriction: e += alpha p,
 // r -= alpha q on the unknowns, with a warp per aggregate walking its bins' node ranges, so
-// that the new residual is summed into r_c[I] as it is written.  Instances without a coarse
-// space take the plain update over their nodes.
+// that the new residual is summed into r_c[I] as it is written, with the aggregate's parts
+// of r.D^-1 r and r.r.
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
   const int lane = threadIdx.x & 31;
@@ -1224,18 +1231,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
     P* e = VecSel<P>::e(k);
     const P* dinv = VecSel<P>::dinv(k);
     const P alpha = (P)k.ds->alpha;
-    if (!k.coarse) {
-      for (int a = gw * 32 + lane; a < k.N; a += warps * 32) {
-        if (dinv[a] == P(0)) continue;
-        e[a] = e[a] + alpha * p[a];
-        rin[a] = rin[a] - alpha * q[a];
-      }
-      continue;
-    }
+    if (!k.coarse) continue;  // engines run the split iteration only when every member has one
     for (int I = gw; I < k.cn; I += warps) {
       const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
       const int bx0 = ax * k.cf, bx1 = min(bx0 + k.cf, k.nb0);
       float acc = 0.0f;
+      double rzf = 0.0, rr = 0.0;  // r.D^-1 r and r.r of the aggregate's nodes
       for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
         for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
           // the aggregate's bins along x are one contiguous node range
@@ -1243,44 +1244,130 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
           const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
           for (int i = i0 + lane; i < i1; i += 32) {
             P r = rin[i];
-            if (dinv[i] != P(0)) {
+            const P di = dinv[i];
+            if (di != P(0)) {
               e[i] = e[i] + alpha * p[i];
               r = r - alpha * q[i];
               rin[i] = r;
+              rzf += (double)r * (double)(r * di);
+              rr += (double)r * (double)r;
             }
             acc += (float)r;
           }
         }
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-      if (lane == 0) k.rc[I] = acc;
+      for (int off = 16; off > 0; off >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, off);
+        rzf += __shfl_down_sync(0xffffffffu, rzf, off);
+        rr += __shfl_down_sync(0xffffffffu, rr, off);
+      }
+      if (lane == 0) {
+        k.rc[I] = acc;
+        k.cdots[I] = rzf;
+        k.cdots[k.cn + I] = rr;
+      }
     }
   }
 }
 
-// warp per row of an instance's inverse: x_c = A_c^-1 r_c (four accumulators, fixed order)
-__global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which) {
+// warp per row of an instance's inverse: x_c = A_c^-1 r_c (r_c in shared memory, 16-byte
+// row loads, eight accumulators combined in a fixed order).  With dots (the CG update of the
+// split iteration), also r_c[I] x_c[I] = (P^T r).(x_c) per row, and the last CTA forms
+// r.z = r.D^-1 r + r_c.x_c and r.r from the per-aggregate parts and makes the CG decisions.
+__global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which, cudaGraphConditionalHandle hc,
+                                                        int dots) {
+  extern __shared__ __align__(16) float srv[];
+  __shared__ double sm[3 * kBlock / 32];
+  __shared__ int s_last;
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   for (int inst = 0; inst < v.M; ++inst) {
     const KParams& k = v.inst[inst];
     if (!k.coarse || !coarse_active(k, which)) continue;
-    const int n = k.cn;
-    const float* rc = k.rc;
+    const int n = k.cn, ld = k.cld;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ld; i += kBlock) srv[i] = i < n ? k.rc[i] : 0.0f;
+    __syncthreads();
+    const float4* sr4 = reinterpret_cast<const float4*>(srv);
+    const int nq = ld >> 2;  // 16-byte groups per row
     for (int I = gw; I < n; I += warps) {
-      const float* row = k.cinv + (size_t)I * n;
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const float4* row = reinterpret_cast<const float4*>(k.cinv + (size_t)I * ld);
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       int j = lane;
-      for (; j + 96 < n; j += 128) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) acc[u] = fmaf(__ldg(row + j + 32 * u), __ldg(rc + j + 32 * u), acc[u]);
+      for (; j + 32 < nq; j += 64) {
+        const float4 a0 = __ldg(row + j), a1 = __ldg(row + j + 32);
+        const float4 b0 = sr4[j], b1 = sr4[j + 32];
+        acc[0] = fmaf(a0.x, b0.x, acc[0]);
+        acc[1] = fmaf(a0.y, b0.y, acc[1]);
+        acc[2] = fmaf(a0.z, b0.z, acc[2]);
+        acc[3] = fmaf(a0.w, b0.w, acc[3]);
+        acc[4] = fmaf(a1.x, b1.x, acc[4]);
+        acc[5] = fmaf(a1.y, b1.y, acc[5]);
+        acc[6] = fmaf(a1.z, b1.z, acc[6]);
+        acc[7] = fmaf(a1.w, b1.w, acc[7]);
       }
-      for (; j < n; j += 32) acc[0] = fmaf(__ldg(row + j), __ldg(rc + j), acc[0]);
-      float x = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+      if (j < nq) {
+        const float4 a0 = __ldg(row + j);
+        const float4 b0 = sr4[j];
+        acc[0] = fmaf(a0.x, b0.x, acc[0]);
+        acc[1] = fmaf(a0.y, b0.y, acc[1]);
+        acc[2] = fmaf(a0.z, b0.z, acc[2]);
+        acc[3] = fmaf(a0.w, b0.w, acc[3]);
+      }
+      float x = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-      if (lane == 0) k.xc[I] = x;
+      if (lane == 0) {
+        k.xc[I] = x;
+        if (dots) k.cdots[2 * n + I] = (double)srv[I] * (double)x;
+      }
+    }
+  }
+  if (!dots) return;
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      const KParams& k = v.inst[i];
+      double tot[3] = {0.0, 0.0, 0.0};
+      if (k.coarse) reduce_items<3>(k.cdots, k.cn, 0, k.cn, tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (!k.coarse) {
+          ds->inner_active = 0;  // not reached: split engines have a coarse space per member
+        } else if (ds->inner_active) {
+          const double rz = tot[0] + tot[2];
+          const double alpha_d = ds->alpha;
+          ds->beta = ds->rz != 0.0 ? rz / ds->rz : 0.0;
+          ds->rz = rz;
+          ds->rr = tot[1];
+          ds->inner_it += 1;
+          ds->solve_iters += 1;
+          ds->cg_iters += 1;
+          const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
+                          ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
+          ds->inner_active = go ? 1 : 0;
+        }
+        instance_finished(v, i, 1, hc);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
+// z = D^-1 r + x_c[agg] on the unknowns (after the decisions of k_coarse_gemv)
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_z_form(EngineView v) {
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    if (!coarse_active(k, 1)) continue;
+    const P* rin = VecSel<P>::rin(k);
+    P* z = VecSel<P>::z(k);
+    const P* dinv = VecSel<P>::dinv(k);
+    for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+      const P di = dinv[a];
+      z[a] = di == P(0) ? P(0) : rin[a] * di + (P)k.xc[k.agg[a]];
     }
   }
 }
@@ -2667,8 +2754,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, con
       const unsigned short* cs = sell_code(k, d) + lane;
       const int len = k.row[a + 1] - k.row[a];
       for (int c = 0; c < len; ++c) {
-        const float w = __ldcs(ws + kSellW * c);
-        const int n = code_node(hb, __ldcs(cs + kSellC * c));
+        const float w = ld_stream(ws + kSellW * c);
+        const int n = code_node(hb, ld_stream(cs + kSellC * c));
         const float4 cn = __ldg(rec + 3 * n), ln = __ldg(rec + 3 * n + 1), pn = __ldg(rec + 3 * n + 2);
         const bool nsol = pn.z != 0.0f;
         iface |= (pm && !nsol) ? 1 : 0;
@@ -2966,6 +3053,13 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
   });
 }
 
+// largest row stride of the members' coarse inverses (shared memory of k_coarse_gemv)
+int cld_max(const Engine& e) {
+  int m = 4;
+  for (const Handle* h : e.members) m = std::max(m, h->coarse.valid ? h->coarse.ld : 0);
+  return m;
+}
+
 // z = M^-1 r with the two-level preconditioner: restriction, coarse solve, z and the dots
 template <typename P>
 nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t st, cudaGraphConditionalHandle hc,
@@ -2975,7 +3069,7 @@ nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t s
   const int which = init ? 0 : 1;
   const int rg = std::max(1, std::min((nmax * 32 + kBlock - 1) / kBlock, e.sms * 8));
   k_coarse_restrict<P><<<rg, kBlock, 0, st>>>(v, which);
-  k_coarse_gemv<<<rg, kBlock, 0, st>>>(v, which);
+  k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, which, 0, 0);
   k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, init,
                                                                                sizeof(P) == 8 ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
@@ -2984,8 +3078,8 @@ nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t s
 
 bool engine_coarse(const Engine& e) {
   for (const Handle* h : e.members)
-    if (h->coarse_enabled && h->coarse.valid) return true;
-  return false;
+    if (!h->coarse_enabled || !h->coarse.valid) return false;
+  return !e.members.empty();
 }
 
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
@@ -3029,8 +3123,16 @@ nnpp_status launch_coarse_update(const Engine& e, const EngineView& v, cudaStrea
   for (const Handle* h : e.members) nmax = std::max(nmax, h->coarse.valid ? h->coarse.n : 0);
   const int rg = std::max(1, std::min((nmax * 32 + kBlock - 1) / kBlock, e.sms * 8));
   k_cg_update_restrict<P><<<rg, kBlock, 0, st>>>(v);
-  k_coarse_gemv<<<rg, kBlock, 0, st>>>(v, 1);
-  k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0, sizeof(P) == 8 ? 1 : 0);
+  if (e.members.size() == 1) {
+    // one instance: the dots come from the aggregates, the decisions from the coarse product's
+    // last CTA, and z is a plain elementwise pass
+    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, hc, 1);
+    k_z_form<P><<<occ_grid(k_z_form<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+  } else {
+    // ensembles: per-instance reductions in parallel (the last chunk of each instance)
+    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, 0, 0);
+    k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0, sizeof(P) == 8 ? 1 : 0);
+  }
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
@@ -3197,6 +3299,8 @@ KParams make_kparams(Handle& h, int cur) {
   k.xc = const_cast<float*>(co.xc.get());
   k.bin_start = h.lay.bin_start.get();
   k.cn = co.n;
+  k.cld = co.ld;
+  k.cdots = co.dots.get();
   k.cf = co.f;
   k.cna0 = co.na[0];
   k.cna1 = co.na[1];

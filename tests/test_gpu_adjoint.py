@@ -39,11 +39,15 @@ def case(gpu, orc):
     return inp, target
 
 
-def _sim(nn, inp, p, tol=1e-13):
+def _sim(nn, inp, p, tol=1e-13, pin=False):
+    """pin: a fixed execution configuration (the autotuner's timing-based choice changes the
+    summation order, so bit-for-bit comparisons between handles pin it)."""
     sim = nn.Simulation(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"],
                         inp["phase0"])
     sim.build_neighbours()
     sim.set_solver(tol, 4000)
+    if pin:
+        sim.set_tuning(4, 8, 0)
     return sim
 
 
@@ -103,7 +107,7 @@ def test_checkpoint_interval_does_not_change_result(gpu, case):
     inp, target = case
     out = []
     for ck in (7, 25, 60):
-        sim = _sim(gpu, inp, _params(inp))
+        sim = _sim(gpu, inp, _params(inp), pin=True)
         sim.set_adjoint_store(1)
         curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
         gD, gk = sim.backward(2.0 * (curve - target))
@@ -124,7 +128,7 @@ def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
     target = np.zeros(N_STEPS // SE)
     out = []
     for every, ck in ((4, 7), (4, 25), (4, 60), (0, 25)):
-        sim = _sim(gpu, inp, p)
+        sim = _sim(gpu, inp, p, pin=True)
         sim.set_adjoint_store(1)
         sim.set_preconditioner(gpu.PRECOND_TWO_LEVEL, every)
         curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
@@ -150,7 +154,7 @@ def test_stored_snapshots_equal_recomputation(gpu, case, prec):
     inp, target = case
     out = []
     for mode in (1, 2, 0):
-        sim = _sim(gpu, inp, _params(inp))
+        sim = _sim(gpu, inp, _params(inp), pin=True)
         sim.set_adjoint_store(mode)
         curve = sim.forward_ckpt(N_STEPS, prec, 25, SE)
         gD, gk = sim.backward(2.0 * (curve - target))
