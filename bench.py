@@ -438,8 +438,9 @@ def run_ours(args):
     bytes_ir = 4 * nnz + 4 * (N + 1) + N * (b + 8 + 8 + 8)
     bytes_upd = N * b * 6 + N * b
     if cn:
-        # restriction (r), coarse product (the n x n inverse), z = D^-1 r + x_c[agg] (r, dinv, agg, z)
-        bytes_upd += N * b + 4 * cn * cn + N * (b + b + 4 + b)
+        # restricting update (as above), coarse product (the n x n inverse),
+        # z = D^-1 r + x_c[agg] (r, dinv, agg, z)
+        bytes_upd += 4 * cn * cn + N * (b + b + 4 + b)
     dom = max(shares, key=shares.get)
     alg = {"cg_spmv": (bytes_spmv, t_spmv), "transport": (bytes_tr, t_tr), "ir_residual": (bytes_ir, t_ir),
            "cg_update": (bytes_upd, t_upd)}

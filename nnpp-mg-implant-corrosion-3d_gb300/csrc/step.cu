@@ -1242,17 +1242,30 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
           // the aggregate's bins along x are one contiguous node range
           const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
           const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
-          for (int i = i0 + lane; i < i1; i += 32) {
-            P r = rin[i];
-            const P di = dinv[i];
-            if (di != P(0)) {
-              e[i] = e[i] + alpha * p[i];
-              r = r - alpha * q[i];
-              rin[i] = r;
-              rzf += (double)r * (double)(r * di);
-              rr += (double)r * (double)r;
+          // two nodes per lane per round (their loads in flight together), summed in order
+          for (int i = i0 + lane; i < i1; i += 64) {
+            const bool two = i + 32 < i1;
+            P r0 = rin[i], r1 = two ? rin[i + 32] : P(0);
+            const P d0 = dinv[i], d1 = two ? dinv[i + 32] : P(0);
+            const P p0 = p[i], p1 = two ? p[i + 32] : P(0);
+            const P q0 = q[i], q1 = two ? q[i + 32] : P(0);
+            const P e0 = e[i], e1 = two ? e[i + 32] : P(0);
+            if (d0 != P(0)) {
+              e[i] = e0 + alpha * p0;
+              r0 = r0 - alpha * q0;
+              rin[i] = r0;
+              rzf += (double)r0 * (double)(r0 * d0);
+              rr += (double)r0 * (double)r0;
             }
-            acc += (float)r;
+            acc += (float)r0;
+            if (d1 != P(0)) {
+              e[i + 32] = e1 + alpha * p1;
+              r1 = r1 - alpha * q1;
+              rin[i + 32] = r1;
+              rzf += (double)r1 * (double)(r1 * d1);
+              rr += (double)r1 * (double)r1;
+            }
+            acc += (float)r1;
           }
         }
 #pragma unroll
@@ -1271,9 +1284,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
 }
 
 // warp per row of an instance's inverse: x_c = A_c^-1 r_c (r_c in shared memory, 16-byte
-// row loads, eight accumulators combined in a fixed order).  With dots (the CG update of the
+// row loads, four accumulators combined in a fixed order).  With dots (the CG update of the
 // split iteration), also r_c[I] x_c[I] = (P^T r).(x_c) per row, and the last CTA forms
 // r.z = r.D^-1 r + r_c.x_c and r.r from the per-aggregate parts and makes the CG decisions.
+constexpr int kGemvU = 12;  // 16-byte loads per lane in flight (12 x 32 x 4 = 1536 floats a round)
 __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which, cudaGraphConditionalHandle hc,
                                                         int dots) {
   extern __shared__ __align__(16) float srv[];
@@ -1293,29 +1307,24 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
     const int nq = ld >> 2;  // 16-byte groups per row
     for (int I = gw; I < n; I += warps) {
       const float4* row = reinterpret_cast<const float4*>(k.cinv + (size_t)I * ld);
-      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      int j = lane;
-      for (; j + 32 < nq; j += 64) {
-        const float4 a0 = __ldg(row + j), a1 = __ldg(row + j + 32);
-        const float4 b0 = sr4[j], b1 = sr4[j + 32];
-        acc[0] = fmaf(a0.x, b0.x, acc[0]);
-        acc[1] = fmaf(a0.y, b0.y, acc[1]);
-        acc[2] = fmaf(a0.z, b0.z, acc[2]);
-        acc[3] = fmaf(a0.w, b0.w, acc[3]);
-        acc[4] = fmaf(a1.x, b1.x, acc[4]);
-        acc[5] = fmaf(a1.y, b1.y, acc[5]);
-        acc[6] = fmaf(a1.z, b1.z, acc[6]);
-        acc[7] = fmaf(a1.w, b1.w, acc[7]);
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      // rounds of kGemvU 16-byte loads per lane, all in flight before their products
+      for (int j0 = lane; j0 < nq; j0 += 32 * kGemvU) {
+        float4 a[kGemvU];
+#pragma unroll
+        for (int u = 0; u < kGemvU; ++u)
+          if (j0 + 32 * u < nq) a[u] = __ldg(row + j0 + 32 * u);
+#pragma unroll
+        for (int u = 0; u < kGemvU; ++u)
+          if (j0 + 32 * u < nq) {
+            const float4 b = sr4[j0 + 32 * u];
+            acc[0] = fmaf(a[u].x, b.x, acc[0]);
+            acc[1] = fmaf(a[u].y, b.y, acc[1]);
+            acc[2] = fmaf(a[u].z, b.z, acc[2]);
+            acc[3] = fmaf(a[u].w, b.w, acc[3]);
+          }
       }
-      if (j < nq) {
-        const float4 a0 = __ldg(row + j);
-        const float4 b0 = sr4[j];
-        acc[0] = fmaf(a0.x, b0.x, acc[0]);
-        acc[1] = fmaf(a0.y, b0.y, acc[1]);
-        acc[2] = fmaf(a0.z, b0.z, acc[2]);
-        acc[3] = fmaf(a0.w, b0.w, acc[3]);
-      }
-      float x = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+      float x = (acc[0] + acc[1]) + (acc[2] + acc[3]);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
       if (lane == 0) {
