@@ -2726,8 +2726,9 @@ __global__ void k_adj_pack(KParams k, const Rec64* snap, const Rec64* snap1, con
   }
 }
 
+constexpr int kAdjB = 2;  // bond columns per batch of the FP32 adjoint transport
 template <int W>
-__global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, const float4* rec,
+__global__ void __launch_bounds__(kBlock, 2) k_adj_transport32(EngineView v, const float4* rec,
                                                                double* mu, double* nu, double* acc) {
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[5 * kBlock / 32];
@@ -2762,25 +2763,47 @@ __global__ void __launch_bounds__(kBlock, 3) k_adj_transport32(EngineView v, con
       const float* ws = sell_w(k, d) + lane;
       const unsigned short* cs = sell_code(k, d) + lane;
       const int len = k.row[a + 1] - k.row[a];
-      for (int c = 0; c < len; ++c) {
-        const float w = ld_stream(ws + kSellW * c);
-        const int n = code_node(hb, ld_stream(cs + kSellC * c));
-        const float4 cn = __ldg(rec + 3 * n), ln = __ldg(rec + 3 * n + 1), pn = __ldg(rec + 3 * n + 2);
-        const bool nsol = pn.z != 0.0f;
-        iface |= (pm && !nsol) ? 1 : 0;
-        const float dphi = (pm4.x - pn.x) + (pm4.y - pn.y);  // phi_m - phi_i
+      // bonds in batches of kAdjB columns (codes, weights and records in flight together;
+      // the column order of the sums is kept)
+      for (int c0 = 0; c0 < len; c0 += kAdjB) {
+        float wv[kAdjB];
+        unsigned int code[kAdjB];
 #pragma unroll
-        for (int q = 0; q < S; ++q) {
-          const float Dw = (nsol ? cfS[q] : cfL[q]) * w;
-          const float li = sel4(ln, q), ci = sel4(cn, q);
-          A1[q] = fmaf(Dw, li - sel4(lm4, q), A1[q]);
-          a1[q] = fmaf(Dw, ci - sel4(cm4, q), a1[q]);
-          const float tl = Dw * li, tc = Dw * ci;
-          A2[q] = fmaf(tl, dphi, A2[q]);
-          a2[q] = fmaf(-tc, dphi, a2[q]);
-          sl[q] += tl;
-          sc[q] += tc;
-        }
+        for (int u = 0; u < kAdjB; ++u)
+          if (c0 + u < len) {
+            wv[u] = ld_stream(ws + kSellW * (c0 + u));
+            code[u] = ld_stream(cs + kSellC * (c0 + u));
+          }
+        float4 cnv[kAdjB], lnv[kAdjB], pnv[kAdjB];
+#pragma unroll
+        for (int u = 0; u < kAdjB; ++u)
+          if (c0 + u < len) {
+            const int n = code_node(hb, code[u]);
+            cnv[u] = __ldg(rec + 3 * n);
+            lnv[u] = __ldg(rec + 3 * n + 1);
+            pnv[u] = __ldg(rec + 3 * n + 2);
+          }
+#pragma unroll
+        for (int u = 0; u < kAdjB; ++u)
+          if (c0 + u < len) {
+            const float w = wv[u];
+            const float4 cn = cnv[u], ln = lnv[u], pn = pnv[u];
+            const bool nsol = pn.z != 0.0f;
+            iface |= (pm && !nsol) ? 1 : 0;
+            const float dphi = (pm4.x - pn.x) + (pm4.y - pn.y);  // phi_m - phi_i
+#pragma unroll
+            for (int q = 0; q < S; ++q) {
+              const float Dw = (nsol ? cfS[q] : cfL[q]) * w;
+              const float li = sel4(ln, q), ci = sel4(cn, q);
+              A1[q] = fmaf(Dw, li - sel4(lm4, q), A1[q]);
+              a1[q] = fmaf(Dw, ci - sel4(cm4, q), a1[q]);
+              const float tl = Dw * li, tc = Dw * ci;
+              A2[q] = fmaf(tl, dphi, A2[q]);
+              a2[q] = fmaf(-tc, dphi, a2[q]);
+              sl[q] += tl;
+              sc[q] += tc;
+            }
+          }
       }
       const unsigned char dm = k.dirmask[a];
       const bool src = iface && !(dm & 1);
@@ -2916,7 +2939,7 @@ nnpp_status launch_adj_transport32(const Engine& e, const EngineView& v, Handle&
   KParams kp = make_kparams(h, h.cur);
   k_adj_pack<<<h.grid, kBlock, 0, st>>>(kp, snap, snap1, lam, rec);
   NNPP_CUDA(cudaGetLastError());
-  k_adj_transport32<4><<<occ_grid(k_adj_transport32<4>, 0, e.sms, (v.nslices + 7) / 8), kBlock, 0, st>>>(
+  k_adj_transport32<4><<<slice_grid(k_adj_transport32<4>, 0, e.sms, v.nslices), kBlock, 0, st>>>(
       v, rec, mu, nu, acc);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
