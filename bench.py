@@ -214,6 +214,17 @@ def adjoint_cost(nn, steps, ck=50, se=20):
     sim.reset()
     ms_fwd = sim.forward_timed(steps, nn.MIXED)
     fwd_ckpt, bwd = 1e3 * (t1 - t0), 1e3 * (t2 - t1)
+    # the same gradient with checkpoints every ck steps and recomputation in backward
+    sim.set_adjoint_store(1)
+    sim.reset()
+    t0 = time.perf_counter()
+    curve_r = sim.forward_ckpt(steps, nn.MIXED, ck, se)
+    t1 = time.perf_counter()
+    gD_r, gk_r = sim.backward(2.0 * (curve_r - target))
+    t2 = time.perf_counter()
+    recompute = {"forward_ckpt_ms": 1e3 * (t1 - t0), "backward_ms": 1e3 * (t2 - t1),
+                 "gradient_over_forward": 1e3 * (t2 - t0) / ms_fwd,
+                 "same_gradient_bits": bool(np.array_equal(gD_r, gD) and gk_r == gk)}
     return {"workload": "jittered 64^3 lattice minus 8-node shell (%d nodes), solid cylinder "
                         "r=0.25, loss = L2 misfit of the Mg mass-loss curve" % inp["N"],
             "steps": steps, "ckpt_every": ck, "sample_every": se,
@@ -224,7 +235,8 @@ def adjoint_cost(nn, steps, ck=50, se=20):
             "gradient_over_forward": (fwd_ckpt + bwd) / ms_fwd,
             "backward_over_forward": bwd / ms_fwd,
             "grad_D": [float(x) for x in gD], "grad_k": float(gk),
-            "loss": float(((curve - target) ** 2).sum())}
+            "loss": float(((curve - target) ** 2).sum()),
+            "checkpoint_recompute": recompute}
 
 
 class ProfileRange:
