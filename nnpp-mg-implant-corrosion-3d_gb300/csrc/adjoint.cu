@@ -105,11 +105,7 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   h.coarse_event_cur = -1;
   h.coarse_record = false;
   if (engine_coarse(*h.engine)) {
-    h.coarse_events.emplace_back();
-    const size_t nn = h.coarse.inv_elems();
-    if (!h.coarse_events[0].inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
-    NNPP_CUDA(cudaMemcpyAsync(h.coarse_events[0].inv.get(), h.coarse.inv.get(), sizeof(float) * nn,
-                              cudaMemcpyDeviceToDevice, h.st));
+    NNPP_TRY(coarse_record_event(h, 0));
     h.coarse_base = h.nstep;
     h.coarse_record = true;
   }
@@ -260,7 +256,7 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       NNPP_TRY(load_ckpt(h, h.ckpts[g]));
       NNPP_TRY(launch_snap_state(h, snap.get()));
       for (int n = s0; n < s1; ++n) {
-        NNPP_TRY(coarse_select(h, n));
+        NNPP_TRY(coarse_select(h, n, true));
         NNPP_TRY(engine_run(e, 1, prec));
         NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
         NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));

@@ -111,6 +111,52 @@ __global__ void k_coarse_assemble(KParams k, const int* bin_start, int nb0, int 
   }
 }
 
+// Rows of A P off the diagonal term, for the deflated CG: for an unknown i and an aggregate
+// J, -sum of w_ij over the unknowns j of J (liquid, off the Dirichlet set).  Thread per node,
+// the 27 neighbour aggregates accumulated in fixed slots in the row's bond order; fill == 0
+// counts the touched slots into cnt, fill == 1 writes them in slot order from ptr.
+__global__ void k_ap_rows(KParams k, int mixed, int na0, int na1, int na2, int fill, int* cnt,
+                          const int* ptr, int* col, float* val) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.N; i += gridDim.x * blockDim.x) {
+    float acc[27];
+    unsigned int touched = 0u;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) acc[q] = 0.0f;
+    const bool unk = node_liquid(k, i, mixed) && !((k.dirmask[i] >> S) & 1);
+    if (unk) {
+      const int I = k.agg[i];
+      const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
+      for (int j = k.row[i]; j < k.row[i + 1]; ++j) {
+        const int m = k.col[j];
+        if (!node_liquid(k, m, mixed) || ((k.dirmask[m] >> S) & 1)) continue;
+        const int J = k.agg[m];
+        const int jx = J % na0, jy = (J / na0) % na1, jz = J / (na0 * na1);
+        const int q = (jx - ax + 1) + 3 * ((jy - ay + 1) + 3 * (jz - az + 1));
+        const float w = k.w32[j];
+#pragma unroll
+        for (int t = 0; t < 27; ++t)
+          if (t == q) acc[t] -= w;
+        touched |= 1u << q;
+      }
+    }
+    if (!fill) {
+      cnt[i] = __popc(touched);
+      continue;
+    }
+    if (!touched) continue;
+    const int I = k.agg[i];
+    const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
+    int o = ptr[i];
+#pragma unroll
+    for (int q = 0; q < 27; ++q)
+      if ((touched >> q) & 1u) {
+        col[o] = (ax + q % 3 - 1) + na0 * ((ay + (q / 3) % 3 - 1) + na1 * (az + q / 9 - 1));
+        val[o] = acc[q];
+        ++o;
+      }
+  }
+}
+
 // X = I / max_i rowabs[i]  (column-major n x n)
 __global__ void k_ns_init(int n, const float* rowabs, float* X) {
   __shared__ float smax;
@@ -177,9 +223,14 @@ nnpp_status coarse_build(Handle& h) {
   for (int d = 0; d < 3; ++d) c.na[d] = (L.nb[d] + f - 1) / f;
   c.n = (int)count(f);
   c.ld = (c.n + 3) & ~3;
+  // A P rows hold at most 27 aggregates each: allocated once, so that no pointer the
+  // kernels hold changes when the operator is rebuilt or replayed
   if (!c.agg.alloc(h.N) || !c.inv.alloc(c.inv_elems()) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) ||
-      !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n))
+      !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n) || !c.ap_ptr.alloc((size_t)h.N + 1) ||
+      !c.ap_col.alloc(27 * (size_t)h.N) || !c.ap_val.alloc(27 * (size_t)h.N))
     return set_error(NNPP_ERR_NOMEM, "coarse space");
+  NNPP_CUDA(cudaMemsetAsync(c.dots.get(), 0, sizeof(double) * 3 * (size_t)c.n, h.st));
+  c.ap_nnz = 0;
   NNPP_CUDA(cudaMemsetAsync(c.inv.get(), 0, sizeof(float) * c.inv_elems(), h.st));  // padding stays 0
   k_agg_fill<<<std::max(1, std::min((L.nbins + 255) / 256, 4096)), 256, 0, h.st>>>(
       L.bin_start.get(), L.nb[0], L.nb[1], L.nb[2], f, c.na[0], c.na[1], c.agg.get());
@@ -234,6 +285,21 @@ nnpp_status coarse_refresh(Handle& h) {
   // x holds the last iterate; its symmetrised copy goes to c.inv (rows of stride ld)
   k_symmetrize<<<eg, 256, 0, h.st>>>(n, c.ld, x, c.inv.get());
   NNPP_CUDA(cudaGetLastError());
+  // A P for the deflated CG (the same phases as A_c)
+  {
+    DBuf<int> cnt;
+    if (!cnt.alloc(h.N)) return set_error(NNPP_ERR_NOMEM, "A P rows");
+    const int gb = std::max(1, std::min((h.N + 255) / 256, 152 * 16));
+    const int mixed = h.state_prec == NNPP_MIXED ? 1 : 0;
+    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 0, cnt.get(), nullptr, nullptr, nullptr);
+    NNPP_CUDA(cudaGetLastError());
+    long long nnz = 0;
+    NNPP_TRY(scan_ints(h.st, cnt.get(), c.ap_ptr.get(), h.N, &nnz));
+    c.ap_nnz = (size_t)nnz;  // at most 27 per node: within the arrays allocated at build
+    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 1, nullptr, c.ap_ptr.get(),
+                                    c.ap_col.get(), c.ap_val.get());
+    NNPP_CUDA(cudaGetLastError());
+  }
   if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
   k_phase_snap<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
       kp, h.state_prec == NNPP_MIXED ? 1 : 0, c.snap.get());
@@ -242,6 +308,9 @@ nnpp_status coarse_refresh(Handle& h) {
   c.stale = false;
   c.rebuilds += 1;
   h.coarse_event_cur = -1;
+  // the coarse operator and A P match the phases now
+  static const int kOne = 1;
+  NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->defl, &kOne, sizeof(int), cudaMemcpyHostToDevice, h.st));
   return NNPP_OK;
 }
 
@@ -258,26 +327,48 @@ nnpp_status coarse_check(Handle& h) {
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (changed == 0) return NNPP_OK;
   NNPP_TRY(coarse_refresh(h));
-  if (h.coarse_record) {
-    h.coarse_events.emplace_back();
-    Handle::CoarseEvent& ev = h.coarse_events.back();
-    ev.step = h.nstep - h.coarse_base;
-    const size_t nn = c.inv_elems();
-    if (!ev.inv.alloc(nn)) return set_error(NNPP_ERR_NOMEM, "recorded coarse inverse");
-    NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
-  }
+  if (h.coarse_record) NNPP_TRY(coarse_record_event(h, h.nstep - h.coarse_base));
   return NNPP_OK;
 }
 
-nnpp_status coarse_select(Handle& h, long long step) {
+nnpp_status coarse_record_event(Handle& h, long long step) {
+  const Coarse& c = h.coarse;
+  h.coarse_events.emplace_back();
+  Handle::CoarseEvent& ev = h.coarse_events.back();
+  ev.step = step;
+  const size_t nn = c.inv_elems();
+  const size_t na = std::max<size_t>(c.ap_nnz, 1);
+  ev.ap_nnz = c.ap_nnz;
+  if (!ev.inv.alloc(nn) || !ev.ap_ptr.alloc((size_t)h.N + 1) || !ev.ap_col.alloc(na) || !ev.ap_val.alloc(na))
+    return set_error(NNPP_ERR_NOMEM, "recorded coarse operator");
+  NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(ev.ap_ptr.get(), c.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(ev.ap_col.get(), c.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(ev.ap_val.get(), c.ap_val.get(), sizeof(float) * na, cudaMemcpyDeviceToDevice, h.st));
+  return NNPP_OK;
+}
+
+nnpp_status coarse_select(Handle& h, long long step, bool recompute) {
   if (h.coarse_events.empty()) return NNPP_OK;
   int e = 0;
   while (e + 1 < (int)h.coarse_events.size() && h.coarse_events[e + 1].step <= step) ++e;
-  if (e == h.coarse_event_cur) return NNPP_OK;
-  const size_t nn = h.coarse.inv_elems();
-  NNPP_CUDA(cudaMemcpyAsync(h.coarse.inv.get(), h.coarse_events[e].inv.get(), sizeof(float) * nn,
-                            cudaMemcpyDeviceToDevice, h.st));
-  h.coarse_event_cur = e;
+  if (e != h.coarse_event_cur) {
+    Coarse& c = h.coarse;
+    const Handle::CoarseEvent& ev = h.coarse_events[e];
+    const size_t nn = c.inv_elems();
+    const size_t na = std::max<size_t>(ev.ap_nnz, 1);
+    c.ap_nnz = ev.ap_nnz;
+    NNPP_CUDA(cudaMemcpyAsync(c.inv.get(), ev.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(c.ap_ptr.get(), ev.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(c.ap_col.get(), ev.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(c.ap_val.get(), ev.ap_val.get(), sizeof(float) * na, cudaMemcpyDeviceToDevice, h.st));
+    h.coarse_event_cur = e;
+  }
+  // recomputing the step the forward rebuilt the operator before: the deflation resumed there
+  if (recompute && step > 0 && h.coarse_events[e].step == step) {
+    static const int kOn = 1;
+    NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->defl, &kOn, sizeof(int), cudaMemcpyHostToDevice, h.st));
+  }
   return NNPP_OK;
 }
 

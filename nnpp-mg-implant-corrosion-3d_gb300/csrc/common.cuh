@@ -75,6 +75,7 @@ struct DevState {
   double rr;          // inner: current ||r||^2
   double rz;          // inner: r.z
   double alpha, beta;
+  double pq;          // inner: p.A p of the current direction (deflated CG's step length)
   double tol;         // relative tolerance of the solve
   double inner_rel;   // inner relative reduction per refinement sweep
   double inner_target;  // inner: stop when ||r||^2 <= inner_target
@@ -96,7 +97,8 @@ struct DevState {
   int hist_n;
   int hist_head;
   int warm_nd;        // differences used by the next guess (0: keep the extrapolation)
-  int pad2;
+  int defl;           // 1: the coarse operator and A P match the current phases (the mixed
+                      // inner CG runs deflated); cleared by a flip or a phase change
   double warm_coef[kHistMax];
   // block tickets for last-block reductions
   unsigned int ticket[8];

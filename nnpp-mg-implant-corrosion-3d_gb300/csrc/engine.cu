@@ -34,6 +34,7 @@ nnpp_status refresh_params(Engine& e) {
   for (int i = 0; i < M; ++i) {
     k0[i] = make_kparams(*e.members[i], e.members[i]->cur);
     k1[i] = make_kparams(*e.members[i], e.members[i]->cur ^ 1);
+    k0[i].defl_ok = k1[i].defl_ok = M == 1 ? 1 : 0;
   }
   // pageable sources: the copies are staged before the calls return, and the kernels that
   // read the blocks are ordered after them on e.st
@@ -228,6 +229,7 @@ nnpp_status capture_solve(Engine& e, const EngineView& v, int prec) {
   NNPP_TRY(launch_cg_update_b(e, v, prec, e.st_b2, hin));
   cudaGraph_t tmp;
   NNPP_CUDA(cudaStreamEndCapture(e.st_b2, &tmp));
+  NNPP_TRY(launch_cg_final_b(e, v, prec, e.st_b1));
   NNPP_TRY(launch_ir_update_b(e, v, prec, e.st_b1, hout));
   NNPP_CUDA(cudaStreamEndCapture(e.st_b1, &tmp));
   return NNPP_OK;
@@ -261,6 +263,7 @@ nnpp_status eager_solve(Engine& e, const EngineView& v, int prec) {
       NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
       NNPP_TRY(launch_cg_update_b(e, v, prec, e.st, 0));
     }
+    NNPP_TRY(launch_cg_final_b(e, v, prec, e.st));
     NNPP_TRY(launch_ir_update_b(e, v, prec, e.st, 0));
   }
   return NNPP_OK;

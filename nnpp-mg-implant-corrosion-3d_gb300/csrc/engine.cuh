@@ -141,7 +141,8 @@ nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cud
 nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc);
-bool engine_coarse(const Engine& e);  // the two-level preconditioner applies (one member, inverse ready)
+bool engine_coarse(const Engine& e);  // the two-level preconditioner applies (every member has one)
+nnpp_status launch_cg_final_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc);
 nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,

@@ -75,6 +75,16 @@ struct KParams {
   int cn;                        // coarse unknowns
   int cld;                       // row stride of cinv
   double* cdots;                 // 3 cn: per-aggregate dot contributions
+  // deflated CG (mixed inner solves while k.ds->defl): A P without its diagonal term (CSR
+  // over nodes: aggregate, -sum of the weights to the unknowns of that aggregate), the
+  // correction equation's right-hand side r0 and t = A e
+  int defl_ok;                   // single-instance engine (ensembles take the additive form)
+  int pad_defl;
+  const int* ap_ptr;
+  const int* ap_col;
+  const float* ap_val;
+  float* r0_32;
+  float* t32;
   int cf, cna0, cna1, cna2, nb0, nb1, nb2;
 };
 
@@ -91,6 +101,9 @@ struct Coarse {
   DBuf<float> inv;    // n x ld: the coarse inverse (symmetric: row I = column I)
   DBuf<float> rc, xc; // n: restricted residual, coarse correction
   DBuf<double> dots;  // 3n: per aggregate r.D^-1 r and r.r of the update, r_c x_c of the product
+  DBuf<int> ap_ptr, ap_col;  // A P off its diagonal term (N + 1, 27 N capacity): see KParams
+  DBuf<float> ap_val;
+  size_t ap_nnz = 0;
   DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
   DBuf<float> a, t, x, y; // n x n: A_c and the Newton-Schulz work matrices
   size_t inv_elems() const { return (size_t)n * ld; }
@@ -139,7 +152,7 @@ struct Handle {
   DBuf<int> flip_step;
   // solver
   DBuf<double> b64, r64, dsum64, cpl64, dinv64, rin64, z64, p64, q64, e64;
-  DBuf<float> d32, dinv32, rin32, z32, p32, q32, e32;
+  DBuf<float> d32, dinv32, rin32, z32, p32, q32, e32, r0_32, t32;
   DBuf<unsigned char> freem;
   DBuf<DevState> dstate;
   DBuf<double> scratch_d;       // small device scratch (voln1rel override, ...)
@@ -162,6 +175,9 @@ struct Handle {
   struct CoarseEvent {
     long long step = 0;
     DBuf<float> inv;
+    DBuf<int> ap_ptr, ap_col;
+    DBuf<float> ap_val;
+    size_t ap_nnz = 0;
   };
   std::vector<CoarseEvent> coarse_events;
   bool coarse_record = false, coarse_replay = false;
@@ -202,9 +218,12 @@ nnpp_status coarse_build(Handle& h);
 nnpp_status coarse_refresh(Handle& h);
 // at a refresh point: recompute the inverse if a phase changed since the last refresh
 nnpp_status coarse_check(Handle& h);
-// during backward: put the inverse of the last recorded refresh at or before `step`
-// (relative to the start of forward_ckpt) into coarse.inv
-nnpp_status coarse_select(Handle& h, long long step);
+// during forward_ckpt: record the current coarse inverse and A P as used from `step` on
+nnpp_status coarse_record_event(Handle& h, long long step);
+// during backward: put the inverse and A P of the last recorded refresh at or before `step`
+// (relative to the start of forward_ckpt) in place; recompute: `step` is about to be
+// recomputed (a refresh recorded at it re-enables the deflation, as in the forward)
+nnpp_status coarse_select(Handle& h, long long step, bool recompute = false);
 
 // step.cu
 nnpp_status step_alloc(Handle& h);

@@ -429,6 +429,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
           p[a] = P(0);
           q[a] = P(0);
           e[a] = P(0);
+          if (sizeof(P) == 4) {  // the deflated solve's right-hand side and t = A e^
+            k.r0_32[a] = (float)k.r64[a];
+            k.t32[a] = 0.0f;
+          }
         }
       }
       continue;
@@ -691,7 +695,10 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
       reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
-        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+        if (ds->inner_active) {
+          ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+          ds->pq = tot[0];
+        }
       }
     }
     if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
@@ -870,7 +877,10 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
       reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
-        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+        if (ds->inner_active) {
+          ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+          ds->pq = tot[0];
+        }
       }
     }
     if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
@@ -1054,7 +1064,10 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32s(EngineView v, int stag
     reduce_items<1>(v.partials, v.stride, v.slice_first[0], v.slice_count[0], tot, sm);
     if (threadIdx.x == 0) {
       DevState* ds = k.ds;
-      if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+      if (ds->inner_active) {
+          ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+          ds->pq = tot[0];
+        }
       v.ticket[v.M + 1] = 0;
     }
   }
@@ -1111,7 +1124,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv64(EngineView v) {
       reduce_items<1>(v.partials, v.stride, v.tile_first[t.inst], v.tile_count[t.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
-        if (ds->inner_active) ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+        if (ds->inner_active) {
+          ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+          ds->pq = tot[0];
+        }
         v.ticket[t.inst] = 0;
       }
     }
@@ -1185,6 +1201,22 @@ __device__ __forceinline__ bool coarse_active(const KParams& k, int which) {
   return (which ? *((volatile int*)&k.ds->inner_active) : *((volatile int*)&k.ds->outer_active)) != 0;
 }
 
+// The mixed inner CG runs deflated (DEF1: CG on P_d A e^ = P_d r with P_d = I - A Q,
+// Q = P A_c^-1 P^T, e = Q r + e^ - Q A e^) while the coarse operator and A P match the
+// phases; otherwise it takes the additive coarse correction.
+template <typename P>
+__device__ __forceinline__ bool deflating(const KParams& k) {
+  return sizeof(P) == 4 && k.coarse && k.defl_ok && *((volatile const int*)&k.ds->defl) != 0;
+}
+
+// (A P x_c)_i of an unknown i: its diagonal term from the CG operator's diagonal, the rest
+// from the stored rows
+__device__ __forceinline__ float ap_apply(const KParams& k, int i) {
+  float s = k.d32[i] * k.xc[k.agg[i]];
+  for (int kk = k.ap_ptr[i]; kk < k.ap_ptr[i + 1]; ++kk) s = fmaf(k.ap_val[kk], k.xc[k.ap_col[kk]], s);
+  return s;
+}
+
 // warp per aggregate, the instances one after another
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int which) {
@@ -1193,7 +1225,8 @@ __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int wh
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   for (int inst = 0; inst < v.M; ++inst) {
     const KParams& k = v.inst[inst];
-    if (!k.coarse || !coarse_active(k, which)) continue;
+    if (!k.coarse || !coarse_active(k, which == 2 ? 0 : which)) continue;
+    if (which == 2 && !deflating<P>(k)) continue;  // the deflated solve's final correction only
     const P* r = VecSel<P>::rin(k);
     for (int I = gw; I < k.cn; I += warps) {
       const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
@@ -1232,9 +1265,24 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
     const P* dinv = VecSel<P>::dinv(k);
     const P alpha = (P)k.ds->alpha;
     if (!k.coarse) continue;  // engines run the split iteration only when every member has one
+    const bool def = deflating<P>(k);
     for (int I = gw; I < k.cn; I += warps) {
       const int ax = I % k.cna0, ay = (I / k.cna0) % k.cna1, az = I / (k.cna0 * k.cna1);
       const int bx0 = ax * k.cf, bx1 = min(bx0 + k.cf, k.nb0);
+      if (def) {
+        // deflated iteration: restrict q = A p (the update follows the coarse product)
+        float acc = 0.0f;
+        for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
+          for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
+            const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
+            const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
+            for (int i = i0 + lane; i < i1; i += 32) acc += (float)(dinv[i] != P(0) ? q[i] : P(0));
+          }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (lane == 0) k.rc[I] = acc;
+        continue;
+      }
       float acc = 0.0f;
       double rzf = 0.0, rr = 0.0;  // r.D^-1 r and r.r of the aggregate's nodes
       for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
@@ -1289,7 +1337,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
 // r.z = r.D^-1 r + r_c.x_c and r.r from the per-aggregate parts and makes the CG decisions.
 constexpr int kGemvU = 12;  // 16-byte loads per lane in flight (12 x 32 x 4 = 1536 floats a round)
 __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which, cudaGraphConditionalHandle hc,
-                                                        int dots) {
+                                                        int dots, int def_mixed) {
   extern __shared__ __align__(16) float srv[];
   __shared__ double sm[3 * kBlock / 32];
   __shared__ int s_last;
@@ -1298,7 +1346,8 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   for (int inst = 0; inst < v.M; ++inst) {
     const KParams& k = v.inst[inst];
-    if (!k.coarse || !coarse_active(k, which)) continue;
+    if (!k.coarse || !coarse_active(k, which == 2 ? 0 : which)) continue;
+    if (which == 2 && !deflating<float>(k)) continue;  // the deflated solve's final correction only
     const int n = k.cn, ld = k.cld;
     __syncthreads();
     for (int i = threadIdx.x; i < ld; i += kBlock) srv[i] = i < n ? k.rc[i] : 0.0f;
@@ -1341,13 +1390,94 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
       if (k.coarse) reduce_items<3>(k.cdots, k.cn, 0, k.cn, tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
-        if (!k.coarse) {
-          ds->inner_active = 0;  // not reached: split engines have a coarse space per member
-        } else if (ds->inner_active) {
-          const double rz = tot[0] + tot[2];
+        if (def_mixed && k.coarse && k.defl_ok && ds->defl) {
+          // deflated step length: p.P_d A p = p.q - r_c.x_c (r_c = P^T q); the update kernel
+          // makes the decisions and drives the loop
+          if (ds->inner_active) {
+            const double pw = ds->pq - tot[2];
+            ds->alpha = (pw > 0.0 && isfinite(pw)) ? ds->rz / pw : 0.0;
+          }
+        } else {
+          if (!k.coarse) {
+            ds->inner_active = 0;  // not reached: split engines have a coarse space per member
+          } else if (ds->inner_active) {
+            const double rz = tot[0] + tot[2];
+            const double alpha_d = ds->alpha;
+            ds->beta = ds->rz != 0.0 ? rz / ds->rz : 0.0;
+            ds->rz = rz;
+            ds->rr = tot[1];
+            ds->inner_it += 1;
+            ds->solve_iters += 1;
+            ds->cg_iters += 1;
+            const bool go = alpha_d != 0.0 && isfinite(tot[1]) && tot[1] > ds->inner_target &&
+                            ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
+            ds->inner_active = go ? 1 : 0;
+          }
+          instance_finished(v, i, 1, hc);
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+  }
+}
+
+// Additive form: z = D^-1 r + x_c[agg] on the unknowns (after the decisions of
+// k_coarse_gemv).  Deflated form: w = q - A P x_c, e^ += alpha p, r^ -= alpha w, t += alpha q,
+// z = D^-1 r^, with the dots and the CG decisions (last chunk of the instance).
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_z_form(EngineView v, cudaGraphConditionalHandle hc) {
+  __shared__ double sm[2 * kBlock / 32];
+  __shared__ int s_last;
+  for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
+    const Chunk c = v.chunks[item];
+    const KParams& k = v.inst[c.inst];
+    const bool active = coarse_active(k, 1);
+    P* rin = VecSel<P>::rin(k);
+    P* z = VecSel<P>::z(k);
+    const P* dinv = VecSel<P>::dinv(k);
+    if (!deflating<P>(k)) {
+      if (!active) continue;
+      for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+        const P di = dinv[a];
+        z[a] = di == P(0) ? P(0) : rin[a] * di + (P)k.xc[k.agg[a]];
+      }
+      continue;
+    }
+    double part[2] = {0.0, 0.0};
+    if constexpr (sizeof(P) == 4) {
+      if (active) {
+        const float* p = k.p32;
+        const float* q = k.q32;
+        float* e = k.e32;
+        float* t = k.t32;
+        const float alpha = (float)k.ds->alpha;
+        for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
+          const float di = dinv[a];
+          if (di == 0.0f) continue;
+          const float qa = q[a];
+          const float w = qa - ap_apply(k, a);
+          e[a] = e[a] + alpha * p[a];
+          const float r = rin[a] - alpha * w;
+          rin[a] = r;
+          t[a] = t[a] + alpha * qa;
+          const float zz = r * di;
+          z[a] = zz;
+          part[0] += (double)r * (double)zz;
+          part[1] += (double)r * (double)r;
+        }
+      }
+    }
+    write_partials<2>(v, item, part, sm);
+    if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
+      double tot[2];
+      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = k.ds;
+        if (ds->inner_active) {
           const double alpha_d = ds->alpha;
-          ds->beta = ds->rz != 0.0 ? rz / ds->rz : 0.0;
-          ds->rz = rz;
+          ds->beta = ds->rz != 0.0 ? tot[0] / ds->rz : 0.0;
+          ds->rz = tot[0];
           ds->rr = tot[1];
           ds->inner_it += 1;
           ds->solve_iters += 1;
@@ -1356,27 +1486,26 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
                           ds->inner_it < ds->max_iter && ds->solve_iters < ds->max_iter;
           ds->inner_active = go ? 1 : 0;
         }
-        instance_finished(v, i, 1, hc);
+        instance_finished(v, c.inst, 1, hc);
       }
-      __syncthreads();
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    __syncthreads();
   }
 }
 
-// z = D^-1 r + x_c[agg] on the unknowns (after the decisions of k_coarse_gemv)
-template <typename P>
-__global__ void __launch_bounds__(kBlock) k_z_form(EngineView v) {
+// Deflated solve, after the inner loop: e = e^ + Q (r0 - t).  Step 1 writes r0 - t into r
+// (restricted and solved next), step 2 adds P x_c.
+__global__ void __launch_bounds__(kBlock) k_def_final(EngineView v, int step) {
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
-    if (!coarse_active(k, 1)) continue;
-    const P* rin = VecSel<P>::rin(k);
-    P* z = VecSel<P>::z(k);
-    const P* dinv = VecSel<P>::dinv(k);
+    if (!deflating<float>(k) || !coarse_active(k, 0)) continue;
     for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
-      const P di = dinv[a];
-      z[a] = di == P(0) ? P(0) : rin[a] * di + (P)k.xc[k.agg[a]];
+      const bool unk = k.dinv32[a] != 0.0f;
+      if (step == 1)
+        k.rin32[a] = unk ? k.r0_32[a] - k.t32[a] : 0.0f;
+      else if (unk)
+        k.e32[a] = k.e32[a] + k.xc[k.agg[a]];
     }
   }
 }
@@ -1384,30 +1513,42 @@ __global__ void __launch_bounds__(kBlock) k_z_form(EngineView v) {
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphConditionalHandle hc, int init,
                                                      int fp64) {
-  __shared__ double sm[2 * kBlock / 32];
+  __shared__ double sm[3 * kBlock / 32];
   __shared__ int s_last;
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
     const bool active = coarse_active(k, init ? 0 : 1);
-    double part[2] = {0.0, 0.0};
+    double part[3] = {0.0, 0.0, 0.0};
     if (active) {
-      const P* rin = VecSel<P>::rin(k);
+      P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
       const P* dinv = VecSel<P>::dinv(k);
+      // deflated start (mixed, operator fresh): r^ = r - A P x_c, z = D^-1 r^
+      const bool def = init && deflating<P>(k);
       for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
         const P di = dinv[a];
-        const P r = rin[a];
-        const P zz = di == P(0) ? P(0) : (k.coarse ? r * di + (P)k.xc[k.agg[a]] : r * di);
+        P r = rin[a];
+        part[2] += (double)r * (double)r;
+        P zz;
+        if (def) {
+          if (di != P(0)) {
+            r = r - (P)ap_apply(k, a);
+            rin[a] = r;
+          }
+          zz = r * di;
+        } else {
+          zz = di == P(0) ? P(0) : (k.coarse ? r * di + (P)k.xc[k.agg[a]] : r * di);
+        }
         z[a] = zz;
         part[0] += (double)r * (double)zz;
         part[1] += (double)r * (double)r;
       }
     }
-    write_partials<2>(v, item, part, sm);
+    write_partials<3>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
-      double tot[2];
-      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      double tot[3];
+      reduce_items<3>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (init) {
@@ -1417,8 +1558,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
             ds->beta = 0.0;
             ds->alpha = 0.0;
             ds->inner_it = 0;
+            // the reduction is relative to the correction equation's residual r (before
+            // the deflation), the stop test on the (deflated) iterated residual
             const double target = fp64 ? 0.25 * ds->tol * ds->tol * ds->bnorm2
-                                       : fmax(ds->inner_rel * ds->inner_rel * tot[1],
+                                       : fmax(ds->inner_rel * ds->inner_rel * tot[2],
                                               0.09 * ds->tol * ds->tol * ds->bnorm2);
             ds->inner_target = target;
             ds->inner_active = (tot[1] > target && ds->max_iter > 0) ? 1 : 0;
@@ -2164,6 +2307,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
           pnew = 0.0f;
           k.flip_step[a] = (int)(k.ds->steps + 1);
           k.ds->op_valid = 0;
+          k.ds->defl = 0;
         }
         record_history(k, a, k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0);
         const double g = next_phi_guess(k, a);
@@ -2335,6 +2479,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
         pnew = 0.0;
         k.flip_step[a] = (int)step_no;
         k.ds->op_valid = 0;
+        k.ds->defl = 0;
       }
       record_history(k, a, hslot);
       const double g = next_phi_guess(k, a);
@@ -2374,7 +2519,10 @@ __global__ void k_load_state(KParams k, const int* perm, const double* c_user, c
     if (dirichlet_phi && ((k.dirmask[a] >> S) & 1)) phi = k.bcval[(size_t)S * N + a];
     const float ph_old = mixed ? k.rec32_cur[a].phase : (float)k.rec64_cur[a].phase;
     const float ph = phase_user ? (phase_user[u] != 0 ? 1.0f : 0.0f) : ph_old;
-    if (ph != ph_old) k.ds->op_valid = 0;  // a new liquid mask: the prep recomputes the diagonal
+    if (ph != ph_old) {  // a new liquid mask: the prep recomputes the diagonal, no deflation
+      k.ds->op_valid = 0;
+      k.ds->defl = 0;
+    }
     k.phi64[a] = phi;
     k.phi_prev[a] = phi;
     if (mixed) {
@@ -2975,6 +3123,8 @@ nnpp_status launch_record_solve(Handle& h, int slot) {
 
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev) {
   NNPP_TRY(invalidate_operator(h));  // the adjoint solve's unknowns are those of step n
+  // the adjoint solves use the additive coarse correction (A P belongs to other phases)
+  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->defl, 0, sizeof(int), h.st));
   KParams kp = make_kparams(h, h.cur);
   k_adj_solve_setup<<<h.grid, kBlock, 0, h.st>>>(kp, snap, psi_prev);
   NNPP_CUDA(cudaGetLastError());
@@ -3101,7 +3251,7 @@ nnpp_status launch_coarse_z(const Engine& e, const EngineView& v, cudaStream_t s
   const int which = init ? 0 : 1;
   const int rg = std::max(1, std::min((nmax * 32 + kBlock - 1) / kBlock, e.sms * 8));
   k_coarse_restrict<P><<<rg, kBlock, 0, st>>>(v, which);
-  k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, which, 0, 0);
+  k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, which, 0, 0, 0);
   k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, init,
                                                                                sizeof(P) == 8 ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
@@ -3148,6 +3298,20 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   });
 }
 
+// after the inner loop of a mixed solve: the deflated CG's final correction e = e^ + Q (r0 - t)
+// (every kernel passes over instances that are not deflating)
+nnpp_status launch_cg_final_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
+  if (prec != NNPP_MIXED || !engine_coarse(e) || e.members.size() != 1) return NNPP_OK;
+  const int rg = std::max(1, std::min((cld_max(e) * 32 + kBlock - 1) / kBlock, e.sms * 8));
+  const int cg = occ_grid(k_def_final, 0, e.sms, v.nchunks);
+  k_def_final<<<cg, kBlock, 0, st>>>(v, 1);
+  k_coarse_restrict<float><<<rg, kBlock, 0, st>>>(v, 2);
+  k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 2, 0, 0, 1);
+  k_def_final<<<cg, kBlock, 0, st>>>(v, 2);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 // update fused with the restriction, coarse product, z and the dots
 template <typename P>
 nnpp_status launch_coarse_update(const Engine& e, const EngineView& v, cudaStream_t st, cudaGraphConditionalHandle hc) {
@@ -3158,11 +3322,11 @@ nnpp_status launch_coarse_update(const Engine& e, const EngineView& v, cudaStrea
   if (e.members.size() == 1) {
     // one instance: the dots come from the aggregates, the decisions from the coarse product's
     // last CTA, and z is a plain elementwise pass
-    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, hc, 1);
-    k_z_form<P><<<occ_grid(k_z_form<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
+    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, hc, 1, sizeof(P) == 4 ? 1 : 0);
+    k_z_form<P><<<occ_grid(k_z_form<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc);
   } else {
     // ensembles: per-instance reductions in parallel (the last chunk of each instance)
-    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, 0, 0);
+    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, 0, 0, 0);
     k_cg_zdots<P><<<occ_grid(k_cg_zdots<P>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, hc, 0, sizeof(P) == 8 ? 1 : 0);
   }
   NNPP_CUDA(cudaGetLastError());
@@ -3230,7 +3394,8 @@ nnpp_status step_alloc(Handle& h) {
             h.r64.alloc(N) && h.dsum64.alloc(N) && h.cpl64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
             h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
             h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N + 16) && h.p32.alloc(N) &&
-            h.q32.alloc(N) && h.e32.alloc(N) && h.freem.alloc(N) && h.phi4.alloc(N) && h.dstate.alloc(1) &&
+            h.q32.alloc(N) && h.e32.alloc(N) && h.r0_32.alloc(N) && h.t32.alloc(N) && h.freem.alloc(N) &&
+            h.phi4.alloc(N) && h.dstate.alloc(1) &&
             h.scratch_d.alloc(16 + 7 * 4096) && h.user_stage.alloc((S + 1) * N) &&
             h.user_stage_i.alloc(N);
   if (ok && h.warm_hist >= 3) ok = h.xh.alloc((size_t)h.warm_hist * N) && h.bh.alloc((size_t)h.warm_hist * N);
@@ -3325,6 +3490,8 @@ KParams make_kparams(Handle& h, int cur) {
   k.bh = h.warm_b_alt ? h.warm_b_alt : h.bh.get();
   const Coarse& co = h.coarse;
   k.coarse = (h.coarse_enabled && co.valid) ? 1 : 0;
+  k.defl_ok = 0;  // set by the engine for single-instance runs
+  k.pad_defl = 0;
   k.agg = co.agg.get();
   k.cinv = co.inv.get();
   k.rc = const_cast<float*>(co.rc.get());
@@ -3333,6 +3500,11 @@ KParams make_kparams(Handle& h, int cur) {
   k.cn = co.n;
   k.cld = co.ld;
   k.cdots = co.dots.get();
+  k.ap_ptr = co.ap_ptr.get();
+  k.ap_col = co.ap_col.get();
+  k.ap_val = co.ap_val.get();
+  k.r0_32 = h.r0_32.get();
+  k.t32 = h.t32.get();
   k.cf = co.f;
   k.cna0 = co.na[0];
   k.cna1 = co.na[1];
