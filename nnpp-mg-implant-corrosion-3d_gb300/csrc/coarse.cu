@@ -200,6 +200,9 @@ __global__ void k_phase_diff(KParams k, int mixed, const unsigned char* snap, in
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
 }
 
+// deflation flag from a phase comparison: on when no node differs from the operator's phases
+__global__ void k_defl_from_count(DevState* ds, const int* count) { ds->defl = *count == 0 ? 1 : 0; }
+
 }  // namespace
 
 Coarse::~Coarse() {
@@ -339,8 +342,10 @@ nnpp_status coarse_record_event(Handle& h, long long step) {
   const size_t nn = c.inv_elems();
   const size_t na = std::max<size_t>(c.ap_nnz, 1);
   ev.ap_nnz = c.ap_nnz;
-  if (!ev.inv.alloc(nn) || !ev.ap_ptr.alloc((size_t)h.N + 1) || !ev.ap_col.alloc(na) || !ev.ap_val.alloc(na))
+  if (!ev.inv.alloc(nn) || !ev.ap_ptr.alloc((size_t)h.N + 1) || !ev.ap_col.alloc(na) || !ev.ap_val.alloc(na) ||
+      !ev.snap.alloc(h.N))
     return set_error(NNPP_ERR_NOMEM, "recorded coarse operator");
+  NNPP_CUDA(cudaMemcpyAsync(ev.snap.get(), c.snap.get(), (size_t)h.N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.ap_ptr.get(), c.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.ap_col.get(), c.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
@@ -362,6 +367,7 @@ nnpp_status coarse_select(Handle& h, long long step, bool recompute) {
     NNPP_CUDA(cudaMemcpyAsync(c.ap_ptr.get(), ev.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
     NNPP_CUDA(cudaMemcpyAsync(c.ap_col.get(), ev.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
     NNPP_CUDA(cudaMemcpyAsync(c.ap_val.get(), ev.ap_val.get(), sizeof(float) * na, cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(c.snap.get(), ev.snap.get(), (size_t)h.N, cudaMemcpyDeviceToDevice, h.st));
     h.coarse_event_cur = e;
   }
   // recomputing the step the forward rebuilt the operator before: the deflation resumed there
@@ -369,6 +375,21 @@ nnpp_status coarse_select(Handle& h, long long step, bool recompute) {
     static const int kOn = 1;
     NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->defl, &kOn, sizeof(int), cudaMemcpyHostToDevice, h.st));
   }
+  return NNPP_OK;
+}
+
+nnpp_status coarse_defl_check(Handle& h) {
+  Coarse& c = h.coarse;
+  if (!h.coarse_enabled || !c.valid) {
+    NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->defl, 0, sizeof(int), h.st));
+    return NNPP_OK;
+  }
+  KParams kp = make_kparams(h, h.cur);
+  NNPP_CUDA(cudaMemsetAsync(c.count.get(), 0, sizeof(int), h.st));
+  k_phase_diff<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
+      kp, h.state_prec == NNPP_MIXED ? 1 : 0, c.snap.get(), c.count.get());
+  k_defl_from_count<<<1, 1, 0, h.st>>>(h.dstate.get(), c.count.get());
+  NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }
 

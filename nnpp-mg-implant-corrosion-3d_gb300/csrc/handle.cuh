@@ -178,6 +178,7 @@ struct Handle {
     DBuf<int> ap_ptr, ap_col;
     DBuf<float> ap_val;
     size_t ap_nnz = 0;
+    DBuf<unsigned char> snap;  // the phases it was built from
   };
   std::vector<CoarseEvent> coarse_events;
   bool coarse_record = false, coarse_replay = false;
@@ -224,6 +225,9 @@ nnpp_status coarse_record_event(Handle& h, long long step);
 // (relative to the start of forward_ckpt) in place; recompute: `step` is about to be
 // recomputed (a refresh recorded at it re-enables the deflation, as in the forward)
 nnpp_status coarse_select(Handle& h, long long step, bool recompute = false);
+// deflation on (device flag) exactly when the current phases are those of the installed
+// coarse operator (asynchronous; the adjoint solves)
+nnpp_status coarse_defl_check(Handle& h);
 
 // step.cu
 nnpp_status step_alloc(Handle& h);

@@ -3123,12 +3123,11 @@ nnpp_status launch_record_solve(Handle& h, int slot) {
 
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev) {
   NNPP_TRY(invalidate_operator(h));  // the adjoint solve's unknowns are those of step n
-  // the adjoint solves use the additive coarse correction (A P belongs to other phases)
-  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->defl, 0, sizeof(int), h.st));
   KParams kp = make_kparams(h, h.cur);
   k_adj_solve_setup<<<h.grid, kBlock, 0, h.st>>>(kp, snap, psi_prev);
   NNPP_CUDA(cudaGetLastError());
-  return NNPP_OK;
+  // deflated adjoint solve when the step's phases are those of the installed coarse operator
+  return coarse_defl_check(h);
 }
 
 nnpp_status launch_sum_c0(Handle& h, double* out) {
