@@ -220,9 +220,12 @@ nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict
 nnpp_status nnpp_set_warm_start(nnpp_handle* h, int history);
 
 /* Preconditioner of the potential CG (both precisions).  NNPP_PRECOND_TWO_LEVEL (the
- * default) adds to the Jacobi scaling a coarse correction on aggregates of f x f x f hash
- * bins (at most 3000 aggregates): the Galerkin coarse operator P^T A P of the phases,
- * inverted on the GPU and applied as one dense product per iteration.  It is rebuilt when
+ * default) adds to the Jacobi scaling a coarse space of aggregates of f x f x f hash bins (at
+ * most 3000 aggregates): the Galerkin coarse operator P^T A P of the phases, inverted on the
+ * GPU and applied as one dense product per iteration.  The mixed-precision inner CG of a
+ * single-instance run is deflated by that space while the coarse operator matches the
+ * phases, and adds the coarse correction to the Jacobi scaling otherwise (as the FP64 path
+ * and ensembles do).  It is rebuilt when
  * the state is replaced (nnpp_set_state, nnpp_reset) and, when refresh_every > 0 (default
  * 64), after every refresh_every steps counted from then if a phase has changed; backward
  * replays the rebuilds of forward_ckpt.  In an ensemble every member applies its own
