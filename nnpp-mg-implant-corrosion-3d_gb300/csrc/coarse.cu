@@ -113,19 +113,21 @@ __global__ void k_coarse_assemble(KParams k, const int* bin_start, int nb0, int 
 
 // Rows of A P off the diagonal term, for the deflated CG: for an unknown i and an aggregate
 // J, -sum of w_ij over the unknowns j of J (liquid, off the Dirichlet set).  Thread per node,
-// the 27 neighbour aggregates accumulated in fixed slots in the row's bond order; fill == 0
-// counts the touched slots into cnt, fill == 1 writes them in slot order from ptr.
-__global__ void k_ap_rows(KParams k, int mixed, int na0, int na1, int na2, int fill, int* cnt,
-                          const int* ptr, int* col, float* val) {
+// the 27 neighbour aggregates accumulated in fixed slots in the row's bond order.  fill == 0
+// takes the largest number of touched slots (kmax); fill == 1 writes them in slot order into
+// the K-slot layout col/val[s * N + i], the unused slots with value 0 (sliced like ELLPACK:
+// the threads of a warp read consecutive words).
+__global__ void k_ap_rows(KParams k, int mixed, int na0, int na1, int na2, int fill, int K, int* kmax,
+                          int* col, float* val) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k.N; i += gridDim.x * blockDim.x) {
     float acc[27];
     unsigned int touched = 0u;
 #pragma unroll
     for (int q = 0; q < 27; ++q) acc[q] = 0.0f;
     const bool unk = node_liquid(k, i, mixed) && !((k.dirmask[i] >> S) & 1);
+    const int I = k.agg[i];
+    const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
     if (unk) {
-      const int I = k.agg[i];
-      const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
       for (int j = k.row[i]; j < k.row[i + 1]; ++j) {
         const int m = k.col[j];
         if (!node_liquid(k, m, mixed) || ((k.dirmask[m] >> S) & 1)) continue;
@@ -140,20 +142,22 @@ __global__ void k_ap_rows(KParams k, int mixed, int na0, int na1, int na2, int f
       }
     }
     if (!fill) {
-      cnt[i] = __popc(touched);
+      const int c = __popc(touched);
+      if (c) atomicMax(kmax, c);
       continue;
     }
-    if (!touched) continue;
-    const int I = k.agg[i];
-    const int ax = I % na0, ay = (I / na0) % na1, az = I / (na0 * na1);
-    int o = ptr[i];
+    int o = 0;
 #pragma unroll
     for (int q = 0; q < 27; ++q)
       if ((touched >> q) & 1u) {
-        col[o] = (ax + q % 3 - 1) + na0 * ((ay + (q / 3) % 3 - 1) + na1 * (az + q / 9 - 1));
-        val[o] = acc[q];
+        col[(size_t)o * k.N + i] = (ax + q % 3 - 1) + na0 * ((ay + (q / 3) % 3 - 1) + na1 * (az + q / 9 - 1));
+        val[(size_t)o * k.N + i] = acc[q];
         ++o;
       }
+    for (; o < K; ++o) {
+      col[(size_t)o * k.N + i] = I;
+      val[(size_t)o * k.N + i] = 0.0f;
+    }
   }
 }
 
@@ -229,11 +233,11 @@ nnpp_status coarse_build(Handle& h) {
   // A P rows hold at most 27 aggregates each: allocated once, so that no pointer the
   // kernels hold changes when the operator is rebuilt or replayed
   if (!c.agg.alloc(h.N) || !c.inv.alloc(c.inv_elems()) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) ||
-      !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n) || !c.ap_ptr.alloc((size_t)h.N + 1) ||
-      !c.ap_col.alloc(27 * (size_t)h.N) || !c.ap_val.alloc(27 * (size_t)h.N))
+      !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n) || !c.ap_col.alloc(27 * (size_t)h.N) ||
+      !c.ap_val.alloc(27 * (size_t)h.N))
     return set_error(NNPP_ERR_NOMEM, "coarse space");
   NNPP_CUDA(cudaMemsetAsync(c.dots.get(), 0, sizeof(double) * 3 * (size_t)c.n, h.st));
-  c.ap_nnz = 0;
+  c.ap_k = 1;
   NNPP_CUDA(cudaMemsetAsync(c.inv.get(), 0, sizeof(float) * c.inv_elems(), h.st));  // padding stays 0
   k_agg_fill<<<std::max(1, std::min((L.nbins + 255) / 256, 4096)), 256, 0, h.st>>>(
       L.bin_start.get(), L.nb[0], L.nb[1], L.nb[2], f, c.na[0], c.na[1], c.agg.get());
@@ -288,22 +292,23 @@ nnpp_status coarse_refresh(Handle& h) {
   // x holds the last iterate; its symmetrised copy goes to c.inv (rows of stride ld)
   k_symmetrize<<<eg, 256, 0, h.st>>>(n, c.ld, x, c.inv.get());
   NNPP_CUDA(cudaGetLastError());
+  if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
   // A P for the deflated CG (the same phases as A_c)
   {
-    DBuf<int> cnt;
-    if (!cnt.alloc(h.N)) return set_error(NNPP_ERR_NOMEM, "A P rows");
     const int gb = std::max(1, std::min((h.N + 255) / 256, 152 * 16));
     const int mixed = h.state_prec == NNPP_MIXED ? 1 : 0;
-    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 0, cnt.get(), nullptr, nullptr, nullptr);
+    NNPP_CUDA(cudaMemsetAsync(c.count.get(), 0, sizeof(int), h.st));
+    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 0, 0, c.count.get(), nullptr, nullptr);
     NNPP_CUDA(cudaGetLastError());
-    long long nnz = 0;
-    NNPP_TRY(scan_ints(h.st, cnt.get(), c.ap_ptr.get(), h.N, &nnz));
-    c.ap_nnz = (size_t)nnz;  // at most 27 per node: within the arrays allocated at build
-    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 1, nullptr, c.ap_ptr.get(),
-                                    c.ap_col.get(), c.ap_val.get());
+    int K = 0;
+    NNPP_CUDA(cudaMemcpyAsync(&K, c.count.get(), sizeof(int), cudaMemcpyDeviceToHost, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+    c.ap_k = std::max(1, std::min(K, 27));  // at most 27: within the arrays allocated at build
+    k_ap_rows<<<gb, 256, 0, h.st>>>(kp, mixed, c.na[0], c.na[1], c.na[2], 1, c.ap_k, nullptr, c.ap_col.get(),
+                                    c.ap_val.get());
     NNPP_CUDA(cudaGetLastError());
   }
-  if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
+
   k_phase_snap<<<std::max(1, std::min((h.N + 255) / 256, 152 * 16)), 256, 0, h.st>>>(
       kp, h.state_prec == NNPP_MIXED ? 1 : 0, c.snap.get());
   NNPP_CUDA(cudaGetLastError());
@@ -340,14 +345,12 @@ nnpp_status coarse_record_event(Handle& h, long long step) {
   Handle::CoarseEvent& ev = h.coarse_events.back();
   ev.step = step;
   const size_t nn = c.inv_elems();
-  const size_t na = std::max<size_t>(c.ap_nnz, 1);
-  ev.ap_nnz = c.ap_nnz;
-  if (!ev.inv.alloc(nn) || !ev.ap_ptr.alloc((size_t)h.N + 1) || !ev.ap_col.alloc(na) || !ev.ap_val.alloc(na) ||
-      !ev.snap.alloc(h.N))
+  const size_t na = (size_t)c.ap_k * h.N;
+  ev.ap_k = c.ap_k;
+  if (!ev.inv.alloc(nn) || !ev.ap_col.alloc(na) || !ev.ap_val.alloc(na) || !ev.snap.alloc(h.N))
     return set_error(NNPP_ERR_NOMEM, "recorded coarse operator");
   NNPP_CUDA(cudaMemcpyAsync(ev.snap.get(), c.snap.get(), (size_t)h.N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.inv.get(), c.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
-  NNPP_CUDA(cudaMemcpyAsync(ev.ap_ptr.get(), c.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.ap_col.get(), c.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(ev.ap_val.get(), c.ap_val.get(), sizeof(float) * na, cudaMemcpyDeviceToDevice, h.st));
   return NNPP_OK;
@@ -361,10 +364,9 @@ nnpp_status coarse_select(Handle& h, long long step, bool recompute) {
     Coarse& c = h.coarse;
     const Handle::CoarseEvent& ev = h.coarse_events[e];
     const size_t nn = c.inv_elems();
-    const size_t na = std::max<size_t>(ev.ap_nnz, 1);
-    c.ap_nnz = ev.ap_nnz;
+    const size_t na = (size_t)ev.ap_k * h.N;
+    c.ap_k = ev.ap_k;
     NNPP_CUDA(cudaMemcpyAsync(c.inv.get(), ev.inv.get(), sizeof(float) * nn, cudaMemcpyDeviceToDevice, h.st));
-    NNPP_CUDA(cudaMemcpyAsync(c.ap_ptr.get(), ev.ap_ptr.get(), sizeof(int) * ((size_t)h.N + 1), cudaMemcpyDeviceToDevice, h.st));
     NNPP_CUDA(cudaMemcpyAsync(c.ap_col.get(), ev.ap_col.get(), sizeof(int) * na, cudaMemcpyDeviceToDevice, h.st));
     NNPP_CUDA(cudaMemcpyAsync(c.ap_val.get(), ev.ap_val.get(), sizeof(float) * na, cudaMemcpyDeviceToDevice, h.st));
     NNPP_CUDA(cudaMemcpyAsync(c.snap.get(), ev.snap.get(), (size_t)h.N, cudaMemcpyDeviceToDevice, h.st));

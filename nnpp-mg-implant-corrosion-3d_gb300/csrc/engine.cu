@@ -447,6 +447,7 @@ nnpp_status engine_run(Engine& e, int n_steps, int prec, bool prepared) {
         NNPP_TRY(coarse_check(*h));
         if (h->st != e.st) NNPP_CUDA(cudaStreamSynchronize(h->st));
       }
+      NNPP_TRY(refresh_params(e));  // a rebuilt operator may have another A P width
     }
   }
   if (e.members.size() > 1 || e.members[0]->st != e.st) NNPP_CUDA(cudaStreamSynchronize(e.st));

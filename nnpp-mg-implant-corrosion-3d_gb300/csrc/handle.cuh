@@ -75,12 +75,11 @@ struct KParams {
   int cn;                        // coarse unknowns
   int cld;                       // row stride of cinv
   double* cdots;                 // 3 cn: per-aggregate dot contributions
-  // deflated CG (mixed inner solves while k.ds->defl): A P without its diagonal term (CSR
-  // over nodes: aggregate, -sum of the weights to the unknowns of that aggregate), the
-  // correction equation's right-hand side r0 and t = A e
+  // deflated CG (mixed inner solves while k.ds->defl): A P without its diagonal term (ap_k
+  // slots per node, slot-major: aggregate, -sum of the weights to the unknowns of that
+  // aggregate), the correction equation's right-hand side r0 and t = A e
   int defl_ok;                   // single-instance engine (ensembles take the additive form)
-  int pad_defl;
-  const int* ap_ptr;
+  int ap_k;
   const int* ap_col;
   const float* ap_val;
   float* r0_32;
@@ -101,9 +100,9 @@ struct Coarse {
   DBuf<float> inv;    // n x ld: the coarse inverse (symmetric: row I = column I)
   DBuf<float> rc, xc; // n: restricted residual, coarse correction
   DBuf<double> dots;  // 3n: per aggregate r.D^-1 r and r.r of the update, r_c x_c of the product
-  DBuf<int> ap_ptr, ap_col;  // A P off its diagonal term (N + 1, 27 N capacity): see KParams
+  DBuf<int> ap_col;   // A P off its diagonal term (27 N capacity, ap_k used): see KParams
   DBuf<float> ap_val;
-  size_t ap_nnz = 0;
+  int ap_k = 1;
   DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
   DBuf<float> a, t, x, y; // n x n: A_c and the Newton-Schulz work matrices
   size_t inv_elems() const { return (size_t)n * ld; }
@@ -175,9 +174,9 @@ struct Handle {
   struct CoarseEvent {
     long long step = 0;
     DBuf<float> inv;
-    DBuf<int> ap_ptr, ap_col;
+    DBuf<int> ap_col;
     DBuf<float> ap_val;
-    size_t ap_nnz = 0;
+    int ap_k = 1;
     DBuf<unsigned char> snap;  // the phases it was built from
   };
   std::vector<CoarseEvent> coarse_events;

@@ -1213,7 +1213,10 @@ __device__ __forceinline__ bool deflating(const KParams& k) {
 // from the stored rows
 __device__ __forceinline__ float ap_apply(const KParams& k, int i) {
   float s = k.d32[i] * k.xc[k.agg[i]];
-  for (int kk = k.ap_ptr[i]; kk < k.ap_ptr[i + 1]; ++kk) s = fmaf(k.ap_val[kk], k.xc[k.ap_col[kk]], s);
+  for (int q = 0; q < k.ap_k; ++q) {
+    const size_t o = (size_t)q * k.N + i;
+    s = fmaf(k.ap_val[o], k.xc[k.ap_col[o]], s);
+  }
   return s;
 }
 
@@ -3490,7 +3493,6 @@ KParams make_kparams(Handle& h, int cur) {
   const Coarse& co = h.coarse;
   k.coarse = (h.coarse_enabled && co.valid) ? 1 : 0;
   k.defl_ok = 0;  // set by the engine for single-instance runs
-  k.pad_defl = 0;
   k.agg = co.agg.get();
   k.cinv = co.inv.get();
   k.rc = const_cast<float*>(co.rc.get());
@@ -3499,7 +3501,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.cn = co.n;
   k.cld = co.ld;
   k.cdots = co.dots.get();
-  k.ap_ptr = co.ap_ptr.get();
+  k.ap_k = co.ap_k;
   k.ap_col = co.ap_col.get();
   k.ap_val = co.ap_val.get();
   k.r0_32 = h.r0_32.get();
