@@ -117,6 +117,62 @@ __device__ __forceinline__ void two_sum_d(double a, double b, double& s, double&
   e = (a - (s - bb)) + (b - bb);
 }
 
+// (hi, lo) += a * b on FP32 pairs: the product's rounding error from an FMA, the sum's
+// from TwoSum.  A dot product accumulated this way is as accurate as an FP64 one and runs
+// on the FP32 pipes (the GB300's FP64 rate is a small fraction of its FP32 rate).
+__device__ __forceinline__ void pair_fma(float& hi, float& lo, float a, float b) {
+  const float p = a * b;
+  const float pe = fmaf(a, b, -p);
+  float s, e;
+  two_sum(hi, p, s, e);
+  hi = s;
+  lo += e + pe;
+}
+
+// warp sum of FP32 pairs (hi, lo) with TwoSum at each level; lane 0 holds the pair sum to
+// ~2^-48 relative (as good as an FP64 sum of 32 terms, on the FP32 pipes)
+__device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, hi, off);
+    const float ol = __shfl_down_sync(0xffffffffu, lo, off);
+    float sum, err;
+    two_sum(hi, oh, sum, err);
+    hi = sum;
+    lo = lo + ol + err;
+  }
+}
+
+// Sum of products a*b of one thread: FP64 on the FP64 path, FP32 pairs on the FP32 path.
+template <typename P>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s += a * b; }
+  __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) { pair_fma(hi, lo, a, b); }
+  // += (ah + al) * (bh + bl), the product of two pairs to ~2^-46 relative
+  __device__ __forceinline__ void add_pair(float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    const float pe = fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
+    float s, e;
+    two_sum(hi, p, s, e);
+    hi = s;
+    lo += e + pe;
+  }
+  __device__ __forceinline__ void warp_sum() { pair_warp_sum(hi, lo); }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // Compensated reduction of (value, error) pairs over `width` lanes of a warp segment.
 template <int WIDTH>
 __device__ __forceinline__ float comp_reduce(float v) {

@@ -141,6 +141,41 @@ __device__ __forceinline__ void write_partials(const EngineView& v, int item, do
     for (int k = 0; k < NV; ++k) v.partials[(size_t)k * v.stride + item] = part[k];
 }
 
+// Item partials of per-thread dot accumulators: FP64 block sums on the FP64 path; on the
+// FP32 path FP32-pair warp sums, then warp 0 sums the warps' pairs (sm: NV * kBlock / 32
+// doubles, reused as pairs).  Thread 0 writes the FP64 partials.
+template <int NV, typename P>
+__device__ __forceinline__ void write_dot_partials(const EngineView& v, int item, DotAcc<P> (&acc)[NV], double* sm) {
+  if constexpr (sizeof(P) == 8) {
+    double part[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) part[q] = acc[q].s;
+    write_partials<NV>(v, item, part, sm);
+  } else {
+    float2* smf = reinterpret_cast<float2*>(sm);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      acc[q].warp_sum();
+      if (lane == 0) smf[q * (kBlock / 32) + wid] = make_float2(acc[q].hi, acc[q].lo);
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        DotAcc<float> t;
+        if (lane < kBlock / 32) {
+          t.hi = smf[q * (kBlock / 32) + lane].x;
+          t.lo = smf[q * (kBlock / 32) + lane].y;
+        }
+        t.warp_sum();
+        if (lane == 0) v.partials[(size_t)q * v.stride + item] = t.value();
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <typename P>
 struct VecSel;
 template <>
@@ -211,6 +246,37 @@ __device__ __forceinline__ void pair_add(float& sh, float& sl, float ah, float a
 __device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
   ph = ah * bh;
   pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
+}
+// FP32 pair (hi, lo) of a double by bit manipulation, with no FP64 arithmetic: hi keeps the
+// leading 24 significant bits (truncated), lo the rest rounded to 24 bits, so that
+// |t - hi - lo| <= 2^-48 |t|.  Zero and subnormals give (0, 0); magnitudes outside
+// [2^-60, 2^100) and non-finite values take the FP64 conversion.
+__device__ __forceinline__ void split_pair(double t, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  if (e == 0) {
+    hi = lo = 0.0f;
+    return;
+  }
+  if (e < 1023 - 60 || e >= 1023 + 100) {
+    hi = (float)t;
+    lo = isfinite(hi) ? (float)(t - (double)hi) : 0.0f;
+    return;
+  }
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29));
+  const float r = (float)(unsigned int)(m & 0x1fffffffu) * 0x1p-29f;            // in [0, 1)
+  const float sc = __uint_as_float((unsigned int)(e - 1023 - 23 + 127) << 23);  // 2^(E-23)
+  lo = __uint_as_float(__float_as_uint(r * sc) | sign);
+}
+// (ah, al) - (bh, bl), renormalised (|lo| <= half an ulp of hi)
+__device__ __forceinline__ void pair_sub(float ah, float al, float bh, float bl, float& dh, float& dl) {
+  float s, e;
+  two_sum(ah, -bh, s, e);
+  e += al - bl;
+  dh = s + e;
+  dl = e - (dh - s);
 }
 // sum of pairs over the W lanes of a node's segment (lane 0 of the segment holds it)
 template <int WIDTH>
@@ -416,7 +482,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
     const bool active = *((volatile int*)&k.ds->outer_active) != 0;
-    double part[2] = {0.0, 0.0};
+    DotAcc<P> part[2];
     if (split) {
       // two-level preconditioner: r, p, q, e here; z and the dots after the coarse solve
       if (active) {
@@ -452,11 +518,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
         p[a] = P(0);
         q[a] = P(0);
         e[a] = P(0);
-        part[0] += (double)r * (double)zz;
-        part[1] += (double)r * (double)r;
+        part[0].add(r, zz);
+        part[1].add(r, r);
       }
     }
-    write_partials<2>(v, item, part, sm);
+    write_dot_partials<2, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
       reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
@@ -500,19 +566,6 @@ __device__ __forceinline__ double warp_sum_d(double x) {
   return x;
 }
 
-// warp sum of FP32 pairs (hi, lo) with TwoSum at each level; lane 0 holds the pair sum to
-// ~2^-48 relative (as good as an FP64 sum of 32 terms, on the FP32 pipes)
-__device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const float oh = __shfl_down_sync(0xffffffffu, hi, off);
-    const float ol = __shfl_down_sync(0xffffffffu, lo, off);
-    float sum, err;
-    two_sum(hi, oh, sum, err);
-    hi = sum;
-    lo = lo + ol + err;
-  }
-}
 
 // Interleaved sliced operator: bond column c of a slice holds 32 FP32 weights then 32 16-bit
 // slot codes (kSellW floats = 192 bytes), so one contiguous copy moves both.
@@ -592,7 +645,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    double part = 0.0;
+    DotAcc<float> part;
     if (slice_active(v, sg)) {
       if (WIN) {
         // the window (z of the 9 window rows, 16-byte aligned row segments) by 16-byte
@@ -681,13 +734,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
           const float pn = za + beta * k.p32[a];
           k.q32[a] = qn;
           k.p32[a] = pn;
-          part = (double)pn * (double)qn;
+          part.add(pn, qn);
         }
       }
       __syncwarp();
     }
-    part = warp_sum_d(part);
-    if (lane == 0) v.partials[sg] = part;
+    part.warp_sum();
+    if (lane == 0) v.partials[sg] = part.value();
   }
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
@@ -811,7 +864,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
   for (int sg = s0; sg < s1; ++sg) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    double part = 0.0;
+    DotAcc<float> part;
     if (slice_active(v, sg)) {
       // the next slice's window goes to the other buffer (free: its slice is done), then
       // this slice's window (the older commit group) is waited for
@@ -861,13 +914,13 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
         const float pn = za + beta * pa;
         k.q32[a] = qn;
         k.p32[a] = pn;
-        part = (double)pn * (double)qn;
+        part.add(pn, qn);
       }
       __syncwarp();
       wb ^= 1;
     }
-    part = warp_sum_d(part);
-    if (lane == 0) v.partials[sg] = part;
+    part.warp_sum();
+    if (lane == 0) v.partials[sg] = part.value();
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   if (timed_out >= 0 && lane == 0) v.inst[timed_out].ds->wait_timeout = 1;
@@ -1038,7 +1091,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32s(EngineView v, int stag
           cis = 0;
         }
       }
-      double part = 0.0;
+      DotAcc<float> part;
       if (live) {
         const float sa = dd * za - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
         const float beta = (float)k.ds->beta;
@@ -1046,12 +1099,12 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32s(EngineView v, int stag
         const float pn = za + beta * pa;
         k.q32[a] = qn;
         k.p32[a] = pn;
-        part = (double)pn * (double)qn;
+        part.add(pn, qn);
       }
       __syncwarp();
       wb ^= 1;
-      part = warp_sum_d(part);
-      if (lane == 0) v.partials[sg] = part;
+      part.warp_sum();
+      if (lane == 0) v.partials[sg] = part.value();
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
@@ -1144,7 +1197,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
     const bool active = *((volatile int*)&k.ds->inner_active) != 0;
-    double part[2] = {0.0, 0.0};
+    DotAcc<P> part[2];
     if (active) {
       P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
@@ -1162,11 +1215,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
         e[a] = ee;
         rin[a] = r;
         z[a] = zz;
-        part[0] += (double)r * (double)zz;
-        part[1] += (double)r * (double)r;
+        part[0].add(r, zz);
+        part[1].add(r, r);
       }
     }
-    write_partials<2>(v, item, part, sm);
+    write_dot_partials<2, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
       reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
@@ -1287,7 +1340,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
         continue;
       }
       float acc = 0.0f;
-      double rzf = 0.0, rr = 0.0;  // r.D^-1 r and r.r of the aggregate's nodes
+      DotAcc<P> rzf, rr;  // r.D^-1 r and r.r of the aggregate's nodes
       for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
         for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
           // the aggregate's bins along x are one contiguous node range
@@ -1305,30 +1358,28 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
               e[i] = e0 + alpha * p0;
               r0 = r0 - alpha * q0;
               rin[i] = r0;
-              rzf += (double)r0 * (double)(r0 * d0);
-              rr += (double)r0 * (double)r0;
+              rzf.add(r0, r0 * d0);
+              rr.add(r0, r0);
             }
             acc += (float)r0;
             if (d1 != P(0)) {
               e[i + 32] = e1 + alpha * p1;
               r1 = r1 - alpha * q1;
               rin[i + 32] = r1;
-              rzf += (double)r1 * (double)(r1 * d1);
-              rr += (double)r1 * (double)r1;
+              rzf.add(r1, r1 * d1);
+              rr.add(r1, r1);
             }
             acc += (float)r1;
           }
         }
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        acc += __shfl_down_sync(0xffffffffu, acc, off);
-        rzf += __shfl_down_sync(0xffffffffu, rzf, off);
-        rr += __shfl_down_sync(0xffffffffu, rr, off);
-      }
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+      rzf.warp_sum();
+      rr.warp_sum();
       if (lane == 0) {
         k.rc[I] = acc;
-        k.cdots[I] = rzf;
-        k.cdots[k.cn + I] = rr;
+        k.cdots[I] = rzf.value();
+        k.cdots[k.cn + I] = rr.value();
       }
     }
   }
@@ -1390,10 +1441,18 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
     for (int i = 0; i < v.M; ++i) {
       const KParams& k = v.inst[i];
       double tot[3] = {0.0, 0.0, 0.0};
-      if (k.coarse) reduce_items<3>(k.cdots, k.cn, 0, k.cn, tot, sm);
+      // the deflated iteration needs only r_c.x_c (the update kernel forms the dots)
+      const bool dm = def_mixed && k.coarse && k.defl_ok && *((volatile const int*)&k.ds->defl) != 0;
+      if (dm) {
+        double t2[1];
+        reduce_items<1>(k.cdots + 2 * (size_t)k.cn, k.cn, 0, k.cn, t2, sm);
+        tot[2] = t2[0];
+      } else if (k.coarse) {
+        reduce_items<3>(k.cdots, k.cn, 0, k.cn, tot, sm);
+      }
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
-        if (def_mixed && k.coarse && k.defl_ok && ds->defl) {
+        if (dm) {
           // deflated step length: p.P_d A p = p.q - r_c.x_c (r_c = P^T q); the update kernel
           // makes the decisions and drives the loop
           if (ds->inner_active) {
@@ -1447,7 +1506,7 @@ __global__ void __launch_bounds__(kBlock) k_z_form(EngineView v, cudaGraphCondit
       }
       continue;
     }
-    double part[2] = {0.0, 0.0};
+    DotAcc<float> part[2];
     if constexpr (sizeof(P) == 4) {
       if (active) {
         const float* p = k.p32;
@@ -1466,12 +1525,12 @@ __global__ void __launch_bounds__(kBlock) k_z_form(EngineView v, cudaGraphCondit
           t[a] = t[a] + alpha * qa;
           const float zz = r * di;
           z[a] = zz;
-          part[0] += (double)r * (double)zz;
-          part[1] += (double)r * (double)r;
+          part[0].add(r, zz);
+          part[1].add(r, r);
         }
       }
     }
-    write_partials<2>(v, item, part, sm);
+    write_dot_partials<2, float>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
       reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
@@ -1522,7 +1581,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
     const bool active = coarse_active(k, init ? 0 : 1);
-    double part[3] = {0.0, 0.0, 0.0};
+    DotAcc<P> part[3];
     if (active) {
       P* rin = VecSel<P>::rin(k);
       P* z = VecSel<P>::z(k);
@@ -1532,7 +1591,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
       for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
         const P di = dinv[a];
         P r = rin[a];
-        part[2] += (double)r * (double)r;
+        part[2].add(r, r);
         P zz;
         if (def) {
           if (di != P(0)) {
@@ -1544,11 +1603,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
           zz = di == P(0) ? P(0) : (k.coarse ? r * di + (P)k.xc[k.agg[a]] : r * di);
         }
         z[a] = zz;
-        part[0] += (double)r * (double)zz;
-        part[1] += (double)r * (double)r;
+        part[0].add(r, zz);
+        part[1].add(r, r);
       }
     }
-    write_partials<3>(v, item, part, sm);
+    write_dot_partials<3, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[3];
       reduce_items<3>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
@@ -1608,17 +1667,6 @@ __device__ __forceinline__ int warm_history(const KParams& k) {
   return n < k.hist_m ? n : k.hist_m;
 }
 
-// backward differences D^1..D^{H-1} of t[0..H-1] (newest first) into d; t is consumed
-__device__ __forceinline__ void warm_diffs(double (&t)[kHistMax], int H, double (&d)[kWarmD]) {
-#pragma unroll
-  for (int l = 1; l < kHistMax; ++l) {
-#pragma unroll
-    for (int j = 0; j + 1 < kHistMax; ++j)
-      if (j + l < H) t[j] -= t[j + 1];
-    d[l - 1] = l < H ? t[0] : 0.0;
-  }
-}
-
 // Solve the scaled Galerkin system by Cholesky; differences whose pivot falls below 1e-12
 // (near-dependent) or whose A-norm is below 1e-12 of the solution's (rounding level) end
 // the basis.  Thread 0 of one CTA.
@@ -1664,6 +1712,33 @@ __device__ void warm_solve(const double (&tot)[kWarmSlots], int nd, DevState* ds
   ds->warm_nd = ok ? m : 0;
 }
 
+// backward differences D^1..D^{H-1} of the FP32 pairs t[0..H-1] (newest first) into d;
+// t is consumed
+__device__ __forceinline__ void pair_warm_diffs(float (&th)[kHistMax], float (&tl)[kHistMax], int H,
+                                                float (&dh)[kWarmD], float (&dl)[kWarmD]) {
+#pragma unroll
+  for (int l = 1; l < kHistMax; ++l) {
+#pragma unroll
+    for (int j = 0; j + 1 < kHistMax; ++j)
+      if (j + l < H) pair_sub(th[j], tl[j], th[j + 1], tl[j + 1], th[j], tl[j]);
+    dh[l - 1] = l < H ? th[0] : 0.0f;
+    dl[l - 1] = l < H ? tl[0] : 0.0f;
+  }
+}
+
+// the history of node a as FP32 pairs, newest first (zero beyond H)
+__device__ __forceinline__ void load_history_pairs(const double* ring, const int (&slot)[kHistMax], int H,
+                                                   size_t N, int a, float (&th)[kHistMax], float (&tl)[kHistMax]) {
+#pragma unroll
+  for (int j = 0; j < kHistMax; ++j) {
+    th[j] = tl[j] = 0.0f;
+    if (j < H) split_pair(ring[(size_t)slot[j] * N + a], th[j], tl[j]);
+  }
+}
+
+// The Galerkin system's dot products, on FP32 pairs (the FP64 rate of the GB300 would
+// bound this pass): the history is split into pairs, differenced and multiplied with the
+// pair operations, ~2^-46 relative per operation.
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
   __shared__ double sm[kWarmSlots * kBlock / 32];
@@ -1672,46 +1747,60 @@ __global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
     const int H = warm_history(k);
-    double part[kWarmSlots];
-#pragma unroll
-    for (int q = 0; q < kWarmSlots; ++q) part[q] = 0.0;
+    DotAcc<float> part[kWarmSlots];
     if (H >= 3) {
       const int head = k.ds->hist_head, m = k.hist_m;
       const size_t N = (size_t)k.N;
+      int slot[kHistMax];
+#pragma unroll
+      for (int j = 0; j < kHistMax; ++j) slot[j] = (head - j + 2 * m) % m;
+      float lamh, laml, zh[S], zl[S];
+      split_pair(k.lam, lamh, laml);
+#pragma unroll
+      for (int s2 = 0; s2 < S; ++s2) split_pair(k.z[s2], zh[s2], zl[s2]);
       for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
         if (!k.freem[a]) continue;
-        double tx[kHistMax], tb[kHistMax];
-#pragma unroll
-        for (int j = 0; j < kHistMax; ++j) {
-          const size_t o = (size_t)((head - j + 2 * m) % m) * N + a;
-          tx[j] = j < H ? k.xh[o] : 0.0;
-          tb[j] = j < H ? k.bh[o] : 0.0;
-        }
-        double bn;
+        float xh[kHistMax], xl[kHistMax], bh[kHistMax], bl[kHistMax];
+        load_history_pairs(k.xh, slot, H, N, a, xh, xl);
+        load_history_pairs(k.bh, slot, H, N, a, bh, bl);
+        float bnh, bnl;
         if (k.b_override) {
-          bn = k.b_override[a];  // adjoint solves: the given right-hand side
+          split_pair(k.b_override[a], bnh, bnl);  // adjoint solves: the given right-hand side
         } else {
-          double R11 = 0.0;
+          // b = lam sum_s z_s c_s
+          float rh = 0.0f, rl = 0.0f;
 #pragma unroll
-          for (int s2 = 0; s2 < S; ++s2) R11 += k.z[s2] * conc_of<P>(k, a, s2);
-          bn = k.lam * R11;
+          for (int s2 = 0; s2 < S; ++s2) {
+            float ch, cl, ph, pl;
+            if constexpr (sizeof(P) == 4) {
+              const float4 lo4 = k.clo[a];
+              ch = k.rec32_cur[a].c[s2];
+              cl = sel4(lo4, s2);
+            } else {
+              split_pair(k.rec64_cur[a].c[s2], ch, cl);
+            }
+            pair_mul(zh[s2], zl[s2], ch, cl, ph, pl);
+            pair_add(rh, rl, ph, pl);
+          }
+          pair_mul(lamh, laml, rh, rl, bnh, bnl);
         }
-        const double g = bn - tb[0];
-        const double xax = tx[0] * tb[0];
-        double dx[kWarmD], db[kWarmD];
-        warm_diffs(tx, H, dx);
-        warm_diffs(tb, H, db);
+        float gh, gl;
+        pair_sub(bnh, bnl, bh[0], bl[0], gh, gl);
+        const float x0h = xh[0], x0l = xl[0], b0h = bh[0], b0l = bl[0];
+        float dxh[kWarmD], dxl[kWarmD], dbh[kWarmD], dbl[kWarmD];
+        pair_warm_diffs(xh, xl, H, dxh, dxl);
+        pair_warm_diffs(bh, bl, H, dbh, dbl);
         int q = 0;
 #pragma unroll
         for (int i = 0; i < kWarmD; ++i)
 #pragma unroll
-          for (int j = i; j < kWarmD; ++j) part[q++] += dx[i] * db[j];
+          for (int j = i; j < kWarmD; ++j) part[q++].add_pair(dxh[i], dxl[i], dbh[j], dbl[j]);
 #pragma unroll
-        for (int i = 0; i < kWarmD; ++i) part[q++] += dx[i] * g;
-        part[q] += xax;
+        for (int i = 0; i < kWarmD; ++i) part[q++].add_pair(dxh[i], dxl[i], gh, gl);
+        part[q].add_pair(x0h, x0l, b0h, b0l);
       }
     }
-    write_partials<kWarmSlots>(v, item, part, sm);
+    write_dot_partials<kWarmSlots, float>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[kWarmSlots];
       reduce_items<kWarmSlots>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
@@ -1736,6 +1825,7 @@ __global__ void k_record_solve(KParams k, int slot) {
 }
 
 // x0 = x_n + sum_l a_l D^l x_n on the unknowns, into phi64 and the state's potential
+// (FP32-pair arithmetic as k_warm_dots; x0 is exact in FP64 as the sum of its pair)
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_warm_apply(EngineView v) {
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
@@ -1745,25 +1835,39 @@ __global__ void __launch_bounds__(kBlock) k_warm_apply(EngineView v) {
     if (H < 3) continue;
     const int nd = k.ds->warm_nd;
     if (nd <= 0) continue;
-    double coef[kWarmD];
+    float ch[kWarmD], cl[kWarmD];
 #pragma unroll
-    for (int i = 0; i < kWarmD; ++i) coef[i] = k.ds->warm_coef[i];
+    for (int i = 0; i < kWarmD; ++i) split_pair(k.ds->warm_coef[i], ch[i], cl[i]);
     const int head = k.ds->hist_head, m = k.hist_m;
     const size_t N = (size_t)k.N;
+    int slot[kHistMax];
+#pragma unroll
+    for (int j = 0; j < kHistMax; ++j) slot[j] = (head - j + 2 * m) % m;
     for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
       if (!k.freem[a]) continue;
-      double tx[kHistMax];
+      float th[kHistMax], tl[kHistMax];
+      load_history_pairs(k.xh, slot, H, N, a, th, tl);
+      const float xh0 = th[0], xl0 = tl[0];
+      float dh[kWarmD], dl[kWarmD];
+      pair_warm_diffs(th, tl, H, dh, dl);
+      float sh = 0.0f, sl = 0.0f;
 #pragma unroll
-      for (int j = 0; j < kHistMax; ++j)
-        tx[j] = j < H ? k.xh[(size_t)((head - j + 2 * m) % m) * N + a] : 0.0;
-      const double x = tx[0];
-      double dx[kWarmD];
-      warm_diffs(tx, H, dx);
-      double x0 = x;
-#pragma unroll
-      for (int i = 0; i < kWarmD; ++i) x0 += coef[i] * dx[i];
-      k.phi64[a] = x0;
-      set_phi_rec(k, a, x0, sizeof(P) == 4);
+      for (int i = 0; i < kWarmD; ++i) {
+        float ph, pl;
+        pair_mul(ch[i], cl[i], dh[i], dl[i], ph, pl);
+        pair_add(sh, sl, ph, pl);
+      }
+      pair_add(sh, sl, xh0, xl0);
+      // normalised pair: hi the FP32 rounding of the sum, lo its exact remainder
+      const float hi = sh + sl;
+      const float lo = sl - (hi - sh);
+      k.phi64[a] = (double)hi + (double)lo;
+      if constexpr (sizeof(P) == 4) {
+        k.rec32_cur[a].phi_hi = hi;
+        k.rec32_cur[a].phi_lo = lo;
+      } else {
+        k.rec64_cur[a].phi = (double)hi + (double)lo;
+      }
     }
   }
 }
