@@ -7,10 +7,12 @@
 // as dense n x n FP32 matrices (n <= kCoarseMax).  The inverse comes from the Newton-Schulz
 // iteration X <- X (2I - A_c X), X_0 = I / ||A_c||_inf (every iterate is a positive
 // polynomial of A_c, so the preconditioner stays symmetric positive definite even when the
-// iteration is stopped early), on cuBLAS SGEMM.  The coarse operator is rebuilt when the
-// state is replaced, and every `coarse_every` steps (counted from the last replacement) if a
-// phase changed since the last rebuild; in between a stale one is still a valid
-// preconditioner.  The schedule depends only on the step count and the phases, so it is
+// iteration is stopped early), on cuBLAS SGEMM.  A periodic rebuild within a run starts
+// instead from the previous inverse when ||I - A_c X_0||_F < 1/2: the error then squares
+// every step, and a few steps replace the 18 of the cold start.  The coarse operator is
+// rebuilt when the state is replaced, and every `coarse_every` steps (counted from the last
+// replacement) if a phase changed since the last rebuild; in between a stale one is still a
+// valid preconditioner.  The schedule depends only on the step count and the phases, so it is
 // reproducible, and forward_ckpt records each rebuilt inverse for backward to replay.
 #include <algorithm>
 #include <cmath>
@@ -25,6 +27,30 @@ namespace nnpp {
 namespace {
 
 constexpr int kNsIterations = 18;
+constexpr int kNormBlocks = 128;      // block partials of the warm start's residual norm
+constexpr double kNsWarmMax = 0.5;    // warm start when ||I - A_c X_0||_F is below this
+constexpr double kNsTarget = 1e-8;    // warm start: steps until the bound ||.||^(2^m) meets this
+
+// block partials of ||I - T||_F^2 (T n x n): FP32 sums per thread, FP64 across the block
+__global__ void k_resid_sq(int n, const float* T, double* partials) {
+  __shared__ double sm[256 / 32];
+  const size_t nn = (size_t)n * n;
+  float s = 0.0f;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+    const float d = ((e / n == e % n) ? 1.0f : 0.0f) - T[e];
+    s = fmaf(d, d, s);
+  }
+  double x = s;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 256 / 32; ++w) t += sm[w];
+    partials[blockIdx.x] = t;
+  }
+}
 
 // aggregate of every node (internal order), from the bins' node ranges
 __global__ void k_agg_fill(const int* bin_start, int nb0, int nb1, int nb2, int f, int na0, int na1,
@@ -270,17 +296,47 @@ nnpp_status coarse_refresh(Handle& h) {
       h.state_prec == NNPP_MIXED ? 1 : 0, A.get(), c.rowabs.get());
   NNPP_CUDA(cudaGetLastError());
   const int eg = (int)std::min<size_t>((nn + 255) / 256, 152 * 64);
-  k_ns_init<<<eg, 256, 0, h.st>>>(n, c.rowabs.get(), X.get());
-  NNPP_CUDA(cudaGetLastError());
   cublasHandle_t hb = static_cast<cublasHandle_t>(c.cublas);
   if (cublasSetStream(hb, h.st) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasSetStream");
   const float one = 1.0f, zero = 0.0f;
   float* x = X.get();
   float* y = c.y.get();
-  for (int it = 0; it < kNsIterations; ++it) {
-    // T = A X ; T = 2I - T ; X <- X T
+  // a rebuild within a run (phases changed since the last one, the state not replaced)
+  // starts from the last inverse if it is close enough: T = A X_0 is then the first step's
+  // product already.  The residual norm is summed on the host in block order, so the
+  // number of steps is reproducible.
+  int steps = kNsIterations;
+  bool warm = false;
+  if (c.valid && !c.stale && h.coarse_event_cur < 0) {
+    if (!c.nrm.alloc(kNormBlocks)) return set_error(NNPP_ERR_NOMEM, "coarse inverse");
+    NNPP_CUDA(cudaMemcpy2DAsync(x, sizeof(float) * n, c.inv.get(), sizeof(float) * c.ld, sizeof(float) * n, n,
+                                cudaMemcpyDeviceToDevice, h.st));
     if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
         CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    k_resid_sq<<<kNormBlocks, 256, 0, h.st>>>(n, T.get(), c.nrm.get());
+    NNPP_CUDA(cudaGetLastError());
+    std::vector<double> part(kNormBlocks);
+    NNPP_CUDA(cudaMemcpyAsync(part.data(), c.nrm.get(), sizeof(double) * kNormBlocks, cudaMemcpyDeviceToHost, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+    double ss = 0.0;
+    for (double v : part) ss += v;
+    const double r0 = std::sqrt(ss);
+    if (std::isfinite(r0) && r0 < kNsWarmMax) {
+      warm = true;
+      steps = 1;
+      while (steps < kNsIterations && std::pow(r0, std::ldexp(1.0, steps)) > kNsTarget) ++steps;
+    }
+  }
+  if (!warm) {
+    k_ns_init<<<eg, 256, 0, h.st>>>(n, c.rowabs.get(), X.get());
+    NNPP_CUDA(cudaGetLastError());
+  }
+  for (int it = 0; it < steps; ++it) {
+    // T = A X ; T = 2I - T ; X <- X T
+    if (!(warm && it == 0) &&
+        cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
+            CUBLAS_STATUS_SUCCESS)
       return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
     k_two_i_minus<<<eg, 256, 0, h.st>>>(n, T.get());
     NNPP_CUDA(cudaGetLastError());
@@ -315,6 +371,8 @@ nnpp_status coarse_refresh(Handle& h) {
   c.valid = true;
   c.stale = false;
   c.rebuilds += 1;
+  c.warm_rebuilds += warm ? 1 : 0;
+  c.ns_steps = steps;
   h.coarse_event_cur = -1;
   // the coarse operator and A P match the phases now
   static const int kOne = 1;

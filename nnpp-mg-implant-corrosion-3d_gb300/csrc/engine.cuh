@@ -69,7 +69,8 @@ struct EngineView {
   const SliceDesc* slices;  // grouped by instance, tiles in order
   const int* slice_first;
   const int* slice_count;
-  unsigned int* ticket;     // per instance completion counters, + [M] global, + [M+1] grid
+  unsigned int* ticket;     // per instance completion counters, + [M] global, + [M+1] grid,
+                            // + [M+2] slice claims
   double* partials;         // kReduceSlots * stride
   int ntiles, nchunks, M, in_graph;
   int nslices;

@@ -105,6 +105,7 @@ struct Coarse {
   int ap_k = 1;
   DBuf<float> rowabs; // n: row sums of |A_c| (Newton-Schulz scaling)
   DBuf<float> a, t, x, y; // n x n: A_c and the Newton-Schulz work matrices
+  DBuf<double> nrm;        // block partials of ||I - A_c X_0||_F^2 (warm-started rebuilds)
   size_t inv_elems() const { return (size_t)n * ld; }
   DBuf<unsigned char> snap;  // N: phases (internal order) the inverse was computed from
   DBuf<int> count;           // phase changes since (coarse_check)
@@ -112,6 +113,8 @@ struct Coarse {
   bool valid = false; // inv holds an inverse
   bool stale = true;  // the phases changed since inv was computed
   long long rebuilds = 0;  // inverses computed since the handle was built
+  long long warm_rebuilds = 0;  // of which Newton-Schulz started from the previous inverse
+  int ns_steps = 0;        // Newton-Schulz steps of the last rebuild
   ~Coarse();
 };
 

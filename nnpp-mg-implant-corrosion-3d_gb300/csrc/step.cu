@@ -560,6 +560,14 @@ __device__ __forceinline__ void warp_slices(const EngineView& v, int* s0, int* s
   *s1 = (int)(((long long)v.nslices * (gw + 1)) / nw);
 }
 
+// the next slice of a kernel whose warps claim slices one at a time from the grid-wide
+// counter ticket[M + 2] (reset by the kernel's last CTA); lane 0 claims, the warp shares it
+__device__ __forceinline__ int claim_slice(const EngineView& v, int lane) {
+  int s = 0;
+  if (lane == 0) s = (int)atomicAdd(&v.ticket[v.M + 2], 1u);
+  return __shfl_sync(0xffffffffu, s, 0);
+}
+
 __device__ __forceinline__ double warp_sum_d(double x) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
@@ -623,8 +631,17 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // PF == 0: warps claim slices one at a time (slices of solid nodes and narrow ones cost
+  // less than full ones, and a static split leaves warps idle at the end of the single
+  // wave); PF > 0 keeps each warp's contiguous range for its prefetch stream
+  constexpr bool kClaim = PF == 0;
   int s0, s1;
-  warp_slices(v, &s0, &s1);
+  if (kClaim) {
+    s0 = claim_slice(v, lane);
+    s1 = v.nslices;
+  } else {
+    warp_slices(v, &s0, &s1);
+  }
   float* zw = zwin + (WIN ? (size_t)warp * kWinCap : 0);
   // prefetch window of the operator stream: [pf_next, pf_end) of the warp's byte range
   const char* pf_next = nullptr;
@@ -642,7 +659,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
         bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
     }
   }
-  for (int sg = s0; sg < s1; ++sg) {
+  for (int sg = s0; sg < s1; sg = kClaim ? claim_slice(v, lane) : sg + 1) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     DotAcc<float> part;
@@ -754,7 +771,10 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
         }
       }
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
   }
 }
 
@@ -1263,12 +1283,30 @@ __device__ __forceinline__ bool deflating(const KParams& k) {
 }
 
 // (A P x_c)_i of an unknown i: its diagonal term from the CG operator's diagonal, the rest
-// from the stored rows
+// from the stored rows.  Eight slots at a time (with aggregates two or more bins wide, a
+// node's bonds reach at most 8 aggregates): their loads and gathers are in flight together,
+// the sum runs in slot order.
 __device__ __forceinline__ float ap_apply(const KParams& k, int i) {
-  float s = k.d32[i] * k.xc[k.agg[i]];
-  for (int q = 0; q < k.ap_k; ++q) {
-    const size_t o = (size_t)q * k.N + i;
-    s = fmaf(k.ap_val[o], k.xc[k.ap_col[o]], s);
+  const float* xc = k.xc;
+  float s = __ldg(k.d32 + i) * __ldg(xc + __ldg(k.agg + i));
+  const size_t N = (size_t)k.N;
+  int q = 0;
+  for (; q + 8 <= k.ap_k; q += 8) {
+    int col[8];
+    float val[8], xv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      col[u] = __ldg(k.ap_col + (size_t)(q + u) * N + i);
+      val[u] = __ldg(k.ap_val + (size_t)(q + u) * N + i);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) xv[u] = __ldg(xc + col[u]);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s = fmaf(val[u], xv[u], s);
+  }
+  for (; q < k.ap_k; ++q) {
+    const size_t o = (size_t)q * N + i;
+    s = fmaf(__ldg(k.ap_val + o), __ldg(xc + __ldg(k.ap_col + o)), s);
   }
   return s;
 }
@@ -1517,12 +1555,17 @@ __global__ void __launch_bounds__(kBlock) k_z_form(EngineView v, cudaGraphCondit
         for (int a = c.begin + threadIdx.x; a < c.end; a += kBlock) {
           const float di = dinv[a];
           if (di == 0.0f) continue;
-          const float qa = q[a];
+          // every load before the first store (loads are not moved across the stores)
+          const float qa = __ldg(q + a);
+          const float pa = __ldg(p + a);
+          const float ea = e[a];
+          const float ra = rin[a];
+          const float ta = t[a];
           const float w = qa - ap_apply(k, a);
-          e[a] = e[a] + alpha * p[a];
-          const float r = rin[a] - alpha * w;
+          e[a] = ea + alpha * pa;
+          const float r = ra - alpha * w;
           rin[a] = r;
-          t[a] = t[a] + alpha * qa;
+          t[a] = ta + alpha * qa;
           const float zz = r * di;
           z[a] = zz;
           part[0].add(r, zz);
@@ -2786,6 +2829,12 @@ int slice_grid(K kern, size_t smem, int sms, int nslices) {
   return g2 < 1 ? 1 : g2;
 }
 
+// kernels whose warps claim slices: every CTA resident at once (at most one slice a warp)
+template <typename K>
+int claim_grid(K kern, size_t smem, int sms, int nslices) {
+  return occ_grid(kern, smem, sms, (nslices + 7) / 8);
+}
+
 size_t smem_slots(int B) { return (size_t)(B + 16) * sizeof(unsigned short); }
 size_t smem_prep(int H, int B) { return align16((size_t)H * (sizeof(double) + 1)) + smem_slots(B); }
 size_t smem_vec64(int H, int B) { return align16((size_t)H * sizeof(double)) + smem_slots(B); }
@@ -3278,15 +3327,15 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
   switch (variant) {
     case 2: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 8, true, 3><<<slice_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 8, true, 3><<<claim_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     case 3:
-      k_cg_spmv32<W, false, 16, false, 5><<<slice_grid(k_cg_spmv32<W, false, 16, false, 5>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 16, false, 5><<<claim_grid(k_cg_spmv32<W, false, 16, false, 5>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
       break;
     case 4: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 16, false, 3><<<slice_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 16, false, 3><<<claim_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
       break;
     }
     case 5: {
@@ -3303,7 +3352,7 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
       break;
     }
     default:
-      k_cg_spmv32<W, false, 8, false, 8><<<slice_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 8, false, 8><<<claim_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
   }
 }
 
