@@ -2034,9 +2034,9 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
   __shared__ double sm[2 * kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int s0, s1;
-  warp_slices(v, &s0, &s1);
-  for (int sg = s0; sg < s1; ++sg) {
+  // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
+  // cost less than full ones)
+  for (int sg = claim_slice(v, lane); sg < v.nslices; sg = claim_slice(v, lane)) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     const bool cached = k.ds->op_valid != 0;
@@ -2168,7 +2168,10 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
       }
       __syncthreads();
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
   }
 }
 
@@ -2179,9 +2182,9 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
   __shared__ double sm[kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int s0, s1;
-  warp_slices(v, &s0, &s1);
-  for (int sg = s0; sg < s1; ++sg) {
+  // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
+  // cost less than full ones)
+  for (int sg = claim_slice(v, lane); sg < v.nslices; sg = claim_slice(v, lane)) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     double part = 0.0;
@@ -2259,7 +2262,10 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
       }
       __syncthreads();
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
   }
 }
 
@@ -2338,9 +2344,18 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
+  // cost less than full ones); the residual form, which has no last CTA to reset the
+  // counter, keeps the static split
+  constexpr bool kClaim = !RESID;
   int s0, s1;
-  warp_slices(v, &s0, &s1);
-  for (int sg = s0; sg < s1; ++sg) {
+  if (kClaim) {
+    s0 = claim_slice(v, lane);
+    s1 = v.nslices;
+  } else {
+    warp_slices(v, &s0, &s1);
+  }
+  for (int sg = s0; sg < s1; sg = kClaim ? claim_slice(v, lane) : sg + 1) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     if (lane < 9) s_hb[warp][lane] = v.slices[sg].gbase[lane];
@@ -2518,7 +2533,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
       if (threadIdx.x == 0) finish_instance(v.inst[i], tot);
       __syncthreads();
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
   }
 }
 
@@ -3038,9 +3056,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_adj_transport32(EngineView v, con
   __shared__ double sm[5 * kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int s0, s1;
-  warp_slices(v, &s0, &s1);
-  for (int sg = s0; sg < s1; ++sg) {
+  // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
+  // cost less than full ones)
+  for (int sg = claim_slice(v, lane); sg < v.nslices; sg = claim_slice(v, lane)) {
     const SliceDesc d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
     if (lane < 9) s_hb[warp][lane] = v.slices[sg].gbase[lane];
@@ -3151,7 +3169,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_adj_transport32(EngineView v, con
         for (int q = 0; q < 5; ++q) acc[q] += tot[q];
       __syncthreads();
     }
-    if (threadIdx.x == 0) v.ticket[v.M + 1] = 0;
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
   }
 }
 
@@ -3243,7 +3264,7 @@ nnpp_status launch_adj_transport32(const Engine& e, const EngineView& v, Handle&
   KParams kp = make_kparams(h, h.cur);
   k_adj_pack<<<h.grid, kBlock, 0, st>>>(kp, snap, snap1, lam, rec);
   NNPP_CUDA(cudaGetLastError());
-  k_adj_transport32<4><<<slice_grid(k_adj_transport32<4>, 0, e.sms, v.nslices), kBlock, 0, st>>>(
+  k_adj_transport32<4><<<claim_grid(k_adj_transport32<4>, 0, e.sms, v.nslices), kBlock, 0, st>>>(
       v, rec, mu, nu, acc);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
@@ -3374,7 +3395,7 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
                           cudaGraphConditionalHandle hc, double* F11_out) {
   if (prec == NNPP_MIXED && !F11_out) {
     k_phi4<<<occ_grid(k_phi4, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v);
-    k_prep_slices<<<slice_grid(k_prep_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
+    k_prep_slices<<<claim_grid(k_prep_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   }
@@ -3503,7 +3524,7 @@ nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, c
 nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
   if (prec == NNPP_MIXED) {
-    k_ir_slices<<<slice_grid(k_ir_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
+    k_ir_slices<<<claim_grid(k_ir_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   }
@@ -3527,7 +3548,7 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
       if (F_out)
         k_transport32<W, true><<<slice_grid(k_transport32<W, true>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, F_out);
       else
-        k_transport32<W, false><<<slice_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
+        k_transport32<W, false><<<claim_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
     } else {
       const size_t sh = smem_tr64(v.halo_max, v.bond_max);
       if (F_out)
