@@ -143,6 +143,49 @@ __device__ __forceinline__ void pair_warp_sum(float& hi, float& lo) {
   }
 }
 
+// FP32 pairs (hi, lo) standing in for FP64 where GB300's FP64 rate would bound a bond pass:
+// products by FMA-based TwoProd, sums by TwoSum; ~2^-46 relative per operation.
+__device__ __forceinline__ void pair_add(float& sh, float& sl, float ah, float al) {
+  float s, e;
+  two_sum(sh, ah, s, e);
+  sh = s;
+  sl += e + al;
+}
+__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+  ph = ah * bh;
+  pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
+}
+// FP32 pair (hi, lo) of a double by bit manipulation, with no FP64 arithmetic: hi keeps the
+// leading 24 significant bits (truncated), lo the rest rounded to 24 bits, so that
+// |t - hi - lo| <= 2^-48 |t|.  Zero and subnormals give (0, 0); magnitudes outside
+// [2^-60, 2^100) and non-finite values take the FP64 conversion.
+__device__ __forceinline__ void split_pair(double t, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  if (e == 0) {
+    hi = lo = 0.0f;
+    return;
+  }
+  if (e < 1023 - 60 || e >= 1023 + 100) {
+    hi = (float)t;
+    lo = isfinite(hi) ? (float)(t - (double)hi) : 0.0f;
+    return;
+  }
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29));
+  const float r = (float)(unsigned int)(m & 0x1fffffffu) * 0x1p-29f;            // in [0, 1)
+  const float sc = __uint_as_float((unsigned int)(e - 1023 - 23 + 127) << 23);  // 2^(E-23)
+  lo = __uint_as_float(__float_as_uint(r * sc) | sign);
+}
+// (ah, al) - (bh, bl), renormalised (|lo| <= half an ulp of hi)
+__device__ __forceinline__ void pair_sub(float ah, float al, float bh, float bl, float& dh, float& dl) {
+  float s, e;
+  two_sum(ah, -bh, s, e);
+  e += al - bl;
+  dh = s + e;
+  dl = e - (dh - s);
+}
 // Sum of products a*b of one thread: FP64 on the FP64 path, FP32 pairs on the FP32 path.
 template <typename P>
 struct DotAcc;

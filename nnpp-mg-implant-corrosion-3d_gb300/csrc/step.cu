@@ -141,9 +141,96 @@ __device__ __forceinline__ void write_partials(const EngineView& v, int item, do
     for (int k = 0; k < NV; ++k) v.partials[(size_t)k * v.stride + item] = part[k];
 }
 
+// Pair partials: the FP32 path's item partials are FP32 pairs (hi, lo) stored in the 8-byte
+// slots of the partials buffer, so that the last CTA sums them on the FP32 pipes (an FP64
+// sum of the ~19k slice partials of a 512k-node pass would hold one SM's FP64 pipe for
+// microseconds).
+__device__ __forceinline__ void store_pair(double* partials, size_t idx, float hi, float lo) {
+  reinterpret_cast<float2*>(partials)[idx] = make_float2(hi, lo);
+}
+
+// FP32 pair of an FP64 value x*x (x split into a pair, the square to ~2^-46 relative)
+__device__ __forceinline__ void pair_square(double x, float& h, float& l) {
+  float xh, xl;
+  split_pair(x, xh, xl);
+  h = xh * xh;
+  l = fmaf(xh, xh, -h) + 2.0f * xh * xl;
+}
+
+// block sums of NV pairs per thread; thread 0 gets the FP64 values (sm: NV * kBlock / 32
+// doubles, used as pairs)
+template <int NV>
+__device__ __forceinline__ void block_pair_sum(float (&h)[NV], float (&l)[NV], double (&out)[NV], double* sm) {
+  float2* smf = reinterpret_cast<float2*>(sm);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    pair_warp_sum(h[q], l[q]);
+    if (lane == 0) smf[q * (kBlock / 32) + wid] = make_float2(h[q], l[q]);
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      float th = 0.0f, tl = 0.0f;
+      if (lane < kBlock / 32) {
+        th = smf[q * (kBlock / 32) + lane].x;
+        tl = smf[q * (kBlock / 32) + lane].y;
+      }
+      pair_warp_sum(th, tl);
+      out[q] = (double)th + (double)tl;
+    }
+  }
+  __syncthreads();
+}
+
+// reduce NV pair partials of items [first, first+count) (layout partials[k*stride + item]);
+// four independent pair accumulators per thread, combined in a fixed order
+template <int NV>
+__device__ __forceinline__ void reduce_pair_items(const double* partials, int stride, int first, int count,
+                                                  double (&out)[NV], double* sm) {
+  constexpr int U = 4;
+  const float2* pp = reinterpret_cast<const float2*>(partials);
+  float hh[NV], ll[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const float2* p = pp + (size_t)k * stride + first;
+    float h[U], l[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) h[u] = l[u] = 0.0f;
+    int b = threadIdx.x;
+    for (; b + (U - 1) * kBlock < count; b += U * kBlock) {
+      float2 x[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) x[u] = p[b + u * kBlock];
+#pragma unroll
+      for (int u = 0; u < U; ++u) pair_add(h[u], l[u], x[u].x, x[u].y);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (b + u * kBlock < count) pair_add(h[u], l[u], p[b + u * kBlock].x, p[b + u * kBlock].y);
+    pair_add(h[0], l[0], h[1], l[1]);
+    pair_add(h[2], l[2], h[3], l[3]);
+    pair_add(h[0], l[0], h[2], l[2]);
+    hh[k] = h[0];
+    ll[k] = l[0];
+  }
+  block_pair_sum<NV>(hh, ll, out, sm);
+}
+
+// the last CTA's reduction of items written by write_dot_partials
+template <int NV, typename P>
+__device__ __forceinline__ void reduce_dot_items(const double* partials, int stride, int first, int count,
+                                                 double (&out)[NV], double* sm) {
+  if constexpr (sizeof(P) == 8)
+    reduce_items<NV>(partials, stride, first, count, out, sm);
+  else
+    reduce_pair_items<NV>(partials, stride, first, count, out, sm);
+}
+
 // Item partials of per-thread dot accumulators: FP64 block sums on the FP64 path; on the
 // FP32 path FP32-pair warp sums, then warp 0 sums the warps' pairs (sm: NV * kBlock / 32
-// doubles, reused as pairs).  Thread 0 writes the FP64 partials.
+// doubles, reused as pairs) and stores the pair partials (reduce_dot_items sums them).
 template <int NV, typename P>
 __device__ __forceinline__ void write_dot_partials(const EngineView& v, int item, DotAcc<P> (&acc)[NV], double* sm) {
   if constexpr (sizeof(P) == 8) {
@@ -169,7 +256,7 @@ __device__ __forceinline__ void write_dot_partials(const EngineView& v, int item
           t.lo = smf[q * (kBlock / 32) + lane].y;
         }
         t.warp_sum();
-        if (lane == 0) v.partials[(size_t)q * v.stride + item] = t.value();
+        if (lane == 0) store_pair(v.partials, (size_t)q * v.stride + item, t.hi, t.lo);
       }
     }
     __syncthreads();
@@ -235,49 +322,6 @@ __device__ __forceinline__ float sel4(const float4& v, int s) {
   return s == 0 ? v.x : s == 1 ? v.y : s == 2 ? v.z : v.w;
 }
 
-// FP32 pairs (hi, lo) standing in for FP64 where GB300's FP64 rate would bound a bond pass:
-// products by FMA-based TwoProd, sums by TwoSum; ~2^-46 relative per operation.
-__device__ __forceinline__ void pair_add(float& sh, float& sl, float ah, float al) {
-  float s, e;
-  two_sum(sh, ah, s, e);
-  sh = s;
-  sl += e + al;
-}
-__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
-  ph = ah * bh;
-  pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
-}
-// FP32 pair (hi, lo) of a double by bit manipulation, with no FP64 arithmetic: hi keeps the
-// leading 24 significant bits (truncated), lo the rest rounded to 24 bits, so that
-// |t - hi - lo| <= 2^-48 |t|.  Zero and subnormals give (0, 0); magnitudes outside
-// [2^-60, 2^100) and non-finite values take the FP64 conversion.
-__device__ __forceinline__ void split_pair(double t, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
-  const int e = (int)((b >> 52) & 0x7ffu);
-  if (e == 0) {
-    hi = lo = 0.0f;
-    return;
-  }
-  if (e < 1023 - 60 || e >= 1023 + 100) {
-    hi = (float)t;
-    lo = isfinite(hi) ? (float)(t - (double)hi) : 0.0f;
-    return;
-  }
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  const unsigned long long m = b & 0xfffffffffffffull;
-  hi = __uint_as_float(sign | ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29));
-  const float r = (float)(unsigned int)(m & 0x1fffffffu) * 0x1p-29f;            // in [0, 1)
-  const float sc = __uint_as_float((unsigned int)(e - 1023 - 23 + 127) << 23);  // 2^(E-23)
-  lo = __uint_as_float(__float_as_uint(r * sc) | sign);
-}
-// (ah, al) - (bh, bl), renormalised (|lo| <= half an ulp of hi)
-__device__ __forceinline__ void pair_sub(float ah, float al, float bh, float bl, float& dh, float& dl) {
-  float s, e;
-  two_sum(ah, -bh, s, e);
-  e += al - bl;
-  dh = s + e;
-  dl = e - (dh - s);
-}
 // sum of pairs over the W lanes of a node's segment (lane 0 of the segment holds it)
 template <int WIDTH>
 __device__ __forceinline__ double seg_reduce_pair(float h, float l) {
@@ -525,7 +569,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(EngineView v, cudaGraphCondi
     write_dot_partials<2, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
-      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      reduce_dot_items<2, P>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (ds->outer_active) {
@@ -757,12 +801,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
       __syncwarp();
     }
     part.warp_sum();
-    if (lane == 0) v.partials[sg] = part.value();
+    if (lane == 0) store_pair(v.partials, sg, part.hi, part.lo);
   }
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         if (ds->inner_active) {
@@ -940,14 +984,14 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32t(EngineView v) {
       wb ^= 1;
     }
     part.warp_sum();
-    if (lane == 0) v.partials[sg] = part.value();
+    if (lane == 0) store_pair(v.partials, sg, part.hi, part.lo);
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   if (timed_out >= 0 && lane == 0) v.inst[timed_out].ds->wait_timeout = 1;
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         if (ds->inner_active) {
@@ -1124,17 +1168,17 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_spmv32s(EngineView v, int stag
       __syncwarp();
       wb ^= 1;
       part.warp_sum();
-      if (lane == 0) v.partials[sg] = part.value();
+      if (lane == 0) store_pair(v.partials, sg, part.hi, part.lo);
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
     for (int sg = s0; sg < s1; ++sg)
-      if (lane == 0) v.partials[sg] = 0.0;
+      if (lane == 0) store_pair(v.partials, sg, 0.0f, 0.0f);
   }
   if (timed_out && lane == 0) k.ds->wait_timeout = 1;
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     double tot[1];
-    reduce_items<1>(v.partials, v.stride, v.slice_first[0], v.slice_count[0], tot, sm);
+    reduce_pair_items<1>(v.partials, v.stride, v.slice_first[0], v.slice_count[0], tot, sm);
     if (threadIdx.x == 0) {
       DevState* ds = k.ds;
       if (ds->inner_active) {
@@ -1242,7 +1286,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(EngineView v, cudaGraphCon
     write_dot_partials<2, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
-      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      reduce_dot_items<2, P>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (ds->inner_active) {
@@ -1576,7 +1620,7 @@ __global__ void __launch_bounds__(kBlock) k_z_form(EngineView v, cudaGraphCondit
     write_dot_partials<2, float>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[2];
-      reduce_items<2>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      reduce_dot_items<2, float>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (ds->inner_active) {
@@ -1653,7 +1697,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(EngineView v, cudaGraphCond
     write_dot_partials<3, P>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[3];
-      reduce_items<3>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      reduce_dot_items<3, P>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         if (init) {
@@ -1846,7 +1890,7 @@ __global__ void __launch_bounds__(kBlock) k_warm_dots(EngineView v) {
     write_dot_partials<kWarmSlots, float>(v, item, part, sm);
     if (item_done(&v.ticket[c.inst], v.chunk_count[c.inst], &s_last)) {
       double tot[kWarmSlots];
-      reduce_items<kWarmSlots>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
+      reduce_dot_items<kWarmSlots, float>(v.partials, v.stride, v.chunk_first[c.inst], v.chunk_count[c.inst], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = k.ds;
         ds->warm_nd = 0;
@@ -2100,7 +2144,7 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
         }
       }
     }
-    double part0 = 0.0, part1 = 0.0;
+    float b2h = 0.0f, b2l = 0.0f, r2h = 0.0f, r2l = 0.0f;  // b.b and r.r as FP32 pairs
     if (rowok) {
       double b;
       if (k.b_override) {
@@ -2134,21 +2178,21 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
       k.b64[a] = bb;
       k.r64[a] = r;
       const double be = bb + (fr ? cpl : 0.0);
-      part0 = be * be;
-      part1 = r * r;
+      pair_square(be, b2h, b2l);
+      pair_square(r, r2h, r2l);
     }
-    part0 = warp_sum_d(part0);
-    part1 = warp_sum_d(part1);
+    pair_warp_sum(b2h, b2l);
+    pair_warp_sum(r2h, r2l);
     if (lane == 0) {
-      v.partials[sg] = part0;
-      v.partials[(size_t)v.stride + sg] = part1;
+      store_pair(v.partials, sg, b2h, b2l);
+      store_pair(v.partials, (size_t)v.stride + sg, r2h, r2l);
     }
     __syncwarp();
   }
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[2];
-      reduce_items<2>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<2>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         ds->op_valid = 1;
@@ -2187,7 +2231,7 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
   for (int sg = claim_slice(v, lane); sg < v.nslices; sg = claim_slice(v, lane)) {
     const SliceDesc& d = v.slices[sg];
     const KParams& k = v.inst[d.inst];
-    double part = 0.0;
+    float rh = 0.0f, rl = 0.0f;  // r.r of the slice as an FP32 pair
     if (*((volatile int*)&k.ds->outer_active) != 0) {
       if (lane < 9) s_hb[warp][lane] = d.gbase[lane];
       __syncwarp();
@@ -2231,17 +2275,17 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
         const double ph = k.phi64[a] + ea;
         k.phi64[a] = ph;
         set_phi_rec(k, a, ph, true);
-        part = r * r;
+        pair_square(r, rh, rl);
       }
       __syncwarp();
     }
-    part = warp_sum_d(part);
-    if (lane == 0) v.partials[sg] = part;
+    pair_warp_sum(rh, rl);
+    if (lane == 0) store_pair(v.partials, sg, rh, rl);
   }
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         if (ds->outer_active) {
@@ -2513,15 +2557,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
       n_solid = __reduce_add_sync(0xffffffffu, n_solid);
       n_bad = __reduce_add_sync(0xffffffffu, n_bad);
       if (lane == 0) {
-        double* pp = v.partials + sg;
         const size_t st = v.stride;
 #pragma unroll
-        for (int s = 0; s < S; ++s) pp[s * st] = (double)ph_hi[s] + (double)ph_lo[s];
-        pp[4 * st] = (double)n_solid;
-        pp[5 * st] = (double)ph_hi[4] + (double)ph_lo[4];
-        pp[6 * st] = (double)ph_hi[5] + (double)ph_lo[5];
-        pp[7 * st] = (double)n_bad;
-        pp[8 * st] = 0.0;
+        for (int s = 0; s < S; ++s) store_pair(v.partials, s * st + sg, ph_hi[s], ph_lo[s]);
+        store_pair(v.partials, 4 * st + sg, (float)n_solid, 0.0f);  // counts <= 32: exact
+        store_pair(v.partials, 5 * st + sg, ph_hi[4], ph_lo[4]);
+        store_pair(v.partials, 6 * st + sg, ph_hi[5], ph_lo[5]);
+        store_pair(v.partials, 7 * st + sg, (float)n_bad, 0.0f);
+        store_pair(v.partials, 8 * st + sg, 0.0f, 0.0f);
       }
     }
   }
@@ -2529,7 +2572,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[kDiagSlots];
-      reduce_items<kDiagSlots>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<kDiagSlots>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0) finish_instance(v.inst[i], tot);
       __syncthreads();
     }
@@ -3159,12 +3202,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_adj_transport32(EngineView v, con
     for (int q = 0; q < 5; ++q) pair_warp_sum(gh[q], gl[q]);
     if (lane == 0)
 #pragma unroll
-      for (int q = 0; q < 5; ++q) v.partials[(size_t)q * v.stride + sg] = (double)gh[q] + (double)gl[q];
+      for (int q = 0; q < 5; ++q) store_pair(v.partials, (size_t)q * v.stride + sg, gh[q], gl[q]);
   }
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[5];
-      reduce_items<5>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<5>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
       if (threadIdx.x == 0)
         for (int q = 0; q < 5; ++q) acc[q] += tot[q];
       __syncthreads();
