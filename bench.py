@@ -437,6 +437,9 @@ def run_ours(args):
         t_tr = sim.time_kernel(0, nn.MIXED, reps=20)
         t_ir = sim.time_kernel(2, nn.MIXED, reps=20)
         t_upd = sim.time_kernel(3, nn.MIXED, reps=50)
+        # the update's three kernels one by one (single instance, two-level preconditioner)
+        t_parts = ({name: sim.time_kernel(4 + i, nn.MIXED, reps=50)
+                    for i, name in enumerate(("restrict", "coarse_product", "z_and_dots"))} if cn else None)
     tuned = sim.tuning()
     variants = {}
     with ProfileRange("variants"):
@@ -490,6 +493,8 @@ def run_ours(args):
     roofline["share_of_step"] = {k: v / ms_step for k, v in shares.items()}
     roofline["fp64_path_ms_per_launch"] = k64
     roofline["cg_operator_variants_ms"] = variants
+    if t_parts:
+        roofline["cg_update_parts_ms"] = t_parts
 
     adj = None
     if rank == 0 and args.adjoint_steps > 0:

@@ -281,7 +281,9 @@ nnpp_status nnpp_forward_timed(nnpp_handle* h, int n_steps, int precision, doubl
 /* Average duration of one launch of a single step kernel on the current state, CUDA-event
  * timed on the handle's stream over `reps` launches after 3 warm-up launches; the state is
  * restored afterwards.  kernel_id: 0 transport (bond sums), 1 CG matrix-vector product,
- * 2 FP64 refinement residual, 3 CG vector update. */
+ * 2 FP64 refinement residual, 3 CG vector update; for one instance with the two-level
+ * preconditioner the three kernels of 3 one by one: 4 restriction (with the additive form's
+ * update), 5 coarse product, 6 z and the dots. */
 nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int reps,
                              double* ms_per_launch);
 

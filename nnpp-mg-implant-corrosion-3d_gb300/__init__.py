@@ -335,7 +335,8 @@ class Simulation:
 
     def time_kernel(self, kernel_id, precision=MIXED, reps=20):
         """Average milliseconds per launch of one step kernel (0 transport, 1 CG SpMV,
-        2 FP64 refinement residual)."""
+        2 FP64 refinement residual, 3 CG update; with the two-level preconditioner on one
+        instance 4, 5, 6 time the update's restriction, coarse product and z pass alone)."""
         ms = C.c_double(0.0)
         _check(lib().nnpp_time_kernel(self._h, kernel_id, precision, reps, C.byref(ms)))
         return ms.value

@@ -604,7 +604,7 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
                              double* ms_per_launch) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
-  if (reps < 1 || !ms_per_launch || kernel_id < 0 || kernel_id > 3)
+  if (reps < 1 || !ms_per_launch || kernel_id < 0 || kernel_id > 6)
     return set_error(NNPP_ERR_INVALID, "time_kernel: bad argument");
   if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
   Handle& h = hp->h;
@@ -639,6 +639,7 @@ nnpp_status nnpp_time_kernel(nnpp_handle* hp, int kernel_id, int precision, int 
     if (kernel_id == 0) return launch_transport_b(e, v, precision, h.st, nullptr);
     if (kernel_id == 1) return launch_cg_spmv_b(e, v, precision, h.st);
     if (kernel_id == 3) return launch_cg_update_b(e, v, precision, h.st, 0);
+    if (kernel_id >= 4) return launch_coarse_part_b(e, v, precision, kernel_id - 4, h.st);
     return launch_ir_update_b(e, v, precision, h.st, 0);
   };
   for (int w = 0; w < 3 && st == NNPP_OK; ++w) st = one();

@@ -140,6 +140,7 @@ nnpp_status launch_prep_b(const Engine& e, const EngineView& v, int prec, cudaSt
 nnpp_status launch_cg_init_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                              cudaGraphConditionalHandle hc);
 nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
+nnpp_status launch_coarse_part_b(const Engine& e, const EngineView& v, int prec, int part, cudaStream_t st);
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc);
 bool engine_coarse(const Engine& e);  // the two-level preconditioner applies (every member has one)

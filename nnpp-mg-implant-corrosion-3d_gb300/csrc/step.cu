@@ -3552,6 +3552,27 @@ nnpp_status launch_coarse_update(const Engine& e, const EngineView& v, cudaStrea
   return NNPP_OK;
 }
 
+// one kernel of a single instance's split-iteration update (0 restriction and CG update,
+// 1 coarse product, 2 z and the dots), for timing them one by one
+nnpp_status launch_coarse_part_b(const Engine& e, const EngineView& v, int prec, int part, cudaStream_t st) {
+  if (!engine_coarse(e) || e.members.size() != 1 || part < 0 || part > 2)
+    return set_error(NNPP_ERR_INVALID, "time_kernel: the coarse update parts need one instance with a coarse space");
+  const int n = std::max(1, e.members[0]->coarse.valid ? e.members[0]->coarse.n : 0);
+  const int rg = std::max(1, std::min((n * 32 + kBlock - 1) / kBlock, e.sms * 8));
+  const bool mixed = prec == NNPP_MIXED;
+  if (part == 0) {
+    if (mixed) k_cg_update_restrict<float><<<rg, kBlock, 0, st>>>(v);
+    else k_cg_update_restrict<double><<<rg, kBlock, 0, st>>>(v);
+  } else if (part == 1) {
+    k_coarse_gemv<<<rg, kBlock, (size_t)cld_max(e) * sizeof(float), st>>>(v, 1, 0, 1, mixed ? 1 : 0);
+  } else {
+    if (mixed) k_z_form<float><<<occ_grid(k_z_form<float>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, 0);
+    else k_z_form<double><<<occ_grid(k_z_form<double>, 0, e.sms, v.nchunks), kBlock, 0, st>>>(v, 0);
+  }
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
   if (engine_coarse(e))
