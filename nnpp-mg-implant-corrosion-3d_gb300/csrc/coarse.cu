@@ -258,11 +258,12 @@ nnpp_status coarse_build(Handle& h) {
   c.ld = (c.n + 3) & ~3;
   // A P rows hold at most 27 aggregates each: allocated once, so that no pointer the
   // kernels hold changes when the operator is rebuilt or replayed
-  if (!c.agg.alloc(h.N) || !c.inv.alloc(c.inv_elems()) || !c.rc.alloc(c.n) || !c.xc.alloc(c.n) ||
+  if (!c.agg.alloc(h.N) || !c.inv.alloc(c.inv_elems()) || !c.rc.alloc(c.ld) || !c.xc.alloc(c.n) ||
       !c.dots.alloc(3 * (size_t)c.n) || !c.rowabs.alloc(c.n) || !c.ap_col.alloc(27 * (size_t)h.N) ||
       !c.ap_val.alloc(27 * (size_t)h.N))
     return set_error(NNPP_ERR_NOMEM, "coarse space");
   NNPP_CUDA(cudaMemsetAsync(c.dots.get(), 0, sizeof(double) * 3 * (size_t)c.n, h.st));
+  NNPP_CUDA(cudaMemsetAsync(c.rc.get(), 0, sizeof(float) * c.ld, h.st));  // padding to ld stays 0
   c.ap_k = 1;
   NNPP_CUDA(cudaMemsetAsync(c.inv.get(), 0, sizeof(float) * c.inv_elems(), h.st));  // padding stays 0
   k_agg_fill<<<std::max(1, std::min((L.nbins + 255) / 256, 4096)), 256, 0, h.st>>>(

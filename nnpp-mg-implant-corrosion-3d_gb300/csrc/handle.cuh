@@ -98,7 +98,7 @@ struct Coarse {
   int ld = 0;         // row stride of inv: n rounded up to 4 (16-byte rows, zero padding)
   DBuf<int> agg;      // N: aggregate of each node
   DBuf<float> inv;    // n x ld: the coarse inverse (symmetric: row I = column I)
-  DBuf<float> rc, xc; // n: restricted residual, coarse correction
+  DBuf<float> rc, xc; // restricted residual (ld, zero padding), coarse correction (n)
   DBuf<double> dots;  // 3n: per aggregate r.D^-1 r and r.r of the update, r_c x_c of the product
   DBuf<int> ap_col;   // A P off its diagonal term (27 N capacity, ap_k used): see KParams
   DBuf<float> ap_val;

@@ -1390,6 +1390,7 @@ __global__ void __launch_bounds__(kBlock) k_coarse_restrict(EngineView v, int wh
 // of r.D^-1 r and r.r.
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
+  __shared__ int2 s_runs[kBlock / 32][32];
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1410,12 +1411,55 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
       if (def) {
         // deflated iteration: restrict q = A p (the update follows the coarse product)
         float acc = 0.0f;
-        for (int bz = az * k.cf; bz < min(az * k.cf + k.cf, k.nb2); ++bz)
-          for (int by = ay * k.cf; by < min(ay * k.cf + k.cf, k.nb1); ++by) {
-            const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
-            const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
-            for (int i = i0 + lane; i < i1; i += 32) acc += (float)(dinv[i] != P(0) ? q[i] : P(0));
+        const int y0 = ay * k.cf, ny = min(y0 + k.cf, k.nb1) - y0;
+        const int z0 = az * k.cf, nr = ny * (min(z0 + k.cf, k.nb2) - z0);
+        if (nr <= 32) {
+          // the aggregate's runs (cf bins along x each): their bounds loaded one run a lane,
+          // then the warp walks the runs' concatenation, eight elements a lane in flight
+          int lo = 0, len = 0;
+          if (lane < nr) {
+            const int b0 = bx0 + k.nb0 * ((y0 + lane % ny) + k.nb1 * (z0 + lane / ny));
+            lo = k.bin_start[b0];
+            len = k.bin_start[b0 + (bx1 - bx0)] - lo;
           }
+          int pre = len;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, pre, off);
+            if (lane >= off) pre += t;
+          }
+          const int total = __shfl_sync(0xffffffffu, pre, 31);
+          int2* runs = s_runs[(threadIdx.x >> 5)];
+          __syncwarp();
+          if (lane < nr) runs[lane] = make_int2(pre - len, lo);  // (first position, first node)
+          __syncwarp();
+          for (int base = 0; base < total; base += 32 * 8) {
+            P qv[8], dv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int idx = base + lane + 32 * u;
+              qv[u] = dv[u] = P(0);
+              if (idx < total) {
+                int node = 0;
+                for (int r = 0; r < nr; ++r) {
+                  const int2 ru = runs[r];
+                  if (idx >= ru.x) node = ru.y + (idx - ru.x);
+                }
+                dv[u] = dinv[node];
+                qv[u] = q[node];
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += (float)(dv[u] != P(0) ? qv[u] : P(0));
+          }
+        } else {
+          for (int bz = z0; bz < min(z0 + k.cf, k.nb2); ++bz)
+            for (int by = y0; by < y0 + ny; ++by) {
+              const int b0 = bx0 + k.nb0 * (by + k.nb1 * bz);
+              const int i0 = k.bin_start[b0], i1 = k.bin_start[b0 + (bx1 - bx0)];
+              for (int i = i0 + lane; i < i1; i += 32) acc += (float)(dinv[i] != P(0) ? q[i] : P(0));
+            }
+        }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
         if (lane == 0) k.rc[I] = acc;
@@ -1485,8 +1529,24 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
     if (!k.coarse || !coarse_active(k, which == 2 ? 0 : which)) continue;
     if (which == 2 && !deflating<float>(k)) continue;  // the deflated solve's final correction only
     const int n = k.cn, ld = k.cld;
+    const bool dm = def_mixed && k.defl_ok && *((volatile const int*)&k.ds->defl) != 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < ld; i += kBlock) srv[i] = i < n ? k.rc[i] : 0.0f;
+    {
+      // r_c into shared memory: 16-byte loads, four per thread in flight (rc holds ld
+      // floats, its padding zero)
+      const float4* rc4 = reinterpret_cast<const float4*>(k.rc);
+      float4* sv4 = reinterpret_cast<float4*>(srv);
+      const int nq = ld >> 2;
+      for (int i0 = threadIdx.x; i0 < nq; i0 += 4 * kBlock) {
+        float4 t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (i0 + u * kBlock < nq) t[u] = rc4[i0 + u * kBlock];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (i0 + u * kBlock < nq) sv4[i0 + u * kBlock] = t[u];
+      }
+    }
     __syncthreads();
     const float4* sr4 = reinterpret_cast<const float4*>(srv);
     const int nq = ld >> 2;  // 16-byte groups per row
@@ -1514,7 +1574,15 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
       for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
       if (lane == 0) {
         k.xc[I] = x;
-        if (dots) k.cdots[2 * n + I] = (double)srv[I] * (double)x;
+        if (dots) {
+          if (dm) {
+            // deflated (FP32 path): r_c[I] x_c[I] as an exact FP32 pair
+            const float pr = srv[I] * x;
+            store_pair(k.cdots, 2 * (size_t)n + I, pr, fmaf(srv[I], x, -pr));
+          } else {
+            k.cdots[2 * n + I] = (double)srv[I] * (double)x;
+          }
+        }
       }
     }
   }
@@ -1527,7 +1595,7 @@ __global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which,
       const bool dm = def_mixed && k.coarse && k.defl_ok && *((volatile const int*)&k.ds->defl) != 0;
       if (dm) {
         double t2[1];
-        reduce_items<1>(k.cdots + 2 * (size_t)k.cn, k.cn, 0, k.cn, t2, sm);
+        reduce_pair_items<1>(k.cdots + 2 * (size_t)k.cn, k.cn, 0, k.cn, t2, sm);
         tot[2] = t2[0];
       } else if (k.coarse) {
         reduce_items<3>(k.cdots, k.cn, 0, k.cn, tot, sm);
