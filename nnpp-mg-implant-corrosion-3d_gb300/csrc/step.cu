@@ -1515,8 +1515,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_update_restrict(EngineView v) {
 // row loads, four accumulators combined in a fixed order).  With dots (the CG update of the
 // split iteration), also r_c[I] x_c[I] = (P^T r).(x_c) per row, and the last CTA forms
 // r.z = r.D^-1 r + r_c.x_c and r.r from the per-aggregate parts and makes the CG decisions.
-constexpr int kGemvU = 12;  // 16-byte loads per lane in flight (12 x 32 x 4 = 1536 floats a round)
-__global__ void __launch_bounds__(kBlock) k_coarse_gemv(EngineView v, int which, cudaGraphConditionalHandle hc,
+// 16-byte loads per lane in flight (8 x 32 x 4 = 1024 floats a round); with at most 80
+// registers three CTAs fit an SM, so the 343 CTAs of the 512k workload run in one wave
+constexpr int kGemvU = 8;
+__global__ void __launch_bounds__(kBlock, 3) k_coarse_gemv(EngineView v, int which, cudaGraphConditionalHandle hc,
                                                         int dots, int def_mixed) {
   extern __shared__ __align__(16) float srv[];
   __shared__ double sm[3 * kBlock / 32];
