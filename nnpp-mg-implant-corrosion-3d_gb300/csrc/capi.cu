@@ -90,6 +90,7 @@ bool have_gpu() {
 struct StateBackup {
   int cur, prec;
   DBuf<double> phi, phi_prev;
+  DBuf<double> xh, bh;  // the warm-start history ring (a timed transport records into it)
   DBuf<float4> clo;
   DBuf<Rec32> rec32;
   DBuf<Rec64> rec64;
@@ -110,6 +111,11 @@ nnpp_status backup(Handle& h, StateBackup& b) {
   NNPP_CUDA(cudaMemcpyAsync(b.rec32.get(), h.rec32[h.cur].get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(b.rec64.get(), h.rec64[h.cur].get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(b.flip.get(), h.flip_step.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
+  if (h.xh.size() > 0) {
+    if (!b.xh.alloc(h.xh.size()) || !b.bh.alloc(h.bh.size())) return set_error(NNPP_ERR_NOMEM, "backup");
+    NNPP_CUDA(cudaMemcpyAsync(b.xh.get(), h.xh.get(), h.xh.bytes(), cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(b.bh.get(), h.bh.get(), h.bh.bytes(), cudaMemcpyDeviceToDevice, h.st));
+  }
   NNPP_TRY(read_state(h, &b.ds));
   return NNPP_OK;
 }
@@ -124,6 +130,10 @@ nnpp_status restore(Handle& h, StateBackup& b) {
   NNPP_CUDA(cudaMemcpyAsync(h.rec32[h.cur].get(), b.rec32.get(), sizeof(Rec32) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.rec64[h.cur].get(), b.rec64.get(), sizeof(Rec64) * N, cudaMemcpyDeviceToDevice, h.st));
   NNPP_CUDA(cudaMemcpyAsync(h.flip_step.get(), b.flip.get(), sizeof(int) * N, cudaMemcpyDeviceToDevice, h.st));
+  if (b.xh.size() > 0 && b.xh.size() == h.xh.size() && b.bh.size() == h.bh.size()) {
+    NNPP_CUDA(cudaMemcpyAsync(h.xh.get(), b.xh.get(), h.xh.bytes(), cudaMemcpyDeviceToDevice, h.st));
+    NNPP_CUDA(cudaMemcpyAsync(h.bh.get(), b.bh.get(), h.bh.bytes(), cudaMemcpyDeviceToDevice, h.st));
+  }
   NNPP_CUDA(cudaMemcpyAsync(h.dstate.get(), &b.ds, sizeof(DevState), cudaMemcpyHostToDevice, h.st));
   h.settings_pushed = false;
   NNPP_CUDA(cudaStreamSynchronize(h.st));

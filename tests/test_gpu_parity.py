@@ -471,3 +471,38 @@ def test_set_tuning_rejects_bad_configuration(gpu):
         with pytest.raises(nn.NNPPError) as e:
             sim.set_tuning(*bad)
         assert e.value.status == 1
+
+
+def test_time_kernel_parts_leave_the_state(gpu):
+    """nnpp_time_kernel times the split update's three kernels one by one on a single
+    instance with the coarse space (ids 4-6), restores the state afterwards, and rejects
+    them without a coarse space and out-of-range ids."""
+    nn = gpu
+    inp = nn.synth(1, 16, seed=3)
+    sim = nn.Simulation.from_synth(inp)
+    sim.build_neighbours()
+    sim.set_tuning(4, 8, 0)
+    sim.forward(3, nn.MIXED)
+    before = sim.state()
+    for kid in range(7):
+        assert sim.time_kernel(kid, nn.MIXED, reps=3) > 0.0
+    for a, b in zip(before, sim.state()):
+        assert np.array_equal(a, b)
+    ref = nn.Simulation.from_synth(inp)
+    ref.build_neighbours()
+    ref.set_tuning(4, 8, 0)
+    ref.forward(3, nn.MIXED)
+    sim.forward(2, nn.MIXED)
+    ref.forward(2, nn.MIXED)
+    for a, b in zip(sim.state(), ref.state()):
+        assert np.array_equal(a, b)
+    jac = nn.Simulation.from_synth(inp)
+    jac.build_neighbours()
+    jac.set_preconditioner(nn.PRECOND_JACOBI)
+    jac.forward(1, nn.MIXED)
+    with pytest.raises(nn.NNPPError) as e:
+        jac.time_kernel(5, nn.MIXED, reps=1)
+    assert e.value.status == 1
+    with pytest.raises(nn.NNPPError) as e:
+        sim.time_kernel(7, nn.MIXED, reps=1)
+    assert e.value.status == 1
