@@ -2960,7 +2960,8 @@ int slice_grid(K kern, size_t smem, int sms, int nslices) {
   return g2 < 1 ? 1 : g2;
 }
 
-// kernels whose warps claim slices: every CTA resident at once (at most one slice a warp)
+// kernels whose warps claim slices: as many CTAs as the SMs hold at once (fewer when the
+// slices are fewer than the warps)
 template <typename K>
 int claim_grid(K kern, size_t smem, int sms, int nslices) {
   return occ_grid(kern, smem, sms, (nslices + 7) / 8);
