@@ -2451,7 +2451,9 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
 // Each warp streams 32-row slices of the sliced operator, one lane per node, gathering the
 // neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
 // partials of the diagnostics are reduced per instance by the last CTA.
-constexpr int kTrB = 4;  // bond columns per batch of the FP32 transport
+// bond columns per batch of the FP32 transport: 6 at 126 registers (2 CTAs an SM) measured
+// 0.378 ms at 512k, against 0.389 for 5, 0.405 for 4 and 0.467 for 2 (8 spills)
+constexpr int kTrB = 6;
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double* F_out) {
   __shared__ int s_hb[kBlock / 32][12];
