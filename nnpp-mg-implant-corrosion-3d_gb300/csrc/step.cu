@@ -3164,7 +3164,9 @@ __global__ void k_adj_pack(KParams k, const Rec64* snap, const Rec64* snap1, con
   }
 }
 
-constexpr int kAdjB = 2;  // bond columns per batch of the FP32 adjoint transport
+// bond columns per batch of the FP32 adjoint transport: 4 at 127 registers (2 CTAs an SM);
+// the 400-step backward of the 262k calibration workload took 1014 ms against 1059 with 2
+constexpr int kAdjB = 4;
 template <int W>
 __global__ void __launch_bounds__(kBlock, 2) k_adj_transport32(EngineView v, const float4* rec,
                                                                double* mu, double* nu, double* acc) {
