@@ -460,3 +460,34 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------ result errors ---------
+def compare_states(params, c, phi, phase, c_ref, phi_ref, phase_ref, mg_lost=None,
+                   mg_lost_ref=None):
+    """The error of a run against a reference run of the same workload, in the four
+    quantities every result states: relative L2 of the concentrations and of the potential,
+    the front position in lattice spacings and the Mg mass lost.
+
+    The front position is the radius of the sphere of the solid volume,
+    (3 V_solid / 4 pi)^(1/3) with V_solid = solid nodes x dV (the solid/liquid mask of
+    main.cpp:914-922); front_dx is the difference of the two radii in units of dx.
+    mask_mismatch counts the nodes whose phase differs."""
+    dV = params.dx * params.dy * params.dz
+
+    def r_eq(ph):
+        return (3.0 * float(np.sum(ph)) * dV / (4.0 * np.pi)) ** (1.0 / 3.0)
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) /
+                     max(float(np.linalg.norm(b)), 1e-300))
+
+    out = {"rel_l2_c": rel(c, c_ref), "rel_l2_phi": rel(phi, phi_ref),
+           "mask_mismatch": int(np.sum(np.asarray(phase) != np.asarray(phase_ref))),
+           "front_dx": abs(r_eq(phase) - r_eq(phase_ref)) / params.dx,
+           "front_radius_dx": r_eq(phase_ref) / params.dx,
+           "solid_nodes": int(np.sum(phase_ref))}
+    if mg_lost is not None and mg_lost_ref is not None:
+        out["mg_mass_lost"] = float(mg_lost_ref)
+        out["mg_mass_lost_rel"] = abs(mg_lost - mg_lost_ref) / max(abs(mg_lost_ref), 1e-300)
+    return out

@@ -456,6 +456,24 @@ __global__ void k_weights(int n, const int* row, const int* col, const double* p
   }
 }
 
+// The hash of grid.h:81-85 is an int; mx, my come from static_cast<int> of a double
+// (grid.h:75-78).  A wide bounding box with small cells overflows both, after which
+// wrapped hashes would index the cell arrays out of bounds.  The cell counts per axis are
+// therefore formed in double first; the grid must hold at most `limit` cells (the int
+// range for the allocating build, the scratch size for the allocation-free one).  A NaN
+// extent (non-finite coordinates) fails the test as well.
+nnpp_status check_hash_grid(const double bb[6], double cx, double cy, double cz, double limit) {
+  const double ncx = std::floor((bb[1] - bb[0]) / cx) + 1.0;
+  const double ncy = std::floor((bb[3] - bb[2]) / cy) + 1.0;
+  const double ncz = std::floor((bb[5] - bb[4]) / cz) + 1.0;
+  const double cells = ncx * ncy * ncz;
+  if (!(cells <= limit))
+    return set_error(NNPP_ERR_INVALID,
+                     "build: hash grid of the bounding box has too many cells (cell sizes too "
+                     "small for the node extent, or non-finite coordinates)");
+  return NNPP_OK;
+}
+
 int grid_for(long long n, int block, int cap = 152 * 16) {
   long long g = (n + block - 1) / block;
   if (g < 1) g = 1;
@@ -510,6 +528,7 @@ nnpp_status build_ref_lists(cudaStream_t st, int N, const double* x, const doubl
   NNPP_TRY(bbox_gpu(st, x, y, z, N, out.bbox));
   const double x0 = out.bbox[0], x1 = out.bbox[1], y0 = out.bbox[2], y1 = out.bbox[3],
                z0 = out.bbox[4];
+  NNPP_TRY(check_hash_grid(out.bbox, cx, cy, cz, (double)INT_MAX));
   // Step 1 (grid.h:75-86); multipliers computed on the host as in the reference
   const int mx = static_cast<int>((x1 - x0) / cx) + 1;
   const int my = static_cast<int>((y1 - y0) / cy) + 1;
@@ -616,6 +635,9 @@ nnpp_status build_canonical_into(cudaStream_t st, int N, const double* x, const 
   double bb[6];
   NNPP_CUDA(cudaMemcpyAsync(bb, sc.bbox, sizeof(bb), cudaMemcpyDeviceToHost, st));
   NNPP_CUDA(cudaStreamSynchronize(st));
+  // The whole grid, not only its occupied part, must fit the scratch cell arrays: then
+  // no hash can wrap, and every hash indexes them in bounds.
+  NNPP_TRY(check_hash_grid(bb, cx, cy, cz, (double)sc.max_cells));
   const int mx = static_cast<int>((bb[1] - bb[0]) / cx) + 1;
   const int my = static_cast<int>((bb[3] - bb[2]) / cy) + 1;
   // hashes (grid.h:81-85)

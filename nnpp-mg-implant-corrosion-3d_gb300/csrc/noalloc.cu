@@ -6,7 +6,7 @@
 // nnpp_build_clouds_hash_noalloc builds the neighbour lists into buffers the caller owns,
 // with every temporary in one file-scope device array of fixed size.  That array exists on
 // every GPU on which this library is loaded, for the life of the process.
-#include <mutex>
+#include <string>
 
 #include "neighbours.cuh"
 
@@ -22,24 +22,16 @@ constexpr size_t kWords = kDoubles + (kInts + 1) / 2;  // 8-byte words, about 6.
 // array; its device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned long long g_build_scratch[kWords];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
-// Device address of the scratch on the current device, looked up once per device.
+// Device address of the scratch on the current device.  It is looked up on every call
+// (cheap next to the call's stream synchronisations) rather than cached: after a
+// cudaDeviceReset the module is loaded again and an address cached before it would be
+// stale.
 nnpp_status scratch_address(void** out) {
-  int dev = 0;
-  NNPP_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return nnpp::set_error(NNPP_ERR_UNSUPPORTED, "device ordinal too large");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_build_scratch);
-    if (e != cudaSuccess || !p)
-      return nnpp::set_error(NNPP_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_addr[dev] = p;
-  }
-  *out = g_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_build_scratch);
+  if (e != cudaSuccess || !p)
+    return nnpp::set_error(NNPP_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  *out = p;
   return NNPP_OK;
 }
 

@@ -23,7 +23,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
-REFERENCE_ROOT = os.environ.get("NNPP_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: NNPP_REFERENCE_ROOT, else "reference" beside this repository
+REFERENCE_ROOT = os.environ.get("NNPP_REFERENCE_ROOT",
+                                os.path.normpath(os.path.join(ROOT, "..", "reference")))
 
 SMALL = [(0, 20, 11), (1, 16, 11), (2, 14, 11), (3, 20, 11), (4, 15, 11)]
 FULL = [("lattice_block_20", 0, 20, 0), ("jittered_sphere_80", 1, 80, 1),

@@ -233,6 +233,10 @@ def test_torch_autograd_binding(gpu, orc, case):
     got = theta.grad.numpy()
     assert abs(got[0] - ref[0]) <= 1e-8 * abs(ref[0])
     assert abs(got[4] - ref[4]) <= 1e-8 * abs(ref[4])
+    # species 1-3 act through the potential only (gradients 100-1000x smaller) and carry the
+    # solves' tolerance, as in test_adjoint_fp64_matches_oracle
+    for k in range(1, 4):
+        assert abs(got[k] - ref[k]) <= 1e-5 * abs(ref[k]), (k, got, ref)
     # a second call from the reset state gives the same curve
     curve2 = ag.mass_loss_curve(theta.detach(), sim, base, N_STEPS, gpu.FP64, 25, SE)
     assert torch.equal(curve.detach(), curve2)
