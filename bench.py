@@ -124,11 +124,39 @@ def traffic_table():
         return {}
 
 
-def cpu_baseline(inp, max_seconds=25.0):
-    """FP64 oracle (the reference's algorithm restated, OpenMP, all host threads) on the same
-    512k workload; a bounded sample of whole steps."""
+def cpu_model():
+    """The host CPU's model name (lscpu), with the core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    if not name:
+        import platform
+        name = platform.processor() or platform.machine()
+    return "%s, %d cores" % (name, os.cpu_count() or 1)
+
+
+def load_oracle_module():
+    """The oracle (test infrastructure, the checker and the CPU baseline), built for the
+    host's own instruction set where the compiler supports it (the same bits as the portable
+    build: no FP contraction)."""
+    os.environ.setdefault("NNPP_ORACLE_NATIVE", "1")
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    return O
+
+
+def cpu_baseline(inp, max_seconds=25.0):
+    """FP64 oracle (the reference's algorithm restated, OpenMP, all host threads) on the same
+    512k workload; a bounded sample of whole steps from t = 0.  Returns the line's
+    cpu_baseline object and the oracle's state after those steps (the errors of the GPU run
+    are stated against it)."""
+    O = load_oracle_module()
     cores = O.set_threads(os.cpu_count() or 1)
     o = O.Oracle.from_synth(inp)
     t0 = time.perf_counter()
@@ -144,9 +172,12 @@ def cpu_baseline(inp, max_seconds=25.0):
         if el > max_seconds or steps >= 50:
             break
     value = inp["N"] * steps / el
+    c, phi, ph, _ = o.state()
+    state = (steps, c, phi, ph, o.diagnostics()["mg_mass_lost"])
     return {"value": value, "unit": "node-steps/s", "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(), "library": O.library_path(),
             "sample": "%d whole explicit steps of the 512k workload from t=0 (FP64 CG to 1e-10); "
-                      "neighbour build %.2f s" % (steps, t_build)}
+                      "neighbour build %.2f s" % (steps, t_build)}, state
 
 
 # the benchmarked workload, named the same in both arms
@@ -158,10 +189,10 @@ def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
         return 0
-    nn = load_package()
-    inp = nn.synth(WORKLOAD["kind"], WORKLOAD["n_side"], WORKLOAD["seed"])
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    # inputs from the oracle library's copy of the seeded generator: this arm loads no
+    # product code
+    O = load_oracle_module()
+    inp = O.synth(WORKLOAD["kind"], WORKLOAD["n_side"], WORKLOAD["seed"])
     cores = O.set_threads(os.cpu_count() or 1)
     o = O.Oracle.from_synth(inp)
     o.build_neighbours()
@@ -183,12 +214,13 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD_DESC,
-                       "precision": "mixed (FP32 bond sums and inner CG, FP32-pair/FP64 refinement to 1e-10)", "n_nodes": inp["N"], "parallelism": "single",
+            "config": {"workload": WORKLOAD_DESC, "n_nodes": inp["N"], "parallelism": "single",
                        "potential_tol": 1e-10,
                        "precision": "fp64 (oracle restatement of the reference's explicit step, "
-                                    "OpenMP on the host cores)"},
+                                    "OpenMP on the host cores)",
+                       "cpu_model": cpu_model()},
             "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": cores, "kind": "port",
+                             "cpu_model": cpu_model(), "library": O.library_path(),
                              "sample": "%d explicit steps of the 512k workload after 1 untimed step (bounded to ~60 s)" % steps},
             "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -296,6 +328,38 @@ def ensemble_cost(nn, steps, members=64, seed=4):
     return out
 
 
+def moving_front_cost(nn, inp, pre_steps, steps):
+    """The 512k workload in its dissolving phase: after pre_steps steps the implant front
+    moves (solid nodes flip every few steps), so the two-level preconditioner's coarse
+    inverse is rebuilt at every refresh check (every 64 steps) that sees a changed phase.
+    Times `steps` steps of the mixed and of the FP64 path from there, with the rebuilds
+    inside the timed window, and states their share."""
+    out = {"pre_steps": pre_steps, "steps": steps}
+    ms_by = {}
+    for name, prec in (("mixed", nn.MIXED), ("fp64", nn.FP64)):
+        sim = nn.Simulation.from_synth(inp)
+        sim.build_neighbours()
+        sim.forward(pre_steps, prec)
+        d0, c0 = sim.diagnostics(), sim.coarse_stats()
+        ms = sim.forward_timed(steps, prec)
+        d1, c1 = sim.diagnostics(), sim.coarse_stats()
+        rb = c1["run_rebuilds"] - c0["run_rebuilds"]
+        rms = c1["run_rebuild_ms"] - c0["run_rebuild_ms"]
+        ms_by[name] = ms
+        out[name] = {"ms_per_step": ms / steps, "value": inp["N"] * steps / (ms / 1e3),
+                     "coarse_rebuilds": rb,
+                     "warm_rebuilds": c1["warm_rebuilds"] - c0["warm_rebuilds"],
+                     "ms_per_rebuild": rms / rb if rb else None,
+                     "rebuild_share_of_window": rms / ms,
+                     "amortised_rebuild_ms_per_step": rms / steps,
+                     "newton_schulz_steps_last": c1["last_ns_steps"],
+                     "inner_cg_per_step": (d1["cg_iterations_total"] - d0["cg_iterations_total"]) / steps,
+                     "solid_nodes_flipped_in_window": int(d0["solid_count"] - d1["solid_count"])}
+        del sim
+    out["mixed_over_fp64"] = ms_by["fp64"] / ms_by["mixed"]
+    return out
+
+
 def large_cost(nn, steps):
     """The 2M-node screw: neighbour build in the reference's order (bit-exact) and the mixed
     step throughput."""
@@ -309,10 +373,6 @@ def large_cost(nn, steps):
     return {"workload": "jittered, randomly permuted 126^3 lattice (%d nodes), screw implant" % inp["N"],
             "neighbour_build_s": t_build, "steps": steps,
             "value": inp["N"] * steps / (ms / 1e3), "unit": "node-steps/s"}
-
-
-def rel_l2(a, b):
-    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
 def run_ours(args):
@@ -376,12 +436,9 @@ def run_ours(args):
     # accuracy of the mixed path against the FP64 path after the same steps
     c_m, phi_m, ph_m = sim.state()
     c_d, phi_d, ph_d = sim64.state()
-    acc = {"rel_l2_c": rel_l2(c_m, c_d), "rel_l2_phi": rel_l2(phi_m, phi_d),
-           "mask_mismatch": int((ph_m != ph_d).sum()),
-           "front_dx": float(((3 * (ph_m.sum() - ph_d.sum()) * p.dx * p.dy * p.dz / (4 * np.pi))
-                              ** (1 / 3) if ph_m.sum() != ph_d.sum() else 0.0) / p.dx),
-           "mg_mass_lost_rel": abs(d1["mg_mass_lost"] - d64["mg_mass_lost"]) /
-                               max(abs(d64["mg_mass_lost"]), 1e-300)}
+    acc = nn.compare_states(p, c_m, phi_m, ph_m, c_d, phi_d, ph_d, d1["mg_mass_lost"],
+                            d64["mg_mass_lost"])
+    acc["steps"] = args.warmup + args.steps
 
     inner = d1["cg_iterations_total"] - d0["cg_iterations_total"]
     outer = d1["outer_iterations_total"] - d0["outer_iterations_total"]
@@ -445,7 +502,7 @@ def run_ours(args):
     with ProfileRange("variants"):
         for var, key in ((0, "gather8"), (1, "bulk_staged"), (2, "smem_window8"), (3, "gather16"),
                          (4, "smem_window16"), (5, "smem_window16_l2pf"), (6, "gather16_l2pf"),
-                         (7, "smem_window8_l2pf")):
+                         (7, "smem_window8_l2pf"), (8, "halo_recompute")):
             try:
                 sim.set_tuning(tuned[0], tuned[1], var)
                 with ProfileRange("variant%d" % var):
@@ -504,14 +561,29 @@ def run_ours(args):
     if rank == 0 and args.ensemble_steps > 0:
         ensemble = ensemble_cost(nn, args.ensemble_steps)
         log("ensemble: %s" % json.dumps(ensemble))
+    front = None
+    if rank == 0 and args.front_steps > 0:
+        front = moving_front_cost(nn, inp, args.front_pre, args.front_steps)
+        log("moving front: %s" % json.dumps(front))
     large = None
     if rank == 0 and args.large_steps > 0:
         large = large_cost(nn, args.large_steps)
         log("large: %s" % json.dumps(large))
 
     cpu = None
+    acc_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(inp)
+        cpu, ostate = cpu_baseline(inp)
+        # the mixed GPU path from t = 0 for the oracle's steps: its errors against the FP64
+        # oracle (rel-L2 of c and phi, front position in dx, Mg mass lost)
+        simo = nn.Simulation.from_synth(inp)
+        simo.build_neighbours()
+        simo.forward(ostate[0], nn.MIXED)
+        c_g, phi_g, ph_g = simo.state()
+        acc_oracle = nn.compare_states(p, c_g, phi_g, ph_g, ostate[1], ostate[2], ostate[3],
+                                       simo.diagnostics()["mg_mass_lost"], ostate[4])
+        acc_oracle["steps"] = ostate[0]
+        del simo
 
     if rank != 0:
         return 0
@@ -529,6 +601,7 @@ def run_ours(args):
             "fp64_gpu": {"value": value64, "ms_per_step": ms64 / args.steps,
                          "mixed_over_fp64": value / world / value64},
             "accuracy_vs_fp64_gpu": acc,
+            "accuracy_vs_oracle": acc_oracle,
             "solver": {"inner_cg_per_step": inner / args.steps, "outer_per_step": outer / args.steps,
                        "fp64_cg_per_step": (d64["cg_iterations_total"] - d64_0["cg_iterations_total"]) / args.steps,
                        "preconditioner": "two-level (Jacobi + coarse aggregates)" if pk else "jacobi",
@@ -541,6 +614,7 @@ def run_ours(args):
             "adjoint": adj,
             "ensemble": ensemble,
             "large_2m": large,
+            "moving_front": front,
             "neighbour_build_s": t_build,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -561,6 +635,10 @@ def main():
                     help="steps of the 64-instance ensemble measurement (0: skip)")
     ap.add_argument("--large-steps", type=int, default=10,
                     help="steps of the 2M-node measurement (0: skip)")
+    ap.add_argument("--front-steps", type=int, default=640,
+                    help="timed steps of the 512k workload's dissolving phase (0: skip)")
+    ap.add_argument("--front-pre", type=int, default=2000,
+                    help="steps run before the dissolving-phase window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

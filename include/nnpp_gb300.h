@@ -58,6 +58,17 @@ typedef enum nnpp_preconditioner {
   NNPP_PRECOND_TWO_LEVEL = 1   /* z = D^-1 r + P A_c^-1 P^T r, aggregates of bin blocks     */
 } nnpp_preconditioner;
 
+/* Device-side checks (nnpp_set_checks), for debugging and for tests of the failure paths. */
+typedef enum nnpp_check {
+  NNPP_CHECK_BOUNDS = 1,       /* the halo-staged CG operator (operator 8) checks every quad,
+                                  row and neighbour code against its array before using it;
+                                  a violation is skipped and reported as NNPP_ERR_CUDA */
+  NNPP_CHECK_WAIT_PROBE = 2    /* test of the bounded-wait path: after each tile's copies have
+                                  landed, operator 8 also waits, bounded, on a barrier that
+                                  nothing completes; the call then returns NNPP_ERR_CUDA (its
+                                  results are invalid; nnpp_reset makes the handle usable) */
+} nnpp_check;
+
 typedef enum nnpp_order_mode {
   NNPP_ORDER_REFERENCE = 0,  /* within-cell order of std::sort as in grid.h:90 (bit-exact) */
   NNPP_ORDER_CANONICAL = 1   /* within-cell order by node index (stable counting sort)   */
@@ -150,12 +161,13 @@ nnpp_status nnpp_build_clouds_hash(int max_node_no, double r, double dx, double 
  * 0) and d_cloud_lengths (N ints) -- on `stream` (a cudaStream_t; NULL for the legacy
  * default stream).  It calls no cudaMalloc/cudaFree: every temporary lives in one
  * fixed-size device array (about 6.3 MB) that each GPU loading this library holds until
- * the process exits.  N is limited to 262,144 nodes and the hash grid to 262,144 cells;
- * larger inputs return NNPP_ERR_INVALID.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress), so make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU (other streams, other host threads)
- * race and must be serialised by the caller.  The call synchronises `stream` three times
- * to read the bounding box, the grid size and the capacity flag. */
+ * the process exits.  N is limited to 262,144 nodes and the hash grid over the nodes'
+ * bounding box (cells of dx x dy x dz) to 262,144 cells; larger inputs return
+ * NNPP_ERR_INVALID.  Every call looks up that array's device address on the current device
+ * (cudaGetSymbolAddress).  Calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.  The call
+ * synchronises `stream` three times to read the bounding box, the grid size and the
+ * capacity flag back to the host. */
 nnpp_status nnpp_build_clouds_hash_noalloc(int max_node_no, double r, double dx, double dy,
                                            double dz, int n_nodes, const double* d_nodes_colmajor,
                                            int* d_clouds_colmajor, int* d_cloud_lengths,
@@ -240,6 +252,21 @@ nnpp_status nnpp_set_preconditioner(nnpp_handle* h, int kind, int refresh_every)
 nnpp_status nnpp_get_preconditioner(nnpp_handle* h, int* kind, int* coarse_unknowns, int* refresh_every,
                                     int64_t* rebuilds);
 
+/* Device-side checks of the handle's kernels: a combination of nnpp_check flags (0: none,
+ * the default).  Runs with checks launch the checked build of the kernels that have one.  No
+ * counterpart in the reference (whose only failure path is grid.h:187-189). */
+nnpp_status nnpp_set_checks(nnpp_handle* h, int flags);
+
+/* Rebuild statistics of the two-level preconditioner's coarse inverse: inverses computed
+ * since the handle was built, of which warm-started (Newton-Schulz from the previous
+ * inverse); rebuilds triggered by phase changes during runs and their summed duration in
+ * milliseconds (host clock, the stream drained before and after: the time a run spends on
+ * them); the Newton-Schulz steps of the last rebuild.  Any pointer may be NULL.  No
+ * counterpart in the reference (measurement). */
+nnpp_status nnpp_get_coarse_stats(nnpp_handle* h, int64_t* rebuilds, int64_t* warm_rebuilds,
+                                  int64_t* run_rebuilds, double* run_rebuild_ms,
+                                  int* last_ns_steps);
+
 /* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
  * NULL. */
 nnpp_status nnpp_get_state(nnpp_handle* h, double* c, double* phi, int* phase);
@@ -292,9 +319,13 @@ nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int r
  * of 8 / 16 bond columns), 1 operator and slice windows streamed by bulk copies into shared
  * memory, 2 / 4 slice windows copied into shared memory by asynchronous copies (batches of
  * 8 / 16), 5 / 6 / 7 the variants 4 / 3 / 2 with bulk L2 prefetches of the operator stream
- * a few batches ahead.  Chosen by the autotuner on the first run (0 / -1 before);
- * nnpp_set_tuning pins a configuration instead (bins in {2,4,8,16}, lanes in {4,8,16},
- * operator 0..7; NNPP_ERR_UNSUPPORTED when a tile halo or a slice window does not fit). */
+ * a few batches ahead, 8 the tile's halo (positions and the CG vector) staged in shared
+ * memory, rows and columns restricted to the nodes without a Dirichlet value of the
+ * potential, 2-byte neighbour codes streamed and the bond weights recomputed from the
+ * positions.  Chosen by the autotuner on the first run (0 / -1 before); nnpp_set_tuning pins
+ * a configuration instead (bins in {2,4,8,16}, lanes in {4,8,16}, operator 0..8;
+ * NNPP_ERR_UNSUPPORTED when a tile halo, a slice window or a tile's code block does not fit,
+ * or, for operator 8, the kernel exponent s is not 0 or the tiles are longer than 8 bins). */
 nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_node,
                             int* cg_operator);
 nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_node,
@@ -312,9 +343,12 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* h, int n_steps, int precision, int ck
 
 /* Storage of the recorded forward run.  0 (default): automatic, every step's FP64
  * snapshot (64 bytes per node and step) when they fit a quarter of the free device memory,
- * else checkpoints; 1: checkpoints every ckpt_every steps, backward recomputes each segment;
- * 2: every step's snapshot, NNPP_ERR_NOMEM when they do not fit.  The gradients do not depend
- * on the mode (bit for bit).  Discards a recorded run. */
+ * else as 1; 1: a state checkpoint every ckpt_every steps plus every step's solved potential
+ * (8 bytes per node and step) when those fit a quarter of the free memory: backward
+ * recomputes each segment's bond sums and updates from its checkpoint without re-solving the
+ * potential (else as 3); 2: every step's snapshot, NNPP_ERR_NOMEM when they do not fit;
+ * 3: checkpoints only, backward recomputes each segment's whole steps (the least memory).
+ * The gradients do not depend on the mode (bit for bit).  Discards a recorded run. */
 nnpp_status nnpp_set_adjoint_store(nnpp_handle* h, int mode);
 
 /* Backward half: given dL/d(mass_curve) (same length), run the adjoint of the explicit step

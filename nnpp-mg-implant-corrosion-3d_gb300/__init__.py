@@ -24,6 +24,8 @@ ORDER_REFERENCE = 0
 ORDER_CANONICAL = 1
 PRECOND_JACOBI = 0
 PRECOND_TWO_LEVEL = 1
+CHECK_BOUNDS = 1
+CHECK_WAIT_PROBE = 2
 
 STATUS = {0: "NNPP_OK", 1: "NNPP_ERR_INVALID", 2: "NNPP_ERR_CAPACITY", 3: "NNPP_ERR_NONFINITE",
           4: "NNPP_ERR_CG_NO_CONVERGE", 5: "NNPP_ERR_CUDA", 6: "NNPP_ERR_UNSUPPORTED",
@@ -111,6 +113,9 @@ _SIGS = {
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
+    "nnpp_set_checks": (C.c_int, [_P, C.c_int]),
+    "nnpp_get_coarse_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64), _DP, _IP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
     "nnpp_ensemble_forward": (C.c_int, [_P, C.c_int, C.c_int]),
     "nnpp_ensemble_forward_timed": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
@@ -311,6 +316,21 @@ class Simulation:
         _check(lib().nnpp_get_preconditioner(self._h, C.byref(k), C.byref(n), C.byref(r), C.byref(b)))
         return k.value, n.value, r.value, b.value
 
+    def set_checks(self, flags):
+        """Device-side checks (nnpp_set_checks): CHECK_BOUNDS, CHECK_WAIT_PROBE."""
+        _check(lib().nnpp_set_checks(self._h, int(flags)))
+
+    def coarse_stats(self):
+        """Coarse-inverse rebuilds: total, warm-started, triggered during runs, the run
+        rebuilds' summed milliseconds, Newton-Schulz steps of the last one."""
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        ms = C.c_double(0.0)
+        ns = C.c_int(0)
+        _check(lib().nnpp_get_coarse_stats(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(ms),
+                                           C.byref(ns)))
+        return {"rebuilds": a.value, "warm_rebuilds": b.value, "run_rebuilds": c.value,
+                "run_rebuild_ms": ms.value, "last_ns_steps": ns.value}
+
     def reset(self):
         """Back to the initial state of build_neighbours (lists and tuning kept)."""
         _check(lib().nnpp_reset(self._h))
@@ -350,8 +370,9 @@ class Simulation:
         return curve
 
     def set_adjoint_store(self, mode):
-        """Storage of the recorded forward run: 0 automatic, 1 checkpoints (backward
-        recomputes the segments), 2 every step's snapshot."""
+        """Storage of the recorded forward run: 0 automatic, 1 checkpoints and every step's
+        solved potential (backward recomputes the segments' bond sums only), 2 every step's
+        snapshot, 3 checkpoints only (backward recomputes whole steps)."""
         _check(lib().nnpp_set_adjoint_store(self._h, mode))
 
     def backward(self, dL_dcurve):

@@ -140,6 +140,27 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
     h.snap_all.reset();
     h.ckpts.resize((n_steps + ckpt_every - 1) / ckpt_every);
   }
+  // checkpoints: keep every step's solved potential as well (8 bytes per node and step) when
+  // it fits a quarter of the free memory; backward then recomputes only the bond sums
+  bool store_phi = false;
+  h.phi_all_valid = false;
+  if (!store_all && h.adjoint_store != 3) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      free_b = 0;
+    }
+    const size_t need = (size_t)n_steps * N;
+    store_phi = h.phi_all.size() >= need || need * sizeof(double) <= free_b / 4;
+    if (store_phi && h.phi_all.size() < need) {
+      h.phi_all.reset();
+      if (!h.phi_all.alloc(need)) {
+        cudaGetLastError();
+        store_phi = false;
+      }
+    }
+    if (!store_phi) h.phi_all.reset();
+  }
   double m0 = 0.0;
   NNPP_TRY(launch_sum_c0(h, h.scratch_d.get() + 8));
   NNPP_CUDA(cudaMemcpyAsync(&m0, h.scratch_d.get() + 8, sizeof(double), cudaMemcpyDeviceToHost, h.st));
@@ -155,6 +176,13 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
       NNPP_TRY(engine_run(*h.engine, 1, precision));
       NNPP_TRY(launch_snap_phi(h, h.snap_all.get() + (size_t)s * N));
       NNPP_TRY(launch_snap_state(h, h.snap_all.get() + (size_t)(s + 1) * N));
+      next = s + 1;
+    } else if (store_phi) {
+      // one step at a time: its solved potential (phi_prev after the step) is kept
+      if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
+      NNPP_TRY(engine_run(*h.engine, 1, precision));
+      NNPP_CUDA(cudaMemcpyAsync(h.phi_all.get() + (size_t)s * N, h.phi_prev.get(), sizeof(double) * N,
+                                cudaMemcpyDeviceToDevice, h.st));
       next = s + 1;
     } else {
       if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
@@ -173,6 +201,7 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   }
   NNPP_TRY(save_ckpt(h, h.fwd_end));
   h.snap_all_valid = store_all;
+  h.phi_all_valid = store_phi;
   h.fwd_nstep_end = h.nstep;
   h.coarse_event_cur = (int)h.coarse_events.size() - 1;
   std::copy(h.curve.begin(), h.curve.end(), mass_curve);
@@ -182,16 +211,20 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
 nnpp_status nnpp_set_adjoint_store(nnpp_handle* hp, int mode) {
   clear_error();
   if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
-  if (mode < 0 || mode > 2) return set_error(NNPP_ERR_INVALID, "adjoint store: 0 automatic, 1 checkpoints, 2 every step");
+  if (mode < 0 || mode > 3)
+    return set_error(NNPP_ERR_INVALID,
+                     "adjoint store: 0 automatic, 1 checkpoints, 2 every step, 3 checkpoints without potentials");
   Handle& h = hp->h;
   h.adjoint_store = mode;
   h.fwd_steps = 0;
   h.ckpts.clear();
   h.snap_all_valid = false;
-  if (mode == 1) {
+  h.phi_all_valid = false;
+  if (mode == 1 || mode == 3) {
     NNPP_CUDA(cudaSetDevice(h.device));
     NNPP_CUDA(cudaStreamSynchronize(h.st));
     h.snap_all.reset();
+    if (mode == 3) h.phi_all.reset();
   }
   return NNPP_OK;
 }
@@ -256,9 +289,18 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       NNPP_TRY(load_ckpt(h, h.ckpts[g]));
       NNPP_TRY(launch_snap_state(h, snap.get()));
       for (int n = s0; n < s1; ++n) {
-        NNPP_TRY(coarse_select(h, n, true));
-        NNPP_TRY(engine_run(e, 1, prec));
-        NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
+        if (h.phi_all_valid) {
+          // the step's potential as its solve left it, then its bond sums and update (the
+          // transport reads nothing else the solve writes): the forward's state bit for bit
+          NNPP_TRY(launch_load_phi(h, h.phi_all.get() + (size_t)n * N, snap.get() + (size_t)(n - s0) * N));
+          NNPP_TRY(launch_transport_b(e, make_view(e, 0, 0), prec, h.st, nullptr));
+          h.cur ^= 1;
+          NNPP_TRY(engine_params(e));
+        } else {
+          NNPP_TRY(coarse_select(h, n, true));
+          NNPP_TRY(engine_run(e, 1, prec));
+          NNPP_TRY(launch_snap_phi(h, snap.get() + (size_t)(n - s0) * N));
+        }
         NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
       }
     }

@@ -55,6 +55,7 @@ nnpp_status check_after(Handle& h, long long nc_before) {
   DevState ds;
   NNPP_TRY(read_state(h, &ds));
   if (ds.wait_timeout) return set_error(NNPP_ERR_CUDA, "a bounded device wait timed out");
+  if (ds.bounds_error) return set_error(NNPP_ERR_CUDA, "a device index check failed (nnpp_set_checks)");
   if (ds.nonfinite) return set_error(NNPP_ERR_NONFINITE, "non-finite concentration in the state");
   if (h.strict && ds.cg_nc > nc_before)
     return set_error(NNPP_ERR_CG_NO_CONVERGE, "potential solve hit its iteration cap");
@@ -744,6 +745,30 @@ nnpp_status nnpp_get_preconditioner(nnpp_handle* hp, int* kind, int* coarse_unkn
   return NNPP_OK;
 }
 
+nnpp_status nnpp_set_checks(nnpp_handle* hp, int flags) {
+  NNPP_GUARD(hp);
+  if (flags & ~(NNPP_CHECK_BOUNDS | NNPP_CHECK_WAIT_PROBE))
+    return set_error(NNPP_ERR_INVALID, "set_checks: unknown flag");
+  Handle& h = hp->h;
+  NNPP_CUDA(cudaSetDevice(h.device));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  h.checks = flags;
+  if (h.engine && h.built) NNPP_TRY(engine_params(*h.engine));
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_coarse_stats(nnpp_handle* hp, int64_t* rebuilds, int64_t* warm_rebuilds,
+                                  int64_t* run_rebuilds, double* run_rebuild_ms, int* last_ns_steps) {
+  NNPP_GUARD(hp);
+  const Coarse& c = hp->h.coarse;
+  if (rebuilds) *rebuilds = c.rebuilds;
+  if (warm_rebuilds) *warm_rebuilds = c.warm_rebuilds;
+  if (run_rebuilds) *run_rebuilds = c.timed_rebuilds;
+  if (run_rebuild_ms) *run_rebuild_ms = c.rebuild_ms;
+  if (last_ns_steps) *last_ns_steps = c.ns_steps;
+  return NNPP_OK;
+}
+
 nnpp_status nnpp_set_params(nnpp_handle* hp, const nnpp_params* p) {
   NNPP_GUARD(hp);
   NNPP_TRY(check_params(p));
@@ -780,7 +805,7 @@ nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_no
   const int T = bins_per_tile, W = lanes_per_node;
   if ((T != 2 && T != 4 && T != 8 && T != 16) || (W != 4 && W != 8 && W != 16) ||
       cg_operator < 0 || cg_operator >= kSpmvVariants)
-    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, operator 0..7");
+    return set_error(NNPP_ERR_INVALID, "set_tuning: bins per tile in {2,4,8,16}, lanes in {4,8,16}, operator 0..8");
   Handle& h = hp->h;
   Engine& e = *h.engine;
   NNPP_CUDA(cudaStreamSynchronize(h.st));
@@ -788,6 +813,10 @@ nnpp_status nnpp_set_tuning(nnpp_handle* hp, int bins_per_tile, int lanes_per_no
   NNPP_TRY(prepare_kernels(e.halo_max, e.bond_max, W));
   if (spmv_needs_windows(cg_operator) && !spmv_staged_fits(e))
     return set_error(NNPP_ERR_UNSUPPORTED, "set_tuning: a slice window exceeds the staged operators' capacity");
+  if (cg_operator == kSpmvHalo && !spmv_halo_fits(e))
+    return set_error(NNPP_ERR_UNSUPPORTED,
+                     "set_tuning: the halo-staged operator needs s = 0, tiles of at most 8 bins and a "
+                     "tile halo and code block within a CTA's shared memory");
   e.W = W;
   e.spmv_variant = cg_operator;
   e.tuned = true;

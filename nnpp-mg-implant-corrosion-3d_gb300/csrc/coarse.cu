@@ -15,6 +15,7 @@
 // valid preconditioner.  The schedule depends only on the step count and the phases, so it is
 // reproducible, and forward_ckpt records each rebuilt inverse for backward to replay.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -393,7 +394,11 @@ nnpp_status coarse_check(Handle& h) {
   NNPP_CUDA(cudaMemcpyAsync(&changed, c.count.get(), sizeof(int), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
   if (changed == 0) return NNPP_OK;
+  const auto t0 = std::chrono::steady_clock::now();
   NNPP_TRY(coarse_refresh(h));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  c.rebuild_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  c.timed_rebuilds += 1;
   if (h.coarse_record) NNPP_TRY(coarse_record_event(h, h.nstep - h.coarse_base));
   return NNPP_OK;
 }

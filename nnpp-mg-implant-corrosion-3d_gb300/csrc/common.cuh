@@ -68,6 +68,7 @@ struct DevState {
   long long outer_total;
   int nonfinite;
   int wait_timeout;   // a bounded device wait gave up (the step's results are invalid)
+  int bounds_error;   // a device index check (nnpp_set_checks) found an index out of range
   // potential solve
   double bnorm2;      // ||b_eff||^2
   double rnorm2;      // ||r||^2 of the outer (FP64) residual

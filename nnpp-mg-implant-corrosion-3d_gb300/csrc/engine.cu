@@ -55,17 +55,25 @@ nnpp_status build_lists(Engine& e, int T) {
   std::vector<TileDesc> tiles;
   std::vector<Chunk> chunks;
   std::vector<SliceDesc> slices;
+  std::vector<HTile> htiles;
   std::vector<int> meta(6 * M);
-  bool fit = true;
-  int hm = 0, bmax = 0;
+  bool fit = true, hop = true;
+  int hm = 0, bmax = 0, cmax = 0, qmax = 0;
   for (int i = 0; i < M; ++i) {
     Handle& h = *e.members[i];
     meta[i] = (int)tiles.size();
     int hmi = 0, bmi = 0;
     meta[4 * M + i] = (int)slices.size();
     bool wf = false;
+    const int tile0 = (int)tiles.size();
     NNPP_TRY(build_tiles(h, T, tiles, slices, i, &hmi, &bmi, &wf));
     fit = fit && wf;
+    int cmi = 0, qmi = 0;
+    bool hok = false;
+    NNPP_TRY(build_halo_op(h, T, tiles, tile0, htiles, &cmi, &qmi, &hok));
+    hop = hop && hok;
+    cmax = std::max(cmax, cmi);
+    qmax = std::max(qmax, qmi);
     meta[5 * M + i] = (int)slices.size() - meta[4 * M + i];
     meta[M + i] = (int)tiles.size() - meta[i];
     hm = std::max(hm, hmi);
@@ -85,6 +93,9 @@ nnpp_status build_lists(Engine& e, int T) {
   e.nchunks = (int)chunks.size();
   e.nslices = (int)slices.size();
   e.windows_fit = fit;
+  e.halo_op = hop;
+  e.hcode_max16 = cmax;
+  e.hquad_max = qmax;
   int wmax = 16;
   for (const SliceDesc& d : slices) wmax = std::max(wmax, d.wtotal);
   e.win_cap = (wmax + 15) & ~15;
@@ -93,7 +104,8 @@ nnpp_status build_lists(Engine& e, int T) {
   e.T = T;
   const int stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
   if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
-      !e.d_slices.alloc(std::max<size_t>(slices.size(), 1)) || !e.d_ticket.alloc(M + 3) ||
+      !e.d_slices.alloc(std::max<size_t>(slices.size(), 1)) || !e.d_htiles.alloc(std::max<size_t>(htiles.size(), 1)) ||
+      !e.d_ticket.alloc(M + 3) ||
       !e.d_partials.alloc((size_t)kReduceSlots * stride) ||
       !e.d_inst[0].alloc(M) || !e.d_inst[1].alloc(M))
     return set_error(NNPP_ERR_NOMEM, "engine work lists");
@@ -102,6 +114,8 @@ nnpp_status build_lists(Engine& e, int T) {
   NNPP_CUDA(cudaMemcpyAsync(e.d_meta.get(), meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, e.st));
   if (!slices.empty())
     NNPP_CUDA(cudaMemcpyAsync(e.d_slices.get(), slices.data(), sizeof(SliceDesc) * slices.size(), cudaMemcpyHostToDevice, e.st));
+  if (!htiles.empty())
+    NNPP_CUDA(cudaMemcpyAsync(e.d_htiles.get(), htiles.data(), sizeof(HTile) * htiles.size(), cudaMemcpyHostToDevice, e.st));
   NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, sizeof(unsigned int) * (M + 3), e.st));
   NNPP_CUDA(cudaStreamSynchronize(e.st));
   engine_destroy_graphs(e);
@@ -156,6 +170,7 @@ nnpp_status tune(Engine& e, int prec) {
       const int nvar = prec == NNPP_MIXED ? kSpmvVariants : 1;
       for (int var = 0; var < nvar; ++var) {
         if (!win && spmv_needs_windows(var)) continue;
+        if (var == kSpmvHalo && !spmv_halo_fits(e)) continue;
         e.spmv_variant = var;
         NNPP_TRY(set_active(e, 1, 1));
         NNPP_TRY(launch_cg_spmv_b(e, v, prec, e.st));
@@ -329,6 +344,13 @@ nnpp_status prepare_run(Engine& e, int prec) {
     engine_destroy_graphs(e);
     e.coarse_graphs = split;
   }
+  // the graphs hold the checked or the plain build of the kernels
+  int checks = 0;
+  for (Handle* h : e.members) checks |= h->checks;
+  if (checks != e.checks) {
+    engine_destroy_graphs(e);
+    e.checks = checks;
+  }
   NNPP_TRY(refresh_params(e));
   return NNPP_OK;
 }
@@ -365,6 +387,8 @@ EngineView make_view(Engine& e, int parity, int in_graph) {
   v.slice_first = e.d_meta.get() + 4 * M;
   v.slice_count = e.d_meta.get() + 5 * M;
   v.slices = e.d_slices.get();
+  v.htiles = e.d_htiles.get();
+  v.hcode_max16 = e.hcode_max16;
   v.nslices = e.nslices;
   v.ticket = e.d_ticket.get();
   v.partials = e.d_partials.get();

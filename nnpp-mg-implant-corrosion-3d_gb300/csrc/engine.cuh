@@ -24,6 +24,21 @@ struct TileDesc {
   int bond1;               // one past the last bond of the own nodes
 };
 
+// The halo-staged CG operator (variant 8) over the rows and columns that can be unknowns of
+// the potential solve (nodes without a Dirichlet value of the potential; phases only change
+// from solid to liquid, so the set is fixed for the run).  A tile's such rows are sorted by
+// their number of such neighbours (initially solid rows last) and grouped in quads of four
+// rows; a warp runs a quad with eight lanes per row.  A quad's codes (the 16-bit halo slot of
+// each neighbour, the tile's padding slot after the row's end) lie pass-major: pass p, row g,
+// lane j at coff + 32 p + 8 g + j, so that a pass of the warp reads 64 contiguous bytes.
+struct HTile {             // parallel to the engine's tile list
+  int q0, nq;              // the tile's quads (instance-local quad indices)
+  int cstart16, clen16;    // its code block in the instance's code array, in 16-byte units
+  int bx0, by, bz;         // first own bin along x, bin row (y, z)
+  int T;                   // bins per tile
+};
+// (HQuad, the quad descriptor, is in handle.cuh)
+
 // An elementwise work item: nodes [begin, end) of one instance.
 struct Chunk {
   int inst;
@@ -66,6 +81,7 @@ struct EngineView {
   const int* tile_count;    // per instance: number of tiles
   const int* chunk_first;
   const int* chunk_count;
+  const HTile* htiles;      // parallel to tiles (halo-staged CG operator)
   const SliceDesc* slices;  // grouped by instance, tiles in order
   const int* slice_first;
   const int* slice_count;
@@ -77,10 +93,12 @@ struct EngineView {
   int stride;               // max(ntiles, nchunks, nslices): slot stride of partials
   int halo_max;             // largest halo (dynamic shared memory sizing)
   int bond_max;             // largest staged bond range of a tile (bond1 - bond0)
+  int hcode_max16;          // largest code block of a tile (16-byte units, variant 8)
 };
 
 constexpr int kChunk = 1024;  // nodes per elementwise work item
-constexpr int kSpmvVariants = 8;  // FP32 CG operator variants the autotuner times
+constexpr int kSpmvVariants = 9;  // FP32 CG operator variants the autotuner times
+constexpr int kSpmvHalo = 8;      // the halo-staged variant with recomputed weights
 
 struct Engine {
   std::vector<Handle*> members;
@@ -90,7 +108,12 @@ struct Engine {
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
   int spmv_variant = 0;     // FP32 CG operator: 0, 3 L1/L2 gathers (batches of 8, 16),
                             // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16),
-                            // 5, 6, 7: 4, 3, 2 with L2 prefetch of the operator stream
+                            // 5, 6, 7: 4, 3, 2 with L2 prefetch of the operator stream,
+                            // 8 tile halo in shared memory, weights recomputed
+  bool halo_op = false;     // every member has the variant 8 layout
+  int checks = 0;           // nnpp_set_checks flags of any member (the checked kernels run)
+  int hcode_max16 = 0;      // largest tile code block (16-byte units)
+  int hquad_max = 0;        // most quads of a tile
   bool windows_fit = false; // every slice window fits kWinCap (the staged operator runs)
   int win_cap = 0;          // largest slice window (nodes, multiple of 16)
   int grid = 0;
@@ -102,6 +125,7 @@ struct Engine {
   DBuf<Chunk> d_chunks;
   DBuf<int> d_meta;         // tile/chunk/slice first and count (6*M)
   DBuf<SliceDesc> d_slices;
+  DBuf<HTile> d_htiles;
   DBuf<unsigned int> d_ticket;
   DBuf<double> d_partials;
   int ntiles = 0, nchunks = 0, nslices = 0;
@@ -127,10 +151,17 @@ void engine_destroy_graphs(Engine& e);
 // tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& slices,
                         int inst, int* halo_max, int* bond_max, bool* windows_fit);
+// the variant 8 layout of one instance (after build_tiles, same T): its HTile entries are
+// appended to htiles (parallel to the instance's tiles); false in *ok when the layout does
+// not apply (a kernel exponent s != 0, a halo of 65535 nodes or more)
+nnpp_status build_halo_op(Handle& h, int T, const std::vector<TileDesc>& tiles, int tile0,
+                          std::vector<HTile>& htiles, int* code_max16, int* quad_max, bool* ok);
 
 // step.cu launchers (batched)
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st);
 bool spmv_staged_fits(const Engine& e);
+// the halo-staged variant fits the shared memory of a CTA
+bool spmv_halo_fits(const Engine& e);
 // the variant gathers from per-slice shared-memory windows (needs spmv_staged_fits)
 inline bool spmv_needs_windows(int variant) {
   return variant == 1 || variant == 2 || variant == 4 || variant == 5 || variant == 7;
@@ -159,6 +190,8 @@ nnpp_status launch_adj_transport(const Engine& e, const EngineView& v, const Rec
 nnpp_status launch_adj_combine(Handle& h, const double* mu, double* lam, double inject);
 nnpp_status launch_snap_state(Handle& h, Rec64* dst);
 nnpp_status launch_snap_phi(Handle& h, Rec64* dst);
+// a stored solved potential into phi64, the current records and the snapshot dst
+nnpp_status launch_load_phi(Handle& h, const double* phi, Rec64* dst);
 nnpp_status launch_adj_solve_setup(Handle& h, const Rec64* snap, const double* psi_prev);
 nnpp_status launch_record_solve(Handle& h, int slot);
 nnpp_status launch_adj_transport32(const Engine& e, const EngineView& v, Handle& h, const Rec64* snap,

@@ -10,6 +10,16 @@
 
 namespace nnpp {
 
+// A quad of the halo-staged CG operator (variant 8, see HTile in engine.cuh): four rows of
+// one tile run by one warp, eight lanes per row.
+struct HQuad {
+  int rows[4];             // internal node index of row g, -1 for an empty row
+  int npass;               // passes of eight codes per row
+  int coff_abs;            // first code in the instance's code array
+  int coff_rel;            // first code relative to the tile's code block
+  int padcode;             // the tile's padding slot (its halo size)
+};
+
 // Everything a step kernel reads or writes for one instance; stored in device memory, one
 // per instance of a batched launch.  Pointers are device pointers into the instance's
 // buffers (internal node order).
@@ -85,6 +95,15 @@ struct KParams {
   float* r0_32;
   float* t32;
   int cf, cna0, cna1, cna2, nb0, nb1, nb2;
+  // halo-staged CG operator (variant 8): quads, codes, FP32 bin-local positions and the
+  // weight in bin units w = beta / xi^3 with beta = min(1, hc0 - hc1 xi); the operator's
+  // off-diagonal sum is hsw * sum w z (hsw = dV / h^3)
+  const HQuad* hquad;
+  const unsigned short* hcode;
+  const float4* posrec;
+  float hinv, hc0, hc1, hsw;
+  int hquad_n;                   // quads of the instance
+  int checks;                    // nnpp_set_checks flags
 };
 
 enum GraphKind { kGraphStep2 = 0, kGraphStep1 = 1, kGraphSolve = 2, kGraphKinds = 3 };
@@ -115,6 +134,8 @@ struct Coarse {
   long long rebuilds = 0;  // inverses computed since the handle was built
   long long warm_rebuilds = 0;  // of which Newton-Schulz started from the previous inverse
   int ns_steps = 0;        // Newton-Schulz steps of the last rebuild
+  long long timed_rebuilds = 0;  // rebuilds triggered by phase changes within a run
+  double rebuild_ms = 0.0;       // their host-observed duration (stream drained on both sides)
   ~Coarse();
 };
 
@@ -140,6 +161,10 @@ struct Handle {
   DBuf<float4> phi4;
   DBuf<float4> posrec;
   float h32 = 0.f;
+  DBuf<HQuad> hquad;     // halo-staged CG operator (variant 8) of the current tiles
+  DBuf<unsigned short> hcode;
+  bool halo_op_ok = false;
+  int checks = 0;               // nnpp_set_checks flags
   int tiles_T = 0;
   // per-node constants, internal order
   DBuf<unsigned char> dirmask;
@@ -211,6 +236,10 @@ struct Handle {
   int adjoint_store = 0;
   DBuf<Rec64> snap_all;         // (steps + 1) x N snapshots of the recorded forward
   bool snap_all_valid = false;
+  // with checkpoints: every step's solved potential (steps x N), so that backward
+  // recomputes a segment's steps without their potential solves
+  DBuf<double> phi_all;
+  bool phi_all_valid = false;
   int fwd_steps = 0, ck_every = 0, sample_every = 0, fwd_prec = NNPP_FP64;
   std::vector<double> curve;
   ~Handle();

@@ -822,6 +822,246 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   }
 }
 
+// Halo-staged FP32 CG operator with recomputed weights (variant 8): the product of
+// k_cg_spmv32 (q = A z + beta q, p = z + beta p, partial p.q) over the rows and columns that
+// can be unknowns of the potential solve (no Dirichlet value of the potential; the other
+// columns hold z = 0).  A CTA claims tiles one at a time; for each it
+//   - starts one bulk copy of the tile's code block into shared memory (an mbarrier wait,
+//     bounded: a timeout is recorded in the instance's state and reported as NNPP_ERR_CUDA),
+//   - stages the tile's halo as float4 {X, Y, Z, z}: the node's position in units of the bin
+//     side, relative to the centre of the halo's box (|X| <= T/2 + 1, |Y|, |Z| <= 1.5, so
+//     FP32 keeps it to ~1e-7 of a bin), and the CG vector z,
+//   - then its warps take the tile's quads (longest first, from a shared counter); eight
+//     lanes per row walk the row's codes (halo slots) and recompute each bond's weight
+//     beta(xi) dV / xi^3 (utils.h:17-25, s = 0) from the two staged positions.
+// HBM sees the 2-byte codes; positions and z of the halo come through L2.
+constexpr unsigned kHaloWaitPolls = 1u << 22;  // polls of the tile copies' mbarrier
+// z staging of a halo of hal_cap - 1 nodes: every row rounded out to 16-byte boundaries
+__host__ __device__ constexpr int halo_zcap(int hal_cap) { return ((hal_cap - 1 + 9 * 8) + 3) & ~3; }
+
+__device__ __forceinline__ float halo_bond(const float4& pa, const float4& pb, float hc0, float hc1) {
+  const float dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
+  const float x2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float ri = rsqrtf(x2);
+  const float be = fminf(1.0f, fmaf(-hc1, x2 * ri, hc0));
+  return be * (ri * ri) * ri * pb.w;
+}
+
+// CHECK (nnpp_set_checks): every quad, row and code is checked against its bounds before
+// it indexes an array (a bad one is recorded in bounds_error and replaced by the padding
+// slot or an empty row), and with NNPP_CHECK_WAIT_PROBE the kernel also waits, bounded, on a
+// barrier that nothing completes after each tile's copies have landed -- the timeout path
+// without a copy in flight.
+template <bool CHECK>
+__global__ void __launch_bounds__(kBlock, 3) k_cg_spmv32h(EngineView v, int hal_cap, int quad_cap) {
+  extern __shared__ __align__(16) float4 hal[];
+  // after the halo: the z rows (each from a 16-byte aligned node, kHaloZPad floats of slack
+  // per row), then the code block
+  float* zst = reinterpret_cast<float*>(hal + hal_cap);
+  // per quad of the tile: its rows' p.q as an FP32 pair (reduced in quad order, so that the
+  // sum does not depend on which warp took which quad)
+  float2* qpart = reinterpret_cast<float2*>(zst + halo_zcap(hal_cap));
+  unsigned short* cod = reinterpret_cast<unsigned short*>(qpart + quad_cap);
+  __shared__ __align__(8) uint64_t bar, probe_bar;
+  __shared__ int s_tile, s_quad, s_last, s_stop;
+  __shared__ int s_hb[9], s_pre[10], s_zb[9];
+  __shared__ double sm[kBlock / 32];
+  const int lane = threadIdx.x & 31;
+  const int g = lane >> 3, j = lane & 7;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    if (CHECK) mbar_init(&probe_bar, 1);  // one arrival expected, none ever made
+    fence_mbar_init();
+    s_stop = 0;
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_tile = s_stop ? v.ntiles : (int)atomicAdd(&v.ticket[v.M + 2], 1u);
+      s_quad = 0;
+    }
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= v.ntiles) break;
+    const int inst = v.tiles[t].inst;
+    const KParams& k = v.inst[inst];
+    const HTile ht = v.htiles[t];
+    const bool run = ht.nq > 0 && __ldg(&k.ds->inner_active) != 0;
+    if (run) {
+      if (threadIdx.x == 0) {
+        // every row of the halo by bulk copies on one mbarrier: the position records (16
+        // bytes a node, rows start 16-byte aligned) into their slots, the row's z values
+        // from the 16-byte boundary at or below its first node (z is padded past N), and the
+        // tile's code block
+        int acc = 0, zacc = 0;
+        unsigned bytes = (unsigned)ht.clen16 * 16u;
+        for (int r = 0; r < 9; ++r) {
+          const int hb = v.tiles[t].hb[r], hl = v.tiles[t].hl[r];
+          s_hb[r] = hb;
+          s_pre[r] = acc;
+          const int a0 = hb & ~3;
+          s_zb[r] = zacc - a0;  // z of node n of row r at zst[s_zb[r] + n]
+          if (hl > 0) {
+            bytes += (unsigned)hl * 16u + (unsigned)(((hb + hl + 3) & ~3) - a0) * 4u;
+            zacc += ((hb + hl + 3) & ~3) - a0;
+          }
+          acc += hl;
+        }
+        s_pre[9] = acc;
+        // the previous tile's reads and writes of these buffers come before the copies
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar, bytes);
+        for (int r = 0; r < 9; ++r) {
+          const int hb = s_hb[r], hl = s_pre[r + 1] - s_pre[r];
+          if (hl <= 0) continue;
+          const int a0 = hb & ~3;
+          bulk_g2s(hal + s_pre[r], k.posrec + hb, (unsigned)hl * 16u, &bar);
+          bulk_g2s(zst + s_zb[r] + a0, k.z32 + a0, (unsigned)(((hb + hl + 3) & ~3) - a0) * 4u, &bar);
+        }
+        if (ht.clen16 > 0) bulk_g2s(cod, k.hcode + (size_t)ht.cstart16 * 8, (unsigned)ht.clen16 * 16u, &bar);
+      }
+      __syncthreads();
+      if (!mbar_wait_bounded(&bar, phase, kHaloWaitPolls)) {
+        k.ds->wait_timeout = 1;
+        s_stop = 1;
+      }
+      phase ^= 1u;
+      if (CHECK && (k.checks & NNPP_CHECK_WAIT_PROBE) && !mbar_wait_bounded(&probe_bar, 0, 1u << 10)) {
+        k.ds->wait_timeout = 1;
+        s_stop = 1;
+      }
+      // the records as float4 {X, Y, Z, z} in the halo's frame, in place
+      const float hinv = k.hinv;
+      const float xoff = 0.5f * (float)ht.T;
+      const int halo = s_pre[9];
+      for (int i = threadIdx.x; i < halo; i += kBlock) {
+        int r = 0;
+#pragma unroll
+        for (int q = 1; q < 9; ++q) r += i >= s_pre[q] ? 1 : 0;
+        const float4 pr = hal[i];
+        const int pb = __float_as_int(pr.w);
+        float4 o;
+        o.x = fmaf(pr.x, hinv, (float)((pb & 1023) - ht.bx0) - xoff);
+        o.y = fmaf(pr.y, hinv, (float)(((pb >> 10) & 1023) - ht.by) - 0.5f);
+        o.z = fmaf(pr.z, hinv, (float)(((pb >> 20) & 1023) - ht.bz) - 0.5f);
+        o.w = zst[s_zb[r] + s_hb[r] + (i - s_pre[r])];
+        hal[i] = o;
+      }
+      // the padding slot: far away (weight 0) and z = 0
+      if (threadIdx.x == 0) hal[halo] = make_float4(1e18f, 0.0f, 0.0f, 0.0f);
+      __syncthreads();
+      const int own = s_pre[4] - s_hb[4];  // slot of own node a: own + a
+      const float hc0 = k.hc0, hc1 = k.hc1, hsw = k.hsw;
+      const float beta = (float)k.ds->beta;
+      for (;;) {
+        int qi = 0;
+        if (lane == 0) qi = atomicAdd(&s_quad, 1);
+        qi = __shfl_sync(0xffffffffu, qi, 0);
+        if (qi >= ht.nq) break;
+        if (CHECK && (ht.q0 + qi < 0 || ht.q0 + qi >= k.hquad_n)) {
+          if (lane == 0) k.ds->bounds_error = 1;
+          break;
+        }
+        const HQuad* qd = k.hquad + ht.q0 + qi;
+        int a = __ldg(&qd->rows[g]);
+        int npass = __ldg(&qd->npass);
+        if (CHECK) {
+          const TileDesc& td = v.tiles[t];
+          const int coff = __ldg(&qd->coff_rel);
+          const bool bad_row = a != -1 && (a < td.own_begin || a >= td.own_end);
+          const bool bad_codes = npass < 0 || coff < 0 || coff + 32 * npass > 8 * ht.clen16;
+          if (bad_row || bad_codes) k.ds->bounds_error = 1;
+          if (bad_row) a = -1;
+          if (__any_sync(0xffffffffu, bad_codes)) npass = 0;
+        }
+        const bool live = a >= 0 && k.freem[a] != 0;
+        if (!__any_sync(0xffffffffu, live)) {
+          if (lane == 0) qpart[qi] = make_float2(0.0f, 0.0f);
+          continue;
+        }
+        const float4 pa = a >= 0 ? hal[own + a] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const unsigned short* cq = cod + __ldg(&qd->coff_rel) + lane;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        int p = 0;
+        for (; p + 4 <= npass; p += 4) {
+          unsigned sl[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) sl[u] = cq[32 * (p + u)];
+          if (CHECK)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (sl[u] > (unsigned)halo) {
+                k.ds->bounds_error = 1;
+                sl[u] = (unsigned)halo;
+              }
+          float4 pb[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) pb[u] = hal[sl[u]];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[u] += halo_bond(pa, pb[u], hc0, hc1);
+        }
+        for (; p < npass; ++p) {
+          unsigned sl = cq[32 * p];
+          if (CHECK && sl > (unsigned)halo) {
+            k.ds->bounds_error = 1;
+            sl = (unsigned)halo;
+          }
+          acc[0] += halo_bond(pa, hal[sl], hc0, hc1);
+        }
+        float sum = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        float ph = 0.0f, pl = 0.0f;  // this row's p.q, TwoProd
+        if (j == 0 && live) {
+          const float za = pa.w;
+          const float sa = __ldg(k.d32 + a) * za - hsw * sum;
+          const float qn = sa + beta * k.q32[a];
+          const float pn = za + beta * k.p32[a];
+          k.q32[a] = qn;
+          k.p32[a] = pn;
+          ph = pn * qn;
+          pl = fmaf(pn, qn, -ph);
+        }
+        // the quad's sum, rows in order
+        float qh = __shfl_sync(0xffffffffu, ph, 0), ql = __shfl_sync(0xffffffffu, pl, 0);
+#pragma unroll
+        for (int r = 1; r < 4; ++r)
+          pair_add(qh, ql, __shfl_sync(0xffffffffu, ph, 8 * r), __shfl_sync(0xffffffffu, pl, 8 * r));
+        if (lane == 0) qpart[qi] = make_float2(qh, ql);
+      }
+    }
+    __syncthreads();
+    // the tile's partial: its quads' sums in quad order (lane l takes quads l, l + 32, ...,
+    // then a fixed shuffle tree)
+    if (threadIdx.x < 32) {
+      float th = 0.0f, tl = 0.0f;
+      if (run)
+        for (int q = lane; q < ht.nq; q += 32) pair_add(th, tl, qpart[q].x, qpart[q].y);
+      pair_warp_sum(th, tl);
+      if (lane == 0) store_pair(v.partials, t, th, tl);
+    }
+  }
+  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
+    for (int i = 0; i < v.M; ++i) {
+      double tot[1];
+      reduce_pair_items<1>(v.partials, v.stride, v.tile_first[i], v.tile_count[i], tot, sm);
+      if (threadIdx.x == 0) {
+        DevState* ds = v.inst[i].ds;
+        if (ds->inner_active) {
+          ds->alpha = (tot[0] > 0.0 && isfinite(tot[0])) ? ds->rz / tot[0] : 0.0;
+          ds->pq = tot[0];
+        }
+      }
+    }
+    if (threadIdx.x == 0) {
+      v.ticket[v.M + 1] = 0;
+      v.ticket[v.M + 2] = 0;
+    }
+  }
+}
+
 // Staged FP32 CG operator (the same product as k_cg_spmv32, same work split).  Every warp
 // owns, in shared memory,
 //   - a ring of kTmaStages stages of kTmaCol interleaved bond columns of its slices (one
@@ -3323,6 +3563,19 @@ __global__ void k_snap_state(KParams k, Rec64* dst, int mixed) {
   }
 }
 
+// Recomputation without the potential solve: a step's solved potential (stored by
+// forward_ckpt) as the solve leaves it -- phi64 and the current records' potential (the
+// FP32 pair as set_phi_rec writes it) -- and into the step's snapshot.  On the nodes the
+// solve does not change the stored value is the one the records already hold.
+__global__ void k_load_phi(KParams k, const double* phi, Rec64* snap, int mixed) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x) {
+    const double ph = phi[a];
+    k.phi64[a] = ph;
+    set_phi_rec(k, a, ph, mixed != 0);
+    snap[a].phi = ph;
+  }
+}
+
 // phi^n (the last solve's potential) into a snapshot
 __global__ void k_snap_phi(KParams k, Rec64* dst) {
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < k.N; a += gridDim.x * blockDim.x)
@@ -3409,6 +3662,13 @@ nnpp_status launch_snap_phi(Handle& h, Rec64* dst) {
   return NNPP_OK;
 }
 
+nnpp_status launch_load_phi(Handle& h, const double* phi, Rec64* snap) {
+  KParams kp = make_kparams(h, h.cur);
+  k_load_phi<<<h.grid, kBlock, 0, h.st>>>(kp, phi, snap, h.state_prec == NNPP_MIXED ? 1 : 0);
+  NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
 nnpp_status launch_record_solve(Handle& h, int slot) {
   KParams kp = make_kparams(h, h.cur);
   k_record_solve<<<h.grid, kBlock, 0, h.st>>>(kp, slot);
@@ -3438,6 +3698,8 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
   // every tile kernel, the adjoint's included, must fit its staged halo
   if (smem_tr64(H, B) > 220 * 1024 || smem_adj(H, B) > 220 * 1024)
     return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
+  NNPP_TRY(allow_smem(k_cg_spmv32h<false>, 200 * 1024));  // spmv_halo_fits bounds the size used
+  NNPP_TRY(allow_smem(k_cg_spmv32h<true>, 200 * 1024));
   return dispatch_lanes(lanes, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
@@ -3498,6 +3760,18 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
 }
 
 bool spmv_staged_fits(const Engine& e) { return e.windows_fit && smem_spmv_staged() <= 227 * 1024; }
+
+// the halo-staged operator's dynamic shared memory: the halo (plus the padding slot) as
+// float4 and the largest tile code block
+size_t smem_spmv_halo(int halo_max, int code_max16, int quad_max) {
+  return (size_t)(halo_max + 1) * sizeof(float4) + (size_t)halo_zcap(halo_max + 1) * sizeof(float) +
+         (size_t)((quad_max + 1) & ~1) * sizeof(float2) + (size_t)code_max16 * 16;
+}
+// variant 8 runs when every member has its layout, the tiles are at most 8 bins long (the
+// halo-frame coordinates keep ~1e-7 of a bin) and a CTA's halo and code block fit
+bool spmv_halo_fits(const Engine& e) {
+  return e.halo_op && e.T <= 8 && smem_spmv_halo(e.halo_max, e.hcode_max16, e.hquad_max) <= 200 * 1024;
+}
 
 nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st) {
   if (prec == NNPP_MIXED) {
@@ -3576,7 +3850,16 @@ nnpp_status launch_cg_spmv_b(const Engine& e, const EngineView& v, int prec, cud
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     if (prec == NNPP_MIXED)
-      if (e.spmv_variant == 1 && e.members.size() == 1) {
+      if (e.spmv_variant == kSpmvHalo) {
+        const size_t sh = smem_spmv_halo(e.halo_max, e.hcode_max16, e.hquad_max);
+        const int qcap = (e.hquad_max + 1) & ~1;  // keeps the code block 16-byte aligned
+        if (e.checks)
+          k_cg_spmv32h<true><<<occ_grid(k_cg_spmv32h<true>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(
+              v, e.halo_max + 1, qcap);
+        else
+          k_cg_spmv32h<false><<<occ_grid(k_cg_spmv32h<false>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(
+              v, e.halo_max + 1, qcap);
+      } else if (e.spmv_variant == 1 && e.members.size() == 1) {
         int stages = 2;
         const size_t sh = smem_spmv_stream(e.win_cap, &stages);
         k_cg_spmv32s<W, kStreamCol><<<occ_grid(k_cg_spmv32s<W, kStreamCol>, sh, e.sms, (v.nslices + 7) / 8), kBlock, sh, st>>>(
@@ -3781,6 +4064,19 @@ KParams make_kparams(Handle& h, int cur) {
   k.ds = h.dstate.get();
   k.bv_ptr = &h.dstate.get()->BV;
   k.b_override = h.b_override;
+  // halo-staged CG operator: weights in units of the bin side hb (FP32 of the bins' side)
+  k.hquad = h.hquad.get();
+  k.hquad_n = (int)h.hquad.size();
+  k.checks = h.checks;
+  k.hcode = h.hcode.get();
+  k.posrec = h.posrec.get();
+  {
+    const double hb = (double)h.h32;
+    k.hinv = (float)(1.0 / hb);
+    k.hc0 = (float)((p.delta + 0.5 * p.dx) / p.dx);
+    k.hc1 = (float)(hb / p.dx);
+    k.hsw = (float)(p.dx * p.dy * p.dz / (hb * hb * hb));
+  }
   k.dt = p.dt;
   k.csat = p.CSat / p.CSolid;
   k.c_floor = p.c_floor;

@@ -175,6 +175,45 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
   }
 }
 
+// per node: -1 for a node with a Dirichlet value of the potential, else its number of
+// neighbours without one (the row length of the halo-staged CG operator)
+__global__ void k_omega_degree(int n, const int* row, const int* col, const unsigned char* dirmask,
+                               int* deg) {
+  constexpr unsigned char kPhiDir = 1u << S;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    if (dirmask[a] & kPhiDir) {
+      deg[a] = -1;
+      continue;
+    }
+    int d = 0;
+    for (int j = row[a]; j < row[a + 1]; ++j) d += (dirmask[col[j]] & kPhiDir) ? 0 : 1;
+    deg[a] = d;
+  }
+}
+
+// thread per (quad, row): the row's codes in CSR order (ascending halo slot), then the
+// tile's padding slot up to the quad's pass count
+__global__ void k_fill_hcode(int nquads, const HQuad* quads, const int* row, const int* col,
+                             const unsigned short* slot16, const unsigned char* dirmask,
+                             unsigned short* code) {
+  constexpr unsigned char kPhiDir = 1u << S;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 4 * nquads; idx += gridDim.x * blockDim.x) {
+    const HQuad q = quads[idx >> 2];
+    const int g = idx & 3;
+    const int a = q.rows[g];
+    const int base = q.coff_abs + 8 * g;
+    const int total = 8 * q.npass;
+    int m = 0;
+    if (a >= 0)
+      for (int j = row[a]; j < row[a + 1] && m < total; ++j)
+        if (!(dirmask[col[j]] & kPhiDir)) {
+          code[base + 32 * (m >> 3) + (m & 7)] = slot16[j];
+          ++m;
+        }
+    for (; m < total; ++m) code[base + 32 * (m >> 3) + (m & 7)] = (unsigned short)q.padcode;
+  }
+}
+
 }  // namespace
 
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& gslices,
@@ -315,6 +354,102 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
   *halo_max = hm;
   *bond_max = bm;
   h.tiles_T = T;
+  return NNPP_OK;
+}
+
+nnpp_status build_halo_op(Handle& h, int T, const std::vector<TileDesc>& tiles, int tile0,
+                          std::vector<HTile>& htiles, int* code_max16, int* quad_max, bool* ok) {
+  const Layout& L = h.lay;
+  const int N = h.N;
+  const int ntile = (int)tiles.size() - tile0;
+  *ok = false;
+  *code_max16 = 0;
+  *quad_max = 0;
+  h.halo_op_ok = false;
+  HTile none = {0, 0, 0, 0, 0, 0, 0, T};
+  // the weights are recomputed as beta / xi^3: kernel exponent s = 0 only; the padding slot
+  // of a tile is its halo size, which must fit 16 bits
+  bool fits = h.p.s_phi == 0.0;
+  for (int t = tile0; t < (int)tiles.size() && fits; ++t) fits = tiles[t].halo < 65535;
+  if (!fits) {
+    htiles.insert(htiles.end(), ntile, none);
+    return NNPP_OK;
+  }
+  DBuf<int> ddeg;
+  if (!ddeg.alloc(N)) return set_error(NNPP_ERR_NOMEM, "halo operator degrees");
+  const int blocks = std::max(1, std::min((N + 255) / 256, 152 * 16));
+  k_omega_degree<<<blocks, 256, 0, h.st>>>(N, L.row.get(), L.col.get(), h.dirmask.get(), ddeg.get());
+  NNPP_CUDA(cudaGetLastError());
+  std::vector<int> deg(N), perm(N), bs(L.nbins + 1);
+  NNPP_CUDA(cudaMemcpyAsync(deg.data(), ddeg.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(perm.data(), L.perm.get(), sizeof(int) * N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(bs.data(), L.bin_start.get(), sizeof(int) * (L.nbins + 1), cudaMemcpyDeviceToHost,
+                            h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  std::vector<HQuad> quads;
+  long long total16 = 0;
+  int cmax = 0;
+  std::vector<int> rows;
+  for (int t = tile0; t < (int)tiles.size(); ++t) {
+    const TileDesc& td = tiles[t];
+    HTile ht;
+    ht.q0 = (int)quads.size();
+    ht.cstart16 = (int)total16;
+    // bin of the first own node: bins are counting-sorted, so the last bin starting at or
+    // before it
+    const int b = (int)(std::upper_bound(bs.begin(), bs.end(), td.own_begin) - bs.begin()) - 1;
+    ht.by = (b / L.nb[0]) % L.nb[1];
+    ht.bz = b / (L.nb[0] * L.nb[1]);
+    ht.bx0 = ((b % L.nb[0]) / T) * T;
+    ht.T = T;
+    rows.clear();
+    for (int a = td.own_begin; a < td.own_end; ++a)
+      if (deg[a] >= 0) rows.push_back(a);
+    // rows of liquid nodes first, longest first (quads of similar length, little padding);
+    // nodes solid at the start last, so that slices of solid rows are skipped whole
+    std::stable_sort(rows.begin(), rows.end(), [&](int x, int y) {
+      const int sx = h.h_phase0[perm[x]] != 0, sy = h.h_phase0[perm[y]] != 0;
+      if (sx != sy) return sx < sy;
+      return deg[x] > deg[y];
+    });
+    int coff = 0;
+    for (size_t i = 0; i < rows.size(); i += 4) {
+      HQuad q;
+      int mx = 0;
+      for (int g = 0; g < 4; ++g) {
+        q.rows[g] = i + g < rows.size() ? rows[i + g] : -1;
+        if (q.rows[g] >= 0) mx = std::max(mx, deg[q.rows[g]]);
+      }
+      q.npass = (mx + 7) / 8;
+      q.coff_rel = coff;
+      q.coff_abs = (int)(8 * total16) + coff;
+      q.padcode = td.halo;
+      coff += 32 * q.npass;
+      quads.push_back(q);
+    }
+    ht.nq = (int)quads.size() - ht.q0;
+    *quad_max = std::max(*quad_max, ht.nq);
+    ht.clen16 = (coff + 7) / 8;
+    total16 += ht.clen16;
+    if (8 * total16 > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "halo operator above 2^31 codes");
+    cmax = std::max(cmax, ht.clen16);
+    htiles.push_back(ht);
+  }
+  if (!h.hquad.alloc(std::max<size_t>(quads.size(), 1)) || !h.hcode.alloc((size_t)total16 * 8 + 8))
+    return set_error(NNPP_ERR_NOMEM, "halo operator");
+  NNPP_CUDA(cudaMemsetAsync(h.hcode.get(), 0, ((size_t)total16 * 8 + 8) * sizeof(unsigned short), h.st));
+  if (!quads.empty()) {
+    NNPP_CUDA(cudaMemcpyAsync(h.hquad.get(), quads.data(), sizeof(HQuad) * quads.size(), cudaMemcpyHostToDevice,
+                              h.st));
+    const int qb = std::max(1, std::min((int)((4 * quads.size() + 255) / 256), 152 * 16));
+    k_fill_hcode<<<qb, 256, 0, h.st>>>((int)quads.size(), h.hquad.get(), L.row.get(), L.col.get(),
+                                       h.slot16.get(), h.dirmask.get(), h.hcode.get());
+    NNPP_CUDA(cudaGetLastError());
+  }
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  *code_max16 = cmax;
+  *ok = true;
+  h.halo_op_ok = true;
   return NNPP_OK;
 }
 

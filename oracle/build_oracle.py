@@ -3,7 +3,9 @@
 Compiles
   oracle/nnpp_oracle.cpp  -> oracle/liboracle.so        (always; g++ with OpenMP)
   oracle/ref_shim.cpp     -> oracle/_ref/libnnpp_ref.so (only where the reference's
-                             sources are present, i.e. REFERENCE_ROOT exists)
+                             sources are present: the checkout named by the environment
+                             variable NNPP_REFERENCE_ROOT, else a checkout named
+                             "reference" beside this repository)
 The reference shim is compiled from the reference's own headers where they lie; nothing of
 the reference is copied into this repository.  Both libraries are checkers for the tests,
 never part of the product.
@@ -13,7 +15,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = os.environ.get("NNPP_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get(
+    "NNPP_REFERENCE_ROOT", os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 # -ffp-contract=off: the reference is built without FMA contraction on x86-64 (-msse2,
 # CMakeLists.txt:51-54); keeping products and sums separate makes the restatement give the
@@ -28,12 +31,42 @@ def _newer(target, sources):
     return all(os.path.getmtime(s) <= t for s in sources)
 
 
-def build_oracle(force=False, verbose=False):
-    out = os.path.join(HERE, "liboracle.so")
+# The seeded workload generator (host C++, no CUDA) is compiled into the oracle library as
+# well, so that the CPU-baseline and reference arms of the benchmark build their inputs
+# without loading the product library.
+PKG_CSRC = os.path.join(HERE, "..", "nnpp-mg-implant-corrosion-3d_gb300", "csrc")
+SYNTH_SRCS = [os.path.join(PKG_CSRC, "synth.cpp"), os.path.join(PKG_CSRC, "errors.cpp")]
+
+
+def _native_flag():
+    """The host's own instruction set: -march=native where GCC accepts it (x86-64), else
+    -mcpu=native (aarch64); None when neither compiles."""
+    for flag in ("-march=native", "-mcpu=native"):
+        r = subprocess.run(["g++", flag, "-x", "c++", "-fsyntax-only", "-"], input="int main(){}",
+                           capture_output=True, text=True)
+        if r.returncode == 0:
+            return flag
+    return None
+
+
+def build_oracle(force=False, verbose=False, native=False):
+    """liboracle.so (portable flags), or with native=True liboracle_native.so, the same
+    sources for the host's own instruction set (the timed CPU baseline; -ffp-contract=off
+    keeps every rounding, so both give the same bits).  Returns None for a native build the
+    compiler does not support."""
+    extra = []
+    if native:
+        flag = _native_flag()
+        if flag is None:
+            return None
+        extra = [flag]
+    out = os.path.join(HERE, "liboracle_native.so" if native else "liboracle.so")
     srcs = [os.path.join(HERE, "nnpp_oracle.cpp"),
-            os.path.join(HERE, "..", "include", "nnpp_gb300.h")]
+            os.path.join(HERE, "..", "include", "nnpp_gb300.h"),
+            os.path.abspath(__file__)] + SYNTH_SRCS
     if force or not _newer(out, srcs):
-        cmd = ["g++"] + CXXFLAGS + [srcs[0], "-o", out]
+        cmd = ["g++"] + CXXFLAGS + extra + ["-I", os.path.join(HERE, "..", "include"), "-I", PKG_CSRC,
+                                            srcs[0]] + SYNTH_SRCS + ["-o", out]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)
@@ -62,4 +95,5 @@ def build_reference_shim(force=False, verbose=False):
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force, True))
+    print(build_oracle(force, True, native=True))
     print(build_reference_shim(force, True))

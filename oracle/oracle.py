@@ -34,10 +34,16 @@ def _lp(a):
 
 
 def load_oracle():
+    """liboracle.so, or liboracle_native.so (the same sources for the host's instruction set,
+    the same bits) when NNPP_ORACLE_NATIVE=1 was set before the first call."""
     global _orc
     if _orc is None:
         from build_oracle import build_oracle  # noqa: E402 (same directory)
-        path = build_oracle()
+        path = None
+        if os.environ.get("NNPP_ORACLE_NATIVE") == "1":
+            path = build_oracle(native=True)
+        if path is None:
+            path = build_oracle()
         L = C.CDLL(path)
         sig = {
             "orc_create": (_P, [_P, C.c_int, _DP, _IP, _DP, _DP, _IP]),
@@ -56,6 +62,9 @@ def load_oracle():
             "orc_get_state": (C.c_int, [_P, _DP, _DP, _IP, _IP]),
             "orc_set_state": (C.c_int, [_P, _DP, _DP, _IP]),
             "orc_get_diag": (C.c_int, [_P, _DP]),
+            "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
+            "nnpp_synth_fill": (C.c_int, [C.c_int, C.c_int, C.c_uint64, _DP, _IP, _DP, _DP, _IP,
+                                          C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -84,6 +93,37 @@ def load_reference():
                                      _DP, _DP, _DP, _LP, _IP, _IP, _DP]
         _ref = L
     return _ref
+
+
+class Params(C.Structure):
+    """nnpp_params of include/nnpp_gb300.h (the oracle takes the product's parameter block)."""
+    _fields_ = [("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("delta", C.c_double), ("CSolid", C.c_double), ("CSat", C.c_double),
+                ("F", C.c_double), ("R", C.c_double), ("T", C.c_double), ("vol_red", C.c_double),
+                ("z", C.c_double * 4), ("D_solid", C.c_double * 4), ("D_liquid", C.c_double * 4),
+                ("s1", C.c_double * 4), ("s2", C.c_double * 4), ("K1", C.c_double * 4),
+                ("K2", C.c_double * 4), ("sigma", C.c_double), ("s_phi", C.c_double),
+                ("K_phi", C.c_double), ("k_diss", C.c_double), ("switch_width", C.c_double),
+                ("c_floor", C.c_double), ("sub_step_no", C.c_int), ("reserved", C.c_int)]
+
+
+def synth(kind, n_side, seed=0):
+    """The seeded workloads of nnpp_synth_fill, generated by the oracle library's copy of the
+    generator (the same source file), without the product library."""
+    L = load_oracle()
+    N = L.nnpp_synth_count(kind, n_side)
+    if N <= 0:
+        raise ValueError("bad synthetic kind/n_side")
+    nodes = np.empty((3, N), dtype=np.float64)
+    bct = np.empty(N, dtype=np.int32)
+    bcv = np.empty((NSPECIES + 1, N), dtype=np.float64)
+    icv = np.empty((NSPECIES + 1, N), dtype=np.float64)
+    ph = np.empty(N, dtype=np.int32)
+    p = Params()
+    if L.nnpp_synth_fill(kind, n_side, seed, _dp(nodes), _ip(bct), _dp(bcv), _dp(icv), _ip(ph),
+                         C.cast(C.byref(p), C.c_void_p)) != 0:
+        raise RuntimeError("synthetic workload generation failed")
+    return dict(nodes=nodes, bctypes=bct, bcvalues=bcv, icvalues=icv, phase0=ph, params=p, N=N)
 
 
 DIAG_KEYS = ["steps", "solid_count", "voln1rel", "vol0rel", "mass0", "mass1", "mass2", "mass3",
@@ -198,6 +238,12 @@ class Oracle:
 
 def set_threads(n):
     return load_oracle().orc_set_threads(n)
+
+
+def library_path():
+    """File name of the loaded oracle library."""
+    L = load_oracle()
+    return os.path.basename(L._name)
 
 
 # ---------------------------------------------------------------- reference shim --------

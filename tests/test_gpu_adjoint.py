@@ -118,18 +118,20 @@ def test_checkpoint_interval_does_not_change_result(gpu, case):
         assert gk == out[0][2]
 
 
-def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
+@pytest.mark.parametrize("store", [1, 3])
+def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case, store):
     """The implant dissolves between steps 35 and 40 (k_diss = 0.1), so the coarse operator of
     the two-level preconditioner is rebuilt during the forward run (refresh period 4);
-    backward replays the recorded inverses, and the gradients stay independent of the
-    checkpoint interval, and equal to a run that never rebuilds to the solver tolerance."""
+    backward replays the recorded inverses (for the adjoint solves, and with store 3 for the
+    recomputed forward solves too), and the gradients stay independent of the checkpoint
+    interval, and equal to a run that never rebuilds to the solver tolerance."""
     inp, _ = case
     p = _params(inp, 1.0, 0.1)
     target = np.zeros(N_STEPS // SE)
     out = []
     for every, ck in ((4, 7), (4, 25), (4, 60), (0, 25)):
         sim = _sim(gpu, inp, p, pin=True)
-        sim.set_adjoint_store(1)
+        sim.set_adjoint_store(store)
         sim.set_preconditioner(gpu.PRECOND_TWO_LEVEL, every)
         curve = sim.forward_ckpt(N_STEPS, gpu.FP64, ck, SE)
         built = sim.preconditioner()[3]
@@ -149,11 +151,12 @@ def test_checkpoint_invariance_with_coarse_rebuilds(gpu, case):
 
 @pytest.mark.parametrize("prec", [0, 1])
 def test_stored_snapshots_equal_recomputation(gpu, case, prec):
-    """Keeping every step's snapshot (no recomputation) and recomputing checkpoint segments
-    give the same curve and gradients bit for bit, and the automatic mode picks one of them."""
+    """Keeping every step's snapshot (no recomputation), recomputing checkpoint segments from
+    the stored potentials (bond sums only) and recomputing them whole give the same curve and
+    gradients bit for bit, and the automatic mode picks one of them."""
     inp, target = case
     out = []
-    for mode in (1, 2, 0):
+    for mode in (1, 2, 3, 0):
         sim = _sim(gpu, inp, _params(inp), pin=True)
         sim.set_adjoint_store(mode)
         curve = sim.forward_ckpt(N_STEPS, prec, 25, SE)
@@ -170,7 +173,7 @@ def test_stored_snapshots_equal_recomputation(gpu, case, prec):
 def test_adjoint_store_rejects_bad_mode(gpu, case):
     inp, _ = case
     sim = _sim(gpu, inp, _params(inp))
-    for bad in (-1, 3):
+    for bad in (-1, 4):
         with pytest.raises(gpu.NNPPError) as e:
             sim.set_adjoint_store(bad)
         assert e.value.status == 1

@@ -150,6 +150,10 @@ def test_residuals_fp64_and_mixed(gpu, orc, kind, n):
     for k in range(4):
         scale = np.abs(Fo[k]).max()
         assert np.abs(F32[k] - Fo[k]).max() <= 2e-5 * scale, k
+    # the mixed path's potential residual F11: FP64 arithmetic on the potential held as an
+    # FP32 pair (hi + lo, ~2^-48 of the value)
+    scale = np.abs(Fo[4]).max()
+    assert np.abs(F32[4] - Fo[4]).max() <= 1e-10 * scale
 
 
 @pytest.mark.parametrize("prec", [0, 1])
@@ -438,11 +442,12 @@ def test_warm_start_rejects_bad_history(gpu):
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_cg_operator_variants_vs_oracle(gpu, orc, variant):
     """Every FP32 CG operator (L1/L2 gathers; bulk-copy staged; shared-memory windows; with
-    and without L2 prefetch of the operator stream) reaches the oracle's state to the
-    mixed-precision tolerance, configuration pinned."""
+    and without L2 prefetch of the operator stream; the halo-staged operator with recomputed
+    weights) reaches the oracle's state to the mixed-precision tolerance, configuration
+    pinned."""
     nn = gpu
     inp = nn.synth(1, 20, seed=11)
     o = orc.Oracle.from_synth(inp)
@@ -467,7 +472,7 @@ def test_set_tuning_rejects_bad_configuration(gpu):
     inp = nn.synth(1, 12, seed=4)
     sim = nn.Simulation.from_synth(inp)
     sim.build_neighbours()
-    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 8), (8, 8, -1)):
+    for bad in ((3, 8, 0), (8, 5, 0), (8, 8, 9), (8, 8, -1)):
         with pytest.raises(nn.NNPPError) as e:
             sim.set_tuning(*bad)
         assert e.value.status == 1
