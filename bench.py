@@ -329,11 +329,11 @@ def ensemble_cost(nn, steps, members=64, seed=4):
 
 
 def moving_front_cost(nn, inp, pre_steps, steps):
-    """The 512k workload in its dissolving phase: after pre_steps steps the implant front
-    moves (solid nodes flip every few steps), so the two-level preconditioner's coarse
-    inverse is rebuilt at every refresh check (every 64 steps) that sees a changed phase.
-    Times `steps` steps of the mixed and of the FP64 path from there, with the rebuilds
-    inside the timed window, and states their share."""
+    """The 512k workload in its dissolving phase: steps 2,000-4,000 hold the first burst of
+    the front's motion (the sphere's outer layers flip, 57,983 -> 40,181 solid nodes), so
+    the two-level preconditioner's coarse inverse is rebuilt at the refresh checks (every 64
+    steps) that see a changed phase.  Times `steps` steps of the mixed and of the FP64 path
+    from pre_steps on, with the rebuilds inside the timed window, and states their share."""
     out = {"pre_steps": pre_steps, "steps": steps}
     ms_by = {}
     for name, prec in (("mixed", nn.MIXED), ("fp64", nn.FP64)):
@@ -635,7 +635,7 @@ def main():
                     help="steps of the 64-instance ensemble measurement (0: skip)")
     ap.add_argument("--large-steps", type=int, default=10,
                     help="steps of the 2M-node measurement (0: skip)")
-    ap.add_argument("--front-steps", type=int, default=640,
+    ap.add_argument("--front-steps", type=int, default=2000,
                     help="timed steps of the 512k workload's dissolving phase (0: skip)")
     ap.add_argument("--front-pre", type=int, default=2000,
                     help="steps run before the dissolving-phase window")

@@ -173,6 +173,21 @@ nnpp_status nnpp_build_clouds_hash_noalloc(int max_node_no, double r, double dx,
                                            int* d_clouds_colmajor, int* d_cloud_lengths,
                                            int* max_cloud_length, void* stream);
 
+/* ---- implant mask (main.cpp:316-325, 422-457) ------------------------------------------- */
+
+/* The phase of every node from the implant's point cloud, as the reference sets it up when
+ * it starts from a surface-mesh implant (BunnyConditions): counts[i] is the number of points
+ * within r of node i -- inside the FP64 box node +- r (libkdtree++'s find_within_range) and
+ * at Euclidean distance sqrt(x*x + y*y + z*z) <= r, kd_tree_interface.h:156-252 -- and
+ * phase[i] = 1 (solid) where counts[i] > 0, else 0.  The reference calls it with
+ * r = 3 * 0.4 * dx * (1 + 1e-5).  nodes and points are column-major (x[], y[], z[]) host
+ * arrays; counts and phase may each be NULL.  NNPP_ERR_CAPACITY where a count exceeds
+ * max_node_no (the reference's runtime_error of kd_tree_interface.h:213-216; the outputs are
+ * still written). */
+nnpp_status nnpp_implant_mask(int n_nodes, const double* nodes_colmajor, int n_points,
+                              const double* points_colmajor, double r, int max_node_no,
+                              int* counts, int* phase);
+
 /* ---- simulation handle ---------------------------------------------------------------- */
 
 /* Create a handle for N nodes.  bcvalues/icvalues hold (S+1)*N doubles in the reference's
@@ -202,6 +217,21 @@ nnpp_status nnpp_get_neighbours_csr(nnpp_handle* h, int* row_ptr, int* cols, int
  * Dirichlet values and the positivity clamp, flip saturated solid nodes, update the
  * diagnostics.  The step sequence is captured once into a CUDA graph per precision. */
 nnpp_status nnpp_forward(nnpp_handle* h, int n_steps, int precision);
+
+/* The reference's own time integration (main.cpp:640-922) for n_steps steps from the
+ * handle's state, in FP64: backward Euler with one tangent per step (utils::NewtonMatrices,
+ * utils.h:844-1849) and modified Newton iterations -- the residual of utils::Residuals at the
+ * iterate with the migration on the previous step's potential, Dirichlet rows U - bc, every
+ * field's correction from K_f dU_f = -F_f by GMRES(30) with the diagonal preconditioner to
+ * EPS = 1e-5 (Eigen::GMRES as main.cpp:714-779 calls it: initial guess the right-hand side,
+ * at most MAX_ITER = 200 iterations), the positivity clamp, until the update norms change by
+ * less than EPS (main.cpp:847-895) -- then the phase flip.  The five fields' Krylov solves run
+ * together on the GPU (one pass over the bonds serves all five).  newton_iterations and
+ * krylov_iterations (GMRES iterations summed over fields and steps) may be NULL.  The state,
+ * flip steps and diagnostics continue as after nnpp_forward; the step is the reference's, so
+ * it is stable at time steps far above the explicit limit. */
+nnpp_status nnpp_forward_implicit(nnpp_handle* h, int n_steps, int64_t* newton_iterations,
+                                  int64_t* krylov_iterations);
 
 /* Return to the initial state of nnpp_build_neighbours (initial values, phase0, zeroed
  * counters and diagnostics, no flipped node), keeping the lists, solver settings and tuning.
@@ -270,7 +300,10 @@ nnpp_status nnpp_get_coarse_stats(nnpp_handle* h, int64_t* rebuilds, int64_t* wa
 /* Copy the state to host buffers (user node order).  c: S*N, phi: N, phase: N; any may be
  * NULL. */
 nnpp_status nnpp_get_state(nnpp_handle* h, double* c, double* phi, int* phase);
-/* Overwrite the state from host buffers (user node order); phase may be NULL. */
+/* Overwrite the state from host buffers (user node order); phase may be NULL.  As after the
+ * reference's restart from file (main.cpp:527-533), the relative volume voln1rel and the
+ * interface factor BV are recomputed for the new state against the initial state's vol0rel;
+ * the step counter and the initial Mg mass are kept. */
 nnpp_status nnpp_set_state(nnpp_handle* h, const double* c, const double* phi,
                            const int* phase);
 nnpp_status nnpp_get_diagnostics(nnpp_handle* h, nnpp_diag* out);

@@ -87,6 +87,7 @@ _SIGS = {
     "nnpp_build_clouds_hash_noalloc": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double,
                                                  C.c_double, C.c_int, C.c_void_p, C.c_void_p,
                                                  C.c_void_p, _IP, C.c_void_p]),
+    "nnpp_implant_mask": (C.c_int, [C.c_int, _DP, C.c_int, _DP, C.c_double, C.c_int, _IP, _IP]),
     "nnpp_create": (C.c_int, [C.POINTER(_P), C.POINTER(Params), C.c_int, _DP, _IP, _DP, _DP, _IP]),
     "nnpp_destroy": (C.c_int, [_P]),
     "nnpp_build_neighbours": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -114,6 +115,7 @@ _SIGS = {
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
     "nnpp_set_checks": (C.c_int, [_P, C.c_int]),
+    "nnpp_forward_implicit": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "nnpp_get_coarse_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                         C.POINTER(C.c_int64), _DP, _IP]),
     "nnpp_ensemble_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int]),
@@ -225,6 +227,20 @@ def build_clouds_hash_noalloc(max_node_no, r, dx, dy, dz, n_nodes, d_nodes, d_cl
     _check(lib().nnpp_build_clouds_hash_noalloc(max_node_no, r, dx, dy, dz, n_nodes, d_nodes,
                                                 d_clouds, d_lengths, C.byref(ml), stream))
     return ml.value
+
+
+def implant_mask(nodes, points, r, max_node_no=1024):
+    """The nodes' phase from an implant point cloud (nnpp_implant_mask; main.cpp:316-325,
+    422-457 with kd_tree_interface.h:156-252): (counts of points within r, phase = counts >
+    0).  nodes, points: (3, N) / (3, M) or (N, 3) / (M, 3) float64."""
+    xyz = _colmajor_nodes(nodes)
+    pts = _colmajor_nodes(points) if len(points) else np.zeros((3, 0))
+    N, M = xyz.shape[1], pts.shape[1]
+    counts = np.empty(N, dtype=np.int32)
+    phase = np.empty(N, dtype=np.int32)
+    _check(lib().nnpp_implant_mask(N, _dp(xyz), M, _dp(np.ascontiguousarray(pts)), r, max_node_no,
+                                   _ip(counts), _ip(phase)))
+    return counts, phase
 
 
 def _colmajor_nodes(nodes):
@@ -346,6 +362,13 @@ class Simulation:
 
     def forward(self, n_steps, precision=MIXED):
         _check(lib().nnpp_forward(self._h, n_steps, precision))
+
+    def forward_implicit(self, n_steps):
+        """n steps of the reference's backward-Euler Newton/GMRES integration (FP64,
+        nnpp_forward_implicit); returns (Newton iterations, GMRES iterations)."""
+        nw, kr = C.c_int64(0), C.c_int64(0)
+        _check(lib().nnpp_forward_implicit(self._h, n_steps, C.byref(nw), C.byref(kr)))
+        return nw.value, kr.value
 
     def forward_timed(self, n_steps, precision=MIXED):
         """forward() timed with CUDA events on the handle's stream; returns milliseconds."""

@@ -94,7 +94,7 @@ def _build_driver(verbose):
     """The C++ job-file driver, linked against the library (rpath $ORIGIN)."""
     if not _stale(DRIVER, [DRIVER_SRC, LIB, os.path.join(INCLUDE, "nnpp_gb300.h")]):
         return DRIVER
-    cmd = ["g++"] + CXX_FLAGS + [DRIVER_SRC, "-o", DRIVER, "-L", HERE, "-lnnpp_gb300",
+    cmd = ["g++"] + CXX_FLAGS + [DRIVER_SRC, "-o", DRIVER, "-L", HERE, "-lnnpp_gb300", "-pthread",
                                  "-Wl,-rpath,$ORIGIN"]
     if verbose:
         print(" ".join(cmd), flush=True)

@@ -454,6 +454,9 @@ nnpp_status nnpp_set_state(nnpp_handle* hp, const double* c, const double* phi, 
   if (!c) return set_error(NNPP_ERR_INVALID, "c is NULL");
   Handle& h = hp->h;
   NNPP_TRY(upload_state(h, c, phi, phase, h.state_prec));
+  // the relative volume and the interface factor of the new state, as after the reference's
+  // restart from file (main.cpp:527-533); vol0rel stays the initial state's
+  NNPP_TRY(init_diag(h, true));
   h.coarse.stale = true;
   h.nstep = 0;
   NNPP_CUDA(cudaStreamSynchronize(h.st));

@@ -272,7 +272,9 @@ nnpp_status store_state(Handle& h, double* d_c_user, double* d_phi_user, int* d_
 nnpp_status convert_state(Handle& h, int to_prec);
 // the potential operator's mask-dependent arrays must be recomputed by the next prep
 nnpp_status invalidate_operator(Handle& h);
-nnpp_status init_diag(Handle& h);
+// restart: keep vol0rel and the initial Mg mass, recompute voln1rel and BV of the current
+// state (main.cpp:527-533)
+nnpp_status init_diag(Handle& h, bool restart = false);
 
 }  // namespace nnpp
 

@@ -3125,8 +3125,10 @@ __global__ void k_convert(KParams k, int to_mixed) {
   }
 }
 
-// initial diagnostics (main.cpp:472-480): solid count, vol0rel, masses
-__global__ void k_init_diag(KParams k, int mixed, double* partials) {
+// initial diagnostics (main.cpp:472-480): solid count, vol0rel, masses; restart != 0 keeps
+// vol0rel and the initial Mg mass and recomputes the relative volume of the current state
+// instead (main.cpp:527-533, after a restart from file)
+__global__ void k_init_diag(KParams k, int mixed, double* partials, int restart) {
   __shared__ double sm[7 * kBlock / 32];
   __shared__ int s_last;
   double part[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -3159,12 +3161,16 @@ __global__ void k_init_diag(KParams k, int mixed, double* partials) {
     DevState* ds = k.ds;
     ds->ticket[0] = 0;
     for (int s = 0; s < S; ++s) ds->mass[s] = tot[s];
-    ds->mg_mass_t0 = tot[0];
     ds->mg_mass_now = tot[0];
     ds->solid_count = (long long)tot[4];
-    ds->vol0rel = tot[5];
-    ds->voln1rel = 0.0;
-    ds->BV = pow(10., -k.vol_red);
+    if (restart) {
+      ds->voln1rel = ds->vol0rel != 0.0 ? tot[5] / ds->vol0rel : 0.0;
+    } else {
+      ds->mg_mass_t0 = tot[0];
+      ds->vol0rel = tot[5];
+      ds->voln1rel = 0.0;
+    }
+    ds->BV = pow(10., -k.vol_red * (1. - ds->voln1rel));
   }
 }
 
@@ -4165,10 +4171,10 @@ nnpp_status convert_state(Handle& h, int to_prec) {
   return invalidate_operator(h);
 }
 
-nnpp_status init_diag(Handle& h) {
+nnpp_status init_diag(Handle& h, bool restart) {
   KParams kp = make_kparams(h, h.cur);
   k_init_diag<<<h.grid, kBlock, 0, h.st>>>(kp, h.state_prec == NNPP_MIXED ? 1 : 0,
-                                           h.scratch_d.get() + 16);
+                                           h.scratch_d.get() + 16, restart ? 1 : 0);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }

@@ -1,7 +1,8 @@
 // nnpp_run -- C++ host driver over the C ABI, in the reference's job-file layout.
 //
-//   nnpp_run <prefix> <jobname> [--steps N] [--every K] [--precision mixed|fp64]
-//            [--k-diss K] [--switch-width W] [--tol T] [--device D] [--no-output]
+//   nnpp_run <prefix> <jobname> [<startfileNo>] [--steps N] [--every K]
+//            [--precision mixed|fp64] [--k-diss K] [--switch-width W] [--tol T] [--device D]
+//            [--no-output] [--restart S0]
 //   nnpp_run --write-synth <kind> <n_side> <seed> <jobname> [--steps N]
 //
 // Run mode mirrors the reference executable's start-up and time loop (main.cpp:153-1025):
@@ -16,7 +17,16 @@
 // hold the initial values of those species (read from .icvalues5..10 when present).
 //
 // The initial phase is read from <jobname>.phase0 (N ints) when that file exists; otherwise
-// a node is solid when icvalues1 > 10E-6 (main.cpp:413-421, BunnyConditions = 0).
+// a node is solid when icvalues1 > 10E-6 (main.cpp:413-421, BunnyConditions = 0).  When
+// data1[3] > 0 and <jobname>.bunnyNodes holds that many points, the implant comes from that
+// point cloud instead (BunnyConditions = 1, main.cpp:316-325, 422-457; nnpp_implant_mask).
+//
+// Restart (main.cpp:507-542): with a start file number s0 (the reference's third argument,
+// or --restart s0) the state is read by column name from <jobname><prefix>-<s0>.output.csv
+// and the run continues from step s0.
+//
+// Text input, the output CSV and the restart file are parsed and formatted by all host
+// threads (at millions of nodes the reference's serial streams dominate the run's I/O).
 //
 // --write-synth writes one of the library's seeded synthetic workloads in that layout (plus
 // .phase0, since those workloads hold Mg in the electrolyte too).
@@ -27,7 +37,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "nnpp_gb300.h"
@@ -50,21 +62,73 @@ bool slurp(const std::string& path, std::string& out) {
   return got == out.size();
 }
 
+// Host threads of the parallel text passes.
+int host_threads() {
+  const unsigned n = std::thread::hardware_concurrency();
+  return n == 0 ? 1 : (int)std::min(n, 64u);
+}
+
+// Run f(t) for t in [0, n) on n threads.
+template <class F>
+void parallel(int n, F f) {
+  std::vector<std::thread> th;
+  for (int t = 1; t < n; ++t) th.emplace_back(f, t);
+  f(0);
+  for (auto& x : th) x.join();
+}
+
+bool is_space(char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
 // Whitespace-separated numbers, the first `count` of them (operator>> semantics of
-// read_vector_from_file / read_matrix_from_file).  Returns false when the file is missing
-// or holds fewer numbers.
+// read_vector_from_file / read_matrix_from_file, utils.h:1852-1887).  Returns false when
+// the file is missing or holds fewer numbers.  The buffer is cut at whitespace into one
+// piece per thread; each piece's tokens are counted, then parsed with strtod into their
+// places, so the values are those of a serial pass.
 bool read_doubles(const std::string& path, size_t count, std::vector<double>& v) {
   std::string buf;
   if (!slurp(path, buf)) return false;
   v.resize(count);
-  const char* p = buf.c_str();
-  for (size_t i = 0; i < count; ++i) {
-    char* end = nullptr;
-    const double x = std::strtod(p, &end);
-    if (end == p) return false;
-    v[i] = x;
-    p = end;
+  const size_t L = buf.size();
+  const int T = L < (1u << 20) ? 1 : host_threads();
+  std::vector<size_t> cut(T + 1, L);
+  cut[0] = 0;
+  for (int t = 1; t < T; ++t) {
+    size_t c = std::max(cut[t - 1], L * t / T);
+    while (c < L && !is_space(buf[c])) ++c;
+    cut[t] = c;
   }
+  std::vector<size_t> ntok(T, 0);
+  parallel(T, [&](int t) {
+    size_t n = 0;
+    bool in = false;
+    for (size_t i = cut[t]; i < cut[t + 1]; ++i) {
+      const bool sp = is_space(buf[i]);
+      if (!sp && !in) ++n;
+      in = !sp;
+    }
+    ntok[t] = n;
+  });
+  std::vector<size_t> first(T + 1, 0);
+  for (int t = 0; t < T; ++t) first[t + 1] = first[t] + ntok[t];
+  if (first[T] < count) return false;
+  std::vector<char> bad(T, 0);
+  parallel(T, [&](int t) {
+    const char* p = buf.c_str() + cut[t];
+    const char* e = buf.c_str() + cut[t + 1];
+    for (size_t k = first[t]; k < first[t + 1] && k < count; ++k) {
+      while (p < e && is_space(*p)) ++p;
+      char* end = nullptr;
+      const double x = std::strtod(p, &end);
+      if (end == p) {
+        bad[t] = 1;
+        return;
+      }
+      v[k] = x;
+      p = end;
+    }
+  });
+  for (int t = 0; t < T; ++t)
+    if (bad[t]) return false;
   return true;
 }
 
@@ -96,6 +160,91 @@ struct Out {
 // input files written here use %.17g, which reads back to the same double.
 void put(FILE* f, double x) { std::fprintf(f, "%.16g", x); }
 void put_exact(FILE* f, double x) { std::fprintf(f, "%.17g", x); }
+
+// The 15-column output CSV of main.cpp:935-999 (utils.h:2054-2100) with its rows formatted
+// by all host threads into per-thread buffers, written in order.
+bool write_output_csv(const std::string& path, size_t N, const std::vector<double>& rows,
+                      const std::vector<double>& c, const std::vector<double>& passive,
+                      const std::vector<double>& phi, const std::vector<int>& phase, int species) {
+  const int T = N < 4096 ? 1 : host_threads();
+  std::vector<std::string> out(T);
+  parallel(T, [&](int t) {
+    const size_t i0 = N * t / T, i1 = N * (t + 1) / T;
+    std::string& o = out[t];
+    o.reserve((i1 - i0) * 300);
+    char tmp[40];
+    for (size_t i = i0; i < i1; ++i) {
+      for (int d = 0; d < 3; ++d) o.append(tmp, std::snprintf(tmp, sizeof tmp, "%.16g,", rows[3 * i + d]));
+      for (int k = 0; k < species; ++k) o.append(tmp, std::snprintf(tmp, sizeof tmp, "%.16g,", c[(size_t)k * N + i]));
+      for (int k = 0; k < 6; ++k) o.append(tmp, std::snprintf(tmp, sizeof tmp, "%.16g,", passive[(size_t)k * N + i]));
+      o.append(tmp, std::snprintf(tmp, sizeof tmp, "%.16g,%d\n", phi[i], phase[i]));
+    }
+  });
+  Out f(path);
+  if (!f.ok()) return false;
+  std::fputs("X,Y,Z,Mg++,H+,OH-,HCO3-,CO32-,HPO42-,PO43-,Ca++,Na+,Cl-,Phi,Phase\n", f.f);
+  for (const std::string& o : out) std::fwrite(o.data(), 1, o.size(), f.f);
+  return true;
+}
+
+// Restart file (utils.h:1929-2027, read_vector_from_startfile as main.cpp:507-542 calls it):
+// the header names the columns (a repeated name keeps its last position); every named column
+// that is present fills its vector row by row (std::stod / std::stoi), rows beyond num_nodes
+// are ignored and missing ones stay zero.  Lines are parsed by all host threads.
+bool read_start_csv(const std::string& path, size_t N, const std::vector<std::string>& names,
+                    std::vector<std::vector<double> >& cols, std::vector<int>& phase) {
+  std::string buf;
+  if (!slurp(path, buf)) return false;
+  std::vector<size_t> line;  // starts of the data lines
+  size_t e = buf.find('\n');
+  const std::string header = buf.substr(0, e == std::string::npos ? buf.size() : e);
+  std::map<std::string, size_t> pos;
+  {
+    size_t i = 0, k = 0;
+    while (i <= header.size()) {
+      size_t j = header.find(',', i);
+      if (j == std::string::npos) j = header.size();
+      pos[header.substr(i, j - i)] = k++;
+      i = j + 1;
+    }
+  }
+  for (size_t p = e == std::string::npos ? buf.size() : e + 1; p < buf.size() && line.size() < N;) {
+    line.push_back(p);
+    const size_t q = buf.find('\n', p);
+    p = q == std::string::npos ? buf.size() : q + 1;
+  }
+  std::vector<long> want(names.size() + 1, -1);  // column of each name, phase last
+  for (size_t n = 0; n < names.size(); ++n) {
+    auto it = pos.find(names[n]);
+    if (it != pos.end()) want[n] = (long)it->second;
+  }
+  {
+    auto it = pos.find("Phase");
+    if (it != pos.end()) want[names.size()] = (long)it->second;
+  }
+  cols.assign(names.size(), std::vector<double>(N, 0.0));
+  phase.assign(N, 0);
+  const int T = line.size() < 4096 ? 1 : host_threads();
+  parallel(T, [&](int t) {
+    std::vector<const char*> field;
+    for (size_t r = line.size() * t / T; r < line.size() * (t + 1) / T; ++r) {
+      const char* p = buf.c_str() + line[r];
+      const char* end = buf.c_str() + (r + 1 < line.size() ? line[r + 1] : buf.size());
+      field.clear();
+      field.push_back(p);
+      for (const char* q = p; q < end && *q != '\n'; ++q)
+        if (*q == ',') field.push_back(q + 1);
+      for (size_t n = 0; n <= names.size(); ++n) {
+        if (want[n] < 0 || (size_t)want[n] >= field.size()) continue;
+        if (n < names.size())
+          cols[n][r] = std::strtod(field[want[n]], nullptr);
+        else
+          phase[r] = (int)std::strtol(field[want[n]], nullptr, 10);
+      }
+    }
+  });
+  return true;
+}
 
 int fail_status(const char* what, nnpp_status st) {
   std::fprintf(stderr, "nnpp_run: %s failed (status %d): %s\n", what, (int)st, nnpp_last_error());
@@ -216,6 +365,7 @@ struct Options {
   double tol = 1e-10;
   int device = 0;
   bool output = true;
+  int restart = -1;  // start file number (main.cpp's third argument), -1: start from t = 0
 };
 
 int run(const std::string& prefix, const std::string& job, const Options& opt) {
@@ -260,7 +410,34 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
       std::copy(tmp.begin(), tmp.end(), passive.begin() + (size_t)(f - 5) * N);
 
   std::vector<int> phase0;
-  const bool have_phase = read_ints(job + ".phase0", N, phase0);
+  bool have_phase = read_ints(job + ".phase0", N, phase0);
+  // implant from its point cloud (BunnyConditions = 1, main.cpp:236-240, 316-325, 422-457):
+  // data1[3] points in <job>.bunnyNodes; a node within 3 * 0.4 dx (1 + 1e-5) of one is solid
+  // (Mg2+ at CSolid / CSolid, the other species 0), the others liquid with the reference's
+  // electrolyte (Mg2+ 0, H+ and OH- 1e-4 / CSolid, HCO3- C0HCO3 / CSolid = data2[11] / CSolid),
+  // the potential 0
+  std::vector<double> bunny;
+  if (d1[3] > 0 && read_doubles(job + ".bunnyNodes", 3 * (size_t)d1[3], bunny)) {
+    const size_t M = d1[3];
+    std::vector<double> pts(3 * M);
+    for (size_t j = 0; j < M; ++j)
+      for (int d = 0; d < 3; ++d) pts[d * M + j] = bunny[3 * j + d];
+    phase0.assign(N, 0);
+    const double t0 = now_s();
+    CALL("nnpp_implant_mask", nnpp_implant_mask(N, xyz.data(), (int)M, pts.data(), 3. * 0.4 * p.dx * (1.00 + 1e-5),
+                                               kMaxHorizon, nullptr, phase0.data()));
+    long long solid = 0;
+    const double liquid[kSpecies] = {0.0, 1e-4 / p.CSolid, 1e-4 / p.CSolid, d2[11] / p.CSolid};
+    for (size_t i = 0; i < (size_t)N; ++i) {
+      solid += phase0[i];
+      for (int k = 0; k < kSpecies; ++k)
+        ic[(size_t)k * N + i] = phase0[i] ? (k == 0 ? p.CSolid / p.CSolid : 0.0) : liquid[k];
+      ic[(size_t)kSpecies * N + i] = 0.0;
+    }
+    have_phase = true;
+    std::printf("Building bunnyNodes took %g seconds (%zu implant points, %lld solid nodes)\n", now_s() - t0, M,
+                solid);
+  }
 
   CALL("nnpp_set_device", nnpp_set_device(opt.device));
   nnpp_handle* h = nullptr;
@@ -274,6 +451,23 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
   std::printf("Building horizons took %g seconds. Max. horizon length: %d\n", now_s() - t0, max_len);
   std::printf("%d nodes; horizon radius: %.16g\n", N, p.delta);
   CALL("nnpp_set_solver", nnpp_set_solver(h, opt.tol, 2000, 0));
+  int s = 0;
+  if (opt.restart >= 0) {
+    // main.cpp:507-542: the state of <job><prefix>-<s0>.output.csv, read by column name
+    const std::string path = job + prefix + "-" + std::to_string(opt.restart) + ".output.csv";
+    const std::vector<std::string> names = {"Mg++", "H+", "OH-", "HCO3-", "CO32-", "HPO42-",
+                                            "PO43-", "Ca++", "Na+", "Cl-", "Phi"};
+    std::vector<std::vector<double> > cols;
+    std::vector<int> ph;
+    const double tr = now_s();
+    if (!read_start_csv(path, N, names, cols, ph)) return std::fprintf(stderr, "No start file found!\n"), 1;
+    std::vector<double> c0((size_t)kSpecies * N);
+    for (int k = 0; k < kSpecies; ++k) std::copy(cols[k].begin(), cols[k].end(), c0.begin() + (size_t)k * N);
+    for (int k = 0; k < 6; ++k) std::copy(cols[4 + k].begin(), cols[4 + k].end(), passive.begin() + (size_t)k * N);
+    CALL("nnpp_set_state", nnpp_set_state(h, c0.data(), cols[10].data(), ph.data()));
+    s = opt.restart;
+    std::printf("Restart from %s (%.3f s)\n", path.c_str(), now_s() - tr);
+  }
 
   const double dV = p.dx * p.dy * p.dz;
   std::vector<double> c((size_t)kSpecies * N), phi(N);
@@ -283,7 +477,6 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
     Out e(job + prefix + ".energy");
   }
   std::printf("Time Marching started:\n");
-  int s = 0;
   t0 = now_s();
   while (s < steps) {
     const int n = std::min(every - s % every, steps - s);
@@ -312,16 +505,9 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
       put(e.f, energy);
       std::fputc('\n', e.f);
     }
-    Out o(job + prefix + "-" + std::to_string(s) + ".output.csv");
-    if (!o.ok()) return std::fprintf(stderr, "nnpp_run: cannot write output\n"), 1;
-    std::fputs("X,Y,Z,Mg++,H+,OH-,HCO3-,CO32-,HPO42-,PO43-,Ca++,Na+,Cl-,Phi,Phase\n", o.f);
-    for (size_t i = 0; i < (size_t)N; ++i) {
-      for (int d = 0; d < 3; ++d) put(o.f, rows[3 * i + d]), std::fputc(',', o.f);
-      for (int k = 0; k < kSpecies; ++k) put(o.f, c[(size_t)k * N + i]), std::fputc(',', o.f);
-      for (int k = 0; k < 6; ++k) put(o.f, passive[(size_t)k * N + i]), std::fputc(',', o.f);
-      put(o.f, phi[i]);
-      std::fprintf(o.f, ",%d\n", phase[i]);
-    }
+    if (!write_output_csv(job + prefix + "-" + std::to_string(s) + ".output.csv", N, rows, c, passive, phi, phase,
+                          kSpecies))
+      return std::fprintf(stderr, "nnpp_run: cannot write output\n"), 1;
   }
   nnpp_destroy(h);
   return 0;
@@ -329,8 +515,9 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
 
 int usage() {
   std::fprintf(stderr,
-               "usage: nnpp_run <prefix> <jobname> [--steps N] [--every K] [--precision mixed|fp64]\n"
-               "                [--k-diss K] [--switch-width W] [--tol T] [--device D] [--no-output]\n"
+               "usage: nnpp_run <prefix> <jobname> [<startfileNo>] [--steps N] [--every K]\n"
+               "                [--precision mixed|fp64] [--k-diss K] [--switch-width W] [--tol T]\n"
+               "                [--device D] [--no-output] [--restart S0]\n"
                "       nnpp_run --write-synth <kind> <n_side> <seed> <jobname> [--steps N]\n");
   return 1;
 }
@@ -357,6 +544,8 @@ int main(int argc, char** argv) {
     else if (a == "--switch-width" && has) opt.switch_width = std::atof(argv[++i]);
     else if (a == "--tol" && has) opt.tol = std::atof(argv[++i]);
     else if (a == "--device" && has) opt.device = std::atoi(argv[++i]);
+    else if (a == "--restart" && has) opt.restart = std::atoi(argv[++i]);
+    else if (i == 3 && a.size() && a[0] != '-') opt.restart = std::atoi(argv[i]);  // main.cpp's 3rd argument
     else if (a == "--precision" && has) {
       const std::string v = argv[++i];
       if (v == "fp64") opt.precision = NNPP_FP64;

@@ -77,15 +77,17 @@ def build_reference_shim(force=False, verbose=False):
     """Returns the path of the shim, or None when the reference is not present."""
     helpers = os.path.join(REFERENCE_ROOT, "src", "helpers")
     eigen = os.path.join(REFERENCE_ROOT, "eigen")
+    kdtree = os.path.join(REFERENCE_ROOT, "libraries", "libkdtree++")
     if not (os.path.isdir(helpers) and os.path.isdir(eigen)):
         return None
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
     out = os.path.join(outdir, "libnnpp_ref.so")
     src = os.path.join(HERE, "ref_shim.cpp")
-    deps = [src, os.path.join(helpers, "grid.h"), os.path.join(helpers, "utils.h")]
+    deps = [src, os.path.join(helpers, "grid.h"), os.path.join(helpers, "utils.h"),
+            os.path.join(helpers, "kd_tree_interface.h"), os.path.abspath(__file__)]
     if force or not _newer(out, deps):
-        cmd = ["g++"] + CXXFLAGS + ["-w", "-I", helpers, "-I", eigen, src, "-o", out]
+        cmd = ["g++"] + CXXFLAGS + ["-w", "-I", helpers, "-I", eigen, "-I", kdtree, src, "-o", out]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

@@ -638,6 +638,273 @@ double mg_mass_lost(const Oracle& o) {
 }  // namespace
 
 // ================================================================ C interface =============
+// ---------------------------------------------------------------- implicit step ----------
+// The reference's production time step (main.cpp:640-922): backward Euler with one tangent
+// per step (utils::NewtonMatrices, utils.h:844-1790), then Newton iterations of
+//   F = Residuals(U^{n+1}, U^n)  (utils.h:29-842; Dirichlet rows F = U - bc, main.cpp:676-712)
+//   K_f dU_f = -F_f for every field f separately (Eigen::GMRES, restart 30, diagonal
+//   preconditioner, tolerance EPS, MAX_ITER iterations: main.cpp:714-779),
+//   U += dU, the positivity clamp (main.cpp:805-837),
+// until max_f | ||dU_f|| - ||dU_f|| of the previous iteration | < EPS (main.cpp:847-895), then
+// the phase flip (main.cpp:914-922).  Here with four species and the potential: the migration
+// terms use the lagged potential phi^n (U11n, utils.h:126), the potential's residual the
+// new one.  EPS = 10E-6, MAX_ITER = 200 (main.cpp:33-36).
+constexpr double kNewtonEps = 10E-6;
+constexpr int kNewtonMaxIter = 200;
+
+// Residual of the implicit step (utils.h:72-178, 181-257, 798-841 with U^{n+1} = c1, phi1 and
+// U^n = c0, phi0): the time term (c1 - c0) / dt, the bond sums at c1 with the migration
+// potential phi0, the dissolution source at c1; F11 at (c1, phi1).
+void residuals_implicit(const Oracle& o, const double* c1, const double* phi1, const double* c0,
+                        const double* phi0, const int* phase, double voln1rel, double* F) {
+  residuals(o, c1, phi0, phase, voln1rel, F, nullptr, nullptr);
+  const int N = o.N;
+  std::vector<double> F11(F + (int64_t)S * N, F + (int64_t)(S + 1) * N);
+  std::vector<double> tmp((int64_t)(S + 1) * N);
+  residuals(o, c1, phi1, phase, voln1rel, tmp.data(), nullptr, nullptr);
+#pragma omp parallel for
+  for (int i = 0; i < N; ++i) {
+    for (int k = 0; k < S; ++k) {
+      const int64_t q = (int64_t)k * N + i;
+      // residuals() adds (c - c) / dt = 0; the reference's (U^{n+1} - U^n) / dt first
+      F[q] = ((c1[q] - c0[q]) / o.p.dt) + F[q];
+    }
+    F[(int64_t)S * N + i] = tmp[(int64_t)S * N + i];
+  }
+}
+
+// Tangent of species k (utils.h:900-1010 for Mg, 1012-1102 for the generic species; the
+// reaction terms of the diagonal vanish for this model): per bond (slot j of row i)
+//   off[j] = -( K1 D(BV) / xi^(3+2s1) + K2 D(BV) z F / (R T) (phi_n - phi_i) / xi^(3+2s2) ) beta dV
+// with the generic species' solid-solid bonds absent; diag[i] = 1/dt - sum_K,
+// sum_K = sum -(K1 D(BV) / xi^(3+2s1)) beta dV; Dirichlet rows identity.
+void species_tangent(const Oracle& o, int k, const double* phi0, const int* phase, double voln1rel,
+                     std::vector<double>& diag, std::vector<double>& off) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  const double BVmix = std::pow(10., -p.vol_red * (1. - voln1rel));
+  diag.assign(N, 1.0);
+  off.assign(o.cols.size(), 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    if (o.dir[(int64_t)k * N + i]) continue;
+    double sumK = 0.0;
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) {
+      const int n = o.cols[j];
+      const int pi = phase[i], pn = phase[n];
+      double D, BV = 1.0;
+      if (k == 0) {
+        if ((pi == 1 && pn == 0) || (pn == 1 && pi == 0)) BV = BVmix;
+        D = (pi == 0 && pn == 0) ? p.D_liquid[0] : p.D_solid[0];
+      } else {
+        if (pi == 1 && pn == 1) continue;
+        D = (pi == 0 && pn == 0) ? p.D_liquid[k] : p.D_solid[k];
+      }
+      const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+      const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+      const double bt = beta_fn(xi, p.delta, p.dx);
+      if (k == 0) {
+        sumK += -(p.K1[0] * D * BV / std::pow(xi, 3.0 + 2.0 * p.s1[0])) * bt * p.dx * p.dy * p.dz;
+        off[j] = -((p.K1[0] * D * BV / std::pow(xi, 3.0 + 2.0 * p.s1[0])) +
+                   (p.K2[0] * D * BV * p.z[0] * p.F / (p.R * p.T) * (phi0[n] - phi0[i]) /
+                    std::pow(xi, 3.0 + 2.0 * p.s2[0]))) *
+                 bt * p.dx * p.dy * p.dz;
+      } else {
+        sumK += -(p.K1[k] * D / std::pow(xi, 3.0 + 2.0 * p.s1[k])) * bt * p.dx * p.dy * p.dz;
+        off[j] = -((p.K1[k] * D / std::pow(xi, 3.0 + 2.0 * p.s1[k])) +
+                   (p.K2[k] * D * p.z[k] * p.F / (p.R * p.T) * (phi0[n] - phi0[i]) /
+                    std::pow(xi, 3.0 + 2.0 * p.s2[k]))) *
+                 bt * p.dx * p.dy * p.dz;
+      }
+    }
+    diag[i] = (1. / p.dt) - sumK - 0.0;
+  }
+}
+
+// y = K x for a field's tangent: diag and per-bond off-diagonals (rows of the reference's
+// neighbour lists, slot 0 the node itself)
+void apply_tangent(const Oracle& o, const std::vector<double>& diag, const std::vector<double>& off,
+                   const double* x, double* y) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < o.N; ++i) {
+    double acc = diag[i] * x[i];
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) acc += off[j] * x[o.cols[j]];
+    y[i] = acc;
+  }
+}
+
+double norm2(const double* a, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += a[i] * a[i];
+  return std::sqrt(s);
+}
+
+// Eigen::GMRES (GMRES.h:56-203) as the reference calls it: initial guess x = b
+// (_solve_impl, GMRES.h:330-334; nothing to do for b = 0), the diagonal (Jacobi) preconditioner
+// applied on the left, restarts of `restart` steps, iterations counted over restarts up to
+// maxit, stop when |g_k| / ||M^-1 (b - A x_0)|| < tol (the initial preconditioned residual,
+// kept across restarts).  The Arnoldi basis is built by modified Gram-Schmidt (the reference
+// uses Householder reflections: the same Krylov space and least-squares problem).  Returns
+// the iterations.
+int gmres(const Oracle& o, const std::vector<double>& diag, const std::vector<double>& off, const double* b,
+          double* x, double tol, int restart, int maxit) {
+  const int n = o.N;
+  bool zero = true;
+  for (int i = 0; i < n && zero; ++i) zero = b[i] == 0.0;
+  if (zero) {
+    std::fill(x, x + n, 0.0);
+    return 0;
+  }
+  std::copy(b, b + n, x);
+  std::vector<double> r(n), t(n);
+  auto presid = [&]() {
+    apply_tangent(o, diag, off, x, t.data());
+    for (int i = 0; i < n; ++i) r[i] = (b[i] - t[i]) / diag[i];
+  };
+  presid();
+  const double r0norm = norm2(r.data(), n);
+  if (r0norm == 0.0) return 0;
+  int iters = 0;
+  std::vector<std::vector<double> > V(restart + 1, std::vector<double>(n));
+  std::vector<double> H((size_t)(restart + 1) * restart), cs(restart), sn(restart), g(restart + 1);
+  for (;;) {
+    const double beta = norm2(r.data(), n);
+    for (int i = 0; i < n; ++i) V[0][i] = r[i] / beta;
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    bool stop = false;
+    for (k = 1; k <= restart; ++k) {
+      ++iters;
+      std::vector<double>& w = V[k];
+      apply_tangent(o, diag, off, V[k - 1].data(), t.data());
+      for (int i = 0; i < n; ++i) w[i] = t[i] / diag[i];
+      for (int q = 0; q < k; ++q) {
+        double h = 0.0;
+        for (int i = 0; i < n; ++i) h += w[i] * V[q][i];
+        H[(size_t)q * restart + (k - 1)] = h;
+        for (int i = 0; i < n; ++i) w[i] -= h * V[q][i];
+      }
+      const double hk = norm2(w.data(), n);
+      H[(size_t)k * restart + (k - 1)] = hk;
+      if (hk != 0.0)
+        for (int i = 0; i < n; ++i) w[i] /= hk;
+      for (int q = 0; q < k - 1; ++q) {  // earlier rotations on the new column
+        const double a = H[(size_t)q * restart + (k - 1)], c = H[(size_t)(q + 1) * restart + (k - 1)];
+        H[(size_t)q * restart + (k - 1)] = cs[q] * a + sn[q] * c;
+        H[(size_t)(q + 1) * restart + (k - 1)] = -sn[q] * a + cs[q] * c;
+      }
+      const double a = H[(size_t)(k - 1) * restart + (k - 1)], c = H[(size_t)k * restart + (k - 1)];
+      const double den = std::hypot(a, c);
+      cs[k - 1] = den == 0.0 ? 1.0 : a / den;
+      sn[k - 1] = den == 0.0 ? 0.0 : c / den;
+      H[(size_t)(k - 1) * restart + (k - 1)] = den;
+      H[(size_t)k * restart + (k - 1)] = 0.0;
+      g[k] = -sn[k - 1] * g[k - 1];
+      g[k - 1] = cs[k - 1] * g[k - 1];
+      const double err = std::abs(g[k]) / r0norm;
+      stop = k == n || err < tol || iters == maxit;
+      if (stop || k == restart) break;
+    }
+    if (k > restart) k = restart;
+    // y = H^-1 g (upper triangular), x += V y
+    std::vector<double> y(k);
+    for (int q = k - 1; q >= 0; --q) {
+      double sum = g[q];
+      for (int u = q + 1; u < k; ++u) sum -= H[(size_t)q * restart + u] * y[u];
+      y[q] = sum / H[(size_t)q * restart + q];
+    }
+    for (int q = 0; q < k; ++q)
+      for (int i = 0; i < n; ++i) x[i] += y[q] * V[q][i];
+    if (stop) return iters;
+    presid();
+  }
+}
+
+// K11 (the potential's tangent, utils.h:1797-1848) in the diag/off form of apply_tangent:
+// off-diagonal -w on liquid-liquid bonds of free rows, identity rows elsewhere
+void potential_tangent(Oracle& o, const int* phase, std::vector<double>& diag, std::vector<double>& off) {
+  build_operator(o, phase);
+  diag = o.diag;
+  off.assign(o.cols.size(), 0.0);
+  for (size_t j = 0; j < off.size(); ++j) off[j] = -o.wphi[j];
+}
+
+struct ImplicitStats {
+  int newton = 0;
+  int64_t krylov = 0;
+};
+
+// One implicit step of the reference's time loop from the oracle's state (c, phi = U^n).
+int implicit_step(Oracle& o, ImplicitStats* st) {
+  const nnpp_params& p = o.p;
+  const int N = o.N;
+  const int F1 = S + 1;
+  std::vector<double> u0((int64_t)F1 * N), u1, F((int64_t)F1 * N), dU((int64_t)F1 * N), rhs(N);
+  std::copy(o.c.begin(), o.c.end(), u0.begin());
+  std::copy(o.phi.begin(), o.phi.end(), u0.begin() + (int64_t)S * N);
+  u1 = u0;
+  const double* phi0 = u0.data() + (int64_t)S * N;
+  // the tangents once per step, at U^{n+1} = U^n (main.cpp:657-662)
+  std::vector<double> diag[S + 1], off[S + 1];
+  for (int k = 0; k < S; ++k) species_tangent(o, k, phi0, o.phase.data(), o.voln1rel, diag[k], off[k]);
+  potential_tangent(o, o.phase.data(), diag[S], off[S]);
+  double res_old[S + 1] = {0, 0, 0, 0, 0};
+  const double floor_c = 1.0e-8 / p.CSolid;
+  int it = 0;
+  for (it = 0; it < kNewtonMaxIter; ++it) {
+    residuals_implicit(o, u1.data(), u1.data() + (int64_t)S * N, u0.data(), phi0, o.phase.data(), o.voln1rel,
+                       F.data());
+    // main.cpp:676-712: species' boundary values divided by CSolid, the potential's not
+    for (int f = 0; f <= S; ++f)
+      for (int i = 0; i < N; ++i)
+        if (o.dir[(int64_t)f * N + i])
+          F[(int64_t)f * N + i] =
+              u1[(int64_t)f * N + i] - (f < S ? o.bcv[(int64_t)f * N + i] / p.CSolid : o.bcv[(int64_t)f * N + i]);
+    double res[S + 1];
+    for (int f = 0; f <= S; ++f) {
+      for (int i = 0; i < N; ++i) rhs[i] = -F[(int64_t)f * N + i];
+      const int kit = gmres(o, diag[f], off[f], rhs.data(), dU.data() + (int64_t)f * N, kNewtonEps, 30,
+                            kNewtonMaxIter);
+      if (st) st->krylov += kit;
+    }
+    for (int f = 0; f <= S; ++f) {
+      for (int i = 0; i < N; ++i) u1[(int64_t)f * N + i] += dU[(int64_t)f * N + i];
+      res[f] = norm2(dU.data() + (int64_t)f * N, N);
+    }
+    for (int k = 0; k < S; ++k)
+      for (int i = 0; i < N; ++i)
+        if (u1[(int64_t)k * N + i] < floor_c) u1[(int64_t)k * N + i] = floor_c;
+    double resMax = 0.0;
+    for (int f = 0; f <= S; ++f) resMax = std::max(resMax, std::abs(res[f] - res_old[f]));
+    if (resMax < kNewtonEps) {
+      ++it;
+      break;
+    }
+    for (int f = 0; f <= S; ++f) res_old[f] = res[f];
+  }
+  if (st) st->newton = it;
+  std::copy(u1.begin(), u1.begin() + (int64_t)S * N, o.c.begin());
+  std::copy(u1.begin() + (int64_t)S * N, u1.end(), o.phi.begin());
+  // phase flip (main.cpp:914-922) and the volume (main.cpp:944-949) as in the explicit step
+  const double csat = p.CSat / p.CSolid;
+  for (int i = 0; i < N; ++i)
+    if (o.phase[i] == 1 && o.c[i] <= csat) {
+      o.phase[i] = 0;
+      o.flip_step[i] = (int)(o.steps_done + 1);
+      o.solid_count -= 1;
+      o.op_valid = false;
+    }
+  o.steps_done += 1;
+  if (p.sub_step_no > 0 && o.steps_done % p.sub_step_no == 0) {
+    double v = 0.0;
+    for (int i = 0; i < N; ++i)
+      if (o.phase[i] == 1) v += o.c[i] - csat;
+    o.voln1rel = o.vol0rel != 0.0 ? v / o.vol0rel : 0.0;
+  }
+  return 0;
+}
+
 extern "C" {
 
 void* orc_create(const nnpp_params* p, int N, const double* xyz, const int* bctypes,
@@ -850,6 +1117,77 @@ int orc_get_diag(void* h, double* out) {
   out[12] = (double)o->cg_nc;
   out[13] = o->last_relres;
   return 0;
+}
+
+// The implant mask's counts (main.cpp:316-325 with kd_tree_interface.h:156-252): for each
+// node the implant points inside the box node +- r (libkdtree++ region bounds c - r, c + r,
+// region.hpp:50-51, inclusive as region.hpp:86-93 tests them) whose Euclidean distance
+// sqrt(x*x + y*y + z*z) (kd_tree_interface.h:42-48, x = point - node) is <= r.  Every point
+// is tested against every node (OpenMP over the nodes): the restatement needs no tree.
+int orc_implant_counts(int N, const double* nodes, int M, const double* points, double r, int* counts) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < N; ++i) {
+    const double c[3] = {nodes[i], nodes[(int64_t)N + i], nodes[2 * (int64_t)N + i]};
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = c[d] - r;
+      hi[d] = c[d] + r;
+    }
+    int cnt = 0;
+    for (int j = 0; j < M; ++j) {
+      const double q[3] = {points[j], points[(int64_t)M + j], points[2 * (int64_t)M + j]};
+      bool in = true;
+      for (int d = 0; d < 3; ++d) in = in && !(q[d] < lo[d]) && !(hi[d] < q[d]);
+      if (!in) continue;
+      const double x = q[0] - c[0], y = q[1] - c[1], z = q[2] - c[2];
+      if (std::sqrt(x * x + y * y + z * z) <= r) ++cnt;
+    }
+    counts[i] = cnt;
+  }
+  return 0;
+}
+
+// n implicit steps (main.cpp:640-922); Newton iterations and GMRES iterations over them
+int orc_implicit_forward(void* h, int n_steps, int64_t* newton, int64_t* krylov) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb) return 7;
+  int64_t nw = 0, kr = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    ImplicitStats st;
+    implicit_step(*o, &st);
+    nw += st.newton;
+    kr += st.krylov;
+  }
+  if (newton) *newton = nw;
+  if (krylov) *krylov = kr;
+  return 0;
+}
+
+// The tangent of field f (0..3 species, 4 potential) at the current state, in the layout of
+// the neighbour lists (off[j] for slot j, slot 0 of a row unused)
+int orc_tangent(void* h, int f, double* diag, double* off) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb || f < 0 || f > S) return 1;
+  std::vector<double> d, q;
+  if (f < S)
+    species_tangent(*o, f, o->phi.data(), o->phase.data(), o->voln1rel, d, q);
+  else
+    potential_tangent(*o, o->phase.data(), d, q);
+  std::copy(d.begin(), d.end(), diag);
+  std::copy(q.begin(), q.end(), off);
+  return 0;
+}
+
+// x = GMRES(K_f, b) as the implicit step solves its corrections
+int orc_tangent_gmres(void* h, int f, const double* b, double* x, double tol, int restart, int maxit) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!o->have_nb || f < 0 || f > S) return -1;
+  std::vector<double> d, q;
+  if (f < S)
+    species_tangent(*o, f, o->phi.data(), o->phase.data(), o->voln1rel, d, q);
+  else
+    potential_tangent(*o, o->phase.data(), d, q);
+  return gmres(*o, d, q, b, x, tol, restart, maxit);
 }
 
 }  // extern "C"

@@ -62,6 +62,10 @@ def load_oracle():
             "orc_get_state": (C.c_int, [_P, _DP, _DP, _IP, _IP]),
             "orc_set_state": (C.c_int, [_P, _DP, _DP, _IP]),
             "orc_get_diag": (C.c_int, [_P, _DP]),
+            "orc_implant_counts": (C.c_int, [C.c_int, _DP, C.c_int, _DP, C.c_double, _IP]),
+            "orc_implicit_forward": (C.c_int, [_P, C.c_int, _LP, _LP]),
+            "orc_tangent": (C.c_int, [_P, C.c_int, _DP, _DP]),
+            "orc_tangent_gmres": (C.c_int, [_P, C.c_int, _DP, _DP, C.c_double, C.c_int, C.c_int]),
             "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
             "nnpp_synth_fill": (C.c_int, [C.c_int, C.c_int, C.c_uint64, _DP, _IP, _DP, _DP, _IP,
                                           C.c_void_p]),
@@ -91,6 +95,14 @@ def load_reference():
                                     _DP, _DP, _DP, _DP]
         L.ref_newton_k11.argtypes = [C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
                                      _DP, _DP, _DP, _LP, _IP, _IP, _DP]
+        for name in ("ref_newton_k", "ref_gmres"):
+            getattr(L, name).restype = C.c_int
+        L.ref_newton_k.argtypes = [C.c_int, C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
+                                   _DP, _DP, _DP, _LP, _IP, _IP, _DP]
+        L.ref_gmres.argtypes = [C.c_int, C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
+                                _DP, _DP, _DP, _DP, _DP]
+        L.ref_implant_counts.restype = C.c_int
+        L.ref_implant_counts.argtypes = [C.c_int, _DP, C.c_int, _DP, C.c_double, C.c_int, _IP]
         _ref = L
     return _ref
 
@@ -105,6 +117,11 @@ class Params(C.Structure):
                 ("K2", C.c_double * 4), ("sigma", C.c_double), ("s_phi", C.c_double),
                 ("K_phi", C.c_double), ("k_diss", C.c_double), ("switch_width", C.c_double),
                 ("c_floor", C.c_double), ("sub_step_no", C.c_int), ("reserved", C.c_int)]
+
+    def copy(self):
+        q = Params()
+        C.memmove(C.byref(q), C.byref(self), C.sizeof(Params))
+        return q
 
 
 def synth(kind, n_side, seed=0):
@@ -124,6 +141,34 @@ def synth(kind, n_side, seed=0):
                          C.cast(C.byref(p), C.c_void_p)) != 0:
         raise RuntimeError("synthetic workload generation failed")
     return dict(nodes=nodes, bctypes=bct, bcvalues=bcv, icvalues=icv, phase0=ph, params=p, N=N)
+
+
+def implant_counts(nodes, points, r):
+    """Implant points within r of every node (the oracle's restatement of the reference's
+    kd-tree query, kd_tree_interface.h:156-252); nodes (3, N), points (3, M)."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    points = np.ascontiguousarray(points, dtype=np.float64)
+    counts = np.empty(nodes.shape[1], dtype=np.int32)
+    load_oracle().orc_implant_counts(nodes.shape[1], _dp(nodes), points.shape[1], _dp(points), r,
+                                     _ip(counts))
+    return counts
+
+
+def synth_implant_points(n_side, seed, shape="sphere"):
+    """A seeded implant point cloud (the reference's implant meshes are not available): the
+    points of a jittered lattice of spacing 0.4 / n_side (0.4 of the node spacing of an
+    n_side^3 node lattice on the unit cube) that fall inside a sphere of radius 0.3 at the
+    centre ("sphere") or inside the sphere's shell of thickness 0.05 ("shell"), from numpy's
+    PCG64 (the same points on every machine)."""
+    rng = np.random.default_rng(seed)
+    h = 0.4 / n_side
+    m = int(round(1.0 / h))
+    g = (np.arange(m) + 0.5) * h
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    P = np.stack([X.ravel(), Y.ravel(), Z.ravel()]) + rng.uniform(-0.25 * h, 0.25 * h, (3, m ** 3))
+    rr = np.sqrt(((P - 0.5) ** 2).sum(axis=0))
+    keep = rr <= 0.3 if shape == "sphere" else (rr <= 0.3) & (rr >= 0.25)
+    return np.ascontiguousarray(P[:, keep])
 
 
 DIAG_KEYS = ["steps", "solid_count", "voln1rel", "vol0rel", "mass0", "mass1", "mass2", "mass3",
@@ -230,6 +275,30 @@ class Oracle:
         phase = None if phase is None else np.ascontiguousarray(phase, dtype=np.int32)
         load_oracle().orc_set_state(self._h, _dp(c), _dp(phi), _ip(phase))
 
+    def implicit_forward(self, n_steps):
+        """n implicit steps of the reference's Newton/GMRES loop (main.cpp:640-922); returns
+        (Newton iterations, GMRES iterations) summed over the steps."""
+        nw, kr = C.c_int64(0), C.c_int64(0)
+        st = load_oracle().orc_implicit_forward(self._h, n_steps, C.byref(nw), C.byref(kr))
+        if st != 0:
+            raise RuntimeError("oracle implicit step failed with status %d" % st)
+        return nw.value, kr.value
+
+    def tangent(self, field):
+        """(diag (N,), off (nnz incl. self slots,)) of the implicit step's tangent of field
+        0..3 (species) or 4 (potential) at the current state, in the layout of clouds()."""
+        L = load_oracle()
+        diag = np.empty(self.N)
+        off = np.empty(L.orc_nnz(self._h))
+        L.orc_tangent(self._h, field, _dp(diag), _dp(off))
+        return diag, off
+
+    def tangent_gmres(self, field, b, tol=10e-6, restart=30, maxit=200):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty(self.N)
+        it = load_oracle().orc_tangent_gmres(self._h, field, _dp(b), _dp(x), tol, restart, maxit)
+        return x, it
+
     def diagnostics(self):
         out = np.empty(len(DIAG_KEYS))
         load_oracle().orc_get_diag(self._h, _dp(out))
@@ -334,6 +403,46 @@ def ref_k11(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel=0.0)
     val = np.empty(nnz.value)
     L.ref_newton_k11(*args, C.byref(nnz), _ip(ri), _ip(ci), _dp(val))
     return ri, ci, val
+
+
+def _ref_tangent_args(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel):
+    N = nodes.shape[1]
+    d2, dc, d11 = reference_params_vectors(p)
+    U = _u11(c, phi, N)
+    B = _bc11(bctypes, bcvalues, N)
+    keep = [np.ascontiguousarray(nodes), np.ascontiguousarray(ptr, dtype=np.int64),
+            np.ascontiguousarray(cols, dtype=np.int32), U, np.ascontiguousarray(phase, dtype=np.int32),
+            np.ascontiguousarray(bctypes, dtype=np.int32), B, d2, np.ascontiguousarray(dc), d11]
+    args = [N, _dp(keep[0]), _lp(keep[1]), _ip(keep[2]), _dp(keep[3]), _ip(keep[4]), _ip(keep[5]),
+            _dp(keep[6]), voln1rel, _dp(keep[7]), _dp(keep[8]), _dp(keep[9])]
+    return args, keep
+
+
+def ref_newton_k(which, p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel=0.0):
+    """K_(which+1) of the reference's utils::NewtonMatrices as COO (rows, cols, values)."""
+    L = load_reference()
+    if L is None:
+        return None
+    args, keep = _ref_tangent_args(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel)
+    nnz = C.c_int64(0)
+    L.ref_newton_k(which, *args, C.byref(nnz), None, None, None)
+    ri = np.empty(nnz.value, dtype=np.int32)
+    ci = np.empty(nnz.value, dtype=np.int32)
+    val = np.empty(nnz.value)
+    L.ref_newton_k(which, *args, C.byref(nnz), _ip(ri), _ip(ci), _dp(val))
+    return ri, ci, val
+
+
+def ref_gmres(which, p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, b, voln1rel=0.0):
+    """The reference's Eigen::GMRES solve of K_(which+1) x = b (main.cpp:714-779)."""
+    L = load_reference()
+    if L is None:
+        return None
+    args, keep = _ref_tangent_args(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty(nodes.shape[1])
+    it = L.ref_gmres(which, *args, _dp(b), _dp(x))
+    return x, it
 
 
 def _adjoint_sigs():

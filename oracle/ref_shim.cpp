@@ -7,13 +7,16 @@
 // tests/golden/.  Nothing here is part of the product.
 #include <cstdint>
 #include <cstring>
+#include <iostream>
 #include <vector>
 
 #include <Eigen/Dense>
 #include <Eigen/Sparse>
+#include <unsupported/Eigen/IterativeSolvers>
 
 #include "grid.h"
 #include "utils.h"
+#include "kd_tree_interface.h"
 
 namespace {
 
@@ -122,11 +125,13 @@ int ref_residuals(int N, const double* xyz, const int64_t* row_ptr, const int* c
   return 0;
 }
 
-// K11 of utils::NewtonMatrices (utils.h:1794-1848) as COO; call with out == NULL for nnz.
-int ref_newton_k11(int N, const double* xyz, const int64_t* row_ptr, const int* cols,
-                   const double* U, const int* phase, const int* bctypes, const double* bcvalues,
-                   double voln1rel, const double* data2, const double* datac,
-                   const double* datac11, int64_t* nnz, int* ri, int* ci, double* val) {
+// All eleven tangents of utils::NewtonMatrices (utils.h:844-1849) at the state U (used as
+// both U^{n+1} and U^n), kept for the entry points below.
+std::vector<SpMat> g_K;
+
+void newton_matrices(int N, const double* xyz, const int64_t* row_ptr, const int* cols, const double* U,
+                     const int* phase, const int* bctypes, const double* bcvalues, double voln1rel,
+                     const double* data2, const double* datac, const double* datac11) {
   utils::parameter prm;
   make_params(prm, N, data2, datac, datac11);
   Eigen::MatrixXd nodes(N, 3);
@@ -152,13 +157,24 @@ int ref_newton_k11(int N, const double* xyz, const int64_t* row_ptr, const int* 
     u[k] = Eigen::Map<const Eigen::VectorXd>(U + (int64_t)k * N, N);
   }
   std::vector<Eigen::VectorXd> un1(u);
-  std::vector<SpMat> K(11, SpMat(N, N));
+  g_K.assign(11, SpMat(N, N));
+  std::vector<SpMat>& K = g_K;
   utils::NewtonMatrices(K[0], K[1], K[2], K[3], K[4], K[5], K[6], K[7], K[8], K[9], K[10], nodes,
                         hz, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], bc[6], bc[7], bc[8], bc[9],
                         bc[10], un1[0], un1[1], un1[2], un1[3], un1[4], un1[5], un1[6], un1[7],
                         un1[8], un1[9], un1[10], u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7],
                         u[8], u[9], u[10], ph, hl, bt, voln1rel, prm);
-  const SpMat& A = K[10];
+}
+
+// K_(which+1) of utils::NewtonMatrices (which 0..10; 10 is K11, utils.h:1794-1848) as COO;
+// call with ri == NULL for nnz.
+int ref_newton_k(int which, int N, const double* xyz, const int64_t* row_ptr, const int* cols,
+                 const double* U, const int* phase, const int* bctypes, const double* bcvalues,
+                 double voln1rel, const double* data2, const double* datac, const double* datac11,
+                 int64_t* nnz, int* ri, int* ci, double* val) {
+  if (which < 0 || which > 10) return 1;
+  newton_matrices(N, xyz, row_ptr, cols, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11);
+  const SpMat& A = g_K[which];
   *nnz = A.nonZeros();
   if (!ri) return 0;
   int64_t t = 0;
@@ -169,6 +185,55 @@ int ref_newton_k11(int N, const double* xyz, const int64_t* row_ptr, const int* 
       val[t] = it.value();
       ++t;
     }
+  return 0;
+}
+
+int ref_newton_k11(int N, const double* xyz, const int64_t* row_ptr, const int* cols,
+                   const double* U, const int* phase, const int* bctypes, const double* bcvalues,
+                   double voln1rel, const double* data2, const double* datac,
+                   const double* datac11, int64_t* nnz, int* ri, int* ci, double* val) {
+  return ref_newton_k(10, N, xyz, row_ptr, cols, U, phase, bctypes, bcvalues, voln1rel, data2, datac,
+                      datac11, nnz, ri, ci, val);
+}
+
+// x = GMRES(K_(which+1)) b as main.cpp:714-779 solves the Newton corrections: Eigen::GMRES
+// with the diagonal preconditioner, tolerance EPS = 10E-6, MAX_ITER = 200 iterations.
+// Returns the iterations.
+int ref_gmres(int which, int N, const double* xyz, const int64_t* row_ptr, const int* cols,
+              const double* U, const int* phase, const int* bctypes, const double* bcvalues,
+              double voln1rel, const double* data2, const double* datac, const double* datac11,
+              const double* b, double* x) {
+  if (which < 0 || which > 10) return -1;
+  newton_matrices(N, xyz, row_ptr, cols, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11);
+  Eigen::GMRES<SpMat, Eigen::DiagonalPreconditioner<double> > solver(g_K[which]);
+  solver.setTolerance(10E-6);
+  solver.setMaxIterations(200);
+  Eigen::VectorXd bb = Eigen::Map<const Eigen::VectorXd>(b, N);
+  Eigen::VectorXd xx = solver.solve(bb);
+  for (int i = 0; i < N; ++i) x[i] = xx[i];
+  return (int)solver.iterations();
+}
+
+// The implant mask's point counts as main.cpp:316-325 computes them: build_clouds(0,
+// max_node_no, r, 0, nodes, implant points, ...) of kd_tree_interface.h:156-252 (libkdtree++
+// range query, Euclidean filter); the cloud lengths are the counts.  2 where it throws.
+int ref_implant_counts(int N, const double* xyz, int M, const double* pts, double r, int max_node_no,
+                       int* counts) {
+  Eigen::MatrixXd nodes(N, 3), implant(M, 3);
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) nodes(i, d) = xyz[(int64_t)d * N + i];
+  for (int j = 0; j < M; ++j)
+    for (int d = 0; d < 3; ++d) implant(j, d) = pts[(int64_t)d * M + j];
+  Eigen::MatrixXi clouds;
+  Eigen::VectorXi lengths;
+  int ml = 0;
+  double mean = 0.0;
+  try {
+    build_clouds(0, max_node_no, r, 0.0, nodes, implant, clouds, lengths, ml, mean);
+  } catch (const std::runtime_error&) {
+    return 2;
+  }
+  for (int i = 0; i < N; ++i) counts[i] = lengths[i];
   return 0;
 }
 

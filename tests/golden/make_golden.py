@@ -10,6 +10,8 @@ by oracle/build_oracle.py, on the synthetic workloads of nnpp_synth_fill, and st
   k11.json        SHA-256 and sums of the reference's K11 entries on a small case
   synth.json      SHA-256 of the generated node coordinates (cross-platform determinism)
   params.json     the reference's control vectors of data/NNPP.data2, .datac1-4, .datac11
+  implant.json    SHA-256 of the point counts of the reference's kd-tree implant query for
+                  seeded implant point clouds
 Needs the reference's sources (REFERENCE_ROOT); run:  python tests/golden/make_golden.py
 """
 import hashlib
@@ -51,7 +53,43 @@ def residual_state(N, seed):
     return c, phi
 
 
+# implant point clouds (oracle.synth_implant_points) on the nodes of synthetic workloads
+IMPLANT = [(0, 20, 0, "sphere"), (1, 24, 3, "shell"), (1, 16, 5, "sphere")]
+
+
+def implant_fixtures():
+    """Point counts of the reference's kd-tree implant query (kd_tree_interface.h:156-252,
+    as main.cpp:316-325 calls it with r = 3 * 0.4 dx (1 + 1e-5)) -> implant.json."""
+    import ctypes as C
+    import oracle as O
+    L = O.load_reference()
+    out = {}
+    for kind, n, seed, shape in IMPLANT:
+        inp = O.synth(kind, n, seed)
+        nodes = np.ascontiguousarray(inp["nodes"])
+        pts = O.synth_implant_points(n, seed, shape)
+        r = 3 * 0.4 * inp["params"].dx * (1 + 1e-5)
+        N = nodes.shape[1]
+        counts = np.empty(N, dtype=np.int32)
+        st = L.ref_implant_counts(N, nodes.ctypes.data_as(C.POINTER(C.c_double)), pts.shape[1],
+                                  pts.ctypes.data_as(C.POINTER(C.c_double)), r, 1024,
+                                  counts.ctypes.data_as(C.POINTER(C.c_int)))
+        if st != 0:
+            raise SystemExit("reference implant query failed")
+        key = "kind%d_n%d_seed%d_%s" % (kind, n, seed, shape)
+        out[key] = {"kind": kind, "n_side": n, "seed": seed, "shape": shape, "r": r, "N": int(N),
+                    "M": int(pts.shape[1]), "points_sha256": nodes_digest(pts),
+                    "counts_sha256": hashlib.sha256(counts.tobytes()).hexdigest(),
+                    "solid": int((counts > 0).sum()), "sum": int(counts.sum())}
+        print(key, out[key], flush=True)
+    with open(os.path.join(HERE, "implant.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
 def main():
+    if "--only-implant" in sys.argv:
+        implant_fixtures()
+        return
     from conftest import load_package
     import oracle as O
     nn = load_package()
@@ -125,6 +163,7 @@ def main():
         params[name] = vals
     with open(os.path.join(HERE, "params.json"), "w") as f:
         json.dump(params, f, indent=1)
+    implant_fixtures()
     print("fixtures written", flush=True)
 
 

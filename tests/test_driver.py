@@ -102,3 +102,55 @@ def test_driver_run_matches_oracle(nn, orc, tmp_path):
     vol = [float(x.strip().rstrip(",")) for x in open(job + "-fp64.volume") if x.strip()]
     assert len(vol) == steps // 8
     assert len(open(job + "-fp64.energy").read().split()) == steps // 8
+
+
+@pytest.mark.gpu
+def test_driver_restart_continues_the_run(nn, tmp_path):
+    """main.cpp:507-542: a run restarted from its own step-8 output CSV (state read back by
+    column name) ends at step 16 where the uninterrupted run does (to the solver tolerance:
+    the file holds 16 significant digits and the restart has no warm-start history)."""
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    import shutil
+    job = str(tmp_path / "SYN")
+    _write(job, 1, 12, 7, 16)
+    common = ["--precision", "fp64", "--tol", "1e-12", "--every", "8"]
+    r = subprocess.run([_driver(), "-a", job] + common, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    shutil.copy(job + "-a-8.output.csv", job + "-b-8.output.csv")
+    r = subprocess.run([_driver(), "-b", job, "8"] + common, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Restart from" in r.stdout
+    a = np.loadtxt(job + "-a-16.output.csv", delimiter=",", skiprows=1)
+    b = np.loadtxt(job + "-b-16.output.csv", delimiter=",", skiprows=1)
+    assert np.array_equal(a[:, :3], b[:, :3]) and np.array_equal(a[:, 14], b[:, 14])
+    assert np.array_equal(a[:, 7:13], b[:, 7:13])  # the passive columns carried through
+    for col in list(range(3, 7)) + [13]:
+        assert np.linalg.norm(a[:, col] - b[:, col]) <= 1e-9 * np.linalg.norm(a[:, col]), col
+    assert len([x for x in open(job + "-b.volume") if x.strip()]) == 1
+
+
+@pytest.mark.gpu
+def test_driver_implant_point_cloud(nn, orc, tmp_path):
+    """BunnyConditions = 1 (main.cpp:236-240, 316-325, 422-457): with data1[3] implant points
+    in <job>.bunnyNodes the nodes within 3 * 0.4 dx (1 + 1e-5) of one start solid (Mg2+ 1),
+    the others liquid; the driver's phases equal the oracle's kd-tree restatement."""
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    job = str(tmp_path / "SYN")
+    _write(job, 1, 16, 5, 8)
+    pts = orc.synth_implant_points(16, 5, "sphere")
+    d1 = _load(job + ".data1", int)
+    d1[3] = pts.shape[1]
+    np.savetxt(job + ".data1", d1, fmt="%d")
+    np.savetxt(job + ".bunnyNodes", pts.T, fmt="%.17g")
+    r = subprocess.run([_driver(), "-i", job, "--precision", "fp64", "--every", "8"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Building bunnyNodes took" in r.stdout
+    inp = orc.synth(1, 16, 5)
+    rad = 3 * 0.4 * inp["params"].dx * (1 + 1e-5)
+    mask = (orc.implant_counts(inp["nodes"], pts, rad) > 0).astype(int)
+    out = np.loadtxt(job + "-i-8.output.csv", delimiter=",", skiprows=1)
+    assert np.array_equal(out[:, 14].astype(int), mask)
+    assert mask.sum() > 0 and np.all(out[mask == 1, 3] > 0.9)
