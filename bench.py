@@ -231,7 +231,9 @@ def run_reference(args):
 def adjoint_cost(nn, steps, ck=50, se=20):
     """Cost of one gradient of the mass-loss misfit on the calibration workload (jittered
     64^3 lattice minus an 8-node shell, solid cylinder r=0.25, sigmoid switch of width
-    0.01): forward with checkpoints + backward, against the plain forward of the same steps."""
+    0.01): forward_ckpt + backward against the plain forward of the same steps, with every
+    step's snapshot kept (store 2) and with checkpoints every ck steps plus the solved
+    potentials (store 1: backward recomputes each segment's bond sums, no potential solve)."""
     inp = nn.synth(3, 64, 1)
     base = inp["params"].copy()
     sim = nn.Simulation.from_synth(inp)
@@ -245,37 +247,37 @@ def adjoint_cost(nn, steps, ck=50, se=20):
     target = sim.forward_ckpt(steps, nn.MIXED, ck, se)
     sim.set_params(base)
     sim.reset()
-    t0 = time.perf_counter()
-    curve = sim.forward_ckpt(steps, nn.MIXED, ck, se)
-    t1 = time.perf_counter()
-    gD, gk = sim.backward(2.0 * (curve - target))
-    t2 = time.perf_counter()
-    sim.reset()
     ms_fwd = sim.forward_timed(steps, nn.MIXED)
-    fwd_ckpt, bwd = 1e3 * (t1 - t0), 1e3 * (t2 - t1)
-    # the same gradient with checkpoints every ck steps and recomputation in backward
-    sim.set_adjoint_store(1)
-    sim.reset()
-    t0 = time.perf_counter()
-    curve_r = sim.forward_ckpt(steps, nn.MIXED, ck, se)
-    t1 = time.perf_counter()
-    gD_r, gk_r = sim.backward(2.0 * (curve_r - target))
-    t2 = time.perf_counter()
-    recompute = {"forward_ckpt_ms": 1e3 * (t1 - t0), "backward_ms": 1e3 * (t2 - t1),
-                 "gradient_over_forward": 1e3 * (t2 - t0) / ms_fwd,
-                 "same_gradient_bits": bool(np.array_equal(gD_r, gD) and gk_r == gk)}
-    return {"workload": "jittered 64^3 lattice minus 8-node shell (%d nodes), solid cylinder "
-                        "r=0.25, loss = L2 misfit of the Mg mass-loss curve" % inp["N"],
-            "steps": steps, "ckpt_every": ck, "sample_every": se,
-            "precision": "mixed forward, FP32 sliced adjoint bond sums, mixed adjoint potential solve",
-            "storage": "every step's FP64 snapshot kept (no recomputation) when it fits a quarter "
-                       "of the free device memory, else checkpoints every %d steps" % ck,
-            "forward_ms": ms_fwd, "forward_ckpt_ms": fwd_ckpt, "backward_ms": bwd,
-            "gradient_over_forward": (fwd_ckpt + bwd) / ms_fwd,
-            "backward_over_forward": bwd / ms_fwd,
-            "grad_D": [float(x) for x in gD], "grad_k": float(gk),
-            "loss": float(((curve - target) ** 2).sum()),
-            "checkpoint_recompute": recompute}
+    out = {"workload": "jittered 64^3 lattice minus 8-node shell (%d nodes), solid cylinder "
+                       "r=0.25, loss = L2 misfit of the Mg mass-loss curve" % inp["N"],
+           "steps": steps, "ckpt_every": ck, "sample_every": se,
+           "precision": "mixed forward, FP32 sliced adjoint bond sums, mixed adjoint potential solve",
+           "forward_ms": ms_fwd}
+    grads = {}
+    for mode, key in ((2, "stored_snapshots"), (1, "checkpoint_recompute")):
+        sim.set_adjoint_store(mode)
+        sim.reset()
+        d0 = sim.diagnostics()
+        t0 = time.perf_counter()
+        curve = sim.forward_ckpt(steps, nn.MIXED, ck, se)
+        t1 = time.perf_counter()
+        d1 = sim.diagnostics()
+        gD, gk = sim.backward(2.0 * (curve - target))
+        t2 = time.perf_counter()
+        d2 = sim.diagnostics()
+        grads[key] = (gD, gk)
+        out[key] = {"forward_ckpt_ms": 1e3 * (t1 - t0), "backward_ms": 1e3 * (t2 - t1),
+                    "gradient_over_forward": 1e3 * (t2 - t0) / ms_fwd,
+                    "backward_over_forward": 1e3 * (t2 - t1) / ms_fwd,
+                    "forward_cg_per_step": (d1["cg_iterations_total"] - d0["cg_iterations_total"]) / steps,
+                    "adjoint_cg_per_step": (d2["cg_iterations_total"] - d1["cg_iterations_total"]) / steps}
+        out["loss"] = float(((curve - target) ** 2).sum())
+    a, b = grads["stored_snapshots"], grads["checkpoint_recompute"]
+    out["checkpoint_recompute"]["same_gradient_bits"] = bool(np.array_equal(a[0], b[0]) and a[1] == b[1])
+    out["gradient_over_forward"] = out["checkpoint_recompute"]["gradient_over_forward"]
+    out["grad_D"] = [float(x) for x in b[0]]
+    out["grad_k"] = float(b[1])
+    return out
 
 
 class ProfileRange:
@@ -629,7 +631,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--adjoint-steps", type=int, default=400,
+    ap.add_argument("--adjoint-steps", type=int, default=2000,
                     help="steps of the gradient-cost measurement (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=20,
                     help="steps of the 64-instance ensemble measurement (0: skip)")

@@ -153,4 +153,9 @@ def test_driver_implant_point_cloud(nn, orc, tmp_path):
     mask = (orc.implant_counts(inp["nodes"], pts, rad) > 0).astype(int)
     out = np.loadtxt(job + "-i-8.output.csv", delimiter=",", skiprows=1)
     assert np.array_equal(out[:, 14].astype(int), mask)
-    assert mask.sum() > 0 and np.all(out[mask == 1, 3] > 0.9)
+    # solid nodes start at Mg2+ 1 and lose a few percent in 8 steps; the implant reaches into
+    # the Dirichlet shell, whose nodes hold their boundary value (main.cpp:676-712)
+    dirichlet = (inp["bctypes"] == 0) & (inp["bcvalues"][0] != -1)
+    inner = (mask == 1) & ~dirichlet
+    assert inner.sum() > 0 and np.all(out[inner, 3] > 0.9)
+    assert np.all(out[(mask == 1) & dirichlet, 3] == inp["bcvalues"][0][(mask == 1) & dirichlet])
