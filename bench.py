@@ -264,13 +264,14 @@ def adjoint_cost(nn, steps, ck=50, se=20):
         d1 = sim.diagnostics()
         gD, gk = sim.backward(2.0 * (curve - target))
         t2 = time.perf_counter()
-        d2 = sim.diagnostics()
         grads[key] = (gD, gk)
+        adj = sim.adjoint_stats()
         out[key] = {"forward_ckpt_ms": 1e3 * (t1 - t0), "backward_ms": 1e3 * (t2 - t1),
                     "gradient_over_forward": 1e3 * (t2 - t0) / ms_fwd,
                     "backward_over_forward": 1e3 * (t2 - t1) / ms_fwd,
                     "forward_cg_per_step": (d1["cg_iterations_total"] - d0["cg_iterations_total"]) / steps,
-                    "adjoint_cg_per_step": (d2["cg_iterations_total"] - d1["cg_iterations_total"]) / steps}
+                    "adjoint_cg_per_solve": adj["cg_iterations"] / max(adj["solves"], 1),
+                    "adjoint_sweeps_per_solve": adj["sweeps"] / max(adj["solves"], 1)}
         out["loss"] = float(((curve - target) ** 2).sum())
     a, b = grads["stored_snapshots"], grads["checkpoint_recompute"]
     out["checkpoint_recompute"]["same_gradient_bits"] = bool(np.array_equal(a[0], b[0]) and a[1] == b[1])

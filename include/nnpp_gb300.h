@@ -392,6 +392,18 @@ nnpp_status nnpp_set_adjoint_store(nnpp_handle* h, int mode);
 nnpp_status nnpp_backward(nnpp_handle* h, const double* dL_dmass, double* grad_D,
                           double* grad_k);
 
+/* Relative tolerance of backward's adjoint potential solves (no counterpart in the
+ * reference, which has no adjoint); 0 (default): the forward's tolerance (nnpp_set_solver).
+ * The recomputed forward steps always use the forward's tolerance. */
+nnpp_status nnpp_set_adjoint_solver(nnpp_handle* h, double tol);
+
+/* The last nnpp_backward's adjoint potential solves: their inner CG iterations, count and
+ * refinement sweeps (any pointer may be NULL; the handle's diagnostics are those of the
+ * forward run), and, when iterations_per_step is not NULL, each step's inner iterations
+ * (n_steps of the recorded run, indexed by step). */
+nnpp_status nnpp_get_adjoint_stats(nnpp_handle* h, int64_t* cg_iterations, int64_t* solves,
+                                   int64_t* sweeps, int* iterations_per_step);
+
 /* ---- ensembles -------------------------------------------------------------------------- */
 
 typedef struct nnpp_ensemble nnpp_ensemble;

@@ -114,6 +114,9 @@ _SIGS = {
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
+    "nnpp_set_adjoint_solver": (C.c_int, [_P, C.c_double]),
+    "nnpp_get_adjoint_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int64), _IP]),
     "nnpp_set_checks": (C.c_int, [_P, C.c_int]),
     "nnpp_forward_implicit": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "nnpp_get_coarse_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
@@ -390,6 +393,7 @@ class Simulation:
         curve = np.empty(n_steps // sample_every, dtype=np.float64)
         _check(lib().nnpp_forward_ckpt(self._h, n_steps, precision, ckpt_every, sample_every,
                                        _dp(curve)))
+        self._fwd_steps = int(n_steps)
         return curve
 
     def set_adjoint_store(self, mode):
@@ -397,6 +401,22 @@ class Simulation:
         solved potential (backward recomputes the segments' bond sums only), 2 every step's
         snapshot, 3 checkpoints only (backward recomputes whole steps)."""
         _check(lib().nnpp_set_adjoint_store(self._h, mode))
+
+    def set_adjoint_solver(self, tol):
+        """Relative tolerance of the adjoint potential solves (0: the forward's)."""
+        _check(lib().nnpp_set_adjoint_solver(self._h, float(tol)))
+
+    def adjoint_stats(self, per_step=False):
+        """{"cg_iterations", "solves", "sweeps"} of the last backward's adjoint potential
+        solves, plus "per_step" (each step's inner iterations, int32) if per_step."""
+        it, n, sw = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        log = np.zeros(getattr(self, "_fwd_steps", 0) if per_step else 0, dtype=np.int32)
+        _check(lib().nnpp_get_adjoint_stats(self._h, C.byref(it), C.byref(n), C.byref(sw),
+                                            _ip(log) if per_step else None))
+        out = {"cg_iterations": it.value, "solves": n.value, "sweeps": sw.value}
+        if per_step:
+            out["per_step"] = log
+        return out
 
     def backward(self, dL_dcurve):
         """Backward half: dL/dD_liquid (4,) and dL/dk_diss for dL/d(curve)."""

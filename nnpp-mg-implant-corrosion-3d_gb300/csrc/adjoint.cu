@@ -77,6 +77,9 @@ nnpp_status load_ckpt(Handle& h, const Handle::Ckpt& c) {
   return NNPP_OK;
 }
 
+// the inner iterations of the solve that just ended (one thread)
+__global__ void k_adj_log(const DevState* ds, int* out) { *out = ds->solve_iters; }
+
 nnpp_status read_ds(Handle& h, DevState* ds) {
   NNPP_CUDA(cudaMemcpyAsync(ds, h.dstate.get(), sizeof(DevState), cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
@@ -111,7 +114,10 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
   }
   struct RecordOff {
     Handle& h;
-    ~RecordOff() { h.coarse_record = false; }
+    ~RecordOff() {
+      h.coarse_record = false;
+      h.phi_keep[0] = h.phi_keep[1] = nullptr;
+    }
   } record_off{h};
   h.fwd_steps = n_steps;
   h.ck_every = ckpt_every;
@@ -178,12 +184,15 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
       NNPP_TRY(launch_snap_state(h, h.snap_all.get() + (size_t)(s + 1) * N));
       next = s + 1;
     } else if (store_phi) {
-      // one step at a time: its solved potential (phi_prev after the step) is kept
+      // up to two steps per graph launch, one per record parity: each step's transport also
+      // writes the potential its solve left into phi_all (stops at checkpoints and samples)
       if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
-      NNPP_TRY(engine_run(*h.engine, 1, precision));
-      NNPP_CUDA(cudaMemcpyAsync(h.phi_all.get() + (size_t)s * N, h.phi_prev.get(), sizeof(double) * N,
-                                cudaMemcpyDeviceToDevice, h.st));
-      next = s + 1;
+      next = std::min(n_steps, s + 2);
+      next = std::min(next, (s / ckpt_every + 1) * ckpt_every);
+      next = std::min(next, (s / sample_every + 1) * sample_every);
+      h.phi_keep[h.cur & 1] = h.phi_all.get() + (size_t)s * N;
+      h.phi_keep[(h.cur ^ 1) & 1] = next - s > 1 ? h.phi_all.get() + (size_t)(s + 1) * N : nullptr;
+      NNPP_TRY(engine_run(*h.engine, next - s, precision));
     } else {
       if (s % ckpt_every == 0) NNPP_TRY(save_ckpt(h, h.ckpts[s / ckpt_every]));
       next = std::min(n_steps, (s / ckpt_every + 1) * ckpt_every);
@@ -199,12 +208,41 @@ nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int c
       h.curve[s / sample_every - 1] = dV * (m0 - ds.mg_mass_now);
     }
   }
+  h.phi_keep[0] = h.phi_keep[1] = nullptr;
+  NNPP_TRY(engine_params(*h.engine));
   NNPP_TRY(save_ckpt(h, h.fwd_end));
   h.snap_all_valid = store_all;
   h.phi_all_valid = store_phi;
   h.fwd_nstep_end = h.nstep;
   h.coarse_event_cur = (int)h.coarse_events.size() - 1;
   std::copy(h.curve.begin(), h.curve.end(), mass_curve);
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_get_adjoint_stats(nnpp_handle* hp, int64_t* cg_iterations, int64_t* solves,
+                                   int64_t* sweeps, int* iterations_per_step) {
+  clear_error();
+  if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
+  Handle& h = hp->h;
+  if (cg_iterations) *cg_iterations = h.adj_cg_iters;
+  if (solves) *solves = h.adj_solves;
+  if (sweeps) *sweeps = h.adj_sweeps;
+  if (iterations_per_step) {
+    if (h.fwd_steps < 1 || h.adj_log.size() < (size_t)h.fwd_steps)
+      return set_error(NNPP_ERR_STATE, "adjoint stats: no backward run");
+    NNPP_CUDA(cudaSetDevice(h.device));
+    NNPP_CUDA(cudaMemcpyAsync(iterations_per_step, h.adj_log.get(), sizeof(int) * h.fwd_steps,
+                              cudaMemcpyDeviceToHost, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+  }
+  return NNPP_OK;
+}
+
+nnpp_status nnpp_set_adjoint_solver(nnpp_handle* hp, double tol) {
+  clear_error();
+  if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
+  if (!(tol >= 0.0) || !(tol < 1.0)) return set_error(NNPP_ERR_INVALID, "adjoint tolerance must be in [0, 1)");
+  hp->h.adj_tol = tol;
   return NNPP_OK;
 }
 
@@ -253,6 +291,11 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
   if ((!all && !snap.alloc((size_t)(ck + 1) * N)) || !lam.alloc(S * N) || !mu.alloc(S * N) || !nu.alloc(N) ||
       !psi.alloc(N) || !acc.alloc(8))
     return set_error(NNPP_ERR_NOMEM, "adjoint buffers");
+  if (h.adj_log.size() < (size_t)n_steps) {
+    h.adj_log.reset();
+    if (!h.adj_log.alloc(n_steps)) return set_error(NNPP_ERR_NOMEM, "adjoint iteration log");
+  }
+  NNPP_CUDA(cudaMemsetAsync(h.adj_log.get(), 0, sizeof(int) * n_steps, h.st));
   if (!all) NNPP_CUDA(cudaMemsetAsync(snap.get(), 0, sizeof(Rec64) * (size_t)(ck + 1) * N, h.st));
   NNPP_CUDA(cudaMemsetAsync(lam.get(), 0, sizeof(double) * S * N, h.st));
   NNPP_CUDA(cudaMemsetAsync(psi.get(), 0, sizeof(double) * N, h.st));
@@ -279,6 +322,27 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       h.nstep = h.fwd_nstep_end;
     }
   } replay_off{h};
+  // the adjoint solves run to adj_tol (when set), the recomputed forward steps to tol
+  const double fwd_tol = h.tol, adj_tol = h.adj_tol > 0.0 ? h.adj_tol : h.tol;
+  struct TolBack {
+    Handle& h;
+    double tol;
+    ~TolBack() {
+      if (h.tol != tol) {
+        h.tol = tol;
+        h.settings_pushed = false;
+      }
+    }
+  } tol_back{h, fwd_tol};
+  auto use_tol = [&](double t) {
+    if (h.tol != t) {
+      h.tol = t;
+      h.settings_pushed = false;
+    }
+  };
+  h.adj_cg_iters = 0;
+  h.adj_solves = 0;
+  h.adj_sweeps = 0;
   // with every step's snapshot one segment covers the run and nothing is recomputed
   const int nseg = all ? 1 : (int)h.ckpts.size();
   const int seg_len = all ? n_steps : ck;
@@ -286,6 +350,7 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
     const int s0 = g * seg_len, s1 = std::min(n_steps, s0 + seg_len);
     const Rec64* base = all ? h.snap_all.get() : snap.get();
     if (!all) {
+      use_tol(fwd_tol);
       NNPP_TRY(load_ckpt(h, h.ckpts[g]));
       NNPP_TRY(launch_snap_state(h, snap.get()));
       for (int n = s0; n < s1; ++n) {
@@ -304,6 +369,11 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
         NNPP_TRY(launch_snap_state(h, snap.get() + (size_t)(n - s0 + 1) * N));
       }
     }
+    // the adjoint solves' inner iterations of this segment (the device counters come back
+    // with each checkpoint)
+    use_tol(adj_tol);
+    DevState dseg;
+    NNPP_TRY(read_ds(h, &dseg));
     for (int n = s1 - 1; n >= s0; --n) {
       const Rec64* sn = base + (size_t)(n - s0) * N;
       const Rec64* sn1 = base + (size_t)(n - s0 + 1) * N;
@@ -325,6 +395,10 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
         NNPP_CUDA(cudaMemcpyAsync(&h.dstate.get()->hist_n, hs, sizeof(hs), cudaMemcpyHostToDevice, h.st));
       }
       st = engine_solve(e, prec);
+      if (st == NNPP_OK) {
+        k_adj_log<<<1, 1, 0, h.st>>>(h.dstate.get(), h.adj_log.get() + n);
+        if (cudaGetLastError() != cudaSuccess) st = set_error(NNPP_ERR_CUDA, "adjoint iteration log");
+      }
       if (st == NNPP_OK && hm >= 3) {
         ahead = (ahead + 1) % hm;
         an = an < hm ? an + 1 : hm;
@@ -337,10 +411,17 @@ nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_
       const double inject = (n > 0 && n % se == 0) ? -dV * dL_dmass[n / se - 1] : 0.0;
       NNPP_TRY(launch_adj_combine(h, mu.get(), lam.get(), inject));
     }
+    if (st != NNPP_OK) break;
+    DevState dend;
+    NNPP_TRY(read_ds(h, &dend));
+    h.adj_cg_iters += dend.cg_iters - dseg.cg_iters;
+    h.adj_solves += dend.cg_solves - dseg.cg_solves;
+    h.adj_sweeps += dend.outer_total - dseg.outer_total;
   }
   double g5[8];
   NNPP_CUDA(cudaMemcpyAsync(g5, acc.get(), sizeof(double) * 8, cudaMemcpyDeviceToHost, h.st));
   NNPP_CUDA(cudaStreamSynchronize(h.st));
+  use_tol(fwd_tol);
   nnpp_status st2 = load_ckpt(h, h.fwd_end);
   if (st != NNPP_OK) return st;
   for (int k = 0; k < S; ++k) grad_D[k] = g5[k];

@@ -7,7 +7,9 @@
 // as dense n x n FP32 matrices (n <= kCoarseMax).  The inverse comes from the Newton-Schulz
 // iteration X <- X (2I - A_c X), X_0 = I / ||A_c||_inf (every iterate is a positive
 // polynomial of A_c, so the preconditioner stays symmetric positive definite even when the
-// iteration is stopped early), on cuBLAS SGEMM.  A periodic rebuild within a run starts
+// iteration is stopped early).  Its GEMMs are FP32 products that cuBLAS runs on the BF16
+// tensor cores by the BF16x9 split (each FP32 operand as three BF16 parts, nine partial
+// products accumulated in FP32: FP32 accuracy, not TF32's).  A periodic rebuild within a run starts
 // instead from the previous inverse when ||I - A_c X_0||_F < 1/2: the error then squares
 // every step, and a few steps replace the 18 of the cold start.  The coarse operator is
 // rebuilt when the state is replaced, and every `coarse_every` steps (counted from the last
@@ -31,6 +33,15 @@ constexpr int kNsIterations = 18;
 constexpr int kNormBlocks = 128;      // block partials of the warm start's residual norm
 constexpr double kNsWarmMax = 0.5;    // warm start when ||I - A_c X_0||_F is below this
 constexpr double kNsTarget = 1e-8;    // warm start: steps until the bound ||.||^(2^m) meets this
+
+// C = A B for n x n column-major FP32 matrices, emulated FP32 on the BF16 tensor cores (the
+// handle's emulation strategy is EAGER, so cuBLAS takes the emulated kernels wherever they
+// exist and its FP32 kernels elsewhere)
+cublasStatus_t ns_gemm(cublasHandle_t hb, int n, const float* a, const float* b, float* c) {
+  const float one = 1.0f, zero = 0.0f;
+  return cublasGemmEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, a, CUDA_R_32F, n, b, CUDA_R_32F, n, &zero, c,
+                      CUDA_R_32F, n, CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT);
+}
 
 // block partials of ||I - T||_F^2 (T n x n): FP32 sums per thread, FP64 across the block
 __global__ void k_resid_sq(int n, const float* T, double* partials) {
@@ -274,6 +285,8 @@ nnpp_status coarse_build(Handle& h) {
     cublasHandle_t hb = nullptr;
     if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasCreate");
     c.cublas = hb;
+    if (cublasSetEmulationStrategy(hb, CUBLAS_EMULATION_STRATEGY_EAGER) != CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "cublasSetEmulationStrategy");
   }
   c.stale = true;
   return NNPP_OK;
@@ -300,7 +313,6 @@ nnpp_status coarse_refresh(Handle& h) {
   const int eg = (int)std::min<size_t>((nn + 255) / 256, 152 * 64);
   cublasHandle_t hb = static_cast<cublasHandle_t>(c.cublas);
   if (cublasSetStream(hb, h.st) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "cublasSetStream");
-  const float one = 1.0f, zero = 0.0f;
   float* x = X.get();
   float* y = c.y.get();
   // a rebuild within a run (phases changed since the last one, the state not replaced)
@@ -313,9 +325,8 @@ nnpp_status coarse_refresh(Handle& h) {
     if (!c.nrm.alloc(kNormBlocks)) return set_error(NNPP_ERR_NOMEM, "coarse inverse");
     NNPP_CUDA(cudaMemcpy2DAsync(x, sizeof(float) * n, c.inv.get(), sizeof(float) * c.ld, sizeof(float) * n, n,
                                 cudaMemcpyDeviceToDevice, h.st));
-    if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
-        CUBLAS_STATUS_SUCCESS)
-      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    if (ns_gemm(hb, n, A.get(), x, T.get()) != CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "coarse inverse: GEMM");
     k_resid_sq<<<kNormBlocks, 256, 0, h.st>>>(n, T.get(), c.nrm.get());
     NNPP_CUDA(cudaGetLastError());
     std::vector<double> part(kNormBlocks);
@@ -336,15 +347,11 @@ nnpp_status coarse_refresh(Handle& h) {
   }
   for (int it = 0; it < steps; ++it) {
     // T = A X ; T = 2I - T ; X <- X T
-    if (!(warm && it == 0) &&
-        cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A.get(), n, x, n, &zero, T.get(), n) !=
-            CUBLAS_STATUS_SUCCESS)
-      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    if (!(warm && it == 0) && ns_gemm(hb, n, A.get(), x, T.get()) != CUBLAS_STATUS_SUCCESS)
+      return set_error(NNPP_ERR_CUDA, "coarse inverse: GEMM");
     k_two_i_minus<<<eg, 256, 0, h.st>>>(n, T.get());
     NNPP_CUDA(cudaGetLastError());
-    if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, x, n, T.get(), n, &zero, y, n) !=
-        CUBLAS_STATUS_SUCCESS)
-      return set_error(NNPP_ERR_CUDA, "coarse inverse: SGEMM");
+    if (ns_gemm(hb, n, x, T.get(), y) != CUBLAS_STATUS_SUCCESS) return set_error(NNPP_ERR_CUDA, "coarse inverse: GEMM");
     std::swap(x, y);
   }
   // x holds the last iterate; its symmetrised copy goes to c.inv (rows of stride ld)

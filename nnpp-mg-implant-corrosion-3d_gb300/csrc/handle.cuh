@@ -47,6 +47,8 @@ struct KParams {
   Rec64* rec64_nxt;
   double* phi64;                 // potential (FP64, both precisions)
   double* phi_prev;              // potential of the previous step (linear extrapolation)
+  double* phi_keep;              // non-null: the transport also writes the step's solved
+                                 // potential here (forward_ckpt's per-step potentials)
   int* flip_step;
   // potential solve
   double* b64;
@@ -240,6 +242,12 @@ struct Handle {
   // recomputes a segment's steps without their potential solves
   DBuf<double> phi_all;
   bool phi_all_valid = false;
+  double* phi_keep[2] = {nullptr, nullptr};  // KParams.phi_keep of each record parity
+  // the last backward's adjoint potential solves: inner iterations, solves, refinement
+  // sweeps, and the inner iterations of each step's solve (fwd_steps entries)
+  long long adj_cg_iters = 0, adj_solves = 0, adj_sweeps = 0;
+  DBuf<int> adj_log;
+  double adj_tol = 0.0;         // relative tolerance of the adjoint solves (0: tol)
   int fwd_steps = 0, ck_every = 0, sample_every = 0, fwd_prec = NNPP_FP64;
   std::vector<double> curve;
   ~Handle();

@@ -2676,6 +2676,7 @@ __device__ __forceinline__ void record_history(const KParams& k, int a, int hslo
 // phi^n); the returned value also goes into the next record so that both agree.
 __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
   const double ph = k.phi64[a];
+  if (k.phi_keep) k.phi_keep[a] = ph;  // the step's solved potential (forward_ckpt)
   if (!k.extrapolate || !k.freem[a]) {
     k.phi_prev[a] = ph;
     return ph;
@@ -4048,6 +4049,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.rec64_nxt = h.rec64[cur ^ 1].get();
   k.phi64 = h.phi64.get();
   k.phi_prev = h.phi_prev.get();
+  k.phi_keep = h.phi_keep[cur & 1];
   k.flip_step = h.flip_step.get();
   k.b64 = h.b64.get();
   k.r64 = h.r64.get();
