@@ -393,8 +393,11 @@ nnpp_status nnpp_backward(nnpp_handle* h, const double* dL_dmass, double* grad_D
                           double* grad_k);
 
 /* Relative tolerance of backward's adjoint potential solves (no counterpart in the
- * reference, which has no adjoint); 0 (default): the forward's tolerance (nnpp_set_solver).
- * The recomputed forward steps always use the forward's tolerance. */
+ * reference, which has no adjoint).  0 (default): a mixed-precision run solves to
+ * max(tol, 1e-8) and an FP64 run to tol, tol being the forward's (nnpp_set_solver); the
+ * mixed gradient's own error (FP32 adjoint bond sums, ~5e-7 relative on the calibration
+ * workload) is far above what a 1e-8 adjoint solve adds (~2e-12).  The recomputed forward
+ * steps always use the forward's tolerance. */
 nnpp_status nnpp_set_adjoint_solver(nnpp_handle* h, double tol);
 
 /* The last nnpp_backward's adjoint potential solves: their inner CG iterations, count and

@@ -403,7 +403,8 @@ class Simulation:
         _check(lib().nnpp_set_adjoint_store(self._h, mode))
 
     def set_adjoint_solver(self, tol):
-        """Relative tolerance of the adjoint potential solves (0: the forward's)."""
+        """Relative tolerance of the adjoint potential solves (0, the default: max(tol, 1e-8)
+        for mixed runs, tol for FP64 runs, tol being the forward's)."""
         _check(lib().nnpp_set_adjoint_solver(self._h, float(tol)))
 
     def adjoint_stats(self, per_step=False):

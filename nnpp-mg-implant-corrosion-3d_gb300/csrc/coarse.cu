@@ -133,10 +133,11 @@ __global__ void k_coarse_assemble(KParams k, const int* bin_start, int nb0, int 
       ra += fabsf(x);
     }
     if (lane == 0) {
-      // no unknown in the aggregate: an identity row keeps A_c regular
+      // no unknown in the aggregate: an identity row keeps A_c regular (rowabs -1 marks it:
+      // the inverse's diagonal entry there is zeroed after the iteration)
       if (unknowns == 0) {
         mat[(size_t)I * n + I] = 1.0f;
-        ra = 1.0f;
+        ra = -1.0f;
       } else {
         for (int q = 0; q < 27; ++q) {
           const int jx = ax + q % 3 - 1, jy = ay + (q / 3) % 3 - 1, jz = az + q / 9 - 1;
@@ -204,7 +205,7 @@ __global__ void k_ns_init(int n, const float* rowabs, float* X) {
   __shared__ float smax;
   if (threadIdx.x == 0) {
     float m = 0.0f;
-    for (int i = 0; i < n; ++i) m = fmaxf(m, rowabs[i]);
+    for (int i = 0; i < n; ++i) m = fmaxf(m, fabsf(rowabs[i]));  // identity rows count 1
     smax = m > 0.0f ? m : 1.0f;
   }
   __syncthreads();
@@ -219,11 +220,15 @@ __global__ void k_two_i_minus(int n, float* T) {
     T[e] = ((e / n == e % n) ? 2.0f : 0.0f) - T[e];
 }
 
-// Y = (X + X^T) / 2, Y with rows of stride ld
-__global__ void k_symmetrize(int n, int ld, const float* X, float* Y) {
+// Y = (X + X^T) / 2, Y with rows of stride ld; the diagonal entry of an aggregate that held
+// no unknown (rowabs < 0) is zero.  Its row and column of X are those of the identity; once
+// a front reaches the aggregate, a coarse inverse that has not been rebuilt yet would scale
+// the aggregate's residual sum by 1 instead of by the inverse of its new diagonal, so the
+// stale additive correction leaves such aggregates to the diagonal part.
+__global__ void k_symmetrize(int n, int ld, const float* X, const float* rowabs, float* Y) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x) {
     const size_t i = e / n, j = e % n;
-    Y[i * ld + j] = 0.5f * (X[e] + X[j * n + i]);
+    Y[i * ld + j] = (i == j && rowabs[i] < 0.0f) ? 0.0f : 0.5f * (X[e] + X[j * n + i]);
   }
 }
 
@@ -355,7 +360,7 @@ nnpp_status coarse_refresh(Handle& h) {
     std::swap(x, y);
   }
   // x holds the last iterate; its symmetrised copy goes to c.inv (rows of stride ld)
-  k_symmetrize<<<eg, 256, 0, h.st>>>(n, c.ld, x, c.inv.get());
+  k_symmetrize<<<eg, 256, 0, h.st>>>(n, c.ld, x, c.rowabs.get(), c.inv.get());
   NNPP_CUDA(cudaGetLastError());
   if (!c.snap.alloc(h.N) || !c.count.alloc(1)) return set_error(NNPP_ERR_NOMEM, "coarse phase snapshot");
   // A P for the deflated CG (the same phases as A_c)

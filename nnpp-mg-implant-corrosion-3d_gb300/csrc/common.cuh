@@ -69,6 +69,8 @@ struct DevState {
   int nonfinite;
   int wait_timeout;   // a bounded device wait gave up (the step's results are invalid)
   int bounds_error;   // a device index check (nnpp_set_checks) found an index out of range
+  int nflip;          // nodes the last transport turned liquid (listed in flip_list; reset
+                      // by the next-guess pass that follows the transport)
   // potential solve
   double bnorm2;      // ||b_eff||^2
   double rnorm2;      // ||r||^2 of the outer (FP64) residual

@@ -105,7 +105,7 @@ nnpp_status build_lists(Engine& e, int T) {
   const int stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
   if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
       !e.d_slices.alloc(std::max<size_t>(slices.size(), 1)) || !e.d_htiles.alloc(std::max<size_t>(htiles.size(), 1)) ||
-      !e.d_ticket.alloc(M + 3) ||
+      !e.d_ticket.alloc(M + 4) ||
       !e.d_partials.alloc((size_t)kReduceSlots * stride) ||
       !e.d_inst[0].alloc(M) || !e.d_inst[1].alloc(M))
     return set_error(NNPP_ERR_NOMEM, "engine work lists");
@@ -116,7 +116,7 @@ nnpp_status build_lists(Engine& e, int T) {
     NNPP_CUDA(cudaMemcpyAsync(e.d_slices.get(), slices.data(), sizeof(SliceDesc) * slices.size(), cudaMemcpyHostToDevice, e.st));
   if (!htiles.empty())
     NNPP_CUDA(cudaMemcpyAsync(e.d_htiles.get(), htiles.data(), sizeof(HTile) * htiles.size(), cudaMemcpyHostToDevice, e.st));
-  NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, sizeof(unsigned int) * (M + 3), e.st));
+  NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, e.d_ticket.bytes(), e.st));
   NNPP_CUDA(cudaStreamSynchronize(e.st));
   engine_destroy_graphs(e);
   return NNPP_OK;

@@ -86,7 +86,7 @@ struct EngineView {
   const int* slice_first;
   const int* slice_count;
   unsigned int* ticket;     // per instance completion counters, + [M] global, + [M+1] grid,
-                            // + [M+2] slice claims
+                            // + [M+2] slice claims, + [M+3] the next-guess pass
   double* partials;         // kReduceSlots * stride
   int ntiles, nchunks, M, in_graph;
   int nslices;

@@ -34,6 +34,10 @@ struct KParams {
   // 16-bit slot codes (window row << 12 | offset)
   const float* sell;
   const float* sell_lo;          // sliced like sell's weights: wlo32 (32 floats per column)
+  float* sell_cg;                // sliced like sell: each row's bonds to columns that can be
+                                 // unknowns of the potential solve (liquid, no potential
+                                 // Dirichlet value), compacted to the front, zero padding
+  int* cg_width;                 // per slice of the handle: the columns of sell_cg in use
   float4* phi4;                  // per node {phi_hi, phi_lo} (zero on solid nodes), liquid, Dirichlet
   const double* w64;
   const float* w32;
@@ -50,6 +54,7 @@ struct KParams {
   double* phi_keep;              // non-null: the transport also writes the step's solved
                                  // potential here (forward_ckpt's per-step potentials)
   int* flip_step;
+  int* flip_list;                // nodes this step's transport turned liquid (N capacity)
   // potential solve
   double* b64;
   double* r64;
@@ -160,6 +165,8 @@ struct Handle {
   DBuf<unsigned short> slot16;
   DBuf<float> sell;
   DBuf<float> sell_lo;
+  DBuf<float> sell_cg;          // the CG operator's compacted copy of sell (see KParams)
+  DBuf<int> cg_width;
   DBuf<float4> phi4;
   DBuf<float4> posrec;
   float h32 = 0.f;
@@ -183,6 +190,7 @@ struct Handle {
   DBuf<double> b64, r64, dsum64, cpl64, dinv64, rin64, z64, p64, q64, e64;
   DBuf<float> d32, dinv32, rin32, z32, p32, q32, e32, r0_32, t32;
   DBuf<unsigned char> freem;
+  DBuf<int> flip_list;          // N: the nodes the last transport turned liquid
   DBuf<DevState> dstate;
   DBuf<double> scratch_d;       // small device scratch (voln1rel override, ...)
   DBuf<double> user_stage;      // (S+1)*N FP64 staging for host transfers

@@ -630,6 +630,14 @@ __device__ __forceinline__ const unsigned short* sell_code(const KParams& k, con
   return reinterpret_cast<const unsigned short*>(sell_w(k, d) + 32);
 }
 
+// the CG operator's compacted copy (same layout and offsets; columns in use: cg_width)
+__device__ __forceinline__ const float* sell_cg_w(const KParams& k, const SliceDesc& d) {
+  return k.sell_cg + (size_t)(d.off >> 5) * kSellW;
+}
+__device__ __forceinline__ const unsigned short* sell_cg_code(const KParams& k, const SliceDesc& d) {
+  return reinterpret_cast<const unsigned short*>(sell_cg_w(k, d) + 32);
+}
+
 // the inner-loop flag of a slice's instance (constant while the operator runs)
 __device__ __forceinline__ bool slice_active(const EngineView& v, int sg) {
   return __ldg(&v.inst[__ldg(&v.slices[sg].inst)].ds->inner_active) != 0;
@@ -693,8 +701,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   if (PF > 0 && s0 < s1) {
     const SliceDesc& da = v.slices[s0];
     const SliceDesc& db = v.slices[s1 - 1];
-    pf_next = reinterpret_cast<const char*>(sell_w(v.inst[da.inst], da));
-    pf_end = reinterpret_cast<const char*>(sell_w(v.inst[db.inst], db)) + (size_t)db.width * kSellW * 4;
+    pf_next = reinterpret_cast<const char*>(sell_cg_w(v.inst[da.inst], da));
+    pf_end = reinterpret_cast<const char*>(sell_cg_w(v.inst[db.inst], db)) + (size_t)db.width * kSellW * 4;
     if (da.inst != db.inst) pf_end = pf_next;  // the range spans instances: no prefetch
     if (lane == 0) {
       const char* stop = pf_next + (size_t)PF * B * kSellW * 4;
@@ -729,7 +737,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
       const bool live = lane < d.nrows && k.freem[a];
       if (PF > 0 && lane == 0) {
         // keep the prefetches at least PF batches ahead of this slice's first column
-        const char* target = reinterpret_cast<const char*>(sell_w(k, d)) + (size_t)PF * B * kSellW * 4;
+        const char* target = reinterpret_cast<const char*>(sell_cg_w(k, d)) + (size_t)PF * B * kSellW * 4;
         if (target > pf_end) target = pf_end;
         for (; pf_next < target; pf_next += B * kSellW * 4)
           bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
@@ -738,13 +746,15 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
       // hold code 0, weight 0), so that lane 0 can issue the prefetches
       if (PF > 0 ? __any_sync(0xffffffffu, live) : live) {
         const int* hb = s_hb[warp];
-        const float* ws = sell_w(k, d) + lane;
-        const unsigned short* cs = sell_code(k, d) + lane;
+        // the compacted copy: only bonds to columns that can hold a nonzero z
+        const float* ws = sell_cg_w(k, d) + lane;
+        const unsigned short* cs = sell_cg_code(k, d) + lane;
+        const int width = k.cg_width[sg - v.slice_first[d.inst]];
         const float* z = k.z32;
         // B columns per batch; PIPE: the next batch of streamed columns is in flight while
         // the current batch's neighbour values are gathered (more registers, fewer warps)
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        const int nb = d.width / B;
+        const int nb = width / B;
         float w[B];
         unsigned int code[B];
         if (PIPE && nb > 0) {
@@ -783,7 +793,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
 #pragma unroll
           for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
-        for (int c = nb * B; c < d.width; ++c) {
+        for (int c = nb * B; c < width; ++c) {
           const unsigned int cc = ld_stream(cs + kSellC * c);
           acc[0] = fmaf(ld_stream(ws + kSellW * c), WIN ? zw[cc & 4095u] : __ldg(z + code_node(hb, cc)), acc[0]);
         }
@@ -2409,6 +2419,11 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
     const float* ws = sell_w(k, d) + lane;
     const float* wls = sell_lo_col(k, d) + lane;
     const unsigned short* cs = sell_code(k, d) + lane;
+    // with the mask sums the row's bonds to possible unknowns (liquid columns without a
+    // potential Dirichlet value) go, in bond order, to the CG operator's compacted copy
+    float* wcg = k.sell_cg + (size_t)(d.off >> 5) * kSellW + lane;
+    unsigned short* ccg = reinterpret_cast<unsigned short*>(k.sell_cg + (size_t)(d.off >> 5) * kSellW + 32) + lane;
+    int ncg = 0;
     float dh = 0.f, dl = 0.f, sh = 0.f, sl = 0.f, ch = 0.f, cl = 0.f;
     int anyll = 0;
     if (__any_sync(0xffffffffu, scan)) {
@@ -2449,10 +2464,25 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
               pair_add(dh, dl, w[u], wl[u]);
               pair_add(sh, sl, ph, pl);
               anyll = 1;
-              if (f[u].w != 0.0f) pair_add(ch, cl, ph, pl);
+              if (f[u].w != 0.0f) {
+                pair_add(ch, cl, ph, pl);
+              } else if (scan) {
+                wcg[(size_t)kSellW * ncg] = w[u];
+                ccg[(size_t)kSellC * ncg] = (unsigned short)code[u];
+                ++ncg;
+              }
             }
         }
       }
+    }
+    if (!cached) {
+      // zero padding of the shorter rows up to the slice's compacted width
+      const int wcgmax = __reduce_max_sync(0xffffffffu, ncg);
+      for (int c = ncg; c < wcgmax; ++c) {
+        wcg[(size_t)kSellW * c] = 0.0f;
+        ccg[(size_t)kSellC * c] = 0;
+      }
+      if (lane == 0) k.cg_width[sg - v.slice_first[d.inst]] = wcgmax;
     }
     float b2h = 0.0f, b2l = 0.0f, r2h = 0.0f, r2l = 0.0f;  // b.b and r.r as FP32 pairs
     if (rowok) {
@@ -2673,11 +2703,12 @@ __device__ __forceinline__ void record_history(const KParams& k, int a, int hslo
 }
 
 // Warm start of the next solve: phi = 2 phi^n - phi^{n-1} on the unknowns (phi_prev keeps
-// phi^n); the returned value also goes into the next record so that both agree.
+// phi^n); the returned value also goes into the next record so that both agree.  A node the
+// previous transport turned liquid (its phi^{n-1} is the solid's) is not extrapolated.
 __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
   const double ph = k.phi64[a];
   if (k.phi_keep) k.phi_keep[a] = ph;  // the step's solved potential (forward_ckpt)
-  if (!k.extrapolate || !k.freem[a]) {
+  if (!k.extrapolate || !k.freem[a] || k.flip_step[a] == (int)k.ds->steps) {
     k.phi_prev[a] = ph;
     return ph;
   }
@@ -2828,6 +2859,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
         if (pa != 0.0f && (double)hi[0] + (double)lo[0] <= k.csat) {
           pnew = 0.0f;
           k.flip_step[a] = (int)(k.ds->steps + 1);
+          k.flip_list[atomicAdd(&k.ds->nflip, 1)] = a;
           k.ds->op_valid = 0;
           k.ds->defl = 0;
         }
@@ -2893,6 +2925,56 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
       v.ticket[v.M + 1] = 0;
       v.ticket[v.M + 2] = 0;
     }
+  }
+}
+
+// Next-solve guess of the nodes a transport turned liquid.  As solids they carried no
+// potential (zero); a potential solve started from that zero spends its first refinement
+// sweeps on those few nodes.  Each listed node instead takes the w-weighted mean of the
+// potentials that its liquid neighbours carry into the next solve, counting only neighbours
+// that were liquid before this step (so every value read is one this pass does not write, and
+// the result does not depend on the list's order), and the same value in every slot of the
+// warm-start history, where the backward differences then vanish.  phi_prev keeps the step's
+// potential (the adjoint's snapshots read it), and the next transport does not extrapolate
+// these nodes.  Potential-Dirichlet nodes keep their boundary value.  The last CTA resets the
+// count for the next transport.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_flip_guess(EngineView v) {
+  __shared__ int s_last;
+  for (int i = 0; i < v.M; ++i) {
+    const KParams& k = v.inst[i];
+    const int n = k.ds->nflip;
+    const int step_no = (int)k.ds->steps;  // the transport's last CTA has counted its step
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+      const int a = k.flip_list[q];
+      if ((k.dirmask[a] >> S) & 1) continue;
+      double sw = 0.0, swp = 0.0;
+      for (int j = k.row[a]; j < k.row[a + 1]; ++j) {
+        const int m = k.col[j];
+        if (m == a || k.flip_step[m] == step_no) continue;
+        const bool liq = sizeof(P) == 4 ? k.rec32_nxt[m].phase == 0.0f : k.rec64_nxt[m].phase == 0.0;
+        if (!liq) continue;
+        const double w = (double)k.w32[j];
+        sw += w;
+        swp += w * k.phi64[m];
+      }
+      if (!(sw > 0.0)) continue;
+      const double g = swp / sw;
+      k.phi64[a] = g;
+      if constexpr (sizeof(P) == 4) {
+        const float hi = (float)g;
+        k.rec32_nxt[a].phi_hi = hi;
+        k.rec32_nxt[a].phi_lo = (float)(g - (double)hi);
+      } else {
+        k.rec64_nxt[a].phi = g;
+      }
+      if (k.hist_m >= 3)
+        for (int sl = 0; sl < k.hist_m; ++sl) k.xh[(size_t)sl * k.N + a] = g;
+    }
+  }
+  if (take_last_ticket(&v.ticket[v.M + 3], &s_last) && threadIdx.x == 0) {
+    for (int i = 0; i < v.M; ++i) v.inst[i].ds->nflip = 0;
+    v.ticket[v.M + 3] = 0;
   }
 }
 
@@ -3002,6 +3084,7 @@ __global__ void __launch_bounds__(kBlock) k_transport64(EngineView v, double* F_
       if (pa != 0.0 && val[0] <= k.csat) {
         pnew = 0.0;
         k.flip_step[a] = (int)step_no;
+        k.flip_list[atomicAdd(&k.ds->nflip, 1)] = a;
         k.ds->op_valid = 0;
         k.ds->defl = 0;
       }
@@ -3971,6 +4054,9 @@ nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, c
   });
 }
 
+// CTAs of the next-guess pass (a step turns at most a few thousand nodes liquid)
+constexpr int kFlipGuessCtas = 32;
+
 nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                double* F_out) {
   return dispatch_lanes(e.W, [&](auto wc) -> nnpp_status {
@@ -3978,14 +4064,18 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
     if (prec == NNPP_MIXED) {
       if (F_out)
         k_transport32<W, true><<<slice_grid(k_transport32<W, true>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, F_out);
-      else
+      else {
         k_transport32<W, false><<<claim_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
+        k_flip_guess<float><<<kFlipGuessCtas, kBlock, 0, st>>>(v);
+      }
     } else {
       const size_t sh = smem_tr64(v.halo_max, v.bond_max);
       if (F_out)
         k_transport64<W, true><<<occ_grid(k_transport64<W, true>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, F_out);
-      else
+      else {
         k_transport64<W, false><<<occ_grid(k_transport64<W, false>, sh, e.sms, v.ntiles), kBlock, sh, st>>>(v, nullptr);
+        k_flip_guess<double><<<kFlipGuessCtas, kBlock, 0, st>>>(v);
+      }
     }
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
@@ -3997,7 +4087,8 @@ nnpp_status step_alloc(Handle& h) {
   const size_t N = (size_t)h.N;
   bool ok = h.dirmask.alloc(N) && h.bcval.alloc((S + 1) * N) && h.rec32[0].alloc(N) &&
             h.rec32[1].alloc(N) && h.clo.alloc(N) && h.rec64[0].alloc(N) && h.rec64[1].alloc(N) &&
-            h.phi64.alloc(N) && h.phi_prev.alloc(N) && h.flip_step.alloc(N) && h.b64.alloc(N) &&
+            h.phi64.alloc(N) && h.phi_prev.alloc(N) && h.flip_step.alloc(N) && h.flip_list.alloc(N) &&
+            h.b64.alloc(N) &&
             h.r64.alloc(N) && h.dsum64.alloc(N) && h.cpl64.alloc(N) && h.dinv64.alloc(N) && h.rin64.alloc(N) &&
             h.z64.alloc(N) && h.p64.alloc(N) && h.q64.alloc(N) && h.e64.alloc(N) && h.d32.alloc(N) &&
             h.dinv32.alloc(N) && h.rin32.alloc(N) && h.z32.alloc(N + 16) && h.p32.alloc(N) &&
@@ -4036,6 +4127,8 @@ KParams make_kparams(Handle& h, int cur) {
   k.slot16 = h.slot16.get();
   k.sell = h.sell.get();
   k.sell_lo = h.sell_lo.get();
+  k.sell_cg = h.sell_cg.get();
+  k.cg_width = h.cg_width.get();
   k.phi4 = h.phi4.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();
@@ -4051,6 +4144,7 @@ KParams make_kparams(Handle& h, int cur) {
   k.phi_prev = h.phi_prev.get();
   k.phi_keep = h.phi_keep[cur & 1];
   k.flip_step = h.flip_step.get();
+  k.flip_list = h.flip_list.get();
   k.b64 = h.b64.get();
   k.r64 = h.r64.get();
   k.dsum64 = h.dsum64.get();

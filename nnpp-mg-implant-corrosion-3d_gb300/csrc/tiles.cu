@@ -305,8 +305,14 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
       }
   // sliced copy of the slot codes and FP32 weights for the CG operator and the transport
   const size_t ns = slices.size();
-  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48) || !h.sell_lo.alloc((size_t)(soff / 32) * 32 + 32))
+  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48) || !h.sell_lo.alloc((size_t)(soff / 32) * 32 + 32) ||
+      !h.sell_cg.alloc((size_t)(soff / 32) * 48 + 48) || !h.cg_width.alloc(std::max<size_t>(slices.size(), 1)))
     return set_error(NNPP_ERR_NOMEM, "sliced operator");
+  // the CG operator's compacted copy is filled by the next prep (which forms it whenever the
+  // unknowns change): until then empty rows, valid codes
+  NNPP_CUDA(cudaMemsetAsync(h.sell_cg.get(), 0, h.sell_cg.bytes(), h.st));
+  NNPP_CUDA(cudaMemsetAsync(h.cg_width.get(), 0, h.cg_width.bytes(), h.st));
+  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->op_valid, 0, sizeof(int), h.st));
   DBuf<SliceDesc> dsl;
   DBuf<int> dpre, dlohi;
   bool fit = true;

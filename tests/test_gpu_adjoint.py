@@ -202,6 +202,35 @@ def test_adjoint_mixed_close_to_fp64(gpu, case):
     assert np.linalg.norm(gD32 - gD64) <= 1e-3 * np.linalg.norm(gD64)
 
 
+def test_adjoint_solver_tolerance_and_stats(gpu, case):
+    """The mixed adjoint's potential solves run to 1e-8 by default: the gradient moves by far
+    less than the mixed-vs-FP64 difference when they run to 1e-12 instead, at more inner
+    iterations; the per-step iteration log adds up to the reported total, one solve a step."""
+    inp, target = case
+    res = {}
+    for tol in (0.0, 1e-12):
+        sim = _sim(gpu, inp, _params(inp), tol=1e-12, pin=True)
+        sim.set_adjoint_solver(tol)
+        curve = sim.forward_ckpt(N_STEPS, gpu.MIXED, 25, SE)
+        gD, gk = sim.backward(2.0 * (curve - target))
+        res[tol] = (gD, gk, sim.adjoint_stats(per_step=True))
+    (gD0, gk0, st0), (gD1, gk1, st1) = res[0.0], res[1e-12]
+    assert np.linalg.norm(gD0 - gD1) <= 1e-7 * np.linalg.norm(gD1)
+    assert abs(gk0 - gk1) <= 1e-7 * abs(gk1)
+    for st in (st0, st1):
+        assert st["solves"] == N_STEPS
+        assert st["sweeps"] >= st["solves"]
+        assert st["per_step"].shape == (N_STEPS,)
+        assert int(st["per_step"].sum()) == st["cg_iterations"]
+        assert (st["per_step"] >= 0).all() and st["cg_iterations"] > 0
+    assert st1["cg_iterations"] > st0["cg_iterations"]
+    sim = _sim(gpu, inp, _params(inp))
+    for bad in (-1.0, 1.0, float("nan")):
+        with pytest.raises(gpu.NNPPError) as e:
+            sim.set_adjoint_solver(bad)
+        assert e.value.status == 1
+
+
 def test_backward_errors(gpu, case):
     inp, _ = case
     sim = _sim(gpu, inp, _params(inp))
