@@ -252,6 +252,11 @@ nnpp_status nnpp_set_params(nnpp_handle* h, const nnpp_params* p);
  * the CG (default 2000), strict != 0 turns a capped solve into NNPP_ERR_CG_NO_CONVERGE. */
 nnpp_status nnpp_set_solver(nnpp_handle* h, double tol, int max_iter, int strict);
 
+/* Mixed-precision refinement of the potential solve (no counterpart in the reference, which
+ * solves in FP64): each FP32 inner CG sweep reduces its residual by inner_rel (default 1e-4;
+ * the last sweep stops at what the tolerance needs), at most max_outer sweeps (default 30). */
+nnpp_status nnpp_set_refinement(nnpp_handle* h, double inner_rel, int max_outer);
+
 /* Initial guess of each potential solve.  history 0: the previous potential (the
  * reference's warm start, main.cpp:764-779); 1 or 2: linear extrapolation 2 phi^n -
  * phi^{n-1}; 3..6 (default 6): the combination of the last `history` potentials and their

@@ -114,6 +114,7 @@ _SIGS = {
     "nnpp_forward_ckpt": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
+    "nnpp_set_refinement": (C.c_int, [_P, C.c_double, C.c_int]),
     "nnpp_set_adjoint_solver": (C.c_int, [_P, C.c_double]),
     "nnpp_get_adjoint_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64), _IP]),
@@ -362,6 +363,10 @@ class Simulation:
 
     def set_solver(self, tol=1e-10, max_iter=2000, strict=False):
         _check(lib().nnpp_set_solver(self._h, tol, max_iter, 1 if strict else 0))
+
+    def set_refinement(self, inner_rel=1e-4, max_outer=30):
+        """Mixed path: relative reduction of each FP32 inner CG sweep, sweep cap."""
+        _check(lib().nnpp_set_refinement(self._h, float(inner_rel), int(max_outer)))
 
     def forward(self, n_steps, precision=MIXED):
         _check(lib().nnpp_forward(self._h, n_steps, precision))

@@ -422,6 +422,17 @@ nnpp_status nnpp_set_solver(nnpp_handle* hp, double tol, int max_iter, int stric
   return NNPP_OK;
 }
 
+nnpp_status nnpp_set_refinement(nnpp_handle* hp, double inner_rel, int max_outer) {
+  NNPP_GUARD(hp);
+  if (!(inner_rel > 0.0) || !(inner_rel < 1.0) || max_outer < 1)
+    return set_error(NNPP_ERR_INVALID, "refinement: inner_rel in (0, 1), max_outer >= 1");
+  Handle& h = hp->h;
+  h.inner_rel = inner_rel;
+  h.max_outer = max_outer;
+  h.settings_pushed = false;
+  return NNPP_OK;
+}
+
 nnpp_status nnpp_forward(nnpp_handle* hp, int n_steps, int precision) {
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);

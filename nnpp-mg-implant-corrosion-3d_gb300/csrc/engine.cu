@@ -56,7 +56,8 @@ nnpp_status build_lists(Engine& e, int T) {
   std::vector<Chunk> chunks;
   std::vector<SliceDesc> slices;
   std::vector<HTile> htiles;
-  std::vector<int> meta(6 * M);
+  std::vector<SliceDesc> cslices;
+  std::vector<int> meta(8 * M);
   bool fit = true, hop = true;
   int hm = 0, bmax = 0, cmax = 0, qmax = 0;
   for (int i = 0; i < M; ++i) {
@@ -75,6 +76,11 @@ nnpp_status build_lists(Engine& e, int T) {
     cmax = std::max(cmax, cmi);
     qmax = std::max(qmax, qmi);
     meta[5 * M + i] = (int)slices.size() - meta[4 * M + i];
+    meta[6 * M + i] = (int)cslices.size();
+    bool cf = false;
+    NNPP_TRY(build_cg_slices(h, cslices, i, &cf));
+    fit = fit && cf;
+    meta[7 * M + i] = (int)cslices.size() - meta[6 * M + i];
     meta[M + i] = (int)tiles.size() - meta[i];
     hm = std::max(hm, hmi);
     bmax = std::max(bmax, bmi);
@@ -92,19 +98,22 @@ nnpp_status build_lists(Engine& e, int T) {
   e.ntiles = (int)tiles.size();
   e.nchunks = (int)chunks.size();
   e.nslices = (int)slices.size();
+  e.ncslices = (int)cslices.size();
   e.windows_fit = fit;
   e.halo_op = hop;
   e.hcode_max16 = cmax;
   e.hquad_max = qmax;
   int wmax = 16;
   for (const SliceDesc& d : slices) wmax = std::max(wmax, d.wtotal);
+  for (const SliceDesc& d : cslices) wmax = std::max(wmax, d.wtotal);
   e.win_cap = (wmax + 15) & ~15;
   e.halo_max = hm;
   e.bond_max = bmax;
   e.T = T;
-  const int stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
+  const int stride = std::max(std::max(e.ntiles, e.nchunks), std::max(e.nslices, e.ncslices));
   if (!e.d_tiles.alloc(tiles.size()) || !e.d_chunks.alloc(chunks.size()) || !e.d_meta.alloc(meta.size()) ||
       !e.d_slices.alloc(std::max<size_t>(slices.size(), 1)) || !e.d_htiles.alloc(std::max<size_t>(htiles.size(), 1)) ||
+      !e.d_cslices.alloc(std::max<size_t>(cslices.size(), 1)) ||
       !e.d_ticket.alloc(M + 4) ||
       !e.d_partials.alloc((size_t)kReduceSlots * stride) ||
       !e.d_inst[0].alloc(M) || !e.d_inst[1].alloc(M))
@@ -116,6 +125,8 @@ nnpp_status build_lists(Engine& e, int T) {
     NNPP_CUDA(cudaMemcpyAsync(e.d_slices.get(), slices.data(), sizeof(SliceDesc) * slices.size(), cudaMemcpyHostToDevice, e.st));
   if (!htiles.empty())
     NNPP_CUDA(cudaMemcpyAsync(e.d_htiles.get(), htiles.data(), sizeof(HTile) * htiles.size(), cudaMemcpyHostToDevice, e.st));
+  if (!cslices.empty())
+    NNPP_CUDA(cudaMemcpyAsync(e.d_cslices.get(), cslices.data(), sizeof(SliceDesc) * cslices.size(), cudaMemcpyHostToDevice, e.st));
   NNPP_CUDA(cudaMemsetAsync(e.d_ticket.get(), 0, e.d_ticket.bytes(), e.st));
   NNPP_CUDA(cudaStreamSynchronize(e.st));
   engine_destroy_graphs(e);
@@ -388,6 +399,10 @@ EngineView make_view(Engine& e, int parity, int in_graph) {
   v.slice_count = e.d_meta.get() + 5 * M;
   v.slices = e.d_slices.get();
   v.htiles = e.d_htiles.get();
+  v.cslices = e.d_cslices.get();
+  v.cslice_first = e.d_meta.get() + 6 * M;
+  v.cslice_count = e.d_meta.get() + 7 * M;
+  v.ncslices = e.ncslices;
   v.hcode_max16 = e.hcode_max16;
   v.nslices = e.nslices;
   v.ticket = e.d_ticket.get();
@@ -396,7 +411,7 @@ EngineView make_view(Engine& e, int parity, int in_graph) {
   v.nchunks = e.nchunks;
   v.M = M;
   v.in_graph = in_graph;
-  v.stride = std::max(std::max(e.ntiles, e.nchunks), e.nslices);
+  v.stride = std::max(std::max(e.ntiles, e.nchunks), std::max(e.nslices, e.ncslices));
   v.halo_max = e.halo_max;
   v.bond_max = e.bond_max;
   return v;

@@ -85,12 +85,18 @@ struct EngineView {
   const SliceDesc* slices;  // grouped by instance, tiles in order
   const int* slice_first;
   const int* slice_count;
+  // the CG operator's slices: 32 of a bin row's nodes without a potential Dirichlet value
+  // (row0: the first of its 32 slots in the instance's cg_rows; tile: the bin row, by | bz << 16)
+  const SliceDesc* cslices; // grouped by instance
+  const int* cslice_first;
+  const int* cslice_count;
   unsigned int* ticket;     // per instance completion counters, + [M] global, + [M+1] grid,
                             // + [M+2] slice claims, + [M+3] the next-guess pass
   double* partials;         // kReduceSlots * stride
   int ntiles, nchunks, M, in_graph;
   int nslices;
-  int stride;               // max(ntiles, nchunks, nslices): slot stride of partials
+  int ncslices;
+  int stride;               // max(ntiles, nchunks, nslices, ncslices): slot stride of partials
   int halo_max;             // largest halo (dynamic shared memory sizing)
   int bond_max;             // largest staged bond range of a tile (bond1 - bond0)
   int hcode_max16;          // largest code block of a tile (16-byte units, variant 8)
@@ -123,12 +129,13 @@ struct Engine {
   DBuf<KParams> d_inst[2];  // indexed by the parity of the current record buffer
   DBuf<TileDesc> d_tiles;
   DBuf<Chunk> d_chunks;
-  DBuf<int> d_meta;         // tile/chunk/slice first and count (6*M)
+  DBuf<int> d_meta;         // tile/chunk/slice/CG slice first and count (8*M)
   DBuf<SliceDesc> d_slices;
+  DBuf<SliceDesc> d_cslices;
   DBuf<HTile> d_htiles;
   DBuf<unsigned int> d_ticket;
   DBuf<double> d_partials;
-  int ntiles = 0, nchunks = 0, nslices = 0;
+  int ntiles = 0, nchunks = 0, nslices = 0, ncslices = 0;
   cudaStream_t st = nullptr, st_b1 = nullptr, st_b2 = nullptr;
   int device = 0;
   int cur = 0;              // record parity shared by all members
@@ -151,6 +158,10 @@ void engine_destroy_graphs(Engine& e);
 // tiles.cu: tile descriptors, 16-bit halo slots and FP32 position records of one instance
 nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vector<SliceDesc>& slices,
                         int inst, int* halo_max, int* bond_max, bool* windows_fit);
+// the CG operator's slices of one instance (bin rows' nodes without a potential Dirichlet
+// value, 32 a slice, with their windows) and its compacted arrays (filled by the prep); the
+// slices are appended to cslices; false in *windows_fit when a window exceeds kWinCap
+nnpp_status build_cg_slices(Handle& h, std::vector<SliceDesc>& cslices, int inst, bool* windows_fit);
 // the variant 8 layout of one instance (after build_tiles, same T): its HTile entries are
 // appended to htiles (parallel to the instance's tiles); false in *ok when the layout does
 // not apply (a kernel exponent s != 0, a halo of 65535 nodes or more)

@@ -34,10 +34,17 @@ struct KParams {
   // 16-bit slot codes (window row << 12 | offset)
   const float* sell;
   const float* sell_lo;          // sliced like sell's weights: wlo32 (32 floats per column)
-  float* sell_cg;                // sliced like sell: each row's bonds to columns that can be
-                                 // unknowns of the potential solve (liquid, no potential
-                                 // Dirichlet value), compacted to the front, zero padding
-  int* cg_width;                 // per slice of the handle: the columns of sell_cg in use
+  // the CG operator (and the refinement's residual update) on its own slices: 32 of a bin
+  // row's nodes without a potential Dirichlet value a slice; each row holds its bonds to
+  // columns that can be unknowns (liquid, no potential Dirichlet value) in bond order,
+  // interleaved like sell (weights, codes relative to the CG slice's windows) and sell_lo
+  float* sell_cg;
+  float* sell_cg_lo;
+  int* cg_width;                 // per CG slice of the handle: its longest row (the shorter
+                                 // rows are zero-padded to the slice's capacity)
+  const int* cg_rows;            // per slot: the node, -1 for padding
+  const int* cg_pos;             // per node: its slot, -1 for potential-Dirichlet nodes
+  const int* xrow;               // per node: its bin row, by | bz << 16
   float4* phi4;                  // per node {phi_hi, phi_lo} (zero on solid nodes), liquid, Dirichlet
   const double* w64;
   const float* w32;
@@ -165,8 +172,9 @@ struct Handle {
   DBuf<unsigned short> slot16;
   DBuf<float> sell;
   DBuf<float> sell_lo;
-  DBuf<float> sell_cg;          // the CG operator's compacted copy of sell (see KParams)
-  DBuf<int> cg_width;
+  DBuf<float> sell_cg;          // the CG operator's slices (see KParams)
+  DBuf<float> sell_cg_lo;
+  DBuf<int> cg_width, cg_rows, cg_pos, xrow;
   DBuf<float4> phi4;
   DBuf<float4> posrec;
   float h32 = 0.f;

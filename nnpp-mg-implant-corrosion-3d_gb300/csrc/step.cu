@@ -668,14 +668,15 @@ __device__ __forceinline__ int code_node(const int* hb, unsigned int code) {
 }
 
 // q = A z + beta q, p = z + beta p (so that q = A p), partial p.q -> alpha.
-// FP32, sliced operator: each warp streams 32-row slices (slot codes and weights
-// column-major: one coalesced load per bond column), one lane per row.  WIN: the warp first
-// copies the slice's window (the z values of its 9 window rows) into its shared-memory
-// buffer with asynchronous 16-byte copies and gathers from there (the code's low 12 bits
-// are the position in the window); otherwise it gathers from L1/L2.  PF > 0: lane 0 keeps
-// bulk L2 prefetches of the warp's operator stream PF batches ahead of the batch being read
-// (the warp's slices are contiguous in the sliced array), so that the batch loads hit L2.
-// Slice partials are reduced per instance by the last CTA.
+// FP32, on the CG operator's slices (32 of a bin row's nodes without a potential Dirichlet
+// value; each row holds only its bonds to possible unknowns, in bond order, zero-padded to
+// the slice's longest; codes and weights column-major: one coalesced load per bond column),
+// one lane per row.  WIN: the warp first copies the slice's window (the z values of its 9 window rows)
+// into its shared-memory buffer with asynchronous 16-byte copies and gathers from there (the
+// code's low 12 bits are the position in the window); otherwise it gathers from L1/L2.
+// PF > 0: lane 0 keeps bulk L2 prefetches of the warp's operator stream PF batches ahead of
+// the batch being read (the warp's slices are contiguous in the sliced array), so that the
+// batch loads hit L2.  Slice partials are reduced per instance by the last CTA.
 template <int W, bool WIN, int B, bool PIPE, int MINB, int PF = 0>
 __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   extern __shared__ __align__(16) float zwin[];
@@ -687,20 +688,24 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   // less than full ones, and a static split leaves warps idle at the end of the single
   // wave); PF > 0 keeps each warp's contiguous range for its prefetch stream
   constexpr bool kClaim = PF == 0;
+  const int ns = v.ncslices;
   int s0, s1;
   if (kClaim) {
     s0 = claim_slice(v, lane);
-    s1 = v.nslices;
+    s1 = ns;
   } else {
-    warp_slices(v, &s0, &s1);
+    const long long nw = (long long)gridDim.x * (kBlock / 32);
+    const long long gw = (long long)blockIdx.x * (kBlock / 32) + warp;
+    s0 = (int)(((long long)ns * gw) / nw);
+    s1 = (int)(((long long)ns * (gw + 1)) / nw);
   }
   float* zw = zwin + (WIN ? (size_t)warp * kWinCap : 0);
   // prefetch window of the operator stream: [pf_next, pf_end) of the warp's byte range
   const char* pf_next = nullptr;
   const char* pf_end = nullptr;
   if (PF > 0 && s0 < s1) {
-    const SliceDesc& da = v.slices[s0];
-    const SliceDesc& db = v.slices[s1 - 1];
+    const SliceDesc& da = v.cslices[s0];
+    const SliceDesc& db = v.cslices[s1 - 1];
     pf_next = reinterpret_cast<const char*>(sell_cg_w(v.inst[da.inst], da));
     pf_end = reinterpret_cast<const char*>(sell_cg_w(v.inst[db.inst], db)) + (size_t)db.width * kSellW * 4;
     if (da.inst != db.inst) pf_end = pf_next;  // the range spans instances: no prefetch
@@ -712,29 +717,31 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
     }
   }
   for (int sg = s0; sg < s1; sg = kClaim ? claim_slice(v, lane) : sg + 1) {
-    const SliceDesc d = v.slices[sg];
-    const KParams& k = v.inst[d.inst];
+    const SliceDesc& d = v.cslices[sg];
+    const int inst = __ldg(&d.inst);
+    const KParams& k = v.inst[inst];
     DotAcc<float> part;
-    if (slice_active(v, sg)) {
-      if (WIN) {
+    if (__ldg(&k.ds->inner_active) != 0) {
+      const int cs = sg - __ldg(&v.cslice_first[inst]);
+      const int width = k.cg_width[cs];
+      const int a = k.cg_rows[__ldg(&d.row0) + lane];
+      const bool live = a >= 0 && k.freem[a];
+      if (WIN && width > 0) {
         // the window (z of the 9 window rows, 16-byte aligned row segments) by 16-byte
         // cp.async, all copies in flight before the one wait
-        const SliceDesc& dg = v.slices[sg];
         const float* zg = k.z32;
 #pragma unroll 1
         for (int r = 0; r < 9; ++r) {
-          const int n = dg.wlen[r], lo = dg.lo[r], wo = dg.woff[r];
+          const int n = d.wlen[r], lo = d.lo[r], wo = d.woff[r];
           for (int i = 4 * lane; i < n; i += 128)
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(zw + wo + i)), "l"(zg + lo + i)
                          : "memory");
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
       } else if (lane < 9) {
-        s_hb[warp][lane] = v.slices[sg].gbase[lane];
+        s_hb[warp][lane] = d.gbase[lane];
       }
       __syncwarp();
-      const int a = d.row0 + lane;
-      const bool live = lane < d.nrows && k.freem[a];
       if (PF > 0 && lane == 0) {
         // keep the prefetches at least PF batches ahead of this slice's first column
         const char* target = reinterpret_cast<const char*>(sell_cg_w(k, d)) + (size_t)PF * B * kSellW * 4;
@@ -742,14 +749,12 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
         for (; pf_next < target; pf_next += B * kSellW * 4)
           bulk_prefetch_l2(pf_next, (unsigned)min((size_t)B * kSellW * 4, (size_t)(pf_end - pf_next)));
       }
-      // every lane of a slice with a live row runs the bond loop (padding columns and rows
-      // hold code 0, weight 0), so that lane 0 can issue the prefetches
+      // every lane of a slice with a live row runs the slice's columns (the shorter rows hold
+      // code 0, weight 0), so that lane 0 can issue the prefetches
       if (PF > 0 ? __any_sync(0xffffffffu, live) : live) {
         const int* hb = s_hb[warp];
-        // the compacted copy: only bonds to columns that can hold a nonzero z
         const float* ws = sell_cg_w(k, d) + lane;
-        const unsigned short* cs = sell_cg_code(k, d) + lane;
-        const int width = k.cg_width[sg - v.slice_first[d.inst]];
+        const unsigned short* cs16 = sell_cg_code(k, d) + lane;
         const float* z = k.z32;
         // B columns per batch; PIPE: the next batch of streamed columns is in flight while
         // the current batch's neighbour values are gathered (more registers, fewer warps)
@@ -761,7 +766,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
 #pragma unroll
           for (int u = 0; u < B; ++u) {
             w[u] = ld_stream(ws + kSellW * u);
-            code[u] = ld_stream(cs + kSellC * u);
+            code[u] = ld_stream(cs16 + kSellC * u);
           }
         }
         for (int b = 0; b < nb; ++b) {
@@ -773,7 +778,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
 #pragma unroll
             for (int u = 0; u < B; ++u) {
               w[u] = ld_stream(ws + kSellW * (b * B + u));
-              code[u] = ld_stream(cs + kSellC * (b * B + u));
+              code[u] = ld_stream(cs16 + kSellC * (b * B + u));
             }
           }
           float zv[B];
@@ -787,14 +792,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
 #pragma unroll
             for (int u = 0; u < B; ++u) {
               w[u] = ld_stream(ws + kSellW * (c1 + u));
-              code[u] = ld_stream(cs + kSellC * (c1 + u));
+              code[u] = ld_stream(cs16 + kSellC * (c1 + u));
             }
           }
 #pragma unroll
           for (int u = 0; u < B; ++u) acc[u & 3] = fmaf(wc[u], zv[u], acc[u & 3]);
         }
         for (int c = nb * B; c < width; ++c) {
-          const unsigned int cc = ld_stream(cs + kSellC * c);
+          const unsigned int cc = ld_stream(cs16 + kSellC * c);
           acc[0] = fmaf(ld_stream(ws + kSellW * c), WIN ? zw[cc & 4095u] : __ldg(z + code_node(hb, cc)), acc[0]);
         }
         if (live) {
@@ -816,7 +821,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cg_spmv32(EngineView v) {
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_pair_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<1>(v.partials, v.stride, v.cslice_first[i], v.cslice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         if (ds->inner_active) {
@@ -2377,6 +2382,13 @@ __device__ __forceinline__ const float* sell_lo_col(const KParams& k, const Slic
 
 // per node {phi_hi, phi_lo} (zero on solid nodes), liquid flag, potential-Dirichlet flag
 __global__ void __launch_bounds__(kBlock) k_phi4(EngineView v) {
+  // a prep that forms the mask sums rewrites the CG operator's rows: their slices' longest
+  // rows start from zero
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < v.ncslices; g += gridDim.x * blockDim.x) {
+    const int inst = v.cslices[g].inst;
+    const KParams& k = v.inst[inst];
+    if (k.ds->op_valid == 0) k.cg_width[g - v.cslice_first[inst]] = 0;
+  }
   for (int item = blockIdx.x; item < v.nchunks; item += gridDim.x) {
     const Chunk c = v.chunks[item];
     const KParams& k = v.inst[c.inst];
@@ -2419,10 +2431,26 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
     const float* ws = sell_w(k, d) + lane;
     const float* wls = sell_lo_col(k, d) + lane;
     const unsigned short* cs = sell_code(k, d) + lane;
-    // with the mask sums the row's bonds to possible unknowns (liquid columns without a
-    // potential Dirichlet value) go, in bond order, to the CG operator's compacted copy
-    float* wcg = k.sell_cg + (size_t)(d.off >> 5) * kSellW + lane;
-    unsigned short* ccg = reinterpret_cast<unsigned short*>(k.sell_cg + (size_t)(d.off >> 5) * kSellW + 32) + lane;
+    // sum_j w phi_j over the row's possible unknowns (liquid, no potential Dirichlet value)
+    // as an FP32 pair in bond order; the Dirichlet part is summed apart (and cached with the
+    // mask sums: Dirichlet potentials are constant).  The mask sums also write the row into
+    // the CG operator's slices: its bonds to possible unknowns, codes relative to that
+    // slice's windows, its length, and the slice's longest row.
+    const int cpos = scan && !cached ? k.cg_pos[a] : -1;
+    const SliceDesc* cd = nullptr;
+    float* wcg = nullptr;
+    float* wlcg = nullptr;
+    unsigned short* ccg = nullptr;
+    int cby = 0, cbz = 0;
+    if (cpos >= 0) {
+      cd = v.cslices + v.cslice_first[d.inst] + (cpos >> 5);
+      const size_t col0 = (size_t)(cd->off >> 5);
+      wcg = k.sell_cg + col0 * kSellW + (cpos & 31);
+      wlcg = k.sell_cg_lo + col0 * 32 + (cpos & 31);
+      ccg = reinterpret_cast<unsigned short*>(k.sell_cg + col0 * kSellW + 32) + (cpos & 31);
+      cby = cd->tile & 0xffff;
+      cbz = cd->tile >> 16;
+    }
     int ncg = 0;
     float dh = 0.f, dl = 0.f, sh = 0.f, sl = 0.f, ch = 0.f, cl = 0.f;
     int anyll = 0;
@@ -2439,50 +2467,44 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
             wl[u] = ld_stream(wls + 32 * (c0 + u));
             code[u] = ld_stream(cs + kSellC * (c0 + u));
           }
-        if (cached) {
-          float2 f[kResB];
+        float4 f[kResB];
 #pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) f[u] = __ldg(reinterpret_cast<const float2*>(k.phi4 + code_node(hb, code[u])));
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc) f[u] = __ldg(k.phi4 + code_node(hb, code[u]));
 #pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) {
-              float ph, pl;
-              pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc && c0 + u < len && f[u].z != 0.0f) {
+            float ph, pl;
+            pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+            if (f[u].w != 0.0f) {
+              if (!cached) pair_add(ch, cl, ph, pl);
+            } else {
               pair_add(sh, sl, ph, pl);
             }
-        } else {
-          float4 f[kResB];
-#pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) f[u] = __ldg(k.phi4 + code_node(hb, code[u]));
-#pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc && c0 + u < len && f[u].z != 0.0f) {
-              float ph, pl;
-              pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+            if (!cached) {
               pair_add(dh, dl, w[u], wl[u]);
-              pair_add(sh, sl, ph, pl);
               anyll = 1;
-              if (f[u].w != 0.0f) {
-                pair_add(ch, cl, ph, pl);
-              } else if (scan) {
+              if (f[u].w == 0.0f && cpos >= 0) {
+                const int m = code_node(hb, code[u]);
+                const int xr = k.xrow[m];
+                const int r = ((xr & 0xffff) - cby + 1) + 3 * ((xr >> 16) - cbz + 1);
                 wcg[(size_t)kSellW * ncg] = w[u];
-                ccg[(size_t)kSellC * ncg] = (unsigned short)code[u];
+                wlcg[(size_t)32 * ncg] = wl[u];
+                ccg[(size_t)kSellC * ncg] = (unsigned short)((r << 12) | (m - cd->gbase[r]));
                 ++ncg;
               }
             }
-        }
+          }
       }
     }
-    if (!cached) {
-      // zero padding of the shorter rows up to the slice's compacted width
-      const int wcgmax = __reduce_max_sync(0xffffffffu, ncg);
-      for (int c = ncg; c < wcgmax; ++c) {
+    if (cpos >= 0) {
+      // zero padding up to the slice's capacity (its longest full row)
+      for (int c = ncg; c < cd->width; ++c) {
         wcg[(size_t)kSellW * c] = 0.0f;
+        wlcg[(size_t)32 * c] = 0.0f;
         ccg[(size_t)kSellC * c] = 0;
       }
-      if (lane == 0) k.cg_width[sg - v.slice_first[d.inst]] = wcgmax;
+      atomicMax(&k.cg_width[cpos >> 5], ncg);
     }
     float b2h = 0.0f, b2l = 0.0f, r2h = 0.0f, r2l = 0.0f;  // b.b and r.r as FP32 pairs
     if (rowok) {
@@ -2514,7 +2536,8 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
         k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
       }
       const double bb = fr ? b : 0.0;
-      const double r = fr ? bb - (dsum * pha - swphi) : 0.0;
+      // sum_j w phi_j over the liquid neighbours: the unknowns' pair plus the Dirichlet part
+      const double r = fr ? bb - (dsum * pha - (swphi + cpl)) : 0.0;
       k.b64[a] = bb;
       k.r64[a] = r;
       const double be = bb + (fr ? cpl : 0.0);
@@ -2568,45 +2591,45 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
   // cost less than full ones)
-  for (int sg = claim_slice(v, lane); sg < v.nslices; sg = claim_slice(v, lane)) {
-    const SliceDesc& d = v.slices[sg];
-    const KParams& k = v.inst[d.inst];
+  for (int sg = claim_slice(v, lane); sg < v.ncslices; sg = claim_slice(v, lane)) {
+    const SliceDesc& d = v.cslices[sg];
+    const int inst = __ldg(&d.inst);
+    const KParams& k = v.inst[inst];
     float rh = 0.0f, rl = 0.0f;  // r.r of the slice as an FP32 pair
     if (*((volatile int*)&k.ds->outer_active) != 0) {
       if (lane < 9) s_hb[warp][lane] = d.gbase[lane];
       __syncwarp();
-      const int a = d.row0 + lane;
-      const bool live = lane < d.nrows && k.freem[a];
+      // the CG operator's slices: the correction e is zero off the unknowns
+      const int a = k.cg_rows[__ldg(&d.row0) + lane];
+      const bool live = a >= 0 && k.freem[a];
+      const int len = __any_sync(0xffffffffu, live) ? k.cg_width[sg - __ldg(&v.cslice_first[inst])] : 0;
       const int* hb = s_hb[warp];
-      const float* ws = sell_w(k, d) + lane;
-      const float* wls = sell_lo_col(k, d) + lane;
-      const unsigned short* cs = sell_code(k, d) + lane;
+      const float* ws = sell_cg_w(k, d) + lane;
+      const float* wls = k.sell_cg_lo + (size_t)(__ldg(&d.off) >> 5) * 32 + lane;
+      const unsigned short* cs = sell_cg_code(k, d) + lane;
       const float* e = k.e32;
       float sh = 0.f, sl = 0.f;
-      if (__any_sync(0xffffffffu, live)) {
-        const int width = d.width;
-        for (int c0 = 0; c0 < width; c0 += kResB) {
-          const int nc = min(kResB, width - c0);
-          float w[kResB], wl[kResB], ev[kResB];
-          unsigned int code[kResB];
+      for (int c0 = 0; c0 < len; c0 += kResB) {
+        const int nc = min(kResB, len - c0);
+        float w[kResB], wl[kResB], ev[kResB];
+        unsigned int code[kResB];
 #pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) {
-              w[u] = ld_stream(ws + kSellW * (c0 + u));
-              wl[u] = ld_stream(wls + 32 * (c0 + u));
-              code[u] = ld_stream(cs + kSellC * (c0 + u));
-            }
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc) {
+            w[u] = ld_stream(ws + kSellW * (c0 + u));
+            wl[u] = ld_stream(wls + 32 * (c0 + u));
+            code[u] = ld_stream(cs + kSellC * (c0 + u));
+          }
 #pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) ev[u] = __ldg(e + code_node(hb, code[u]));
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc) ev[u] = __ldg(e + code_node(hb, code[u]));
 #pragma unroll
-          for (int u = 0; u < kResB; ++u)
-            if (u < nc) {
-              float ph, pl;
-              pair_mul(w[u], wl[u], ev[u], 0.0f, ph, pl);
-              pair_add(sh, sl, ph, pl);
-            }
-        }
+        for (int u = 0; u < kResB; ++u)
+          if (u < nc) {
+            float ph, pl;
+            pair_mul(w[u], wl[u], ev[u], 0.0f, ph, pl);
+            pair_add(sh, sl, ph, pl);
+          }
       }
       if (live) {
         const double ea = (double)e[a];
@@ -2625,7 +2648,7 @@ __global__ void __launch_bounds__(kBlock) k_ir_slices(EngineView v, cudaGraphCon
   if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
     for (int i = 0; i < v.M; ++i) {
       double tot[1];
-      reduce_pair_items<1>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+      reduce_pair_items<1>(v.partials, v.stride, v.cslice_first[i], v.cslice_count[i], tot, sm);
       if (threadIdx.x == 0) {
         DevState* ds = v.inst[i].ds;
         if (ds->outer_active) {
@@ -3818,34 +3841,34 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
   switch (variant) {
     case 2: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 8, true, 3><<<claim_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 8, true, 3><<<claim_grid(k_cg_spmv32<W, true, 8, true, 3>, sh, sms, v.ncslices), kBlock, sh, st>>>(v);
       break;
     }
     case 3:
       // 40 registers: six CTAs an SM (measured 0.087 ms at 512k; five CTAs 0.088, eight with
       // 32 registers 0.120, batches of 32 columns at four 0.089)
-      k_cg_spmv32<W, false, 16, false, 6><<<claim_grid(k_cg_spmv32<W, false, 16, false, 6>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 16, false, 6><<<claim_grid(k_cg_spmv32<W, false, 16, false, 6>, 0, sms, v.ncslices), kBlock, 0, st>>>(v);
       break;
     case 4: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 16, false, 3><<<claim_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 16, false, 3><<<claim_grid(k_cg_spmv32<W, true, 16, false, 3>, sh, sms, v.ncslices), kBlock, sh, st>>>(v);
       break;
     }
     case 5: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 16, false, 3, 3><<<slice_grid(k_cg_spmv32<W, true, 16, false, 3, 3>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 16, false, 3, 3><<<slice_grid(k_cg_spmv32<W, true, 16, false, 3, 3>, sh, sms, v.ncslices), kBlock, sh, st>>>(v);
       break;
     }
     case 6:
-      k_cg_spmv32<W, false, 16, false, 5, 3><<<slice_grid(k_cg_spmv32<W, false, 16, false, 5, 3>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 16, false, 5, 3><<<slice_grid(k_cg_spmv32<W, false, 16, false, 5, 3>, 0, sms, v.ncslices), kBlock, 0, st>>>(v);
       break;
     case 7: {
       const size_t sh = smem_spmv_win();
-      k_cg_spmv32<W, true, 8, true, 3, 4><<<slice_grid(k_cg_spmv32<W, true, 8, true, 3, 4>, sh, sms, v.nslices), kBlock, sh, st>>>(v);
+      k_cg_spmv32<W, true, 8, true, 3, 4><<<slice_grid(k_cg_spmv32<W, true, 8, true, 3, 4>, sh, sms, v.ncslices), kBlock, sh, st>>>(v);
       break;
     }
     default:
-      k_cg_spmv32<W, false, 8, false, 8><<<claim_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.nslices), kBlock, 0, st>>>(v);
+      k_cg_spmv32<W, false, 8, false, 8><<<claim_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.ncslices), kBlock, 0, st>>>(v);
   }
 }
 
@@ -4038,7 +4061,7 @@ nnpp_status launch_cg_update_b(const Engine& e, const EngineView& v, int prec, c
 nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, cudaStream_t st,
                                cudaGraphConditionalHandle hc) {
   if (prec == NNPP_MIXED) {
-    k_ir_slices<<<claim_grid(k_ir_slices, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, hc);
+    k_ir_slices<<<claim_grid(k_ir_slices, 0, e.sms, v.ncslices), kBlock, 0, st>>>(v, hc);
     NNPP_CUDA(cudaGetLastError());
     return NNPP_OK;
   }
@@ -4128,7 +4151,11 @@ KParams make_kparams(Handle& h, int cur) {
   k.sell = h.sell.get();
   k.sell_lo = h.sell_lo.get();
   k.sell_cg = h.sell_cg.get();
+  k.sell_cg_lo = h.sell_cg_lo.get();
   k.cg_width = h.cg_width.get();
+  k.cg_rows = h.cg_rows.get();
+  k.cg_pos = h.cg_pos.get();
+  k.xrow = h.xrow.get();
   k.phi4 = h.phi4.get();
   k.w64 = h.lay.w64.get();
   k.w32 = h.lay.w32.get();

@@ -7,6 +7,7 @@
 // ranges).  A kernel stages a tile's halo into shared memory and reaches a neighbour through
 // its slot: the neighbour's position in the concatenation of the halo rows.
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "engine.cuh"
@@ -175,6 +176,51 @@ __global__ void k_sell_fill(int nslices, const SliceDesc* sl, const int* pre_hb,
   }
 }
 
+// warp per CG slice: the node range [lo, hi) of its rows' neighbours without a potential
+// Dirichlet value in each of the 9 window rows (the bin rows by + dy, bz + dz, dy, dz in
+// -1..1, row (dy + 1) + 3 (dz + 1))
+__global__ void k_cg_windows(int nslices, const SliceDesc* sl, const int* cg_rows, const int* row,
+                             const int* col, const unsigned char* dirmask, const int* xrow, int* lohi) {
+  constexpr unsigned char kPhiDir = 1u << S;
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nslices; s += warps) {
+    const SliceDesc& d = sl[s];
+    const int by = d.tile & 0xffff, bz = d.tile >> 16;
+    int lo[9], hi[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      lo[q] = 0x7fffffff;
+      hi[q] = -1;
+    }
+    const int a = lane < d.nrows ? cg_rows[d.row0 + lane] : -1;
+    if (a >= 0)
+      for (int j = row[a]; j < row[a + 1]; ++j) {
+        const int m = col[j];
+        if (dirmask[m] & kPhiDir) continue;
+        const int xr = xrow[m];
+        const int r = ((xr & 0xffff) - by + 1) + 3 * ((xr >> 16) - bz + 1);
+#pragma unroll
+        for (int q = 0; q < 9; ++q)
+          if (q == r) {
+            lo[q] = min(lo[q], m);
+            hi[q] = max(hi[q], m + 1);
+          }
+      }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      lo[q] = __reduce_min_sync(0xffffffffu, lo[q]);
+      hi[q] = __reduce_max_sync(0xffffffffu, hi[q]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        lohi[18 * s + q] = lo[q];
+        lohi[18 * s + 9 + q] = hi[q];
+      }
+  }
+}
+
 // per node: -1 for a node with a Dirichlet value of the potential, else its number of
 // neighbours without one (the row length of the halo-staged CG operator)
 __global__ void k_omega_degree(int n, const int* row, const int* col, const unsigned char* dirmask,
@@ -305,14 +351,8 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
       }
   // sliced copy of the slot codes and FP32 weights for the CG operator and the transport
   const size_t ns = slices.size();
-  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48) || !h.sell_lo.alloc((size_t)(soff / 32) * 32 + 32) ||
-      !h.sell_cg.alloc((size_t)(soff / 32) * 48 + 48) || !h.cg_width.alloc(std::max<size_t>(slices.size(), 1)))
+  if (!h.sell.alloc((size_t)(soff / 32) * 48 + 48) || !h.sell_lo.alloc((size_t)(soff / 32) * 32 + 32))
     return set_error(NNPP_ERR_NOMEM, "sliced operator");
-  // the CG operator's compacted copy is filled by the next prep (which forms it whenever the
-  // unknowns change): until then empty rows, valid codes
-  NNPP_CUDA(cudaMemsetAsync(h.sell_cg.get(), 0, h.sell_cg.bytes(), h.st));
-  NNPP_CUDA(cudaMemsetAsync(h.cg_width.get(), 0, h.cg_width.bytes(), h.st));
-  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->op_valid, 0, sizeof(int), h.st));
   DBuf<SliceDesc> dsl;
   DBuf<int> dpre, dlohi;
   bool fit = true;
@@ -360,6 +400,121 @@ nnpp_status build_tiles(Handle& h, int T, std::vector<TileDesc>& tiles, std::vec
   *halo_max = hm;
   *bond_max = bm;
   h.tiles_T = T;
+  return NNPP_OK;
+}
+
+// Window rows of a slice from the node ranges its bonds reach: [lo, hi) rounded out to
+// multiples of 4 nodes (16-byte copies), the codes' 12-bit offsets reaching hi - 1.
+static nnpp_status finish_windows(SliceDesc& d, const int* lohi, bool* fit) {
+  int acc = 0;
+  for (int r = 0; r < 9; ++r) {
+    const int lo = lohi[r], hi = lohi[9 + r];
+    if (hi <= lo) {
+      d.lo[r] = 0;
+      d.wlen[r] = 0;
+    } else {
+      d.lo[r] = lo & ~3;
+      d.wlen[r] = (hi - d.lo[r] + 3) & ~3;
+      if (hi - 1 - d.lo[r] > 4095) return set_error(NNPP_ERR_UNSUPPORTED, "slice window row wider than 4096 nodes");
+    }
+    d.woff[r] = acc;
+    acc += d.wlen[r];
+  }
+  d.wtotal = acc;
+  for (int r = 0; r < 9; ++r) d.gbase[r] = acc <= 4096 ? d.lo[r] - d.woff[r] : d.lo[r];
+  *fit = *fit && acc <= kWinCap;
+  return NNPP_OK;
+}
+
+nnpp_status build_cg_slices(Handle& h, std::vector<SliceDesc>& gcs, int inst, bool* windows_fit) {
+  constexpr unsigned char kPhiDir = 1u << S;
+  const Layout& L = h.lay;
+  const int N = h.N;
+  const int nb0 = L.nb[0], nb1 = L.nb[1], nb2 = L.nb[2];
+  if (nb1 > 0xffff || nb2 > 0x7fff) return set_error(NNPP_ERR_UNSUPPORTED, "CG slices: too many bin rows");
+  std::vector<int> bs(L.nbins + 1), rows(N + 1);
+  std::vector<unsigned char> dm(N);
+  NNPP_CUDA(cudaMemcpyAsync(bs.data(), L.bin_start.get(), sizeof(int) * (L.nbins + 1), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(rows.data(), L.row.get(), sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(dm.data(), h.dirmask.get(), (size_t)N, cudaMemcpyDeviceToHost, h.st));
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  std::vector<int> xrow(N, 0), pos(N, -1), slots;
+  std::vector<SliceDesc> cs;
+  long long coff = 0;
+  std::vector<int> rr, rbx;
+  for (int bz = 0; bz < nb2; ++bz)
+    for (int by = 0; by < nb1; ++by) {
+      const int b0 = nb0 * (by + nb1 * bz);
+      const int tag = by | (bz << 16);
+      // the row's nodes without a potential Dirichlet value with their bins, in order; a
+      // slice takes up to 32 of them from at most two adjacent bins, so that its windows stay
+      // a few bins wide where Dirichlet nodes interrupt the row
+      rr.clear();
+      rbx.clear();
+      for (int bx = 0; bx < nb0; ++bx)
+        for (int a = bs[b0 + bx]; a < bs[b0 + bx + 1]; ++a) {
+          xrow[a] = tag;
+          if (!(dm[a] & kPhiDir)) {
+            rr.push_back(a);
+            rbx.push_back(bx);
+          }
+        }
+      for (size_t i = 0; i < rr.size();) {
+        size_t e = i + 1;
+        while (e < rr.size() && e - i < 32 && rbx[e] <= rbx[i] + 1) ++e;
+        SliceDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.inst = inst;
+        d.tile = tag;
+        d.row0 = (int)slots.size();
+        d.nrows = (int)(e - i);
+        d.off = (int)coff;
+        for (int l = 0; l < 32; ++l) {
+          const int a = i + l < e ? rr[i + l] : -1;
+          slots.push_back(a);
+          if (a >= 0) {
+            pos[a] = d.row0 + l;
+            d.width = std::max(d.width, rows[a + 1] - rows[a]);
+          }
+        }
+        coff += 32LL * d.width;
+        if (coff > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "CG operator above 2^31 entries");
+        cs.push_back(d);
+        i = e;
+      }
+    }
+  const size_t ns = cs.size(), nslot = std::max<size_t>(slots.size(), 1);
+  if (!h.xrow.alloc(N) || !h.cg_pos.alloc(N) || !h.cg_rows.alloc(nslot) ||
+      !h.cg_width.alloc(std::max<size_t>(ns, 1)) || !h.sell_cg.alloc((size_t)(coff / 32) * 48 + 48) ||
+      !h.sell_cg_lo.alloc((size_t)(coff / 32) * 32 + 32))
+    return set_error(NNPP_ERR_NOMEM, "CG operator");
+  NNPP_CUDA(cudaMemcpyAsync(h.xrow.get(), xrow.data(), sizeof(int) * N, cudaMemcpyHostToDevice, h.st));
+  NNPP_CUDA(cudaMemcpyAsync(h.cg_pos.get(), pos.data(), sizeof(int) * N, cudaMemcpyHostToDevice, h.st));
+  if (!slots.empty())
+    NNPP_CUDA(cudaMemcpyAsync(h.cg_rows.get(), slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice, h.st));
+  // filled by the next prep, which forms the rows whenever the unknowns change (every
+  // slice empty until then)
+  NNPP_CUDA(cudaMemsetAsync(h.cg_width.get(), 0, h.cg_width.bytes(), h.st));
+  NNPP_CUDA(cudaMemsetAsync(h.sell_cg.get(), 0, h.sell_cg.bytes(), h.st));
+  NNPP_CUDA(cudaMemsetAsync(h.sell_cg_lo.get(), 0, h.sell_cg_lo.bytes(), h.st));
+  NNPP_CUDA(cudaMemsetAsync(&h.dstate.get()->op_valid, 0, sizeof(int), h.st));
+  bool fit = true;
+  if (ns) {
+    DBuf<SliceDesc> dsl;
+    DBuf<int> dlohi;
+    if (!dsl.alloc(ns) || !dlohi.alloc(18 * ns)) return set_error(NNPP_ERR_NOMEM, "CG operator");
+    NNPP_CUDA(cudaMemcpyAsync(dsl.get(), cs.data(), sizeof(SliceDesc) * ns, cudaMemcpyHostToDevice, h.st));
+    const int sb = std::max(1, std::min((int)((ns * 32 + 255) / 256), 152 * 32));
+    k_cg_windows<<<sb, 256, 0, h.st>>>((int)ns, dsl.get(), h.cg_rows.get(), L.row.get(), L.col.get(),
+                                       h.dirmask.get(), h.xrow.get(), dlohi.get());
+    NNPP_CUDA(cudaGetLastError());
+    std::vector<int> lohi(18 * ns);
+    NNPP_CUDA(cudaMemcpyAsync(lohi.data(), dlohi.get(), sizeof(int) * 18 * ns, cudaMemcpyDeviceToHost, h.st));
+    NNPP_CUDA(cudaStreamSynchronize(h.st));
+    for (size_t q = 0; q < ns; ++q) NNPP_TRY(finish_windows(cs[q], lohi.data() + 18 * q, &fit));
+  }
+  *windows_fit = fit;
+  gcs.insert(gcs.end(), cs.begin(), cs.end());
   return NNPP_OK;
 }
 
