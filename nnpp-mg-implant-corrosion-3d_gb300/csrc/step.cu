@@ -2431,11 +2431,11 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
     const float* ws = sell_w(k, d) + lane;
     const float* wls = sell_lo_col(k, d) + lane;
     const unsigned short* cs = sell_code(k, d) + lane;
-    // sum_j w phi_j over the row's possible unknowns (liquid, no potential Dirichlet value)
-    // as an FP32 pair in bond order; the Dirichlet part is summed apart (and cached with the
-    // mask sums: Dirichlet potentials are constant).  The mask sums also write the row into
-    // the CG operator's slices: its bonds to possible unknowns, codes relative to that
-    // slice's windows, its length, and the slice's longest row.
+    // sum_j w phi_j over the liquid columns as an FP32 pair in bond order (the cached pass
+    // adds the solid columns' exact zeros, so both passes give the same bits).  The mask
+    // sums also write the row into the CG operator's slices: its bonds to possible unknowns
+    // (liquid, no potential Dirichlet value), codes relative to that slice's windows, zero
+    // padding, and the slice's longest row.
     const int cpos = scan && !cached ? k.cg_pos[a] : -1;
     const SliceDesc* cd = nullptr;
     float* wcg = nullptr;
@@ -2467,6 +2467,20 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
             wl[u] = ld_stream(wls + 32 * (c0 + u));
             code[u] = ld_stream(cs + kSellC * (c0 + u));
           }
+        if (cached) {
+          float2 f[kResB];
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) f[u] = __ldg(reinterpret_cast<const float2*>(k.phi4 + code_node(hb, code[u])));
+#pragma unroll
+          for (int u = 0; u < kResB; ++u)
+            if (u < nc) {
+              float ph, pl;
+              pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+              pair_add(sh, sl, ph, pl);
+            }
+          continue;
+        }
         float4 f[kResB];
 #pragma unroll
         for (int u = 0; u < kResB; ++u)
@@ -2476,23 +2490,19 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
           if (u < nc && c0 + u < len && f[u].z != 0.0f) {
             float ph, pl;
             pair_mul(w[u], wl[u], f[u].x, f[u].y, ph, pl);
+            pair_add(sh, sl, ph, pl);
+            pair_add(dh, dl, w[u], wl[u]);
+            anyll = 1;
             if (f[u].w != 0.0f) {
-              if (!cached) pair_add(ch, cl, ph, pl);
-            } else {
-              pair_add(sh, sl, ph, pl);
-            }
-            if (!cached) {
-              pair_add(dh, dl, w[u], wl[u]);
-              anyll = 1;
-              if (f[u].w == 0.0f && cpos >= 0) {
-                const int m = code_node(hb, code[u]);
-                const int xr = k.xrow[m];
-                const int r = ((xr & 0xffff) - cby + 1) + 3 * ((xr >> 16) - cbz + 1);
-                wcg[(size_t)kSellW * ncg] = w[u];
-                wlcg[(size_t)32 * ncg] = wl[u];
-                ccg[(size_t)kSellC * ncg] = (unsigned short)((r << 12) | (m - cd->gbase[r]));
-                ++ncg;
-              }
+              pair_add(ch, cl, ph, pl);
+            } else if (cpos >= 0) {
+              const int m = code_node(hb, code[u]);
+              const int xr = k.xrow[m];
+              const int r = ((xr & 0xffff) - cby + 1) + 3 * ((xr >> 16) - cbz + 1);
+              wcg[(size_t)kSellW * ncg] = w[u];
+              wlcg[(size_t)32 * ncg] = wl[u];
+              ccg[(size_t)kSellC * ncg] = (unsigned short)((r << 12) | (m - cd->gbase[r]));
+              ++ncg;
             }
           }
       }
@@ -2536,8 +2546,7 @@ __global__ void __launch_bounds__(kBlock) k_prep_slices(EngineView v, cudaGraphC
         k.dinv32[a] = fr ? (float)(1.0 / dsum) : 0.0f;
       }
       const double bb = fr ? b : 0.0;
-      // sum_j w phi_j over the liquid neighbours: the unknowns' pair plus the Dirichlet part
-      const double r = fr ? bb - (dsum * pha - (swphi + cpl)) : 0.0;
+      const double r = fr ? bb - (dsum * pha - swphi) : 0.0;
       k.b64[a] = bb;
       k.r64[a] = r;
       const double be = bb + (fr ? cpl : 0.0);
