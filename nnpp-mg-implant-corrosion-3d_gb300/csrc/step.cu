@@ -2750,14 +2750,24 @@ __device__ __forceinline__ double next_phi_guess(const KParams& k, int a) {
   return g;
 }
 
+// A neighbour's whole 32-byte record (c[4] | phi_hi, phi_lo, phase, pad) in one 256-bit
+// read-only load (records are 32-byte aligned): half the gather instructions and L1 requests
+// of two 16-byte loads of the same sector.
+__device__ __forceinline__ void ld_rec32(const float4* p, float4& c, float4& t) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(c.x), "=f"(c.y), "=f"(c.z), "=f"(c.w), "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+      : "l"(p));
+}
+
 // Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
 // (single instance) and change nothing; otherwise advance the state into rec32_nxt / clo.
 // Each warp streams 32-row slices of the sliced operator, one lane per node, gathering the
 // neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
 // partials of the diagnostics are reduced per instance by the last CTA.
-// bond columns per batch of the FP32 transport: 6 at 126 registers (2 CTAs an SM) measured
-// 0.378 ms at 512k, against 0.389 for 5, 0.405 for 4 and 0.467 for 2 (8 spills)
-constexpr int kTrB = 6;
+// bond columns per batch of the FP32 transport: with 256-bit record loads 7 (128 registers,
+// 2 CTAs an SM) measured 0.358 ms at 512k against 0.366 for 6 (8 spills); with two 16-byte
+// loads a record 6 took 0.378 ms, 5 0.389, 4 0.405, 2 0.467
+constexpr int kTrB = 7;
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double* F_out) {
   __shared__ int s_hb[kBlock / 32][12];
@@ -2833,8 +2843,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
         for (int u = 0; u < kTrB; ++u)
           if (c0 + u < len) {
             const int n = code_node(hb, code[u]);
-            cn[u] = __ldg(rc + 2 * n);
-            nb[u] = __ldg(rc + 2 * n + 1);
+            ld_rec32(rc + 2 * n, cn[u], nb[u]);
           }
 #pragma unroll
         for (int u = 0; u < kTrB; ++u)

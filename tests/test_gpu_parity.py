@@ -433,6 +433,66 @@ def test_coarse_rebuild_follows_dissolution(gpu, orc, prec):
     assert rebuilds[(nn.PRECOND_JACOBI, 4)] == 0
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_nodes_turned_liquid_start_from_their_neighbours_potential(gpu, prec):
+    """After the step in which a node turns liquid, its potential (the next solve's guess) is a
+    weighted mean of the potentials of its neighbours that were liquid before that step: it
+    lies between their extremes, not at the solid's zero."""
+    nn = gpu
+    inp = nn.synth(1, 12, 5)
+    p = inp["params"].copy()
+    p.switch_width = 0.01
+    p.k_diss = 0.1
+    sim = nn.Simulation(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+    sim.build_neighbours()
+    ptr, cols = sim.neighbours_csr()
+    phi_dir = (np.asarray(inp["bctypes"]) == 0) & (np.asarray(inp["bcvalues"])[4] != -1)
+    checked = 0
+    for step in range(1, 61):
+        _, _, ph0 = sim.state()
+        sim.forward(1, prec)
+        _, phi, ph1 = sim.state()
+        flipped = np.nonzero((ph0 != 0) & (ph1 == 0))[0]
+        for a in flipped:
+            if phi_dir[a]:
+                continue
+            nb = cols[ptr[a]:ptr[a + 1]]
+            nb = nb[(ph0[nb] == 0)]
+            if nb.size == 0:
+                continue
+            lo, hi = phi[nb].min(), phi[nb].max()
+            span = max(hi - lo, 1e-12 * max(abs(lo), abs(hi), 1.0))
+            assert lo - 1e-9 * span <= phi[a] <= hi + 1e-9 * span
+            assert phi[a] != 0.0 or (lo <= 0.0 <= hi)
+            checked += 1
+    assert checked > 0
+
+
+def test_refinement_settings(gpu):
+    """A looser inner reduction per FP32 sweep costs refinement sweeps, not accuracy; bad
+    settings are rejected."""
+    nn = gpu
+    inp = nn.synth(1, 16, 3)
+    out = {}
+    for rel in (1e-4, 1e-2):
+        sim = nn.Simulation.from_synth(inp)
+        sim.build_neighbours()
+        sim.set_refinement(rel, 30)
+        sim.forward(20, nn.MIXED)
+        d = sim.diagnostics()
+        out[rel] = (sim.state(), d["outer_iterations_total"], d["cg_not_converged"])
+    (s4, o4, nc4), (s2, o2, nc2) = out[1e-4], out[1e-2]
+    assert nc4 == 0 and nc2 == 0
+    assert o2 > o4
+    for a, b in zip(s4[:2], s2[:2]):
+        assert np.linalg.norm(a - b) <= 1e-8 * np.linalg.norm(a)
+    sim = nn.Simulation.from_synth(inp)
+    for bad in ((0.0, 30), (1.0, 30), (1e-4, 0)):
+        with pytest.raises(nn.NNPPError) as e:
+            sim.set_refinement(*bad)
+        assert e.value.status == 1
+
+
 def test_warm_start_rejects_bad_history(gpu):
     nn = gpu
     inp = nn.synth(1, 12, seed=4)
