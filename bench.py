@@ -503,7 +503,7 @@ def run_ours(args):
     tuned = sim.tuning()
     variants = {}
     with ProfileRange("variants"):
-        for var, key in ((0, "gather8"), (1, "bulk_staged"), (2, "smem_window8"), (3, "gather16"),
+        for var, key in ((0, "gather16_pipelined"), (1, "bulk_staged"), (2, "smem_window8"), (3, "gather16"),
                          (4, "smem_window16"), (5, "smem_window16_l2pf"), (6, "gather16_l2pf"),
                          (7, "smem_window8_l2pf"), (8, "halo_recompute")):
             try:

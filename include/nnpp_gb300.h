@@ -354,7 +354,7 @@ nnpp_status nnpp_time_kernel(nnpp_handle* h, int kernel_id, int precision, int r
 
 /* The execution configuration of the handle's kernels: bins per tile, lanes per node of the
  * FP64 tile kernels, and the FP32 CG operator's variant: 0 / 3 gathers from L1/L2 (batches
- * of 8 / 16 bond columns), 1 operator and slice windows streamed by bulk copies into shared
+ * of 16 bond columns; 0 keeps the next batch's stream in flight), 1 operator and slice windows streamed by bulk copies into shared
  * memory, 2 / 4 slice windows copied into shared memory by asynchronous copies (batches of
  * 8 / 16), 5 / 6 / 7 the variants 4 / 3 / 2 with bulk L2 prefetches of the operator stream
  * a few batches ahead, 8 the tile's halo (positions and the CG vector) staged in shared

@@ -112,7 +112,8 @@ struct Engine {
   int W = 8;                // lanes per node (autotuned)
   bool tuned = false;
   bool eager = false;       // NNPP_EAGER=1: launch kernel by kernel, loops driven by the host
-  int spmv_variant = 0;     // FP32 CG operator: 0, 3 L1/L2 gathers (batches of 8, 16),
+  int spmv_variant = 0;     // FP32 CG operator: 0, 3 L1/L2 gathers (batches of 16, 0
+                            // pipelined),
                             // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16),
                             // 5, 6, 7: 4, 3, 2 with L2 prefetch of the operator stream,
                             // 8 tile halo in shared memory, weights recomputed

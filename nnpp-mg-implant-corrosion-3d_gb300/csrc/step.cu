@@ -3851,7 +3851,8 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
 }
 
 // FP32 CG operator variants without the staged ring (the autotuner's list): 0 L1/L2 gathers
-// in batches of 8, 32 registers (64 warps per SM); 2 shared-memory windows, pipelined batches
+// in batches of 16, pipelined (the next batch's weights and codes in flight while the current
+// one gathers), 64 registers (32 warps per SM); 2 shared-memory windows, pipelined batches
 // of 8; 3 L1/L2 gathers in batches of 16 (40 warps per SM); 4 shared-memory windows, batches
 // of 16; 5, 6, 7: 4, 3, 2 with bulk L2 prefetches of the operator stream 3, 3, 4 batches ahead
 template <int W>
@@ -3886,7 +3887,9 @@ void launch_spmv_gather(int variant, const EngineView& v, int sms, cudaStream_t 
       break;
     }
     default:
-      k_cg_spmv32<W, false, 8, false, 8><<<claim_grid(k_cg_spmv32<W, false, 8, false, 8>, 0, sms, v.ncslices), kBlock, 0, st>>>(v);
+      // measured 0.071 ms at 512k against 0.076 for 3; batches of 8 at 64 warps an SM took
+      // 0.105, pipelined 16 at 3 CTAs 0.072, pipelined 24 at 3 CTAs (spilling) slower
+      k_cg_spmv32<W, false, 16, true, 4><<<claim_grid(k_cg_spmv32<W, false, 16, true, 4>, 0, sms, v.ncslices), kBlock, 0, st>>>(v);
   }
 }
 
