@@ -378,6 +378,118 @@ def large_cost(nn, steps):
             "value": inp["N"] * steps / (ms / 1e3), "unit": "node-steps/s"}
 
 
+def fp64_peak_tflops(torch):
+    """A measured FP64 ceiling for the residual's roofline: cuBLAS DGEMM 4096^3 through
+    torch.matmul, best of 5 (CUDA events)."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2.0 * 4096 ** 3 / (best / 1e3) / 1e12
+
+
+# FP64 operations of one bond of the complete residual as the kernel forms it (an FMA counts
+# two): offset and length 9, dphi 1, beta dx dy dz and the two weights 3, 1 / xi^3 3, ten
+# species at 8, the potential's bond 4
+CHEM_FLOPS_PER_BOND = 100
+
+
+def chemistry_cost(nn, reps, with_cpu):
+    """The reference's complete residual (ten species, their reactions, the potential;
+    utils::Residuals) on the 512k lattice with the reference's physical constants: the device
+    entry point's time per evaluation (inputs resident), the host entry point's time with its
+    copies, an FP64 roofline, and the oracle on the host cores on the 64k lattice of the same
+    node spacing (the same horizon) as the CPU baseline."""
+    import ctypes as C
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import chem_case
+    g = np.load(os.path.join(ROOT, "tests", "golden", "chemistry.npz"))
+    d2, dc, d11 = (np.ascontiguousarray(g[k]) for k in ("data2", "datac", "datac11"))
+    nodes, phase, Un1, Un, r, cell = chem_case.case_inputs(nn.synth, 1, 80, 1, d2)
+    N = nodes.shape[1]
+    clouds, lengths, ml = nn.build_clouds_hash(160, r, cell, cell, cell, nodes)
+    bonds = int(lengths.sum()) - N
+    dev = torch.device("cuda")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    dx, dcl, dl = t(nodes), t(clouds[:, :ml].T), t(lengths)
+    du1, du0, dph = t(Un1), t(Un), t(phase)
+    dF = torch.zeros((11, N), dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream()
+    L = nn.lib()
+
+    def call():
+        rc = L.nnpp_residuals_full_device(N, dx.data_ptr(), dcl.data_ptr(), dl.data_ptr(), du1.data_ptr(),
+                                          du0.data_ptr(), dph.data_ptr(), chem_case.VOLN1REL, nn._dp(d2),
+                                          nn._dp(dc), nn._dp(d11), dF.data_ptr(), C.c_void_p(st.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(L.nnpp_last_error())
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        call()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # end to end: the host entry point with its validation and copies in and out
+    cl_host = clouds[:, :ml]
+    nn.residuals_full(nodes, cl_host, lengths, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        F = nn.residuals_full(nodes, cl_host, lengths, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
+    ms_e2e = (time.perf_counter() - t0) / 3 * 1e3
+    same = bool(np.array_equal(F, dF.cpu().numpy()))
+    peak = fp64_peak_tflops(torch)
+    achieved = CHEM_FLOPS_PER_BOND * bonds / (ms / 1e3) / 1e12
+    out = {"workload": "jittered 80^3 lattice (512,000 nodes) at the reference's node spacing and "
+                       "physical constants, seeded concentrations of the ten species and potential "
+                       "at two time levels",
+           "n_nodes": N, "bonds": bonds, "ms_per_evaluation": ms, "value": N / (ms / 1e3),
+           "unit": "node residuals/s",
+           "e2e": {"value": N / (ms_e2e / 1e3), "ms": ms_e2e,
+                   "h2d_bytes": int(nodes.nbytes + cl_host.nbytes + lengths.nbytes + Un1.nbytes + Un.nbytes +
+                                    phase.nbytes),
+                   "d2h_bytes": int(F.nbytes)},
+           "host_entry_equals_device_entry": same,
+           "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak, "flops_per_bond": CHEM_FLOPS_PER_BOND,
+                        "peak_source": "measured here: cuBLAS DGEMM 4096^3"}}
+    del dx, dcl, dl, du1, du0, dph, dF
+    if with_cpu:
+        O = load_oracle_module()
+        cores = O.set_threads(os.cpu_count() or 1)
+        nodes_s, phase_s, Un1_s, Un_s, r_s, cell_s = chem_case.case_inputs(nn.synth, 1, 40, 1, d2)
+        cs, ls, mls = nn.build_clouds_hash(160, r_s, cell_s, cell_s, cell_s, nodes_s)
+        ptr = np.zeros(ls.size + 1, dtype=np.int64)
+        ptr[1:] = np.cumsum(ls)
+        cols = cs[:, :mls][np.arange(mls)[None, :] < ls[:, None]].astype(np.int32)
+        reps_c, t0 = 0, time.perf_counter()
+        while True:
+            O.residuals_full(nodes_s, ptr, cols, Un1_s, Un_s, phase_s, chem_case.VOLN1REL, d2, dc, d11)
+            reps_c += 1
+            el = time.perf_counter() - t0
+            if el > 10.0 or reps_c >= 20:
+                break
+        out["cpu_baseline"] = {"value": nodes_s.shape[1] * reps_c / el, "unit": "node residuals/s",
+                               "cores": cores, "kind": "port",
+                               "sample": "%d evaluations on the 40^3 lattice (%d nodes) of the same "
+                                         "spacing" % (reps_c, nodes_s.shape[1])}
+    return out
+
+
 def run_ours(args):
     rank, world, local = dist_info()
     nn = load_package()
@@ -585,6 +697,11 @@ def run_ours(args):
         large = large_cost(nn, args.large_steps)
         log("large: %s" % json.dumps(large))
 
+    chem = None
+    if rank == 0 and args.chem_reps > 0:
+        chem = chemistry_cost(nn, args.chem_reps, world == 1 and not args.no_cpu_baseline)
+        log("chemistry: %s" % json.dumps(chem))
+
     cpu = None
     acc_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -630,6 +747,7 @@ def run_ours(args):
             "ensemble": ensemble,
             "large_2m": large,
             "moving_front": front,
+            "chemistry_10_species": chem,
             "neighbour_build_s": t_build,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -654,6 +772,8 @@ def main():
                     help="timed steps of the 512k workload's dissolving phase (0: skip)")
     ap.add_argument("--front-pre", type=int, default=2000,
                     help="steps run before the dissolving-phase window")
+    ap.add_argument("--chem-reps", type=int, default=10,
+                    help="timed evaluations of the ten-species residual on the 512k lattice (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

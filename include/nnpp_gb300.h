@@ -173,6 +173,33 @@ nnpp_status nnpp_build_clouds_hash_noalloc(int max_node_no, double r, double dx,
                                            int* d_clouds_colmajor, int* d_cloud_lengths,
                                            int* max_cloud_length, void* stream);
 
+/* ---- the complete ten-species residual (utils.h:29-842) -------------------------------- */
+
+/* The reference's complete residual, utils::Residuals (utils.h:29-842): the ten species
+ * with their reactions (utils.h:162-174, 241-253, 321-330, 396-401, 466-476, 541-547,
+ * 612-618, 683-690, including the interface's Butler-Volmer H+ source) and the potential, in
+ * FP64.  Inputs as the reference holds them: nodes N x 3 column-major, clouds N x max_node_no
+ * column-major (self in column 0, as build_clouds_hash fills them) with cloud_lengths,
+ * U_n1 and U_n 11*N (fields 1..10 then the potential, field-major), phase N (1 solid), the
+ * volume ratio voln1rel, and the parameter arrays of the reference's data files: data2 (51
+ * values, the .data2 file), datac (10 x 7, the .datac1..datac10 files one after another) and
+ * datac11 (4).  Writes F: 11*N (F1..F11).  (The reference's U^{n0} arguments are not read by
+ * utils.h:29-842 and are not taken.)  Copies in and out of the device inside the call. */
+nnpp_status nnpp_residuals_full(int n_nodes, const double* nodes_colmajor, const int* clouds_colmajor,
+                                int max_node_no, const int* cloud_lengths, const double* U_n1,
+                                const double* U_n, const int* phase, double voln1rel,
+                                const double* data2, const double* datac, const double* datac11,
+                                double* F);
+
+/* The same on device arrays (clouds with N rows and at least the longest length in columns;
+ * every index checked by the caller), launched on the given CUDA stream (NULL: the legacy
+ * default stream); returns after the launch. */
+nnpp_status nnpp_residuals_full_device(int n_nodes, const double* d_nodes, const int* d_clouds,
+                                       const int* d_lengths, const double* d_U_n1,
+                                       const double* d_U_n, const int* d_phase, double voln1rel,
+                                       const double* data2, const double* datac,
+                                       const double* datac11, double* d_F, void* stream);
+
 /* ---- implant mask (main.cpp:316-325, 422-457) ------------------------------------------- */
 
 /* The phase of every node from the implant's point cloud, as the reference sets it up when

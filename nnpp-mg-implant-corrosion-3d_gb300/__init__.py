@@ -115,6 +115,11 @@ _SIGS = {
     "nnpp_backward": (C.c_int, [_P, _DP, _DP, _DP]),
     "nnpp_set_adjoint_store": (C.c_int, [_P, C.c_int]),
     "nnpp_set_refinement": (C.c_int, [_P, C.c_double, C.c_int]),
+    "nnpp_residuals_full": (C.c_int, [C.c_int, _DP, _IP, C.c_int, _IP, _DP, _DP, _IP, C.c_double,
+                                      _DP, _DP, _DP, _DP]),
+    "nnpp_residuals_full_device": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_double, _DP, _DP, _DP,
+                                             C.c_void_p, C.c_void_p]),
     "nnpp_set_adjoint_solver": (C.c_int, [_P, C.c_double]),
     "nnpp_get_adjoint_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                          C.POINTER(C.c_int64), _IP]),
@@ -204,6 +209,34 @@ def params_from_reference(data2, datac, datac11, k_diss=0.0, switch_width=0.0):
                                             _dp(dc[3]), _dp(d11), k_diss, switch_width,
                                             C.byref(p)))
     return p
+
+
+# ------------------------------------------------------------- ten-species residual -----
+def residuals_full(nodes, clouds, cloud_lengths, U_n1, U_n, phase, voln1rel, data2, datac, datac11):
+    """nnpp_residuals_full: the reference's complete residual utils::Residuals (ten species,
+    their reactions, the potential).  nodes (3, N) or (N, 3); clouds (N, M) as
+    build_clouds_hash returns them (self in column 0); U_n1, U_n (11, N); phase (N,);
+    data2 (51,), datac (10, 7), datac11 (4,) the reference's control vectors.  Returns F
+    (11, N)."""
+    xyz = _colmajor_nodes(nodes)
+    N = xyz.shape[1]
+    cl = np.ascontiguousarray(np.asarray(clouds, dtype=np.int32).T)  # (M, N): column-major N x M
+    M = cl.shape[0]
+    lens = np.ascontiguousarray(cloud_lengths, dtype=np.int32)
+    u1 = np.ascontiguousarray(U_n1, dtype=np.float64)
+    u0 = np.ascontiguousarray(U_n, dtype=np.float64)
+    ph = np.ascontiguousarray(phase, dtype=np.int32)
+    if u1.shape != (11, N) or u0.shape != (11, N) or ph.shape != (N,) or lens.shape != (N,):
+        raise ValueError("residuals_full: U_n1, U_n (11, N), phase and cloud_lengths (N,)")
+    d2 = np.ascontiguousarray(data2, dtype=np.float64)
+    dc = np.ascontiguousarray(datac, dtype=np.float64)
+    d11 = np.ascontiguousarray(datac11, dtype=np.float64)
+    if d2.size != 51 or dc.size != 70 or d11.size != 4:
+        raise ValueError("residuals_full: data2 (51), datac (10, 7), datac11 (4)")
+    F = np.zeros((11, N))
+    _check(lib().nnpp_residuals_full(N, _dp(xyz), _ip(cl), M, _ip(lens), _dp(u1), _dp(u0), _ip(ph),
+                                     float(voln1rel), _dp(d2), _dp(dc), _dp(d11), _dp(F)))
+    return F
 
 
 # ------------------------------------------------------------------ neighbour build -----

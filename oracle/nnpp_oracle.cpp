@@ -635,7 +635,154 @@ double mg_mass_lost(const Oracle& o) {
   return m * o.p.dx * o.p.dy * o.p.dz;
 }
 
+// ---------------------------------------------------------------------------------------
+// The reference's complete residual, utils::Residuals (utils.h:29-842): ten species, their
+// reactions, the potential.  A restatement of its formulas in its operand order, each field's
+// sums over the horizon in order, so that it reproduces the reference bit for bit (pinned
+// against tests/golden/chemistry.npz).  Parameter arrays as the reference's data files hold
+// them (utils.h:2343-2484): data2 (51), datac (10 x 7: z, D_solid, D_liquid, s_1, s_2,
+// K_prop1, K_prop2), datac11 (sigma0, sigma1, s_11, K11prop1).  Clouds in the reference's
+// format: row i's horizon cols[row_ptr[i] .. row_ptr[i+1]), the node itself first.
+void residuals_full(int N, const double* x, const int64_t* rp, const int* cols, const double* Un1,
+                    const double* Un, const int* phase, double voln1rel, const double* d2,
+                    const double* dc, const double* d11, double* Fout) {
+  const double dt = d2[2], dx = d2[3], dy = d2[4], dz = d2[5], delta = d2[6];
+  const double CSolid = d2[7], CSat = d2[8];
+  const double phim = d2[23], phimse = d2[24], alphaC = d2[27];
+  const double k1b = d2[29], k2b = d2[31], k3b = d2[33], k4b = d2[35], k5b = d2[37], k6b = d2[39];
+  const double k7b = d2[41], k8b = d2[43], k9b = d2[45];
+  const double JHp = d2[46], T = d2[47], R = d2[48], Fc = d2[49], vol_red = d2[50];
+  auto P = [&](int i) { return std::pow(10., -d2[i]) / CSolid; };  // 10^-pK / CSolid
+  const double pMgOH2 = P(14), pMgCO3 = P(15), pMgHCO3 = P(16), pMgPO4 = P(17), pCaCO3 = P(18);
+  const double pCa5 = P(19), pH2O = P(20), pHCO3 = P(21), pHPO4 = P(22);
+  const double sigma1 = d11[1], s111 = d11[2], K11 = d11[3];
+  auto U1 = [&](int k, int i) { return Un1[(int64_t)k * N + i]; };  // U_{k+1}^{n+1}
+  auto U0 = [&](int k, int i) { return Un[(int64_t)k * N + i]; };   // U_{k+1}^n
+  for (int k = 0; k <= 10; ++k)
+    for (int i = 0; i < N; ++i) Fout[(int64_t)k * N + i] = 0.0;
+  // species k (0-based): bond sums and the reaction term of node i
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    int iface = 0;
+    if (phase[i] == 1)
+      for (int64_t j = rp[i] + 1; j < rp[i + 1]; ++j)
+        if (phase[cols[j]] == 0) {
+          iface = 1;
+          break;
+        }
+    for (int k = 0; k < 10; ++k) {
+      const double* c = dc + 7 * k;
+      const double z = c[0], Ds = c[1], Dl = c[2], s1 = c[3], s2 = c[4], K1 = c[5], K2 = c[6];
+      double sum1 = 0.0, sum2 = 0.0;
+      for (int64_t j = rp[i] + 1; j < rp[i + 1]; ++j) {
+        const int n = cols[j];
+        const double xx = x[n] - x[i], yy = x[N + n] - x[N + i], zz = x[2 * N + n] - x[2 * N + i];
+        const double xi = std::sqrt(xx * xx + yy * yy + zz * zz);
+        const bool ss = phase[i] == 1 && phase[n] == 1, ll = phase[i] == 0 && phase[n] == 0;
+        const double b = beta_fn(xi, delta, dx);
+        const double du = U1(k, n) - U1(k, i), dphi = U0(10, n) - U0(10, i);
+        if (k == 0) {
+          // Mg (utils.h:100-160): BV on bonds touching the solid, solid-solid bonds kept
+          if (!ll) {
+            const double BV = ss ? 1.0 : std::pow(10., -vol_red * (1. - voln1rel));
+            sum1 += -(K1 * Ds * BV * du / std::pow(xi, 3.0 + 2.0 * s1)) * b * dx * dy * dz;
+            sum2 += -(K2 * Ds * BV * z * Fc * U1(k, n) * dphi / (R * T * std::pow(xi, 3.0 + 2.0 * s2))) * b * dx * dy * dz;
+          } else {
+            sum1 += -(K1 * Dl * du / std::pow(xi, 3.0 + 2.0 * s1)) * b * dx * dy * dz;
+            sum2 += -(K2 * Dl * z * Fc * U1(k, n) * dphi / (R * T * std::pow(xi, 3.0 + 2.0 * s2))) * b * dx * dy * dz;
+          }
+        } else {
+          // the other species (utils.h:205-239 and alike): solid-solid bonds skipped
+          if (ss) continue;
+          const double D = ll ? Dl : Ds;
+          sum1 += -(K1 * D * du / std::pow(xi, 3.0 + 2.0 * s1)) * b * dx * dy * dz;
+          sum2 += -(K2 * D * z * Fc * U1(k, n) * dphi / (R * T * std::pow(xi, 3.0 + 2.0 * s2))) * b * dx * dy * dz;
+        }
+      }
+      const bool liq = phase[i] == 0, act = iface == 1 || liq;
+      double Rk = 0.0;
+      const double u8 = U0(7, i), u7 = U0(6, i);
+      auto ca5 = [&](double a) { return a * u8 * u8 * u8 * u8 * u8 * u7 * u7 * u7; };
+      switch (k) {
+        case 0:  // utils.h:162-174
+          if (act)
+            Rk = -k1b * std::max((U1(0, i) * U0(2, i) * U0(2, i) - pMgOH2), 0.0) -
+                 k2b * std::max((U1(0, i) * U0(4, i) - pMgCO3), 0.0) -
+                 k3b * std::max((U1(0, i) * U0(4, i) - pMgHCO3), 0.0) -
+                 k4b * std::max((U0(0, i) * U0(0, i) * U0(0, i) * U0(5, i) * U0(5, i) - pMgPO4), 0.0);
+          break;
+        case 1:  // utils.h:241-253
+          if (iface == 1) {
+            const double phic = (R * T / (Fc * dc[0])) * std::log(U0(0, i) / (CSat / CSolid));
+            const double eta = phim + phimse - U0(10, i) - phic;
+            Rk += (JHp / (z * Fc * CSolid)) * std::exp(-alphaC * Fc * eta / (R * T));
+          } else if (liq) {
+            Rk = k7b * (pH2O - U1(1, i) * U0(2, i)) + k8b * (pHCO3 - U1(1, i) * U0(4, i)) +
+                 k9b * (pHPO4 - U1(1, i) * U0(6, i));
+          }
+          break;
+        case 2:  // utils.h:321-330
+          if (act) {
+            Rk = -k1b * std::max((U0(2, i) * U0(2, i) * U0(0, i) - pMgOH2), 0.0) -
+                 k6b * std::max((ca5(U1(2, i)) - pCa5), 0.0);
+            if (liq) Rk += k7b * (pH2O - U1(2, i) * U0(1, i));
+          }
+          break;
+        case 3:  // utils.h:396-401
+          if (liq) Rk = k8b * (pHCO3 - U1(3, i) * U0(1, i));
+          break;
+        case 4:  // utils.h:466-476
+          if (act) {
+            Rk = -k2b * std::max((U1(4, i) * U0(0, i) - pMgCO3), 0.0) -
+                 k3b * std::max((U1(4, i) * U0(0, i) - pMgHCO3), 0.0) -
+                 k5b * std::max((U1(4, i) * U0(7, i) - pCaCO3), 0.0);
+            if (liq) Rk += k8b * (pHCO3 - U0(1, i) * U1(4, i));
+          }
+          break;
+        case 5:  // utils.h:541-547
+          if (act) {
+            Rk = -k4b * std::max((U0(0, i) * U0(0, i) * U0(0, i) * U0(5, i) * U0(5, i) - pMgPO4), 0.0);
+            if (liq) Rk += k9b * (-pHPO4 + U0(6, i) * U0(1, i));
+          }
+          break;
+        case 6:  // utils.h:612-618
+          if (act) {
+            Rk = -k6b * std::max((ca5(U0(2, i)) - pCa5), 0.0);
+            if (liq) Rk += k9b * (pHPO4 - U1(6, i) * U0(1, i));
+          }
+          break;
+        case 7:  // utils.h:683-690
+          if (act)
+            Rk = -k5b * std::max((U1(7, i) * U0(4, i) - pCaCO3), 0.0) -
+                 k6b * std::max((ca5(U0(2, i)) - pCa5), 0.0);
+          break;
+        default:  // species 9, 10: no reaction (utils.h:744, 795)
+          break;
+      }
+      Fout[(int64_t)k * N + i] = ((U1(k, i) - U0(k, i)) / dt) + sum1 + sum2 - Rk;
+    }
+    // potential (utils.h:801-841)
+    double s11 = 0.0;
+    int flag = 0;
+    for (int64_t j = rp[i] + 1; j < rp[i + 1]; ++j) {
+      const int n = cols[j];
+      if (!(phase[i] == 0 && phase[n] == 0)) continue;
+      const double xx = x[n] - x[i], yy = x[N + n] - x[N + i], zz = x[2 * N + n] - x[2 * N + i];
+      const double xi = std::sqrt(xx * xx + yy * yy + zz * zz);
+      s11 += -(K11 * sigma1 * (U1(10, n) - U1(10, i)) / std::pow(xi, 3.0 + 2.0 * s111)) *
+             beta_fn(xi, delta, dx) * dx * dy * dz;
+      flag = 1;
+    }
+    if (flag) {
+      double r11 = 0.0;
+      for (int k = 0; k < 10; ++k) r11 = (k == 0) ? dc[0] * U0(0, i) : r11 + dc[7 * k] * U0(k, i);
+      Fout[(int64_t)10 * N + i] = (1. / (K11 * sigma1)) * s11 - (1. / (K11 * sigma1)) * Fc * CSolid * r11;
+    }
+  }
+}
+
 }  // namespace
+
 
 // ================================================================ C interface =============
 // ---------------------------------------------------------------- implicit step ----------
@@ -906,6 +1053,13 @@ int implicit_step(Oracle& o, ImplicitStats* st) {
 }
 
 extern "C" {
+
+int orc_residuals_full(int N, const double* nodes, const int64_t* row_ptr, const int* cols, const double* Un1,
+                       const double* Un, const int* phase, double voln1rel, const double* data2,
+                       const double* datac, const double* datac11, double* F) {
+  residuals_full(N, nodes, row_ptr, cols, Un1, Un, phase, voln1rel, data2, datac, datac11, F);
+  return 0;
+}
 
 void* orc_create(const nnpp_params* p, int N, const double* xyz, const int* bctypes,
                  const double* bcvalues, const double* icvalues, const int* phase0) {

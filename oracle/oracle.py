@@ -56,6 +56,8 @@ def load_oracle():
             "orc_get_clouds": (C.c_int, [_P, _IP, _LP, _IP]),
             "orc_set_clouds": (C.c_int, [_P, _LP, _IP]),
             "orc_residuals": (C.c_int, [_P, _DP, _DP, _IP, C.c_double, _DP]),
+            "orc_residuals_full": (C.c_int, [C.c_int, _DP, _LP, _IP, _DP, _DP, _IP, C.c_double, _DP,
+                                             _DP, _DP, _DP]),
             "orc_poisson_matrix": (C.c_int, [_P, _IP, _DP, _DP, C.POINTER(C.c_ubyte)]),
             "orc_solve_potential": (C.c_int, [_P, _DP, _IP, _DP, _IP, _DP]),
             "orc_forward": (C.c_int, [_P, C.c_int]),
@@ -101,6 +103,8 @@ def load_reference():
                                    _DP, _DP, _DP, _LP, _IP, _IP, _DP]
         L.ref_gmres.argtypes = [C.c_int, C.c_int, _DP, _LP, _IP, _DP, _IP, _IP, _DP, C.c_double,
                                 _DP, _DP, _DP, _DP, _DP]
+        L.ref_residuals2.argtypes = [C.c_int, _DP, _LP, _IP, _DP, _DP, _IP, _IP, _DP, C.c_double,
+                                     _DP, _DP, _DP, _DP]
         L.ref_implant_counts.restype = C.c_int
         L.ref_implant_counts.argtypes = [C.c_int, _DP, C.c_int, _DP, C.c_double, C.c_int, _IP]
         _ref = L
@@ -379,6 +383,44 @@ def ref_residuals(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1re
                     _ip(np.ascontiguousarray(phase, dtype=np.int32)),
                     _ip(np.ascontiguousarray(bctypes, dtype=np.int32)), _dp(B), voln1rel,
                     _dp(d2), _dp(np.ascontiguousarray(dc)), _dp(d11), _dp(F))
+    return F
+
+
+def residuals_full(nodes, ptr, cols, Un1, Un, phase, voln1rel, data2, datac, datac11):
+    """The oracle's restatement of the reference's complete residual (ten species, their
+    reactions, the potential; utils.h:29-842): clouds in the reference format (ptr int64,
+    cols with the node itself first), Un1, Un (11, N).  Returns F (11, N)."""
+    N = nodes.shape[1]
+    F = np.zeros((11, N))
+    load_oracle().orc_residuals_full(N, _dp(np.ascontiguousarray(nodes, dtype=np.float64)),
+                                     _lp(np.ascontiguousarray(ptr, dtype=np.int64)),
+                                     _ip(np.ascontiguousarray(cols, dtype=np.int32)),
+                                     _dp(np.ascontiguousarray(Un1, dtype=np.float64)),
+                                     _dp(np.ascontiguousarray(Un, dtype=np.float64)),
+                                     _ip(np.ascontiguousarray(phase, dtype=np.int32)), float(voln1rel),
+                                     _dp(np.ascontiguousarray(data2, dtype=np.float64)),
+                                     _dp(np.ascontiguousarray(datac, dtype=np.float64)),
+                                     _dp(np.ascontiguousarray(datac11, dtype=np.float64)), _dp(F))
+    return F
+
+
+def ref_residuals_full(nodes, ptr, cols, Un1, Un, phase, voln1rel, data2, datac, datac11):
+    """utils::Residuals of the reference with all ten species, their reactions and the given
+    parameter arrays (data2 51, datac (10, 7), datac11 4); Un1, Un (11, N).  Returns F (11, N).
+    No Dirichlet values are passed (the residual does not read them)."""
+    L = load_reference()
+    if L is None:
+        return None
+    N = nodes.shape[1]
+    F = np.zeros((11, N))
+    bct = np.ones(N, dtype=np.int32)
+    B = -np.ones((11, N))
+    L.ref_residuals2(N, _dp(np.ascontiguousarray(nodes)), _lp(np.ascontiguousarray(ptr, dtype=np.int64)),
+                     _ip(np.ascontiguousarray(cols, dtype=np.int32)), _dp(np.ascontiguousarray(Un1)),
+                     _dp(np.ascontiguousarray(Un)), _ip(np.ascontiguousarray(phase, dtype=np.int32)),
+                     _ip(bct), _dp(B), voln1rel, _dp(np.ascontiguousarray(data2, dtype=np.float64)),
+                     _dp(np.ascontiguousarray(datac, dtype=np.float64)),
+                     _dp(np.ascontiguousarray(datac11, dtype=np.float64)), _dp(F))
     return F
 
 

@@ -125,6 +125,50 @@ int ref_residuals(int N, const double* xyz, const int64_t* row_ptr, const int* c
   return 0;
 }
 
+// utils::Residuals (utils.h:29-842) with separate U^{n+1} (Un1) and U^n (Un), each 11*N,
+// and the reference's parameter arrays as given (data2 51, datac 10 x 7, datac11 4): the
+// complete ten-species residual with its reactions.  Writes F: 11*N.
+int ref_residuals2(int N, const double* xyz, const int64_t* row_ptr, const int* cols,
+                   const double* Un1, const double* Un, const int* phase, const int* bctypes,
+                   const double* bcvalues, double voln1rel, const double* data2, const double* datac,
+                   const double* datac11, double* F) {
+  utils::parameter prm;
+  make_params(prm, N, data2, datac, datac11);
+  Eigen::MatrixXd nodes(N, 3);
+  int maxlen = 1;
+  for (int i = 0; i < N; ++i) {
+    nodes(i, 0) = xyz[i];
+    nodes(i, 1) = xyz[N + i];
+    nodes(i, 2) = xyz[2 * N + i];
+    maxlen = std::max(maxlen, (int)(row_ptr[i + 1] - row_ptr[i]));
+  }
+  Eigen::MatrixXi hz(N, maxlen);
+  hz.setConstant(-1);
+  Eigen::VectorXi hl(N), ph(N), bt(N);
+  for (int i = 0; i < N; ++i) {
+    hl[i] = (int)(row_ptr[i + 1] - row_ptr[i]);
+    for (int j = 0; j < hl[i]; ++j) hz(i, j) = cols[row_ptr[i] + j];
+    ph[i] = phase[i];
+    bt[i] = bctypes[i];
+  }
+  std::vector<Eigen::VectorXd> bc(11), u1(11), u(11), u0(11), f(11);
+  for (int k = 0; k < 11; ++k) {
+    bc[k] = Eigen::Map<const Eigen::VectorXd>(bcvalues + (int64_t)k * N, N);
+    u1[k] = Eigen::Map<const Eigen::VectorXd>(Un1 + (int64_t)k * N, N);
+    u[k] = Eigen::Map<const Eigen::VectorXd>(Un + (int64_t)k * N, N);
+    u0[k] = Eigen::VectorXd::Zero(N);
+    f[k] = Eigen::VectorXd::Zero(N);
+  }
+  utils::Residuals(nodes, hz, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], bc[6], bc[7], bc[8],
+                   bc[9], bc[10], u1[0], u1[1], u1[2], u1[3], u1[4], u1[5], u1[6], u1[7],
+                   u1[8], u1[9], u1[10], u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8],
+                   u[9], u[10], u0[0], u0[1], u0[2], u0[3], u0[4], u0[5], u0[6], u0[7], u0[8],
+                   u0[9], u0[10], f[0], f[1], f[2], f[3], f[4], f[5], f[6], f[7], f[8], f[9],
+                   f[10], ph, hl, bt, voln1rel, prm);
+  for (int k = 0; k < 11; ++k) std::memcpy(F + (int64_t)k * N, f[k].data(), sizeof(double) * N);
+  return 0;
+}
+
 // All eleven tangents of utils::NewtonMatrices (utils.h:844-1849) at the state U (used as
 // both U^{n+1} and U^n), kept for the entry points below.
 std::vector<SpMat> g_K;

@@ -12,6 +12,8 @@ by oracle/build_oracle.py, on the synthetic workloads of nnpp_synth_fill, and st
   params.json     the reference's control vectors of data/NNPP.data2, .datac1-4, .datac11
   implant.json    SHA-256 of the point counts of the reference's kd-tree implant query for
                   seeded implant point clouds
+  chemistry.npz   F1..F11 of the reference's complete residual (ten species, reactions) with
+                  the control vectors of its data files, on the cases of tests/chem_case.py
 Needs the reference's sources (REFERENCE_ROOT); run:  python tests/golden/make_golden.py
 """
 import hashlib
@@ -86,9 +88,48 @@ def implant_fixtures():
         json.dump(out, f, indent=1, sort_keys=True)
 
 
+def read_control(name):
+    """A whitespace-separated control vector of the reference's data directory."""
+    with open(os.path.join(REFERENCE_ROOT, "data", name)) as f:
+        return np.array([float(x) for x in f.read().split()])
+
+
+def chemistry_fixtures():
+    """chemistry.npz: the reference's complete residual (ten species, their reactions, the
+    potential; utils.h:29-842) with the control vectors of its data files (NNPP.data2,
+    .datac1-10, .datac11) on the cases of tests/chem_case.py, and those vectors."""
+    import chem_case
+    import oracle as O
+    if O.load_reference() is None:
+        raise SystemExit("reference sources not found at %s" % REFERENCE_ROOT)
+    d2 = read_control("NNPP.data2")
+    dc = np.stack([read_control("NNPP.datac%d" % k) for k in range(1, 11)])
+    d11 = read_control("NNPP.datac11")
+    assert d2.shape == (51,) and dc.shape == (10, 7) and d11.shape == (4,)
+    arrays = {"data2": d2, "datac": dc, "datac11": d11}
+    d2r = chem_case.reactive_data2(d2)
+    d2z = d2r.copy()
+    d2z[[29, 31, 33, 35, 37, 39, 41, 43, 45, 46]] = 0.0  # no reaction, no H+ source
+    for kind, n, seed in chem_case.CASES:
+        nodes, phase, Un1, Un, r, cell = chem_case.case_inputs(O.synth, kind, n, seed, d2)
+        lo, po, co, ml = O.ref_build_clouds_hash(1024, r, cell, cell, cell, nodes)
+        key = "kind%d_n%d_seed%d" % (kind, n, seed)
+        F = O.ref_residuals_full(nodes, po, co, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
+        Fr = O.ref_residuals_full(nodes, po, co, Un1, Un, phase, chem_case.VOLN1REL, d2r, dc, d11)
+        Fz = O.ref_residuals_full(nodes, po, co, Un1, Un, phase, chem_case.VOLN1REL, d2z, dc, d11)
+        arrays[key + "_F"] = F
+        arrays[key + "_Freactive"] = Fr
+        print(key, "N", nodes.shape[1], "max|F| per field", np.abs(F).max(axis=1), flush=True)
+        print("   reactive: max|F|", np.abs(Fr).max(axis=1), "max|R|", np.abs(Fr - Fz).max(axis=1), flush=True)
+    np.savez_compressed(os.path.join(HERE, "chemistry.npz"), **arrays)
+
+
 def main():
     if "--only-implant" in sys.argv:
         implant_fixtures()
+        return
+    if "--only-chemistry" in sys.argv:
+        chemistry_fixtures()
         return
     from conftest import load_package
     import oracle as O
