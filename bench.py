@@ -53,6 +53,32 @@ def dist_info():
     return rank, world, local
 
 
+class Replicas:
+    """The replicas of a multi-process run (one independent instance per GPU, no data
+    exchange): a gloo group for the barriers around the timed region and the max over ranks
+    of its time.  One process: no group, the calls return at once."""
+
+    def __init__(self, world):
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -510,6 +536,7 @@ def run_ours(args):
     log("N=%d nnz=%d neighbour build %.3f s" % (N, nnz, t_build))
 
     # warm-up (the first solve starts from phi = 0)
+    reps = Replicas(world)
     sim.forward(args.warmup, nn.MIXED)
     sim64.forward(args.warmup, nn.FP64)
     # the coarse operator is checked every `refresh` steps and rebuilt if the phases changed;
@@ -519,8 +546,10 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
+    reps.barrier()
     with ProfileRange("timed"):
-        ms = sim.forward_timed(args.steps, nn.MIXED)
+        ms = sim.forward_timed(args.steps, nn.MIXED)  # synchronises the device on both sides
+    reps.barrier()
     clk = clocks.stop()
     d1 = sim.diagnostics()
     rb1 = sim.preconditioner()[3]
@@ -538,13 +567,7 @@ def run_ours(args):
     del simj
 
     # max over ranks
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reps.max(ms)
     value = N * args.steps * world / (ms / 1e3)
     value64 = N * args.steps / (ms64 / 1e3)
 
