@@ -648,6 +648,16 @@ def run_ours(args):
             except nn.NNPPError as ex:
                 variants[key] = "unsupported: %s" % ex
     sim.set_tuning(*tuned)
+    # the FP32 transport's two forms (the default: L1/L2 gathers)
+    tr_variants = {}
+    with ProfileRange("transport_variants"):
+        for var, key in ((0, "l1_gathers"), (1, "halo_staged")):
+            try:
+                sim.set_transport_variant(var)
+                tr_variants[key] = sim.time_kernel(0, nn.MIXED, reps=20)
+            except nn.NNPPError as ex:
+                tr_variants[key] = "unsupported: %s" % ex
+    sim.set_transport_variant(0)
     k64 = {"cg_spmv": sim64.time_kernel(1, nn.FP64, reps=20),
            "transport": sim64.time_kernel(0, nn.FP64, reps=10),
            "cg_update": sim64.time_kernel(3, nn.FP64, reps=20)}
@@ -700,6 +710,7 @@ def run_ours(args):
     roofline["bonds"] = {"all": nnz, "liquid_liquid": nnz_ll, "between_unknowns": nnz_uu}
     roofline["fp64_path_ms_per_launch"] = k64
     roofline["cg_operator_variants_ms"] = variants
+    roofline["transport_variants_ms"] = tr_variants
     if t_parts:
         roofline["cg_update_parts_ms"] = t_parts
 

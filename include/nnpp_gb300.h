@@ -396,6 +396,13 @@ nnpp_status nnpp_get_tuning(nnpp_handle* h, int* bins_per_tile, int* lanes_per_n
 nnpp_status nnpp_set_tuning(nnpp_handle* h, int bins_per_tile, int lanes_per_node,
                             int cg_operator);
 
+/* The FP32 transport's form (no counterpart in the reference): 0 (the default, the faster on
+ * a GB300) gathers the bonds' neighbour records from L1/L2; 1 stages each tile's halo
+ * records in shared memory by bulk copies and gathers them there.  Both compute the same
+ * sums in the same order (the same states bit for bit).  NNPP_ERR_UNSUPPORTED for 1 when a
+ * tile halo exceeds a CTA's shared memory. */
+nnpp_status nnpp_set_transport_variant(nnpp_handle* h, int variant);
+
 /* ---- differentiation ------------------------------------------------------------------ */
 
 /* Forward half of a forward/backward pair: from the handle's current state run n_steps

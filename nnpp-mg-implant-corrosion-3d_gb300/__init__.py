@@ -106,6 +106,7 @@ _SIGS = {
     "nnpp_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP, _IP]),
     "nnpp_set_tuning": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "nnpp_set_transport_variant": (C.c_int, [_P, C.c_int]),
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
     "nnpp_set_warm_start": (C.c_int, [_P, C.c_int]),
@@ -475,6 +476,11 @@ class Simulation:
         """Pin the execution configuration instead of autotuning it (cg_operator: 0 L1/L2
         gathers, 1 bulk-copy staged, 2 shared-memory windows)."""
         _check(lib().nnpp_set_tuning(self._h, bins_per_tile, lanes_per_node, int(cg_operator)))
+
+    def set_transport_variant(self, variant):
+        """FP32 transport: 0 neighbour records gathered from L1/L2 (the default), 1 tile
+        halos staged in shared memory; the same sums in the same order."""
+        _check(lib().nnpp_set_transport_variant(self._h, int(variant)))
 
     def state(self):
         c = np.empty((NSPECIES, self.N), dtype=np.float64)

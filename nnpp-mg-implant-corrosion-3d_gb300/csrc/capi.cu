@@ -771,6 +771,21 @@ nnpp_status nnpp_set_checks(nnpp_handle* hp, int flags) {
   return NNPP_OK;
 }
 
+nnpp_status nnpp_set_transport_variant(nnpp_handle* hp, int variant) {
+  NNPP_GUARD(hp);
+  NNPP_NEED_BUILT(hp);
+  if (variant < 0 || variant > kTrVariants - 1)
+    return set_error(NNPP_ERR_INVALID, "set_transport_variant: 0 or 1");
+  Handle& h = hp->h;
+  Engine& e = *h.engine;
+  NNPP_CUDA(cudaStreamSynchronize(h.st));
+  if (variant > 0 && !transport_halo_fits(e))
+    return set_error(NNPP_ERR_UNSUPPORTED, "set_transport_variant: a tile halo exceeds a CTA's shared memory");
+  e.tr_variant = variant;
+  engine_destroy_graphs(e);  // the captured steps launch the previous kernel
+  return NNPP_OK;
+}
+
 nnpp_status nnpp_get_coarse_stats(nnpp_handle* hp, int64_t* rebuilds, int64_t* warm_rebuilds,
                                   int64_t* run_rebuilds, double* run_rebuild_ms, int* last_ns_steps) {
   NNPP_GUARD(hp);

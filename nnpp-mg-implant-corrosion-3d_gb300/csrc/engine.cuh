@@ -105,6 +105,7 @@ struct EngineView {
 constexpr int kChunk = 1024;  // nodes per elementwise work item
 constexpr int kSpmvVariants = 9;  // FP32 CG operator variants the autotuner times
 constexpr int kSpmvHalo = 8;      // the halo-staged variant with recomputed weights
+constexpr int kTrVariants = 2;    // FP32 transport forms (0 L1/L2 gathers, 1 halo staged)
 
 struct Engine {
   std::vector<Handle*> members;
@@ -117,6 +118,8 @@ struct Engine {
                             // 1 bulk-copy staged, 2, 4 shared-memory windows (8, 16),
                             // 5, 6, 7: 4, 3, 2 with L2 prefetch of the operator stream,
                             // 8 tile halo in shared memory, weights recomputed
+  int tr_variant = 0;       // FP32 transport: 0 neighbour records gathered from L1/L2 (the
+                            // faster), 1 the tile's halo records staged in shared memory
   bool halo_op = false;     // every member has the variant 8 layout
   int checks = 0;           // nnpp_set_checks flags of any member (the checked kernels run)
   int hcode_max16 = 0;      // largest tile code block (16-byte units)
@@ -174,6 +177,7 @@ nnpp_status launch_warm_b(const Engine& e, const EngineView& v, int prec, cudaSt
 bool spmv_staged_fits(const Engine& e);
 // the halo-staged variant fits the shared memory of a CTA
 bool spmv_halo_fits(const Engine& e);
+bool transport_halo_fits(const Engine& e);
 // the variant gathers from per-slice shared-memory windows (needs spmv_staged_fits)
 inline bool spmv_needs_windows(int variant) {
   return variant == 1 || variant == 2 || variant == 4 || variant == 5 || variant == 7;

@@ -157,25 +157,25 @@ __device__ __forceinline__ void pair_square(double x, float& h, float& l) {
   l = fmaf(xh, xh, -h) + 2.0f * xh * xl;
 }
 
-// block sums of NV pairs per thread; thread 0 gets the FP64 values (sm: NV * kBlock / 32
+// block sums of NV pairs per thread; thread 0 gets the FP64 values (sm: NV * BLK / 32
 // doubles, used as pairs)
-template <int NV>
+template <int NV, int BLK = kBlock>
 __device__ __forceinline__ void block_pair_sum(float (&h)[NV], float (&l)[NV], double (&out)[NV], double* sm) {
   float2* smf = reinterpret_cast<float2*>(sm);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     pair_warp_sum(h[q], l[q]);
-    if (lane == 0) smf[q * (kBlock / 32) + wid] = make_float2(h[q], l[q]);
+    if (lane == 0) smf[q * (BLK / 32) + wid] = make_float2(h[q], l[q]);
   }
   __syncthreads();
   if (wid == 0) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
       float th = 0.0f, tl = 0.0f;
-      if (lane < kBlock / 32) {
-        th = smf[q * (kBlock / 32) + lane].x;
-        tl = smf[q * (kBlock / 32) + lane].y;
+      if (lane < BLK / 32) {
+        th = smf[q * (BLK / 32) + lane].x;
+        tl = smf[q * (BLK / 32) + lane].y;
       }
       pair_warp_sum(th, tl);
       out[q] = (double)th + (double)tl;
@@ -186,7 +186,7 @@ __device__ __forceinline__ void block_pair_sum(float (&h)[NV], float (&l)[NV], d
 
 // reduce NV pair partials of items [first, first+count) (layout partials[k*stride + item]);
 // four independent pair accumulators per thread, combined in a fixed order
-template <int NV>
+template <int NV, int BLK = kBlock>
 __device__ __forceinline__ void reduce_pair_items(const double* partials, int stride, int first, int count,
                                                   double (&out)[NV], double* sm) {
   constexpr int U = 4;
@@ -199,23 +199,23 @@ __device__ __forceinline__ void reduce_pair_items(const double* partials, int st
 #pragma unroll
     for (int u = 0; u < U; ++u) h[u] = l[u] = 0.0f;
     int b = threadIdx.x;
-    for (; b + (U - 1) * kBlock < count; b += U * kBlock) {
+    for (; b + (U - 1) * BLK < count; b += U * BLK) {
       float2 x[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) x[u] = p[b + u * kBlock];
+      for (int u = 0; u < U; ++u) x[u] = p[b + u * BLK];
 #pragma unroll
       for (int u = 0; u < U; ++u) pair_add(h[u], l[u], x[u].x, x[u].y);
     }
 #pragma unroll
     for (int u = 0; u < U; ++u)
-      if (b + u * kBlock < count) pair_add(h[u], l[u], p[b + u * kBlock].x, p[b + u * kBlock].y);
+      if (b + u * BLK < count) pair_add(h[u], l[u], p[b + u * BLK].x, p[b + u * BLK].y);
     pair_add(h[0], l[0], h[1], l[1]);
     pair_add(h[2], l[2], h[3], l[3]);
     pair_add(h[0], l[0], h[2], l[2]);
     hh[k] = h[0];
     ll[k] = l[0];
   }
-  block_pair_sum<NV>(hh, ll, out, sm);
+  block_pair_sum<NV, BLK>(hh, ll, out, sm);
 }
 
 // the last CTA's reduction of items written by write_dot_partials
@@ -2759,24 +2759,236 @@ __device__ __forceinline__ void ld_rec32(const float4* p, float4& c, float4& t) 
       : "l"(p));
 }
 
-// Mixed transport.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k (utils.h:177) to F_out
-// (single instance) and change nothing; otherwise advance the state into rec32_nxt / clo.
-// Each warp streams 32-row slices of the sliced operator, one lane per node, gathering the
-// neighbours' 32-byte records from L1/L2; the per-node update runs on full warps.  Slice
-// partials of the diagnostics are reduced per instance by the last CTA.
+// Mixed transport of one 32-row slice sg.  RESID: write F_k = sum_KRk1 + sum_KRk2 - R_k
+// (utils.h:177) to F_out (single instance) and change nothing; otherwise advance the state
+// into rec32_nxt / clo and store the slice's diagnostics partials.  One lane per node streams
+// the row's bond columns (codes and weights, column-major: one coalesced load per column) and
+// gathers each neighbour's 32-byte record through rec(i), where i = hb[code >> 12] +
+// (code & 4095) and hb[r] = gbase[r] - radj[r] (radj == nullptr: i is the node).  hb is the
+// warp's 9-int table in shared memory.
 // bond columns per batch of the FP32 transport: with 256-bit record loads 7 (128 registers,
 // 2 CTAs an SM) measured 0.358 ms at 512k against 0.366 for 6 (8 spills); with two 16-byte
 // loads a record 6 took 0.378 ms, 5 0.389, 4 0.405, 2 0.467
 constexpr int kTrB = 7;
+template <bool RESID, int B, bool EARLY, bool PIPE, typename Rec>
+__device__ __forceinline__ void transport_slice(const EngineView& v, int sg, int lane, int* hbw,
+                                                const int* radj, Rec rec, double* F_out) {
+  const SliceDesc& d = v.slices[sg];
+  const KParams& k = v.inst[__ldg(&d.inst)];
+  if (lane < 9) hbw[lane] = __ldg(&d.gbase[lane]) - (radj ? radj[lane] : 0);
+  __syncwarp();
+  float ph_hi[6], ph_lo[6];  // masses[4], solid volume sum, dissolved (FP32 pairs)
+#pragma unroll
+  for (int q = 0; q < 6; ++q) ph_hi[q] = ph_lo[q] = 0.0f;
+  int n_solid = 0, n_bad = 0;
+  const int a = __ldg(&d.row0) + lane;
+  if (lane < __ldg(&d.nrows)) {
+    const float4* rc = reinterpret_cast<const float4*>(k.rec32_cur);
+    const double BV = *k.bv_ptr;
+    float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      cLL[s] = (float)k.DL[s];
+      cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
+      cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
+      K1f[s] = (float)k.K1[s];
+      K2f[s] = (float)k.K2zF[s];
+    }
+    const float4 ca = rc[2 * a];
+    const float4 cb = rc[2 * a + 1];  // phi_hi, phi_lo, phase, pad
+    const float pa = cb.z;
+    // bond coefficient by the neighbour's phase (utils.h:100-153): liquid-liquid D_liquid,
+    // mixed D_solid (BV for Mg), solid-solid D_solid for Mg only
+    float cfL[S], cfS[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      cfL[s] = pa == 0.0f ? cLL[s] : cX[s];
+      cfS[s] = pa == 0.0f ? cX[s] : cSS[s];
+    }
+    float a1[S], a2[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
+    int iface = 0;
+    const float* ws = sell_w(k, d) + lane;
+    const unsigned short* cs = sell_code(k, d) + lane;
+    const int len = k.row[a + 1] - k.row[a];
+    // bonds in batches of B columns: the batch's streamed codes and weights, then its
+    // neighbour records, all in flight before the arithmetic (column order is kept, so the
+    // sums do not depend on the batch size)
+    // PIPE: the next batch's codes and weights are loaded before the current batch's terms
+    float wn[PIPE ? B : 1];
+    unsigned int coden[PIPE ? B : 1];
+    if (PIPE)
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (u < len) {
+          wn[PIPE ? u : 0] = ld_stream(ws + kSellW * u);
+          coden[PIPE ? u : 0] = ld_stream(cs + kSellC * u);
+        }
+    for (int c0 = 0; c0 < len; c0 += B) {
+      float w[B];
+      unsigned int code[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (PIPE) {
+          w[u] = wn[PIPE ? u : 0];
+          code[u] = coden[PIPE ? u : 0];
+        } else if (c0 + u < len) {
+          w[u] = ld_stream(ws + kSellW * (c0 + u));
+          code[u] = ld_stream(cs + kSellC * (c0 + u));
+        }
+      if (PIPE)
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+          if (c0 + B + u < len) {
+            wn[PIPE ? u : 0] = ld_stream(ws + kSellW * (c0 + B + u));
+            coden[PIPE ? u : 0] = ld_stream(cs + kSellC * (c0 + B + u));
+          }
+      // EARLY: the batch's records all in flight before the arithmetic (L1/L2 latency);
+      // otherwise each one just before its bond's terms (shared memory)
+      float4 cn[EARLY ? B : 1], nb[EARLY ? B : 1];
+      if (EARLY)
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+          if (c0 + u < len) rec(code_node(hbw, code[u]), cn[EARLY ? u : 0], nb[EARLY ? u : 0]);
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (c0 + u < len) {
+          const int ur = EARLY ? u : 0;
+          if (!EARLY) rec(code_node(hbw, code[u]), cn[0], nb[0]);
+          const bool nsol = nb[ur].z != 0.0f;
+          const float dphi = (nb[ur].x - cb.x) + (nb[ur].y - cb.y);
+          iface |= (pa != 0.0f && !nsol) ? 1 : 0;
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            const float cw = (nsol ? cfS[s] : cfL[s]) * w[u];
+            const float cns = sel4(cn[ur], s);
+            a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
+            a2[s] = fmaf(cw * cns, dphi, a2[s]);
+          }
+        }
+    }
+    const unsigned char dm = k.dirmask[a];
+    const float4 lo4 = k.clo[a];
+    const bool src_on = iface && !(dm & 1);
+    const double swv = src_on ? dissolve_switch((double)ca.x + (double)lo4.x, k.csat, k.sw) : 0.0;
+    const float Rmg = src_on ? (float)(-k.k_diss * swv) : 0.0f;
+    if (RESID) {
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        F_out[(size_t)s * k.N + a] =
+            -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
+    } else {
+      // c + dt (K1 a1 + K2 a2 + R) on the compensated pair (hi, lo), renormalised: hi is
+      // the FP32 rounding of the exact pair sum and lo its exact remainder
+      const float dtf = (float)k.dt;
+      float hi[S], lo[S];
+      bool bad = false;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
+        float tt, e1, sh, e2;
+        two_sum(sel4(lo4, s), inc, tt, e1);
+        two_sum(sel4(ca, s), tt, sh, e2);
+        two_sum(sh, e1 + e2, hi[s], lo[s]);
+        if ((dm >> s) & 1) {
+          const double x = k.bcval[(size_t)s * k.N + a];
+          hi[s] = (float)x;
+          lo[s] = (float)(x - (double)hi[s]);
+        }
+        // clamp c >= c_floor (main.cpp:805-837), compared on the normalised pairs
+        if (hi[s] < k.cfl_hi || (hi[s] == k.cfl_hi && lo[s] < k.cfl_lo)) {
+          hi[s] = k.cfl_hi;
+          lo[s] = k.cfl_lo;
+        }
+        bad = bad || !isfinite(hi[s]);
+      }
+      float pnew = pa;
+      // saturation test in FP64 (main.cpp:914-922)
+      if (pa != 0.0f && (double)hi[0] + (double)lo[0] <= k.csat) {
+        pnew = 0.0f;
+        k.flip_step[a] = (int)(k.ds->steps + 1);
+        k.flip_list[atomicAdd(&k.ds->nflip, 1)] = a;
+        k.ds->op_valid = 0;
+        k.ds->defl = 0;
+      }
+      record_history(k, a, k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0);
+      const double g = next_phi_guess(k, a);
+      Rec32 out;
+#pragma unroll
+      for (int s = 0; s < S; ++s) out.c[s] = hi[s];
+      out.phi_hi = (float)g;
+      out.phi_lo = (float)(g - (double)out.phi_hi);
+      out.phase = pnew;
+      out.pad = 0.0f;
+      k.rec32_nxt[a] = out;
+      k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+      // diagnostics as FP32 pairs: masses, solid volume sum (c_0 - CSat/CSolid), dissolved
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        ph_hi[s] = hi[s];
+        ph_lo[s] = lo[s];
+      }
+      if (pnew != 0.0f) {
+        n_solid = 1;
+        float vs, ve;
+        two_sum(hi[0], -k.csat_hi, vs, ve);
+        ph_hi[4] = vs;
+        ph_lo[4] = ve + (lo[0] - k.csat_lo);
+      }
+      if (src_on) {
+        const double dv = k.k_diss * swv;
+        ph_hi[5] = (float)dv;
+        ph_lo[5] = (float)(dv - (double)ph_hi[5]);
+      }
+      n_bad = bad ? 1 : 0;
+    }
+  }
+  __syncwarp();
+  if (!RESID) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) pair_warp_sum(ph_hi[q], ph_lo[q]);
+    n_solid = __reduce_add_sync(0xffffffffu, n_solid);
+    n_bad = __reduce_add_sync(0xffffffffu, n_bad);
+    if (lane == 0) {
+      const size_t st = v.stride;
+#pragma unroll
+      for (int s = 0; s < S; ++s) store_pair(v.partials, s * st + sg, ph_hi[s], ph_lo[s]);
+      store_pair(v.partials, 4 * st + sg, (float)n_solid, 0.0f);  // counts <= 32: exact
+      store_pair(v.partials, 5 * st + sg, ph_hi[4], ph_lo[4]);
+      store_pair(v.partials, 6 * st + sg, ph_hi[5], ph_lo[5]);
+      store_pair(v.partials, 7 * st + sg, (float)n_bad, 0.0f);
+      store_pair(v.partials, 8 * st + sg, 0.0f, 0.0f);
+    }
+  }
+}
+
+// the transport's last CTA: every instance's diagnostics from its slices' partials, then
+// the counters' reset
+template <int BLK>
+__device__ __forceinline__ void transport_last_cta(const EngineView& v, double* sm, int* s_last) {
+  if (!take_last_ticket(&v.ticket[v.M + 1], s_last)) return;
+  for (int i = 0; i < v.M; ++i) {
+    double tot[kDiagSlots];
+    reduce_pair_items<kDiagSlots, BLK>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
+    if (threadIdx.x == 0) finish_instance(v.inst[i], tot);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    v.ticket[v.M + 1] = 0;
+    v.ticket[v.M + 2] = 0;
+  }
+}
+
+// Mixed transport, neighbour records gathered from L1/L2.  Warps claim slices one at a time
+// (slices of solid nodes, narrow and partial slices cost less than full ones); the residual
+// form, which has no last CTA to reset the counter, keeps the static split.
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double* F_out) {
   __shared__ int s_hb[kBlock / 32][12];
   __shared__ double sm[kDiagSlots * kBlock / 32];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // warps claim slices one at a time (slices of solid nodes, narrow and partial slices
-  // cost less than full ones); the residual form, which has no last CTA to reset the
-  // counter, keeps the static split
   constexpr bool kClaim = !RESID;
   int s0, s1;
   if (kClaim) {
@@ -2786,187 +2998,84 @@ __global__ void __launch_bounds__(kBlock, 2) k_transport32(EngineView v, double*
     warp_slices(v, &s0, &s1);
   }
   for (int sg = s0; sg < s1; sg = kClaim ? claim_slice(v, lane) : sg + 1) {
-    const SliceDesc d = v.slices[sg];
-    const KParams& k = v.inst[d.inst];
-    if (lane < 9) s_hb[warp][lane] = v.slices[sg].gbase[lane];
-    __syncwarp();
-    float ph_hi[6], ph_lo[6];  // masses[4], solid volume sum, dissolved (FP32 pairs)
-#pragma unroll
-    for (int q = 0; q < 6; ++q) ph_hi[q] = ph_lo[q] = 0.0f;
-    int n_solid = 0, n_bad = 0;
-    const int a = d.row0 + lane;
-    if (lane < d.nrows) {
-      const int* hb = s_hb[warp];
-      const float4* rc = reinterpret_cast<const float4*>(k.rec32_cur);
-      const double BV = *k.bv_ptr;
-      float cLL[S], cX[S], cSS[S], K1f[S], K2f[S];
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        cLL[s] = (float)k.DL[s];
-        cX[s] = (float)(s == 0 ? k.DSo[0] * BV : k.DSo[s]);
-        cSS[s] = s == 0 ? (float)k.DSo[0] : 0.0f;
-        K1f[s] = (float)k.K1[s];
-        K2f[s] = (float)k.K2zF[s];
-      }
-      const float4 ca = rc[2 * a];
-      const float4 cb = rc[2 * a + 1];  // phi_hi, phi_lo, phase, pad
-      const float pa = cb.z;
-      // bond coefficient by the neighbour's phase (utils.h:100-153): liquid-liquid D_liquid,
-      // mixed D_solid (BV for Mg), solid-solid D_solid for Mg only
-      float cfL[S], cfS[S];
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        cfL[s] = pa == 0.0f ? cLL[s] : cX[s];
-        cfS[s] = pa == 0.0f ? cX[s] : cSS[s];
-      }
-      float a1[S], a2[S];
-#pragma unroll
-      for (int s = 0; s < S; ++s) a1[s] = a2[s] = 0.0f;
-      int iface = 0;
-      const float* ws = sell_w(k, d) + lane;
-      const unsigned short* cs = sell_code(k, d) + lane;
-      const int len = k.row[a + 1] - k.row[a];
-      // bonds in batches of kTrB columns: the batch's streamed codes and weights, then its
-      // neighbour records, all in flight before the arithmetic (column order is kept, so the
-      // sums do not depend on the batch size)
-      for (int c0 = 0; c0 < len; c0 += kTrB) {
-        float w[kTrB];
-        unsigned int code[kTrB];
-#pragma unroll
-        for (int u = 0; u < kTrB; ++u)
-          if (c0 + u < len) {
-            w[u] = ld_stream(ws + kSellW * (c0 + u));
-            code[u] = ld_stream(cs + kSellC * (c0 + u));
-          }
-        float4 cn[kTrB], nb[kTrB];
-#pragma unroll
-        for (int u = 0; u < kTrB; ++u)
-          if (c0 + u < len) {
-            const int n = code_node(hb, code[u]);
-            ld_rec32(rc + 2 * n, cn[u], nb[u]);
-          }
-#pragma unroll
-        for (int u = 0; u < kTrB; ++u)
-          if (c0 + u < len) {
-            const bool nsol = nb[u].z != 0.0f;
-            const float dphi = (nb[u].x - cb.x) + (nb[u].y - cb.y);
-            iface |= (pa != 0.0f && !nsol) ? 1 : 0;
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-              const float cw = (nsol ? cfS[s] : cfL[s]) * w[u];
-              const float cns = sel4(cn[u], s);
-              a1[s] = fmaf(cw, cns - sel4(ca, s), a1[s]);
-              a2[s] = fmaf(cw * cns, dphi, a2[s]);
-            }
-          }
-      }
-      const unsigned char dm = k.dirmask[a];
-      const float4 lo4 = k.clo[a];
-      const bool src_on = iface && !(dm & 1);
-      const double swv = src_on ? dissolve_switch((double)ca.x + (double)lo4.x, k.csat, k.sw) : 0.0;
-      const float Rmg = src_on ? (float)(-k.k_diss * swv) : 0.0f;
-      if (RESID) {
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-          F_out[(size_t)s * k.N + a] =
-              -(double)K1f[s] * a1[s] - (double)K2f[s] * a2[s] - (s == 0 ? (double)Rmg : 0.0);
-      } else {
-        // c + dt (K1 a1 + K2 a2 + R) on the compensated pair (hi, lo), renormalised: hi is
-        // the FP32 rounding of the exact pair sum and lo its exact remainder
-        const float dtf = (float)k.dt;
-        float hi[S], lo[S];
-        bool bad = false;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const float inc = dtf * (K1f[s] * a1[s] + K2f[s] * a2[s] + (s == 0 ? Rmg : 0.0f));
-          float tt, e1, sh, e2;
-          two_sum(sel4(lo4, s), inc, tt, e1);
-          two_sum(sel4(ca, s), tt, sh, e2);
-          two_sum(sh, e1 + e2, hi[s], lo[s]);
-          if ((dm >> s) & 1) {
-            const double x = k.bcval[(size_t)s * k.N + a];
-            hi[s] = (float)x;
-            lo[s] = (float)(x - (double)hi[s]);
-          }
-          // clamp c >= c_floor (main.cpp:805-837), compared on the normalised pairs
-          if (hi[s] < k.cfl_hi || (hi[s] == k.cfl_hi && lo[s] < k.cfl_lo)) {
-            hi[s] = k.cfl_hi;
-            lo[s] = k.cfl_lo;
-          }
-          bad = bad || !isfinite(hi[s]);
-        }
-        float pnew = pa;
-        // saturation test in FP64 (main.cpp:914-922)
-        if (pa != 0.0f && (double)hi[0] + (double)lo[0] <= k.csat) {
-          pnew = 0.0f;
-          k.flip_step[a] = (int)(k.ds->steps + 1);
-          k.flip_list[atomicAdd(&k.ds->nflip, 1)] = a;
-          k.ds->op_valid = 0;
-          k.ds->defl = 0;
-        }
-        record_history(k, a, k.hist_m >= 3 ? (k.ds->hist_head + 1) % k.hist_m : 0);
-        const double g = next_phi_guess(k, a);
-        Rec32 out;
-#pragma unroll
-        for (int s = 0; s < S; ++s) out.c[s] = hi[s];
-        out.phi_hi = (float)g;
-        out.phi_lo = (float)(g - (double)out.phi_hi);
-        out.phase = pnew;
-        out.pad = 0.0f;
-        k.rec32_nxt[a] = out;
-        k.clo[a] = make_float4(lo[0], lo[1], lo[2], lo[3]);
-        // diagnostics as FP32 pairs: masses, solid volume sum (c_0 - CSat/CSolid), dissolved
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-          ph_hi[s] = hi[s];
-          ph_lo[s] = lo[s];
-        }
-        if (pnew != 0.0f) {
-          n_solid = 1;
-          float vs, ve;
-          two_sum(hi[0], -k.csat_hi, vs, ve);
-          ph_hi[4] = vs;
-          ph_lo[4] = ve + (lo[0] - k.csat_lo);
-        }
-        if (src_on) {
-          const double dv = k.k_diss * swv;
-          ph_hi[5] = (float)dv;
-          ph_lo[5] = (float)(dv - (double)ph_hi[5]);
-        }
-        n_bad = bad ? 1 : 0;
-      }
-    }
-    __syncwarp();
-    if (!RESID) {
-#pragma unroll
-      for (int q = 0; q < 6; ++q) pair_warp_sum(ph_hi[q], ph_lo[q]);
-      n_solid = __reduce_add_sync(0xffffffffu, n_solid);
-      n_bad = __reduce_add_sync(0xffffffffu, n_bad);
-      if (lane == 0) {
-        const size_t st = v.stride;
-#pragma unroll
-        for (int s = 0; s < S; ++s) store_pair(v.partials, s * st + sg, ph_hi[s], ph_lo[s]);
-        store_pair(v.partials, 4 * st + sg, (float)n_solid, 0.0f);  // counts <= 32: exact
-        store_pair(v.partials, 5 * st + sg, ph_hi[4], ph_lo[4]);
-        store_pair(v.partials, 6 * st + sg, ph_hi[5], ph_lo[5]);
-        store_pair(v.partials, 7 * st + sg, (float)n_bad, 0.0f);
-        store_pair(v.partials, 8 * st + sg, 0.0f, 0.0f);
-      }
-    }
+    const float4* rc = reinterpret_cast<const float4*>(v.inst[__ldg(&v.slices[sg].inst)].rec32_cur);
+    transport_slice<RESID, kTrB, true, false>(v, sg, lane, s_hb[warp], nullptr,
+                                 [rc](int n, float4& c, float4& t) { ld_rec32(rc + 2 * n, c, t); }, F_out);
   }
   if (RESID) return;
-  if (take_last_ticket(&v.ticket[v.M + 1], &s_last)) {
-    for (int i = 0; i < v.M; ++i) {
-      double tot[kDiagSlots];
-      reduce_pair_items<kDiagSlots>(v.partials, v.stride, v.slice_first[i], v.slice_count[i], tot, sm);
-      if (threadIdx.x == 0) finish_instance(v.inst[i], tot);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      v.ticket[v.M + 1] = 0;
-      v.ticket[v.M + 2] = 0;
-    }
+  transport_last_cta<kBlock>(v, sm, &s_last);
+}
+
+// Halo-staged mixed transport.  A CTA claims tiles one at a time; thread 0 copies the tile's
+// halo records (its 9 halo rows: contiguous node ranges, 32-byte records) into shared memory
+// by bulk copies on one mbarrier (a bounded wait: a timeout is recorded in the instance's state
+// and reported as NNPP_ERR_CUDA), then the CTA's warps take the tile's slices and gather
+// every neighbour's record from shared memory (its slot in the halo: the slice's window code
+// rebased from the slice's window rows onto the tile's halo rows).  HBM and L2 see the
+// streamed codes and weights and one copy of each halo; the per-bond gathers stay on chip.
+constexpr int kTrHBlock = 128;
+__host__ __device__ constexpr size_t smem_tr_halo(int halo_max) { return (size_t)halo_max * 32; }
+// largest halo staged: two CTAs of 4 warps an SM at least
+constexpr size_t kTrHaloSmemMax = 110 * 1024;
+
+template <int B, bool PIPE, int MINB>
+__global__ void __launch_bounds__(kTrHBlock, MINB) k_transport32h(EngineView v) {
+  extern __shared__ __align__(16) float4 hrec[];  // 2 float4 a halo node
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_tile, s_stop, s_last;
+  __shared__ int s_adj[9];  // halo row r: first node - its first slot
+  __shared__ int s_hb[kTrHBlock / 32][12];
+  __shared__ double sm[kDiagSlots * kTrHBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    s_stop = 0;
   }
+  __syncthreads();
+  unsigned phase = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = s_stop ? v.ntiles : (int)atomicAdd(&v.ticket[v.M + 2], 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= v.ntiles) break;
+    const TileDesc& td = v.tiles[t];
+    const KParams& k = v.inst[td.inst];
+    if (threadIdx.x == 0) {
+      const float4* rc = reinterpret_cast<const float4*>(k.rec32_cur);
+      unsigned bytes = 0;
+      int acc = 0;
+      for (int r = 0; r < 9; ++r) {
+        s_adj[r] = td.hb[r] - acc;
+        acc += td.hl[r];
+        bytes += (unsigned)td.hl[r] * 32u;
+      }
+      // the previous tile's reads of the buffer come before the copies
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar, bytes);
+      acc = 0;
+      for (int r = 0; r < 9; ++r) {
+        if (td.hl[r] > 0) bulk_g2s(hrec + 2 * acc, rc + 2 * (size_t)td.hb[r], (unsigned)td.hl[r] * 32u, &bar);
+        acc += td.hl[r];
+      }
+    }
+    __syncthreads();
+    if (!mbar_wait_bounded(&bar, phase, kHaloWaitPolls)) {
+      k.ds->wait_timeout = 1;
+      s_stop = 1;
+    }
+    phase ^= 1u;
+    const int nsl = (td.own_end - td.own_begin + 31) >> 5;
+    for (int q = warp; q < nsl; q += kTrHBlock / 32)
+      transport_slice<false, B, false, PIPE>(v, td.slice0 + q, lane, s_hb[warp], s_adj,
+                                    [](int i, float4& c, float4& tt) {
+                                      c = hrec[2 * i];
+                                      tt = hrec[2 * i + 1];
+                                    },
+                                    nullptr);
+    __syncthreads();
+  }
+  transport_last_cta<kTrHBlock>(v, sm, &s_last);
 }
 
 // Next-solve guess of the nodes a transport turned liquid.  As solids they carried no
@@ -3310,6 +3419,18 @@ nnpp_status dispatch_lanes(int lanes, F&& f) {
 }
 
 // Persistent grid: as many CTAs as fit on the device at once (at most one per item).
+template <typename K>
+int occ_grid_b(K kern, int block, size_t smem, int sms, int items) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem) != cudaSuccess) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  if (nb < 1) nb = 1;
+  const int g = sms * nb;
+  return items < g ? (items > 0 ? items : 1) : g;
+}
+
 template <typename K>
 int occ_grid(K kern, size_t smem, int sms, int items) {
   int nb = 0;
@@ -3831,6 +3952,8 @@ nnpp_status prepare_kernels(int H, int B, int lanes) {
     return set_error(NNPP_ERR_UNSUPPORTED, "tile halo too large for shared memory");
   NNPP_TRY(allow_smem(k_cg_spmv32h<false>, 200 * 1024));  // spmv_halo_fits bounds the size used
   NNPP_TRY(allow_smem(k_cg_spmv32h<true>, 200 * 1024));
+  // transport_halo_fits bounds the size used
+  NNPP_TRY(allow_smem(k_transport32h<8, true, 4>, kTrHaloSmemMax));
   return dispatch_lanes(lanes, [&](auto wc) -> nnpp_status {
     constexpr int W = decltype(wc)::value;
     NNPP_TRY(allow_smem(k_prep<float, W>, smem_prep(H, B)));
@@ -3901,6 +4024,11 @@ size_t smem_spmv_halo(int halo_max, int code_max16, int quad_max) {
   return (size_t)(halo_max + 1) * sizeof(float4) + (size_t)halo_zcap(halo_max + 1) * sizeof(float) +
          (size_t)((quad_max + 1) & ~1) * sizeof(float2) + (size_t)code_max16 * 16;
 }
+// the halo-staged transport runs when the largest tile halo fits a CTA's share
+bool transport_halo_fits(const Engine& e) {
+  return e.halo_max > 0 && smem_tr_halo(e.halo_max) <= kTrHaloSmemMax;
+}
+
 // variant 8 runs when every member has its layout, the tiles are at most 8 bins long (the
 // halo-frame coordinates keep ~1e-7 of a bin) and a CTA's halo and code block fit
 bool spmv_halo_fits(const Engine& e) {
@@ -4098,6 +4226,16 @@ nnpp_status launch_ir_update_b(const Engine& e, const EngineView& v, int prec, c
   });
 }
 
+// The halo-staged FP32 transport (form 1): batches of 8 bond columns, the next batch's codes
+// and weights in flight.  Measured at 512k (bins per tile 4, ms a launch): 0.409, against
+// 0.451 / 0.441 without the next batch in flight (batches of 8 / 16), 0.459 / 0.418 with it
+// (16 / 4), 0.51-0.68 with tiles of 2 bins; the L1/L2 gathers of form 0 take 0.358.
+void launch_transport_staged(const EngineView& v, int sms, cudaStream_t st) {
+  const size_t sh = smem_tr_halo(v.halo_max);
+  k_transport32h<8, true, 4><<<occ_grid_b(k_transport32h<8, true, 4>, kTrHBlock, sh, sms, v.ntiles), kTrHBlock, sh,
+                               st>>>(v);
+}
+
 // CTAs of the next-guess pass (a step turns at most a few thousand nodes liquid)
 constexpr int kFlipGuessCtas = 32;
 
@@ -4109,7 +4247,11 @@ nnpp_status launch_transport_b(const Engine& e, const EngineView& v, int prec, c
       if (F_out)
         k_transport32<W, true><<<slice_grid(k_transport32<W, true>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, F_out);
       else {
-        k_transport32<W, false><<<claim_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
+        if (e.tr_variant > 0 && transport_halo_fits(e)) {
+          launch_transport_staged(v, e.sms, st);
+        } else {
+          k_transport32<W, false><<<claim_grid(k_transport32<W, false>, 0, e.sms, v.nslices), kBlock, 0, st>>>(v, nullptr);
+        }
         k_flip_guess<float><<<kFlipGuessCtas, kBlock, 0, st>>>(v);
       }
     } else {

@@ -527,6 +527,39 @@ def test_cg_operator_variants_vs_oracle(gpu, orc, variant):
     assert sim.diagnostics()["cg_not_converged"] == 0
 
 
+@pytest.mark.parametrize("n,T", [(12, 2), (12, 4), (24, 4), (24, 8)])
+def test_transport_variants_give_the_same_bits(gpu, n, T):
+    """The FP32 transport with each tile's halo records staged in shared memory (form 1) and
+    with the records gathered from L1/L2 (0): the same sums in the same order, so the same
+    states bit for bit, at several tile lengths, through a fast dissolution (phases flip on
+    the small lattice)."""
+    nn = gpu
+    inp = nn.synth(1, n, 5)
+    p = inp["params"].copy()
+    p.switch_width = 0.01
+    p.k_diss = 0.1
+    out = []
+    for variant in range(2):
+        sim = nn.Simulation(p, inp["nodes"], inp["bctypes"], inp["bcvalues"], inp["icvalues"], inp["phase0"])
+        sim.build_neighbours()
+        sim.set_tuning(T, 8, 0)
+        sim.set_transport_variant(variant)
+        sim.forward(60, nn.MIXED)
+        out.append((sim.state(), sim.diagnostics()))
+    s0, d0 = out[0]
+    if n == 12:
+        assert d0["solid_count"] < int((np.asarray(inp["phase0"]) != 0).sum())
+    for s1, d1 in out[1:]:
+        for a, b in zip(s0, s1):
+            assert np.array_equal(a, b)
+        assert d0["solid_count"] == d1["solid_count"]
+        assert abs(d0["mg_mass_lost"] - d1["mg_mass_lost"]) <= 1e-12 * abs(d0["mg_mass_lost"])
+    for bad in (-1, 2):
+        with pytest.raises(nn.NNPPError) as e:
+            sim.set_transport_variant(bad)
+        assert e.value.status == 1
+
+
 def test_set_tuning_rejects_bad_configuration(gpu):
     nn = gpu
     inp = nn.synth(1, 12, seed=4)
