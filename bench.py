@@ -522,6 +522,12 @@ def run_ours(args):
     if nn.device_count() < 1:
         raise SystemExit("no CUDA device")
     nn.set_device(local % nn.device_count())
+    if args.chem_only:
+        # the ten-species residual's leg alone (profiling its kernel)
+        if rank == 0:
+            print(json.dumps({"chemistry_10_species": chemistry_cost(nn, max(1, args.chem_reps),
+                                                                     not args.no_cpu_baseline)}), flush=True)
+        return 0
     inp = nn.synth(WORKLOAD["kind"], WORKLOAD["n_side"], WORKLOAD["seed"] + rank)
     N = inp["N"]
     p = inp["params"]
@@ -808,6 +814,8 @@ def main():
                     help="steps run before the dissolving-phase window")
     ap.add_argument("--chem-reps", type=int, default=10,
                     help="timed evaluations of the ten-species residual on the 512k lattice (0: skip)")
+    ap.add_argument("--chem-only", action="store_true",
+                    help="run only the ten-species residual's leg and print its object")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
