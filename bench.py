@@ -423,9 +423,11 @@ def fp64_peak_tflops(torch):
     return 2.0 * 4096 ** 3 / (best / 1e3) / 1e12
 
 
-# FP64 operations of one bond of the complete residual as the kernel forms it (an FMA counts
-# two): offset and length 9, dphi 1, beta dx dy dz and the two weights 3, 1 / xi^3 3, ten
-# species at 8, the potential's bond 4
+# Algorithmic FP64 operations of one bond of the complete residual (an FMA counts two), the
+# terms' constant factors formed once: offset and length 9, dphi 1, beta dx dy dz and the two
+# weights 3, 1 / xi^3 3, ten species at 8 (the difference, each term's product with its
+# weight and its accumulation), the potential's bond 4.  The kernel executes ~81 (each
+# species' factor applied once per node).
 CHEM_FLOPS_PER_BOND = 100
 
 

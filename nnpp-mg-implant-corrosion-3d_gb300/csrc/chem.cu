@@ -17,13 +17,16 @@
 //
 // A thread per node walks its horizon once and carries the 21 bond sums together; each sum
 // still runs over the horizon in the reference's order.  The reference forms every term as
-// K D (U_n - U_i) / xi^(3+2s) beta dx dy dz with a pow and divisions per term; here the
-// constant factors of a term (K_k1 D, K_k2 D z_k F, K11prop1 sigma1, dx dy dz, 1 / (R T)) are
-// multiplied on the host per bond class and species, and a bond forms 1 / xi^e once when all
-// exponents agree (by products when e is whole, as in the reference's data where s = 0), so
-// a term costs two products and a fused multiply-add.  Reordering the products moves each
-// term by a few ulps; the fields agree with the reference to ~1e-15 of their scale.  The
-// powers of ten of the solubility constants and BV are formed on the host with the C
+// K D (U_n - U_i) / xi^(3+2s) beta dx dy dz with a pow and divisions per term.  Here a bond
+// forms 1 / xi from one reciprocal square root and 1 / xi^e by products when all exponents
+// agree and e is whole (s = 0 in the reference's data), else through pow; the constant
+// factors of a term (K_k1 D, K_k2 D z_k F, K11prop1 sigma1, dx dy dz, 1 / (R T)) are formed on
+// the host, and each species' sums run in units of its liquid-liquid factor, which multiplies
+// them once per node (bonds of the other classes carry their factor's ratio to it).  A
+// species then costs a liquid-liquid bond a subtraction, a product and two fused
+// multiply-adds on the FP64 pipe, which bounds the kernel.  Reordering the products moves
+// each term by a few ulps: the fields agree with the reference to ~1e-15 of their scale.
+// The powers of ten of the solubility constants and BV are formed on the host with the C
 // library's pow, as the reference forms them; exp and log at the interface are CUDA's.
 #include <algorithm>
 #include <cmath>
@@ -57,6 +60,10 @@ struct ChemParams {
   // exponents differ or are not whole)
   double dxyz, a1[3][kSp], a2[3][kSp], KS11;
   int ie, one_exp;
+  // the bond sums' factors: sg = the liquid-liquid factor (1 where it is zero), on = it is
+  // not zero, q[0] / q[1] = the liquid-solid / solid-solid factor over sg
+  double sg1[kSp], sg2[kSp], q1[2][kSp], q2[2][kSp];
+  int on1[kSp], on2[kSp];
 };
 
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
@@ -73,17 +80,18 @@ __device__ __forceinline__ double ca5ohpo4(double a, double u8, double u7) {
   return t;
 }
 
-// 1 / xi^e: by repeated products when e is a small whole number (ie > 0), else through pow
-__device__ __forceinline__ double rpow(double xi, double e, int ie) {
+// 1 / xi^e from rs = 1 / xi: by repeated products when e is a small whole number (ie > 0),
+// else through pow
+__device__ __forceinline__ double rpow(double rs, double xi, double e, int ie) {
   if (ie > 0) {
-    double p = xi;
-    for (int q = 1; q < ie; ++q) p = mul(p, xi);
-    return dvd(1.0, p);
+    double p = rs;
+    for (int q = 1; q < ie; ++q) p = mul(p, rs);
+    return p;
   }
   return dvd(1.0, pow(xi, e));
 }
 
-template <bool kOneExp>
+template <bool kOneExp, bool kAllOn>
 __global__ void k_residuals_full(ChemParams c, int N, const double* __restrict__ xyz, const int* __restrict__ hz,
                                  const int* __restrict__ hl, const double* __restrict__ Un1,
                                  const double* __restrict__ Un, const int* __restrict__ phase,
@@ -100,10 +108,13 @@ __global__ void k_residuals_full(ChemParams c, int N, const double* __restrict__
           iface = 1;
           break;
         }
-    double s1[kSp], s2[kSp], ui[kSp], s11 = 0.0;
+    // S1, S2: the bond sums in units of the species' liquid-liquid factors (sg1, sg2): a
+    // liquid-liquid bond adds w (U_n - U_i) and v U_n dphi, other bonds the same scaled by
+    // their class's factor over the liquid-liquid one
+    double S1[kSp], S2[kSp], ui[kSp], S11 = 0.0;
 #pragma unroll
     for (int k = 0; k < kSp; ++k) {
-      s1[k] = s2[k] = 0.0;
+      S1[k] = S2[k] = 0.0;
       ui[k] = Un1[(size_t)k * N + i];
     }
     int flag = 0;
@@ -112,38 +123,60 @@ __global__ void k_residuals_full(ChemParams c, int N, const double* __restrict__
     for (int j = 1; j < len; ++j) {
       const int n = hz[(size_t)j * N + i];
       const double ex = sub(xyz[n], xi0), ey = sub(xyz[N + n], yi0), ez = sub(xyz[2 * N + n], zi0);
-      const double xi = __dsqrt_rn(fma(ex, ex, fma(ey, ey, mul(ez, ez))));
+      const double x2 = fma(ex, ex, fma(ey, ey, mul(ez, ez)));
+      const double rs = rsqrt(x2);  // 1 / xi
+      const double xi = mul(x2, rs);
       const double beta = beta_fn<double>(xi, c.delta, c.dx);
       const int pn = phase[n];
       const bool ss = pi == 1 && pn == 1, ll = pi == 0 && pn == 0;
+      const int cls = ss ? 1 : 0;  // the factors of a bond that is not liquid-liquid
       const double dphi = sub(Un[(size_t)kSp * N + n], phi_i);
       // the bond's beta dx dy dz, and 1 / (R T) for the migration terms
       const double bd = mul(beta, c.dxyz);
-      const double bdr = mul(bd, rRT);
       double w1 = 0.0, v2 = 0.0;
       if (kOneExp) {
-        w1 = mul(rpow(xi, c.e1[0], c.ie), bd);
+        w1 = mul(rpow(rs, xi, c.e1[0], c.ie), bd);
         v2 = mul(w1, rRT);
       }
+      if (ll) {
+        // liquid-liquid: the sums' own units (ON: a species whose liquid-liquid factor is
+        // zero takes nothing here)
 #pragma unroll
-      for (int k = 0; k < kSp; ++k) {
-        if (k > 0 && ss) continue;  // solid-solid bonds carry only Mg
-        if (!kOneExp) {
-          w1 = mul(rpow(xi, c.e1[k], 0), bd);
-          v2 = mul(rpow(xi, c.e2[k], 0), bdr);
+        for (int k = 0; k < kSp; ++k) {
+          if (!kOneExp) {
+            w1 = mul(rpow(rs, xi, c.e1[k], 0), bd);
+            v2 = mul(mul(rpow(rs, xi, c.e2[k], 0), bd), rRT);
+          }
+          const double un = Un1[(size_t)k * N + n];
+          if (kAllOn || c.on1[k]) S1[k] = fma(w1, sub(un, ui[k]), S1[k]);
+          if (kAllOn || c.on2[k]) S2[k] = fma(v2, mul(un, dphi), S2[k]);
         }
-        const double a1 = ll ? c.a1[0][k] : ss ? c.a1[2][k] : c.a1[1][k];
-        const double a2 = ll ? c.a2[0][k] : ss ? c.a2[2][k] : c.a2[1][k];
-        const double un = Un1[(size_t)k * N + n];
-        s1[k] = fma(-mul(a1, w1), sub(un, ui[k]), s1[k]);
-        s2[k] = fma(-mul(a2, v2), mul(un, dphi), s2[k]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kSp; ++k) {
+          if (k > 0 && ss) continue;  // solid-solid bonds carry only Mg
+          if (!kOneExp) {
+            w1 = mul(rpow(rs, xi, c.e1[k], 0), bd);
+            v2 = mul(mul(rpow(rs, xi, c.e2[k], 0), bd), rRT);
+          }
+          const double un = Un1[(size_t)k * N + n];
+          S1[k] = fma(mul(w1, c.q1[cls][k]), sub(un, ui[k]), S1[k]);
+          S2[k] = fma(mul(v2, c.q2[cls][k]), mul(un, dphi), S2[k]);
+        }
       }
       if (ll) {
-        const double w11 = kOneExp ? w1 : mul(rpow(xi, c.e11, 0), bd);
-        s11 = fma(-c.KS11, mul(sub(Un1[(size_t)kSp * N + n], phi1_i), w11), s11);
+        const double w11 = kOneExp ? w1 : mul(rpow(rs, xi, c.e11, 0), bd);
+        S11 = fma(w11, sub(Un1[(size_t)kSp * N + n], phi1_i), S11);
         flag = 1;
       }
     }
+    double s1[kSp], s2[kSp];
+#pragma unroll
+    for (int k = 0; k < kSp; ++k) {
+      s1[k] = -mul(c.sg1[k], S1[k]);
+      s2[k] = -mul(c.sg2[k], S2[k]);
+    }
+    const double s11 = -mul(c.KS11, S11);
     // the fields' values at the node
     double u1[kSp], u0[kSp];
 #pragma unroll
@@ -288,6 +321,16 @@ ChemParams make_chem_params(const double* d2, const double* dc, const double* d1
     c.a2[2][k] = k == 0 ? c.K2[k] * c.Ds[k] * c.z[k] * c.F : 0.0;
   }
   c.KS11 = c.K11 * c.sigma1;
+  for (int k = 0; k < kSp; ++k) {
+    c.on1[k] = c.a1[0][k] != 0.0;
+    c.on2[k] = c.a2[0][k] != 0.0;
+    c.sg1[k] = c.on1[k] ? c.a1[0][k] : 1.0;
+    c.sg2[k] = c.on2[k] ? c.a2[0][k] : 1.0;
+    for (int q = 0; q < 2; ++q) {
+      c.q1[q][k] = c.a1[q + 1][k] / c.sg1[k];
+      c.q2[q][k] = c.a2[q + 1][k] / c.sg2[k];
+    }
+  }
   c.one_exp = c.e11 == c.e1[0];
   for (int k = 0; k < kSp; ++k) c.one_exp = c.one_exp && c.e1[k] == c.e1[0] && c.e2[k] == c.e1[0];
   c.ie = 0;
@@ -316,12 +359,15 @@ nnpp_status nnpp_residuals_full_device(int n_nodes, const double* d_nodes, const
     return set_error(NNPP_ERR_INVALID, "residuals_full: dt, dx or K11prop1 sigma1 is zero");
   const int blocks = std::max(1, std::min((n_nodes + 127) / 128, 152 * 16));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  bool all_on = true;
+  for (int k = 0; k < kSp; ++k) all_on = all_on && c.on1[k] && c.on2[k];
+  auto go = [&](auto kern) {
+    kern<<<blocks, 128, 0, st>>>(c, n_nodes, d_nodes, d_clouds, d_lengths, d_U_n1, d_U_n, d_phase, d_F);
+  };
   if (c.one_exp)
-    k_residuals_full<true><<<blocks, 128, 0, st>>>(c, n_nodes, d_nodes, d_clouds, d_lengths, d_U_n1, d_U_n, d_phase,
-                                                   d_F);
+    all_on ? go(k_residuals_full<true, true>) : go(k_residuals_full<true, false>);
   else
-    k_residuals_full<false><<<blocks, 128, 0, st>>>(c, n_nodes, d_nodes, d_clouds, d_lengths, d_U_n1, d_U_n, d_phase,
-                                                    d_F);
+    all_on ? go(k_residuals_full<false, true>) : go(k_residuals_full<false, false>);
   NNPP_CUDA(cudaGetLastError());
   return NNPP_OK;
 }

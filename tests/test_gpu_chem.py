@@ -110,3 +110,20 @@ def test_residuals_full_general_exponents(gpu, orc, gold):
     ptr, cols = _oracle_clouds(clouds, lengths, ml)
     Fr = orc.residuals_full(nodes, ptr, cols, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
     _assert_close(F, Fr)
+
+
+def test_residuals_full_species_without_liquid_diffusion(gpu, orc, gold):
+    """A species whose liquid diffusivity is zero (its liquid-liquid bonds carry nothing, the
+    others still do): the kernel's per-class factors against the oracle's."""
+    nn = gpu
+    dc = gold["datac"].copy()
+    dc[3, 2] = 0.0   # D_liquid of species 4
+    dc[6, 6] = 0.0   # K_7prop2: species 7 without migration
+    d2 = chem_case.reactive_data2(gold["data2"])
+    nodes, phase, Un1, Un, r, cell = chem_case.case_inputs(nn.synth, 1, 16, 4, gold["data2"])
+    clouds, lengths, ml = nn.build_clouds_hash(1024, r, cell, cell, cell, nodes)
+    F = nn.residuals_full(nodes, clouds[:, :ml], lengths, Un1, Un, phase, chem_case.VOLN1REL, d2, dc,
+                          gold["datac11"])
+    ptr, cols = _oracle_clouds(clouds, lengths, ml)
+    Fr = orc.residuals_full(nodes, ptr, cols, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, gold["datac11"])
+    _assert_close(F, Fr)
