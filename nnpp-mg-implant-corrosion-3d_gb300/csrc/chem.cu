@@ -260,6 +260,19 @@ __global__ void k_residuals_full(ChemParams c, int N, const double* __restrict__
   }
 }
 
+// every neighbour index of the first len[i] cloud columns names a node (flag set otherwise)
+__global__ void k_check_clouds(int N, const int* __restrict__ hz, const int* __restrict__ hl, int* flag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const int len = hl[i];
+    bool bad = false;
+    for (int j = 0; j < len; ++j) {
+      const int n = hz[(size_t)j * N + i];
+      bad = bad || n < 0 || n >= N;
+    }
+    if (bad) atomicExch(flag, 1);
+  }
+}
+
 ChemParams make_chem_params(const double* d2, const double* dc, const double* d11, double voln1rel) {
   ChemParams c;
   c.dt = d2[2];
@@ -392,16 +405,12 @@ nnpp_status nnpp_residuals_full(int n_nodes, const double* nodes_colmajor, const
     if (l < 1 || l > max_node_no) return set_error(NNPP_ERR_INVALID, "residuals_full: cloud length out of range");
     ml = std::max(ml, l);
   }
-  // only the first ml columns of the clouds matter; every index must name a node
-  for (size_t i = 0; i < N; ++i)
-    for (int j = 0; j < cloud_lengths[i]; ++j) {
-      const int n = clouds_colmajor[(size_t)j * N + i];
-      if (n < 0 || (size_t)n >= N) return set_error(NNPP_ERR_INVALID, "residuals_full: cloud index out of range");
-    }
+  // only the first ml columns of the clouds matter; every index must name a node (checked on
+  // the device after the copy, before the residual runs)
   DBuf<double> dx, du1, du0, df;
-  DBuf<int> dhz, dhl, dph;
+  DBuf<int> dhz, dhl, dph, dflag;
   if (!dx.alloc(3 * N) || !du1.alloc((kSp + 1) * N) || !du0.alloc((kSp + 1) * N) || !df.alloc((kSp + 1) * N) ||
-      !dhz.alloc((size_t)ml * N) || !dhl.alloc(N) || !dph.alloc(N))
+      !dhz.alloc((size_t)ml * N) || !dhl.alloc(N) || !dph.alloc(N) || !dflag.alloc(1))
     return set_error(NNPP_ERR_NOMEM, "residuals_full buffers");
   cudaStream_t st = nullptr;
   NNPP_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -415,6 +424,14 @@ nnpp_status nnpp_residuals_full(int n_nodes, const double* nodes_colmajor, const
   NNPP_CUDA(cudaMemcpyAsync(dhz.get(), clouds_colmajor, sizeof(int) * (size_t)ml * N, cudaMemcpyHostToDevice, st));
   NNPP_CUDA(cudaMemcpyAsync(dhl.get(), cloud_lengths, sizeof(int) * N, cudaMemcpyHostToDevice, st));
   NNPP_CUDA(cudaMemcpyAsync(dph.get(), phase, sizeof(int) * N, cudaMemcpyHostToDevice, st));
+  NNPP_CUDA(cudaMemsetAsync(dflag.get(), 0, sizeof(int), st));
+  k_check_clouds<<<std::max(1, std::min((n_nodes + 255) / 256, 152 * 16)), 256, 0, st>>>(n_nodes, dhz.get(), dhl.get(),
+                                                                                      dflag.get());
+  NNPP_CUDA(cudaGetLastError());
+  int bad = 0;
+  NNPP_CUDA(cudaMemcpyAsync(&bad, dflag.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+  NNPP_CUDA(cudaStreamSynchronize(st));
+  if (bad) return set_error(NNPP_ERR_INVALID, "residuals_full: cloud index out of range");
   NNPP_TRY(nnpp_residuals_full_device(n_nodes, dx.get(), dhz.get(), dhl.get(), du1.get(), du0.get(), dph.get(),
                                       voln1rel, data2, datac, datac11, df.get(), st));
   NNPP_CUDA(cudaMemcpyAsync(F, df.get(), sizeof(double) * (kSp + 1) * N, cudaMemcpyDeviceToHost, st));

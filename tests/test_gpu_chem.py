@@ -127,3 +127,17 @@ def test_residuals_full_species_without_liquid_diffusion(gpu, orc, gold):
     ptr, cols = _oracle_clouds(clouds, lengths, ml)
     Fr = orc.residuals_full(nodes, ptr, cols, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, gold["datac11"])
     _assert_close(F, Fr)
+
+
+def test_residuals_full_512k_matches_oracle(gpu, orc, gold):
+    """The benchmark's chemistry workload itself (the 80^3 lattice, 512,000 nodes, 53.9M bonds,
+    the reference's physical constants) against the oracle's restatement."""
+    nn = gpu
+    d2, dc, d11 = gold["data2"], gold["datac"], gold["datac11"]
+    nodes, phase, Un1, Un, r, cell = chem_case.case_inputs(nn.synth, 1, 80, 1, d2)
+    clouds, lengths, ml = nn.build_clouds_hash(160, r, cell, cell, cell, nodes)
+    F = nn.residuals_full(nodes, clouds[:, :ml], lengths, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
+    ptr, cols = _oracle_clouds(clouds, lengths, ml)
+    del clouds
+    Fr = orc.residuals_full(nodes, ptr, cols, Un1, Un, phase, chem_case.VOLN1REL, d2, dc, d11)
+    _assert_close(F, Fr)
