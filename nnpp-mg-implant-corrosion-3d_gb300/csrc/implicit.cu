@@ -8,7 +8,8 @@
 //              1/dt + sum K1 D(BV) w; the potential K11 (utils.h:1797-1848) -w on
 //              liquid-liquid bonds, their sum on the diagonal; Dirichlet rows (and potential
 //              rows without liquid-liquid bonds) identity; w = beta dV / xi^3.
-//   Newton     F = Residuals(U^{n+1}, U^n) with the migration on phi^n (utils.h:126) and
+//   Newton     F = Residuals(U^{n+1}, U^n) with the migration on phi^n (utils.h:126), F11's
+//              charge from U^n (utils.h:829-831), and
 //              F = U - bc on Dirichlet rows (main.cpp:676-712); K_f dU_f = -F_f by GMRES for
 //              the S species and the potential at once (five independent Krylov solves
 //              advanced together: one gather of a bond serves all five); U += dU; the clamp
@@ -177,10 +178,11 @@ __global__ void k_imp_residual(ImpCtx c, const double* u1, double* F) {
         if (c.dir[(size_t)k * N + i]) f = ci[k] - c.bc[(size_t)k * N + i];
         F[(size_t)k * N + i] = f;
       }
+      // F11 from phi^{n+1} and the charge of U^n (utils.h:829-831)
       double f11 = 0.0;
       if (ll) {
         double r11 = 0.0;
-        for (int k = 0; k < S; ++k) r11 += c.z[k] * ci[k];
+        for (int k = 0; k < S; ++k) r11 += c.z[k] * c.u0[(size_t)k * N + i];
         f11 = (1.0 / c.kphis) * sp - c.lam * r11;
       }
       if (c.dir[(size_t)S * N + i]) f11 = phi1[i] - c.bc[(size_t)S * N + i];

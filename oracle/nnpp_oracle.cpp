@@ -801,14 +801,15 @@ constexpr int kNewtonMaxIter = 200;
 
 // Residual of the implicit step (utils.h:72-178, 181-257, 798-841 with U^{n+1} = c1, phi1 and
 // U^n = c0, phi0): the time term (c1 - c0) / dt, the bond sums at c1 with the migration
-// potential phi0, the dissolution source at c1; F11 at (c1, phi1).
+// potential phi0, the dissolution source at c1; F11 from the potential phi1 and the charge
+// of U^n (utils.h:829-831: R11 = z1 U1n + ... + z10 U10n).
 void residuals_implicit(const Oracle& o, const double* c1, const double* phi1, const double* c0,
                         const double* phi0, const int* phase, double voln1rel, double* F) {
   residuals(o, c1, phi0, phase, voln1rel, F, nullptr, nullptr);
   const int N = o.N;
   std::vector<double> F11(F + (int64_t)S * N, F + (int64_t)(S + 1) * N);
   std::vector<double> tmp((int64_t)(S + 1) * N);
-  residuals(o, c1, phi1, phase, voln1rel, tmp.data(), nullptr, nullptr);
+  residuals(o, c0, phi1, phase, voln1rel, tmp.data(), nullptr, nullptr);
 #pragma omp parallel for
   for (int i = 0; i < N; ++i) {
     for (int k = 0; k < S; ++k) {
@@ -1298,6 +1299,14 @@ int orc_implant_counts(int N, const double* nodes, int M, const double* points, 
     }
     counts[i] = cnt;
   }
+  return 0;
+}
+
+// the implicit step's residual at (c1, phi1) from U^n = (c0, phi0) with the given phases
+int orc_residuals_implicit(void* h, const double* c1, const double* phi1, const double* c0, const double* phi0,
+                           const int* phase, double voln1rel, double* F) {
+  if (!h || !c1 || !phi1 || !c0 || !phi0 || !phase || !F) return 1;
+  residuals_implicit(*static_cast<Oracle*>(h), c1, phi1, c0, phi0, phase, voln1rel, F);
   return 0;
 }
 

@@ -66,6 +66,7 @@ def load_oracle():
             "orc_get_diag": (C.c_int, [_P, _DP]),
             "orc_implant_counts": (C.c_int, [C.c_int, _DP, C.c_int, _DP, C.c_double, _IP]),
             "orc_implicit_forward": (C.c_int, [_P, C.c_int, _LP, _LP]),
+            "orc_residuals_implicit": (C.c_int, [_P, _DP, _DP, _DP, _DP, _IP, C.c_double, _DP]),
             "orc_tangent": (C.c_int, [_P, C.c_int, _DP, _DP]),
             "orc_tangent_gmres": (C.c_int, [_P, C.c_int, _DP, _DP, C.c_double, C.c_int, C.c_int]),
             "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
@@ -240,6 +241,15 @@ class Oracle:
         phase = np.ascontiguousarray(phase, dtype=np.int32)
         F = np.empty((NSPECIES + 1, self.N))
         load_oracle().orc_residuals(self._h, _dp(c), _dp(phi), _ip(phase), voln1rel, _dp(F))
+        return F
+
+    def residuals_implicit(self, c1, phi1, c0, phi0, phase, voln1rel=0.0):
+        """The implicit step's residual (5, N) at U^{n+1} = (c1, phi1) from U^n = (c0, phi0)."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (c1, phi1, c0, phi0)]
+        phase = np.ascontiguousarray(phase, dtype=np.int32)
+        F = np.empty((NSPECIES + 1, self.N))
+        load_oracle().orc_residuals_implicit(self._h, _dp(a[0]), _dp(a[1]), _dp(a[2]), _dp(a[3]), _ip(phase),
+                                             voln1rel, _dp(F))
         return F
 
     def poisson_matrix(self, phase):
