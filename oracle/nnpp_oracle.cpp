@@ -1053,6 +1053,172 @@ int implicit_step(Oracle& o, ImplicitStats* st) {
   return 0;
 }
 
+// ------------------------------------------------ the complete model's implicit step -----
+// The reference's time step with all eleven fields (main.cpp:640-922): the tangents of
+// utils::NewtonMatrices (utils.h:846-1849) once at U^n, then Newton iterations on
+// utils::Residuals (utils.h:29-842, residuals_full above) with the Dirichlet rows of
+// main.cpp:676-712, eleven Eigen::GMRES corrections (gmres above), the update, the clamp of
+// main.cpp:805-837 (U10 on liquid nodes only) and the update-norm test; then the flip of
+// main.cpp:914-922.  Parameters as the reference's data files hold them (data2, datac rows
+// z, D_solid, D_liquid, s_k1, s_k2, K_kprop1, K_kprop2, datac11).
+
+// tangent of species k (Mg utils.h:900-1010; H+ 1012-1102; species 3-10 1104-1792): the
+// off-diagonal and sum_K of species_tangent with the species' own constants; the diagonal
+// 1/dt - sum_K - R_k with the linearised reaction terms at U^n (H+ on interface and liquid
+// nodes, species 3, 4, 5 and 7 on liquid nodes, none for the others)
+void chem_species_tangent(const Oracle& o, int k, const double* Un, const int* phase, const unsigned char* dir,
+                          double voln1rel, const double* d2, const double* dc, std::vector<double>& diag,
+                          std::vector<double>& off) {
+  const int N = o.N;
+  const double dt = d2[2], dx = d2[3], dy = d2[4], dz = d2[5], delta = d2[6];
+  const double T = d2[47], R = d2[48], Fc = d2[49], vol_red = d2[50];
+  const double k7b = d2[41], k8b = d2[43], k9b = d2[45];
+  const double z = dc[7 * k], Ds = dc[7 * k + 1], Dl = dc[7 * k + 2], s1 = dc[7 * k + 3], s2 = dc[7 * k + 4];
+  const double K1 = dc[7 * k + 5], K2 = dc[7 * k + 6];
+  const double BVmix = std::pow(10., -vol_red * (1. - voln1rel));
+  auto U = [&](int f, int i) { return Un[(int64_t)f * N + i]; };
+  diag.assign(N, 1.0);
+  off.assign(o.cols.size(), 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    if (dir[i]) continue;
+    const int pi = phase[i];
+    int iface = 0;
+    if (pi == 1)
+      for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j)
+        if (phase[o.cols[j]] == 0) {
+          iface = 1;
+          break;
+        }
+    double sumK = 0.0;
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) {
+      const int n = o.cols[j];
+      const int pn = phase[n];
+      double D, BV = 1.0;
+      if (k == 0) {
+        if ((pi == 1 && pn == 0) || (pn == 1 && pi == 0)) BV = BVmix;
+        D = (pi == 0 && pn == 0) ? Dl : Ds;
+      } else {
+        if (pi == 1 && pn == 1) continue;
+        D = (pi == 0 && pn == 0) ? Dl : Ds;
+      }
+      const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+      const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+      const double bt = beta_fn(xi, delta, dx);
+      const double dphi = U(10, n) - U(10, i);
+      if (k == 0) {
+        sumK += -(K1 * D * BV / std::pow(xi, 3.0 + 2.0 * s1)) * bt * dx * dy * dz;
+        off[j] = -((K1 * D * BV / std::pow(xi, 3.0 + 2.0 * s1)) +
+                   (K2 * D * BV * z * Fc / (R * T) * dphi / std::pow(xi, 3.0 + 2.0 * s2))) *
+                 bt * dx * dy * dz;
+      } else {
+        sumK += -(K1 * D / std::pow(xi, 3.0 + 2.0 * s1)) * bt * dx * dy * dz;
+        off[j] = -((K1 * D / std::pow(xi, 3.0 + 2.0 * s1)) +
+                   (K2 * D * z * Fc / (R * T) * dphi / std::pow(xi, 3.0 + 2.0 * s2))) *
+                 bt * dx * dy * dz;
+      }
+    }
+    const bool liq = pi == 0;
+    double Rk = 0.0;
+    if (k == 1 && (iface || liq))
+      Rk = k7b * (-U(2, i)) + k8b * (-U(4, i)) + k9b * (-U(6, i));
+    else if (k == 2 && liq)
+      Rk = k7b * (-U(1, i));
+    else if ((k == 3 || k == 4) && liq)
+      Rk = k8b * (-U(1, i));
+    else if (k == 6 && liq)
+      Rk = k9b * (-U(1, i));
+    diag[i] = (1. / dt) - sumK - Rk;
+  }
+}
+
+// K11 (utils.h:1794-1848) with datac11's constants: off-diagonal
+// -(1/(K sigma)) (K sigma / xi^(3+2s)) beta dV on liquid-liquid bonds, diagonal
+// -(1/(K sigma)) sum_K; identity rows on Dirichlet nodes and nodes without such bonds
+void chem_potential_tangent(const Oracle& o, const int* phase, const unsigned char* dir, const double* d2,
+                            const double* d11, std::vector<double>& diag, std::vector<double>& off) {
+  const int N = o.N;
+  const double dx = d2[3], dy = d2[4], dz = d2[5], delta = d2[6];
+  const double sigma1 = d11[1], s111 = d11[2], K11 = d11[3];
+  diag.assign(N, 1.0);
+  off.assign(o.cols.size(), 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < N; ++i) {
+    if (dir[i]) continue;
+    double sumK = 0.0;
+    int flag = 0;
+    for (int64_t j = o.row_ptr[i] + 1; j < o.row_ptr[i + 1]; ++j) {
+      const int n = o.cols[j];
+      if (!(phase[i] == 0 && phase[n] == 0)) continue;
+      const double xix = o.x[n] - o.x[i], xiy = o.y[n] - o.y[i], xiz = o.z[n] - o.z[i];
+      const double xi = std::sqrt(xix * xix + xiy * xiy + xiz * xiz);
+      const double bt = beta_fn(xi, delta, dx);
+      sumK += -(K11 * sigma1 / std::pow(xi, 3.0 + 2.0 * s111)) * bt * dx * dy * dz;
+      off[j] = -(1. / (K11 * sigma1)) * (K11 * sigma1 / std::pow(xi, 3.0 + 2.0 * s111)) * bt * dx * dy * dz;
+      flag = 1;
+    }
+    diag[i] = flag ? -(1. / (K11 * sigma1)) * sumK : 1.0;
+  }
+}
+
+// One step from U (11 N, U^n in, U^{n+1} out) and phase (updated by the flip); dir (11 N)
+// the Dirichlet flags, bcv (11 N) the raw boundary values.  Returns the Newton iterations.
+int chem_implicit_step(const Oracle& o, double* U, int* phase, const unsigned char* dir, const double* bcv,
+                       double voln1rel, const double* d2, const double* dc, const double* d11,
+                       int64_t* krylov) {
+  const int N = o.N;
+  const int NF = 11;
+  const double CSolid = d2[7], CSat = d2[8];
+  std::vector<double> u0(U, U + (int64_t)NF * N), u1 = u0, F((int64_t)NF * N), dU((int64_t)NF * N), rhs(N);
+  std::vector<double> xyz((int64_t)3 * N);
+  std::copy(o.x.begin(), o.x.end(), xyz.begin());
+  std::copy(o.y.begin(), o.y.end(), xyz.begin() + N);
+  std::copy(o.z.begin(), o.z.end(), xyz.begin() + 2 * (int64_t)N);
+  // the tangents once per step (main.cpp:657-662)
+  std::vector<double> diag[11], off[11];
+  for (int k = 0; k < 10; ++k)
+    chem_species_tangent(o, k, u0.data(), phase, dir + (int64_t)k * N, voln1rel, d2, dc, diag[k], off[k]);
+  chem_potential_tangent(o, phase, dir + (int64_t)10 * N, d2, d11, diag[10], off[10]);
+  double res_old[11] = {0.0};
+  const double floor_c = 1.0e-8 / CSolid;
+  int it = 0;
+  for (it = 0; it < kNewtonMaxIter; ++it) {
+    residuals_full(N, xyz.data(), o.row_ptr.data(), o.cols.data(), u1.data(), u0.data(), phase, voln1rel, d2, dc,
+                   d11, F.data());
+    for (int f = 0; f < NF; ++f)
+      for (int i = 0; i < N; ++i)
+        if (dir[(int64_t)f * N + i])
+          F[(int64_t)f * N + i] =
+              u1[(int64_t)f * N + i] - (f < 10 ? bcv[(int64_t)f * N + i] / CSolid : bcv[(int64_t)f * N + i]);
+    double res[11];
+    for (int f = 0; f < NF; ++f) {
+      for (int i = 0; i < N; ++i) rhs[i] = -F[(int64_t)f * N + i];
+      const int kit = gmres(o, diag[f], off[f], rhs.data(), dU.data() + (int64_t)f * N, kNewtonEps, 30,
+                            kNewtonMaxIter);
+      if (krylov) *krylov += kit;
+    }
+    for (int f = 0; f < NF; ++f) {
+      for (int i = 0; i < N; ++i) u1[(int64_t)f * N + i] += dU[(int64_t)f * N + i];
+      res[f] = norm2(dU.data() + (int64_t)f * N, N);
+    }
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < 10; ++k)
+        if (u1[(int64_t)k * N + i] < floor_c && (k < 9 || phase[i] == 0)) u1[(int64_t)k * N + i] = floor_c;
+    double resMax = 0.0;
+    for (int f = 0; f < NF; ++f) resMax = std::max(resMax, std::abs(res[f] - res_old[f]));
+    if (resMax < kNewtonEps) {
+      ++it;
+      break;
+    }
+    for (int f = 0; f < NF; ++f) res_old[f] = res[f];
+  }
+  std::copy(u1.begin(), u1.end(), U);
+  const double csat = CSat / CSolid;
+  for (int i = 0; i < N; ++i)
+    if (phase[i] == 1 && U[i] <= csat) phase[i] = 0;
+  return it;
+}
+
 extern "C" {
 
 int orc_residuals_full(int N, const double* nodes, const int64_t* row_ptr, const int* cols, const double* Un1,
@@ -1299,6 +1465,39 @@ int orc_implant_counts(int N, const double* nodes, int M, const double* points, 
     }
     counts[i] = cnt;
   }
+  return 0;
+}
+
+// one step of the complete model (chem_implicit_step); dir flags from bct (N) and bcv (11 N):
+// bct == 0 and bcv != -1.  Returns the Newton iterations (negative on a bad argument).
+int orc_chem_implicit_step(void* h, double* U, int* phase, const int* bct, const double* bcv, double voln1rel,
+                           const double* d2, const double* dc, const double* d11, int64_t* krylov) {
+  if (!h || !U || !phase || !bct || !bcv || !d2 || !dc || !d11) return -1;
+  const Oracle& o = *static_cast<Oracle*>(h);
+  const int N = o.N;
+  std::vector<unsigned char> dir((int64_t)11 * N, 0);
+  for (int f = 0; f < 11; ++f)
+    for (int i = 0; i < N; ++i) dir[(int64_t)f * N + i] = (bct[i] == 0 && bcv[(int64_t)f * N + i] != -1) ? 1 : 0;
+  if (krylov) *krylov = 0;
+  return chem_implicit_step(o, U, phase, dir.data(), bcv, voln1rel, d2, dc, d11, krylov);
+}
+
+// the tangent of field f (0..10) of the complete model as diag (N) and off (per bond slot)
+int orc_chem_tangent(void* h, int f, const double* Un, const int* phase, const int* bct, const double* bcv,
+                     double voln1rel, const double* d2, const double* dc, const double* d11, double* diag_out,
+                     double* off_out) {
+  if (!h || f < 0 || f > 10) return 1;
+  const Oracle& o = *static_cast<Oracle*>(h);
+  const int N = o.N;
+  std::vector<unsigned char> dir(N);
+  for (int i = 0; i < N; ++i) dir[i] = (bct[i] == 0 && bcv[(int64_t)f * N + i] != -1) ? 1 : 0;
+  std::vector<double> d, q;
+  if (f < 10)
+    chem_species_tangent(o, f, Un, phase, dir.data(), voln1rel, d2, dc, d, q);
+  else
+    chem_potential_tangent(o, phase, dir.data(), d2, d11, d, q);
+  std::copy(d.begin(), d.end(), diag_out);
+  std::copy(q.begin(), q.end(), off_out);
   return 0;
 }
 

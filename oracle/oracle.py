@@ -67,6 +67,9 @@ def load_oracle():
             "orc_implant_counts": (C.c_int, [C.c_int, _DP, C.c_int, _DP, C.c_double, _IP]),
             "orc_implicit_forward": (C.c_int, [_P, C.c_int, _LP, _LP]),
             "orc_residuals_implicit": (C.c_int, [_P, _DP, _DP, _DP, _DP, _IP, C.c_double, _DP]),
+            "orc_chem_implicit_step": (C.c_int, [_P, _DP, _IP, _IP, _DP, C.c_double, _DP, _DP, _DP, _LP]),
+            "orc_chem_tangent": (C.c_int, [_P, C.c_int, _DP, _IP, _IP, _DP, C.c_double, _DP, _DP, _DP, _DP,
+                                           _DP]),
             "orc_tangent": (C.c_int, [_P, C.c_int, _DP, _DP]),
             "orc_tangent_gmres": (C.c_int, [_P, C.c_int, _DP, _DP, C.c_double, C.c_int, C.c_int]),
             "nnpp_synth_count": (C.c_int64, [C.c_int, C.c_int]),
@@ -251,6 +254,36 @@ class Oracle:
         load_oracle().orc_residuals_implicit(self._h, _dp(a[0]), _dp(a[1]), _dp(a[2]), _dp(a[3]), _ip(phase),
                                              voln1rel, _dp(F))
         return F
+
+    def chem_implicit_step(self, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11):
+        """One step of the reference's complete model (ten species and the potential) from
+        U (11, N) and phase: returns (U^{n+1}, phase after the flip, Newton iterations,
+        GMRES iterations)."""
+        U = np.array(U, dtype=np.float64, order="C").reshape(11, self.N)
+        ph = np.array(phase, dtype=np.int32)
+        bt = np.ascontiguousarray(bctypes, dtype=np.int32)
+        bv = np.ascontiguousarray(bcvalues, dtype=np.float64).reshape(11, self.N)
+        arr = [np.ascontiguousarray(a, dtype=np.float64) for a in (data2, datac, datac11)]
+        kr = C.c_int64(0)
+        it = load_oracle().orc_chem_implicit_step(self._h, _dp(U), _ip(ph), _ip(bt), _dp(bv), float(voln1rel),
+                                                  _dp(arr[0]), _dp(arr[1]), _dp(arr[2]), C.byref(kr))
+        if it < 0:
+            raise ValueError("chem_implicit_step: bad argument")
+        return U, ph, it, kr.value
+
+    def chem_tangent(self, f, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11):
+        """The complete model's tangent of field f (0..10): (diag (N,), off per bond slot)."""
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(11, self.N)
+        ph = np.ascontiguousarray(phase, dtype=np.int32)
+        bt = np.ascontiguousarray(bctypes, dtype=np.int32)
+        bv = np.ascontiguousarray(bcvalues, dtype=np.float64).reshape(11, self.N)
+        arr = [np.ascontiguousarray(a, dtype=np.float64) for a in (data2, datac, datac11)]
+        nnz = load_oracle().orc_nnz(self._h)
+        diag = np.empty(self.N)
+        off = np.empty(nnz)
+        load_oracle().orc_chem_tangent(self._h, f, _dp(U), _ip(ph), _ip(bt), _dp(bv), float(voln1rel),
+                                       _dp(arr[0]), _dp(arr[1]), _dp(arr[2]), _dp(diag), _dp(off))
+        return diag, off
 
     def poisson_matrix(self, phase):
         phase = np.ascontiguousarray(phase, dtype=np.int32)
@@ -476,6 +509,29 @@ def ref_newton_k(which, p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, v
     if L is None:
         return None
     args, keep = _ref_tangent_args(p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, voln1rel)
+    nnz = C.c_int64(0)
+    L.ref_newton_k(which, *args, C.byref(nnz), None, None, None)
+    ri = np.empty(nnz.value, dtype=np.int32)
+    ci = np.empty(nnz.value, dtype=np.int32)
+    val = np.empty(nnz.value)
+    L.ref_newton_k(which, *args, C.byref(nnz), _ip(ri), _ip(ci), _dp(val))
+    return ri, ci, val
+
+
+def ref_newton_k_full(which, nodes, ptr, cols, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11):
+    """K_(which+1) of the reference's utils::NewtonMatrices at U (11, N) with the data files'
+    parameter arrays, as COO (rows, cols, values)."""
+    L = load_reference()
+    if L is None:
+        return None
+    N = nodes.shape[1]
+    keep = [np.ascontiguousarray(nodes, dtype=np.float64), np.ascontiguousarray(ptr, dtype=np.int64),
+            np.ascontiguousarray(cols, dtype=np.int32), np.ascontiguousarray(U, dtype=np.float64),
+            np.ascontiguousarray(phase, dtype=np.int32), np.ascontiguousarray(bctypes, dtype=np.int32),
+            np.ascontiguousarray(bcvalues, dtype=np.float64), np.ascontiguousarray(data2, dtype=np.float64),
+            np.ascontiguousarray(datac, dtype=np.float64), np.ascontiguousarray(datac11, dtype=np.float64)]
+    args = [N, _dp(keep[0]), _lp(keep[1]), _ip(keep[2]), _dp(keep[3]), _ip(keep[4]), _ip(keep[5]),
+            _dp(keep[6]), float(voln1rel), _dp(keep[7]), _dp(keep[8]), _dp(keep[9])]
     nnz = C.c_int64(0)
     L.ref_newton_k(which, *args, C.byref(nnz), None, None, None)
     ri = np.empty(nnz.value, dtype=np.int32)

@@ -1,0 +1,86 @@
+"""The oracle's restatement of the reference's time step with its complete model (ten species
+and the potential; main.cpp:640-922): its eleven tangents equal utils::NewtonMatrices'
+(utils.h:846-1849) bit for bit with the data files' constants and with constants that make
+every linearised reaction term count, and one step converges, keeps the Dirichlet values,
+the clamp and the flip rule.  Skipped where the reference's sources are absent."""
+import os
+
+import numpy as np
+import pytest
+
+import chem_case
+import chem_state
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "chemistry.npz")
+
+
+def _case(nn, orc, kind, n, seed, reactive):
+    g = np.load(GOLDEN)
+    d2 = chem_case.reactive_data2(g["data2"]) if reactive else g["data2"].copy()
+    dc, d11 = g["datac"], g["datac11"]
+    nodes, phase, Un1, Un, r, cell = chem_case.case_inputs(orc.synth, kind, n, seed, g["data2"])
+    inp = orc.synth(kind, n, seed)
+    p = nn.params_from_reference(d2, [dc[k] for k in range(4)], d11)
+    o = orc.Oracle(p, nodes, inp["bctypes"], inp["bcvalues"], inp["icvalues"], phase)
+    o.build_neighbours(1024, r, (cell, cell, cell))
+    bt, bv = chem_state.bc11(inp, Un, d2[7])
+    return o, nodes, phase, Un, bt, bv, d2, dc, d11
+
+
+@pytest.mark.parametrize("kind,n,seed", [(0, 12, 3), (1, 12, 3)])
+@pytest.mark.parametrize("reactive", [False, True])
+def test_chem_tangents_bit_exact_vs_reference(nn, orc, kind, n, seed, reactive):
+    o, nodes, phase, U, bt, bv, d2, dc, d11 = _case(nn, orc, kind, n, seed, reactive)
+    N = nodes.shape[1]
+    lengths, ptr, cols = o.clouds()
+    for f in range(11):
+        ref = orc.ref_newton_k_full(f, nodes, ptr, cols, U, phase, bt, bv, chem_case.VOLN1REL, d2, dc, d11)
+        if ref is None:
+            pytest.skip("the reference's sources are not compiled here")
+        diag, off = o.chem_tangent(f, U, phase, bt, bv, chem_case.VOLN1REL, d2, dc, d11)
+        mine = {}
+        for i in range(N):
+            mine[(i, i)] = diag[i]
+            for j in range(ptr[i] + 1, ptr[i + 1]):
+                if off[j] != 0.0:
+                    mine[(i, int(cols[j]))] = mine.get((i, int(cols[j])), 0.0) + off[j]
+        theirs = {}
+        for a, b, v in zip(*ref):
+            theirs[(int(a), int(b))] = theirs.get((int(a), int(b)), 0.0) + v
+        keys = set(mine) | set(theirs)
+        bad = [k for k in keys if mine.get(k, 0.0) != theirs.get(k, 0.0)]
+        assert not bad, (f, bad[:3])
+
+
+def smooth_state(phase, d2):
+    """A state near the model's own scales: uniform species in the liquid (1e-4 + 1e-5 k, in
+    CSolid units), the solid's Mg at 1, a potential of zero."""
+    N = phase.size
+    U = np.zeros((11, N))
+    for k in range(10):
+        U[k] = 1e-4 + 1e-5 * k
+    U[0][phase == 1] = 1.0
+    return U
+
+
+@pytest.mark.parametrize("kind,n,seed", [(1, 12, 5), (0, 14, 2)])
+def test_chem_step_converges_and_keeps_the_rules(nn, orc, kind, n, seed):
+    o, nodes, phase, _, bt, _, d2, dc, d11 = _case(nn, orc, kind, n, seed, False)
+    inp = orc.synth(kind, n, seed)
+    U = smooth_state(phase, d2)
+    bt, bv = chem_state.bc11(inp, U, d2[7])
+    U1, ph1, newton, krylov = o.chem_implicit_step(U, phase, bt, bv, chem_case.VOLN1REL, d2, dc, d11)
+    assert 1 <= newton < 200 and krylov > 0
+    assert np.isfinite(U1).all()
+    cs = d2[7]
+    for f in range(11):
+        m = (bt == 0) & (bv[f] != -1)
+        want = bv[f, m] / (cs if f < 10 else 1.0)
+        assert np.allclose(U1[f, m], want, rtol=1e-9, atol=1e-14), f
+    floor = 1e-8 / cs
+    assert (U1[:9] >= floor).all()
+    assert (U1[9][ph1 == 0] >= floor).all()
+    # the flip rule (main.cpp:914-922): solid nodes at or below CSat/CSolid turn liquid
+    csat = d2[8] / cs
+    assert np.array_equal(ph1, np.where((phase == 1) & (U1[0] <= csat), 0, phase))
+    assert np.abs(U1 - U).max() > 0.0
