@@ -200,6 +200,35 @@ nnpp_status nnpp_residuals_full_device(int n_nodes, const double* d_nodes, const
                                        const double* data2, const double* datac,
                                        const double* datac11, double* d_F, void* stream);
 
+/* ---- the complete model's implicit step (main.cpp:640-922) ------------------------------ */
+
+/* The reference's time step with its complete model: ten species and the potential, backward
+ * Euler with the tangents of utils::NewtonMatrices (utils.h:846-1849) at U^n and modified
+ * Newton iterations on utils::Residuals (utils.h:29-842), each correction by Eigen's left-
+ * Jacobi GMRES(30) (GMRES.h:56-203), the Dirichlet rows of main.cpp:676-712, the clamp of
+ * main.cpp:805-837, the flip of main.cpp:914-922 and the relative volume every 8 steps
+ * (main.cpp:944-949).  FP64 on the GPU in the reference's node order.  Created from the
+ * reference's arrays: nodes N x 3 and clouds N x max_node_no column-major (self in column 0,
+ * as build_clouds_hash fills them) with cloud_lengths, bctypes (N), bcvalues (11*N, the
+ * .bc1..bc11 files field-major), data2 (51), datac (10 x 7), datac11 (4).  The bond weights are
+ * beta dV / xi^3: every kernel exponent s must be 0 (NNPP_ERR_UNSUPPORTED otherwise). */
+typedef struct nnpp_chem nnpp_chem;
+nnpp_status nnpp_chem_create(nnpp_chem** out, int n_nodes, const double* nodes_colmajor,
+                             const int* clouds_colmajor, int max_node_no, const int* cloud_lengths,
+                             const int* bctypes, const double* bcvalues, const double* data2,
+                             const double* datac, const double* datac11);
+/* The state U (11*N: U1..U10 divided by CSolid, then the potential) and phases (1 solid);
+ * voln1rel the relative volume for BV; vol0rel the run's initial volume (<= 0: formed from this
+ * state as main.cpp:472-480 does at t = 0).  Steps are counted from here. */
+nnpp_status nnpp_chem_set_state(nnpp_chem* c, const double* U, const int* phase, double voln1rel,
+                                double vol0rel);
+/* n_steps implicit steps; the Newton and GMRES iterations summed over them (may be NULL). */
+nnpp_status nnpp_chem_step(nnpp_chem* c, int n_steps, int64_t* newton_iterations,
+                           int64_t* krylov_iterations);
+/* The state after the steps (any pointer may be NULL). */
+nnpp_status nnpp_chem_get_state(nnpp_chem* c, double* U, int* phase, double* voln1rel);
+void nnpp_chem_destroy(nnpp_chem* c);
+
 /* ---- implant mask (main.cpp:316-325, 422-457) ------------------------------------------- */
 
 /* The phase of every node from the implant's point cloud, as the reference sets it up when

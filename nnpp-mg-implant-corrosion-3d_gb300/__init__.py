@@ -106,6 +106,11 @@ _SIGS = {
     "nnpp_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP]),
     "nnpp_get_tuning": (C.c_int, [_P, _IP, _IP, _IP]),
     "nnpp_set_tuning": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "nnpp_chem_create": (C.c_int, [C.POINTER(_P), C.c_int, _DP, _IP, C.c_int, _IP, _IP, _DP, _DP, _DP, _DP]),
+    "nnpp_chem_set_state": (C.c_int, [_P, _DP, _IP, C.c_double, C.c_double]),
+    "nnpp_chem_step": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "nnpp_chem_get_state": (C.c_int, [_P, _DP, _IP, C.POINTER(C.c_double)]),
+    "nnpp_chem_destroy": (None, [_P]),
     "nnpp_set_transport_variant": (C.c_int, [_P, C.c_int]),
     "nnpp_set_params": (C.c_int, [_P, C.POINTER(Params)]),
     "nnpp_reset": (C.c_int, [_P]),
@@ -238,6 +243,58 @@ def residuals_full(nodes, clouds, cloud_lengths, U_n1, U_n, phase, voln1rel, dat
     _check(lib().nnpp_residuals_full(N, _dp(xyz), _ip(cl), M, _ip(lens), _dp(u1), _dp(u0), _ip(ph),
                                      float(voln1rel), _dp(d2), _dp(dc), _dp(d11), _dp(F)))
     return F
+
+
+class ChemImplicit:
+    """The reference's implicit time step with its complete model (ten species and the
+    potential) on the GPU: nnpp_chem_create / set_state / step / get_state.  nodes (3, N) or
+    (N, 3); clouds (N, M) as build_clouds_hash returns them; bcvalues (11, N); data2, datac
+    (10, 7), datac11 as the reference's data files hold them."""
+
+    def __init__(self, nodes, clouds, cloud_lengths, bctypes, bcvalues, data2, datac, datac11):
+        xyz = _colmajor_nodes(nodes)
+        self.N = N = xyz.shape[1]
+        cl = np.ascontiguousarray(np.asarray(clouds, dtype=np.int32).T)
+        lens = np.ascontiguousarray(cloud_lengths, dtype=np.int32)
+        bt = np.ascontiguousarray(bctypes, dtype=np.int32)
+        bv = np.ascontiguousarray(bcvalues, dtype=np.float64)
+        d2 = np.ascontiguousarray(data2, dtype=np.float64)
+        dc = np.ascontiguousarray(datac, dtype=np.float64)
+        d11 = np.ascontiguousarray(datac11, dtype=np.float64)
+        if bv.shape != (11, N) or bt.shape != (N,) or lens.shape != (N,) or cl.shape[1] != N:
+            raise ValueError("ChemImplicit: clouds (N, M), cloud_lengths and bctypes (N,), bcvalues (11, N)")
+        if d2.size != 51 or dc.size != 70 or d11.size != 4:
+            raise ValueError("ChemImplicit: data2 (51), datac (10, 7), datac11 (4)")
+        h = _P()
+        _check(lib().nnpp_chem_create(C.byref(h), N, _dp(xyz), _ip(cl), cl.shape[0], _ip(lens), _ip(bt), _dp(bv),
+                                      _dp(d2), _dp(dc), _dp(d11)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().nnpp_chem_destroy(h)
+            self._h = None
+
+    def set_state(self, U, phase, voln1rel=0.0, vol0rel=0.0):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        ph = np.ascontiguousarray(phase, dtype=np.int32)
+        if U.shape != (11, self.N) or ph.shape != (self.N,):
+            raise ValueError("ChemImplicit.set_state: U (11, N), phase (N,)")
+        _check(lib().nnpp_chem_set_state(self._h, _dp(U), _ip(ph), float(voln1rel), float(vol0rel)))
+
+    def step(self, n_steps=1):
+        """n implicit steps; returns (Newton iterations, GMRES iterations)."""
+        nw, kr = C.c_int64(0), C.c_int64(0)
+        _check(lib().nnpp_chem_step(self._h, int(n_steps), C.byref(nw), C.byref(kr)))
+        return nw.value, kr.value
+
+    def state(self):
+        U = np.empty((11, self.N))
+        ph = np.empty(self.N, dtype=np.int32)
+        v = C.c_double(0.0)
+        _check(lib().nnpp_chem_get_state(self._h, _dp(U), _ip(ph), C.byref(v)))
+        return U, ph, v.value
 
 
 # ------------------------------------------------------------------ neighbour build -----
