@@ -518,6 +518,52 @@ def chemistry_cost(nn, reps, with_cpu):
     return out
 
 
+def chem_implicit_cost(nn, steps, with_cpu):
+    """The reference's implicit time step with its complete model (ten species and the
+    potential; nnpp_chem_step) on the 40^3 lattice (64,000 nodes) at the reference's node
+    spacing and physical constants, from a smooth state (uniform species in the liquid, the
+    solid's Mg at 1): GPU time per step after one untimed step, and the oracle's step on the
+    host cores as the CPU baseline."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import chem_case
+    import chem_state
+    g = np.load(os.path.join(ROOT, "tests", "golden", "chemistry.npz"))
+    d2, dc, d11 = (np.ascontiguousarray(g[k]) for k in ("data2", "datac", "datac11"))
+    nodes, phase, _, _, r, cell = chem_case.case_inputs(nn.synth, 1, 40, 1, d2)
+    inp = nn.synth(1, 40, 1)
+    N = nodes.shape[1]
+    U = np.zeros((11, N))
+    for k in range(10):
+        U[k] = 1e-4 + 1e-5 * k
+    U[0][phase == 1] = 1.0
+    bt, bv = chem_state.bc11(inp, U, d2[7])
+    clouds, lengths, ml = nn.build_clouds_hash(1024, r, cell, cell, cell, nodes)
+    ch = nn.ChemImplicit(nodes, clouds[:, :ml], lengths, bt, bv, d2, dc, d11)
+    ch.set_state(U, phase, voln1rel=1.0)
+    ch.step(1)
+    t0 = time.perf_counter()
+    nw, kr = ch.step(steps)
+    el = time.perf_counter() - t0
+    out = {"workload": "jittered 40^3 lattice (64,000 nodes) at the reference's node spacing and physical "
+                       "constants, ten species and the potential, smooth initial state",
+           "n_nodes": N, "steps": steps, "ms_per_step": 1e3 * el / steps, "value": N * steps / el,
+           "unit": "node-steps/s", "newton_per_step": nw / steps, "gmres_per_step": kr / steps}
+    del ch
+    if with_cpu:
+        O = load_oracle_module()
+        cores = O.set_threads(os.cpu_count() or 1)
+        p = nn.params_from_reference(d2, [dc[k] for k in range(4)], d11)
+        o = O.Oracle(p, nodes, inp["bctypes"], inp["bcvalues"], inp["icvalues"], phase)
+        o.build_neighbours(1024, r, (cell, cell, cell))
+        U1, ph1, _, _ = o.chem_implicit_step(U, phase, bt, bv, 1.0, d2, dc, d11)
+        t0 = time.perf_counter()
+        o.chem_implicit_step(U1, ph1, bt, bv, 1.0, d2, dc, d11)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": N / el, "unit": "node-steps/s", "cores": cores, "kind": "port",
+                               "sample": "one step of the same case after one untimed step"}
+    return out
+
+
 def run_ours(args):
     rank, world, local = dist_info()
     nn = load_package()
@@ -744,6 +790,11 @@ def run_ours(args):
         chem = chemistry_cost(nn, args.chem_reps, world == 1 and not args.no_cpu_baseline)
         log("chemistry: %s" % json.dumps(chem))
 
+    chem_imp = None
+    if rank == 0 and args.chem_implicit_steps > 0:
+        chem_imp = chem_implicit_cost(nn, args.chem_implicit_steps, world == 1 and not args.no_cpu_baseline)
+        log("chemistry implicit: %s" % json.dumps(chem_imp))
+
     cpu = None
     acc_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -790,6 +841,7 @@ def run_ours(args):
             "large_2m": large,
             "moving_front": front,
             "chemistry_10_species": chem,
+            "chemistry_implicit_step": chem_imp,
             "neighbour_build_s": t_build,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -816,6 +868,8 @@ def main():
                     help="steps run before the dissolving-phase window")
     ap.add_argument("--chem-reps", type=int, default=10,
                     help="timed evaluations of the ten-species residual on the 512k lattice (0: skip)")
+    ap.add_argument("--chem-implicit-steps", type=int, default=3,
+                    help="timed implicit steps of the complete model on the 64k lattice (0: skip)")
     ap.add_argument("--chem-only", action="store_true",
                     help="run only the ten-species residual's leg and print its object")
     args = ap.parse_args()
