@@ -7,12 +7,14 @@
 //              -(K1 D(BV) + K2 D(BV) z F/(RT) (phi^n_n - phi^n_i)) w per bond, diagonal
 //              1/dt + sum K1 D(BV) w; the potential K11 (utils.h:1797-1848) -w on
 //              liquid-liquid bonds, their sum on the diagonal; Dirichlet rows (and potential
-//              rows without liquid-liquid bonds) identity; w = beta dV / xi^3.
+//              rows without liquid-liquid bonds) identity; w = beta dV / xi^3.  The species'
+//              off-diagonals are stored per bond for the step (the GB300's FP64 rate made
+//              forming them in every GMRES product the product's bound).
 //   Newton     F = Residuals(U^{n+1}, U^n) with the migration on phi^n (utils.h:126), F11's
 //              charge from U^n (utils.h:829-831), and
 //              F = U - bc on Dirichlet rows (main.cpp:676-712); K_f dU_f = -F_f by GMRES for
-//              the S species and the potential at once (five independent Krylov solves
-//              advanced together: one gather of a bond serves all five); U += dU; the clamp
+//              the species and the potential at once (independent Krylov solves advanced
+//              together: one pass over the bonds serves every field); U += dU; the clamp
 //              (main.cpp:805-837); stop when max_f | ||dU_f|| - ||dU_f||_prev | < EPS.
 //   then       the phase flip (main.cpp:914-922) and the volume every sub_step_no steps.
 //
@@ -55,6 +57,8 @@ struct ImpCtxT {
   const int* phase;                // N
   const double* u0;                // (NS + 1) * N: U^n (its potential is the migration's phi^n)
   const double* diag;              // (NS + 1) * N: the tangents' diagonals
+  const double* toff;              // NS * nnz: the species tangents' off-diagonals per bond
+  long long nnz;
   double dt, bvmix, csat, k_diss, sw, lam, kphis;
   double K1[NS], K2zF[NS], DL[NS], DSo[NS], z[NS];
   double k7b, k8b, k9b;            // the complete model's rates in its tangents' diagonals
@@ -218,19 +222,16 @@ __global__ void k_imp_residual(ImpCtx c, const double* u1, double* F) {
   }
 }
 
-// out_f = M^-1 K_f v_f for the fields in mask (bit f): the tangents applied to every field at
-// once, one pass over the bonds (warp per node)
+// the species tangents' off-diagonals of every bond (utils.h:900-1792):
+// -(K1 D(BV) + K2 D(BV) z F/(RT) (phi^n_n - phi^n_i)) w, zero where the bond is absent;
+// formed once a step, read by every GMRES iteration's product (warp per node)
 template <int NS>
-__global__ void k_imp_apply(ImpCtxT<NS> c, const double* v, double* out, int mask) {
-  constexpr int NF = NS + 1;
+__global__ void k_imp_tangent(ImpCtxT<NS> c, double* toff) {
   const int lane = threadIdx.x & 31;
   const int N = c.N;
   const double* phi0 = c.u0 + (size_t)NS * N;
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < N; i += (gridDim.x * blockDim.x) >> 5) {
     const int pi = c.phase[i];
-    double acc[NF];
-#pragma unroll
-    for (int f = 0; f < NF; ++f) acc[f] = 0.0;
     for (int j = c.ptr[i] + lane; j < c.ptr[i + 1]; j += 32) {
       const int n = c.col[j];
       const int pn = c.phase[n];
@@ -238,12 +239,31 @@ __global__ void k_imp_apply(ImpCtxT<NS> c, const double* v, double* out, int mas
       const double dphi0 = phi0[n] - phi0[i];
 #pragma unroll
       for (int k = 0; k < NS; ++k) {
-        if (!((mask >> k) & 1)) continue;
         double a1, a2;
-        if (!species_bond(c, k, pi, pn, &a1, &a2)) continue;
-        acc[k] += -(a1 + a2 * dphi0) * w * v[(size_t)k * N + n];
+        toff[(size_t)k * c.nnz + j] = species_bond(c, k, pi, pn, &a1, &a2) ? -(a1 + a2 * dphi0) * w : 0.0;
       }
-      if (((mask >> NS) & 1) && pi == 0 && pn == 0) acc[NS] += -w * v[(size_t)NS * N + n];
+    }
+  }
+}
+
+// out_f = M^-1 K_f v_f for the fields in mask (bit f): the tangents applied to every field at
+// once, one pass over the bonds (warp per node), the species' off-diagonals from toff
+template <int NS>
+__global__ void k_imp_apply(ImpCtxT<NS> c, const double* v, double* out, int mask) {
+  constexpr int NF = NS + 1;
+  const int lane = threadIdx.x & 31;
+  const int N = c.N;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < N; i += (gridDim.x * blockDim.x) >> 5) {
+    const int pi = c.phase[i];
+    double acc[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) acc[f] = 0.0;
+    for (int j = c.ptr[i] + lane; j < c.ptr[i + 1]; j += 32) {
+      const int n = c.col[j];
+#pragma unroll
+      for (int k = 0; k < NS; ++k)
+        if ((mask >> k) & 1) acc[k] += c.toff[(size_t)k * c.nnz + j] * v[(size_t)k * N + n];
+      if (((mask >> NS) & 1) && pi == 0 && c.phase[n] == 0) acc[NS] += -c.w[j] * v[(size_t)NS * N + n];
     }
 #pragma unroll
     for (int f = 0; f < NF; ++f) acc[f] = warp_sum(acc[f]);
@@ -260,28 +280,27 @@ __global__ void k_imp_apply(ImpCtxT<NS> c, const double* v, double* out, int mas
   }
 }
 
-// block partials of the dot products <a_f, B_{q,f}> for q < nq and the fields of mask:
-// part[(q * NF + f) * gridDim.x + block]; B_q at B + q * NF * N
+// block partials of the dot products <a_f, B_{q,f}> for q < nq and the fields of mask, every
+// product at once (blockIdx.y = q * NF + f): part[(q * NF + f) * gridDim.x + block]; B_q at
+// B + q * NF * N
 template <int NF>
 __global__ void k_imp_dots(int N, const double* a, const double* B, int nq, int mask, double* part) {
   __shared__ double sm[kTB / 32];
-  for (int q = 0; q < nq; ++q)
-    for (int f = 0; f < NF; ++f) {
-      if (!((mask >> f) & 1)) continue;
-      const double* x = a + (size_t)f * N;
-      const double* y = B + ((size_t)q * NF + f) * N;
-      double s = 0.0;
-      for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) s += x[i] * y[i];
-      s = warp_sum(s);
-      if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int u = 0; u < kTB / 32; ++u) t += sm[u];
-        part[((size_t)q * NF + f) * gridDim.x + blockIdx.x] = t;
-      }
-      __syncthreads();
-    }
+  const int v = blockIdx.y;
+  const int q = v / NF, f = v - q * NF;
+  if (q >= nq || !((mask >> f) & 1)) return;
+  const double* x = a + (size_t)f * N;
+  const double* y = B + ((size_t)q * NF + f) * N;
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) s += x[i] * y[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int u = 0; u < kTB / 32; ++u) t += sm[u];
+    part[(size_t)v * gridDim.x + blockIdx.x] = t;
+  }
 }
 
 // out[v] = sum of the nb partials of value v, in block order
@@ -363,7 +382,7 @@ __global__ void k_imp_flip(int N, const double* u1, int* phase, double csat, int
 // Device buffers of the implicit solver (one set per call; a handle keeps its weights).
 struct Work {
   int N = 0;
-  DBuf<double> u0, u1, F, b, dU, x, t, r, diag, V, part, red, coef;
+  DBuf<double> u0, u1, F, b, dU, x, t, r, diag, V, part, red, coef, toff;
   DBuf<unsigned char> dir;
   DBuf<double> bc;
   DBuf<int> phase;
@@ -378,9 +397,11 @@ int grid_for(long long items, int per_block) {
 template <int NF>
 nnpp_status dots(cudaStream_t st, Work& wk, const double* a, const double* B, int nq, int mask, double* h) {
   const int N = wk.N;
-  k_imp_dots<NF><<<kDotBlocks, kTB, 0, st>>>(N, a, B, nq, mask, wk.part.get());
+  // blocks of 8 elements a thread per product (at most kDotBlocks)
+  const int nb = std::max(1, std::min(kDotBlocks, (N + kTB * 8 - 1) / (kTB * 8)));
   const int nv = nq * NF;
-  k_imp_reduce<<<(nv + 127) / 128, 128, 0, st>>>(wk.part.get(), kDotBlocks, nv, wk.red.get());
+  k_imp_dots<NF><<<dim3((unsigned)nb, (unsigned)nv), kTB, 0, st>>>(N, a, B, nq, mask, wk.part.get());
+  k_imp_reduce<<<(nv + 127) / 128, 128, 0, st>>>(wk.part.get(), nb, nv, wk.red.get());
   NNPP_CUDA(cudaGetLastError());
   NNPP_CUDA(cudaMemcpyAsync(h, wk.red.get(), sizeof(double) * nv, cudaMemcpyDeviceToHost, st));
   NNPP_CUDA(cudaStreamSynchronize(st));
@@ -547,7 +568,8 @@ extern "C" nnpp_status nnpp_forward_implicit(nnpp_handle* hp, int n_steps, int64
       !wk.b.alloc(FN) || !wk.x.alloc(FN) || !wk.t.alloc(FN) || !wk.r.alloc(FN) || !wk.diag.alloc(FN) ||
       !wk.V.alloc((size_t)(kRestart + 1) * FN) || !wk.part.alloc((size_t)kDotBlocks * (kRestart + 1) * F5) ||
       !wk.red.alloc((size_t)(kRestart + 1) * F5) || !wk.coef.alloc((size_t)(kRestart + 1) * F5) ||
-      !wk.dir.alloc(FN) || !wk.bc.alloc(FN) || !wk.phase.alloc(N))
+      !wk.dir.alloc(FN) || !wk.bc.alloc(FN) || !wk.phase.alloc(N) ||
+      !wk.toff.alloc((size_t)S * std::max<long long>(nnz, 1)))
     return set_error(NNPP_ERR_NOMEM, "forward_implicit buffers");
   k_imp_weights<<<grid_for((long long)N * 32, kTB), kTB, 0, st>>>(
       N, h.ref.ptr.get(), h.ref.col.get(), h.ux.get(), h.uy.get(), h.uz.get(), p.delta, p.dx,
@@ -584,6 +606,8 @@ extern "C" nnpp_status nnpp_forward_implicit(nnpp_handle* hp, int n_steps, int64
   c.phase = wk.phase.get();
   c.u0 = wk.u0.get();
   c.diag = wk.diag.get();
+  c.toff = wk.toff.get();
+  c.nnz = nnz;
   c.dt = p.dt;
   c.csat = p.CSat / p.CSolid;
   c.k_diss = p.k_diss;
@@ -605,6 +629,7 @@ extern "C" nnpp_status nnpp_forward_implicit(nnpp_handle* hp, int n_steps, int64
     c.bvmix = std::pow(10., -p.vol_red * (1. - voln1rel));  // utils.h:100-116
     // the tangents' diagonals at U^n (main.cpp:657-662), U^{n+1} = U^n to start
     k_imp_diag<S><<<grid_for((long long)N * 32, kTB), kTB, 0, st>>>(c, wk.diag.get());
+    k_imp_tangent<S><<<grid_for((long long)N * 32, kTB), kTB, 0, st>>>(c, wk.toff.get());
     NNPP_CUDA(cudaMemcpyAsync(wk.u1.get(), wk.u0.get(), sizeof(double) * FN, cudaMemcpyDeviceToDevice, st));
     std::fill(res_old.begin(), res_old.end(), 0.0);
     int it = 0;
@@ -673,6 +698,7 @@ extern "C" nnpp_status nnpp_forward_implicit(nnpp_handle* hp, int n_steps, int64
 // main.cpp:914-922 and the relative volume every sub_step_no steps (main.cpp:944-949).
 struct nnpp_chem {
   int N = 0, ml = 0, device = 0;
+  long long nnz = 0;
   cudaStream_t st = nullptr;
   DBuf<double> xyz, w;
   DBuf<int> ptr, col, hz, hl;
@@ -737,6 +763,7 @@ extern "C" nnpp_status nnpp_chem_create(nnpp_chem** out, int n_nodes, const doub
   nnpp_chem* c = new nnpp_chem();
   c->N = N;
   c->ml = ml;
+  c->nnz = nnz;
   cudaGetDevice(&c->device);
   c->d2.assign(data2, data2 + 51);
   c->dc.assign(datac, datac + 70);
@@ -750,7 +777,8 @@ extern "C" nnpp_status nnpp_chem_create(nnpp_chem** out, int n_nodes, const doub
        wk.u1.alloc(FN) && wk.F.alloc(FN) && wk.b.alloc(FN) && wk.x.alloc(FN) && wk.t.alloc(FN) &&
        wk.r.alloc(FN) && wk.diag.alloc(FN) && wk.V.alloc((size_t)(kRestart + 1) * FN) &&
        wk.part.alloc((size_t)kDotBlocks * (kRestart + 1) * kChemNF) && wk.red.alloc((size_t)(kRestart + 1) * kChemNF) &&
-       wk.coef.alloc((size_t)(kRestart + 1) * kChemNF) && wk.dir.alloc(FN) && wk.bc.alloc(FN) && wk.phase.alloc(N);
+       wk.coef.alloc((size_t)(kRestart + 1) * kChemNF) && wk.dir.alloc(FN) && wk.bc.alloc(FN) && wk.phase.alloc(N) &&
+       wk.toff.alloc((size_t)kChemNS * std::max<long long>(nnz, 1));
   if (!ok) {
     cudaGetLastError();
     delete c;
@@ -862,6 +890,8 @@ extern "C" nnpp_status nnpp_chem_step(nnpp_chem* c, int n_steps, int64_t* newton
   x.phase = wk.phase.get();
   x.u0 = wk.u0.get();
   x.diag = wk.diag.get();
+  x.toff = wk.toff.get();
+  x.nnz = c->nnz;
   x.dt = d2[2];
   x.csat = CSat / CSolid;
   x.k7b = d2[41];
@@ -880,6 +910,7 @@ extern "C" nnpp_status nnpp_chem_step(nnpp_chem* c, int n_steps, int64_t* newton
   for (int s = 0; s < n_steps; ++s) {
     x.bvmix = std::pow(10., -vol_red * (1. - c->voln1rel));  // utils.h:100-116
     k_imp_diag<kChemNS><<<grid_for((long long)N * 32, kTB), kTB, 0, st>>>(x, wk.diag.get());
+    k_imp_tangent<kChemNS><<<grid_for((long long)N * 32, kTB), kTB, 0, st>>>(x, wk.toff.get());
     NNPP_CUDA(cudaMemcpyAsync(wk.u1.get(), wk.u0.get(), sizeof(double) * FN, cudaMemcpyDeviceToDevice, st));
     std::fill(res_old.begin(), res_old.end(), 0.0);
     int it = 0;
