@@ -99,6 +99,7 @@ extern "C" {
 
 nnpp_status nnpp_forward_ckpt(nnpp_handle* hp, int n_steps, int precision, int ckpt_every,
                               int sample_every, double* mass_curve) {
+  nnpp::TraceRange trace_("nnpp_forward_ckpt");
   clear_error();
   if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
   Handle& h = hp->h;
@@ -275,6 +276,7 @@ nnpp_status nnpp_set_adjoint_store(nnpp_handle* hp, int mode) {
 }
 
 nnpp_status nnpp_backward(nnpp_handle* hp, const double* dL_dmass, double* grad_D, double* grad_k) {
+  nnpp::TraceRange trace_("nnpp_backward");
   clear_error();
   if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
   Handle& h = hp->h;

@@ -342,6 +342,7 @@ nnpp_status nnpp_destroy(nnpp_handle* hp) {
 nnpp_status nnpp_build_neighbours(nnpp_handle* hp, int max_node_no, double r, double cx, double cy,
                                   double cz, int order_mode, int* clouds_colmajor, int* cloud_lengths,
                                   int* max_cloud_length) {
+  nnpp::TraceRange trace_("nnpp_build_neighbours");
   NNPP_GUARD(hp);
   Handle& h = hp->h;
   if (h.engine) {
@@ -434,6 +435,7 @@ nnpp_status nnpp_set_refinement(nnpp_handle* hp, double inner_rel, int max_outer
 }
 
 nnpp_status nnpp_forward(nnpp_handle* hp, int n_steps, int precision) {
+  nnpp::TraceRange trace_("nnpp_forward");
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   if (n_steps < 0) return set_error(NNPP_ERR_INVALID, "n_steps < 0");
@@ -514,6 +516,7 @@ nnpp_status nnpp_get_flip_steps(nnpp_handle* hp, int* flip_step) {
 
 nnpp_status nnpp_step_host(nnpp_handle* hp, int precision, const double* c_in, const int* phase_in,
                            double* c_out, double* phi_out, int* phase_out) {
+  nnpp::TraceRange trace_("nnpp_step_host");
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   if (precision != NNPP_FP64 && precision != NNPP_MIXED) return set_error(NNPP_ERR_INVALID, "precision");
@@ -569,6 +572,7 @@ nnpp_status nnpp_residuals(nnpp_handle* hp, int precision, const double* c, cons
 
 nnpp_status nnpp_solve_potential(nnpp_handle* hp, int precision, const double* c, const int* phase,
                                  double* phi, int* iterations, double* rel_residual) {
+  nnpp::TraceRange trace_("nnpp_solve_potential");
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   if (!c || !phase || !phi) return set_error(NNPP_ERR_INVALID, "solve_potential: NULL argument");
@@ -598,6 +602,7 @@ nnpp_status nnpp_solve_potential(nnpp_handle* hp, int precision, const double* c
 }
 
 nnpp_status nnpp_forward_timed(nnpp_handle* hp, int n_steps, int precision, double* ms) {
+  nnpp::TraceRange trace_("nnpp_forward_timed");
   NNPP_GUARD(hp);
   NNPP_NEED_BUILT(hp);
   if (n_steps < 0 || !ms) return set_error(NNPP_ERR_INVALID, "forward_timed: bad argument");

@@ -363,6 +363,7 @@ nnpp_status nnpp_residuals_full_device(int n_nodes, const double* d_nodes, const
                                        const int* d_phase, double voln1rel, const double* data2,
                                        const double* datac, const double* datac11, double* d_F,
                                        void* stream) {
+  nnpp::TraceRange trace_("nnpp_residuals_full_device");
   clear_error();
   if (n_nodes <= 0 || !d_nodes || !d_clouds || !d_lengths || !d_U_n1 || !d_U_n || !d_phase || !data2 ||
       !datac || !datac11 || !d_F)
@@ -389,6 +390,7 @@ nnpp_status nnpp_residuals_full(int n_nodes, const double* nodes_colmajor, const
                                 int max_node_no, const int* cloud_lengths, const double* U_n1,
                                 const double* U_n, const int* phase, double voln1rel, const double* data2,
                                 const double* datac, const double* datac11, double* F) {
+  nnpp::TraceRange trace_("nnpp_residuals_full");
   clear_error();
   if (n_nodes <= 0 || max_node_no < 1 || !nodes_colmajor || !clouds_colmajor || !cloud_lengths || !U_n1 ||
       !U_n || !phase || !F)

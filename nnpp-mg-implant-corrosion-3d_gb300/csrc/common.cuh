@@ -3,6 +3,7 @@
 #define NNPP_COMMON_CUH
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -11,6 +12,15 @@
 #include "nnpp_internal.h"
 
 namespace nnpp {
+
+// A named range of a C-ABI call for profilers and tracers (NVTX; nothing is recorded unless a
+// tool is attached).
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 
 constexpr int S = NNPP_NSPECIES;
 constexpr int kReduceSlots = 24;   // values reduced per block by the step kernels

@@ -548,6 +548,7 @@ __global__ void k_imp_negate(size_t n, const double* a, double* b) {
 
 extern "C" nnpp_status nnpp_forward_implicit(nnpp_handle* hp, int n_steps, int64_t* newton_iterations,
                                              int64_t* krylov_iterations) {
+  nnpp::TraceRange trace_("nnpp_forward_implicit");
   clear_error();
   if (!hp) return set_error(NNPP_ERR_INVALID, "handle is NULL");
   Handle& h = hp->h;
@@ -867,6 +868,7 @@ extern "C" nnpp_status nnpp_chem_get_state(nnpp_chem* c, double* U, int* phase, 
 
 extern "C" nnpp_status nnpp_chem_step(nnpp_chem* c, int n_steps, int64_t* newton_iterations,
                                       int64_t* krylov_iterations) {
+  nnpp::TraceRange trace_("nnpp_chem_step");
   clear_error();
   if (!c) return set_error(NNPP_ERR_INVALID, "chem_step: NULL handle");
   if (n_steps < 0) return set_error(NNPP_ERR_INVALID, "chem_step: negative step count");
