@@ -749,6 +749,7 @@ extern "C" nnpp_status nnpp_chem_create(nnpp_chem** out, int n_nodes, const doub
     ml = std::max(ml, l);
     nnz += l - 1;
   }
+  if (nnz > 0x7fffffffLL) return set_error(NNPP_ERR_UNSUPPORTED, "chem_create: more than 2^31 bonds");
   // CSR without the node itself (the tangents) and the padded clouds (the residual)
   std::vector<int> ptr(N + 1), col(std::max<long long>(nnz, 1));
   ptr[0] = 0;
