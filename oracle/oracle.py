@@ -541,6 +541,26 @@ def ref_newton_k_full(which, nodes, ptr, cols, U, phase, bctypes, bcvalues, voln
     return ri, ci, val
 
 
+def ref_gmres_full(which, nodes, ptr, cols, U, phase, bctypes, bcvalues, voln1rel, data2, datac, datac11, b):
+    """The reference's Eigen::GMRES solve of K_(which+1) x = b (main.cpp:714-779), the
+    tangent at U (11, N) with the data files' parameter arrays; returns (x, iterations)."""
+    L = load_reference()
+    if L is None:
+        return None
+    N = nodes.shape[1]
+    keep = [np.ascontiguousarray(nodes, dtype=np.float64), np.ascontiguousarray(ptr, dtype=np.int64),
+            np.ascontiguousarray(cols, dtype=np.int32), np.ascontiguousarray(U, dtype=np.float64),
+            np.ascontiguousarray(phase, dtype=np.int32), np.ascontiguousarray(bctypes, dtype=np.int32),
+            np.ascontiguousarray(bcvalues, dtype=np.float64), np.ascontiguousarray(data2, dtype=np.float64),
+            np.ascontiguousarray(datac, dtype=np.float64), np.ascontiguousarray(datac11, dtype=np.float64),
+            np.ascontiguousarray(b, dtype=np.float64)]
+    x = np.empty(N)
+    it = L.ref_gmres(which, N, _dp(keep[0]), _lp(keep[1]), _ip(keep[2]), _dp(keep[3]), _ip(keep[4]),
+                     _ip(keep[5]), _dp(keep[6]), float(voln1rel), _dp(keep[7]), _dp(keep[8]), _dp(keep[9]),
+                     _dp(keep[10]), _dp(x))
+    return x, it
+
+
 def ref_gmres(which, p, nodes, ptr, cols, c, phi, phase, bctypes, bcvalues, b, voln1rel=0.0):
     """The reference's Eigen::GMRES solve of K_(which+1) x = b (main.cpp:714-779)."""
     L = load_reference()

@@ -1,8 +1,10 @@
 """The oracle's restatement of the reference's time step with its complete model (ten species
 and the potential; main.cpp:640-922): its eleven tangents equal utils::NewtonMatrices'
 (utils.h:846-1849) bit for bit with the data files' constants and with constants that make
-every linearised reaction term count, and one step converges, keeps the Dirichlet values,
-the clamp and the flip rule.  Skipped where the reference's sources are absent."""
+every linearised reaction term count; one step equals the reference's own functions
+(Residuals, NewtonMatrices, Eigen::GMRES) assembled in main.cpp's loop; and a step converges,
+keeps the Dirichlet values, the clamp and the flip rule.  Skipped where the reference's
+sources are absent."""
 import os
 
 import numpy as np
@@ -84,3 +86,64 @@ def test_chem_step_converges_and_keeps_the_rules(nn, orc, kind, n, seed):
     csat = d2[8] / cs
     assert np.array_equal(ph1, np.where((phase == 1) & (U1[0] <= csat), 0, phase))
     assert np.abs(U1 - U).max() > 0.0
+
+
+def _reference_step(orc, nodes, ptr, cols, U0, phase, bt, bv, voln1rel, d2, dc, d11):
+    """main.cpp:640-922 assembled from the reference's own compiled functions (utils::Residuals,
+    utils::NewtonMatrices and Eigen::GMRES through the shim), the loop's glue as written there:
+    the Dirichlet rows (676-712), U += dU, the update norms, the clamp (805-837), the test
+    max |res - res_old| < EPS (849-902) and the flip (914-922)."""
+    N = nodes.shape[1]
+    cs, csat = d2[7], d2[8] / d2[7]
+    dirm = (bt[None, :] == 0) & (bv != -1)
+    bcs = np.where(np.arange(11)[:, None] < 10, bv / cs, bv)
+    U1 = U0.copy()
+    res_old = np.zeros(11)
+    newton = 0
+    for it in range(200):
+        F = orc.ref_residuals_full(nodes, ptr, cols, U1, U0, phase, voln1rel, d2, dc, d11)
+        F = np.where(dirm, U1 - bcs, F)
+        dU = np.empty_like(U1)
+        for f in range(11):
+            # the tangents of the step: NewtonMatrices at U^{n+1} = U^n (main.cpp:657)
+            dU[f], _ = orc.ref_gmres_full(f, nodes, ptr, cols, U0, phase, bt, bv, voln1rel, d2, dc, d11, -F[f])
+        U1 = U1 + dU
+        res = np.sqrt((dU * dU).sum(axis=1))
+        floor = 1.0e-8 / cs
+        for k in range(10):
+            m = U1[k] < floor
+            if k == 9:
+                m &= phase == 0
+            U1[k][m] = floor
+        newton = it + 1
+        if np.abs(res - res_old).max() < 10e-6:
+            break
+        res_old = res
+    ph = np.where((phase == 1) & (U1[0] <= csat), 0, phase).astype(np.int32)
+    return U1, ph, newton
+
+
+@pytest.mark.parametrize("perturbed", [False, True])
+def test_chem_step_matches_the_reference_loop(nn, orc, perturbed):
+    """One step of the oracle's restatement against the reference's own functions assembled
+    in main.cpp's loop: the same Newton iteration count, the state to the GMRES tolerance's
+    rounding, the same phases; from the smooth state and from it perturbed by 1% (every field
+    moves, the potential too)."""
+    if orc.load_reference() is None:
+        pytest.skip("the reference's sources are not compiled here")
+    o, nodes, phase, _, bt, _, d2, dc, d11 = _case(nn, orc, 1, 10, 5, False)
+    inp = orc.synth(1, 10, 5)
+    U = smooth_state(phase, d2)
+    if perturbed:
+        rng = np.random.default_rng(7)
+        U = U * (1 + 0.01 * rng.standard_normal(U.shape))
+        U[10] = 1e-3 * rng.standard_normal(U.shape[1])
+    bt, bv = chem_state.bc11(inp, U, d2[7])
+    lengths, ptr, cols = o.clouds()
+    Ur, phr, nr = _reference_step(orc, nodes, ptr, cols, U, phase, bt, bv, chem_case.VOLN1REL, d2, dc, d11)
+    Uo, pho, no, _ = o.chem_implicit_step(U, phase, bt, bv, chem_case.VOLN1REL, d2, dc, d11)
+    assert no == nr
+    assert np.array_equal(pho, phr)
+    for f in range(11):
+        scale = np.linalg.norm(Ur[f]) or 1.0
+        assert np.linalg.norm(Uo[f] - Ur[f]) <= 1e-9 * scale, f
