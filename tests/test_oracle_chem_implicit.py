@@ -147,3 +147,44 @@ def test_chem_step_matches_the_reference_loop(nn, orc, perturbed):
     for f in range(11):
         scale = np.linalg.norm(Ur[f]) or 1.0
         assert np.linalg.norm(Uo[f] - Ur[f]) <= 1e-9 * scale, f
+
+
+def test_four_species_step_matches_the_reference_loop(nn, orc):
+    """The four-species implicit step (the handle's model, nnpp_forward_implicit's oracle) with
+    the dissolution source off against the reference's own loop with reactions off and
+    species 5-10 absent: fields 1-4 and the potential, the Newton count and the phases agree
+    (within a step species 5-10 reach the others only through F11's charge of U^n, which is
+    zero)."""
+    if orc.load_reference() is None:
+        pytest.skip("the reference's sources are not compiled here")
+    g = np.load(GOLDEN)
+    d2 = g["data2"].copy()
+    d2[[29, 31, 33, 35, 37, 39, 41, 43, 45]] = 0.0
+    d2[46] = 0.0
+    dc, d11 = g["datac"], g["datac11"]
+    p = nn.params_from_reference(d2, [dc[k] for k in range(4)], d11, k_diss=0.0)
+    nodes, phase, _, _, r, cell = chem_case.case_inputs(orc.synth, 1, 10, 5, d2)
+    inp = orc.synth(1, 10, 5)
+    U = smooth_state(phase, d2)
+    rng = np.random.default_rng(3)
+    U[:4] *= 1 + 0.01 * rng.standard_normal((4, U.shape[1]))
+    U[4:10] = 0.0
+    U[10] = 1e-3 * rng.standard_normal(U.shape[1])
+    bc5 = np.asarray(inp["bcvalues"], dtype=np.float64)
+    o = orc.Oracle(p, nodes, inp["bctypes"], bc5, inp["icvalues"], phase)
+    o.build_neighbours(1024, r, (cell, cell, cell))
+    o.set_state(U[:4], U[10], phase)
+    v = o.diagnostics()["voln1rel"]
+    lengths, ptr, cols = o.clouds()
+    bt = np.asarray(inp["bctypes"], dtype=np.int32)
+    bv = -np.ones((11, U.shape[1]))
+    bv[:4] = bc5[:4]
+    bv[10] = bc5[4]
+    Ur, phr, nr = _reference_step(orc, nodes, ptr, cols, U, phase, bt, bv, v, d2, dc, d11)
+    no, _ = o.implicit_forward(1)
+    c, phi, ph, _ = o.state()
+    assert no == nr
+    assert np.array_equal(ph, phr)
+    for k in range(4):
+        assert np.linalg.norm(c[k] - Ur[k]) <= 1e-9 * np.linalg.norm(Ur[k]), k
+    assert np.linalg.norm(phi - Ur[10]) <= 1e-9 * np.linalg.norm(Ur[10])
