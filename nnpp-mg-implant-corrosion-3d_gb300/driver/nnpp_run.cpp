@@ -2,7 +2,7 @@
 //
 //   nnpp_run <prefix> <jobname> [<startfileNo>] [--steps N] [--every K]
 //            [--precision mixed|fp64] [--k-diss K] [--switch-width W] [--tol T] [--device D]
-//            [--no-output] [--restart S0]
+//            [--no-output] [--restart S0] [--model four|full]
 //   nnpp_run --write-synth <kind> <n_side> <seed> <jobname> [--steps N]
 //
 // Run mode mirrors the reference executable's start-up and time loop (main.cpp:153-1025):
@@ -27,6 +27,9 @@
 //
 // Text input, the output CSV and the restart file are parsed and formatted by all host
 // threads (at millions of nodes the reference's serial streams dominate the run's I/O).
+//
+// --model full runs the reference's complete model instead (ten species and the potential)
+// with its own implicit time loop (run_full below).
 //
 // --write-synth writes one of the library's seeded synthetic workloads in that layout (plus
 // .phase0, since those workloads hold Mg in the electrolyte too).
@@ -366,9 +369,13 @@ struct Options {
   int device = 0;
   bool output = true;
   int restart = -1;  // start file number (main.cpp's third argument), -1: start from t = 0
+  bool full = false;  // --model full: the reference's complete model and implicit time loop
 };
 
+int run_full(const std::string& prefix, const std::string& job, const Options& opt);
+
 int run(const std::string& prefix, const std::string& job, const Options& opt) {
+  if (opt.full) return run_full(prefix, job, opt);
   std::vector<int> d1;
   std::vector<double> d2, dc[11];
   if (!read_ints(job + ".data1", 4, d1)) return std::fprintf(stderr, "nnpp_run: cannot read %s.data1\n", job.c_str()), 1;
@@ -513,11 +520,135 @@ int run(const std::string& prefix, const std::string& job, const Options& opt) {
   return 0;
 }
 
+// --model full: the reference's complete model (ten species and the potential) with its own
+// time integration (main.cpp:640-922, backward Euler with Newton/GMRES: nnpp_chem_*), from the
+// same job files (all of .datac1..10, .bcvalues1..11, .icvalues1..11); the phase from .phase0
+// or icvalues1 > 10E-6 (main.cpp:413-421); the relative volume 0 until the first update
+// (main.cpp:474-475), vol0rel from the initial state; restart by column name as above.
+int run_full(const std::string& prefix, const std::string& job, const Options& opt) {
+  std::vector<int> d1;
+  std::vector<double> d2, d11, datac(70), tmp;
+  if (!read_ints(job + ".data1", 4, d1)) return std::fprintf(stderr, "nnpp_run: cannot read %s.data1\n", job.c_str()), 1;
+  if (!read_doubles(job + ".data2", 51, d2)) return std::fprintf(stderr, "nnpp_run: cannot read %s.data2\n", job.c_str()), 1;
+  for (int c = 1; c <= 10; ++c) {
+    if (!read_doubles(job + ".datac" + std::to_string(c), 7, tmp))
+      return std::fprintf(stderr, "nnpp_run: cannot read %s.datac%d\n", job.c_str(), c), 1;
+    std::copy(tmp.begin(), tmp.end(), datac.begin() + 7 * (c - 1));
+  }
+  if (!read_doubles(job + ".datac11", 4, d11)) return std::fprintf(stderr, "nnpp_run: cannot read %s.datac11\n", job.c_str()), 1;
+  if (d1[3] > 0) return std::fprintf(stderr, "nnpp_run: --model full starts from the initial-value files only\n"), 1;
+  const int N = d1[0];
+  const int steps = opt.steps >= 0 ? opt.steps : d1[1];
+  if (N <= 0) return std::fprintf(stderr, "nnpp_run: data1 holds no nodes\n"), 1;
+  const int every = opt.every > 0 ? opt.every : 8;
+  const double dx = d2[3], dy = d2[4], dz = d2[5], delta = d2[6], CSolid = d2[7], CSat = d2[8];
+  std::vector<double> rows, xyz(3 * (size_t)N);
+  if (!read_doubles(job + ".nodes", 3 * (size_t)N, rows)) return std::fprintf(stderr, "nnpp_run: cannot read %s.nodes\n", job.c_str()), 1;
+  double energy_bound = -INFINITY;  // nodes.maxCoeff(), main.cpp:245
+  for (size_t i = 0; i < (size_t)N; ++i)
+    for (int d = 0; d < 3; ++d) {
+      xyz[(size_t)d * N + i] = rows[3 * i + d];
+      energy_bound = std::fmax(energy_bound, rows[3 * i + d]);
+    }
+  std::vector<int> bct;
+  if (!read_ints(job + ".bctypes", N, bct)) return std::fprintf(stderr, "nnpp_run: cannot read %s.bctypes\n", job.c_str()), 1;
+  std::vector<double> bcv((size_t)kFields * N), U((size_t)kFields * N);
+  for (int f = 1; f <= kFields; ++f) {
+    if (!read_doubles(job + ".bcvalues" + std::to_string(f), N, tmp)) return std::fprintf(stderr, "nnpp_run: cannot read bcvalues%d\n", f), 1;
+    std::copy(tmp.begin(), tmp.end(), bcv.begin() + (size_t)(f - 1) * N);
+    if (!read_doubles(job + ".icvalues" + std::to_string(f), N, tmp)) return std::fprintf(stderr, "nnpp_run: cannot read icvalues%d\n", f), 1;
+    std::copy(tmp.begin(), tmp.end(), U.begin() + (size_t)(f - 1) * N);
+  }
+  std::vector<int> phase;
+  if (!read_ints(job + ".phase0", N, phase)) {
+    phase.assign(N, 0);
+    for (int i = 0; i < N; ++i) phase[i] = U[i] > 0.0 + 10E-6 ? 1 : 0;
+  }
+  CALL("nnpp_set_device", nnpp_set_device(opt.device));
+  // the reference's neighbourhoods (main.cpp:304-305), compacted to the longest horizon
+  std::vector<int> clouds((size_t)N * kMaxHorizon), lengths(N);
+  int ml = 0;
+  double t0 = now_s();
+  CALL("nnpp_build_clouds_hash",
+       nnpp_build_clouds_hash(kMaxHorizon, delta * (1.00 + 1e-5), dx * 10., dy * 10., dz * 10., N, xyz.data(),
+                              NNPP_ORDER_REFERENCE, clouds.data(), lengths.data(), &ml));
+  clouds.resize((size_t)N * ml);
+  std::printf("Building horizons took %g seconds. Max. horizon length: %d\n", now_s() - t0, ml);
+  nnpp_chem* ch = nullptr;
+  CALL("nnpp_chem_create", nnpp_chem_create(&ch, N, xyz.data(), clouds.data(), ml, lengths.data(), bct.data(),
+                                            bcv.data(), d2.data(), datac.data(), d11.data()));
+  const double csat = CSat / CSolid;
+  double vol0rel = 0.0;  // main.cpp:474-480, from the initial state
+  for (int i = 0; i < N; ++i)
+    if (phase[i] == 1) vol0rel += U[i] - csat;
+  double voln1rel = 0.0;
+  int s = 0;
+  if (opt.restart >= 0) {
+    const std::string path = job + prefix + "-" + std::to_string(opt.restart) + ".output.csv";
+    const std::vector<std::string> names = {"Mg++", "H+", "OH-", "HCO3-", "CO32-", "HPO42-",
+                                            "PO43-", "Ca++", "Na+", "Cl-", "Phi"};
+    std::vector<std::vector<double> > cols;
+    if (!read_start_csv(path, N, names, cols, phase)) return std::fprintf(stderr, "No start file found!\n"), 1;
+    for (int f = 0; f < kFields; ++f) std::copy(cols[f].begin(), cols[f].end(), U.begin() + (size_t)f * N);
+    voln1rel = 0.0;  // main.cpp:530-536
+    for (int i = 0; i < N; ++i)
+      if (phase[i] == 1) voln1rel += U[i] - csat;
+    voln1rel /= vol0rel;
+    s = opt.restart;
+    std::printf("Restart from %s\n", path.c_str());
+  }
+  CALL("nnpp_chem_set_state", nnpp_chem_set_state(ch, U.data(), phase.data(), voln1rel, vol0rel));
+  const double dV = dx * dy * dz;
+  std::vector<double> c((size_t)kSpecies * N), passive(6 * (size_t)N), phi(N);
+  if (opt.output) {
+    Out v(job + prefix + ".volume");
+    Out e(job + prefix + ".energy");
+  }
+  std::printf("Time Marching started (complete model, implicit):\n");
+  t0 = now_s();
+  while (s < steps) {
+    const int n = std::min(every - s % every, steps - s);
+    int64_t newton = 0, krylov = 0;
+    CALL("nnpp_chem_step", nnpp_chem_step(ch, n, &newton, &krylov));
+    s += n;
+    if (s % every != 0 && s != steps) continue;
+    CALL("nnpp_chem_get_state", nnpp_chem_get_state(ch, U.data(), phase.data(), &voln1rel));
+    long long solid = 0;
+    for (int i = 0; i < N; ++i) solid += phase[i];
+    std::printf("step %d  t: %.6g  solid nodes: %lld  Volume rel: %.16g  Newton: %lld  GMRES: %lld  (%.3f ms/step)\n",
+                s, s * d2[2], solid, voln1rel, (long long)newton, (long long)krylov, 1e3 * (now_s() - t0) / n);
+    t0 = now_s();
+    if (!opt.output) continue;
+    {
+      Out v(job + prefix + ".volume", "ab");
+      put(v.f, voln1rel);
+      std::fputs(",\n", v.f);
+    }
+    double energy = 0.0;  // main.cpp:962-969
+    for (size_t i = 0; i < (size_t)N; ++i)
+      if (std::fabs(rows[3 * i]) < energy_bound || std::fabs(rows[3 * i + 1]) < energy_bound)
+        energy += U[i] * U[i] * dV;
+    {
+      Out e(job + prefix + ".energy", "ab");
+      put(e.f, energy);
+      std::fputc('\n', e.f);
+    }
+    std::copy(U.begin(), U.begin() + (size_t)kSpecies * N, c.begin());
+    std::copy(U.begin() + (size_t)kSpecies * N, U.begin() + (size_t)10 * N, passive.begin());
+    std::copy(U.begin() + (size_t)10 * N, U.end(), phi.begin());
+    if (!write_output_csv(job + prefix + "-" + std::to_string(s) + ".output.csv", N, rows, c, passive, phi, phase,
+                          kSpecies))
+      return std::fprintf(stderr, "nnpp_run: cannot write output\n"), 1;
+  }
+  nnpp_chem_destroy(ch);
+  return 0;
+}
+
 int usage() {
   std::fprintf(stderr,
                "usage: nnpp_run <prefix> <jobname> [<startfileNo>] [--steps N] [--every K]\n"
                "                [--precision mixed|fp64] [--k-diss K] [--switch-width W] [--tol T]\n"
-               "                [--device D] [--no-output] [--restart S0]\n"
+               "                [--device D] [--no-output] [--restart S0] [--model four|full]\n"
                "       nnpp_run --write-synth <kind> <n_side> <seed> <jobname> [--steps N]\n");
   return 1;
 }
@@ -545,6 +676,11 @@ int main(int argc, char** argv) {
     else if (a == "--tol" && has) opt.tol = std::atof(argv[++i]);
     else if (a == "--device" && has) opt.device = std::atoi(argv[++i]);
     else if (a == "--restart" && has) opt.restart = std::atoi(argv[++i]);
+    else if (a == "--model" && has) {
+      const std::string v = argv[++i];
+      if (v == "full") opt.full = true;
+      else if (v != "four") return usage();
+    }
     else if (i == 3 && a.size() && a[0] != '-') opt.restart = std::atoi(argv[i]);  // main.cpp's 3rd argument
     else if (a == "--precision" && has) {
       const std::string v = argv[++i];

@@ -159,3 +159,39 @@ def test_driver_implant_point_cloud(nn, orc, tmp_path):
     inner = (mask == 1) & ~dirichlet
     assert inner.sum() > 0 and np.all(out[inner, 3] > 0.9)
     assert np.all(out[(mask == 1) & dirichlet, 3] == inp["bcvalues"][0][(mask == 1) & dirichlet])
+
+
+@pytest.mark.gpu
+def test_driver_full_model_matches_oracle(nn, orc, tmp_path):
+    """--model full: the reference's complete model with its implicit time loop from the job
+    files (nnpp_chem_*), three steps against the oracle's restatement on the same files."""
+    if nn.device_count() < 1:
+        pytest.skip("no CUDA device")
+    job = str(tmp_path / "SYN")
+    steps = 3
+    _write(job, 1, 10, 5, steps)
+    r = subprocess.run([_driver(), "-full", job, "--model", "full", "--every", "3"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "complete model" in r.stdout
+    N = int(_load(job + ".data1", int)[0])
+    d2 = _load(job + ".data2")
+    dc = np.array([_load(job + ".datac%d" % c) for c in range(1, 11)])
+    d11 = _load(job + ".datac11")
+    nodes = np.ascontiguousarray(_load(job + ".nodes").T)
+    bt = _load(job + ".bctypes", int).astype(np.int32)
+    bv = np.array([_load(job + ".bcvalues%d" % f) for f in range(1, 12)])
+    U = np.array([_load(job + ".icvalues%d" % f) for f in range(1, 12)])
+    ph = _load(job + ".phase0", int).astype(np.int32)
+    p = nn.params_from_reference(d2, dc[:4], d11)
+    o = orc.Oracle(p, nodes, bt, bv[[0, 1, 2, 3, 10]], U[[0, 1, 2, 3, 10]], ph)
+    o.build_neighbours(1024, d2[6] * (1 + 1e-5), (d2[3] * 10, d2[4] * 10, d2[5] * 10))
+    for _ in range(steps):
+        U, ph, _, _ = o.chem_implicit_step(U, ph, bt, bv, 0.0, d2, dc, d11)
+    out = np.loadtxt(job + "-full-%d.output.csv" % steps, delimiter=",", skiprows=1)
+    assert out.shape == (N, 15)
+    assert np.array_equal(out[:, 14].astype(int), ph)
+    for f in range(11):
+        col = 3 + f
+        scale = np.linalg.norm(U[f]) or 1.0
+        assert np.linalg.norm(out[:, col] - U[f]) <= 1e-12 * scale + 1e-300, f
