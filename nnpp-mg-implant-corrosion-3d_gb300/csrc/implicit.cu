@@ -380,9 +380,22 @@ __global__ void k_imp_flip(int N, const double* u1, int* phase, double csat, int
 }
 
 // Device buffers of the implicit solver (one set per call; a handle keeps its weights).
+// pinned host memory (the GMRES's reduction results come back by asynchronous copies)
+struct HostPinned {
+  double* p = nullptr;
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+  bool alloc(size_t n) { return cudaMallocHost(reinterpret_cast<void**>(&p), n * sizeof(double)) == cudaSuccess; }
+};
+
 struct Work {
   int N = 0;
   DBuf<double> u0, u1, F, b, dU, x, t, r, diag, V, part, red, coef, toff;
+  HostPinned hpin;
   DBuf<unsigned char> dir;
   DBuf<double> bc;
   DBuf<int> phase;
@@ -393,9 +406,9 @@ int grid_for(long long items, int per_block) {
   return (int)std::max<long long>(1, std::min<long long>(g, 152 * 16));
 }
 
-// dots <a_f, B_{q,f}> (q < nq, fields of mask) into host h[q * NF + f]
+// dots <a_f, B_{q,f}> (q < nq, fields of mask) into the device array wk.red[q * NF + f]
 template <int NF>
-nnpp_status dots(cudaStream_t st, Work& wk, const double* a, const double* B, int nq, int mask, double* h) {
+nnpp_status dots_dev(cudaStream_t st, Work& wk, const double* a, const double* B, int nq, int mask) {
   const int N = wk.N;
   // blocks of 8 elements a thread per product (at most kDotBlocks)
   const int nb = std::max(1, std::min(kDotBlocks, (N + kTB * 8 - 1) / (kTB * 8)));
@@ -403,6 +416,14 @@ nnpp_status dots(cudaStream_t st, Work& wk, const double* a, const double* B, in
   k_imp_dots<NF><<<dim3((unsigned)nb, (unsigned)nv), kTB, 0, st>>>(N, a, B, nq, mask, wk.part.get());
   k_imp_reduce<<<(nv + 127) / 128, 128, 0, st>>>(wk.part.get(), nb, nv, wk.red.get());
   NNPP_CUDA(cudaGetLastError());
+  return NNPP_OK;
+}
+
+// the same into host h[q * NF + f]
+template <int NF>
+nnpp_status dots(cudaStream_t st, Work& wk, const double* a, const double* B, int nq, int mask, double* h) {
+  NNPP_TRY(dots_dev<NF>(st, wk, a, B, nq, mask));
+  const int nv = nq * NF;
   NNPP_CUDA(cudaMemcpyAsync(h, wk.red.get(), sizeof(double) * nv, cudaMemcpyDeviceToHost, st));
   NNPP_CUDA(cudaStreamSynchronize(st));
   return NNPP_OK;
@@ -427,6 +448,8 @@ nnpp_status gmres_fields(cudaStream_t st, const ImpCtxT<NS>& c, Work& wk, long l
   std::vector<double> H((size_t)F5 * (kRestart + 1) * kRestart), g((size_t)F5 * (kRestart + 1)),
       cs((size_t)F5 * kRestart), sn((size_t)F5 * kRestart);
   std::vector<int> it(F5, 0);
+  if (!wk.hpin.p && !wk.hpin.alloc((size_t)3 * (kRestart + 1) * F5))
+    return set_error(NNPP_ERR_NOMEM, "implicit step: pinned reduction buffer");
   // x = b (GMRES.h:330-334); b = 0 gives x = 0
   NNPP_CUDA(cudaMemcpyAsync(wk.x.get(), wk.b.get(), sizeof(double) * FN, cudaMemcpyDeviceToDevice, st));
   NNPP_TRY(dots<F5>(st, wk, wk.b.get(), wk.b.get(), 1, kAll, bb.data()));
@@ -459,15 +482,22 @@ nnpp_status gmres_fields(cudaStream_t st, const ImpCtxT<NS>& c, Work& wk, long l
     for (int k = 1; k <= kRestart && cycle; ++k) {
       double* w = V + (size_t)k * FN;
       NNPP_TRY(apply(st, c, V + (size_t)(k - 1) * FN, w, cycle));
-      // classical Gram-Schmidt, twice
+      // classical Gram-Schmidt, twice: each pass's coefficients stay on the device (the
+      // combination reads the reduction's output) and come back with the new vector's norm by
+      // asynchronous copies, one synchronisation an iteration
+      const size_t hs = (size_t)(kRestart + 1) * F5;
       for (int pass = 0; pass < 2; ++pass) {
-        std::vector<double>& hh = pass == 0 ? h1 : h2;
-        NNPP_TRY(dots<F5>(st, wk, w, V, k, cycle, hh.data()));
-        NNPP_CUDA(cudaMemcpyAsync(wk.coef.get(), hh.data(), sizeof(double) * k * F5, cudaMemcpyHostToDevice, st));
-        k_imp_combine<F5><<<grid_for(N, kTB), kTB, 0, st>>>(N, w, V, k, wk.coef.get(), -1.0, cycle);
+        NNPP_TRY(dots_dev<F5>(st, wk, w, V, k, cycle));
+        NNPP_CUDA(cudaMemcpyAsync(wk.hpin.p + pass * hs, wk.red.get(), sizeof(double) * k * F5,
+                                  cudaMemcpyDeviceToHost, st));
+        k_imp_combine<F5><<<grid_for(N, kTB), kTB, 0, st>>>(N, w, V, k, wk.red.get(), -1.0, cycle);
       }
-      std::vector<double> nrm(F5);
-      NNPP_TRY(dots<F5>(st, wk, w, w, 1, cycle, nrm.data()));
+      NNPP_TRY(dots_dev<F5>(st, wk, w, w, 1, cycle));
+      NNPP_CUDA(cudaMemcpyAsync(wk.hpin.p + 2 * hs, wk.red.get(), sizeof(double) * F5, cudaMemcpyDeviceToHost, st));
+      NNPP_CUDA(cudaStreamSynchronize(st));
+      std::copy(wk.hpin.p, wk.hpin.p + (size_t)k * F5, h1.begin());
+      std::copy(wk.hpin.p + hs, wk.hpin.p + hs + (size_t)k * F5, h2.begin());
+      std::vector<double> nrm(wk.hpin.p + 2 * hs, wk.hpin.p + 2 * hs + F5);
       for (int f = 0; f < F5; ++f) {
         scale[f] = 0.0;
         if (!((cycle >> f) & 1)) continue;
