@@ -69,6 +69,9 @@ def test_usage_errors():
     r = subprocess.run([_driver(), "--write-synth", "9", "8", "1", "/nonexistent/x"],
                        capture_output=True, text=True, timeout=60)
     assert r.returncode != 0
+    r = subprocess.run([_driver(), "-x", "/nonexistent/x", "--model", "seven"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr and "--model" in r.stderr
 
 
 @pytest.mark.gpu
