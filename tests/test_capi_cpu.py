@@ -119,3 +119,31 @@ def test_synth_permutation_case_is_a_permutation(nn):
     assert sorted(key.tolist()) == list(range(12 ** 3))
     assert not np.all(np.diff(key) > 0)
     assert np.array_equal(lat, inp["nodes"])
+
+
+def test_chem_context_checks_its_arguments_before_the_device(nn):
+    """nnpp_chem_create refuses kernel exponents other than 0 and a zero time step before it
+    looks for a device; without one it reports NNPP_ERR_CUDA."""
+    import chem_case
+    g = np.load(os.path.join(GOLDEN_DIR, "chemistry.npz"))
+    d2, dc, d11 = g["data2"].copy(), g["datac"].copy(), g["datac11"]
+    nodes, phase, U, _, r, cell = chem_case.case_inputs(nn.synth, 0, 6, 1, d2)
+    N = nodes.shape[1]
+    clouds = np.tile(np.arange(N, dtype=np.int32)[:, None], (1, 2))
+    lengths = np.ones(N, dtype=np.int32)
+    bt = np.ones(N, dtype=np.int32)
+    bv = -np.ones((11, N))
+    bad = dc.copy()
+    bad[1, 4] = 0.5
+    with pytest.raises(nn.NNPPError) as e:
+        nn.ChemImplicit(nodes, clouds, lengths, bt, bv, d2, bad, d11)
+    assert e.value.status == 6
+    d2z = d2.copy()
+    d2z[2] = 0.0
+    with pytest.raises(nn.NNPPError) as e:
+        nn.ChemImplicit(nodes, clouds, lengths, bt, bv, d2z, dc, d11)
+    assert e.value.status == 1
+    if nn.device_count() == 0:
+        with pytest.raises(nn.NNPPError) as e:
+            nn.ChemImplicit(nodes, clouds, lengths, bt, bv, d2, dc, d11)
+        assert e.value.status == 5
