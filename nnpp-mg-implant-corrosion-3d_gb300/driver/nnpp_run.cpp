@@ -13,8 +13,9 @@
 // data1[1] explicit steps.  Every K steps (default sub_step_no = 8, main.cpp:39,935) it
 // appends voln1rel to <jobname><prefix>.volume and the energy sum of U1^2 dV to .energy, and
 // writes <jobname><prefix>-<s>.output.csv with the reference's 15 columns (utils.h:2054-2100,
-// 16 significant digits).  The model transports species 1-4 and the potential; columns 5-10
-// hold the initial values of those species (read from .icvalues5..10 when present).
+// 16 significant digits).  The default model transports species 1-4 and the potential;
+// columns 5-10 hold the initial values of those species (read from .icvalues5..10 when
+// present).  --model full advances all eleven fields (run_full below).
 //
 // The initial phase is read from <jobname>.phase0 (N ints) when that file exists; otherwise
 // a node is solid when icvalues1 > 10E-6 (main.cpp:413-421, BunnyConditions = 0).  When
