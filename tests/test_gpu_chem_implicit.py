@@ -70,3 +70,36 @@ def test_chem_rejects_bad_input(gpu):
     with pytest.raises(nn.NNPPError) as e:
         nn.ChemImplicit(nodes, clouds[:, :ml], lengths, bt, bv, d2, dc, d11)
     assert e.value.status == 6
+
+
+def test_chem_ten_steps_with_the_volume_update(gpu, orc):
+    """Ten steps: the relative volume that sets BV is refreshed after the eighth
+    (main.cpp:944-949, from the initial volume of main.cpp:474-480), on the GPU as in the
+    oracle's steps driven here; states and phases agree after it."""
+    nn = gpu
+    g = np.load(GOLDEN)
+    d2, dc, d11 = g["data2"].copy(), g["datac"], g["datac11"]
+    nodes, phase, _, _, r, cell = chem_case.case_inputs(nn.synth, 1, 12, 5, d2)
+    inp = nn.synth(1, 12, 5)
+    U = smooth_state(phase, d2)
+    bt, bv = chem_state.bc11(inp, U, d2[7])
+    clouds, lengths, ml = nn.build_clouds_hash(1024, r, cell, cell, cell, nodes)
+    ch = nn.ChemImplicit(nodes, clouds[:, :ml], lengths, bt, bv, d2, dc, d11)
+    ch.set_state(U, phase, voln1rel=0.0)
+    ch.step(10)
+    Ug, phg, vg = ch.state()
+    p = nn.params_from_reference(d2, [dc[k] for k in range(4)], d11)
+    o = orc.Oracle(p, nodes, inp["bctypes"], inp["bcvalues"], inp["icvalues"], phase)
+    o.build_neighbours(1024, r, (cell, cell, cell))
+    csat = d2[8] / d2[7]
+    vol0 = float(U[0][phase == 1].sum() - csat * (phase == 1).sum())
+    Uo, pho, v = U.copy(), phase.copy(), 0.0
+    for s in range(1, 11):
+        Uo, pho, _, _ = o.chem_implicit_step(Uo, pho, bt, bv, v, d2, dc, d11)
+        if s % 8 == 0:
+            v = float(Uo[0][pho == 1].sum() - csat * (pho == 1).sum()) / vol0
+    assert np.array_equal(phg, pho)
+    assert abs(vg - v) <= 1e-12 * abs(v)
+    for f in range(11):
+        scale = np.linalg.norm(Uo[f]) or 1.0
+        assert np.linalg.norm(Ug[f] - Uo[f]) <= 1e-9 * scale, f
